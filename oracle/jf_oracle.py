@@ -1,0 +1,711 @@
+"""CPU restatement of JAX-Fluids' single-phase finite-volume right-hand side.
+
+TEST INFRASTRUCTURE ONLY -- this module is the oracle the CUDA kernels are
+checked against.  The product package never imports it.
+
+The reference (JAX-Fluids 0.2.x, ``src/jaxfluids``) is written in
+``jax.numpy``; JAX is not available where this oracle runs, so every function
+below restates the reference op for op in ``torch`` on the CPU in float64.
+torch's elementwise CPU kernels round after every operation, like the
+reference's un-fused ``jnp`` graph, and torch autograd follows the same
+conventions as ``jax.grad`` at the non-smooth points used here
+(``where`` selects, ``abs'(0) = 0``, ``maximum``/``minimum`` split ties
+evenly), so ``torch.autograd`` on this oracle stands in for ``jax.grad``
+through ``SimulationManager._feed_forward``.
+
+Each function cites the reference file:line it follows (paths relative to
+``src/jaxfluids``).  Parity pins (``tests/golden``): the per-step dt and
+minimum-density log of ``notebooks/basics/101/01_tutorial`` (HLLC + MINMOD,
+periodic, CFL 0.9), the loss/gradient trace of
+``notebooks/basics/101/02_tutorial`` (Rusanov + MINMOD-AD, zero-gradient,
+fixed dt, through ``jax.grad``) and the reference's own exact Riemann solver
+for Sod at t = 0.2 (physics tolerance).  WENO5-Z, CHAR-PRIMITIVE and the
+viscous flux have no numeric pin in the reference; they are pinned by
+line-by-line citation and by the physics checks in ``tests/``.
+
+Buffers follow the reference layout: ``[5, Nx+2nh, Ny+2nh, Nz+2nh]`` with an
+inactive axis of size 1 and no halo; primitives are (rho, u, v, w, p) and
+conservatives (rho, rho u, rho v, rho w, E).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Tuple
+
+import torch
+
+Tensor = torch.Tensor
+
+# precision.py:50 (jnp.finfo(float64).eps) and :53 (spatial stencil eps)
+EPS = 2.220446049250313e-16
+STENCIL_EPS = 1e-30
+
+FACES = ("east", "west", "north", "south", "top", "bottom")
+FACE_AXIS = {"east": 0, "west": 0, "north": 1, "south": 1, "top": 2, "bottom": 2}
+AXIS_FACES = {0: ("west", "east"), 1: ("south", "north"), 2: ("bottom", "top")}
+
+
+@dataclass
+class OracleCase:
+    """The subset of case_setup / numerical_setup the path reads."""
+    cells: Tuple[int, int, int]
+    ranges: Tuple[Tuple[float, float], ...] = ((0.0, 1.0), (0.0, 1.0), (0.0, 1.0))
+    nh: int = 3
+    gamma: float = 1.4
+    R: float = 1.0
+    bc: Dict[str, str] = field(default_factory=dict)
+    recon: str = "WENO5-Z"                 # WENO5-Z | MINMOD | MINMOD-AD
+    recon_var: str = "PRIMITIVE"           # PRIMITIVE | CHAR-PRIMITIVE
+    frozen_state: str = "ARITHMETIC"       # ARITHMETIC | ROE
+    riemann: str = "HLLC"                  # HLLC | RUSANOV
+    signal_speed: str = "EINFELDT"
+    cfl: float = 0.5
+    fixed_dt: Optional[float] = None
+    viscous: bool = False
+    heat: bool = False
+    mu: float = 0.0
+    bulk_viscosity: float = 0.0
+    prandtl: Optional[float] = None
+    viscous_heat_production: bool = True
+
+    # ---- domain information (domain/domain_information.py:80-206) ----
+    @property
+    def active(self) -> List[int]:
+        return [i for i in range(3) if self.cells[i] > 1]
+
+    @property
+    def dim(self) -> int:
+        return len(self.active)
+
+    def cell_size(self, axis: int) -> float:
+        # domain/mesh_creation/homogenous.py:13
+        lo, hi = self.ranges[axis]
+        return (hi - lo) / self.cells[axis]
+
+    def one_cell_size(self, axis: int) -> float:
+        # domain/domain_information.py:290
+        return 1.0 / self.cell_size(axis)
+
+    @property
+    def min_cell_size(self) -> float:
+        # domain/domain_information.py:698-701
+        return min(self.cell_size(i) for i in self.active)
+
+    def cell_centers(self, axis: int) -> Tensor:
+        # domain/mesh_creation/homogenous.py:14 (np.linspace)
+        import numpy as np
+        lo, hi = self.ranges[axis]
+        d = self.cell_size(axis)
+        return torch.from_numpy(np.linspace(lo + d / 2, hi - d / 2, self.cells[axis]))
+
+    def buffer_shape(self) -> Tuple[int, int, int, int]:
+        # initialization/helper_functions.py:49
+        return (5,) + tuple(n + 2 * self.nh if n > 1 else 1 for n in self.cells)
+
+    def inner(self, axis: int) -> slice:
+        return slice(self.nh, -self.nh) if self.cells[axis] > 1 else slice(None)
+
+    def interior(self) -> Tuple[slice, ...]:
+        return (slice(None),) + tuple(self.inner(i) for i in range(3))
+
+    def cp(self) -> float:
+        # materials/single_materials/ideal_gas.py:32
+        return self.gamma / (self.gamma - 1.0) * self.R
+
+
+def _axis_slice(case: OracleCase, axis: int, s: slice) -> Tuple[slice, ...]:
+    sl = [slice(None)] + [case.inner(i) for i in range(3)]
+    sl[axis + 1] = s
+    return tuple(sl)
+
+
+def _stencil_slice(case: OracleCase, axis: int, k: int, at_center: int = 0) -> Tuple[slice, ...]:
+    # stencils/spatial_stencil.py:96-110 (nlo = n + k, nhi = -n + k + 1 - at_cell_center)
+    n = case.nh
+    nlo = n + k
+    nhi = -n + k + 1 - at_center
+    assert nlo >= 0 and nhi <= 0
+    return _axis_slice(case, axis, slice(nlo, nhi if nhi != 0 else None))
+
+
+# ---------------------------------------------------------------------------
+# Ideal-gas EOS and equation layout
+# ---------------------------------------------------------------------------
+
+def speed_of_sound(p: Tensor, rho: Tensor, gamma: float) -> Tensor:
+    # materials/single_materials/ideal_gas.py:69-71
+    return torch.sqrt(gamma * p / rho)
+
+
+def cons_from_prims(P: Tensor, gamma: float) -> Tensor:
+    # equation_manager.py:93-101, ideal_gas.py:85-88 (e = p / (rho (gamma-1)))
+    rho = P[0]
+    vel = P[1:4]
+    e = P[4] / (rho * (gamma - 1.0))
+    mom = rho * vel
+    sq = vel * vel
+    E = rho * (0.5 * (sq[0] + sq[1] + sq[2]) + e)
+    return torch.stack([rho, mom[0], mom[1], mom[2], E], dim=0)
+
+
+def prims_from_cons(U: Tensor, gamma: float) -> Tensor:
+    # equation_manager.py:164-171, ideal_gas.py:73-75 (p = (gamma-1) e rho)
+    rho = U[0]
+    one_rho = 1.0 / rho
+    vel = U[1:4] * one_rho
+    sq = vel * vel
+    e = U[4] * one_rho - 0.5 * (sq[0] + sq[1] + sq[2])
+    p = (gamma - 1.0) * e * rho
+    return torch.stack([rho, vel[0], vel[1], vel[2], p], dim=0)
+
+
+def fluxes_xi(P: Tensor, U: Tensor, axis: int) -> Tensor:
+    # equation_manager.py:237-252
+    rho_ui = U[axis + 1]
+    f1 = U[axis + 1] * P[1]
+    f2 = U[axis + 1] * P[2]
+    f3 = U[axis + 1] * P[3]
+    ui_Ep = P[axis + 1] * (U[4] + P[4])
+    f = [rho_ui, f1, f2, f3, ui_Ep]
+    f[axis + 1] = f[axis + 1] + P[4]
+    return torch.stack(f, dim=0)
+
+
+# ---------------------------------------------------------------------------
+# Cell-face reconstruction
+# ---------------------------------------------------------------------------
+
+_WENO_DR = (1 / 10, 6 / 10, 3 / 10)                      # weno5_base.py:24
+_WENO_CR = ((1 / 3, -7 / 6, 11 / 6),                      # weno5_base.py:25-27
+            (-1 / 6, 5 / 6, 1 / 3),
+            (1 / 3, 5 / 6, -1 / 6))
+
+
+def weno5z_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
+                   eps: float = STENCIL_EPS) -> Tensor:
+    """WENO5-Z on the five values (u_imm, u_im, u_i, u_ip, u_ipp).
+
+    shock_capturing/weno/weno5_z.py:24-58, weno5_base.py:34-51.
+    """
+    b0 = 13.0 / 12.0 * torch.square(u0 - 2 * u1 + u2) + 1.0 / 4.0 * torch.square(u0 - 4 * u1 + 3 * u2)
+    b1 = 13.0 / 12.0 * torch.square(u1 - 2 * u2 + u3) + 1.0 / 4.0 * torch.square(u1 - u3)
+    b2 = 13.0 / 12.0 * torch.square(u2 - 2 * u3 + u4) + 1.0 / 4.0 * torch.square(3 * u2 - 4 * u3 + u4)
+    tau5 = torch.abs(b0 - b2)
+    a0 = _WENO_DR[0] * (1.0 + tau5 / (b0 + eps))
+    a1 = _WENO_DR[1] * (1.0 + tau5 / (b1 + eps))
+    a2 = _WENO_DR[2] * (1.0 + tau5 / (b2 + eps))
+    one_a = 1.0 / (a0 + a1 + a2)
+    w0 = a0 * one_a
+    w1 = a1 * one_a
+    w2 = a2 * one_a
+    c = _WENO_CR
+    p0 = c[0][0] * u0 + c[0][1] * u1 + c[0][2] * u2
+    p1 = c[1][0] * u1 + c[1][1] * u2 + c[1][2] * u3
+    p2 = c[2][0] * u2 + c[2][1] * u3 + c[2][2] * u4
+    return w0 * p0 + w1 * p1 + w2 * p2
+
+
+def _recon_offsets(recon: str, j: int) -> Tuple[int, ...]:
+    if recon == "WENO5-Z":
+        # weno5_base.py:30 array_slices([range(-3, 2, 1), range(2, -3, -1)])
+        return (-3, -2, -1, 0, 1) if j == 0 else (2, 1, 0, -1, -2)
+    if recon in ("MINMOD", "MINMOD-AD"):
+        # muscl3.py:33, minmod_ad.py:32
+        return (-2, -1, 0) if j == 0 else (1, 0, -1)
+    raise NotImplementedError(recon)
+
+
+def recon_stencil(recon: str, j: int, vals: List[Tensor], eps: float = STENCIL_EPS) -> Tensor:
+    """Face value from the stencil values ordered as the reference's slices."""
+    if recon == "WENO5-Z":
+        return weno5z_stencil(*vals, eps=eps)
+    b0, b1, b2 = vals
+    if recon == "MINMOD":
+        # muscl3.py:53-75, limiter.py:9-10
+        eps_ad = 1e-10
+        if j == 0:
+            dc = b2 - b1
+            du = b1 - b0
+        else:
+            dc = b1 - b2
+            du = b0 - b1
+        r = torch.where(du >= eps, dc / (du + eps_ad), (dc + eps) / (du + eps))
+        lim = torch.maximum(torch.zeros_like(r), torch.minimum(torch.ones_like(r), r))
+        if j == 0:
+            return b1 + 0.5 * lim * du
+        return b1 - 0.5 * lim * du
+    if recon == "MINMOD-AD":
+        # muscl/minmod_ad.py:45-66
+        eps_ad = 1e-100
+        if j == 0:
+            dc = b2 - b1
+            du = b1 - b0
+        else:
+            dc = b1 - b2
+            du = b0 - b1
+        r = torch.where(du >= eps, dc / (du + eps_ad), (dc + eps) / (du + eps))
+        return torch.where(r < 0, b1, torch.where(r < 1, 0.5 * (b1 + b2), 1.5 * b1 - 0.5 * b0))
+    raise NotImplementedError(recon)
+
+
+def reconstruct_xi(buf: Tensor, case: OracleCase, axis: int, j: int) -> Tensor:
+    """SpatialReconstruction.reconstruct_xi on a halo buffer -> face values [.., N+1, ..]."""
+    vals = [buf[_stencil_slice(case, axis, k)] for k in _recon_offsets(case.recon, j)]
+    return recon_stencil(case.recon, j, vals)
+
+
+# ---------------------------------------------------------------------------
+# Characteristic decomposition (CHAR-PRIMITIVE)
+# ---------------------------------------------------------------------------
+
+def _stencil_window(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
+    """Eigendecomposition.get_stencil_window: [5, N+1, ..., S] over the stencil.
+
+    solvers/riemann_solvers/eigendecomposition.py:75-118 (window of
+    ``stencil_size`` cells starting at offset -stencil_size/2 around face i-1/2).
+    """
+    size = 6 if case.recon == "WENO5-Z" else 4
+    half = size // 2
+    wins = [buf[_stencil_slice(case, axis, k)] for k in range(-half, half)]
+    return torch.stack(wins, dim=-1)
+
+
+def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, ...]:
+    """Eigendecomposition.compute_frozen_state (single phase).
+
+    eigendecomposition.py:120-294: ARITHMETIC = mean of the two cells adjacent to
+    the face; ROE = Roe average with H = (E + p) / rho and c^2 = (gamma-1)(H - |u|^2/2).
+    Returns (rho, u, v, w, H, c) at the faces.
+    """
+    g = case.gamma
+    L = P[_stencil_slice(case, axis, -1)]
+    Rr = P[_stencil_slice(case, axis, 0)]
+    if case.frozen_state == "ARITHMETIC":
+        prim = 0.5 * (L + Rr)
+        rho, u, v, w, p = prim
+        vel_sq = u * u + v * v + w * w
+        c = torch.sqrt(g * p / rho)
+        H = (p / (g - 1.0) + 0.5 * rho * vel_sq + p) / rho
+        return rho, u, v, w, H, c
+    if case.frozen_state == "ROE":
+        UL = cons_from_prims(L, g)
+        UR = cons_from_prims(Rr, g)
+        sL = torch.sqrt(L[0])
+        sR = torch.sqrt(Rr[0])
+        one = 1.0 / (sL + sR)
+        u = (sL * L[1] + sR * Rr[1]) * one
+        v = (sL * L[2] + sR * Rr[2]) * one
+        w = (sL * L[3] + sR * Rr[3]) * one
+        HL = (UL[4] + L[4]) / L[0]
+        HR = (UR[4] + Rr[4]) / Rr[0]
+        H = (sL * HL + sR * HR) * one
+        rho = sL * sR
+        vel_sq = u * u + v * v + w * w
+        c = torch.sqrt((g - 1.0) * (H - 0.5 * vel_sq))
+        return rho, u, v, w, H, c
+    raise NotImplementedError(case.frozen_state)
+
+
+def _char_matrices(fs: Tuple[Tensor, ...], axis: int) -> Tuple[List[List[Tensor]], List[List[Tensor]]]:
+    """Primitive-variable eigenvectors of the Euler Jacobian along ``axis``.
+
+    eigendecomposition.py:402-433 / 499-523: left eigenvectors L (prim -> char)
+    and right eigenvectors R (char -> prim) for (rho, u_n, u_t1, u_t2, p).
+    Rows/columns use the reference's variable order (rho, u, v, w, p).
+    """
+    rho, u, v, w, H, c = fs
+    zero = torch.zeros_like(rho)
+    one = torch.ones_like(rho)
+    n = axis + 1
+    # left eigenvectors (rows) in the frame (rho, u_n, p) + tangential velocities
+    Lm = [[zero] * 5 for _ in range(5)]
+    Rm = [[zero] * 5 for _ in range(5)]
+    # wave 0: u - c
+    Lm[0][n] = -0.5 * rho / c
+    Lm[0][4] = 0.5 / (c * c)
+    # wave 1: entropy
+    Lm[1][0] = one
+    Lm[1][4] = -1.0 / (c * c)
+    # waves 2, 3: shear
+    tang = [t for t in (1, 2, 3) if t != n]
+    Lm[2][tang[0]] = one
+    Lm[3][tang[1]] = one
+    # wave 4: u + c
+    Lm[4][n] = 0.5 * rho / c
+    Lm[4][4] = 0.5 / (c * c)
+    # right eigenvectors (columns)
+    Rm[0][0] = one
+    Rm[n][0] = -c / rho
+    Rm[4][0] = c * c
+    Rm[0][1] = one
+    Rm[tang[0]][2] = one
+    Rm[tang[1]][3] = one
+    Rm[0][4] = one
+    Rm[n][4] = c / rho
+    Rm[4][4] = c * c
+    return Lm, Rm
+
+
+# ---------------------------------------------------------------------------
+# Riemann solvers
+# ---------------------------------------------------------------------------
+
+def signal_speeds(name: str, uL, uR, aL, aR, rhoL, rhoR, pL, pR, gamma):
+    # solvers/riemann_solvers/signal_speeds.py
+    if name == "EINFELDT":              # :109-133
+        sL = torch.sqrt(rhoL)
+        sR = torch.sqrt(rhoR)
+        od = 1.0 / (sL + sR)
+        eta2 = 0.5 * sL * sR * od * od
+        ubar = (sL * uL + sR * uR) * od
+        dbar = torch.sqrt((sL * aL * aL + sR * aR * aR) * od + eta2 * torch.square(uR - uL))
+        return torch.minimum(ubar - dbar, uL - aL), torch.maximum(ubar + dbar, uR + aR)
+    if name == "DAVIS":                 # :51-69
+        return torch.minimum(uL - aL, uR - aR), torch.maximum(uL + aL, uR + aR)
+    if name == "ARITHMETIC":            # :10-29
+        um = 0.5 * (uL + uR)
+        am = 0.5 * (aL + aR)
+        return torch.minimum(um - am, uL - aL), torch.maximum(um + am, uR + aR)
+    if name == "RUSANOV":               # :31-49
+        sp = torch.maximum(torch.abs(uL) + aL, torch.abs(uR) + aR)
+        return -sp, sp
+    if name == "TORO":                  # :135-157, :201-231
+        rho_bar = 0.5 * (rhoL + rhoR)
+        a_bar = 0.5 * (aL + aR)
+        p_pvrs = 0.5 * (pL + pR) - 0.5 * (uR - uL) * rho_bar * a_bar
+        p_star = torch.maximum(torch.zeros_like(p_pvrs), p_pvrs)
+        g_ = (gamma + 1) * 0.5 / gamma
+        qL = 1.0 * (p_star <= pL) + torch.sqrt(1 + g_ * (p_star / pL - 1)) * (p_star > pL)
+        qR = 1.0 * (p_star <= pR) + torch.sqrt(1 + g_ * (p_star / pR - 1)) * (p_star > pR)
+        return uL - aL * qL, uR + aR * qR
+    raise NotImplementedError(name)
+
+
+def compute_sstar(uL, uR, pL, pR, rhoL, rhoR, SL, SR):
+    # signal_speeds.py:159-199
+    rdL = rhoL * (SL - uL)
+    rdR = rhoR * (SR - uR)
+    return ((pR - pL) + (uL * rdL - uR * rdR)) / (rdL - rdR)
+
+
+def _hllc_star_flux(P, U, S, Sstar, axis, side):
+    # HLLC.py:41-78
+    n = axis + 1
+    pre = (S - P[n]) / (S - Sstar) * P[0]
+    e_term = pre * (U[4] / U[0] + (Sstar - P[n]) * (Sstar + P[4] / P[0] / (S - P[n])))
+    us = [pre, pre, pre, pre, e_term]
+    us[n] = us[n] * Sstar
+    for t in (1, 2, 3):
+        if t != n:
+            us[t] = us[t] * P[t]
+    us = torch.stack(us, dim=0)
+    F = fluxes_xi(P, U, axis)
+    if side == "L":
+        wave = torch.minimum(S, torch.zeros_like(S))
+    else:
+        wave = torch.maximum(S, torch.zeros_like(S))
+    return F + wave * (us - U)
+
+
+def riemann(PL, PR, UL, UR, case: OracleCase, axis: int) -> Tensor:
+    g = case.gamma
+    n = axis + 1
+    cL = speed_of_sound(PL[4], PL[0], g)
+    cR = speed_of_sound(PR[4], PR[0], g)
+    if case.riemann == "HLLC":
+        # HLLC.py:80-126
+        SL, SR = signal_speeds(case.signal_speed, PL[n], PR[n], cL, cR, PL[0], PR[0], PL[4], PR[4], g)
+        Ss = compute_sstar(PL[n], PR[n], PL[4], PR[4], PL[0], PR[0], SL, SR)
+        FL = _hllc_star_flux(PL, UL, SL, Ss, axis, "L")
+        FR = _hllc_star_flux(PR, UR, SR, Ss, axis, "R")
+        sg = torch.sign(Ss)
+        return 0.5 * (1 + sg) * FL + 0.5 * (1 - sg) * FR
+    if case.riemann == "RUSANOV":
+        # Rusanov.py:25-47
+        alpha = torch.maximum(torch.abs(PL[n]) + cL, torch.abs(PR[n]) + cR)
+        FL = fluxes_xi(PL, UL, axis)
+        FR = fluxes_xi(PR, UR, axis)
+        return 0.5 * (FL + FR) - 0.5 * alpha * (UR - UL)
+    raise NotImplementedError(case.riemann)
+
+
+def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
+    """HighOrderGodunov.compute_flux_xi (high_order_godunov.py:117-231, :233-402)."""
+    g = case.gamma
+    if case.recon_var == "PRIMITIVE":
+        PL = reconstruct_xi(P, case, axis, 0)
+        PR = reconstruct_xi(P, case, axis, 1)
+    elif case.recon_var == "CHAR-PRIMITIVE":
+        win = _stencil_window(P, case, axis)                   # [5, F.., S]
+        fs = frozen_state(P, case, axis)
+        Lm, Rm = _char_matrices(fs, axis)
+        # eigendecomposition.py:402-433 (einsum over the primitive index)
+        char = []
+        for r in range(5):
+            acc = None
+            for c_ in range(5):
+                term = Lm[r][c_].unsqueeze(-1) * win[c_]
+                acc = term if acc is None else acc + term
+            char.append(acc)
+        size = win.shape[-1]
+        half = size // 2
+        offs = _recon_offsets(case.recon, 0)
+        # stencil slices on the window: reconstruction_stencil.set_slices_stencil
+        # spatial_reconstruction.py:21-44 (range(0, S-1) for j=0, range(S-1, 0, -1) for j=1)
+        idx0 = [k + half for k in offs]
+        idx1 = [k + half for k in _recon_offsets(case.recon, 1)]
+        cL = [recon_stencil(case.recon, 0, [ch[..., i] for i in idx0]) for ch in char]
+        cR = [recon_stencil(case.recon, 1, [ch[..., i] for i in idx1]) for ch in char]
+        PL_l, PR_l = [], []
+        for r in range(5):
+            accL = None
+            accR = None
+            for c_ in range(5):
+                tL = Rm[r][c_] * cL[c_]
+                tR = Rm[r][c_] * cR[c_]
+                accL = tL if accL is None else accL + tL
+                accR = tR if accR is None else accR + tR
+            PL_l.append(accL)
+            PR_l.append(accR)
+        PL = torch.stack(PL_l, 0)
+        PR = torch.stack(PR_l, 0)
+    else:
+        raise NotImplementedError(case.recon_var)
+    UL = cons_from_prims(PL, g)
+    UR = cons_from_prims(PR, g)
+    return riemann(PL, PR, UL, UR, case, axis)
+
+
+# ---------------------------------------------------------------------------
+# Viscous flux (CENTRAL4), source_term_solver.py
+# ---------------------------------------------------------------------------
+
+def _c4_face_interp(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
+    # stencils/reconstruction/central/central_4.py:39-50: (-1, 9, 9, -1)/16
+    s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
+    return (-1.0 / 16.0 * s[0] + 9.0 / 16.0 * s[1] + 9.0 / 16.0 * s[2] - 1.0 / 16.0 * s[3])
+
+
+def _c4_face_deriv(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
+    # stencils/derivative/deriv_face_4.py:37-50: (1, -27, 27, -1)/(24 dx)
+    s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
+    dx = case.cell_size(axis)
+    return (1.0 / 24.0 * s[0] - 27.0 / 24.0 * s[1] + 27.0 / 24.0 * s[2] - 1.0 / 24.0 * s[3]) / dx
+
+
+def viscous_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
+    """compute_viscous_flux_xi for constant mu (source_term_solver.py:264-350)."""
+    raise NotImplementedError("viscous flux oracle")
+
+
+# ---------------------------------------------------------------------------
+# Right-hand side, halos, time integration, dt
+# ---------------------------------------------------------------------------
+
+def compute_rhs(U: Tensor, P: Tensor, case: OracleCase) -> Tensor:
+    """SpaceSolver.compute_rhs for the single-phase convective (+viscous) path.
+
+    space_solver.py:151-453 (axis loop :289-314), compute_rhs_xi :456-674:
+    flux = 0 + F_conv (+ -F_visc), rhs_xi = 0 + (1/dx)(F[:-1] - F[1:]),
+    rhs = ((0.0 + rhs_x) + rhs_y) + rhs_z.
+    """
+    rhs = None
+    for axis in case.active:
+        flux = convective_flux_xi(P, case, axis)
+        if case.viscous:
+            visc = viscous_flux_xi(P, case, axis)
+            flux = torch.cat([flux[:1], flux[1:] - visc], 0)
+        sl_lo = [slice(None)] * 4
+        sl_hi = [slice(None)] * 4
+        sl_lo[axis + 1] = slice(None, -1)
+        sl_hi[axis + 1] = slice(1, None)
+        rhs_xi = case.one_cell_size(axis) * (flux[tuple(sl_lo)] - flux[tuple(sl_hi)])
+        rhs = rhs_xi if rhs is None else rhs + rhs_xi
+    return rhs
+
+
+def _face_fill_slice(case: OracleCase, face: str) -> Tuple[slice, ...]:
+    # halos/halo_slices.py:46-75 (east = +x end [-nh:], west = [:nh])
+    axis = FACE_AXIS[face]
+    nh = case.nh
+    s = slice(-nh, None) if face in ("east", "north", "top") else slice(None, nh)
+    return _axis_slice(case, axis, s)
+
+
+def _face_retrieve_slice(case: OracleCase, face: str, btype: str) -> Tuple[slice, ...]:
+    # halos/outer/boundary_condition.py:539-604
+    axis = FACE_AXIS[face]
+    nh = case.nh
+    hi = face in ("east", "north", "top")
+    if btype == "PERIODIC":
+        s = slice(nh, 2 * nh) if hi else slice(-2 * nh, -nh)
+    elif btype == "ZEROGRADIENT":
+        s = slice(-nh - 1, -nh) if hi else slice(nh, nh + 1)
+    elif btype == "SYMMETRY":
+        s = slice(-nh - 1, -2 * nh - 1, -1) if hi else slice(2 * nh - 1, nh - 1, -1)
+    else:
+        raise NotImplementedError(btype)
+    return _axis_slice(case, axis, s)
+
+
+def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tensor, Optional[Tensor]]:
+    """HaloManager.perform_halo_update_material, face halos (outer/material.py:94-287).
+
+    Halo primitives are copied (or mirrored) from the interior; halo
+    conservatives are recomputed from the halo primitives (:248-250).  The
+    reference writes them as ``x.at[fill].mul(0).add(h)``, i.e. a plain set.
+    """
+    P = P.clone()
+    U = U.clone() if U is not None else None
+    for face in FACES:
+        axis = FACE_AXIS[face]
+        if axis not in case.active:
+            continue
+        btype = case.bc[face]
+        h = P[_face_retrieve_slice(case, face, btype)]
+        if btype == "ZEROGRADIENT":
+            reps = [1] * 4
+            reps[axis + 1] = case.nh
+            h = h.repeat(*reps)
+        if btype == "SYMMETRY":
+            sign = torch.ones(5, dtype=P.dtype).reshape(5, 1, 1, 1)
+            sign[axis + 1] = -1.0
+            h = h * sign
+        fill = _face_fill_slice(case, face)
+        P[fill] = h
+        if U is not None:
+            U[fill] = cons_from_prims(h, case.gamma)
+    if case.viscous:
+        P, U = edge_halo_update(P, U, case)
+    return P, U
+
+
+def edge_halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase):
+    """Edge halos for all-PERIODIC boundaries (outer/material.py:289-379).
+
+    For PERIODIC_PERIODIC edges the retrieve location is the opposite edge, which
+    is the same as wrapping each index independently.
+    """
+    for f in FACES:
+        if FACE_AXIS[f] in case.active and case.bc[f] != "PERIODIC":
+            raise NotImplementedError("edge halos are restated for PERIODIC boundaries only")
+    nh = case.nh
+    P = P.clone()
+    for axis in case.active:
+        n = case.cells[axis]
+        # wrap along axis over the full extent of the other axes
+        sl_lo = [slice(None)] * 4
+        sl_hi = [slice(None)] * 4
+        src_lo = [slice(None)] * 4
+        src_hi = [slice(None)] * 4
+        sl_lo[axis + 1] = slice(0, nh)
+        src_lo[axis + 1] = slice(n, n + nh)
+        sl_hi[axis + 1] = slice(n + nh, n + 2 * nh)
+        src_hi[axis + 1] = slice(nh, 2 * nh)
+        P[tuple(sl_lo)] = P[tuple(src_lo)]
+        P[tuple(sl_hi)] = P[tuple(src_hi)]
+    if U is not None:
+        U = U.clone()
+        # recompute conservatives in every halo cell (interior untouched)
+        full = cons_from_prims(P, case.gamma)
+        mask = torch.ones(P.shape[1:], dtype=torch.bool)
+        mask[tuple(case.inner(i) for i in range(3))] = False
+        U[:, mask] = full[:, mask]
+    return P, U
+
+
+RK3_DT_MULT = (1.0, 0.25, 2.0 / 3.0)                 # RK3.py:27
+RK3_CONS_MULT = ((0.25, 0.75), (2.0 / 3.0, 1.0 / 3.0))  # RK3.py:29
+
+
+def rk3_stage_update(U: Tensor, Un: Tensor, rhs: Tensor, dt, stage: int, case: OracleCase) -> Tensor:
+    """TimeIntegrator.perform_stage_integration (time_integrator.py:108-226, RK3.py:31-62)."""
+    if stage > 0:
+        a, b = RK3_CONS_MULT[stage - 1]
+        U = a * U + b * Un
+    ts = dt * RK3_DT_MULT[stage]
+    U = U.clone()
+    inner = case.interior()
+    U[inner] = U[inner] + ts * rhs
+    return U
+
+
+def rk3_step(U: Tensor, P: Tensor, dt, case: OracleCase) -> Tuple[Tensor, Tensor]:
+    """One TVD-RK3 step (simulation_manager.py:670-1077)."""
+    Un = U
+    for stage in range(3):
+        rhs = compute_rhs(U, P, case)
+        U = rk3_stage_update(U, Un, rhs, dt, stage, case)
+        P = prims_from_cons(U, case.gamma)          # simulation_manager.py:943-944
+        P, U = halo_update(P, U, case)              # :961-970
+    return U, P
+
+
+def compute_dt(P: Tensor, case: OracleCase) -> Tensor:
+    """compute_time_step_size (time_integration/time_step_size.py:15-157)."""
+    if case.fixed_dt:
+        return torch.tensor(case.fixed_dt, dtype=torch.float64)
+    Pi = P[case.interior()]
+    rho = Pi[0]
+    c = speed_of_sound(Pi[4], rho, case.gamma)
+    abs_vel = 0.0
+    for i in case.active:
+        abs_vel = abs_vel + (torch.abs(Pi[i + 1]) + c)
+    dt = case.min_cell_size / (torch.max(abs_vel) + EPS)
+    if case.viscous:
+        nu = case.mu / rho
+        dt_v = 3.0 / 14.0 * (case.min_cell_size * case.min_cell_size) / (torch.max(nu) + EPS)
+        dt = torch.minimum(dt, dt_v)
+    if case.heat:
+        kappa = case.mu * case.cp() / case.prandtl
+        alpha = kappa / (rho * case.cp())
+        dt_h = 0.1 * (case.min_cell_size * case.min_cell_size) / (torch.max(alpha) + EPS)
+        dt = torch.minimum(dt, dt_h)
+    return dt * case.cfl
+
+
+def initialize(prims_interior: Tensor, case: OracleCase, inactive_velocity_eps: bool = True) -> Tuple[Tensor, Tensor]:
+    """MaterialFieldsInitializer.create_material_fields (material_fields_initializer.py:148-210).
+
+    The buffer starts as eps everywhere (initialization/helper_functions.py:49-60);
+    the interior is set from the initial primitives; inactive velocity
+    components keep eps unless the caller passes all five components
+    (``feed_forward.py`` sets all five).
+    """
+    shape = case.buffer_shape()
+    P = torch.ones(shape, dtype=torch.float64) * EPS
+    inner = case.interior()
+    if prims_interior.shape[0] == 5:
+        P[inner] = prims_interior
+    else:
+        ids = [0] + [1 + i for i in case.active] + [4]
+        for k, idx in enumerate(ids):
+            P[(idx,) + inner[1:]] = prims_interior[k]
+    U = cons_from_prims(P, case.gamma)
+    P, U = halo_update(P, U, case)
+    return U, P
+
+
+def simulate(U: Tensor, P: Tensor, case: OracleCase, end_time: float = None, end_step: int = None,
+             t0: float = 0.0, log=None):
+    """SimulationManager.advance (simulation_manager.py:297-425) without output.
+
+    ``while t < end_time and step < end_step``; dt is computed from the state at
+    the start of each step and not clipped to end_time.
+    """
+    t = t0
+    step = 0
+    dt = compute_dt(P, case)
+    if log is not None:
+        log.append((t, float(dt), float(P[case.interior()][0].min())))
+    end_time = math.inf if end_time is None else end_time
+    end_step = 1 << 62 if end_step is None else end_step
+    while t < end_time and step < end_step:
+        U, P = rk3_step(U, P, dt, case)
+        t = t + float(dt)
+        step += 1
+        dt = compute_dt(P, case)
+        if log is not None:
+            log.append((t, float(dt), float(P[case.interior()][0].min())))
+    return U, P, t, step
