@@ -1,0 +1,332 @@
+"""Benchmark: FP64 cell-updates/s of the fused TVD-RK3 path on the 3-D
+inviscid Taylor-Green vortex (128^3 periodic on [0, 2 pi]^3, gamma 1.4,
+Ma 0.1, WENO5-Z on primitives + HLLC/Einfeldt, RK3, CFL 0.5).
+
+A step is one full TVD-RK3 step (three fused stage kernels + one time-step
+kernel) of the whole grid; cell-updates/s = cells x steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the oracle, torch on all host threads) on a bounded sample of the same
+workload; the reference itself (JAX) is not installed on these machines.
+Under torchrun each rank advances its own replica (replicas only: the path
+has no multi-GPU exchange), and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TGV = 128
+METRIC = "FP64 cell-updates/s (TGV 128^3, WENO5-Z+HLLC, TVD-RK3)"
+UNIT = "cell-updates/s"
+# Algorithmic HBM bytes per cell-update: stage 1 reads U^n and writes U^1
+# (80 B); stages 2 and 3 read U^k and U^n and write (120 B each) -> 320 B.
+BYTES_PER_CELL_UPDATE = 320.0
+# FP64 operations per cell-update of the stage kernels (double-precision add,
+# mul and fma instructions, fma counted twice) from the ncu capture summarised
+# in profiles/sweep_kernel_tgv.md; None until measured.
+FP64_FLOP_PER_CELL_UPDATE = None
+# DRAM bytes per stage launch at 128^3 from the same capture (scaled from the
+# captured case by cells); None until measured.
+DRAM_BYTES_PER_LAUNCH = None
+
+
+def tgv_state(n, device, dtype=torch.float64):
+    """Conservatives of the TGV initial condition (interior layout [5, n, n, n])."""
+    gamma, ma = 1.4, 0.1
+    p0 = 1.0 / (gamma * ma * ma)
+    x = (torch.arange(n, dtype=dtype, device=device) + 0.5) * (2 * math.pi / n)
+    X, Y, Z = torch.meshgrid(x, x, x, indexing="ij")
+    u = torch.sin(X) * torch.cos(Y) * torch.cos(Z)
+    v = -torch.cos(X) * torch.sin(Y) * torch.cos(Z)
+    w = torch.zeros_like(X)
+    p = p0 + (torch.cos(2 * X) + torch.cos(2 * Y)) * (torch.cos(2 * Z) + 2.0) / 16.0
+    rho = torch.ones_like(X)
+    E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w)
+    return torch.stack([rho, rho * u, rho * v, rho * w, E]).contiguous()
+
+
+def tgv_config(n):
+    from jaxfluids_gb300 import CaseConfig
+    return CaseConfig(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=3, gamma=1.4,
+                      bc={f: "PERIODIC" for f in ("east", "west", "north", "south", "top", "bottom")},
+                      recon="WENO5-Z", riemann="HLLC", signal_speed="EINFELDT", cfl=0.5)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[4 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def fp64_peak_tflops(lib, device):
+    """DFMA-chain rate of this GPU (8 chains/thread, 152 x 8 CTAs of 256 threads)."""
+    blocks, threads, iters = 152 * 8, 256, 2048
+    out = torch.empty(blocks * threads, dtype=torch.float64, device=device)
+    s = torch.cuda.current_stream()
+    import ctypes
+    st = ctypes.c_void_p(s.cuda_stream)
+    lib.gbf_probe_arith(0, ctypes.c_void_p(out.data_ptr()), blocks, threads, 64, st)
+    torch.cuda.synchronize()
+    best = math.inf
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        lib.gbf_probe_arith(0, ctypes.c_void_p(out.data_ptr()), blocks, threads, iters, st)
+        b.record(s)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b) / 1e3)
+    flops = 2.0 * 8 * iters * blocks * threads
+    return flops / best / 1e12
+
+
+def cpu_oracle_rate(n=24, steps=2, threads=None):
+    """Oracle (torch CPU, float64) TVD-RK3 rate on a TGV n^3 sample."""
+    from oracle import jf_oracle as O
+    if threads:
+        torch.set_num_threads(threads)
+    case = O.OracleCase(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=3,
+                        bc={f: "PERIODIC" for f in O.FACES}, recon="WENO5-Z", riemann="HLLC",
+                        signal_speed="EINFELDT", cfl=0.5)
+    U = tgv_state(n, "cpu")
+    P = O.prims_from_cons(U, 1.4)
+    Ub, Pb = O.initialize(P, case)
+    dt = O.compute_dt(Pb, case)
+    Ub, Pb = O.rk3_step(Ub, Pb, dt, case)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = O.compute_dt(Pb, case)
+        Ub, Pb = O.rk3_step(Ub, Pb, dt, case)
+    el = time.perf_counter() - t0
+    return n ** 3 * steps / el, el
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    n = 48
+    from oracle import jf_oracle as O  # noqa: F401
+    # warm-up steps
+    for _ in range(max(0, args.warmup)):
+        cpu_oracle_rate(n, 1, threads)
+    total_cells, total_t = 0, 0.0
+    for _ in range(args.steps):
+        rate, el = cpu_oracle_rate(n, 1, threads)
+        total_cells += n ** 3
+        total_t += el
+    value = total_cells / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"TGV {n}^3 sample of the 128^3 case (same scheme, periodic)",
+                   "cells": n ** 3, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"TGV {n}^3, {args.steps} RK3 steps, CPU restatement (torch float64, "
+                                   f"{threads} threads); the JAX reference is not installed"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_TGV)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import ctypes
+    from jaxfluids_gb300 import FusedRK3, _lib, build
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if rank == 0:
+        build.build()
+    if world > 1:
+        dist.barrier()
+    lib = _lib.load()
+    n = args.n
+    cfg = tgv_config(n)
+    cells = n ** 3
+    U0 = tgv_state(n, device)
+    f = FusedRK3(cfg, device)
+    f.set_state(U0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        f.advance(1)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))          # overwrite L2 (256 MiB > 129 MB) between steps
+        starts[k].record(stream)
+        f.advance(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_dev = sum(step_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_dev], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = tt.item()
+    value = world * cells * args.steps / t_dev
+
+    # ---- per-kernel time of the stage kernels (same stream, CUDA events) ----
+    ka = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    kb = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for k in range(3):
+        ka[k].record(stream)
+        f.advance(1)
+        kb[k].record(stream)
+    torch.cuda.synchronize()
+    per_step_s = min(a.elapsed_time(b) for a, b in zip(ka, kb)) / 1e3
+    # a step = 3 stage launches + 1 one-thread time-step launch (~microseconds)
+    launch_s = per_step_s / 3.0
+    bytes_per_launch = BYTES_PER_CELL_UPDATE / 3.0 * cells
+    hbm_peak = 6795.1
+    try:
+        hbm_peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except Exception:
+        peak_src = "fallback"
+    achieved = bytes_per_launch / launch_s / 1e9
+    fp64_peak = fp64_peak_tflops(lib, device)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak, "peak_source": peak_src,
+        "traffic": DRAM_BYTES_PER_LAUNCH,
+        "kernel": "sweep_kernel<WENO5Z,HLLC,STAGE> (one launch per RK stage)",
+        "fp64": {"peak_tflops_measured": fp64_peak,
+                 "achieved_tflops": (FP64_FLOP_PER_CELL_UPDATE * cells / 3.0 / launch_s / 1e12)
+                 if FP64_FLOP_PER_CELL_UPDATE else None,
+                 "flop_per_cell_update": FP64_FLOP_PER_CELL_UPDATE},
+    }
+
+    # ---- end to end through the public API with host buffers ----
+    host_in = torch.empty((5, n, n, n), dtype=torch.float64, pin_memory=True)
+    host_in.copy_(U0.cpu())
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    ea = torch.cuda.Event(enable_timing=True)
+    eb = torch.cuda.Event(enable_timing=True)
+    ea.record(stream)
+    for _ in range(e2e_steps):
+        f.cons.copy_(host_in, non_blocking=True)
+        f.advance(1)
+        host_out.copy_(f.cons, non_blocking=True)
+    eb.record(stream)
+    torch.cuda.synchronize()
+    e2e_t = ea.elapsed_time(eb) / 1e3
+    e2e = {"value": world * cells * e2e_steps / e2e_t, "unit": UNIT,
+           "h2d_bytes_per_step": host_in.numel() * 8, "d2h_bytes_per_step": host_out.numel() * 8,
+           "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, el = cpu_oracle_rate(64, 3, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"TGV 64^3, 3 RK3 steps ({el:.1f} s), CPU restatement (torch float64)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4",
+                       "cells": cells, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5",
+                       "parallelism": f"replicas x{world}",
+                       "l2": "256 MiB buffer written between timed steps (per-step CUDA events)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 4 * args.steps, "clocks": clocks, "wall_s": wall,
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

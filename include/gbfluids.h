@@ -1,0 +1,190 @@
+/*
+ * gbfluids: C ABI of the GB300 (sm_103a) single-phase finite-volume
+ * right-hand side of JAX-Fluids.
+ *
+ * Every entry point takes plain device pointers, a case descriptor and a CUDA
+ * stream (passed as void*, may be NULL for the legacy stream).  Nothing here
+ * allocates device memory unless its comment says so, nothing synchronises
+ * the device unless its comment says so, and no call traps: failures are
+ * returned as negative status codes (gbf_status_string names them).
+ *
+ * Buffer layouts are the reference's (src/jaxfluids, paths below relative to
+ * it):
+ *   - halo buffers   double[5][Nx+2nh][Ny+2nh][Nz+2nh], C order, an inactive
+ *                    axis (N = 1) has extent 1 and no halo
+ *                    (initialization/helper_functions.py:49,
+ *                    domain/domain_information.py:202-206);
+ *   - interior       double[5][Nx][Ny][Nz] (rhs, solvers/space_solver.py:135-141);
+ *   - primitives     (rho, u, v, w, p), conservatives (rho, rho u, rho v,
+ *                    rho w, E) (equation_information.py:95-105).
+ */
+#ifndef GBFLUIDS_H
+#define GBFLUIDS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBF_ABI_VERSION 1
+
+/* status codes */
+#define GBF_OK 0
+#define GBF_ERR_INVALID_ARGUMENT -1
+#define GBF_ERR_UNSUPPORTED -2
+#define GBF_ERR_CUDA -3
+#define GBF_ERR_SIZE -4
+#define GBF_ERR_ALIGNMENT -5
+
+/* reconstruction_stencil (stencils/__init__.py registry) */
+#define GBF_RECON_WENO5Z 0
+#define GBF_RECON_MINMOD 1
+#define GBF_RECON_MINMOD_AD 2
+
+/* reconstruction_variable (solvers/__init__.py:5-12) */
+#define GBF_RECVAR_PRIMITIVE 0
+#define GBF_RECVAR_CHAR_PRIMITIVE 1
+
+/* frozen_state (input/numerical_setup/read_conservatives.py:162-166) */
+#define GBF_FROZEN_ARITHMETIC 0
+#define GBF_FROZEN_ROE 1
+
+/* riemann_solver (solvers/riemann_solvers/__init__.py:16) */
+#define GBF_RIEMANN_HLLC 0
+#define GBF_RIEMANN_RUSANOV 1
+
+/* signal_speed (solvers/riemann_solvers/__init__.py:27) */
+#define GBF_SIGNAL_EINFELDT 0
+#define GBF_SIGNAL_DAVIS 1
+#define GBF_SIGNAL_ARITHMETIC 2
+#define GBF_SIGNAL_RUSANOV 3
+#define GBF_SIGNAL_TORO 4
+
+/* boundary types (halos/outer/boundary_condition.py:539-604) */
+#define GBF_BC_PERIODIC 0
+#define GBF_BC_ZEROGRADIENT 1
+#define GBF_BC_SYMMETRY 2
+
+/* face order of gbf_case.bc */
+#define GBF_FACE_WEST 0
+#define GBF_FACE_EAST 1
+#define GBF_FACE_SOUTH 2
+#define GBF_FACE_NORTH 3
+#define GBF_FACE_BOTTOM 4
+#define GBF_FACE_TOP 5
+
+/* gbf_case.flags */
+#define GBF_FLAG_VISCOUS 1u
+#define GBF_FLAG_HEAT 2u
+#define GBF_FLAG_VISCOUS_HEAT_PRODUCTION 4u
+
+/* Case descriptor: the numerical_setup / case_setup keys the path reads. */
+typedef struct gbf_case {
+  int32_t n[3];          /* interior cells per axis; 1 marks an inactive axis */
+  int32_t nh;            /* halo cells of the halo buffers (conservatives.halo_cells) */
+  int32_t recon;         /* GBF_RECON_* */
+  int32_t recon_var;     /* GBF_RECVAR_* */
+  int32_t frozen_state;  /* GBF_FROZEN_* */
+  int32_t riemann;       /* GBF_RIEMANN_* */
+  int32_t signal_speed;  /* GBF_SIGNAL_* */
+  int32_t bc[6];         /* GBF_BC_* per face, GBF_FACE_* order */
+  uint32_t flags;        /* GBF_FLAG_* */
+  double dx[3];          /* cell size per axis ((hi - lo) / n, homogenous.py:13) */
+  double gamma;          /* specific_heat_ratio */
+  double R;              /* specific_gas_constant */
+  double mu;             /* constant dynamic viscosity (CUSTOM) */
+  double bulk_mu;        /* bulk viscosity */
+  double kappa;          /* thermal conductivity */
+  double cfl;            /* time_integration.CFL */
+  double fixed_dt;       /* time_integration.fixed_timestep, 0 = CFL time step */
+  double eps;            /* precision epsilon (jnp.finfo(float64).eps) */
+  double stencil_eps;    /* spatial stencil epsilon (1e-30) */
+} gbf_case;
+
+/* Launch shape of the fused sweep kernels; all-zero picks the built-in default. */
+typedef struct gbf_tile {
+  int32_t t[3];          /* cells per tile along each axis (1 on inactive axes) */
+  int32_t threads;       /* threads per CTA (multiple of 32, <= 1024) */
+} gbf_tile;
+
+int gbf_abi_version(void);
+const char* gbf_status_string(int status);
+
+/* Checks a descriptor; returns GBF_OK or the reason it cannot run. */
+int gbf_case_check(const gbf_case* c);
+
+/*
+ * Right-hand side of the conservative variables from a halo-filled primitive
+ * buffer.  Replaces SpaceSolver.compute_rhs (solvers/space_solver.py:151-453,
+ * per axis compute_rhs_xi :456-674) for the single-phase GODUNOV path:
+ * reconstruct -> Riemann flux -> (1/dx)(F[i-1/2] - F[i+1/2]) summed over
+ * the active axes in x, y, z order.  prims: halo buffer; rhs: interior buffer.
+ */
+int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream);
+
+/*
+ * Face halos (and, for viscous cases, edge halos) of the primitive buffer and,
+ * when cons != NULL, the conservatives of the halo cells recomputed from the
+ * halo primitives.  Replaces HaloManager.perform_halo_update_material
+ * (halos/halo_manager.py:146-234, halos/outer/material.py:94-287).
+ */
+int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream);
+
+/* Primitive <-> conservative conversion over `count` cells of SoA buffers with
+ * a variable stride of `count` (equation_manager.py:44-171). */
+int gbf_prims_from_cons(const gbf_case* c, const double* cons, double* prims, int64_t count, void* stream);
+int gbf_cons_from_prims(const gbf_case* c, const double* prims, double* cons, int64_t count, void* stream);
+
+/*
+ * One TVD-RK3 stage update of a halo buffer (RK3.py:31-62,
+ * time_integrator.py:108-226): stage 0: U += dt rhs;
+ * stage s>0: U = a_s U + b_s U0 (whole buffer), then U += (dt m_s) rhs
+ * (interior).  dt is read from the device scalar *dt.
+ */
+int gbf_stage_integrate(const gbf_case* c, double* cons, const double* cons0, const double* rhs,
+                        const double* dt, int stage, void* stream);
+
+/*
+ * CFL time step of a halo-filled primitive buffer
+ * (time_integration/time_step_size.py:15-157), written to the device scalar
+ * *dt_out.  Uses a device scratch of gbf_dt_workspace_bytes() bytes.
+ */
+size_t gbf_dt_workspace_bytes(void);
+int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream);
+
+/*
+ * Fused TVD-RK3 steps on interior conservatives (the hot path).
+ * cons: double[5][Nx][Ny][Nz], advanced in place by `steps` steps.  Each
+ * stage is one kernel: it builds the primitives of a tile plus its halo from
+ * the conservatives (boundary conditions applied by index remapping), sweeps
+ * x, y, z faces and applies the RK combination; the last stage also reduces
+ * the next CFL time step.  dt_state: device double[4] = {dt, t, max_a, max_b}
+ * (dt of the next step, simulation time, reduction slots); initialise with
+ * gbf_rk3_init.  workspace: gbf_rk3_workspace_bytes(c) bytes of device memory
+ * (two stage buffers).  No host synchronisation; graph-capturable.
+ */
+size_t gbf_rk3_workspace_bytes(const gbf_case* c);
+int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream);
+int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
+                    const gbf_tile* tile, void* stream);
+
+/*
+ * Measurement helper with no counterpart in the reference: runs `iters`
+ * iterations of 8 independent dependency chains of one operation per thread
+ * (blocks x threads threads) and stores one value per thread in out, so the
+ * caller can time this GPU's arithmetic rates (FP64 fused multiply-add,
+ * division, square root; FP32 fused multiply-add) for the roofline.
+ */
+#define GBF_PROBE_DFMA 0
+#define GBF_PROBE_DDIV 1
+#define GBF_PROBE_DSQRT 2
+#define GBF_PROBE_FFMA 3
+int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFLUIDS_H */

@@ -1,0 +1,110 @@
+"""ctypes binding of libgbfluids.so (declarations in include/gbfluids.h).
+
+The library is the only compute path: if it is missing or cannot be loaded
+every call raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgbfluids.so")
+
+GBF_OK = 0
+STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported setup", -3: "CUDA launch error",
+          -4: "invalid or unsupported size", -5: "misaligned pointer"}
+
+RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2}
+RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
+FROZEN = {"ARITHMETIC": 0, "ROE": 1}
+RIEMANN = {"HLLC": 0, "RUSANOV": 1}
+SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
+BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2}
+FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
+FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION = 1, 2, 4
+
+# every symbol include/gbfluids.h declares
+EXPORTS = (
+    "gbf_abi_version", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill",
+    "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
+    "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
+    "gbf_rk3_advance", "gbf_probe_arith",
+)
+
+
+class GbfCase(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int32 * 3),
+        ("nh", ctypes.c_int32),
+        ("recon", ctypes.c_int32),
+        ("recon_var", ctypes.c_int32),
+        ("frozen_state", ctypes.c_int32),
+        ("riemann", ctypes.c_int32),
+        ("signal_speed", ctypes.c_int32),
+        ("bc", ctypes.c_int32 * 6),
+        ("flags", ctypes.c_uint32),
+        ("dx", ctypes.c_double * 3),
+        ("gamma", ctypes.c_double),
+        ("R", ctypes.c_double),
+        ("mu", ctypes.c_double),
+        ("bulk_mu", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("fixed_dt", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("stencil_eps", ctypes.c_double),
+    ]
+
+
+class GbfTile(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_int32 * 3), ("threads", ctypes.c_int32)]
+
+
+class GbfError(RuntimeError):
+    pass
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load() -> ctypes.CDLL:
+    """Load the library once; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GbfError(f"{LIB_PATH} is missing: build it with jaxfluids_gb300.build.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    C = ctypes.POINTER(GbfCase)
+    T = ctypes.POINTER(GbfTile)
+    sig = {
+        "gbf_abi_version": (I, []),
+        "gbf_status_string": (ctypes.c_char_p, [I]),
+        "gbf_case_check": (I, [C]),
+        "gbf_rhs": (I, [C, P, P, T, P]),
+        "gbf_halo_fill": (I, [C, P, P, P]),
+        "gbf_prims_from_cons": (I, [C, P, P, ctypes.c_int64, P]),
+        "gbf_cons_from_prims": (I, [C, P, P, ctypes.c_int64, P]),
+        "gbf_stage_integrate": (I, [C, P, P, P, P, I, P]),
+        "gbf_dt_workspace_bytes": (ctypes.c_size_t, []),
+        "gbf_dt": (I, [C, P, P, P, P]),
+        "gbf_rk3_workspace_bytes": (ctypes.c_size_t, [C]),
+        "gbf_rk3_init": (I, [C, P, P, ctypes.c_double, P]),
+        "gbf_rk3_advance": (I, [C, P, P, P, I, T, P]),
+        "gbf_probe_arith": (I, [I, P, I, I, I, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str) -> None:
+    if status != GBF_OK:
+        raise GbfError(f"{what}: {STATUS.get(status, status)} ({status})")

@@ -1,0 +1,211 @@
+// C ABI of the GB300 single-phase right-hand side (declarations and reference
+// citations in include/gbfluids.h).  Every entry point validates its inputs,
+// enqueues work on the caller's stream and returns a status code; none of
+// them traps, synchronises or allocates device memory.
+#include <math.h>
+#include <stdint.h>
+
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+int make_case_info(const gbf_case* c, CaseInfo* ci) {
+  if (!c || !ci) return GBF_ERR_INVALID_ARGUMENT;
+  ci->active_mask = 0;
+  ci->cells = 1;
+  ci->halo_cells = 1;
+  ci->nh = c->nh;
+  double mdx = INFINITY;
+  for (int a = 0; a < 3; ++a) {
+    if (c->n[a] < 1) return GBF_ERR_SIZE;
+    ci->n[a] = c->n[a];
+    const bool act = c->n[a] > 1;
+    if (act) {
+      ci->active_mask |= 1 << a;
+      if (!(c->dx[a] > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
+      mdx = fmin(mdx, c->dx[a]);
+    }
+    ci->hs[a] = act ? c->n[a] + 2 * c->nh : 1;
+    ci->cells *= c->n[a];
+    ci->halo_cells *= ci->hs[a];
+  }
+  if (ci->active_mask == 0) return GBF_ERR_SIZE;
+  if (ci->cells > (1LL << 31) - 1) return GBF_ERR_SIZE;
+  ci->min_dx = mdx;
+  ci->fp.gamma = c->gamma;
+  ci->fp.gm1 = c->gamma - 1.0;
+  ci->fp.stencil_eps = c->stencil_eps;
+  ci->fp.signal_speed = c->signal_speed;
+  ci->fp.frozen_state = c->frozen_state;
+  return GBF_OK;
+}
+
+static int check_case(const gbf_case* c, CaseInfo* ci) {
+  int st = make_case_info(c, ci);
+  if (st != GBF_OK) return st;
+  if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var != GBF_RECVAR_PRIMITIVE) return GBF_ERR_UNSUPPORTED;
+  if (c->riemann != GBF_RIEMANN_HLLC && c->riemann != GBF_RIEMANN_RUSANOV) return GBF_ERR_UNSUPPORTED;
+  if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
+    return GBF_ERR_UNSUPPORTED;
+  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) return GBF_ERR_UNSUPPORTED;
+  if (!(c->gamma > 1.0)) return GBF_ERR_INVALID_ARGUMENT;
+  const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
+  if (c->nh < R) return GBF_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; ++a) {
+    if (c->n[a] > 1) {
+      if (c->n[a] < c->nh) return GBF_ERR_SIZE;  // halo retrieve slices need nh interior cells
+      for (int s = 0; s < 2; ++s) {
+        const int b = c->bc[2 * a + s];
+        if (b != GBF_BC_PERIODIC && b != GBF_BC_ZEROGRADIENT && b != GBF_BC_SYMMETRY)
+          return GBF_ERR_UNSUPPORTED;
+      }
+      if ((c->bc[2 * a] == GBF_BC_PERIODIC) != (c->bc[2 * a + 1] == GBF_BC_PERIODIC))
+        return GBF_ERR_INVALID_ARGUMENT;
+    }
+  }
+  if (!(c->cfl > 0.0) && !(c->fixed_dt > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
+  return GBF_OK;
+}
+
+}  // namespace gbf
+
+using namespace gbf;
+
+extern "C" {
+
+int gbf_abi_version(void) { return GBF_ABI_VERSION; }
+
+const char* gbf_status_string(int status) {
+  switch (status) {
+    case GBF_OK: return "ok";
+    case GBF_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GBF_ERR_UNSUPPORTED: return "unsupported setup";
+    case GBF_ERR_CUDA: return "CUDA launch error";
+    case GBF_ERR_SIZE: return "invalid or unsupported size";
+    case GBF_ERR_ALIGNMENT: return "misaligned pointer";
+    default: return "unknown status";
+  }
+}
+
+int gbf_case_check(const gbf_case* c) {
+  CaseInfo ci;
+  return check_case(c, &ci);
+}
+
+static bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+
+int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!prims || !rhs) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(prims) || !aligned8(rhs)) return GBF_ERR_ALIGNMENT;
+  SweepParams p;
+  int threads;
+  size_t smem;
+  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
+  if (st != GBF_OK) return st;
+  p.prims_halo = prims;
+  p.out = rhs;
+  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS);
+}
+
+int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!prims) return GBF_ERR_INVALID_ARGUMENT;
+  return launch_halo_fill(c, ci, prims, cons, (cudaStream_t)stream);
+}
+
+int gbf_prims_from_cons(const gbf_case* c, const double* cons, double* prims, int64_t count,
+                        void* stream) {
+  if (!c || !cons || !prims || count < 0) return GBF_ERR_INVALID_ARGUMENT;
+  return launch_convert(c, cons, prims, count, 1, (cudaStream_t)stream);
+}
+
+int gbf_cons_from_prims(const gbf_case* c, const double* prims, double* cons, int64_t count,
+                        void* stream) {
+  if (!c || !cons || !prims || count < 0) return GBF_ERR_INVALID_ARGUMENT;
+  return launch_convert(c, prims, cons, count, 0, (cudaStream_t)stream);
+}
+
+int gbf_stage_integrate(const gbf_case* c, double* cons, const double* cons0, const double* rhs,
+                        const double* dt, int stage, void* stream) {
+  CaseInfo ci;
+  int st = make_case_info(c, &ci);
+  if (st != GBF_OK) return st;
+  if (stage < 0 || stage > 2 || !cons || !rhs || !dt) return GBF_ERR_INVALID_ARGUMENT;
+  if (stage > 0 && !cons0) return GBF_ERR_INVALID_ARGUMENT;
+  return launch_stage_integrate(c, ci, cons, cons0, rhs, dt, stage, (cudaStream_t)stream);
+}
+
+size_t gbf_dt_workspace_bytes(void) { return 2 * sizeof(unsigned long long); }
+
+int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream) {
+  CaseInfo ci;
+  int st = make_case_info(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!prims || !dt_out || !workspace) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(workspace)) return GBF_ERR_ALIGNMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* red = (unsigned long long*)workspace;
+  if ((st = launch_reduce_init(red, s)) != GBF_OK) return st;
+  if ((st = launch_reduce_halo_prims(ci, prims, red, s)) != GBF_OK) return st;
+  return launch_dt_finalize(c, ci, red, dt_out, nullptr, 0, s);
+}
+
+size_t gbf_rk3_workspace_bytes(const gbf_case* c) {
+  CaseInfo ci;
+  if (make_case_info(c, &ci) != GBF_OK) return 0;
+  return (size_t)2 * 5 * (size_t)ci.cells * sizeof(double);
+}
+
+// dt_state = {dt, t, max signal speed bits, min density bits}
+int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!cons || !dt_state) return GBF_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((st = launch_set_scalar(dt_state + 1, t0, s)) != GBF_OK) return st;
+  unsigned long long* red = (unsigned long long*)(dt_state + 2);
+  if ((st = launch_reduce_init(red, s)) != GBF_OK) return st;
+  if ((st = launch_reduce_cons(ci, cons, red, s)) != GBF_OK) return st;
+  return launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 0, s);
+}
+
+int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
+                    const gbf_tile* tile, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!cons || !dt_state || !workspace || steps < 0) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(cons) || !aligned8(workspace) || !aligned8(dt_state)) return GBF_ERR_ALIGNMENT;
+  SweepParams p;
+  int threads;
+  size_t smem;
+  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
+  if (st != GBF_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* A = (double*)workspace;
+  double* B = A + 5 * ci.cells;
+  unsigned long long* red = (unsigned long long*)(dt_state + 2);
+  p.dt_state = dt_state;
+  for (int step = 0; step < steps; ++step) {
+    // U1 = U^n + dt L(U^n)
+    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = A; p.reduce_dt = 0;
+    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    // U2 = 3/4 U^n + 1/4 U1 + 1/4 dt L(U1)
+    p.stage = 1; p.cons = A; p.cons0 = cons; p.out = B;
+    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    // U^{n+1} = 1/3 U^n + 2/3 U2 + 2/3 dt L(U2), written over U^n (read pointwise)
+    p.stage = 2; p.cons = B; p.cons0 = cons; p.out = cons; p.reduce_dt = 1;
+    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
+  }
+  return GBF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// Launch-side declarations shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbf_sweep.cuh"
+
+namespace gbf {
+
+// Host-side view of a validated case.
+struct CaseInfo {
+  int n[3];
+  int active_mask;
+  int nh;
+  int hs[3];               // halo-buffer extents
+  long long cells;         // interior cells
+  long long halo_cells;    // cells of a halo buffer
+  double min_dx;
+  FaceParams fp;
+};
+
+int make_case_info(const gbf_case* c, CaseInfo* ci);
+
+// fills p.{n,t,tiles,...} from the case and tile; returns status
+int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
+                      int* threads, size_t* smem);
+
+// launch the sweep kernel instantiation for (recon, riemann, mode)
+int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem,
+                 cudaStream_t s, int mode);
+
+// auxiliary kernels (gbf_aux.cu)
+int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
+                     cudaStream_t s);
+int launch_convert(const gbf_case* c, const double* in, double* out, long long count, int to_prims,
+                   cudaStream_t s);
+int launch_stage_integrate(const gbf_case* c, const CaseInfo& ci, double* cons,
+                           const double* cons0, const double* rhs, const double* dt, int stage,
+                           cudaStream_t s);
+int launch_set_scalar(double* dst, double v, cudaStream_t s);
+// reduction slots: red[0] = max signal speed bits, red[1] = min density bits
+int launch_reduce_init(unsigned long long* red, cudaStream_t s);
+int launch_reduce_halo_prims(const CaseInfo& ci, const double* prims, unsigned long long* red,
+                             cudaStream_t s);
+int launch_reduce_cons(const CaseInfo& ci, const double* cons, unsigned long long* red,
+                       cudaStream_t s);
+// dt from reduction slots; when advance_time, dt_state[1] += previous dt first
+int launch_dt_finalize(const gbf_case* c, const CaseInfo& ci, unsigned long long* red,
+                       double* dt_out, double* t_inout, int advance_time, cudaStream_t s);
+
+}  // namespace gbf

@@ -1,0 +1,284 @@
+// Device-side physics of the single-phase finite-volume right-hand side:
+// ideal-gas EOS, cell-face reconstruction, signal speeds and Riemann fluxes.
+//
+// Every function restates the corresponding JAX-Fluids routine (paths relative
+// to src/jaxfluids) in FP64.  Per-face state lives in small register arrays
+// indexed only with compile-time constants (the sweep axis is a template
+// parameter), so nothing spills to local memory through dynamic indexing.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbfluids.h"
+
+namespace gbf {
+
+struct FaceParams {
+  double gamma;        // specific heat ratio
+  double gm1;          // gamma - 1.0 (computed once on the host, like ideal_gas.py)
+  double stencil_eps;  // WENO / MUSCL epsilon (precision.py:53, 1e-30)
+  int signal_speed;    // GBF_SIGNAL_*
+  int frozen_state;    // GBF_FROZEN_*
+};
+
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+// ---------------------------------------------------------------------------
+// Ideal gas and equation layout
+// ---------------------------------------------------------------------------
+
+// materials/single_materials/ideal_gas.py:69-71
+__device__ __forceinline__ double speed_of_sound(double p, double rho, const FaceParams& fp) {
+  return sqrt(fp.gamma * p / rho);
+}
+
+// equation_manager.py:93-101 (E = rho (|u|^2/2 + p / (rho (gamma-1))))
+__device__ __forceinline__ void cons_from_prims(const double P[5], double U[5], double gm1) {
+  const double rho = P[0];
+  const double e = P[4] / (rho * gm1);
+  U[0] = rho;
+  U[1] = rho * P[1];
+  U[2] = rho * P[2];
+  U[3] = rho * P[3];
+  U[4] = rho * (0.5 * (P[1] * P[1] + P[2] * P[2] + P[3] * P[3]) + e);
+}
+
+// equation_manager.py:164-171 (p = (gamma-1) e rho)
+__device__ __forceinline__ void prims_from_cons(const double U[5], double P[5], double gm1) {
+  const double rho = U[0];
+  const double one_rho = 1.0 / rho;
+  const double u = U[1] * one_rho;
+  const double v = U[2] * one_rho;
+  const double w = U[3] * one_rho;
+  const double e = U[4] * one_rho - 0.5 * (u * u + v * v + w * w);
+  P[0] = rho;
+  P[1] = u;
+  P[2] = v;
+  P[3] = w;
+  P[4] = gm1 * e * rho;
+}
+
+// equation_manager.py:237-252
+template <int AX>
+__device__ __forceinline__ void physical_flux(const double P[5], const double U[5], double F[5]) {
+  const double m = U[AX + 1];
+  F[0] = m;
+  F[1] = m * P[1];
+  F[2] = m * P[2];
+  F[3] = m * P[3];
+  F[4] = P[AX + 1] * (U[4] + P[4]);
+  F[AX + 1] += P[4];
+}
+
+// ---------------------------------------------------------------------------
+// Reconstruction
+// ---------------------------------------------------------------------------
+
+// WENO5-Z, Borges et al. 2008 (stencils/reconstruction/shock_capturing/weno/weno5_z.py:24-58,
+// weno5_base.py:24-51).  Arguments are (u_imm, u_im, u_i, u_ip, u_ipp) in the
+// reference's slice order; the right state passes the mirrored cells.
+__device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
+                                         double eps) {
+  const double b0 = (13.0 / 12.0) * sq(u0 - 2.0 * u1 + u2) + 0.25 * sq(u0 - 4.0 * u1 + 3.0 * u2);
+  const double b1 = (13.0 / 12.0) * sq(u1 - 2.0 * u2 + u3) + 0.25 * sq(u1 - u3);
+  const double b2 = (13.0 / 12.0) * sq(u2 - 2.0 * u3 + u4) + 0.25 * sq(3.0 * u2 - 4.0 * u3 + u4);
+  const double tau5 = fabs(b0 - b2);
+  const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
+  const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
+  const double a2 = 0.3 * (1.0 + tau5 / (b2 + eps));
+  const double one_a = 1.0 / (a0 + a1 + a2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  return (a0 * one_a) * p0 + (a1 * one_a) * p1 + (a2 * one_a) * p2;
+}
+
+// MUSCL3 with the MINMOD limiter (shock_capturing/muscl/muscl3.py:53-75, limiter.py:9-10).
+// (b0, b1, b2) are the reference's s_[0], s_[1], s_[2] for side j.
+template <int J>
+__device__ __forceinline__ double muscl_minmod(double b0, double b1, double b2, double eps) {
+  const double dc = (J == 0) ? b2 - b1 : b1 - b2;
+  const double du = (J == 0) ? b1 - b0 : b0 - b1;
+  const double r = (du >= eps) ? dc / (du + 1e-10) : (dc + eps) / (du + eps);
+  const double lim = fmax(0.0, fmin(1.0, r));
+  return (J == 0) ? b1 + 0.5 * lim * du : b1 - 0.5 * lim * du;
+}
+
+// MINMOD-AD (shock_capturing/muscl/minmod_ad.py:45-66)
+template <int J>
+__device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, double eps) {
+  const double dc = (J == 0) ? b2 - b1 : b1 - b2;
+  const double du = (J == 0) ? b1 - b0 : b0 - b1;
+  const double r = (du >= eps) ? dc / (du + 1e-100) : (dc + eps) / (du + eps);
+  return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : 1.5 * b1 - 0.5 * b0);
+}
+
+// Halo radius (cells each side of a face) of each reconstruction stencil.
+template <int RECON>
+struct ReconTraits;
+template <>
+struct ReconTraits<GBF_RECON_WENO5Z> {
+  static constexpr int R = 3;
+};
+template <>
+struct ReconTraits<GBF_RECON_MINMOD> {
+  static constexpr int R = 2;
+};
+template <>
+struct ReconTraits<GBF_RECON_MINMOD_AD> {
+  static constexpr int R = 2;
+};
+
+// Left (J=0) and right (J=1) face values from the 2R cells around the face;
+// w[k] is the cell at offset k - R from the face (w[R-1] left neighbour,
+// w[R] right neighbour).
+template <int RECON>
+__device__ __forceinline__ void reconstruct_pair(const double* w, double eps, double& L, double& R);
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO5Z>(const double* w, double eps,
+                                                                    double& L, double& R) {
+  // j=0 offsets (-3..1) -> w[0..4]; j=1 offsets (2..-2) -> w[5..1]
+  L = weno5z(w[0], w[1], w[2], w[3], w[4], eps);
+  R = weno5z(w[5], w[4], w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_MINMOD>(const double* w, double eps,
+                                                                    double& L, double& R) {
+  // j=0 offsets (-2,-1,0) -> w[0],w[1],w[2]; j=1 offsets (1,0,-1) -> w[3],w[2],w[1]
+  L = muscl_minmod<0>(w[0], w[1], w[2], eps);
+  R = muscl_minmod<1>(w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_MINMOD_AD>(const double* w, double eps,
+                                                                       double& L, double& R) {
+  L = minmod_ad<0>(w[0], w[1], w[2], eps);
+  R = minmod_ad<1>(w[3], w[2], w[1], eps);
+}
+
+// ---------------------------------------------------------------------------
+// Signal speeds and Riemann solvers (solvers/riemann_solvers/)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void signal_speeds(int kind, double uL, double uR, double aL, double aR,
+                                              double rhoL, double rhoR, double pL, double pR,
+                                              double gamma, double& SL, double& SR) {
+  switch (kind) {
+    case GBF_SIGNAL_EINFELDT: {  // signal_speeds.py:109-133
+      const double sL = sqrt(rhoL);
+      const double sR = sqrt(rhoR);
+      const double od = 1.0 / (sL + sR);
+      const double eta2 = 0.5 * sL * sR * od * od;
+      const double ubar = (sL * uL + sR * uR) * od;
+      const double dbar = sqrt((sL * aL * aL + sR * aR * aR) * od + eta2 * sq(uR - uL));
+      SL = fmin(ubar - dbar, uL - aL);
+      SR = fmax(ubar + dbar, uR + aR);
+      break;
+    }
+    case GBF_SIGNAL_DAVIS:  // :51-69
+      SL = fmin(uL - aL, uR - aR);
+      SR = fmax(uL + aL, uR + aR);
+      break;
+    case GBF_SIGNAL_ARITHMETIC: {  // :10-29
+      const double um = 0.5 * (uL + uR);
+      const double am = 0.5 * (aL + aR);
+      SL = fmin(um - am, uL - aL);
+      SR = fmax(um + am, uR + aR);
+      break;
+    }
+    case GBF_SIGNAL_RUSANOV: {  // :31-49
+      const double sp = fmax(fabs(uL) + aL, fabs(uR) + aR);
+      SL = -sp;
+      SR = sp;
+      break;
+    }
+    default: {  // GBF_SIGNAL_TORO, :135-157 with estimate_pressure :201-231
+      const double rho_bar = 0.5 * (rhoL + rhoR);
+      const double a_bar = 0.5 * (aL + aR);
+      const double p_pvrs = 0.5 * (pL + pR) - 0.5 * (uR - uL) * rho_bar * a_bar;
+      const double p_star = fmax(0.0, p_pvrs);
+      const double g_ = (gamma + 1) * 0.5 / gamma;
+      const double qL = (p_star <= pL) ? 1.0 : sqrt(1 + g_ * (p_star / pL - 1));
+      const double qR = (p_star <= pR) ? 1.0 : sqrt(1 + g_ * (p_star / pR - 1));
+      SL = uL - aL * qL;
+      SR = uR + aR * qR;
+      break;
+    }
+  }
+}
+
+// HLLC star-state flux of side K (HLLC.py:41-78), J=0 left (min(S,0)), J=1 right (max(S,0)).
+template <int AX, int J>
+__device__ __forceinline__ void hllc_star_flux(const double P[5], const double U[5], double S,
+                                               double Ss, double F[5]) {
+  constexpr int N = AX + 1;
+  constexpr int T1 = (AX == 0) ? 2 : 1;
+  constexpr int T2 = (AX == 2) ? 2 : 3;
+  const double pre = (S - P[N]) / (S - Ss) * P[0];
+  const double e_term = pre * (U[4] / U[0] + (Ss - P[N]) * (Ss + P[4] / P[0] / (S - P[N])));
+  double us[5] = {pre, pre, pre, pre, e_term};
+  us[N] *= Ss;
+  us[T1] *= P[T1];
+  us[T2] *= P[T2];
+  physical_flux<AX>(P, U, F);
+  const double wave = (J == 0) ? fmin(S, 0.0) : fmax(S, 0.0);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F[v] = F[v] + wave * (us[v] - U[v]);
+}
+
+// HLLC._solve_riemann_problem_xi_single_phase (HLLC.py:80-126)
+template <int AX>
+__device__ __forceinline__ void hllc(const double PL[5], const double PR[5], const double UL[5],
+                                     const double UR[5], const FaceParams& fp, double F[5]) {
+  constexpr int N = AX + 1;
+  const double cL = speed_of_sound(PL[4], PL[0], fp);
+  const double cR = speed_of_sound(PR[4], PR[0], fp);
+  double SL, SR;
+  signal_speeds(fp.signal_speed, PL[N], PR[N], cL, cR, PL[0], PR[0], PL[4], PR[4], fp.gamma, SL,
+                SR);
+  // compute_sstar, signal_speeds.py:159-199
+  const double rdL = PL[0] * (SL - PL[N]);
+  const double rdR = PR[0] * (SR - PR[N]);
+  const double Ss = ((PR[4] - PL[4]) + (PL[N] * rdL - PR[N] * rdR)) / (rdL - rdR);
+  double FL[5], FR[5];
+  hllc_star_flux<AX, 0>(PL, UL, SL, Ss, FL);
+  hllc_star_flux<AX, 1>(PR, UR, SR, Ss, FR);
+  // jnp.sign: +1, -1 or 0 (and NaN propagates through both weights)
+  const double sg = (Ss > 0.0) ? 1.0 : ((Ss < 0.0) ? -1.0 : ((Ss == 0.0) ? 0.0 : Ss));
+  const double wl = 0.5 * (1.0 + sg);
+  const double wr = 0.5 * (1.0 - sg);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F[v] = wl * FL[v] + wr * FR[v];
+}
+
+// Rusanov._solve_riemann_problem_xi_single_phase (Rusanov.py:25-47)
+template <int AX>
+__device__ __forceinline__ void rusanov(const double PL[5], const double PR[5], const double UL[5],
+                                        const double UR[5], const FaceParams& fp, double F[5]) {
+  constexpr int N = AX + 1;
+  const double cL = speed_of_sound(PL[4], PL[0], fp);
+  const double cR = speed_of_sound(PR[4], PR[0], fp);
+  const double alpha = fmax(fabs(PL[N]) + cL, fabs(PR[N]) + cR);
+  double FL[5], FR[5];
+  physical_flux<AX>(PL, UL, FL);
+  physical_flux<AX>(PR, UR, FR);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F[v] = 0.5 * (FL[v] + FR[v]) - 0.5 * alpha * (UR[v] - UL[v]);
+}
+
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void riemann_flux(const double PL[5], const double PR[5],
+                                             const FaceParams& fp, double F[5]) {
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, fp.gm1);
+  cons_from_prims(PR, UR, fp.gm1);
+  if (RIEMANN == GBF_RIEMANN_HLLC)
+    hllc<AX>(PL, PR, UL, UR, fp, F);
+  else
+    rusanov<AX>(PL, PR, UL, UR, fp, F);
+}
+
+}  // namespace gbf

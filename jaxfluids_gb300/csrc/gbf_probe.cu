@@ -1,0 +1,62 @@
+// Arithmetic-rate probes used by the benchmark to measure this GPU's FP64
+// roofline (no FP64 peak is published for the part): independent dependency
+// chains per thread, results stored so nothing is optimised away.
+#include <cuda_runtime.h>
+
+#include "gbfluids.h"
+
+namespace {
+
+constexpr int kChains = 8;
+
+template <int MODE>
+__global__ void probe_kernel(double* out, int iters, double seed) {
+  double a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = seed + 1e-3 * (threadIdx.x + k);
+  const double m = 0.999999999;
+  const double c = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) {
+      if (MODE == GBF_PROBE_DFMA) a[k] = fma(a[k], m, c);
+      if (MODE == GBF_PROBE_DDIV) a[k] = c + 1.0 / a[k];
+      if (MODE == GBF_PROBE_DSQRT) a[k] = sqrt(a[k]) + 0.5;
+      if (MODE == GBF_PROBE_FFMA) a[k] = (double)fmaf((float)a[k], 0.9999f, 1e-7f);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// FP32 rate: keep the chain in float registers
+__global__ void probe_ffma_kernel(double* out, int iters, double seed) {
+  float a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = (float)seed + 1e-3f * (threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) a[k] = fmaf(a[k], 0.9999f, 1e-7f);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream) {
+  if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) return GBF_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (mode) {
+    case GBF_PROBE_DFMA: probe_kernel<GBF_PROBE_DFMA><<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
+    case GBF_PROBE_DDIV: probe_kernel<GBF_PROBE_DDIV><<<blocks, threads, 0, s>>>(out, iters, 1.5); break;
+    case GBF_PROBE_DSQRT: probe_kernel<GBF_PROBE_DSQRT><<<blocks, threads, 0, s>>>(out, iters, 2.0); break;
+    case GBF_PROBE_FFMA: probe_ffma_kernel<<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
+    default: return GBF_ERR_INVALID_ARGUMENT;
+  }
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}

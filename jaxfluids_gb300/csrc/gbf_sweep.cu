@@ -1,0 +1,122 @@
+// Instantiations and host launch of the sweep kernel.
+#include <algorithm>
+
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+namespace {
+
+constexpr int kMaxCellsPerThread = 4;
+
+template <int RECON>
+constexpr int recon_radius() {
+  return ReconTraits<RECON>::R;
+}
+
+int radius_of(int recon) {
+  return recon == GBF_RECON_WENO5Z ? 3 : 2;
+}
+
+template <int RECON, int RIEMANN, int MODE>
+int launch_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  auto kern = sweep_kernel<RECON, RIEMANN, MODE, kMaxCellsPerThread>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return GBF_ERR_CUDA;
+  const int grid = p.tiles[0] * p.tiles[1] * p.tiles[2];
+  kern<<<grid, threads, smem, s>>>(p);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+template <int RECON, int MODE>
+int launch_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  if (riemann == GBF_RIEMANN_HLLC) return launch_one<RECON, GBF_RIEMANN_HLLC, MODE>(p, threads, smem, s);
+  return launch_one<RECON, GBF_RIEMANN_RUSANOV, MODE>(p, threads, smem, s);
+}
+
+template <int MODE>
+int launch_recon(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  switch (c->recon) {
+    case GBF_RECON_WENO5Z:
+      return launch_riemann<GBF_RECON_WENO5Z, MODE>(c->riemann, p, threads, smem, s);
+    case GBF_RECON_MINMOD:
+      return launch_riemann<GBF_RECON_MINMOD, MODE>(c->riemann, p, threads, smem, s);
+    default:
+      return launch_riemann<GBF_RECON_MINMOD_AD, MODE>(c->riemann, p, threads, smem, s);
+  }
+}
+
+}  // namespace
+
+int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
+                      int* threads, size_t* smem) {
+  SweepParams q{};
+  int t[3];
+  int thr = 256;
+  const int dim = ((ci.active_mask & 1) ? 1 : 0) + ((ci.active_mask & 2) ? 1 : 0) +
+                  ((ci.active_mask & 4) ? 1 : 0);
+  const bool user = tile && (tile->t[0] > 0 || tile->t[1] > 0 || tile->t[2] > 0);
+  if (user) {
+    for (int a = 0; a < 3; ++a) t[a] = std::max(1, tile->t[a]);
+    if (tile->threads > 0) thr = tile->threads;
+  } else {
+    // defaults: 512-cell tiles, longest along the contiguous (last active) axis
+    for (int a = 0; a < 3; ++a) t[a] = 1;
+    if (dim == 1) {
+      for (int a = 0; a < 3; ++a)
+        if (ci.active_mask & (1 << a)) t[a] = 256;
+    } else if (dim == 2) {
+      int k = 0;
+      for (int a = 0; a < 3; ++a)
+        if (ci.active_mask & (1 << a)) t[a] = (k++ == 0) ? 16 : 32;
+    } else {
+      t[0] = 8;
+      t[1] = 8;
+      t[2] = 8;
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    if (ci.n[a] == 1) t[a] = 1;
+    t[a] = std::min(t[a], ci.n[a]);
+  }
+  if (thr % 32 != 0 || thr < 32 || thr > 256) return GBF_ERR_INVALID_ARGUMENT;
+  const long long tvol = (long long)t[0] * t[1] * t[2];
+  if (tvol > (long long)kMaxCellsPerThread * thr) return GBF_ERR_INVALID_ARGUMENT;
+  const int R = radius_of(c->recon);
+  long long pmax = 0, fmax = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a))) continue;
+    long long pv = 1, fv = 1;
+    for (int b = 0; b < 3; ++b) {
+      pv *= t[b] + (b == a ? 2 * R : 0);
+      fv *= t[b] + (b == a ? 1 : 0);
+    }
+    pmax = std::max(pmax, pv);
+    fmax = std::max(fmax, fv);
+  }
+  const size_t bytes = (size_t)(pmax + fmax) * 5 * sizeof(double);
+  if (bytes > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; ++a) {
+    q.n[a] = ci.n[a];
+    q.t[a] = t[a];
+    q.tiles[a] = (ci.n[a] + t[a] - 1) / t[a];
+    q.hs[a] = ci.hs[a];
+    q.one_dx[a] = 1.0 / c->dx[a];
+  }
+  q.nh = ci.nh;
+  for (int f = 0; f < 6; ++f) q.bc[f] = c->bc[f];
+  q.fp = ci.fp;
+  q.active_mask = ci.active_mask;
+  *p = q;
+  *threads = thr;
+  *smem = bytes;
+  return GBF_OK;
+}
+
+int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
+                 int mode) {
+  if (mode == MODE_RHS) return launch_recon<MODE_RHS>(c, p, threads, smem, s);
+  return launch_recon<MODE_STAGE>(c, p, threads, smem, s);
+}
+
+}  // namespace gbf

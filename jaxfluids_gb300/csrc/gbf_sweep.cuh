@@ -1,0 +1,307 @@
+// Fused finite-volume sweep kernel.
+//
+// One CTA owns a tile of T0 x T1 x T2 cells.  For each active axis it stages
+// the primitives of the tile extended by the stencil radius R along that axis
+// (a "pencil box") in shared memory, computes every face flux of the tile
+// exactly once (one face per thread), and adds (1/dx)(F[i-1/2] - F[i+1/2]) to
+// per-thread right-hand-side accumulators in registers.  The epilogue either
+// stores the right-hand side (MODE_RHS, the SpaceSolver.compute_rhs drop-in)
+// or applies the TVD-RK3 stage combination in place of the state
+// (MODE_STAGE, the fused hot path), optionally reducing the next CFL time
+// step of the new state.
+//
+// The path is FP64-arithmetic bound on GB300 (about 2 FP64 lanes per SM and
+// clock against kilobytes of FP64 work per cell), so the layout minimises
+// repeated FP64 work rather than HBM traffic: faces are computed once per
+// tile (redundancy (T+1)/T per axis), the primitive conversion of a pencil
+// box is cheap next to the face work, and the state is re-read from L2 for
+// each axis.
+#pragma once
+
+#include "gbf_physics.cuh"
+
+namespace gbf {
+
+enum { MODE_RHS = 0, MODE_STAGE = 1 };
+
+struct SweepParams {
+  int n[3];          // interior cells per axis (1 = inactive)
+  int t[3];          // tile extents
+  int tiles[3];      // tiles per axis
+  int nh;            // halo width of the halo buffer (MODE_RHS)
+  int hs[3];         // halo buffer extents (MODE_RHS)
+  int bc[6];         // boundary types, GBF_FACE_* order (MODE_STAGE)
+  double one_dx[3];  // 1 / dx per axis
+  FaceParams fp;
+  const double* prims_halo;  // MODE_RHS input
+  const double* cons;        // MODE_STAGE: stage state U^k (interior layout)
+  const double* cons0;       // MODE_STAGE: step state U^n (interior layout)
+  double* out;               // MODE_RHS: rhs; MODE_STAGE: U^{k+1}
+  double* dt_state;          // {dt, t, max_signal, min_rho}
+  int stage;                 // RK stage 0, 1, 2
+  int reduce_dt;             // reduce the next time step of the new state
+  int active_mask;           // bit a set when axis a is active
+};
+
+__device__ __forceinline__ int idx3(int i0, int i1, int i2, int e1, int e2) {
+  return (i0 * e1 + i1) * e2 + i2;
+}
+
+// Boundary index remap along one axis for a logical cell coordinate g that may
+// lie in the halo (g < 0 or g >= n); returns the interior cell and whether the
+// normal velocity flips sign (halos/outer/boundary_condition.py:539-604).
+__device__ __forceinline__ int remap_bc(int g, int n, int bc_lo, int bc_hi, bool& flip) {
+  flip = false;
+  if (g < 0) {
+    if (bc_lo == GBF_BC_PERIODIC) return g + n;
+    if (bc_lo == GBF_BC_ZEROGRADIENT) return 0;
+    flip = true;           // SYMMETRY: halo layer j mirrors interior cell j
+    return -1 - g;
+  }
+  if (g >= n) {
+    if (bc_hi == GBF_BC_PERIODIC) return g - n;
+    if (bc_hi == GBF_BC_ZEROGRADIENT) return n - 1;
+    flip = true;
+    return 2 * n - 1 - g;
+  }
+  return g;
+}
+
+// Orders non-negative doubles as unsigned integers (for atomicMax).
+__device__ __forceinline__ unsigned long long ordered_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+
+template <int AX, int RECON, int RIEMANN, int MODE, int MAXC>
+__device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
+                                           double* sm_prim, double* sm_flux,
+                                           double (&acc)[MAXC][5], bool first) {
+  constexpr int R = ReconTraits<RECON>::R;
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+
+  // pencil box extents
+  int pe[3] = {ext[0], ext[1], ext[2]};
+  pe[AX] += 2 * R;
+  const int pvol = pe[0] * pe[1] * pe[2];
+
+  // ---- stage the primitives of the pencil box -------------------------
+  for (int i = tid; i < pvol; i += nthr) {
+    const int i2 = i % pe[2];
+    const int r = i / pe[2];
+    const int i1 = r % pe[1];
+    const int i0 = r / pe[1];
+    int g[3] = {o[0] + i0, o[1] + i1, o[2] + i2};
+    g[AX] -= R;
+    double P[5];
+    if (MODE == MODE_RHS) {
+      int b[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) b[a] = (p.n[a] > 1) ? g[a] + p.nh : 0;
+      const long long cs = (long long)p.hs[0] * p.hs[1] * p.hs[2];
+      const long long off = ((long long)b[0] * p.hs[1] + b[1]) * p.hs[2] + b[2];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) P[v] = __ldg(p.prims_halo + v * cs + off);
+    } else {
+      bool flip;
+      g[AX] = remap_bc(g[AX], p.n[AX], p.bc[2 * AX], p.bc[2 * AX + 1], flip);
+      const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+      const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+      double U[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
+      prims_from_cons(U, P, p.fp.gm1);
+      if (flip) P[AX + 1] = -P[AX + 1];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sm_prim[v * pvol + i] = P[v];
+  }
+  __syncthreads();
+
+  // ---- face fluxes, one face per thread --------------------------------
+  int fe[3] = {ext[0], ext[1], ext[2]};
+  fe[AX] += 1;
+  const int fvol = fe[0] * fe[1] * fe[2];
+  const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
+  for (int f = tid; f < fvol; f += nthr) {
+    const int f2 = f % fe[2];
+    const int r = f / fe[2];
+    const int f1 = r % fe[1];
+    const int f0 = r / fe[1];
+    // face f_AX lies between pencil cells f_AX + R - 1 and f_AX + R; the
+    // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
+    const int base = idx3(f0, f1, f2, pe[1], pe[2]);
+    double PL[5], PR[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double w[2 * R];
+#pragma unroll
+      for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
+      reconstruct_pair<RECON>(w, p.fp.stencil_eps, PL[v], PR[v]);
+    }
+    double F[5];
+    riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
+  }
+  __syncthreads();
+
+  // ---- divergence into the per-thread accumulators ---------------------
+  const int cvol = ext[0] * ext[1] * ext[2];
+  const int fstride = (AX == 0) ? fe[1] * fe[2] : ((AX == 1) ? fe[2] : 1);
+  const double odx = p.one_dx[AX];
+#pragma unroll
+  for (int k = 0; k < MAXC; ++k) {
+    const int c = tid + k * nthr;
+    if (c < cvol) {
+      const int c2 = c % ext[2];
+      const int r = c / ext[2];
+      const int c1 = r % ext[1];
+      const int c0 = r / ext[1];
+      const int fl = idx3(c0, c1, c2, fe[1], fe[2]);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        // space_solver.py:597-599: one_dx * (F[:-1] - F[1:])
+        const double d = odx * (sm_flux[v * fvol + fl] - sm_flux[v * fvol + fl + fstride]);
+        acc[k][v] = first ? d : __dadd_rn(acc[k][v], d);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+
+// RK3 coefficients (RK3.py:27-29)
+__device__ __forceinline__ double rk3_combine(int stage, double U, double U0, double rhs, double dt) {
+  // time_integrator.py:34-58 + RK3.py:31-62: buf = a U + b U0 (stages 1, 2),
+  // then buf += (dt * m) * rhs; kept un-contracted to follow the reference order.
+  if (stage == 0) return __dadd_rn(U, __dmul_rn(__dmul_rn(dt, 1.0), rhs));
+  if (stage == 1) {
+    const double b = __dadd_rn(__dmul_rn(0.25, U), __dmul_rn(0.75, U0));
+    return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 0.25), rhs));
+  }
+  const double b = __dadd_rn(__dmul_rn(2.0 / 3.0, U), __dmul_rn(1.0 / 3.0, U0));
+  return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 2.0 / 3.0), rhs));
+}
+
+template <int RECON, int RIEMANN, int MODE, int MAXC>
+__global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
+  extern __shared__ double smem[];
+  const int b = blockIdx.x;
+  const int b2 = b % p.tiles[2];
+  const int b1 = (b / p.tiles[2]) % p.tiles[1];
+  const int b0 = b / (p.tiles[2] * p.tiles[1]);
+  const int o[3] = {b0 * p.t[0], b1 * p.t[1], b2 * p.t[2]};
+  const int ext[3] = {min(p.t[0], p.n[0] - o[0]), min(p.t[1], p.n[1] - o[1]),
+                      min(p.t[2], p.n[2] - o[2])};
+
+  // shared memory: pencil primitives, then face fluxes
+  constexpr int R = ReconTraits<RECON>::R;
+  int pmax = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (p.active_mask & (1 << a)) {
+      int v = (p.t[0] + (a == 0 ? 2 * R : 0)) * (p.t[1] + (a == 1 ? 2 * R : 0)) *
+              (p.t[2] + (a == 2 ? 2 * R : 0));
+      pmax = max(pmax, v);
+    }
+  }
+  double* sm_prim = smem;
+  double* sm_flux = smem + 5 * pmax;
+
+  double acc[MAXC][5];
+#pragma unroll
+  for (int k = 0; k < MAXC; ++k)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) acc[k][v] = 0.0;
+
+  bool first = true;
+  if (p.active_mask & 1) {
+    sweep_axis<0, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+    first = false;
+  }
+  if (p.active_mask & 2) {
+    sweep_axis<1, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+    first = false;
+  }
+  if (p.active_mask & 4) {
+    sweep_axis<2, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+  }
+
+  // ---- epilogue ---------------------------------------------------------
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const int cvol = ext[0] * ext[1] * ext[2];
+  double smax = 0.0;
+  double rmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+  double dt = 0.0;
+  if (MODE == MODE_STAGE) dt = p.dt_state[0];
+#pragma unroll
+  for (int k = 0; k < MAXC; ++k) {
+    const int c = threadIdx.x + k * blockDim.x;
+    if (c < cvol) {
+      const int c2 = c % ext[2];
+      const int r = c / ext[2];
+      const int c1 = r % ext[1];
+      const int c0 = r / ext[1];
+      const long long off = ((long long)(o[0] + c0) * p.n[1] + (o[1] + c1)) * p.n[2] + (o[2] + c2);
+      if (MODE == MODE_RHS) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) p.out[v * cs + off] = acc[k][v];
+      } else {
+        double Un[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const double U = p.cons[v * cs + off];
+          const double U0 = (p.stage == 0) ? U : p.cons0[v * cs + off];
+          Un[v] = rk3_combine(p.stage, U, U0, acc[k][v], dt);
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) p.out[v * cs + off] = Un[v];
+        if (p.reduce_dt) {
+          // time_step_size.py:96-109 on the primitives of the new state
+          double P[5];
+          prims_from_cons(Un, P, p.fp.gm1);
+          const double cc = speed_of_sound(P[4], P[0], p.fp);
+          double s = 0.0;
+          if (p.active_mask & 1) s = s + (fabs(P[1]) + cc);
+          if (p.active_mask & 2) s = s + (fabs(P[2]) + cc);
+          if (p.active_mask & 4) s = s + (fabs(P[3]) + cc);
+          smax = fmax(smax, s);
+          rmin = fmin(rmin, P[0]);
+        }
+      }
+    }
+  }
+  if (MODE == MODE_STAGE && p.reduce_dt) {
+    // warp shuffle -> shared -> one atomic per CTA; max/min are exact, so the
+    // result does not depend on the reduction order.
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+    }
+    __shared__ double red[2][32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      red[0][w] = smax;
+      red[1][w] = rmin;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int nw = blockDim.x >> 5;
+      smax = (threadIdx.x < nw) ? red[0][threadIdx.x] : 0.0;
+      rmin = (threadIdx.x < nw) ? red[1][threadIdx.x] : __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+        rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+      }
+      if (threadIdx.x == 0) {
+        atomicMax(reinterpret_cast<unsigned long long*>(p.dt_state + 2), ordered_bits(smax));
+        atomicMin(reinterpret_cast<unsigned long long*>(p.dt_state + 3), ordered_bits(rmin));
+      }
+    }
+  }
+}
+
+}  // namespace gbf

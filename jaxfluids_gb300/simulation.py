@@ -1,0 +1,134 @@
+"""Time stepping on the GB300 path.
+
+``SimulationManager`` mirrors the reference's stage loop
+(simulation_manager.py:670-1077) on halo buffers with the drop-in kernels:
+compute_rhs -> stage integration -> primitives from conservatives -> halo
+update, three times per TVD-RK3 step, and the CFL time step afterwards.
+
+``FusedRK3`` is the hot path: it keeps only the interior conservatives
+([5, Nx, Ny, Nz]) and advances them with one fused sweep kernel per RK stage
+(boundary conditions by index remapping, no halo buffers) plus one tiny
+time-step kernel per step; dt and t stay on the device, so a run of steps
+needs no host synchronisation and can be captured in a CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional, Tuple
+
+import torch
+
+from . import _lib
+from .config import EPS, CaseConfig
+from .solver import (EquationManager, HaloManager, SpaceSolver, TimeIntegrator, TimeStepSize,
+                     _ptr, _stream)
+
+
+class SimulationManager:
+    def __init__(self, config: CaseConfig, tile: Optional[_lib.GbfTile] = None):
+        self.config = config
+        self.equation_manager = EquationManager(config)
+        self.halo_manager = HaloManager(config)
+        self.space_solver = SpaceSolver(config, tile)
+        self.time_integrator = TimeIntegrator(config)
+        self.time_step_size = TimeStepSize(config)
+
+    def initialize(self, prims_interior: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+        """MaterialFieldsInitializer.create_material_fields (material_fields_initializer.py:148-210).
+
+        The buffer starts as eps (initialization/helper_functions.py:49-60), the
+        interior takes the given primitives (5 components, or rho, the active
+        velocities and p), conservatives are computed over the whole buffer and
+        the halos are filled.
+        """
+        cfg = self.config
+        dev = prims_interior.device
+        P = torch.full(cfg.halo_shape(), EPS, dtype=torch.float64, device=dev)
+        inner = cfg.interior_slices()
+        if prims_interior.shape[0] == 5:
+            P[inner] = prims_interior.reshape(cfg.interior_shape())
+        else:
+            ids = [0] + [1 + i for i in cfg.active] + [4]
+            for k, idx in enumerate(ids):
+                P[(idx,) + inner[1:]] = prims_interior[k].reshape(cfg.cells)
+        U = self.equation_manager.get_conservatives_from_primitives(P)
+        P, U = self.halo_manager.perform_halo_update_material(P, 0.0, False, False, U)
+        return U, P
+
+    def compute_time_step_size(self, primitives: torch.Tensor) -> torch.Tensor:
+        return self.time_step_size(primitives)
+
+    def do_integration_step(self, conservatives: torch.Tensor, primitives: torch.Tensor,
+                            dt: torch.Tensor, t: float = 0.0):
+        """One TVD-RK3 step through the drop-in kernels (do_runge_kutta_stages)."""
+        init = conservatives
+        cons, prims = conservatives, primitives
+        for stage in range(3):
+            (rhs_buf, _, _) = self.space_solver.compute_rhs(cons, prims, None, t, dt)
+            rhs = rhs_buf.euler_buffers.conservatives
+            cons = self.time_integrator.perform_stage_integration(
+                cons, rhs, init if stage > 0 else None, dt, stage)
+            prims = self.equation_manager.get_primitives_from_conservatives(cons)
+            prims, cons = self.halo_manager.perform_halo_update_material(prims, t, False, False, cons)
+        return cons, prims
+
+    def simulate(self, conservatives, primitives, end_time: float = math.inf,
+                 end_step: int = 1 << 62, t0: float = 0.0, log=None):
+        """SimulationManager.advance without output: host loop, dt not clipped."""
+        t, step = t0, 0
+        dt = self.compute_time_step_size(primitives)
+        if log is not None:
+            log.append((t, float(dt), float(primitives[self.config.interior_slices()][0].min())))
+        while t < end_time and step < end_step:
+            conservatives, primitives = self.do_integration_step(conservatives, primitives, dt, t)
+            t += float(dt)
+            step += 1
+            dt = self.compute_time_step_size(primitives)
+            if log is not None:
+                log.append((t, float(dt), float(primitives[self.config.interior_slices()][0].min())))
+        return conservatives, primitives, t, step
+
+
+class FusedRK3:
+    """Fused TVD-RK3 stepping of interior conservatives (gbf_rk3_advance)."""
+
+    def __init__(self, config: CaseConfig, device="cuda", tile: Optional[_lib.GbfTile] = None):
+        self.config = config
+        self.lib = _lib.load()
+        self.case = config.to_c()
+        st = self.lib.gbf_case_check(ctypes.byref(self.case))
+        if st == -2:
+            raise NotImplementedError("setup not supported by the fused CUDA path")
+        _lib.check(st, "case check")
+        self.tile = tile
+        nbytes = int(self.lib.gbf_rk3_workspace_bytes(ctypes.byref(self.case)))
+        self.device = torch.device(device)
+        self.workspace = torch.empty(nbytes // 8, dtype=torch.float64, device=self.device)
+        # {dt, t, reduction slot (max signal speed), reduction slot (min density)}
+        self.dt_state = torch.zeros(4, dtype=torch.float64, device=self.device)
+        self.cons = torch.empty(config.interior_shape(), dtype=torch.float64, device=self.device)
+
+    def set_state(self, cons_interior: torch.Tensor, t0: float = 0.0) -> None:
+        self.cons.copy_(cons_interior.reshape(self.config.interior_shape()))
+        _lib.check(self.lib.gbf_rk3_init(ctypes.byref(self.case), _ptr(self.cons), _ptr(self.dt_state),
+                                         float(t0), _stream()), "rk3 init")
+
+    def advance(self, steps: int) -> None:
+        tile = ctypes.byref(self.tile) if self.tile is not None else None
+        _lib.check(self.lib.gbf_rk3_advance(ctypes.byref(self.case), _ptr(self.cons), _ptr(self.dt_state),
+                                            _ptr(self.workspace), int(steps), tile, _stream()), "rk3 advance")
+
+    @property
+    def dt(self) -> torch.Tensor:
+        return self.dt_state[0]
+
+    @property
+    def t(self) -> torch.Tensor:
+        return self.dt_state[1]
+
+    def primitives(self) -> torch.Tensor:
+        out = torch.empty_like(self.cons)
+        _lib.check(self.lib.gbf_prims_from_cons(ctypes.byref(self.case), _ptr(self.cons), _ptr(out),
+                                                self.config.n_cells, _stream()), "prims")
+        return out

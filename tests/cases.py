@@ -1,0 +1,66 @@
+"""Shared test cases: the same setup as an oracle case and as a CaseConfig."""
+import math
+
+import numpy as np
+import torch
+
+from oracle import jf_oracle as O
+
+
+def both(cells, bc, **kw):
+    """(OracleCase, CaseConfig) for the same setup."""
+    from jaxfluids_gb300.config import CaseConfig
+    bcd = {f: bc[f] if isinstance(bc, dict) else bc for f in O.FACES}
+    oc = O.OracleCase(cells=cells, bc=bcd, **kw)
+    fields = {k: v for k, v in kw.items() if k in (
+        "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
+        "cfl", "fixed_dt", "viscous", "heat", "mu")}
+    cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
+    return oc, cc
+
+
+def sod_prims(n=200):
+    x = (np.arange(n) + 0.5) / n
+    rho = np.where(x <= 0.5, 1.0, 0.125)
+    p = np.where(x <= 0.5, 1.0, 0.1)
+    return torch.from_numpy(np.stack([rho, np.zeros(n), p]).reshape(3, n, 1, 1))
+
+
+def quadrant_prims(nx, ny, seed=0):
+    """2-D four-quadrant Riemann problem, states drawn from U ranges."""
+    rng = np.random.default_rng(seed)
+    st = np.stack([rng.uniform(0.1, 2, 4), rng.uniform(-1, 1, 4), rng.uniform(-1, 1, 4),
+                   rng.uniform(0.1, 2, 4)])
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    q = (X >= 0.5).astype(int) + 2 * (Y >= 0.5).astype(int)
+    f = st[:, q]  # [4, nx, ny]
+    return torch.from_numpy(np.stack([f[0], f[1], f[2], f[3]]).reshape(4, nx, ny, 1))
+
+
+def tgv_prims(n, ma=0.1, gamma=1.4, lengths=(2 * math.pi,) * 3, dims=3):
+    """Taylor-Green vortex initial condition on [0, 2 pi]^3 (or a 2-D slice)."""
+    p0 = 1.0 / (gamma * ma * ma)
+    axes = [(np.arange(n) + 0.5) * (lengths[i] / n) for i in range(3)]
+    if dims == 2:
+        axes[2] = np.array([0.0])
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+    u = np.sin(X) * np.cos(Y) * np.cos(Z)
+    v = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    w = np.zeros_like(X)
+    p = p0 + (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
+    rho = np.ones_like(X)
+    return torch.from_numpy(np.stack([rho, u, v, w, p]))
+
+
+def rel_err(a: torch.Tensor, b: torch.Tensor) -> float:
+    """max over variables of ||a_v - b_v||_inf / ||b_v||_inf."""
+    a = a.detach().cpu().reshape(a.shape[0], -1)
+    b = b.detach().cpu().reshape(b.shape[0], -1)
+    worst = 0.0
+    for v in range(a.shape[0]):
+        den = b[v].abs().max().item()
+        num = (a[v] - b[v]).abs().max().item()
+        worst = max(worst, num / den if den > 0 else num)
+    return worst

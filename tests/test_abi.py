@@ -1,0 +1,94 @@
+"""The C-ABI library builds, loads and exports every declared symbol (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from jaxfluids_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "gbfluids.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(gbf_\w+)\s*\(", txt, re.M)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from jaxfluids_gb300 import _lib
+    declared = _declared()
+    assert declared, "no declarations parsed"
+    assert sorted(_lib.EXPORTS) == declared
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_version_and_status_strings(lib):
+    assert lib.gbf_abi_version() == 1
+    assert lib.gbf_status_string(0) == b"ok"
+    assert lib.gbf_status_string(-2) == b"unsupported setup"
+
+
+def _cfg(**kw):
+    from jaxfluids_gb300.config import CaseConfig
+    base = dict(cells=(64, 1, 1), bc={f: "ZEROGRADIENT" for f in ("east", "west")})
+    base.update(kw)
+    return CaseConfig(**base)
+
+
+def test_case_check_accepts_and_rejects(lib):
+    c = _cfg().to_c()
+    assert lib.gbf_case_check(ctypes.byref(c)) == 0
+    c.recon_var = 1  # CHAR-PRIMITIVE is handled by a different kernel family
+    assert lib.gbf_case_check(ctypes.byref(c)) in (0, -2)
+    c = _cfg().to_c()
+    c.nh = 2  # WENO5-Z needs three halo cells
+    assert lib.gbf_case_check(ctypes.byref(c)) == -1
+    c = _cfg().to_c()
+    c.n[0] = 0
+    assert lib.gbf_case_check(ctypes.byref(c)) == -4
+    c = _cfg().to_c()
+    c.riemann = 7
+    assert lib.gbf_case_check(ctypes.byref(c)) == -2
+
+
+def test_null_pointers_are_rejected_without_a_gpu(lib):
+    c = _cfg().to_c()
+    assert lib.gbf_rhs(ctypes.byref(c), None, None, None, None) == -1
+    assert lib.gbf_halo_fill(ctypes.byref(c), None, None, None) == -1
+    assert lib.gbf_rk3_advance(ctypes.byref(c), None, None, None, 1, None, None) == -1
+    assert lib.gbf_rk3_workspace_bytes(ctypes.byref(c)) == 2 * 5 * 64 * 8
+
+
+def test_config_from_reference_setup_dicts():
+    from jaxfluids_gb300.config import CaseConfig, SetupError
+    case = {
+        "domain": {"x": {"cells": 100, "range": [0.0, 1.0]}, "y": {"cells": 1, "range": [0.0, 1.0]},
+                   "z": {"cells": 1, "range": [0.0, 1.0]}},
+        "boundary_conditions": {"east": {"type": "ZEROGRADIENT"}, "west": {"type": "ZEROGRADIENT"},
+                                "north": {"type": "INACTIVE"}, "south": {"type": "INACTIVE"},
+                                "top": {"type": "INACTIVE"}, "bottom": {"type": "INACTIVE"}},
+        "material_properties": {"equation_of_state": {"model": "IdealGas", "specific_heat_ratio": 1.4,
+                                                      "specific_gas_constant": 1.0}},
+    }
+    num = {"conservatives": {"halo_cells": 4, "time_integration": {"integrator": "RK3", "fixed_timestep": 1e-3},
+                             "convective_fluxes": {"convective_solver": "GODUNOV", "godunov": {
+                                 "riemann_solver": "RUSANOV", "signal_speed": "EINFELDT",
+                                 "reconstruction_stencil": "MINMOD-AD", "reconstruction_variable": "PRIMITIVE"}}},
+           "active_physics": {"is_convective_flux": True, "is_viscous_flux": False}}
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.cells == (100, 1, 1) and cfg.nh == 4 and cfg.recon == "MINMOD-AD"
+    assert cfg.riemann == "RUSANOV" and cfg.fixed_dt == 1e-3 and cfg.active == [0]
+    bad = dict(num)
+    bad["conservatives"] = dict(num["conservatives"], halo_cells=2)
+    bad["conservatives"]["convective_fluxes"] = {"godunov": {"reconstruction_stencil": "WENO5-Z"}}
+    with pytest.raises(SetupError):
+        CaseConfig.from_setups(case, bad)
+    with pytest.raises(NotImplementedError):
+        CaseConfig.from_setups(case, {"conservatives": {"convective_fluxes": {"convective_solver": "FLUX-SPLITTING"}}})
