@@ -543,7 +543,9 @@ def _face_retrieve_slice(case: OracleCase, face: str, btype: str) -> Tuple[slice
     elif btype == "ZEROGRADIENT":
         s = slice(-nh - 1, -nh) if hi else slice(nh, nh + 1)
     elif btype == "SYMMETRY":
-        s = slice(-nh - 1, -2 * nh - 1, -1) if hi else slice(2 * nh - 1, nh - 1, -1)
+        # reference: [-nh-1:-2nh-1:-1] (hi) and [2nh-1:nh-1:-1] (lo); torch has no
+        # negative steps, so return the forward slice and let the caller flip it
+        s = slice(-2 * nh, -nh) if hi else slice(nh, 2 * nh)
     else:
         raise NotImplementedError(btype)
     return _axis_slice(case, axis, s)
@@ -569,6 +571,7 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
             reps[axis + 1] = case.nh
             h = h.repeat(*reps)
         if btype == "SYMMETRY":
+            h = torch.flip(h, dims=(axis + 1,))
             sign = torch.ones(5, dtype=P.dtype).reshape(5, 1, 1, 1)
             sign[axis + 1] = -1.0
             h = h * sign

@@ -75,6 +75,8 @@ def test_rhs_matches_oracle(name, kw, kind):
     oc, cc = both(cells, bc, **kw)
     gpu, ref = _rhs_pair(oc, cc, _prims_for(kind, cells))
     assert rel_err(gpu, ref) <= RHS_TOL
+    # same operation order, no contraction, IEEE division and sqrt: bitwise equal
+    assert torch.equal(gpu.cpu(), ref)
 
 
 def test_rhs_xz_plane_with_inactive_middle_axis():
