@@ -37,12 +37,12 @@ UNIT = "cell-updates/s"
 # (80 B); stages 2 and 3 read U^k and U^n and write (120 B each) -> 320 B.
 BYTES_PER_CELL_UPDATE = 320.0
 # FP64 operations per cell-update of the stage kernels (double-precision add,
-# mul and fma instructions, fma counted twice) from the ncu capture summarised
-# in profiles/sweep_kernel_tgv.md; None until measured.
-FP64_FLOP_PER_CELL_UPDATE = None
-# DRAM bytes per stage launch at 128^3 from the same capture (scaled from the
-# captured case by cells); None until measured.
-DRAM_BYTES_PER_LAUNCH = None
+# mul and fma thread instructions, fma counted twice) from the ncu capture of
+# the sweep kernel on this workload (summary kept in the profiles directory).
+FP64_FLOP_PER_CELL_UPDATE = 17070.0
+# DRAM bytes (read + write) of one stage launch at 128^3 from the same capture
+# (the captured launch is the second RK stage: 120 B/cell algorithmic).
+DRAM_BYTES_PER_LAUNCH = 233.7e6
 
 
 def tgv_state(n, device, dtype=torch.float64):
