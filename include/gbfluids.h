@@ -171,6 +171,26 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
                     const gbf_tile* tile, void* stream);
 
 /*
+ * Allocation-free gbf_rk3_advance.  It has no counterpart in the reference.
+ * For callers that can neither pass a workspace nor let the library call
+ * cudaMalloc: an XLA custom call, whose device memory must come from XLA's
+ * allocator (which reserves most of the GPU up front); host code with a fixed
+ * device-memory budget; loops that must not stall on cudaFree, which
+ * synchronises the device.  The two stage buffers live in a fixed 32 MiB
+ * device array inside the library (held by every GPU that loads it until the
+ * process exits), so cases are limited to GBF_NOALLOC_MAX_CELLS interior
+ * cells; larger cases return GBF_ERR_SIZE.  Same arguments and results as
+ * gbf_rk3_advance without the workspace; cons and dt_state are the caller's
+ * (initialise dt_state with gbf_rk3_init).  The first call on each device looks
+ * up the array's device address with that device current; make that first
+ * call before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams, other threads) race on it.
+ */
+#define GBF_NOALLOC_MAX_CELLS 419430
+int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* dt_state, int steps,
+                            const gbf_tile* tile, void* stream);
+
+/*
  * Measurement helper with no counterpart in the reference: runs `iters`
  * iterations of 8 independent dependency chains of one operation per thread
  * (blocks x threads threads) and stores one value per thread in out, so the

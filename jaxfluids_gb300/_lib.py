@@ -30,8 +30,11 @@ EXPORTS = (
     "gbf_abi_version", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
-    "gbf_rk3_advance", "gbf_probe_arith",
+    "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
 )
+
+# interior cells the allocation-free entry point's built-in scratch holds
+NOALLOC_MAX_CELLS = 419430
 
 
 class GbfCase(ctypes.Structure):
@@ -95,6 +98,7 @@ def load() -> ctypes.CDLL:
         "gbf_rk3_workspace_bytes": (ctypes.c_size_t, [C]),
         "gbf_rk3_init": (I, [C, P, P, ctypes.c_double, P]),
         "gbf_rk3_advance": (I, [C, P, P, P, I, T, P]),
+        "gbf_rk3_advance_noalloc": (I, [C, P, P, I, T, P]),
         "gbf_probe_arith": (I, [I, P, I, I, I, P]),
     }
     for name, (res, args) in sig.items():
