@@ -44,7 +44,12 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   int st = make_case_info(c, ci);
   if (st != GBF_OK) return st;
   if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var != GBF_RECVAR_PRIMITIVE) return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var != GBF_RECVAR_PRIMITIVE && c->recon_var != GBF_RECVAR_CHAR_PRIMITIVE)
+    return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE &&
+      (c->recon != GBF_RECON_WENO5Z ||
+       (c->frozen_state != GBF_FROZEN_ARITHMETIC && c->frozen_state != GBF_FROZEN_ROE)))
+    return GBF_ERR_UNSUPPORTED;
   if (c->riemann != GBF_RIEMANN_HLLC && c->riemann != GBF_RIEMANN_RUSANOV) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;

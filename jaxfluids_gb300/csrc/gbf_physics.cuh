@@ -114,9 +114,17 @@ __device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, dou
   return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : 1.5 * b1 - 0.5 * b0);
 }
 
+// Internal reconstruction id: WENO5-Z on Roe-characteristic variables
+// (reconstruction_variable CHAR-PRIMITIVE); same six-cell window as WENO5-Z.
+constexpr int RECON_WENO5Z_CHAR = 3;
+
 // Halo radius (cells each side of a face) of each reconstruction stencil.
 template <int RECON>
 struct ReconTraits;
+template <>
+struct ReconTraits<RECON_WENO5Z_CHAR> {
+  static constexpr int R = 3;
+};
 template <>
 struct ReconTraits<GBF_RECON_WENO5Z> {
   static constexpr int R = 3;
@@ -157,6 +165,107 @@ __device__ __forceinline__ void reconstruct_pair<GBF_RECON_MINMOD_AD>(const doub
                                                                        double& L, double& R) {
   L = minmod_ad<0>(w[0], w[1], w[2], eps);
   R = minmod_ad<1>(w[3], w[2], w[1], eps);
+}
+
+// ---------------------------------------------------------------------------
+// Characteristic decomposition (solvers/riemann_solvers/eigendecomposition.py)
+// ---------------------------------------------------------------------------
+
+// Eigendecomposition.compute_frozen_state, single phase (:120-281): density,
+// speed of sound and its square of the frozen state between cells L and R.
+__device__ __forceinline__ void frozen_state(const double L[5], const double R[5],
+                                             const FaceParams& fp, double& rho_a, double& c,
+                                             double& cc) {
+  if (fp.frozen_state == GBF_FROZEN_ARITHMETIC) {
+    const double rho = 0.5 * (L[0] + R[0]);
+    const double p = 0.5 * (L[4] + R[4]);
+    rho_a = rho;
+    c = sqrt(fp.gamma * p / rho);
+    cc = c * c;
+  } else {
+    // ROE: cc = psi_ave + grueneisen_ave * p_over_rho_ave (:223-268)
+    rho_a = sqrt(L[0] * R[0]);
+    const double sL = sqrt(L[0]);
+    const double sR = sqrt(R[0]);
+    const double rho_div = 1.0 / (sL + sR);
+    const double psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div;
+    const double gr_a = (sL * fp.gm1 + sR * fp.gm1) * rho_div;
+    const double d1 = R[1] - L[1];
+    const double d2 = R[2] - L[2];
+    const double d3 = R[3] - L[3];
+    const double sqvd = d1 * d1 + d2 * d2 + d3 * d3;
+    const double p_over_rho =
+        (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div + 0.5 * rho_a * rho_div * rho_div * sqvd;
+    cc = psi_a + gr_a * p_over_rho;
+    c = sqrt(cc);
+  }
+}
+
+// velocity_minor_axes (equation_information.py:110) and vel_id_eigs
+// (eigendecomposition.py:67-71) for each sweep axis
+template <int AX>
+struct CharIds {
+  static constexpr int m0 = (AX == 0) ? 2 : ((AX == 1) ? 3 : 1);
+  static constexpr int m1 = (AX == 0) ? 3 : ((AX == 1) ? 1 : 2);
+  static constexpr int e0 = (AX == 1) ? 3 : 2;
+  static constexpr int e1 = (AX == 1) ? 2 : 3;
+};
+
+// CHAR-PRIMITIVE face states (high_order_godunov.py:298-316): transform the six
+// window cells to characteristic variables with the face's frozen state
+// (get_characteristics_from_primitives, :402-433), WENO5-Z each variable on
+// both sides, transform back (get_primitives_from_characteristics, :499-523).
+// w(v, k) returns primitive v of window cell k (k = 0..5, face between 2 and 3).
+template <int AX, typename W>
+__device__ __forceinline__ void char_reconstruct(const W& w, const FaceParams& fp, double PL[5],
+                                                 double PR[5]) {
+  constexpr int N = AX + 1;
+  using I = CharIds<AX>;
+  double L[5], R[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    L[v] = w(v, 2);
+    R[v] = w(v, 3);
+  }
+  double rho_a, c, cc;
+  frozen_state(L, R, fp, rho_a, c, cc);
+  const double k_m = -0.5 / c;
+  const double k_p = 0.5 / c;
+  const double k_e = 0.5 / (cc * rho_a);
+  const double k_s = 1.0 / cc;
+  double ch0[6], ch1[6], ch4[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double xn = w(N, k);
+    const double x0 = w(0, k);
+    const double x4 = w(4, k);
+    ch0[k] = k_m * xn + k_e * x4;
+    ch1[k] = x0 - k_s * x4;
+    ch4[k] = k_p * xn + k_e * x4;
+  }
+  const double eps = fp.stencil_eps;
+  double cL[5], cR[5];
+  cL[0] = weno5z(ch0[0], ch0[1], ch0[2], ch0[3], ch0[4], eps);
+  cR[0] = weno5z(ch0[5], ch0[4], ch0[3], ch0[2], ch0[1], eps);
+  cL[1] = weno5z(ch1[0], ch1[1], ch1[2], ch1[3], ch1[4], eps);
+  cR[1] = weno5z(ch1[5], ch1[4], ch1[3], ch1[2], ch1[1], eps);
+  cL[4] = weno5z(ch4[0], ch4[1], ch4[2], ch4[3], ch4[4], eps);
+  cR[4] = weno5z(ch4[5], ch4[4], ch4[3], ch4[2], ch4[1], eps);
+  // shear waves: the characteristic variables are the transverse velocities
+  cL[I::e0] = weno5z(w(I::m0, 0), w(I::m0, 1), w(I::m0, 2), w(I::m0, 3), w(I::m0, 4), eps);
+  cR[I::e0] = weno5z(w(I::m0, 5), w(I::m0, 4), w(I::m0, 3), w(I::m0, 2), w(I::m0, 1), eps);
+  cL[I::e1] = weno5z(w(I::m1, 0), w(I::m1, 1), w(I::m1, 2), w(I::m1, 3), w(I::m1, 4), eps);
+  cR[I::e1] = weno5z(w(I::m1, 5), w(I::m1, 4), w(I::m1, 3), w(I::m1, 2), w(I::m1, 1), eps);
+  PL[0] = rho_a * (cL[0] + cL[4]) + cL[1];
+  PL[N] = c * (-cL[0] + cL[4]);
+  PL[I::m0] = cL[I::e0];
+  PL[I::m1] = cL[I::e1];
+  PL[4] = cc * rho_a * (cL[0] + cL[4]);
+  PR[0] = rho_a * (cR[0] + cR[4]) + cR[1];
+  PR[N] = c * (-cR[0] + cR[4]);
+  PR[I::m0] = cR[I::e0];
+  PR[I::m1] = cR[I::e1];
+  PR[4] = cc * rho_a * (cR[0] + cR[4]);
 }
 
 // ---------------------------------------------------------------------------

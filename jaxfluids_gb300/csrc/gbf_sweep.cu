@@ -36,6 +36,8 @@ int launch_riemann(int riemann, const SweepParams& p, int threads, size_t smem, 
 
 template <int MODE>
 int launch_recon(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+    return launch_riemann<RECON_WENO5Z_CHAR, MODE>(c->riemann, p, threads, smem, s);
   switch (c->recon) {
     case GBF_RECON_WENO5Z:
       return launch_riemann<GBF_RECON_WENO5Z, MODE>(c->riemann, p, threads, smem, s);

@@ -132,12 +132,19 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
+    if (RECON == RECON_WENO5Z_CHAR) {
+      const double* b = sm_prim + base;
+      auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
+      char_reconstruct<AX>(w, p.fp, PL, PR);
+    } else {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      double w[2 * R];
+      for (int v = 0; v < 5; ++v) {
+        double w[2 * R];
 #pragma unroll
-      for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
-      reconstruct_pair<RECON>(w, p.fp.stencil_eps, PL[v], PR[v]);
+        for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
+        reconstruct_pair<(RECON == RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
+                                                                                  PL[v], PR[v]);
+      }
     }
     double F[5];
     riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);

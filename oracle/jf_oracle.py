@@ -259,92 +259,66 @@ def reconstruct_xi(buf: Tensor, case: OracleCase, axis: int, j: int) -> Tensor:
 # Characteristic decomposition (CHAR-PRIMITIVE)
 # ---------------------------------------------------------------------------
 
-def _stencil_window(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
-    """Eigendecomposition.get_stencil_window: [5, N+1, ..., S] over the stencil.
-
-    solvers/riemann_solvers/eigendecomposition.py:75-118 (window of
-    ``stencil_size`` cells starting at offset -stencil_size/2 around face i-1/2).
-    """
-    size = 6 if case.recon == "WENO5-Z" else 4
-    half = size // 2
-    wins = [buf[_stencil_slice(case, axis, k)] for k in range(-half, half)]
-    return torch.stack(wins, dim=-1)
+# equation_information.py:110 and eigendecomposition.py:67-71
+VEL_MINORS = ((2, 3), (3, 1), (1, 2))
+VEL_ID_EIGS = ((2, 3), (3, 2), (2, 3))
 
 
-def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, ...]:
-    """Eigendecomposition.compute_frozen_state (single phase).
+def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, Tensor, Tensor]:
+    """Eigendecomposition.compute_frozen_state, single phase (eigendecomposition.py:120-281).
 
-    eigendecomposition.py:120-294: ARITHMETIC = mean of the two cells adjacent to
-    the face; ROE = Roe average with H = (E + p) / rho and c^2 = (gamma-1)(H - |u|^2/2).
-    Returns (rho, u, v, w, H, c) at the faces.
+    Returns the frozen density, speed of sound and its square at every face
+    (the only parts the primitive characteristic transforms use).
     """
     g = case.gamma
-    L = P[_stencil_slice(case, axis, -1)]
-    Rr = P[_stencil_slice(case, axis, 0)]
+    L = P[_stencil_slice(case, axis, -1)]   # slice_LR[axis][0]: nh-1 : -nh
+    R = P[_stencil_slice(case, axis, 0)]    # slice_LR[axis][1]: nh : -nh+1
     if case.frozen_state == "ARITHMETIC":
-        prim = 0.5 * (L + Rr)
-        rho, u, v, w, p = prim
-        vel_sq = u * u + v * v + w * w
-        c = torch.sqrt(g * p / rho)
-        H = (p / (g - 1.0) + 0.5 * rho * vel_sq + p) / rho
-        return rho, u, v, w, H, c
+        pa = 0.5 * (L + R)
+        c = torch.sqrt(g * pa[4] / pa[0])
+        return pa[0], c, c * c
     if case.frozen_state == "ROE":
-        UL = cons_from_prims(L, g)
-        UR = cons_from_prims(Rr, g)
-        sL = torch.sqrt(L[0])
-        sR = torch.sqrt(Rr[0])
-        one = 1.0 / (sL + sR)
-        u = (sL * L[1] + sR * Rr[1]) * one
-        v = (sL * L[2] + sR * Rr[2]) * one
-        w = (sL * L[3] + sR * Rr[3]) * one
-        HL = (UL[4] + L[4]) / L[0]
-        HR = (UR[4] + Rr[4]) / Rr[0]
-        H = (sL * HL + sR * HR) * one
-        rho = sL * sR
-        vel_sq = u * u + v * v + w * w
-        c = torch.sqrt((g - 1.0) * (H - 0.5 * vel_sq))
-        return rho, u, v, w, H, c
+        rho_a = torch.sqrt(L[0] * R[0])
+        sL, sR = torch.sqrt(L[0]), torch.sqrt(R[0])
+        rho_div = 1.0 / (sL + sR)
+        psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div
+        gr_a = (sL * (g - 1) + sR * (g - 1)) * rho_div
+        d = R[1:4] - L[1:4]
+        d2 = d * d
+        sqvd = d2[0] + d2[1] + d2[2]
+        p_over_rho = (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div \
+            + 0.5 * rho_a * rho_div * rho_div * sqvd
+        cc = psi_a + gr_a * p_over_rho
+        return rho_a, torch.sqrt(cc), cc
     raise NotImplementedError(case.frozen_state)
 
 
-def _char_matrices(fs: Tuple[Tensor, ...], axis: int) -> Tuple[List[List[Tensor]], List[List[Tensor]]]:
-    """Primitive-variable eigenvectors of the Euler Jacobian along ``axis``.
-
-    eigendecomposition.py:402-433 / 499-523: left eigenvectors L (prim -> char)
-    and right eigenvectors R (char -> prim) for (rho, u_n, u_t1, u_t2, p).
-    Rows/columns use the reference's variable order (rho, u, v, w, p).
-    """
-    rho, u, v, w, H, c = fs
-    zero = torch.zeros_like(rho)
-    one = torch.ones_like(rho)
+def chars_from_prims(x: List[Tensor], rho_a, c, cc, axis: int) -> List[Tensor]:
+    """get_characteristics_from_primitives, single phase (eigendecomposition.py:402-433)."""
     n = axis + 1
-    # left eigenvectors (rows) in the frame (rho, u_n, p) + tangential velocities
-    Lm = [[zero] * 5 for _ in range(5)]
-    Rm = [[zero] * 5 for _ in range(5)]
-    # wave 0: u - c
-    Lm[0][n] = -0.5 * rho / c
-    Lm[0][4] = 0.5 / (c * c)
-    # wave 1: entropy
-    Lm[1][0] = one
-    Lm[1][4] = -1.0 / (c * c)
-    # waves 2, 3: shear
-    tang = [t for t in (1, 2, 3) if t != n]
-    Lm[2][tang[0]] = one
-    Lm[3][tang[1]] = one
-    # wave 4: u + c
-    Lm[4][n] = 0.5 * rho / c
-    Lm[4][4] = 0.5 / (c * c)
-    # right eigenvectors (columns)
-    Rm[0][0] = one
-    Rm[n][0] = -c / rho
-    Rm[4][0] = c * c
-    Rm[0][1] = one
-    Rm[tang[0]][2] = one
-    Rm[tang[1]][3] = one
-    Rm[0][4] = one
-    Rm[n][4] = c / rho
-    Rm[4][4] = c * c
-    return Lm, Rm
+    m0, m1 = VEL_MINORS[axis]
+    e0, e1 = VEL_ID_EIGS[axis]
+    out = [None] * 5
+    out[0] = -0.5 / c * x[n] + 0.5 / (cc * rho_a) * x[4]
+    out[1] = x[0] - 1.0 / cc * x[4]
+    out[e0] = x[m0]
+    out[e1] = x[m1]
+    out[4] = 0.5 / c * x[n] + 0.5 / (cc * rho_a) * x[4]
+    return out
+
+
+def prims_from_chars(x: List[Tensor], rho_a, c, cc, axis: int) -> List[Tensor]:
+    """get_primitives_from_characteristics, single phase (eigendecomposition.py:499-523)."""
+    n = axis + 1
+    m0, m1 = VEL_MINORS[axis]
+    e0, e1 = VEL_ID_EIGS[axis]
+    out = [None] * 5
+    out[0] = rho_a * (x[0] + x[4]) + x[1]
+    out[n] = c * (-x[0] + x[4])
+    out[m0] = x[e0]
+    out[m1] = x[e1]
+    out[4] = cc * rho_a * (x[0] + x[4])
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -437,39 +411,18 @@ def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
         PL = reconstruct_xi(P, case, axis, 0)
         PR = reconstruct_xi(P, case, axis, 1)
     elif case.recon_var == "CHAR-PRIMITIVE":
-        win = _stencil_window(P, case, axis)                   # [5, F.., S]
-        fs = frozen_state(P, case, axis)
-        Lm, Rm = _char_matrices(fs, axis)
-        # eigendecomposition.py:402-433 (einsum over the primitive index)
-        char = []
-        for r in range(5):
-            acc = None
-            for c_ in range(5):
-                term = Lm[r][c_].unsqueeze(-1) * win[c_]
-                acc = term if acc is None else acc + term
-            char.append(acc)
-        size = win.shape[-1]
-        half = size // 2
-        offs = _recon_offsets(case.recon, 0)
-        # stencil slices on the window: reconstruction_stencil.set_slices_stencil
-        # spatial_reconstruction.py:21-44 (range(0, S-1) for j=0, range(S-1, 0, -1) for j=1)
-        idx0 = [k + half for k in offs]
-        idx1 = [k + half for k in _recon_offsets(case.recon, 1)]
-        cL = [recon_stencil(case.recon, 0, [ch[..., i] for i in idx0]) for ch in char]
-        cR = [recon_stencil(case.recon, 1, [ch[..., i] for i in idx1]) for ch in char]
-        PL_l, PR_l = [], []
-        for r in range(5):
-            accL = None
-            accR = None
-            for c_ in range(5):
-                tL = Rm[r][c_] * cL[c_]
-                tR = Rm[r][c_] * cR[c_]
-                accL = tL if accL is None else accL + tL
-                accR = tR if accR is None else accR + tR
-            PL_l.append(accL)
-            PR_l.append(accR)
-        PL = torch.stack(PL_l, 0)
-        PR = torch.stack(PR_l, 0)
+        # high_order_godunov.py:298-316: window of the 6 cells around each face
+        # (eigendecomposition.py:75-118), WENO on each characteristic variable
+        # with the window slices (spatial_reconstruction.py:21-44), back-transform
+        if case.recon != "WENO5-Z":
+            raise NotImplementedError("CHAR-PRIMITIVE is restated for WENO5-Z")
+        rho_a, c, cc = frozen_state(P, case, axis)
+        win = [P[_stencil_slice(case, axis, k)] for k in range(-3, 3)]   # window cells 0..5
+        chars = [chars_from_prims([w[v] for v in range(5)], rho_a, c, cc, axis) for w in win]
+        cL = [weno5z_stencil(*[chars[k][v] for k in (0, 1, 2, 3, 4)]) for v in range(5)]
+        cR = [weno5z_stencil(*[chars[k][v] for k in (5, 4, 3, 2, 1)]) for v in range(5)]
+        PL = torch.stack(prims_from_chars(cL, rho_a, c, cc, axis), 0)
+        PR = torch.stack(prims_from_chars(cR, rho_a, c, cc, axis), 0)
     else:
         raise NotImplementedError(case.recon_var)
     UL = cons_from_prims(PL, g)

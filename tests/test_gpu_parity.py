@@ -52,6 +52,15 @@ RHS_CASES = [
     ("quad-2d-sym", dict(cells=(36, 44, 1), bc={"east": "PERIODIC", "west": "PERIODIC", "north": "SYMMETRY",
                                                "south": "SYMMETRY", "top": "PERIODIC", "bottom": "PERIODIC"}), "quad"),
     ("tgv-3d", dict(cells=(24, 24, 24), bc="PERIODIC", ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("sod-char-arith", dict(cells=(200, 1, 1), bc=ZG, recon_var="CHAR-PRIMITIVE"), "sod"),
+    ("sod-char-roe", dict(cells=(200, 1, 1), bc=ZG, recon_var="CHAR-PRIMITIVE", frozen_state="ROE"), "sod"),
+    ("quad-2d-char-roe", dict(cells=(48, 40, 1), bc=ZG, recon_var="CHAR-PRIMITIVE", frozen_state="ROE"), "quad"),
+    ("quad-2d-char-rusanov", dict(cells=(40, 36, 1), bc=ZG, recon_var="CHAR-PRIMITIVE", riemann="RUSANOV"), "quad"),
+    ("tgv-3d-char-roe", dict(cells=(24, 24, 24), bc="PERIODIC", recon_var="CHAR-PRIMITIVE", frozen_state="ROE",
+                             ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-mixed-char", dict(cells=(20, 12, 18), bc={"east": ZG, "west": ZG, "north": "SYMMETRY",
+                                                       "south": "SYMMETRY", "top": "PERIODIC", "bottom": "PERIODIC"},
+                               recon_var="CHAR-PRIMITIVE", ranges=((0, 2 * math.pi),) * 3), "tgv"),
     ("tgv-3d-mixed", dict(cells=(20, 12, 18), bc={"east": ZG, "west": ZG, "north": "SYMMETRY", "south": "SYMMETRY",
                                                   "top": "PERIODIC", "bottom": "PERIODIC"},
                           ranges=((0, 2 * math.pi),) * 3), "tgv"),
@@ -129,7 +138,9 @@ def test_dt_matches_oracle():
 def test_steps_match_oracle(fused):
     from jaxfluids_gb300 import FusedRK3, SimulationManager
     cases = [((200, 1, 1), ZG, "sod", {}), ((48, 40, 1), ZG, "quad", {}),
-             ((16, 16, 16), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3})]
+             ((16, 16, 16), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3}),
+             ((16, 12, 20), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3,
+                                                "recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"})]
     for cells, bc, kind, kw in cases:
         oc, cc = both(cells, bc, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
