@@ -67,6 +67,7 @@ class CaseConfig:
     mu: float = 0.0
     bulk_viscosity: float = 0.0
     kappa: float = 0.0
+    prandtl: Optional[float] = None
     viscous_heat_production: bool = True
     eps: float = EPS
     stencil_eps: float = STENCIL_EPS
@@ -100,6 +101,16 @@ class CaseConfig:
                 raise SetupError("each active axis needs at least halo_cells cells")
         if self.fixed_dt is None and not self.cfl > 0:
             raise SetupError("CFL must be positive")
+        if self.heat and self.prandtl is not None and not self.kappa:
+            # PRANDTL model (materials/single_materials/material.py:115-116)
+            self.kappa = self.gamma / (self.gamma - 1.0) * self.R * self.mu / self.prandtl
+        if self.viscous or self.heat:
+            if self.recon != "WENO5-Z":
+                raise NotImplementedError("dissipative fluxes are built with WENO5-Z convective fluxes")
+            if self.nh < 4:
+                raise SetupError("CENTRAL4 dissipative fluxes need halo_cells >= 4")
+            if any(self.bc[f] != "PERIODIC" for f in FACES if FACE_AXIS[f] in self.active):
+                raise NotImplementedError("dissipative fluxes are built for PERIODIC boundaries")
 
     # domain/domain_information.py:80-206 and mesh_creation/homogenous.py:13
     @property
@@ -211,6 +222,9 @@ class CaseConfig:
                 # materials/single_materials/material.py:70-74, :115-116: kappa = cp mu / Pr
                 cp = gamma / (gamma - 1.0) * R
                 kappa = cp * mu / float(tc["prandtl_number"])
+                if not viscous:
+                    dv = transport.get("dynamic_viscosity", {})
+                    kappa = cp * float(dv.get("value", 0.0)) / float(tc["prandtl_number"])
             elif tc.get("model", "CUSTOM") == "CUSTOM":
                 kappa = float(tc.get("value", 0.0))
             else:
@@ -228,6 +242,7 @@ class CaseConfig:
             signal_speed=god.get("signal_speed", "EINFELDT"),
             cfl=float(ti.get("CFL", 0.5)), fixed_dt=float(fixed) if fixed else None,
             viscous=viscous, heat=heat, mu=mu, kappa=kappa,
+            bulk_viscosity=float(transport.get("bulk_viscosity", 0.0) or 0.0),
             viscous_heat_production=bool(phys.get("is_viscous_heat_production", True)),
             eps=float(prec.get("epsilon", EPS)) if isinstance(prec.get("epsilon"), float) else EPS,
             stencil_eps=float(prec.get("spatial_stencil_epsilon", STENCIL_EPS))

@@ -53,7 +53,16 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if (c->riemann != GBF_RIEMANN_HLLC && c->riemann != GBF_RIEMANN_RUSANOV) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
-  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) return GBF_ERR_UNSUPPORTED;
+  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) {
+    // CENTRAL4 dissipative fluxes: WENO5-Z convective part, periodic
+    // boundaries (edge halos of periodic faces are plain wraps), and four
+    // halo cells for the centre-derivative ring (spatial_stencil.py:86-96)
+    if (c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
+    if (c->nh < 4) return GBF_ERR_INVALID_ARGUMENT;
+    for (int f = 0; f < 6; ++f)
+      if ((c->n[f >> 1] > 1) && c->bc[f] != GBF_BC_PERIODIC) return GBF_ERR_UNSUPPORTED;
+    if (!(c->mu >= 0.0) || !(c->kappa >= 0.0) || !(c->R > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
+  }
   if (!(c->gamma > 1.0)) return GBF_ERR_INVALID_ARGUMENT;
   const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
   if (c->nh < R) return GBF_ERR_INVALID_ARGUMENT;
@@ -121,6 +130,8 @@ int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) 
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
   if (!prims) return GBF_ERR_INVALID_ARGUMENT;
+  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))  // face, edge and vertex halos (all periodic)
+    return launch_halo_wrap(c, ci, prims, cons, (cudaStream_t)stream);
   return launch_halo_fill(c, ci, prims, cons, (cudaStream_t)stream);
 }
 
@@ -161,10 +172,14 @@ int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspa
   return launch_dt_finalize(c, ci, red, dt_out, nullptr, 0, s);
 }
 
+static bool dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0; }
+
 size_t gbf_rk3_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
   if (make_case_info(c, &ci) != GBF_OK) return 0;
-  return (size_t)2 * 5 * (size_t)ci.cells * sizeof(double);
+  // two stage buffers, plus the stage primitives for the dissipative fluxes
+  const size_t states = dissipative(c) ? 3 : 2;
+  return states * 5 * (size_t)ci.cells * sizeof(double);
 }
 
 // dt_state = {dt, t, max signal speed bits, min density bits}
@@ -198,6 +213,26 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
   double* B = A + 5 * ci.cells;
   unsigned long long* red = (unsigned long long*)(dt_state + 2);
   p.dt_state = dt_state;
+  if (dissipative(c)) {
+    // per stage: primitives of the stage state once, then the fused sweep
+    double* Pk = B + 5 * ci.cells;
+    p.prims = Pk;
+    const double* stage_in[3] = {cons, A, B};
+    double* stage_out[3] = {A, B, cons};
+    for (int step = 0; step < steps; ++step) {
+      for (int stage = 0; stage < 3; ++stage) {
+        if ((st = launch_convert(c, stage_in[stage], Pk, ci.cells, 1, s)) != GBF_OK) return st;
+        p.stage = stage;
+        p.cons = stage_in[stage];
+        p.cons0 = cons;
+        p.out = stage_out[stage];
+        p.reduce_dt = (stage == 2);
+        if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE_P)) != GBF_OK) return st;
+      }
+      if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
+    }
+    return GBF_OK;
+  }
   for (int step = 0; step < steps; ++step) {
     // U1 = U^n + dt L(U^n)
     p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = A; p.reduce_dt = 0;

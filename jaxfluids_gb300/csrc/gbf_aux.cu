@@ -87,6 +87,43 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
   }
 }
 
+// All-periodic halos of every kind (faces, edges, vertices): each halo cell
+// copies the interior cell its coordinates wrap to; the halo conservatives are
+// recomputed from the copied primitives (outer/material.py:248-250, :289-379).
+__global__ void halo_wrap_kernel(const HaloParams hp, double* prims, double* cons) {
+  const long long cs = (long long)hp.hs[0] * hp.hs[1] * hp.hs[2];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
+       i += (long long)gridDim.x * blockDim.x) {
+    int b[3] = {(int)(i / ((long long)hp.hs[1] * hp.hs[2])), (int)((i / hp.hs[2]) % hp.hs[1]),
+                (int)(i % hp.hs[2])};
+    int src[3];
+    bool halo = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      src[a] = b[a];
+      if (hp.n[a] > 1) {
+        int g = b[a] - hp.nh;
+        if (g < 0) { g += hp.n[a]; halo = true; }
+        else if (g >= hp.n[a]) { g -= hp.n[a]; halo = true; }
+        src[a] = g + hp.nh;
+      }
+    }
+    if (!halo) continue;
+    const long long so = ((long long)src[0] * hp.hs[1] + src[1]) * hp.hs[2] + src[2];
+    double P[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) P[v] = prims[v * cs + so];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) prims[v * cs + i] = P[v];
+    if (cons) {
+      double U[5];
+      cons_from_prims(P, U, hp.gm1);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) cons[v * cs + i] = U[v];
+    }
+  }
+}
+
 __global__ void convert_kernel(const double* in, double* out, long long count, double gm1,
                                int to_prims) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
@@ -302,6 +339,19 @@ int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, doubl
   hp.total = start;
   if (hp.total == 0) return GBF_OK;
   halo_fill_kernel<<<grid_for(hp.total), kThreads, 0, s>>>(hp, prims, cons);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+int launch_halo_wrap(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
+                     cudaStream_t s) {
+  HaloParams hp{};
+  for (int a = 0; a < 3; ++a) {
+    hp.n[a] = ci.n[a];
+    hp.hs[a] = ci.hs[a];
+  }
+  hp.nh = ci.nh;
+  hp.gm1 = ci.fp.gm1;
+  halo_wrap_kernel<<<grid_for(ci.halo_cells), kThreads, 0, s>>>(hp, prims, cons);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 

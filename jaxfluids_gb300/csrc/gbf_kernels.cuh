@@ -32,6 +32,8 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
 // auxiliary kernels (gbf_aux.cu)
 int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
                      cudaStream_t s);
+int launch_halo_wrap(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
+                     cudaStream_t s);
 int launch_convert(const gbf_case* c, const double* in, double* out, long long count, int to_prims,
                    cudaStream_t s);
 int launch_stage_integrate(const gbf_case* c, const CaseInfo& ci, double* cons,

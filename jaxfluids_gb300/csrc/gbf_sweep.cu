@@ -18,9 +18,9 @@ int radius_of(int recon) {
   return recon == GBF_RECON_WENO5Z ? 3 : 2;
 }
 
-template <int RECON, int RIEMANN, int MODE>
+template <int RECON, int RIEMANN, int MODE, bool VISC>
 int launch_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  auto kern = sweep_kernel<RECON, RIEMANN, MODE, kMaxCellsPerThread>;
+  auto kern = sweep_kernel<RECON, RIEMANN, MODE, kMaxCellsPerThread, VISC>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return GBF_ERR_CUDA;
   const int grid = p.tiles[0] * p.tiles[1] * p.tiles[2];
@@ -28,24 +28,33 @@ int launch_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
-template <int RECON, int MODE>
+template <int RECON, int MODE, bool VISC>
 int launch_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (riemann == GBF_RIEMANN_HLLC) return launch_one<RECON, GBF_RIEMANN_HLLC, MODE>(p, threads, smem, s);
-  return launch_one<RECON, GBF_RIEMANN_RUSANOV, MODE>(p, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLLC) return launch_one<RECON, GBF_RIEMANN_HLLC, MODE, VISC>(p, threads, smem, s);
+  return launch_one<RECON, GBF_RIEMANN_RUSANOV, MODE, VISC>(p, threads, smem, s);
 }
 
+// inviscid kernels: every reconstruction
 template <int MODE>
 int launch_recon(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
-    return launch_riemann<RECON_WENO5Z_CHAR, MODE>(c->riemann, p, threads, smem, s);
+    return launch_riemann<RECON_WENO5Z_CHAR, MODE, false>(c->riemann, p, threads, smem, s);
   switch (c->recon) {
     case GBF_RECON_WENO5Z:
-      return launch_riemann<GBF_RECON_WENO5Z, MODE>(c->riemann, p, threads, smem, s);
+      return launch_riemann<GBF_RECON_WENO5Z, MODE, false>(c->riemann, p, threads, smem, s);
     case GBF_RECON_MINMOD:
-      return launch_riemann<GBF_RECON_MINMOD, MODE>(c->riemann, p, threads, smem, s);
+      return launch_riemann<GBF_RECON_MINMOD, MODE, false>(c->riemann, p, threads, smem, s);
     default:
-      return launch_riemann<GBF_RECON_MINMOD_AD, MODE>(c->riemann, p, threads, smem, s);
+      return launch_riemann<GBF_RECON_MINMOD_AD, MODE, false>(c->riemann, p, threads, smem, s);
   }
+}
+
+// viscous / heat-conducting kernels: WENO5-Z on primitive or characteristic variables
+template <int MODE>
+int launch_recon_visc(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+    return launch_riemann<RECON_WENO5Z_CHAR, MODE, true>(c->riemann, p, threads, smem, s);
+  return launch_riemann<GBF_RECON_WENO5Z, MODE, true>(c->riemann, p, threads, smem, s);
 }
 
 }  // namespace
@@ -109,6 +118,13 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   for (int f = 0; f < 6; ++f) q.bc[f] = c->bc[f];
   q.fp = ci.fp;
   q.active_mask = ci.active_mask;
+  q.viscous = (c->flags & GBF_FLAG_VISCOUS) ? 1 : 0;
+  q.heat = (c->flags & GBF_FLAG_HEAT) ? 1 : 0;
+  q.heat_production = (c->flags & GBF_FLAG_VISCOUS_HEAT_PRODUCTION) ? 1 : 0;
+  q.mu1 = c->mu;
+  q.mu2 = c->bulk_mu - 2.0 / 3.0 * c->mu;  // compute_tau: bulk - 2/3 mu
+  q.kappa = c->kappa;
+  q.R = c->R;
   *p = q;
   *threads = thr;
   *smem = bytes;
@@ -117,7 +133,12 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
 
 int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
                  int mode) {
-  if (mode == MODE_RHS) return launch_recon<MODE_RHS>(c, p, threads, smem, s);
+  const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
+  if (mode == MODE_RHS)
+    return visc ? launch_recon_visc<MODE_RHS>(c, p, threads, smem, s)
+                : launch_recon<MODE_RHS>(c, p, threads, smem, s);
+  if (mode == MODE_STAGE_P) return launch_recon_visc<MODE_STAGE_P>(c, p, threads, smem, s);
+  if (visc) return GBF_ERR_UNSUPPORTED;  // dissipative fluxes need the primitive buffer
   return launch_recon<MODE_STAGE>(c, p, threads, smem, s);
 }
 

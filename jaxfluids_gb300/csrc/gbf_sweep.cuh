@@ -22,7 +22,13 @@
 
 namespace gbf {
 
-enum { MODE_RHS = 0, MODE_STAGE = 1 };
+// MODE_RHS: halo primitive buffer in, rhs out (drop-in).
+// MODE_STAGE: interior conservatives in, RK stage out (primitives of each
+//   pencil derived on the fly).
+// MODE_STAGE_P: as MODE_STAGE, but the primitives of the stage state come from
+//   an interior primitive buffer computed once per stage (used by the viscous
+//   and heat-conduction path, whose face stencils reach across the tile).
+enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_STAGE_P = 2 };
 
 struct SweepParams {
   int n[3];          // interior cells per axis (1 = inactive)
@@ -41,7 +47,36 @@ struct SweepParams {
   int stage;                 // RK stage 0, 1, 2
   int reduce_dt;             // reduce the next time step of the new state
   int active_mask;           // bit a set when axis a is active
+  // dissipative fluxes (CENTRAL4, constant transport properties)
+  const double* prims;       // MODE_STAGE_P: interior primitives of the stage state
+  int viscous;               // viscous flux on
+  int heat;                  // heat flux on
+  int heat_production;       // viscous energy flux sum_k tau_k u_k (is_viscous_heat_production)
+  double mu1;                // dynamic viscosity
+  double mu2;                // bulk viscosity - 2/3 mu
+  double kappa;              // thermal conductivity
+  double R;                  // specific gas constant
 };
+
+// Primitive v of the logical cell (g0, g1, g2), which may lie up to nh cells
+// outside the interior: read from the halo buffer (MODE_RHS) or, with
+// periodic wrapping on every axis, from the interior primitive buffer.
+template <int MODE>
+__device__ __forceinline__ double global_prim(const SweepParams& p, int v, int g0, int g1, int g2) {
+  if (MODE == MODE_RHS) {
+    const int b0 = (p.n[0] > 1) ? g0 + p.nh : 0;
+    const int b1 = (p.n[1] > 1) ? g1 + p.nh : 0;
+    const int b2 = (p.n[2] > 1) ? g2 + p.nh : 0;
+    const long long cs = (long long)p.hs[0] * p.hs[1] * p.hs[2];
+    return __ldg(p.prims_halo + v * cs + ((long long)b0 * p.hs[1] + b1) * p.hs[2] + b2);
+  } else {
+    g0 = (g0 < 0) ? g0 + p.n[0] : ((g0 >= p.n[0]) ? g0 - p.n[0] : g0);
+    g1 = (g1 < 0) ? g1 + p.n[1] : ((g1 >= p.n[1]) ? g1 - p.n[1] : g1);
+    g2 = (g2 < 0) ? g2 + p.n[2] : ((g2 >= p.n[2]) ? g2 - p.n[2] : g2);
+    const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+    return __ldg(p.prims + v * cs + ((long long)g0 * p.n[1] + g1) * p.n[2] + g2);
+  }
+}
 
 __device__ __forceinline__ int idx3(int i0, int i1, int i2, int e1, int e2) {
   return (i0 * e1 + i1) * e2 + i2;
@@ -72,7 +107,98 @@ __device__ __forceinline__ unsigned long long ordered_bits(double x) {
   return (unsigned long long)__double_as_longlong(x);
 }
 
-template <int AX, int RECON, int RIEMANN, int MODE, int MAXC>
+// CENTRAL4 stencils: deriv_center_4.py:37-49, deriv_face_4.py:37-50, central_4.py:39-50
+__device__ __forceinline__ double c4_center_deriv(double one_dx, double m2, double m1, double p1, double p2) {
+  return one_dx * ((1.0 / 12.0) * (m2 - p2) + (8.0 / 12.0) * (p1 - m1));
+}
+__device__ __forceinline__ double c4_face_deriv(double one_dx, double m2, double m1, double c0, double p1) {
+  return one_dx * ((1.0 / 24.0) * (m2 - p1) + (27.0 / 24.0) * (c0 - m1));
+}
+__device__ __forceinline__ double c4_face_interp(double m2, double m1, double c0, double p1) {
+  return (-1.0 / 16.0) * (m2 + p1) + (9.0 / 16.0) * (m1 + c0);
+}
+
+// Viscous and heat fluxes at the face of axis AX with logical face coordinates
+// q (the face lies between cells q[AX]-1 and q[AX]); source_term_solver.py
+// compute_viscous_flux_xi (:264-350), compute_velocity_gradient (:414-448),
+// compute_xi_derivatives_at_xj (:538-580), compute_tau (:504-536),
+// compute_heat_flux_xi (:188-254).  Adds them to the convective flux F the
+// way compute_rhs_xi does: F[1:5] += -visc, then F[4] += heat
+// (space_solver.py:565-585).
+template <int AX, int MODE>
+__device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const int q[3], double F[5]) {
+  auto cell = [&](int v, int kax, int ax2, int k2) {
+    int g[3] = {q[0], q[1], q[2]};
+    g[AX] += kax;
+    g[ax2] += k2;
+    return global_prim<MODE>(p, v, g[0], g[1], g[2]);
+  };
+  const double odx = p.one_dx[AX];
+  if (p.viscous) {
+    // g_[a][b] = d u_a / d x_b at the face (zero for inactive axes)
+    double gr[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      gr[a][AX] = c4_face_deriv(odx, cell(1 + a, -2, AX, 0), cell(1 + a, -1, AX, 0),
+                                cell(1 + a, 0, AX, 0), cell(1 + a, 1, AX, 0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (i == AX || !(p.active_mask & (1 << i))) continue;
+      const double odi = p.one_dx[i];
+      // tangential derivatives needed by tau: d u_AX / d x_i and d u_i / d x_i
+#pragma unroll
+      for (int which = 0; which < 2; ++which) {
+        const int a = (which == 0) ? AX : i;
+        double d[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          d[k] = c4_center_deriv(odi, cell(1 + a, k - 2, i, -2), cell(1 + a, k - 2, i, -1),
+                                 cell(1 + a, k - 2, i, 1), cell(1 + a, k - 2, i, 2));
+        gr[a][i] = c4_face_interp(d[0], d[1], d[2], d[3]);
+      }
+    }
+    double tau[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      tau[k] = (p.active_mask & (1 << k)) ? p.mu1 * (gr[AX][k] + gr[k][AX]) : 0.0;
+    double tr = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (!(p.active_mask & (1 << k))) continue;
+      tr = first ? gr[k][k] : tr + gr[k][k];
+      first = false;
+    }
+    tau[AX] = tau[AX] + p.mu2 * tr;
+    double vt = 0.0;
+    if (p.heat_production) {
+      first = true;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (!(p.active_mask & (1 << k))) continue;
+        const double vf = c4_face_interp(cell(1 + k, -2, AX, 0), cell(1 + k, -1, AX, 0),
+                                         cell(1 + k, 0, AX, 0), cell(1 + k, 1, AX, 0));
+        vt = first ? tau[k] * vf : vt + tau[k] * vf;
+        first = false;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[1 + k] = F[1 + k] + (-tau[k]);
+    F[4] = F[4] + (-vt);
+  }
+  if (p.heat) {
+    double T[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) T[k] = cell(4, k - 2, AX, 0) / (cell(0, k - 2, AX, 0) * p.R);
+    F[4] = F[4] + (-p.kappa) * c4_face_deriv(odx, T[0], T[1], T[2], T[3]);
+  }
+}
+
+template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
 __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
                                            double* sm_prim, double* sm_flux,
                                            double (&acc)[MAXC][5], bool first) {
@@ -107,10 +233,15 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
       g[AX] = remap_bc(g[AX], p.n[AX], p.bc[2 * AX], p.bc[2 * AX + 1], flip);
       const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
       const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
-      double U[5];
+      if (MODE == MODE_STAGE_P) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
-      prims_from_cons(U, P, p.fp.gm1);
+        for (int v = 0; v < 5; ++v) P[v] = __ldg(p.prims + v * cs + off);
+      } else {
+        double U[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
+        prims_from_cons(U, P, p.fp.gm1);
+      }
       if (flip) P[AX + 1] = -P[AX + 1];
     }
 #pragma unroll
@@ -148,6 +279,10 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     }
     double F[5];
     riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
+    if (VISC) {
+      int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
+      add_dissipative_flux<AX, MODE>(p, q, F);
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
   }
@@ -191,7 +326,7 @@ __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, do
   return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 2.0 / 3.0), rhs));
 }
 
-template <int RECON, int RIEMANN, int MODE, int MAXC>
+template <int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
 __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
   extern __shared__ double smem[];
   const int b = blockIdx.x;
@@ -224,15 +359,15 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
 
   bool first = true;
   if (p.active_mask & 1) {
-    sweep_axis<0, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+    sweep_axis<0, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
     first = false;
   }
   if (p.active_mask & 2) {
-    sweep_axis<1, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+    sweep_axis<1, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
     first = false;
   }
   if (p.active_mask & 4) {
-    sweep_axis<2, RECON, RIEMANN, MODE, MAXC>(p, o, ext, sm_prim, sm_flux, acc, first);
+    sweep_axis<2, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
   }
 
   // ---- epilogue ---------------------------------------------------------
@@ -241,7 +376,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
   double smax = 0.0;
   double rmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
   double dt = 0.0;
-  if (MODE == MODE_STAGE) dt = p.dt_state[0];
+  if (MODE != MODE_RHS) dt = p.dt_state[0];
 #pragma unroll
   for (int k = 0; k < MAXC; ++k) {
     const int c = threadIdx.x + k * blockDim.x;
@@ -254,7 +389,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
       if (MODE == MODE_RHS) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) p.out[v * cs + off] = acc[k][v];
-      } else {
+      } else {  // MODE_STAGE, MODE_STAGE_P
         double Un[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
@@ -279,7 +414,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
       }
     }
   }
-  if (MODE == MODE_STAGE && p.reduce_dt) {
+  if (MODE != MODE_RHS && p.reduce_dt) {
     // warp shuffle -> shared -> one atomic per CTA; max/min are exact, so the
     // result does not depend on the reduction order.
 #pragma unroll

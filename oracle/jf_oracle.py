@@ -113,6 +113,10 @@ class OracleCase:
         # materials/single_materials/ideal_gas.py:32
         return self.gamma / (self.gamma - 1.0) * self.R
 
+    def kappa(self) -> float:
+        # PRANDTL model (materials/single_materials/material.py:115-116): cp mu / Pr
+        return self.cp() * self.mu / self.prandtl
+
 
 def _axis_slice(case: OracleCase, axis: int, s: slice) -> Tuple[slice, ...]:
     sl = [slice(None)] + [case.inner(i) for i in range(3)]
@@ -434,22 +438,103 @@ def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
 # Viscous flux (CENTRAL4), source_term_solver.py
 # ---------------------------------------------------------------------------
 
-def _c4_face_interp(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
-    # stencils/reconstruction/central/central_4.py:39-50: (-1, 9, 9, -1)/16
-    s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
-    return (-1.0 / 16.0 * s[0] + 9.0 / 16.0 * s[1] + 9.0 / 16.0 * s[2] - 1.0 / 16.0 * s[3])
+# jnp.array([...]) / c coefficient arrays of the CENTRAL4 stencils
+_C12 = (1.0 / 12.0, 8.0 / 12.0)      # derivative/deriv_center_4.py:35
+_C24 = (1.0 / 24.0, 27.0 / 24.0)     # derivative/deriv_face_4.py:35
+_C16 = (-1.0 / 16.0, 9.0 / 16.0)     # reconstruction/central/central_4.py:37
 
 
-def _c4_face_deriv(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
-    # stencils/derivative/deriv_face_4.py:37-50: (1, -27, 27, -1)/(24 dx)
+def _ring_slices(case: OracleCase, n: int, axis: int, lo: int, hi: Optional[int]) -> Tuple[slice, ...]:
+    sl = [slice(None)] + [slice(n, -n) if case.cells[a] > 1 else slice(None) for a in range(3)]
+    sl[axis + 1] = slice(lo, hi)
+    return tuple(sl)
+
+
+def _deriv_center_ring(buf: Tensor, case: OracleCase, axis_i: int, offset: int = 2) -> Tensor:
+    """DerivativeFourthOrderCenter.derivative_xi with offset (deriv_center_4.py:37-49).
+
+    Built with offset = 2 (source_term_solver.py:63-71): the result covers the
+    interior plus a ring of two cells on every active axis.
+    """
+    n = case.nh - offset
+
+    def sl(k):
+        hi = -n + k   # nhi = -n + k + 1 - at_cell_center
+        return _ring_slices(case, n, axis_i, n + k, hi if hi != 0 else None)
+    return 1.0 / case.cell_size(axis_i) * (_C12[0] * (buf[sl(-2)] - buf[sl(2)]) + _C12[1] * (buf[sl(1)] - buf[sl(-1)]))
+
+
+def _recon4_from_ring(ring: Tensor, case: OracleCase, axis_j: int) -> Tensor:
+    """CentralFourthOrderReconstruction built with nh = 2 on the ring array (central_4.py:39-50)."""
+    n = 2
+
+    def sl(k):
+        hi = -n + k + 1
+        return _ring_slices(case, n, axis_j, n + k, hi if hi != 0 else None)
+    return _C16[0] * (ring[sl(-2)] + ring[sl(1)]) + _C16[1] * (ring[sl(-1)] + ring[sl(0)])
+
+
+def _recon4(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
+    # reconstruct_stencil_ui (central_4.py:39-50) on the halo buffer
     s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
-    dx = case.cell_size(axis)
-    return (1.0 / 24.0 * s[0] - 27.0 / 24.0 * s[1] + 27.0 / 24.0 * s[2] - 1.0 / 24.0 * s[3]) / dx
+    return _C16[0] * (s[0] + s[3]) + _C16[1] * (s[1] + s[2])
+
+
+def _deriv_face(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
+    # DerivativeFourthOrderFace.derivative_xi (deriv_face_4.py:37-50)
+    s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
+    return 1.0 / case.cell_size(axis) * (_C24[0] * (s[0] - s[3]) + _C24[1] * (s[2] - s[1]))
 
 
 def viscous_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
-    """compute_viscous_flux_xi for constant mu (source_term_solver.py:264-350)."""
-    raise NotImplementedError("viscous flux oracle")
+    """compute_viscous_flux_xi for a constant viscosity (source_term_solver.py:264-350).
+
+    vel_grad[a][b] = d u_a / d x_b at the faces of ``axis``: the normal
+    derivative by the face stencil, tangential ones as centre derivatives
+    interpolated to the face (compute_xi_derivatives_at_xj :538-580);
+    tau (compute_tau :504-536); energy flux sum_k tau_k u_k at the face.
+    Returns [tau_x, tau_y, tau_z, sum tau_k u_k] at the faces.
+    """
+    vel = P[1:4]
+    shape = _deriv_face(vel, case, axis).shape[1:]
+    zeros = torch.zeros(shape, dtype=P.dtype)
+    g = [[zeros] * 3 for _ in range(3)]
+    for i in range(3):
+        if i not in case.active:
+            continue
+        if i == axis:
+            d = _deriv_face(vel, case, i)
+        else:
+            d = _recon4_from_ring(_deriv_center_ring(vel, case, i), case, axis)
+        for a in range(3):
+            g[a][i] = d[a]
+    mu1 = case.mu
+    mu2 = case.bulk_viscosity - 2.0 / 3.0 * case.mu
+    tau = []
+    for k in range(3):
+        if axis in case.active and k in case.active:
+            tau.append(mu1 * (g[axis][k] + g[k][axis]))
+        else:
+            tau.append(zeros)
+    tr = sum([g[k][k] for k in case.active])
+    tau[axis] = tau[axis] + mu2 * tr
+    velf = _recon4(vel, case, axis)
+    if case.viscous_heat_production:
+        vt = 0.0
+        for k in case.active:
+            vt = vt + tau[k] * velf[k]
+    else:
+        vt = zeros
+    return torch.stack(tau + [vt], 0)
+
+
+def heat_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
+    """compute_heat_flux_xi (source_term_solver.py:188-254): -kappa dT/dx at the faces.
+
+    T = p / (rho R) (ideal_gas.py:81-83) on the halo buffer.
+    """
+    T = (P[4] / (P[0] * case.R)).unsqueeze(0)
+    return -case.kappa() * _deriv_face(T, case, axis)[0]
 
 
 # ---------------------------------------------------------------------------
@@ -467,8 +552,12 @@ def compute_rhs(U: Tensor, P: Tensor, case: OracleCase) -> Tensor:
     for axis in case.active:
         flux = convective_flux_xi(P, case, axis)
         if case.viscous:
+            # space_solver.py:565-573: flux.at[1:5].add(-visc)
             visc = viscous_flux_xi(P, case, axis)
-            flux = torch.cat([flux[:1], flux[1:] - visc], 0)
+            flux = torch.cat([flux[:1], flux[1:] + (-visc)], 0)
+        if case.heat:
+            # space_solver.py:577-585: flux.at[4].add(heat_flux)
+            flux = torch.cat([flux[:4], (flux[4] + heat_flux_xi(P, case, axis)).unsqueeze(0)], 0)
         sl_lo = [slice(None)] * 4
         sl_hi = [slice(None)] * 4
         sl_lo[axis + 1] = slice(None, -1)
@@ -532,7 +621,7 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
         P[fill] = h
         if U is not None:
             U[fill] = cons_from_prims(h, case.gamma)
-    if case.viscous:
+    if case.viscous or case.heat:
         P, U = edge_halo_update(P, U, case)
     return P, U
 
@@ -614,8 +703,7 @@ def compute_dt(P: Tensor, case: OracleCase) -> Tensor:
         dt_v = 3.0 / 14.0 * (case.min_cell_size * case.min_cell_size) / (torch.max(nu) + EPS)
         dt = torch.minimum(dt, dt_v)
     if case.heat:
-        kappa = case.mu * case.cp() / case.prandtl
-        alpha = kappa / (rho * case.cp())
+        alpha = case.kappa() / (rho * case.cp())
         dt_h = 0.1 * (case.min_cell_size * case.min_cell_size) / (torch.max(alpha) + EPS)
         dt = torch.minimum(dt, dt_h)
     return dt * case.cfl

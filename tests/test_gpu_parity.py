@@ -61,6 +61,17 @@ RHS_CASES = [
     ("tgv-3d-mixed-char", dict(cells=(20, 12, 18), bc={"east": ZG, "west": ZG, "north": "SYMMETRY",
                                                        "south": "SYMMETRY", "top": "PERIODIC", "bottom": "PERIODIC"},
                                recon_var="CHAR-PRIMITIVE", ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-viscous-heat", dict(cells=(24, 24, 24), bc="PERIODIC", nh=4, viscous=True, heat=True, mu=1e-2,
+                                 prandtl=0.71, ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-char-roe-viscous", dict(cells=(20, 16, 24), bc="PERIODIC", nh=4, recon_var="CHAR-PRIMITIVE",
+                                     frozen_state="ROE", viscous=True, heat=True, mu=1.0 / 1600, prandtl=0.71,
+                                     bulk_viscosity=0.3e-3, ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-viscous-noheatprod", dict(cells=(16, 20, 12), bc="PERIODIC", nh=5, viscous=True, mu=5e-3,
+                                       viscous_heat_production=False, ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-heat-only", dict(cells=(16, 16, 16), bc="PERIODIC", nh=4, heat=True, mu=2e-2, prandtl=0.71,
+                              ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("quad-2d-viscous", dict(cells=(40, 32, 1), bc="PERIODIC", nh=4, viscous=True, heat=True, mu=1e-3,
+                             prandtl=0.71, riemann="RUSANOV"), "quad"),
     ("tgv-3d-mixed", dict(cells=(20, 12, 18), bc={"east": ZG, "west": ZG, "north": "SYMMETRY", "south": "SYMMETRY",
                                                   "top": "PERIODIC", "bottom": "PERIODIC"},
                           ranges=((0, 2 * math.pi),) * 3), "tgv"),
@@ -112,10 +123,11 @@ def test_user_tile_shapes_give_the_same_rhs():
 
 def test_initialize_and_halo_fill_match_oracle():
     from jaxfluids_gb300 import SimulationManager
-    for cells, bc, kind in (((200, 1, 1), ZG, "sod"), ((36, 44, 1), {"east": "PERIODIC", "west": "PERIODIC",
-                            "north": "SYMMETRY", "south": "SYMMETRY", "top": "PERIODIC", "bottom": "PERIODIC"}, "quad"),
-                            ((20, 12, 18), "PERIODIC", "tgv")):
-        oc, cc = both(cells, bc)
+    for cells, bc, kind, kw in (((200, 1, 1), ZG, "sod", {}), ((36, 44, 1), {"east": "PERIODIC", "west": "PERIODIC",
+                                "north": "SYMMETRY", "south": "SYMMETRY", "top": "PERIODIC", "bottom": "PERIODIC"},
+                                "quad", {}), ((20, 12, 18), "PERIODIC", "tgv", {}),
+                                ((20, 12, 18), "PERIODIC", "tgv", {"nh": 4, "viscous": True, "mu": 1e-2})):
+        oc, cc = both(cells, bc, **kw)
         prims = _prims_for(kind, cells)
         U, P = O.initialize(prims, oc)
         Ug, Pg = SimulationManager(cc).initialize(prims.cuda())
@@ -125,9 +137,11 @@ def test_initialize_and_halo_fill_match_oracle():
 
 def test_dt_matches_oracle():
     from jaxfluids_gb300 import SimulationManager
-    for cells, bc, kind, cfl in (((200, 1, 1), ZG, "sod", 0.5), ((48, 40, 1), ZG, "quad", 0.9),
-                                 ((24, 24, 24), "PERIODIC", "tgv", 0.5)):
-        oc, cc = both(cells, bc, cfl=cfl)
+    for cells, bc, kind, cfl, kw in (((200, 1, 1), ZG, "sod", 0.5, {}), ((48, 40, 1), ZG, "quad", 0.9, {}),
+                                     ((24, 24, 24), "PERIODIC", "tgv", 0.5, {}),
+                                     ((24, 24, 24), "PERIODIC", "tgv", 0.5,
+                                      {"nh": 4, "viscous": True, "heat": True, "mu": 0.5, "prandtl": 0.71})):
+        oc, cc = both(cells, bc, cfl=cfl, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
         dt = SimulationManager(cc).compute_time_step_size(P.cuda())
         ref = O.compute_dt(P, oc)
@@ -140,7 +154,11 @@ def test_steps_match_oracle(fused):
     cases = [((200, 1, 1), ZG, "sod", {}), ((48, 40, 1), ZG, "quad", {}),
              ((16, 16, 16), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3}),
              ((16, 12, 20), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3,
-                                                "recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"})]
+                                                "recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}),
+             ((16, 16, 16), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3, "nh": 4,
+                                                "recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
+                                                "viscous": True, "heat": True, "mu": 1.0 / 1600, "prandtl": 0.71}),
+             ((24, 20, 1), "PERIODIC", "quad", {"nh": 4, "viscous": True, "mu": 0.05})]
     for cells, bc, kind, kw in cases:
         oc, cc = both(cells, bc, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
