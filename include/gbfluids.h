@@ -171,6 +171,39 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
                     const gbf_tile* tile, void* stream);
 
 /*
+ * Batched fused TVD-RK3 of many independent cases of uneven size sharing one
+ * scheme (the reference batches equal-size cases with jax.vmap over
+ * SimulationManager._feed_forward, simulation_manager.py:1248-1294; here each
+ * case keeps its own size and its own CFL time step).
+ *
+ * Host-prepared device tables: `cases` (one gbf_batch_case per case) and
+ * `worklist` (int32 pairs {case, tile index within the case} for every tile of
+ * every case, tiles of shape `tile`).  States are packed per case: case c
+ * occupies doubles [offset, offset + 5 n_c) of `cons`, variable-major with
+ * stride n_c = cells of c.  `dt_states`: double[4 ncases] = per case {dt, t,
+ * reduction slots}.  `workspace`: two stage buffers of the packed size
+ * (gbf_batch_workspace_bytes).  Each stage is ONE persistent launch of `ctas`
+ * CTAs (0 = 2 per SM) looping over the work list; one more launch per step
+ * updates every case's dt.  No host synchronisation; graph-capturable.
+ * `scheme` supplies everything but the sizes (n, dx are taken per case).
+ */
+typedef struct gbf_batch_case {
+  int32_t n[3];          /* interior cells per axis */
+  int32_t tiles[3];      /* tiles per axis for the batch tile shape */
+  int64_t offset;        /* first double of the case in the packed buffers */
+  double dx[3];          /* cell sizes */
+} gbf_batch_case;
+
+size_t gbf_batch_workspace_bytes(int64_t total_doubles);
+int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                   const int32_t* worklist, int ntiles, const gbf_tile* tile, const double* cons,
+                   double* dt_states, double t0, void* stream);
+int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                      const int32_t* worklist, int ntiles, const gbf_tile* tile, int ctas,
+                      double* cons, double* dt_states, void* workspace, int64_t total_doubles,
+                      int steps, void* stream);
+
+/*
  * Allocation-free gbf_rk3_advance.  It has no counterpart in the reference.
  * For callers that can neither pass a workspace nor let the library call
  * cudaMalloc: an XLA custom call, whose device memory must come from XLA's

@@ -17,9 +17,10 @@ from .config import CaseConfig, SetupError
 from .solver import (DiscretizationCounter, EquationManager, EulerIntegrationBuffers, HaloManager,
                      IntegrationBuffers, PositivityCounter, SpaceSolver, TimeIntegrator, TimeStepSize)
 from .simulation import FusedRK3, SimulationManager
+from .batch import BatchedRK3, autotune
 
 __all__ = [
     "CaseConfig", "SetupError", "SpaceSolver", "HaloManager", "EquationManager", "TimeIntegrator",
     "TimeStepSize", "SimulationManager", "FusedRK3", "IntegrationBuffers", "EulerIntegrationBuffers",
-    "PositivityCounter", "DiscretizationCounter",
+    "PositivityCounter", "DiscretizationCounter", "BatchedRK3", "autotune",
 ]

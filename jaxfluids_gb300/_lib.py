@@ -31,6 +31,7 @@ EXPORTS = (
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
+    "gbf_batch_workspace_bytes", "gbf_batch_init", "gbf_batch_advance",
 )
 
 # interior cells the allocation-free entry point's built-in scratch holds
@@ -100,6 +101,9 @@ def load() -> ctypes.CDLL:
         "gbf_rk3_advance": (I, [C, P, P, P, I, T, P]),
         "gbf_rk3_advance_noalloc": (I, [C, P, P, I, T, P]),
         "gbf_probe_arith": (I, [I, P, I, I, I, P]),
+        "gbf_batch_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+        "gbf_batch_init": (I, [C, P, I, P, I, T, P, P, ctypes.c_double, P]),
+        "gbf_batch_advance": (I, [C, P, I, P, I, T, I, P, P, P, ctypes.c_int64, I, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1,0 +1,256 @@
+// Batched fused TVD-RK3 over many independent cases of uneven size.
+//
+// One persistent kernel per RK stage walks a work list of (case, tile)
+// pairs; each tile runs the same fused sweep as the single-case path with the
+// case's sizes, cell widths, state offsets and time-step slots.  Small cases
+// that would each leave most of the GPU idle (a 64^2 case is 8 tiles) thereby
+// share one launch, and the whole step (3 stage launches + 1 time-step
+// launch) has a fixed launch sequence that can be captured in a CUDA graph.
+#include <algorithm>
+
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+namespace {
+
+constexpr int kMaxCellsPerThread = 4;
+
+struct BatchParams {
+  SweepParams base;            // scheme and tile shape (sizes are per case)
+  const gbf_batch_case* cases;
+  const int32_t* worklist;
+  int ntiles;
+  int stage;
+  const double* cons;          // stage input (packed)
+  const double* cons0;         // step state U^n (packed)
+  double* out;                 // stage output (packed)
+  double* dt_states;           // 4 per case
+  int reduce_dt;
+};
+
+__device__ __forceinline__ void case_params(const BatchParams& bp, int c, SweepParams& p) {
+  p = bp.base;
+  const gbf_batch_case& cs = bp.cases[c];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    p.n[a] = cs.n[a];
+    p.tiles[a] = cs.tiles[a];
+    p.one_dx[a] = 1.0 / cs.dx[a];
+  }
+  p.cons = bp.cons + cs.offset;
+  p.cons0 = bp.cons0 + cs.offset;
+  p.out = bp.out + cs.offset;
+  p.dt_state = bp.dt_states + 4 * c;
+  p.stage = bp.stage;
+  p.reduce_dt = bp.reduce_dt;
+}
+
+template <int RECON, int RIEMANN>
+__global__ void __launch_bounds__(256) batch_sweep_kernel(const BatchParams bp) {
+  extern __shared__ double smem[];
+  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
+    const int c = bp.worklist[2 * item];
+    const int tile = bp.worklist[2 * item + 1];
+    SweepParams p;
+    case_params(bp, c, p);
+    sweep_tile<RECON, RIEMANN, MODE_STAGE, kMaxCellsPerThread, false>(p, tile, smem);
+  }
+}
+
+// Per-case maximum signal speed and minimum density of the packed states
+// (time_step_size.py:96-109), one tile per work item.
+__global__ void batch_reduce_kernel(const BatchParams bp, double gm1, double gamma) {
+  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
+    const int c = bp.worklist[2 * item];
+    const int tile = bp.worklist[2 * item + 1];
+    const gbf_batch_case& cs = bp.cases[c];
+    const int t0 = bp.base.t[0], t1 = bp.base.t[1], t2 = bp.base.t[2];
+    const int b2 = tile % cs.tiles[2];
+    const int b1 = (tile / cs.tiles[2]) % cs.tiles[1];
+    const int b0 = tile / (cs.tiles[2] * cs.tiles[1]);
+    const int o[3] = {b0 * t0, b1 * t1, b2 * t2};
+    const int e[3] = {min(t0, cs.n[0] - o[0]), min(t1, cs.n[1] - o[1]), min(t2, cs.n[2] - o[2])};
+    const long long ncs = (long long)cs.n[0] * cs.n[1] * cs.n[2];
+    double smax = 0.0;
+    double rmin = __longlong_as_double(0x7ff0000000000000LL);
+    for (int i = threadIdx.x; i < e[0] * e[1] * e[2]; i += blockDim.x) {
+      const int i2 = i % e[2], i1 = (i / e[2]) % e[1], i0 = i / (e[2] * e[1]);
+      const long long off = ((long long)(o[0] + i0) * cs.n[1] + (o[1] + i1)) * cs.n[2] + (o[2] + i2);
+      double U[5], P[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) U[v] = bp.cons[cs.offset + v * ncs + off];
+      prims_from_cons(U, P, gm1);
+      const double cc = sqrt(gamma * P[4] / P[0]);
+      double s = 0.0;
+      if (cs.n[0] > 1) s = s + (fabs(P[1]) + cc);
+      if (cs.n[1] > 1) s = s + (fabs(P[2]) + cc);
+      if (cs.n[2] > 1) s = s + (fabs(P[3]) + cc);
+      smax = fmax(smax, s);
+      rmin = fmin(rmin, P[0]);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      unsigned long long* red = reinterpret_cast<unsigned long long*>(bp.dt_states + 4 * c + 2);
+      atomicMax(red, (unsigned long long)__double_as_longlong(smax));
+      atomicMin(red + 1, (unsigned long long)__double_as_longlong(rmin));
+    }
+  }
+}
+
+// Every case's next dt from its reduction slots (time_step_size.py:97-155);
+// t += previous dt when advance_time.  Resets the slots.
+__global__ void batch_dt_kernel(const gbf_batch_case* cases, int ncases, double* dt_states,
+                                double cfl, double eps, double fixed_dt, int advance_time,
+                                double t0, int set_time) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases) return;
+  double* st = dt_states + 4 * c;
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(st + 2);
+  if (set_time) st[1] = t0;
+  if (advance_time) st[1] = st[1] + st[0];
+  double dt;
+  if (fixed_dt > 0.0) {
+    dt = fixed_dt;
+  } else {
+    double mdx = INFINITY;
+    for (int a = 0; a < 3; ++a)
+      if (cases[c].n[a] > 1) mdx = fmin(mdx, cases[c].dx[a]);
+    const double smax = __longlong_as_double((long long)red[0]);
+    dt = mdx / (smax + eps);
+    dt = dt * cfl;
+  }
+  st[0] = dt;
+  red[0] = 0ull;
+  red[1] = (unsigned long long)0x7ff0000000000000ull;
+}
+
+__global__ void batch_slot_init_kernel(double* dt_states, int ncases) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases) return;
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(dt_states + 4 * c + 2);
+  red[0] = 0ull;
+  red[1] = (unsigned long long)0x7ff0000000000000ull;
+}
+
+int launch_batch_sweep(const gbf_case* c, const BatchParams& bp, int threads, size_t smem, int ctas,
+                       cudaStream_t s) {
+  const int grid = std::max(1, std::min(ctas, bp.ntiles));
+#define GBF_LAUNCH(RC, RM)                                                                          \
+  {                                                                                                 \
+    auto k = batch_sweep_kernel<RC, RM>;                                                            \
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=          \
+        cudaSuccess)                                                                                \
+      return GBF_ERR_CUDA;                                                                          \
+    k<<<grid, threads, smem, s>>>(bp);                                                              \
+    return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;                               \
+  }
+  const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE) {
+    if (hllc) GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC) else GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV)
+  }
+  switch (c->recon) {
+    case GBF_RECON_WENO5Z:
+      if (hllc) GBF_LAUNCH(GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV)
+    case GBF_RECON_MINMOD:
+      if (hllc) GBF_LAUNCH(GBF_RECON_MINMOD, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV)
+    default:
+      if (hllc) GBF_LAUNCH(GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV)
+  }
+#undef GBF_LAUNCH
+}
+
+// Scheme checks shared by init and advance; fills the base params from a
+// representative case (the largest tile shape fits every case).
+int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                const int32_t* worklist, int ntiles, const gbf_tile* tile, BatchParams* bp,
+                int* threads, size_t* smem) {
+  if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
+  if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) return GBF_ERR_UNSUPPORTED;
+  // validate the scheme on a case of the tile's size (sizes vary per case)
+  gbf_case rep = *scheme;
+  int st = gbf_case_check(&rep);
+  if (st != GBF_OK) return st;
+  CaseInfo ci;
+  if ((st = make_case_info(&rep, &ci)) != GBF_OK) return st;
+  SweepParams p;
+  if ((st = make_sweep_params(&rep, ci, tile, &p, threads, smem)) != GBF_OK) return st;
+  // the tile shape must be the one the work list was built with
+  for (int a = 0; a < 3; ++a)
+    if (p.t[a] != std::max(1, tile->t[a]) && rep.n[a] > 1) return GBF_ERR_INVALID_ARGUMENT;
+  BatchParams b{};
+  b.base = p;
+  b.cases = cases;
+  b.worklist = worklist;
+  b.ntiles = ntiles;
+  *bp = b;
+  return GBF_OK;
+}
+
+}  // namespace
+
+}  // namespace gbf
+
+using namespace gbf;
+
+extern "C" size_t gbf_batch_workspace_bytes(int64_t total_doubles) {
+  return total_doubles > 0 ? (size_t)2 * (size_t)total_doubles * sizeof(double) : 0;
+}
+
+extern "C" int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                              const int32_t* worklist, int ntiles, const gbf_tile* tile,
+                              const double* cons, double* dt_states, double t0, void* stream) {
+  BatchParams bp;
+  int threads;
+  size_t smem;
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
+  if (st != GBF_OK) return st;
+  if (!cons || !dt_states) return GBF_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int cb = (ncases + 127) / 128;
+  batch_slot_init_kernel<<<cb, 128, 0, s>>>(dt_states, ncases);
+  bp.cons = cons;
+  bp.dt_states = dt_states;
+  batch_reduce_kernel<<<std::min(ntiles, 152 * 8), 256, 0, s>>>(bp, scheme->gamma - 1.0, scheme->gamma);
+  batch_dt_kernel<<<cb, 128, 0, s>>>(cases, ncases, dt_states, scheme->cfl, scheme->eps, scheme->fixed_dt,
+                                     0, t0, 1);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+extern "C" int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                                 const int32_t* worklist, int ntiles, const gbf_tile* tile, int ctas,
+                                 double* cons, double* dt_states, void* workspace,
+                                 int64_t total_doubles, int steps, void* stream) {
+  BatchParams bp;
+  int threads;
+  size_t smem;
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
+  if (st != GBF_OK) return st;
+  if (!cons || !dt_states || !workspace || steps < 0 || total_doubles <= 0) return GBF_ERR_INVALID_ARGUMENT;
+  if (ctas <= 0) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ctas = 2 * sms;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* A = (double*)workspace;
+  double* B = A + total_doubles;
+  const int cb = (ncases + 127) / 128;
+  bp.dt_states = dt_states;
+  for (int step = 0; step < steps; ++step) {
+    bp.stage = 0; bp.cons = cons; bp.cons0 = cons; bp.out = A; bp.reduce_dt = 0;
+    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    bp.stage = 1; bp.cons = A; bp.cons0 = cons; bp.out = B;
+    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    bp.stage = 2; bp.cons = B; bp.cons0 = cons; bp.out = cons; bp.reduce_dt = 1;
+    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    batch_dt_kernel<<<cb, 128, 0, s>>>(cases, ncases, dt_states, scheme->cfl, scheme->eps,
+                                       scheme->fixed_dt, 1, 0.0, 0);
+    if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
+  }
+  return GBF_OK;
+}

@@ -326,10 +326,9 @@ __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, do
   return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 2.0 / 3.0), rhs));
 }
 
+// One tile (index b of the case described by p) of the fused sweep.
 template <int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
-__global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
-  extern __shared__ double smem[];
-  const int b = blockIdx.x;
+__device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* smem) {
   const int b2 = b % p.tiles[2];
   const int b1 = (b / p.tiles[2]) % p.tiles[1];
   const int b0 = b / (p.tiles[2] * p.tiles[1]);
@@ -443,7 +442,14 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
         atomicMin(reinterpret_cast<unsigned long long*>(p.dt_state + 3), ordered_bits(rmin));
       }
     }
+    __syncthreads();  // red[] is reused by the next tile of a persistent CTA
   }
+}
+
+template <int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
+__global__ void __launch_bounds__(256) sweep_kernel(const SweepParams p) {
+  extern __shared__ double smem[];
+  sweep_tile<RECON, RIEMANN, MODE, MAXC, VISC>(p, blockIdx.x, smem);
 }
 
 }  // namespace gbf
