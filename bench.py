@@ -185,6 +185,86 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def batch_cases(ncases=256, seed=0):
+    """Batched 2-D four-quadrant Riemann problems: sides from {64,...,512}
+    (default_rng(0)), per-case quadrant states from default_rng(1000 + i):
+    rho, u, v, p drawn per quadrant from U[0.1,2], U[-1,1], U[-1,1], U[0.1,2]."""
+    import numpy as np
+    from jaxfluids_gb300 import CaseConfig
+    sides = np.random.default_rng(seed).choice([64, 128, 192, 256, 384, 512], size=ncases)
+    cfgs, states = [], []
+    for i, n in enumerate(sides):
+        n = int(n)
+        rng = np.random.default_rng(1000 + i)
+        st = np.stack([rng.uniform(0.1, 2, 4), rng.uniform(-1, 1, 4), rng.uniform(-1, 1, 4), rng.uniform(0.1, 2, 4)])
+        x = (np.arange(n) + 0.5) / n
+        X, Y = np.meshgrid(x, x, indexing="ij")
+        q = (X >= 0.5).astype(int) + 2 * (Y >= 0.5).astype(int)
+        rho, u, v, p = (st[k][q] for k in range(4))
+        E = p / 0.4 + 0.5 * rho * (u * u + v * v)
+        U = np.stack([rho, rho * u, rho * v, np.zeros_like(rho), E]).reshape(5, n, n, 1)
+        cfgs.append(CaseConfig(cells=(n, n, 1), bc={f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")},
+                               recon="WENO5-Z", riemann="HLLC", signal_speed="EINFELDT", cfl=0.5))
+        states.append(torch.from_numpy(U))
+    return cfgs, states
+
+
+def run_batch(args):
+    """Batched (one persistent launch per stage, graph-captured, autotuned)
+    against one case at a time through the single-case fused path."""
+    from jaxfluids_gb300 import BatchedRK3, FusedRK3, autotune, build
+    build.build()
+    device = torch.device("cuda", 0)
+    cfgs, states = batch_cases(args.cases)
+    cells = sum(c.n_cells for c in cfgs)
+    batch = BatchedRK3(cfgs, device)
+    batch.set_states([s.to(device) for s in states])
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    tune = autotune(batch, candidates=[((16, 32, 1), 256, 2 * sms), ((32, 16, 1), 256, 2 * sms),
+                                       ((8, 64, 1), 256, 2 * sms), ((16, 16, 1), 128, 3 * sms),
+                                       ((16, 32, 1), 256, sms), ((32, 32, 1), 256, 2 * sms)], steps=1)
+    graph = batch.capture(args.steps)
+    for _ in range(max(1, args.warmup // max(1, args.steps))):
+        graph.replay()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    graph.replay()
+    b.record()
+    b.synchronize()
+    t_batch = a.elapsed_time(b) / 1e3
+    batched = cells * args.steps / t_batch
+    # one case at a time: every case its own fused launches, cases in sequence
+    singles = []
+    for cfg, s in zip(cfgs, states):
+        f = FusedRK3(cfg, device)
+        f.set_state(s.to(device))
+        singles.append(f)
+    for f in singles:
+        f.advance(1)
+    torch.cuda.synchronize()
+    n_single = max(1, min(args.steps, 3))
+    a.record()
+    for _ in range(n_single):
+        for f in singles:
+            f.advance(1)
+    b.record()
+    b.synchronize()
+    t_single = a.elapsed_time(b) / 1e3
+    single = cells * n_single / t_single
+    line = {"metric": "FP64 cell-updates/s, batched 2-D four-quadrant Riemann problems", "value": batched,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"{len(cfgs)} cases, sides from {{64..512}}, {cells} cells, WENO5-Z+HLLC, ZG",
+                       "autotuned": {"tile": tune["best"][0], "threads": tune["best"][1], "ctas": tune["best"][2]},
+                       "graph_steps": args.steps},
+            "one_case_at_a_time": {"value": single, "steps": n_single, "ms_per_step": 1e3 * t_single / n_single},
+            "speedup_vs_one_at_a_time": batched / single,
+            "autotune_ms_per_step": [[list(c[0]), c[1], c[2], ms] for c, ms in tune["results"]]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -193,7 +273,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_TGV)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "batch"])
+    ap.add_argument("--cases", type=int, default=256)
     args = ap.parse_args()
+    if args.workload == "batch":
+        return run_batch(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -171,6 +171,27 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
                     const gbf_tile* tile, void* stream);
 
 /*
+ * Adjoint (reverse mode) of the fused path, replacing jax.grad through
+ * SimulationManager._feed_forward with a fixed time step
+ * (feed_forward/feed_forward.py:231-524, simulation_manager.py:1296-1412).
+ * Follows jax.grad's conventions at non-smooth points (|x|' = +1 at 0, half
+ * of the cotangent to each argument of a max/min tie, zero derivative of
+ * sign, where() passes the selected branch).  Inviscid, PRIMITIVE
+ * reconstruction with WENO5-Z or MINMOD-AD, HLLC (Einfeldt speeds) or Rusanov.
+ *
+ * gbf_rhs_vjp: out = J(U)^T w with J = d rhs / d U at the interior state
+ *   `cons`; w, out interior [5][N].  workspace >= 5 N doubles.
+ * gbf_rk3_step_vjp: lam_out = (d U^{n+1} / d U^n)^T lam for one TVD-RK3 step
+ *   from U^n = `cons` with the device time step *dt (stage states recomputed).
+ *   workspace: gbf_vjp_workspace_bytes(c).  lam_out must not alias lam.
+ */
+size_t gbf_vjp_workspace_bytes(const gbf_case* c);
+int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out, void* workspace,
+                const gbf_tile* tile, void* stream);
+int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
+                     double* lam_out, void* workspace, const gbf_tile* tile, void* stream);
+
+/*
  * Batched fused TVD-RK3 of many independent cases of uneven size sharing one
  * scheme (the reference batches equal-size cases with jax.vmap over
  * SimulationManager._feed_forward, simulation_manager.py:1248-1294; here each

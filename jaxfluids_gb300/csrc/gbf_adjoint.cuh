@@ -1,0 +1,408 @@
+// Hand-written reverse mode (vector-Jacobian products) of the right-hand side.
+//
+// Each function recomputes the forward intermediates of its counterpart in
+// gbf_physics.cuh and propagates a cotangent backwards through them, with
+// jax.grad's conventions at the non-smooth points the reference hits:
+//   d|x|/dx        = +1 at x = 0  (select(x >= 0, g, -g))
+//   max / min tie  = half of the cotangent to each argument
+//   sign(x)        : zero derivative
+//   where(c, a, b) : cotangent to the selected branch only.
+#pragma once
+
+#include "gbf_physics.cuh"
+
+namespace gbf {
+
+__device__ __forceinline__ double jabs_grad(double x) { return (x >= 0.0) ? 1.0 : -1.0; }
+
+// d min(a, b): weight of a (1, 0.5 at a tie, 0)
+__device__ __forceinline__ double min_weight_a(double a, double b) {
+  return (a < b) ? 1.0 : ((a == b) ? 0.5 : 0.0);
+}
+__device__ __forceinline__ double max_weight_a(double a, double b) {
+  return (a > b) ? 1.0 : ((a == b) ? 0.5 : 0.0);
+}
+
+// Reverse of weno5z(u0..u4): du[k] += g * d out / d u_k.
+__device__ __forceinline__ void weno5z_vjp(double u0, double u1, double u2, double u3, double u4,
+                                           double eps, double g, double du[5]) {
+  constexpr double c13 = 13.0 / 12.0;
+  const double t0 = u0 - 2.0 * u1 + u2;
+  const double t1 = u0 - 4.0 * u1 + 3.0 * u2;
+  const double t2 = u1 - 2.0 * u2 + u3;
+  const double t3 = u1 - u3;
+  const double t4 = u2 - 2.0 * u3 + u4;
+  const double t5 = 3.0 * u2 - 4.0 * u3 + u4;
+  const double b0 = c13 * (t0 * t0) + 0.25 * (t1 * t1);
+  const double b1 = c13 * (t2 * t2) + 0.25 * (t3 * t3);
+  const double b2 = c13 * (t4 * t4) + 0.25 * (t5 * t5);
+  const double tau = fabs(b0 - b2);
+  const double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+  const double q0 = tau / e0, q1 = tau / e1, q2 = tau / e2;
+  const double a0 = 0.1 * (1.0 + q0), a1 = 0.6 * (1.0 + q1), a2 = 0.3 * (1.0 + q2);
+  const double r = 1.0 / (a0 + a1 + a2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  const double w0 = a0 * r, w1 = a1 * r, w2 = a2 * r;
+  // out = w0 p0 + w1 p1 + w2 p2
+  const double dw0 = g * p0, dw1 = g * p1, dw2 = g * p2;
+  const double dp0 = g * w0, dp1 = g * w1, dp2 = g * w2;
+  du[0] += (1.0 / 3.0) * dp0;
+  du[1] += (-7.0 / 6.0) * dp0 + (-1.0 / 6.0) * dp1;
+  du[2] += (11.0 / 6.0) * dp0 + (5.0 / 6.0) * dp1 + (1.0 / 3.0) * dp2;
+  du[3] += (1.0 / 3.0) * dp1 + (5.0 / 6.0) * dp2;
+  du[4] += (-1.0 / 6.0) * dp2;
+  // w_k = a_k r, r = 1 / S
+  const double dr = dw0 * a0 + dw1 * a1 + dw2 * a2;
+  const double dS = -dr * r * r;
+  const double da0 = dw0 * r + dS, da1 = dw1 * r + dS, da2 = dw2 * r + dS;
+  // a_k = d_k (1 + q_k), q_k = tau / e_k
+  const double dq0 = 0.1 * da0, dq1 = 0.6 * da1, dq2 = 0.3 * da2;
+  const double dtau = dq0 / e0 + dq1 / e1 + dq2 / e2;
+  double db0 = -dq0 * q0 / e0;
+  const double db1 = -dq1 * q1 / e1;
+  double db2 = -dq2 * q2 / e2;
+  const double sg = jabs_grad(b0 - b2);
+  db0 += dtau * sg;
+  db2 -= dtau * sg;
+  // b = c13 t^2 + 1/4 t'^2
+  const double dt0 = db0 * c13 * 2.0 * t0, dt1 = db0 * 0.5 * t1;
+  const double dt2 = db1 * c13 * 2.0 * t2, dt3 = db1 * 0.5 * t3;
+  const double dt4 = db2 * c13 * 2.0 * t4, dt5 = db2 * 0.5 * t5;
+  du[0] += dt0 + dt1;
+  du[1] += -2.0 * dt0 - 4.0 * dt1 + dt2 + dt3;
+  du[2] += dt0 + 3.0 * dt1 - 2.0 * dt2 + dt4 + 3.0 * dt5;
+  du[3] += dt2 - dt3 - 2.0 * dt4 - 4.0 * dt5;
+  du[4] += dt4 + dt5;
+}
+
+// Reverse of minmod_ad<J>(b0, b1, b2): the ratio only selects a branch.
+template <int J>
+__device__ __forceinline__ void minmod_ad_vjp(double b0, double b1, double b2, double eps, double g,
+                                              double& db0, double& db1, double& db2) {
+  const double dc = (J == 0) ? b2 - b1 : b1 - b2;
+  const double du = (J == 0) ? b1 - b0 : b0 - b1;
+  const double r = (du >= eps) ? dc / (du + 1e-100) : (dc + eps) / (du + eps);
+  if (r < 0.0) {
+    db1 += g;
+  } else if (r < 1.0) {
+    db1 += 0.5 * g;
+    db2 += 0.5 * g;
+  } else {
+    db1 += 1.5 * g;
+    db0 -= 0.5 * g;
+  }
+}
+
+template <int RECON>
+__device__ __forceinline__ void reconstruct_pair_vjp(const double* w, double eps, double gL, double gR,
+                                                     double* dw);
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5Z>(const double* w, double eps,
+                                                                        double gL, double gR, double* dw) {
+  double dl[5] = {0, 0, 0, 0, 0}, dr[5] = {0, 0, 0, 0, 0};
+  weno5z_vjp(w[0], w[1], w[2], w[3], w[4], eps, gL, dl);
+  weno5z_vjp(w[5], w[4], w[3], w[2], w[1], eps, gR, dr);
+  dw[0] = dl[0];
+  dw[1] = dl[1] + dr[4];
+  dw[2] = dl[2] + dr[3];
+  dw[3] = dl[3] + dr[2];
+  dw[4] = dl[4] + dr[1];
+  dw[5] = dr[0];
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_MINMOD_AD>(const double* w, double eps,
+                                                                           double gL, double gR, double* dw) {
+  double d[4] = {0, 0, 0, 0};
+  minmod_ad_vjp<0>(w[0], w[1], w[2], eps, gL, d[0], d[1], d[2]);
+  minmod_ad_vjp<1>(w[3], w[2], w[1], eps, gR, d[3], d[2], d[1]);
+  dw[0] = d[0];
+  dw[1] = d[1];
+  dw[2] = d[2];
+  dw[3] = d[3];
+}
+
+// Reverse of cons_from_prims: dP += (dU/dP)^T dU.
+__device__ __forceinline__ void cons_from_prims_vjp(const double P[5], const double dU[5], double gm1,
+                                                    double dP[5]) {
+  const double rho = P[0];
+  const double den = rho * gm1;
+  const double e = P[4] / den;
+  const double s = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
+  const double h = 0.5 * s + e;
+  // U0 = rho, Ui = rho Pi, U4 = rho h
+  double drho = dU[0] + dU[1] * P[1] + dU[2] * P[2] + dU[3] * P[3] + dU[4] * h;
+  const double dh = dU[4] * rho;
+  const double ds = 0.5 * dh;
+#pragma unroll
+  for (int i = 1; i <= 3; ++i) dP[i] += dU[i] * rho + ds * 2.0 * P[i];
+  // e = P4 / (rho gm1)
+  dP[4] += dh / den;
+  drho += -dh * e / den * gm1;
+  dP[0] += drho;
+}
+
+// Reverse of prims_from_cons: dU += (dP/dU)^T dP.
+__device__ __forceinline__ void prims_from_cons_vjp(const double U[5], const double dP[5], double gm1,
+                                                    double dU[5]) {
+  const double rho = U[0];
+  const double one_rho = 1.0 / rho;
+  const double u = U[1] * one_rho, v = U[2] * one_rho, w = U[3] * one_rho;
+  const double e = U[4] * one_rho - 0.5 * (u * u + v * v + w * w);
+  // P0 = rho, P1..3 = U1..3 * one_rho, P4 = gm1 e rho
+  double drho = dP[0] + dP[4] * gm1 * e;
+  const double de = dP[4] * gm1 * rho;
+  const double ds = -0.5 * de;
+  const double du = dP[1] + ds * 2.0 * u;
+  const double dv = dP[2] + ds * 2.0 * v;
+  const double dw = dP[3] + ds * 2.0 * w;
+  double done = de * U[4] + du * U[1] + dv * U[2] + dw * U[3];
+  dU[4] += de * one_rho;
+  dU[1] += du * one_rho;
+  dU[2] += dv * one_rho;
+  dU[3] += dw * one_rho;
+  drho += -done * one_rho * one_rho;
+  dU[0] += drho;
+}
+
+
+// Reverse of the physical flux F(P, U) along AX (equation_manager.py:237-252).
+template <int AX>
+__device__ __forceinline__ void physical_flux_vjp(const double P[5], const double U[5], const double dF[5],
+                                                  double dP[5], double dU[5]) {
+  constexpr int N = AX + 1;
+  const double m = U[N];
+  dU[N] += dF[0] + dF[1] * P[1] + dF[2] * P[2] + dF[3] * P[3];
+  dP[1] += dF[1] * m;
+  dP[2] += dF[2] * m;
+  dP[3] += dF[3] * m;
+  dP[N] += dF[4] * (U[4] + P[4]);
+  dU[4] += dF[4] * P[N];
+  dP[4] += dF[4] * P[N] + dF[N];
+}
+
+// Reverse of hllc_star_flux<AX, J> (HLLC.py:41-78).  Accumulates into dP, dU,
+// dS (own wave speed) and dSs (contact speed).
+template <int AX, int J>
+__device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const double U[5], double S,
+                                                   double Ss, const double dF[5], double dP[5], double dU[5],
+                                                   double& dS, double& dSs) {
+  constexpr int N = AX + 1;
+  constexpr int T1 = (AX == 0) ? 2 : 1;
+  constexpr int T2 = (AX == 2) ? 2 : 3;
+  const double n1 = S - P[N];
+  const double d1 = S - Ss;
+  const double m = n1 / d1;
+  const double pre = m * P[0];
+  const double A = U[4] / U[0];
+  const double q = P[4] / P[0];
+  const double D = q / n1;
+  const double B = Ss - P[N];
+  const double C = Ss + D;
+  const double X = A + B * C;
+  const double e_term = pre * X;
+  double us[5] = {pre, pre, pre, pre, e_term};
+  us[N] *= Ss;
+  us[T1] *= P[T1];
+  us[T2] *= P[T2];
+  const double wave = (J == 0) ? fmin(S, 0.0) : fmax(S, 0.0);
+  // F* = F(P, U) + wave (us - U)
+  physical_flux_vjp<AX>(P, U, dF, dP, dU);
+  double dwave = 0.0;
+  double dus[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    dwave += dF[v] * (us[v] - U[v]);
+    dus[v] = wave * dF[v];
+    dU[v] -= wave * dF[v];
+  }
+  dS += dwave * ((J == 0) ? min_weight_a(S, 0.0) : max_weight_a(S, 0.0));
+  // us components
+  double dpre = dus[0] + dus[N] * Ss + dus[T1] * P[T1] + dus[T2] * P[T2] + dus[4] * X;
+  dSs += dus[N] * pre;
+  dP[T1] += dus[T1] * pre;
+  dP[T2] += dus[T2] * pre;
+  const double dX = dus[4] * pre;
+  // X = A + B C
+  dU[4] += dX / U[0];
+  dU[0] += -dX * A / U[0];
+  const double dB = dX * C, dC = dX * B;
+  dSs += dB + dC;
+  double du = -dB;
+  // D = q / n1
+  const double dq = dC / n1;
+  double dn1 = -dC * D / n1;
+  dP[4] += dq / P[0];
+  dP[0] += -dq * q / P[0];
+  // pre = m rho, m = n1 / d1
+  const double dm = dpre * P[0];
+  dP[0] += dpre * m;
+  dn1 += dm / d1;
+  const double dd1 = -dm * m / d1;
+  dS += dn1 + dd1;
+  du -= dn1;
+  dSs -= dd1;
+  dP[N] += du;
+}
+
+// Reverse of hllc<AX> with Einfeldt wave speeds (HLLC.py:80-126,
+// signal_speeds.py:109-133, :159-199); the cons of the face states are
+// recomputed and reversed too.  dPL, dPR are accumulated.
+template <int AX>
+__device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
+                                         const double dF[5], double dPL[5], double dPR[5]) {
+  constexpr int N = AX + 1;
+  const double gamma = fp.gamma;
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, fp.gm1);
+  cons_from_prims(PR, UR, fp.gm1);
+  const double uL = PL[N], uR = PR[N], rL = PL[0], rR = PR[0], pL = PL[4], pR = PR[4];
+  const double yL = gamma * pL / rL, yR = gamma * pR / rR;
+  const double cL = sqrt(yL), cR = sqrt(yR);
+  const double sL = sqrt(rL), sR = sqrt(rR);
+  const double od = 1.0 / (sL + sR);
+  const double eta2 = 0.5 * sL * sR * od * od;
+  const double ubar = (sL * uL + sR * uR) * od;
+  const double duu = uR - uL;
+  const double Wn = sL * cL * cL + sR * cR * cR;
+  const double Z = Wn * od + eta2 * (duu * duu);
+  const double dbar = sqrt(Z);
+  const double X1 = ubar - dbar, X2 = uL - cL, Y1 = ubar + dbar, Y2 = uR + cR;
+  const double SL = fmin(X1, X2), SR = fmax(Y1, Y2);
+  const double rdL = rL * (SL - uL), rdR = rR * (SR - uR);
+  const double num = (pR - pL) + (uL * rdL - uR * rdR);
+  const double den = rdL - rdR;
+  const double Ss = num / den;
+  const double sg = (Ss > 0.0) ? 1.0 : ((Ss < 0.0) ? -1.0 : 0.0);
+  const double wl = 0.5 * (1.0 + sg), wr = 0.5 * (1.0 - sg);
+  double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
+  double dSL = 0.0, dSR = 0.0, dSs = 0.0;
+  if (wl != 0.0) {
+    double g[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) g[v] = wl * dF[v];
+    hllc_star_flux_vjp<AX, 0>(PL, UL, SL, Ss, g, dPL, dUL, dSL, dSs);
+  }
+  if (wr != 0.0) {
+    double g[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) g[v] = wr * dF[v];
+    hllc_star_flux_vjp<AX, 1>(PR, UR, SR, Ss, g, dPR, dUR, dSR, dSs);
+  }
+  // Ss = num / den
+  const double dnum = dSs / den;
+  const double dden = -dSs * Ss / den;
+  dPR[4] += dnum;
+  dPL[4] -= dnum;
+  double duL = dnum * rdL, duR = -dnum * rdR;
+  const double drdL = dnum * uL + dden, drdR = -dnum * uR - dden;
+  // rd = rho (S - u)
+  double drL = drdL * (SL - uL), drR = drdR * (SR - uR);
+  dSL += drdL * rL;
+  duL -= drdL * rL;
+  dSR += drdR * rR;
+  duR -= drdR * rR;
+  // SL = min(X1, X2), SR = max(Y1, Y2)
+  const double wx = min_weight_a(X1, X2), wy = max_weight_a(Y1, Y2);
+  const double dX1 = dSL * wx, dX2 = dSL * (1.0 - wx);
+  const double dY1 = dSR * wy, dY2 = dSR * (1.0 - wy);
+  const double dubar = dX1 + dY1;
+  const double ddbar = -dX1 + dY1;
+  duL += dX2;
+  double dcL = -dX2;
+  duR += dY2;
+  double dcR = dY2;
+  // dbar = sqrt(Z), Z = Wn od + eta2 du^2
+  const double dZ = ddbar * (0.5 / dbar);
+  const double dWn = dZ * od;
+  double dod = dZ * Wn;
+  const double deta2 = dZ * (duu * duu);
+  const double dduu = dZ * eta2 * 2.0 * duu;
+  duR += dduu;
+  duL -= dduu;
+  double dsL = dWn * cL * cL, dsR = dWn * cR * cR;
+  dcL += dWn * sL * 2.0 * cL;
+  dcR += dWn * sR * 2.0 * cR;
+  // eta2 = 0.5 sL sR od od
+  dsL += deta2 * 0.5 * sR * od * od;
+  dsR += deta2 * 0.5 * sL * od * od;
+  dod += deta2 * 0.5 * sL * sR * 2.0 * od;
+  // ubar = (sL uL + sR uR) od
+  dsL += dubar * uL * od;
+  dsR += dubar * uR * od;
+  duL += dubar * sL * od;
+  duR += dubar * sR * od;
+  dod += dubar * (sL * uL + sR * uR);
+  // od = 1 / (sL + sR)
+  const double dsum = -dod * od * od;
+  dsL += dsum;
+  dsR += dsum;
+  drL += dsL * (0.5 / sL);
+  drR += dsR * (0.5 / sR);
+  // c = sqrt(y), y = gamma p / rho
+  const double dyL = dcL * (0.5 / cL), dyR = dcR * (0.5 / cR);
+  drL += -dyL * yL / rL;
+  drR += -dyR * yR / rR;
+  dPL[4] += dyL / rL * gamma;
+  dPR[4] += dyR / rR * gamma;
+  dPL[0] += drL;
+  dPR[0] += drR;
+  dPL[N] += duL;
+  dPR[N] += duR;
+  // U = cons(P)
+  cons_from_prims_vjp(PL, dUL, fp.gm1, dPL);
+  cons_from_prims_vjp(PR, dUR, fp.gm1, dPR);
+}
+
+// Reverse of rusanov<AX> (Rusanov.py:25-47).
+template <int AX>
+__device__ __forceinline__ void rusanov_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
+                                            const double dF[5], double dPL[5], double dPR[5]) {
+  constexpr int N = AX + 1;
+  const double gamma = fp.gamma;
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, fp.gm1);
+  cons_from_prims(PR, UR, fp.gm1);
+  const double yL = gamma * PL[4] / PL[0], yR = gamma * PR[4] / PR[0];
+  const double cL = sqrt(yL), cR = sqrt(yR);
+  const double aL = fabs(PL[N]) + cL, aR = fabs(PR[N]) + cR;
+  const double alpha = fmax(aL, aR);
+  double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
+  // F = 0.5 (FL + FR) - 0.5 alpha (UR - UL)
+  double g[5];
+  double dalpha = 0.0;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    g[v] = 0.5 * dF[v];
+    dalpha += -0.5 * dF[v] * (UR[v] - UL[v]);
+    dUR[v] += -0.5 * alpha * dF[v];
+    dUL[v] += 0.5 * alpha * dF[v];
+  }
+  physical_flux_vjp<AX>(PL, UL, g, dPL, dUL);
+  physical_flux_vjp<AX>(PR, UR, g, dPR, dUR);
+  const double w = max_weight_a(aL, aR);
+  const double daL = dalpha * w, daR = dalpha * (1.0 - w);
+  dPL[N] += daL * jabs_grad(PL[N]);
+  dPR[N] += daR * jabs_grad(PR[N]);
+  const double dyL = daL * (0.5 / cL), dyR = daR * (0.5 / cR);
+  dPL[0] += -dyL * yL / PL[0];
+  dPR[0] += -dyR * yR / PR[0];
+  dPL[4] += dyL / PL[0] * gamma;
+  dPR[4] += dyR / PR[0] * gamma;
+  cons_from_prims_vjp(PL, dUL, fp.gm1, dPL);
+  cons_from_prims_vjp(PR, dUR, fp.gm1, dPR);
+}
+
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void riemann_flux_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
+                                                 const double dF[5], double dPL[5], double dPR[5]) {
+  if (RIEMANN == GBF_RIEMANN_HLLC)
+    hllc_vjp<AX>(PL, PR, fp, dF, dPL, dPR);
+  else
+    rusanov_vjp<AX>(PL, PR, fp, dF, dPL, dPR);
+}
+
+}  // namespace gbf

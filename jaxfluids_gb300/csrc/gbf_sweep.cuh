@@ -198,20 +198,15 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   }
 }
 
-template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
-__device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
-                                           double* sm_prim, double* sm_flux,
-                                           double (&acc)[MAXC][5], bool first) {
-  constexpr int R = ReconTraits<RECON>::R;
+// Primitives of the pencil box (tile extended by R cells along AX) into
+// shared memory, variable-major: from the halo buffer (MODE_RHS), from the
+// interior primitive buffer (MODE_STAGE_P) or derived from the interior
+// conservatives (MODE_STAGE); boundary conditions by index remapping.
+template <int AX, int R, int MODE>
+__device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3], const int pe[3], int pvol,
+                                             double* sm_prim) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
-
-  // pencil box extents
-  int pe[3] = {ext[0], ext[1], ext[2]};
-  pe[AX] += 2 * R;
-  const int pvol = pe[0] * pe[1] * pe[2];
-
-  // ---- stage the primitives of the pencil box -------------------------
   for (int i = tid; i < pvol; i += nthr) {
     const int i2 = i % pe[2];
     const int r = i / pe[2];
@@ -247,6 +242,22 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_prim[v * pvol + i] = P[v];
   }
+}
+
+template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
+__device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
+                                           double* sm_prim, double* sm_flux,
+                                           double (&acc)[MAXC][5], bool first) {
+  constexpr int R = ReconTraits<RECON>::R;
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+
+  // pencil box extents
+  int pe[3] = {ext[0], ext[1], ext[2]};
+  pe[AX] += 2 * R;
+  const int pvol = pe[0] * pe[1] * pe[2];
+
+  stage_pencil<AX, R, MODE>(p, o, pe, pvol, sm_prim);
   __syncthreads();
 
   // ---- face fluxes, one face per thread --------------------------------

@@ -133,6 +133,25 @@ def _stencil_slice(case: OracleCase, axis: int, k: int, at_center: int = 0) -> T
     return _axis_slice(case, axis, slice(nlo, nhi if nhi != 0 else None))
 
 
+class _JaxAbs(torch.autograd.Function):
+    """|x| with jax's derivative convention: d|x|/dx = +1 at x = 0
+    (jax.lax abs JVP, select(x >= 0, g, -g)); torch's own abs gives 0 there."""
+
+    @staticmethod
+    def forward(ctx, x):
+        ctx.save_for_backward(x)
+        return torch.abs(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        (x,) = ctx.saved_tensors
+        return torch.where(x >= 0, g, -g)
+
+
+def jabs(x: Tensor) -> Tensor:
+    return _JaxAbs.apply(x)
+
+
 # ---------------------------------------------------------------------------
 # Ideal-gas EOS and equation layout
 # ---------------------------------------------------------------------------
@@ -195,7 +214,7 @@ def weno5z_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
     b0 = 13.0 / 12.0 * torch.square(u0 - 2 * u1 + u2) + 1.0 / 4.0 * torch.square(u0 - 4 * u1 + 3 * u2)
     b1 = 13.0 / 12.0 * torch.square(u1 - 2 * u2 + u3) + 1.0 / 4.0 * torch.square(u1 - u3)
     b2 = 13.0 / 12.0 * torch.square(u2 - 2 * u3 + u4) + 1.0 / 4.0 * torch.square(3 * u2 - 4 * u3 + u4)
-    tau5 = torch.abs(b0 - b2)
+    tau5 = jabs(b0 - b2)
     a0 = _WENO_DR[0] * (1.0 + tau5 / (b0 + eps))
     a1 = _WENO_DR[1] * (1.0 + tau5 / (b1 + eps))
     a2 = _WENO_DR[2] * (1.0 + tau5 / (b2 + eps))
@@ -346,7 +365,7 @@ def signal_speeds(name: str, uL, uR, aL, aR, rhoL, rhoR, pL, pR, gamma):
         am = 0.5 * (aL + aR)
         return torch.minimum(um - am, uL - aL), torch.maximum(um + am, uR + aR)
     if name == "RUSANOV":               # :31-49
-        sp = torch.maximum(torch.abs(uL) + aL, torch.abs(uR) + aR)
+        sp = torch.maximum(jabs(uL) + aL, jabs(uR) + aR)
         return -sp, sp
     if name == "TORO":                  # :135-157, :201-231
         rho_bar = 0.5 * (rhoL + rhoR)
@@ -401,7 +420,7 @@ def riemann(PL, PR, UL, UR, case: OracleCase, axis: int) -> Tensor:
         return 0.5 * (1 + sg) * FL + 0.5 * (1 - sg) * FR
     if case.riemann == "RUSANOV":
         # Rusanov.py:25-47
-        alpha = torch.maximum(torch.abs(PL[n]) + cL, torch.abs(PR[n]) + cR)
+        alpha = torch.maximum(jabs(PL[n]) + cL, jabs(PR[n]) + cR)
         FL = fluxes_xi(PL, UL, axis)
         FR = fluxes_xi(PR, UR, axis)
         return 0.5 * (FL + FR) - 0.5 * alpha * (UR - UL)
@@ -607,7 +626,7 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
         if axis not in case.active:
             continue
         btype = case.bc[face]
-        h = P[_face_retrieve_slice(case, face, btype)]
+        h = P[_face_retrieve_slice(case, face, btype)].clone()
         if btype == "ZEROGRADIENT":
             reps = [1] * 4
             reps[axis + 1] = case.nh
@@ -729,6 +748,31 @@ def initialize(prims_interior: Tensor, case: OracleCase, inactive_velocity_eps: 
     U = cons_from_prims(P, case.gamma)
     P, U = halo_update(P, U, case)
     return U, P
+
+
+def buffers_from_interior_cons(Uint: Tensor, case: OracleCase) -> Tuple[Tensor, Tensor]:
+    """Halo buffers (U, P) of an interior conservative state: primitives from
+    the conservatives, halos filled (the state after a stage, simulation_manager.py:943-970)."""
+    P = torch.ones(case.buffer_shape(), dtype=torch.float64) * EPS
+    P = P.clone()
+    P[case.interior()] = prims_from_cons(Uint, case.gamma)
+    U = cons_from_prims(P, case.gamma)
+    U = U.clone()
+    U[case.interior()] = Uint
+    return tuple(reversed(halo_update(P, U, case)))
+
+
+def rhs_of_interior_cons(Uint: Tensor, case: OracleCase) -> Tensor:
+    """compute_rhs as a function of the interior conservatives (for autograd)."""
+    U, P = buffers_from_interior_cons(Uint, case)
+    return compute_rhs(U, P, case)
+
+
+def rk3_step_interior(Uint: Tensor, dt, case: OracleCase) -> Tensor:
+    """One fixed-dt TVD-RK3 step as a function of the interior conservatives."""
+    U, P = buffers_from_interior_cons(Uint, case)
+    U, P = rk3_step(U, P, dt, case)
+    return U[case.interior()]
 
 
 def simulate(U: Tensor, P: Tensor, case: OracleCase, end_time: float = None, end_step: int = None,
