@@ -265,6 +265,70 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def kh_state(n, seed, device):
+    """2-D Kelvin-Helmholtz on [0,1]^2: rho = 2, u = +0.5 for |y - 0.5| < 0.25,
+    else rho = 1, u = -0.5; p = 2.5; v = 0.01 sin(4 pi x) + N(0, 1e-3) noise
+    from default_rng(seed).  Returns interior conservatives [5, n, n, 1]."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    inner = np.abs(Y - 0.5) < 0.25
+    rho = np.where(inner, 2.0, 1.0)
+    u = np.where(inner, 0.5, -0.5)
+    v = 0.01 * np.sin(4 * np.pi * X) + rng.normal(0.0, 1e-3, X.shape)
+    p = np.full_like(X, 2.5)
+    E = p / 0.4 + 0.5 * rho * (u * u + v * v)
+    U = np.stack([rho, rho * u, rho * v, np.zeros_like(rho), E]).reshape(5, n, n, 1)
+    return torch.from_numpy(U).to(device)
+
+
+def run_adjoint(args):
+    """Gradient of 1/2 ||rho(T) - rho_target||^2 w.r.t. the initial state through
+    args.adj_steps fixed-dt RK3 steps (dt = CFL 0.5 step of the initial state),
+    checkpoints every 50 steps; cost relative to the plain forward run."""
+    from jaxfluids_gb300 import CaseConfig, FusedRK3, build
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    build.build()
+    device = torch.device("cuda", 0)
+    n = args.adj_n
+    cfg = CaseConfig(cells=(n, n, 1), bc={f: "PERIODIC" for f in ("east", "west", "north", "south")},
+                     recon="WENO5-Z", riemann="HLLC", signal_speed="EINFELDT", cfl=0.5)
+    U0 = kh_state(n, 7, device)
+    f = FusedRK3(cfg, device)
+    f.set_state(U0)
+    dt = float(f.dt)
+    adj = AdjointRK3(cfg, dt, device)
+    target = adj.advance(kh_state(n, 8, device), args.adj_steps)[0]
+    steps = args.adj_steps
+    adj.advance(U0, 5)  # warm-up
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    UN = adj.advance(U0, steps)
+    b.record()
+    b.synchronize()
+    t_fwd = a.elapsed_time(b) / 1e3
+    adj.forward_steps = 0
+    a.record()
+    UN2, grad = adj.gradient(U0, steps, lambda U: torch.stack([U[0] - target] + [torch.zeros_like(target)] * 4),
+                             schedule=args.adj_schedule, every=args.adj_every)
+    b.record()
+    b.synchronize()
+    t_adj = a.elapsed_time(b) / 1e3
+    # gradient w.r.t. the initial v field: U = cons(P), d(rho v)/dv = rho, dE/dv = rho v
+    rho0 = U0[0]
+    dv = grad[2] * rho0 + grad[4] * U0[2]
+    line = {"metric": "adjoint cost / forward cost, 2-D Kelvin-Helmholtz", "value": t_adj / t_fwd,
+            "unit": "x", "higher_is_better": False, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"KH {n}^2 periodic, {steps} fixed-dt RK3 steps (dt {dt:.4e})",
+                       "schedule": args.adj_schedule, "checkpoint_every": args.adj_every, "cells": n * n},
+            "forward_s": t_fwd, "gradient_s": t_adj, "forward_steps_recomputed": adj.forward_steps,
+            "forward_cell_updates_per_s": n * n * steps / t_fwd,
+            "grad_v_norm": float(dv.norm()), "loss": float(0.5 * ((UN[0] - target) ** 2).sum())}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -273,11 +337,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_TGV)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "batch"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "batch", "adjoint"])
+    ap.add_argument("--adj-n", type=int, default=512)
+    ap.add_argument("--adj-steps", type=int, default=1000)
+    ap.add_argument("--adj-every", type=int, default=50)
+    ap.add_argument("--adj-schedule", default="stored", choices=["stored", "uniform", "binomial"])
     ap.add_argument("--cases", type=int, default=256)
     args = ap.parse_args()
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

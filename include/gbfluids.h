@@ -190,6 +190,11 @@ int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* 
                 const gbf_tile* tile, void* stream);
 int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
                      double* lam_out, void* workspace, const gbf_tile* tile, void* stream);
+/* As gbf_rk3_step_vjp with the stage states U1, U2 of the step given by the
+ * caller (kept from the forward run) instead of recomputed. */
+int gbf_rk3_step_vjp_stages(const gbf_case* c, const double* cons, const double* u1, const double* u2,
+                            const double* dt, const double* lam, double* lam_out, void* workspace,
+                            const gbf_tile* tile, void* stream);
 
 /*
  * Batched fused TVD-RK3 of many independent cases of uneven size sharing one

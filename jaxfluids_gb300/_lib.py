@@ -32,7 +32,7 @@ EXPORTS = (
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
     "gbf_batch_workspace_bytes", "gbf_batch_init", "gbf_batch_advance",
-    "gbf_vjp_workspace_bytes", "gbf_rhs_vjp", "gbf_rk3_step_vjp",
+    "gbf_vjp_workspace_bytes", "gbf_rhs_vjp", "gbf_rk3_step_vjp", "gbf_rk3_step_vjp_stages",
 )
 
 # interior cells the allocation-free entry point's built-in scratch holds
@@ -106,6 +106,7 @@ def load() -> ctypes.CDLL:
         "gbf_vjp_workspace_bytes": (ctypes.c_size_t, [C]),
         "gbf_rhs_vjp": (I, [C, P, P, P, P, T, P]),
         "gbf_rk3_step_vjp": (I, [C, P, P, P, P, P, T, P]),
+        "gbf_rk3_step_vjp_stages": (I, [C, P, P, P, P, P, P, P, T, P]),
         "gbf_batch_init": (I, [C, P, I, P, I, T, P, P, ctypes.c_double, P]),
         "gbf_batch_advance": (I, [C, P, I, P, I, T, I, P, P, P, ctypes.c_int64, I, P]),
     }

@@ -9,6 +9,8 @@ trajectory is replayed from checkpoints kept in device memory:
 * uniform: a checkpoint every ``every`` steps (the reference's
   ``FeedForwardSetup(outer_steps, inner_steps, is_checkpoint_inner_step=True)``);
   each segment is recomputed once and its states kept for the reverse sweep;
+* stored: every state and both stage states of every step are kept (when
+  they fit in device memory), so nothing is recomputed;
 * binomial: at most ``slots`` stored states, split points chosen by dynamic
   programming to minimise recomputed steps (Griewank-style revolve), so long
   trajectories of large grids fit in memory.
@@ -63,6 +65,35 @@ class AdjointRK3:
         _lib.check(self.lib.gbf_rk3_step_vjp(ctypes.byref(self.case), _ptr(U), _ptr(self.dt_dev), _ptr(lam),
                                              _ptr(out), _ptr(self.ws), tile, _stream()), "rk3 step vjp")
         return out
+
+    def step_vjp_stages(self, U: torch.Tensor, U1: torch.Tensor, U2: torch.Tensor, lam: torch.Tensor) -> torch.Tensor:
+        out = torch.empty_like(lam)
+        tile = ctypes.byref(self.tile) if self.tile is not None else None
+        _lib.check(self.lib.gbf_rk3_step_vjp_stages(ctypes.byref(self.case), _ptr(U), _ptr(U1), _ptr(U2),
+                                                    _ptr(self.dt_dev), _ptr(lam), _ptr(out), _ptr(self.ws), tile,
+                                                    _stream()), "rk3 step vjp")
+        return out
+
+    def forward_stored(self, U0: torch.Tensor, nsteps: int):
+        """U_N and every step's (U^n, U1, U2), copied out of the fused stage buffers."""
+        n = self.config.n_cells * 5
+        self.fwd.cons.copy_(U0)
+        self.fwd.dt_state.zero_()
+        self.fwd.dt_state[0] = self.dt
+        store = []
+        for _ in range(nsteps):
+            Un = self.fwd.cons.clone()
+            self.fwd.advance(1)
+            self.forward_steps += 1
+            A = self.fwd.workspace[:n].view_as(Un).clone()
+            B = self.fwd.workspace[n:2 * n].view_as(Un).clone()
+            store.append((Un, A, B))
+        return self.fwd.cons.clone(), store
+
+    def backward_stored(self, store, lam: torch.Tensor) -> torch.Tensor:
+        for Un, U1, U2 in reversed(store):
+            lam = self.step_vjp_stages(Un, U1, U2, lam)
+        return lam
 
     def rhs_vjp(self, U: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
         out = torch.empty_like(w)
@@ -141,6 +172,10 @@ class AdjointRK3:
             UN = self.advance(U0, nsteps)
             lam = loss_grad(UN)
             return UN, self.backward_binomial(U0, nsteps, slots, lam)
+        if schedule == "stored":
+            UN, store = self.forward_stored(U0, nsteps)
+            lam = loss_grad(UN)
+            return UN, self.backward_stored(store, lam)
         raise ValueError(schedule)
 
 

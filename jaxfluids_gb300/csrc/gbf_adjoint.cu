@@ -283,8 +283,9 @@ extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* 
   return launch_rhs_vjp(c, ci, tile, cons, w, out, dP, s);
 }
 
-extern "C" int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
-                                double* lam_out, void* workspace, const gbf_tile* tile, void* stream) {
+static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, const double* u2_in,
+                    const double* dt, const double* lam, double* lam_out, void* workspace, const gbf_tile* tile,
+                    void* stream) {
   int st = gbf_case_check(c);
   if (st != GBF_OK) return st;
   if ((st = vjp_check(c)) != GBF_OK) return st;
@@ -299,27 +300,45 @@ extern "C" int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const dou
   double* lam1 = lam2 + m;
   double* j = lam1 + m;
   double* dP = j + m;
-  // recompute the stage states U1, U2 from U^n with the forward stage kernels
-  SweepParams p;
-  int threads;
-  size_t smem;
-  if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
-  // the forward kernels read dt from dt_state[0]; dt points at a device scalar
-  p.dt_state = const_cast<double*>(dt);
-  p.reduce_dt = 0;
-  p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = U1;
-  if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-  p.stage = 1; p.cons = U1; p.cons0 = cons; p.out = U2;
-  if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+  const double* S1 = u1_in;
+  const double* S2 = u2_in;
+  if (!S1 || !S2) {
+    // recompute the stage states U1, U2 from U^n with the forward stage kernels
+    SweepParams p;
+    int threads;
+    size_t smem;
+    if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
+    // the forward kernels read dt from dt_state[0]; dt points at a device scalar
+    p.dt_state = const_cast<double*>(dt);
+    p.reduce_dt = 0;
+    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = U1;
+    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    p.stage = 1; p.cons = U1; p.cons0 = cons; p.out = U2;
+    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    S1 = U1;
+    S2 = U2;
+  }
   zero_kernel<<<grid_for(m), 256, 0, s>>>(dP, m);
   // stage 3: U3 = 1/3 Un + 2/3 U2 + 2/3 dt L(U2)
-  if ((st = launch_rhs_vjp(c, ci, tile, U2, lam, j, dP, s)) != GBF_OK) return st;
+  if ((st = launch_rhs_vjp(c, ci, tile, S2, lam, j, dP, s)) != GBF_OK) return st;
   axpy_dt_kernel<<<grid_for(m), 256, 0, s>>>(lam2, lam, 2.0 / 3.0, j, 2.0 / 3.0, dt, m);
   // stage 2: U2 = 3/4 Un + 1/4 U1 + 1/4 dt L(U1)
-  if ((st = launch_rhs_vjp(c, ci, tile, U1, lam2, j, dP, s)) != GBF_OK) return st;
+  if ((st = launch_rhs_vjp(c, ci, tile, S1, lam2, j, dP, s)) != GBF_OK) return st;
   axpy_dt_kernel<<<grid_for(m), 256, 0, s>>>(lam1, lam2, 0.25, j, 0.25, dt, m);
   // stage 1: U1 = Un + dt L(Un)
   if ((st = launch_rhs_vjp(c, ci, tile, cons, lam1, j, dP, s)) != GBF_OK) return st;
   step_combine_kernel<<<grid_for(m), 256, 0, s>>>(lam_out, lam, lam2, lam1, j, dt, m);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+extern "C" int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
+                                double* lam_out, void* workspace, const gbf_tile* tile, void* stream) {
+  return step_vjp(c, cons, nullptr, nullptr, dt, lam, lam_out, workspace, tile, stream);
+}
+
+extern "C" int gbf_rk3_step_vjp_stages(const gbf_case* c, const double* cons, const double* u1,
+                                       const double* u2, const double* dt, const double* lam, double* lam_out,
+                                       void* workspace, const gbf_tile* tile, void* stream) {
+  if (!u1 || !u2) return GBF_ERR_INVALID_ARGUMENT;
+  return step_vjp(c, cons, u1, u2, dt, lam, lam_out, workspace, tile, stream);
 }
