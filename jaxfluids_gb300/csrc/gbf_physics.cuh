@@ -41,7 +41,7 @@ __device__ __forceinline__ void cons_from_prims(const double P[5], double U[5], 
   U[1] = rho * P[1];
   U[2] = rho * P[2];
   U[3] = rho * P[3];
-  U[4] = rho * (0.5 * (P[1] * P[1] + P[2] * P[2] + P[3] * P[3]) + e);
+  U[4] = rho * fma(0.5, P[1] * P[1] + P[2] * P[2] + P[3] * P[3], e);  // 0.5 s exact
 }
 
 // equation_manager.py:164-171 (p = (gamma-1) e rho)
@@ -51,7 +51,7 @@ __device__ __forceinline__ void prims_from_cons(const double U[5], double P[5], 
   const double u = U[1] * one_rho;
   const double v = U[2] * one_rho;
   const double w = U[3] * one_rho;
-  const double e = U[4] * one_rho - 0.5 * (u * u + v * v + w * w);
+  const double e = fma(-0.5, u * u + v * v + w * w, U[4] * one_rho);  // 0.5 s exact
   P[0] = rho;
   P[1] = u;
   P[2] = v;
@@ -78,11 +78,15 @@ __device__ __forceinline__ void physical_flux(const double P[5], const double U[
 // WENO5-Z, Borges et al. 2008 (stencils/reconstruction/shock_capturing/weno/weno5_z.py:24-58,
 // weno5_base.py:24-51).  Arguments are (u_imm, u_im, u_i, u_ip, u_ipp) in the
 // reference's slice order; the right state passes the mirrored cells.
+//
+// Products by powers of two (2 u, 4 u, 1/4 t^2) are exact, so fusing them with
+// the following addition (explicit fma) rounds exactly like the reference's
+// separate multiply and add; the build forbids every other contraction.
 __device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
                                          double eps) {
-  const double b0 = (13.0 / 12.0) * sq(u0 - 2.0 * u1 + u2) + 0.25 * sq(u0 - 4.0 * u1 + 3.0 * u2);
-  const double b1 = (13.0 / 12.0) * sq(u1 - 2.0 * u2 + u3) + 0.25 * sq(u1 - u3);
-  const double b2 = (13.0 / 12.0) * sq(u2 - 2.0 * u3 + u4) + 0.25 * sq(3.0 * u2 - 4.0 * u3 + u4);
+  const double b0 = fma(0.25, sq(fma(-4.0, u1, u0) + 3.0 * u2), (13.0 / 12.0) * sq(fma(-2.0, u1, u0) + u2));
+  const double b1 = fma(0.25, sq(u1 - u3), (13.0 / 12.0) * sq(fma(-2.0, u2, u1) + u3));
+  const double b2 = fma(0.25, sq(fma(-4.0, u3, 3.0 * u2) + u4), (13.0 / 12.0) * sq(fma(-2.0, u3, u2) + u4));
   const double tau5 = fabs(b0 - b2);
   const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
   const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
@@ -111,7 +115,7 @@ __device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, dou
   const double dc = (J == 0) ? b2 - b1 : b1 - b2;
   const double du = (J == 0) ? b1 - b0 : b0 - b1;
   const double r = (du >= eps) ? dc / (du + 1e-100) : (dc + eps) / (du + eps);
-  return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : 1.5 * b1 - 0.5 * b0);
+  return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : fma(-0.5, b0, 1.5 * b1));
 }
 
 // Internal reconstruction id: WENO5-Z on Roe-characteristic variables
@@ -340,8 +344,8 @@ __device__ __forceinline__ void hllc_star_flux(const double P[5], const double U
 
 // HLLC._solve_riemann_problem_xi_single_phase (HLLC.py:80-126)
 template <int AX>
-__device__ __forceinline__ void hllc(const double PL[5], const double PR[5], const double UL[5],
-                                     const double UR[5], const FaceParams& fp, double F[5]) {
+__device__ __forceinline__ void hllc(const double PL[5], const double PR[5], const FaceParams& fp,
+                                     double F[5]) {
   constexpr int N = AX + 1;
   const double cL = speed_of_sound(PL[4], PL[0], fp);
   const double cR = speed_of_sound(PR[4], PR[0], fp);
@@ -352,15 +356,31 @@ __device__ __forceinline__ void hllc(const double PL[5], const double PR[5], con
   const double rdL = PL[0] * (SL - PL[N]);
   const double rdR = PR[0] * (SR - PR[N]);
   const double Ss = ((PR[4] - PL[4]) + (PL[N] * rdL - PR[N] * rdR)) / (rdL - rdR);
+  // F = 0.5 (1 + sign S*) F*_L + 0.5 (1 - sign S*) F*_R.  With S* != 0 one
+  // weight is exactly 0 and the other exactly 1, so only the upwind star flux
+  // is formed (a finite F* times 0 adds a signed zero, which changes nothing
+  // downstream); S* = 0 and NaN take the general blend.
+  double UL[5], UR[5];
+  if (Ss > 0.0) {
+    cons_from_prims(PL, UL, fp.gm1);
+    hllc_star_flux<AX, 0>(PL, UL, SL, Ss, F);
+    return;
+  }
+  if (Ss < 0.0) {
+    cons_from_prims(PR, UR, fp.gm1);
+    hllc_star_flux<AX, 1>(PR, UR, SR, Ss, F);
+    return;
+  }
+  cons_from_prims(PL, UL, fp.gm1);
+  cons_from_prims(PR, UR, fp.gm1);
   double FL[5], FR[5];
   hllc_star_flux<AX, 0>(PL, UL, SL, Ss, FL);
   hllc_star_flux<AX, 1>(PR, UR, SR, Ss, FR);
-  // jnp.sign: +1, -1 or 0 (and NaN propagates through both weights)
-  const double sg = (Ss > 0.0) ? 1.0 : ((Ss < 0.0) ? -1.0 : ((Ss == 0.0) ? 0.0 : Ss));
+  const double sg = (Ss == 0.0) ? 0.0 : Ss;  // jnp.sign (NaN propagates)
   const double wl = 0.5 * (1.0 + sg);
   const double wr = 0.5 * (1.0 - sg);
 #pragma unroll
-  for (int v = 0; v < 5; ++v) F[v] = wl * FL[v] + wr * FR[v];
+  for (int v = 0; v < 5; ++v) F[v] = fma(wl, FL[v], wr * FR[v]);  // wl in {0, 1/2, 1}: exact product
 }
 
 // Rusanov._solve_riemann_problem_xi_single_phase (Rusanov.py:25-47)
@@ -375,19 +395,20 @@ __device__ __forceinline__ void rusanov(const double PL[5], const double PR[5], 
   physical_flux<AX>(PL, UL, FL);
   physical_flux<AX>(PR, UR, FR);
 #pragma unroll
-  for (int v = 0; v < 5; ++v) F[v] = 0.5 * (FL[v] + FR[v]) - 0.5 * alpha * (UR[v] - UL[v]);
+  for (int v = 0; v < 5; ++v) F[v] = fma(0.5, FL[v] + FR[v], -(0.5 * alpha * (UR[v] - UL[v])));
 }
 
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux(const double PL[5], const double PR[5],
                                              const FaceParams& fp, double F[5]) {
   double UL[5], UR[5];
-  cons_from_prims(PL, UL, fp.gm1);
-  cons_from_prims(PR, UR, fp.gm1);
-  if (RIEMANN == GBF_RIEMANN_HLLC)
-    hllc<AX>(PL, PR, UL, UR, fp, F);
-  else
+  if (RIEMANN == GBF_RIEMANN_HLLC) {
+    hllc<AX>(PL, PR, fp, F);  // forms the conservatives of the side(s) it uses
+  } else {
+    cons_from_prims(PL, UL, fp.gm1);
+    cons_from_prims(PR, UR, fp.gm1);
     rusanov<AX>(PL, PR, UL, UR, fp, F);
+  }
 }
 
 }  // namespace gbf

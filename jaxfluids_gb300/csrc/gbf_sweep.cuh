@@ -115,7 +115,7 @@ __device__ __forceinline__ double c4_face_deriv(double one_dx, double m2, double
   return one_dx * ((1.0 / 24.0) * (m2 - p1) + (27.0 / 24.0) * (c0 - m1));
 }
 __device__ __forceinline__ double c4_face_interp(double m2, double m1, double c0, double p1) {
-  return (-1.0 / 16.0) * (m2 + p1) + (9.0 / 16.0) * (m1 + c0);
+  return fma(-1.0 / 16.0, m2 + p1, (9.0 / 16.0) * (m1 + c0));  // -1/16 x exact
 }
 
 // Viscous and heat fluxes at the face of axis AX with logical face coordinates
@@ -330,7 +330,7 @@ __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, do
   // then buf += (dt * m) * rhs; kept un-contracted to follow the reference order.
   if (stage == 0) return __dadd_rn(U, __dmul_rn(__dmul_rn(dt, 1.0), rhs));
   if (stage == 1) {
-    const double b = __dadd_rn(__dmul_rn(0.25, U), __dmul_rn(0.75, U0));
+    const double b = fma(0.25, U, __dmul_rn(0.75, U0));  // 0.25 U exact
     return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 0.25), rhs));
   }
   const double b = __dadd_rn(__dmul_rn(2.0 / 3.0, U), __dmul_rn(1.0 / 3.0, U0));
