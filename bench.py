@@ -39,10 +39,10 @@ BYTES_PER_CELL_UPDATE = 320.0
 # FP64 operations per cell-update of the stage kernels (double-precision add,
 # mul and fma thread instructions, fma counted twice) from the ncu capture of
 # the sweep kernel on this workload (summary kept in the profiles directory).
-FP64_FLOP_PER_CELL_UPDATE = 17070.0
+FP64_FLOP_PER_CELL_UPDATE = 15798.0
 # DRAM bytes (read + write) of one stage launch at 128^3 from the same capture
 # (the captured launch is the second RK stage: 120 B/cell algorithmic).
-DRAM_BYTES_PER_LAUNCH = 233.7e6
+DRAM_BYTES_PER_LAUNCH = 235.0e6
 
 
 def tgv_state(n, device, dtype=torch.float64):
@@ -65,6 +65,16 @@ def tgv_config(n):
     return CaseConfig(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=3, gamma=1.4,
                       bc={f: "PERIODIC" for f in ("east", "west", "north", "south", "top", "bottom")},
                       recon="WENO5-Z", riemann="HLLC", signal_speed="EINFELDT", cfl=0.5)
+
+
+def viscous_tgv_config(n):
+    """3-D viscous TGV, Re 1600 (mu = 1/1600 with rho0 = U0 = L = 1), Pr 0.71:
+    WENO5-Z on Roe-characteristic variables + HLLC + CENTRAL4 dissipative fluxes."""
+    from jaxfluids_gb300 import CaseConfig
+    return CaseConfig(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=4, gamma=1.4,
+                      bc={f: "PERIODIC" for f in ("east", "west", "north", "south", "top", "bottom")},
+                      recon="WENO5-Z", recon_var="CHAR-PRIMITIVE", frozen_state="ROE", riemann="HLLC",
+                      signal_speed="EINFELDT", cfl=0.5, viscous=True, heat=True, mu=1.0 / 1600, prandtl=0.71)
 
 
 class ClockSampler:
@@ -335,9 +345,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_TGV)
+    ap.add_argument("--n", type=int, default=None, help="grid side (default 128 inviscid, 256 viscous)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "batch", "adjoint"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "adjoint"])
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=1000)
     ap.add_argument("--adj-every", type=int, default=50)
@@ -367,8 +377,9 @@ def main():
     if world > 1:
         dist.barrier()
     lib = _lib.load()
-    n = args.n
-    cfg = tgv_config(n)
+    viscous = args.workload == "viscous"
+    n = args.n if args.n else (256 if viscous else N_TGV)
+    cfg = viscous_tgv_config(n) if viscous else tgv_config(n)
     cells = n ** 3
     U0 = tgv_state(n, device)
     f = FusedRK3(cfg, device)
@@ -464,17 +475,27 @@ def main():
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"TGV 64^3, 3 RK3 steps ({el:.1f} s), CPU restatement (torch float64)"}
 
+    if viscous:
+        roofline["fp64"]["flop_per_cell_update"] = None
+        roofline["fp64"]["achieved_tflops"] = None
+        roofline["traffic"] = None
+        roofline["kernel"] = "sweep_kernel<WENO5Z-CHAR,HLLC,STAGE_P,VISC> + prims conversion"
     if rank == 0:
+        metric = METRIC if not viscous else \
+            f"FP64 cell-updates/s (viscous TGV {n}^3 Re 1600, WENO5-Z CHAR-ROE+HLLC+CENTRAL4, TVD-RK3)"
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4",
-                       "cells": cells, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5",
+            "config": {"workload": (f"3-D viscous Taylor-Green vortex {n}^3 periodic, Re 1600, Pr 0.71, Ma 0.1"
+                                    if viscous else f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4"),
+                       "cells": cells,
+                       "scheme": ("WENO5-Z CHAR-PRIMITIVE (ROE) + HLLC/Einfeldt + CENTRAL4 viscous/heat, TVD-RK3, CFL 0.5"
+                                  if viscous else "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"),
                        "parallelism": f"replicas x{world}",
                        "l2": "256 MiB buffer written between timed steps (per-step CUDA events)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": 4 * args.steps, "clocks": clocks, "wall_s": wall,
+            "gpu_launches": (7 if viscous else 4) * args.steps, "clocks": clocks, "wall_s": wall,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         }
         print(json.dumps(line), flush=True)
