@@ -30,7 +30,7 @@ struct VjpParams {
 
 template <int AX, int RECON, int RIEMANN>
 __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], const int ext[3],
-                                         double* sm_prim, double* sm_slot) {
+                                         double* sm_prim, double* sm_slot, double* sm_jr) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr int K = 2 * R;
   const SweepParams& p = vp.sp;
@@ -73,23 +73,58 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     }
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
+    if constexpr (RECON == GBF_RECON_WENO5Z) {
+      // one pass gives the face states and the stencil gradients; the left
+      // gradient waits in the face's slots 0..4, the right one in this
+      // thread's private rows, until the Riemann cotangents are known
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      double wv[K];
+      for (int v = 0; v < 5; ++v) {
+        double wv[K], jl[5], jr[5];
 #pragma unroll
-      for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
-      reconstruct_pair<RECON>(wv, p.fp.stencil_eps, PL[v], PR[v]);
-    }
-    double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-    riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
+        weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      double wv[K], dw[K];
+        for (int k = 0; k < 5; ++k) {
+          sm_slot[(v * K + k) * fvol + f] = jl[k];
+          sm_jr[(v * 5 + k) * nthr + tid] = jr[k];
+        }
+      }
+      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
 #pragma unroll
-      for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
-      reconstruct_pair_vjp<RECON>(wv, p.fp.stencil_eps, dPL[v], dPR[v], dw);
+      for (int v = 0; v < 5; ++v) {
+        const double gL = dPL[v], gR = dPR[v];
+        double jl[5], jr[5];
 #pragma unroll
-      for (int k = 0; k < K; ++k) sm_slot[(v * K + k) * fvol + f] = dw[k];
+        for (int k = 0; k < 5; ++k) {
+          jl[k] = sm_slot[(v * K + k) * fvol + f];
+          jr[k] = sm_jr[(v * 5 + k) * nthr + tid];
+        }
+        sm_slot[(v * K + 0) * fvol + f] = gL * jl[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) sm_slot[(v * K + k) * fvol + f] = gL * jl[k] + gR * jr[5 - k];
+        sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        reconstruct_pair<RECON>(wv, p.fp.stencil_eps, PL[v], PR[v]);
+      }
+      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K], dw[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        reconstruct_pair_vjp<RECON>(wv, p.fp.stencil_eps, dPL[v], dPR[v], dw);
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm_slot[(v * K + k) * fvol + f] = dw[k];
+      }
     }
   }
   __syncthreads();
@@ -146,11 +181,13 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
     if (p.active_mask & (1 << a))
       pmax = max(pmax, (p.t[0] + (a == 0 ? 2 * R : 0)) * (p.t[1] + (a == 1 ? 2 * R : 0)) *
                            (p.t[2] + (a == 2 ? 2 * R : 0)));
+  // pencil primitives | per-thread right-stencil gradients (WENO only) | face slots
   double* sm_prim = smem;
-  double* sm_slot = smem + 5 * pmax;
-  if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot);
-  if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot);
-  if (p.active_mask & 4) vjp_axis<2, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot);
+  double* sm_jr = smem + 5 * pmax;
+  double* sm_slot = sm_jr + ((RECON == GBF_RECON_WENO5Z) ? 25 * blockDim.x : 0);
+  if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+  if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+  if (p.active_mask & 4) vjp_axis<2, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
 }
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
@@ -217,9 +254,8 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   int st = make_sweep_params(c, ci, tile, &vp.sp, &threads, &smem);
   if (st != GBF_OK) return st;
   const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
-  // shared memory: pencil primitives + 2R x 5 slots per face (replaces the flux slots)
-  const size_t pbytes = smem - 0;  // computed below
-  (void)pbytes;
+  // shared memory: pencil primitives + 2R x 5 slots per face (replaces the
+  // flux slots) + 25 doubles per thread for WENO's right-stencil gradients
   long long pmax = 0, fmax = 0;
   for (int a = 0; a < 3; ++a) {
     if (!(ci.active_mask & (1 << a))) continue;
@@ -231,7 +267,7 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     pmax = std::max(pmax, pv);
     fmax = std::max(fmax, fv);
   }
-  smem = (size_t)(5 * pmax + 10 * R * fmax) * sizeof(double);
+  smem = (size_t)(5 * pmax + 10 * R * fmax + (R == 3 ? 25 * threads : 0)) * sizeof(double);
   if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
   vp.sp.cons = U;
   vp.w = w;

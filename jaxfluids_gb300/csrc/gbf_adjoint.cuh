@@ -23,9 +23,13 @@ __device__ __forceinline__ double max_weight_a(double a, double b) {
   return (a > b) ? 1.0 : ((a == b) ? 0.5 : 0.0);
 }
 
-// Reverse of weno5z(u0..u4): du[k] += g * d out / d u_k.
-__device__ __forceinline__ void weno5z_vjp(double u0, double u1, double u2, double u3, double u4,
-                                           double eps, double g, double du[5]) {
+// weno5z(u0..u4) and its gradient J[k] = d out / d u_k (the reverse pass with
+// unit cotangent), so a caller can scale J by the cotangent once it is known
+// without recomputing the stencil.  One reciprocal per denominator serves the
+// forward ratios and the reverse pass (4 divisions instead of 10); values
+// differ from the forward's divisions at rounding level only.
+__device__ __forceinline__ void weno5z_jac(double u0, double u1, double u2, double u3, double u4,
+                                           double eps, double& out, double J[5]) {
   constexpr double c13 = 13.0 / 12.0;
   const double t0 = u0 - 2.0 * u1 + u2;
   const double t1 = u0 - 4.0 * u1 + 3.0 * u2;
@@ -37,44 +41,39 @@ __device__ __forceinline__ void weno5z_vjp(double u0, double u1, double u2, doub
   const double b1 = c13 * (t2 * t2) + 0.25 * (t3 * t3);
   const double b2 = c13 * (t4 * t4) + 0.25 * (t5 * t5);
   const double tau = fabs(b0 - b2);
-  const double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
-  const double q0 = tau / e0, q1 = tau / e1, q2 = tau / e2;
+  const double ie0 = 1.0 / (b0 + eps), ie1 = 1.0 / (b1 + eps), ie2 = 1.0 / (b2 + eps);
+  const double q0 = tau * ie0, q1 = tau * ie1, q2 = tau * ie2;
   const double a0 = 0.1 * (1.0 + q0), a1 = 0.6 * (1.0 + q1), a2 = 0.3 * (1.0 + q2);
   const double r = 1.0 / (a0 + a1 + a2);
   const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
   const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
   const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  // out = (a0 p0 + a1 p1 + a2 p2) r = w0 p0 + w1 p1 + w2 p2
   const double w0 = a0 * r, w1 = a1 * r, w2 = a2 * r;
-  // out = w0 p0 + w1 p1 + w2 p2
-  const double dw0 = g * p0, dw1 = g * p1, dw2 = g * p2;
-  const double dp0 = g * w0, dp1 = g * w1, dp2 = g * w2;
-  du[0] += (1.0 / 3.0) * dp0;
-  du[1] += (-7.0 / 6.0) * dp0 + (-1.0 / 6.0) * dp1;
-  du[2] += (11.0 / 6.0) * dp0 + (5.0 / 6.0) * dp1 + (1.0 / 3.0) * dp2;
-  du[3] += (1.0 / 3.0) * dp1 + (5.0 / 6.0) * dp2;
-  du[4] += (-1.0 / 6.0) * dp2;
-  // w_k = a_k r, r = 1 / S
-  const double dr = dw0 * a0 + dw1 * a1 + dw2 * a2;
-  const double dS = -dr * r * r;
-  const double da0 = dw0 * r + dS, da1 = dw1 * r + dS, da2 = dw2 * r + dS;
-  // a_k = d_k (1 + q_k), q_k = tau / e_k
-  const double dq0 = 0.1 * da0, dq1 = 0.6 * da1, dq2 = 0.3 * da2;
-  const double dtau = dq0 / e0 + dq1 / e1 + dq2 / e2;
-  double db0 = -dq0 * q0 / e0;
-  const double db1 = -dq1 * q1 / e1;
-  double db2 = -dq2 * q2 / e2;
+  out = w0 * p0 + w1 * p1 + w2 * p2;
+  J[0] = (1.0 / 3.0) * w0;
+  J[1] = (-7.0 / 6.0) * w0 + (-1.0 / 6.0) * w1;
+  J[2] = (11.0 / 6.0) * w0 + (5.0 / 6.0) * w1 + (1.0 / 3.0) * w2;
+  J[3] = (1.0 / 3.0) * w1 + (5.0 / 6.0) * w2;
+  J[4] = (-1.0 / 6.0) * w2;
+  // d out / d a_k = r (p_k - out)
+  const double da0 = r * (p0 - out), da1 = r * (p1 - out), da2 = r * (p2 - out);
+  const double dq0 = 0.1 * da0 * ie0, dq1 = 0.6 * da1 * ie1, dq2 = 0.3 * da2 * ie2;
+  const double dtau = dq0 + dq1 + dq2;
+  double db0 = -dq0 * q0;
+  const double db1 = -dq1 * q1;
+  double db2 = -dq2 * q2;
   const double sg = jabs_grad(b0 - b2);
   db0 += dtau * sg;
   db2 -= dtau * sg;
-  // b = c13 t^2 + 1/4 t'^2
-  const double dt0 = db0 * c13 * 2.0 * t0, dt1 = db0 * 0.5 * t1;
-  const double dt2 = db1 * c13 * 2.0 * t2, dt3 = db1 * 0.5 * t3;
-  const double dt4 = db2 * c13 * 2.0 * t4, dt5 = db2 * 0.5 * t5;
-  du[0] += dt0 + dt1;
-  du[1] += -2.0 * dt0 - 4.0 * dt1 + dt2 + dt3;
-  du[2] += dt0 + 3.0 * dt1 - 2.0 * dt2 + dt4 + 3.0 * dt5;
-  du[3] += dt2 - dt3 - 2.0 * dt4 - 4.0 * dt5;
-  du[4] += dt4 + dt5;
+  const double dt0 = db0 * (2.0 * c13) * t0, dt1 = db0 * 0.5 * t1;
+  const double dt2 = db1 * (2.0 * c13) * t2, dt3 = db1 * 0.5 * t3;
+  const double dt4 = db2 * (2.0 * c13) * t4, dt5 = db2 * 0.5 * t5;
+  J[0] += dt0 + dt1;
+  J[1] += -2.0 * dt0 - 4.0 * dt1 + dt2 + dt3;
+  J[2] += dt0 + 3.0 * dt1 - 2.0 * dt2 + dt4 + 3.0 * dt5;
+  J[3] += dt2 - dt3 - 2.0 * dt4 - 4.0 * dt5;
+  J[4] += dt4 + dt5;
 }
 
 // Reverse of minmod_ad<J>(b0, b1, b2): the ratio only selects a branch.
@@ -102,15 +101,13 @@ __device__ __forceinline__ void reconstruct_pair_vjp(const double* w, double eps
 template <>
 __device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5Z>(const double* w, double eps,
                                                                         double gL, double gR, double* dw) {
-  double dl[5] = {0, 0, 0, 0, 0}, dr[5] = {0, 0, 0, 0, 0};
-  weno5z_vjp(w[0], w[1], w[2], w[3], w[4], eps, gL, dl);
-  weno5z_vjp(w[5], w[4], w[3], w[2], w[1], eps, gR, dr);
-  dw[0] = dl[0];
-  dw[1] = dl[1] + dr[4];
-  dw[2] = dl[2] + dr[3];
-  dw[3] = dl[3] + dr[2];
-  dw[4] = dl[4] + dr[1];
-  dw[5] = dr[0];
+  double jl[5], jr[5], vl, vr;
+  weno5z_jac(w[0], w[1], w[2], w[3], w[4], eps, vl, jl);
+  weno5z_jac(w[5], w[4], w[3], w[2], w[1], eps, vr, jr);
+  dw[0] = gL * jl[0];
+#pragma unroll
+  for (int k = 1; k < 5; ++k) dw[k] = gL * jl[k] + gR * jr[5 - k];
+  dw[5] = gR * jr[0];
 }
 
 template <>
@@ -125,23 +122,46 @@ __device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_MINMOD_AD>(const 
   dw[3] = d[3];
 }
 
+// Face states and their reciprocals, shared by the forward recomputation and
+// the reverse pass of a Riemann solver: U = cons(P) with e = p / (rho gm1)
+// formed as p (1/rho)(1/gm1), and c = sqrt(gamma p / rho) with 1/c from one
+// rsqrt.  Results differ from the forward's divisions at rounding level only.
+struct FaceSide {
+  double U[5];
+  double ir;   // 1 / rho
+  double y;    // gamma p / rho
+  double c;    // speed of sound
+  double ic;   // 1 / c
+};
+
+__device__ __forceinline__ void face_side(const double P[5], double gamma, double igm1, FaceSide& s) {
+  s.ir = 1.0 / P[0];
+  const double e = P[4] * s.ir * igm1;
+  s.U[0] = P[0];
+  s.U[1] = P[0] * P[1];
+  s.U[2] = P[0] * P[2];
+  s.U[3] = P[0] * P[3];
+  s.U[4] = P[0] * (0.5 * (P[1] * P[1] + P[2] * P[2] + P[3] * P[3]) + e);
+  s.y = gamma * P[4] * s.ir;
+  s.ic = rsqrt(s.y);
+  s.c = s.y * s.ic;
+}
+
 // Reverse of cons_from_prims: dP += (dU/dP)^T dU.
-__device__ __forceinline__ void cons_from_prims_vjp(const double P[5], const double dU[5], double gm1,
-                                                    double dP[5]) {
+__device__ __forceinline__ void cons_from_prims_vjp(const double P[5], const double dU[5], double ir,
+                                                    double igm1, double dP[5]) {
   const double rho = P[0];
-  const double den = rho * gm1;
-  const double e = P[4] / den;
+  const double e = P[4] * ir * igm1;
   const double s = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
   const double h = 0.5 * s + e;
   // U0 = rho, Ui = rho Pi, U4 = rho h
   double drho = dU[0] + dU[1] * P[1] + dU[2] * P[2] + dU[3] * P[3] + dU[4] * h;
   const double dh = dU[4] * rho;
-  const double ds = 0.5 * dh;
 #pragma unroll
-  for (int i = 1; i <= 3; ++i) dP[i] += dU[i] * rho + ds * 2.0 * P[i];
-  // e = P4 / (rho gm1)
-  dP[4] += dh / den;
-  drho += -dh * e / den * gm1;
+  for (int i = 1; i <= 3; ++i) dP[i] += dU[i] * rho + dh * P[i];
+  // e = P4 / (rho gm1): de/dP4 = 1/(rho gm1), de/drho = -e/rho
+  dP[4] += dh * ir * igm1;
+  drho -= dh * e * ir;
   dP[0] += drho;
 }
 
@@ -185,9 +205,9 @@ __device__ __forceinline__ void physical_flux_vjp(const double P[5], const doubl
 }
 
 // Reverse of hllc_star_flux<AX, J> (HLLC.py:41-78).  Accumulates into dP, dU,
-// dS (own wave speed) and dSs (contact speed).
+// dS (own wave speed) and dSs (contact speed); ir = 1/rho of this side.
 template <int AX, int J>
-__device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const double U[5], double S,
+__device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const double U[5], double ir, double S,
                                                    double Ss, const double dF[5], double dP[5], double dU[5],
                                                    double& dS, double& dSs) {
   constexpr int N = AX + 1;
@@ -195,11 +215,12 @@ __device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const doub
   constexpr int T2 = (AX == 2) ? 2 : 3;
   const double n1 = S - P[N];
   const double d1 = S - Ss;
-  const double m = n1 / d1;
+  const double in1 = 1.0 / n1, id1 = 1.0 / d1;
+  const double m = n1 * id1;
   const double pre = m * P[0];
-  const double A = U[4] / U[0];
-  const double q = P[4] / P[0];
-  const double D = q / n1;
+  const double A = U[4] * ir;
+  const double q = P[4] * ir;
+  const double D = q * in1;
   const double B = Ss - P[N];
   const double C = Ss + D;
   const double X = A + B * C;
@@ -221,27 +242,27 @@ __device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const doub
   }
   dS += dwave * ((J == 0) ? min_weight_a(S, 0.0) : max_weight_a(S, 0.0));
   // us components
-  double dpre = dus[0] + dus[N] * Ss + dus[T1] * P[T1] + dus[T2] * P[T2] + dus[4] * X;
+  const double dpre = dus[0] + dus[N] * Ss + dus[T1] * P[T1] + dus[T2] * P[T2] + dus[4] * X;
   dSs += dus[N] * pre;
   dP[T1] += dus[T1] * pre;
   dP[T2] += dus[T2] * pre;
   const double dX = dus[4] * pre;
-  // X = A + B C
-  dU[4] += dX / U[0];
-  dU[0] += -dX * A / U[0];
+  // X = A + B C, A = U4 / U0
+  dU[4] += dX * ir;
+  dU[0] -= dX * A * ir;
   const double dB = dX * C, dC = dX * B;
   dSs += dB + dC;
   double du = -dB;
-  // D = q / n1
-  const double dq = dC / n1;
-  double dn1 = -dC * D / n1;
-  dP[4] += dq / P[0];
-  dP[0] += -dq * q / P[0];
+  // D = q / n1, q = P4 / P0
+  const double dq = dC * in1;
+  double dn1 = -dC * D * in1;
+  dP[4] += dq * ir;
+  dP[0] -= dq * q * ir;
   // pre = m rho, m = n1 / d1
   const double dm = dpre * P[0];
   dP[0] += dpre * m;
-  dn1 += dm / d1;
-  const double dd1 = -dm * m / d1;
+  dn1 += dm * id1;
+  const double dd1 = -dm * m * id1;
   dS += dn1 + dd1;
   du -= dn1;
   dSs -= dd1;
@@ -256,26 +277,29 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
                                          const double dF[5], double dPL[5], double dPR[5]) {
   constexpr int N = AX + 1;
   const double gamma = fp.gamma;
-  double UL[5], UR[5];
-  cons_from_prims(PL, UL, fp.gm1);
-  cons_from_prims(PR, UR, fp.gm1);
+  const double igm1 = 1.0 / fp.gm1;
+  FaceSide L, R;
+  face_side(PL, gamma, igm1, L);
+  face_side(PR, gamma, igm1, R);
   const double uL = PL[N], uR = PR[N], rL = PL[0], rR = PR[0], pL = PL[4], pR = PR[4];
-  const double yL = gamma * pL / rL, yR = gamma * pR / rR;
-  const double cL = sqrt(yL), cR = sqrt(yR);
-  const double sL = sqrt(rL), sR = sqrt(rR);
+  const double cL = L.c, cR = R.c;
+  const double isL = rsqrt(rL), isR = rsqrt(rR);
+  const double sL = rL * isL, sR = rR * isR;
   const double od = 1.0 / (sL + sR);
   const double eta2 = 0.5 * sL * sR * od * od;
   const double ubar = (sL * uL + sR * uR) * od;
   const double duu = uR - uL;
   const double Wn = sL * cL * cL + sR * cR * cR;
   const double Z = Wn * od + eta2 * (duu * duu);
-  const double dbar = sqrt(Z);
+  const double idbar = rsqrt(Z);
+  const double dbar = Z * idbar;
   const double X1 = ubar - dbar, X2 = uL - cL, Y1 = ubar + dbar, Y2 = uR + cR;
   const double SL = fmin(X1, X2), SR = fmax(Y1, Y2);
   const double rdL = rL * (SL - uL), rdR = rR * (SR - uR);
   const double num = (pR - pL) + (uL * rdL - uR * rdR);
   const double den = rdL - rdR;
-  const double Ss = num / den;
+  const double iden = 1.0 / den;
+  const double Ss = num * iden;
   const double sg = (Ss > 0.0) ? 1.0 : ((Ss < 0.0) ? -1.0 : 0.0);
   const double wl = 0.5 * (1.0 + sg), wr = 0.5 * (1.0 - sg);
   double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
@@ -284,17 +308,17 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
     double g[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) g[v] = wl * dF[v];
-    hllc_star_flux_vjp<AX, 0>(PL, UL, SL, Ss, g, dPL, dUL, dSL, dSs);
+    hllc_star_flux_vjp<AX, 0>(PL, L.U, L.ir, SL, Ss, g, dPL, dUL, dSL, dSs);
   }
   if (wr != 0.0) {
     double g[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) g[v] = wr * dF[v];
-    hllc_star_flux_vjp<AX, 1>(PR, UR, SR, Ss, g, dPR, dUR, dSR, dSs);
+    hllc_star_flux_vjp<AX, 1>(PR, R.U, R.ir, SR, Ss, g, dPR, dUR, dSR, dSs);
   }
   // Ss = num / den
-  const double dnum = dSs / den;
-  const double dden = -dSs * Ss / den;
+  const double dnum = dSs * iden;
+  const double dden = -dSs * Ss * iden;
   dPR[4] += dnum;
   dPL[4] -= dnum;
   double duL = dnum * rdL, duR = -dnum * rdR;
@@ -316,7 +340,7 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   duR += dY2;
   double dcR = dY2;
   // dbar = sqrt(Z), Z = Wn od + eta2 du^2
-  const double dZ = ddbar * (0.5 / dbar);
+  const double dZ = ddbar * 0.5 * idbar;
   const double dWn = dZ * od;
   double dod = dZ * Wn;
   const double deta2 = dZ * (duu * duu);
@@ -327,9 +351,10 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   dcL += dWn * sL * 2.0 * cL;
   dcR += dWn * sR * 2.0 * cR;
   // eta2 = 0.5 sL sR od od
-  dsL += deta2 * 0.5 * sR * od * od;
-  dsR += deta2 * 0.5 * sL * od * od;
-  dod += deta2 * 0.5 * sL * sR * 2.0 * od;
+  const double od2 = od * od;
+  dsL += deta2 * 0.5 * sR * od2;
+  dsR += deta2 * 0.5 * sL * od2;
+  dod += deta2 * sL * sR * od;
   // ubar = (sL uL + sR uR) od
   dsL += dubar * uL * od;
   dsR += dubar * uR * od;
@@ -337,24 +362,24 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   duR += dubar * sR * od;
   dod += dubar * (sL * uL + sR * uR);
   // od = 1 / (sL + sR)
-  const double dsum = -dod * od * od;
+  const double dsum = -dod * od2;
   dsL += dsum;
   dsR += dsum;
-  drL += dsL * (0.5 / sL);
-  drR += dsR * (0.5 / sR);
+  drL += dsL * 0.5 * isL;
+  drR += dsR * 0.5 * isR;
   // c = sqrt(y), y = gamma p / rho
-  const double dyL = dcL * (0.5 / cL), dyR = dcR * (0.5 / cR);
-  drL += -dyL * yL / rL;
-  drR += -dyR * yR / rR;
-  dPL[4] += dyL / rL * gamma;
-  dPR[4] += dyR / rR * gamma;
+  const double dyL = dcL * 0.5 * L.ic, dyR = dcR * 0.5 * R.ic;
+  drL -= dyL * L.y * L.ir;
+  drR -= dyR * R.y * R.ir;
+  dPL[4] += dyL * L.ir * gamma;
+  dPR[4] += dyR * R.ir * gamma;
   dPL[0] += drL;
   dPR[0] += drR;
   dPL[N] += duL;
   dPR[N] += duR;
   // U = cons(P)
-  cons_from_prims_vjp(PL, dUL, fp.gm1, dPL);
-  cons_from_prims_vjp(PR, dUR, fp.gm1, dPR);
+  cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
+  cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
 
 // Reverse of rusanov<AX> (Rusanov.py:25-47).
@@ -363,12 +388,11 @@ __device__ __forceinline__ void rusanov_vjp(const double PL[5], const double PR[
                                             const double dF[5], double dPL[5], double dPR[5]) {
   constexpr int N = AX + 1;
   const double gamma = fp.gamma;
-  double UL[5], UR[5];
-  cons_from_prims(PL, UL, fp.gm1);
-  cons_from_prims(PR, UR, fp.gm1);
-  const double yL = gamma * PL[4] / PL[0], yR = gamma * PR[4] / PR[0];
-  const double cL = sqrt(yL), cR = sqrt(yR);
-  const double aL = fabs(PL[N]) + cL, aR = fabs(PR[N]) + cR;
+  const double igm1 = 1.0 / fp.gm1;
+  FaceSide L, R;
+  face_side(PL, gamma, igm1, L);
+  face_side(PR, gamma, igm1, R);
+  const double aL = fabs(PL[N]) + L.c, aR = fabs(PR[N]) + R.c;
   const double alpha = fmax(aL, aR);
   double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
   // F = 0.5 (FL + FR) - 0.5 alpha (UR - UL)
@@ -377,23 +401,23 @@ __device__ __forceinline__ void rusanov_vjp(const double PL[5], const double PR[
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     g[v] = 0.5 * dF[v];
-    dalpha += -0.5 * dF[v] * (UR[v] - UL[v]);
+    dalpha += -0.5 * dF[v] * (R.U[v] - L.U[v]);
     dUR[v] += -0.5 * alpha * dF[v];
     dUL[v] += 0.5 * alpha * dF[v];
   }
-  physical_flux_vjp<AX>(PL, UL, g, dPL, dUL);
-  physical_flux_vjp<AX>(PR, UR, g, dPR, dUR);
+  physical_flux_vjp<AX>(PL, L.U, g, dPL, dUL);
+  physical_flux_vjp<AX>(PR, R.U, g, dPR, dUR);
   const double w = max_weight_a(aL, aR);
   const double daL = dalpha * w, daR = dalpha * (1.0 - w);
   dPL[N] += daL * jabs_grad(PL[N]);
   dPR[N] += daR * jabs_grad(PR[N]);
-  const double dyL = daL * (0.5 / cL), dyR = daR * (0.5 / cR);
-  dPL[0] += -dyL * yL / PL[0];
-  dPR[0] += -dyR * yR / PR[0];
-  dPL[4] += dyL / PL[0] * gamma;
-  dPR[4] += dyR / PR[0] * gamma;
-  cons_from_prims_vjp(PL, dUL, fp.gm1, dPL);
-  cons_from_prims_vjp(PR, dUR, fp.gm1, dPR);
+  const double dyL = daL * 0.5 * L.ic, dyR = daR * 0.5 * R.ic;
+  dPL[0] -= dyL * L.y * L.ir;
+  dPR[0] -= dyR * R.y * R.ir;
+  dPL[4] += dyL * L.ir * gamma;
+  dPR[4] += dyR * R.ir * gamma;
+  cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
+  cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
 
 template <int AX, int RIEMANN>
