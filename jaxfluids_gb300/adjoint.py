@@ -116,10 +116,20 @@ class AdjointRK3:
         return U, ckpt
 
     def backward_uniform(self, ckpt: Dict[int, torch.Tensor], nsteps: int, every: int,
-                         lam: torch.Tensor) -> torch.Tensor:
+                         lam: torch.Tensor, keep_stages: bool = True) -> torch.Tensor:
+        """Reverse sweep over the uniform checkpoints.  Each segment is replayed
+        once from its checkpoint; with keep_stages the replay keeps both stage
+        states of every step (3 states per step of the segment) so the step
+        VJPs recompute nothing, otherwise it keeps one state per step and each
+        step VJP recomputes its two stage states."""
         starts = sorted(s for s in ckpt if s < nsteps)
         for s in reversed(starts):
             m = min(every, nsteps - s)
+            if keep_stages:
+                _, store = self.forward_stored(ckpt[s], m)
+                lam = self.backward_stored(store, lam)
+                del store
+                continue
             states = [ckpt[s]]
             for _ in range(m - 1):
                 states.append(self.advance(states[-1], 1))
@@ -162,12 +172,12 @@ class AdjointRK3:
 
     # ---- gradient -----------------------------------------------------------
     def gradient(self, U0: torch.Tensor, nsteps: int, loss_grad: Callable[[torch.Tensor], torch.Tensor],
-                 schedule: str = "uniform", every: int = 50, slots: int = 8):
+                 schedule: str = "uniform", every: int = 50, slots: int = 8, keep_stages: bool = True):
         """(U_N, dL/dU_0) for a loss whose gradient w.r.t. U_N is loss_grad(U_N)."""
         if schedule == "uniform":
             UN, ckpt = self.forward_uniform(U0, nsteps, every)
             lam = loss_grad(UN)
-            return UN, self.backward_uniform(ckpt, nsteps, every, lam)
+            return UN, self.backward_uniform(ckpt, nsteps, every, lam, keep_stages)
         if schedule == "binomial":
             UN = self.advance(U0, nsteps)
             lam = loss_grad(UN)

@@ -28,6 +28,129 @@ struct VjpParams {
   double* dP;           // primitive cotangent accumulator, interior [5][N]
 };
 
+// CHAR-PRIMITIVE face (char_reconstruct of the forward): frozen state of the
+// two cells adjacent to the face, characteristic variables of the six window
+// cells, WENO5-Z with its gradients on each, back-projection, Riemann VJP, and
+// the reverse of all of it onto the window cells' primitives.  win points at
+// window cell 0 of variable 0 in the staged pencil (variable stride pvol, cell
+// stride ps); slot(v, k) = slot[(v * 6 + k) * fvol] receives the cotangent of
+// primitive v of window cell k; jr is this thread's private row block.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void char_face_vjp(const FaceParams& fp, const double* win, int pvol, int ps,
+                                              const double dF[5], double* slot, int fvol, double* jr_rows,
+                                              int nthr) {
+  constexpr int N = AX + 1;
+  using I = CharIds<AX>;
+  auto x = [&](int v, int k) { return win[v * pvol + k * ps]; };
+  auto SL = [&](int j, int k) -> double& { return slot[(j * 6 + k) * fvol]; };
+  auto JR = [&](int j, int i) -> double& { return jr_rows[(j * 5 + i) * nthr]; };
+  double Lc[5], Rc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    Lc[v] = x(v, 2);
+    Rc[v] = x(v, 3);
+  }
+  double rho_a, c, cc;
+  frozen_state(Lc, Rc, fp, rho_a, c, cc);
+  const double ic = 1.0 / c;
+  const double k_m = -0.5 * ic, k_p = 0.5 * ic;
+  const double k_e = 0.5 / (cc * rho_a);
+  const double k_s = 1.0 / cc;
+  const double eps = fp.stencil_eps;
+  // characteristic face values cL[j], cR[j]; gradients of char var j: left in
+  // slot(j, 0..4), right in the private rows
+  double cL[5], cR[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    double ch[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      if (j == 0) ch[k] = k_m * x(N, k) + k_e * x(4, k);
+      else if (j == 1) ch[k] = x(0, k) - k_s * x(4, k);
+      else if (j == 4) ch[k] = k_p * x(N, k) + k_e * x(4, k);
+      else ch[k] = x(j == I::e0 ? I::m0 : I::m1, k);
+    }
+    double jl[5], jr[5];
+    weno5z_jac(ch[0], ch[1], ch[2], ch[3], ch[4], eps, cL[j], jl);
+    weno5z_jac(ch[5], ch[4], ch[3], ch[2], ch[1], eps, cR[j], jr);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      SL(j, k) = jl[k];
+      JR(j, k) = jr[k];
+    }
+  }
+  double PL[5], PR[5];
+  PL[0] = rho_a * (cL[0] + cL[4]) + cL[1];
+  PL[N] = c * (-cL[0] + cL[4]);
+  PL[I::m0] = cL[I::e0];
+  PL[I::m1] = cL[I::e1];
+  PL[4] = cc * rho_a * (cL[0] + cL[4]);
+  PR[0] = rho_a * (cR[0] + cR[4]) + cR[1];
+  PR[N] = c * (-cR[0] + cR[4]);
+  PR[I::m0] = cR[I::e0];
+  PR[I::m1] = cR[I::e1];
+  PR[4] = cc * rho_a * (cR[0] + cR[4]);
+  double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+  riemann_flux_vjp<AX, RIEMANN>(PL, PR, fp, dF, dPL, dPR);
+  // back-projection reverse
+  double drho_a = 0.0, dc = 0.0, dcc = 0.0;
+  double gL[5], gR[5];
+  {
+    const double sL4 = cL[0] + cL[4], sR4 = cR[0] + cR[4];
+    const double ccr = cc * rho_a;
+    gL[0] = rho_a * dPL[0] - c * dPL[N] + ccr * dPL[4];
+    gL[4] = rho_a * dPL[0] + c * dPL[N] + ccr * dPL[4];
+    gL[1] = dPL[0];
+    gL[I::e0] = dPL[I::m0];
+    gL[I::e1] = dPL[I::m1];
+    gR[0] = rho_a * dPR[0] - c * dPR[N] + ccr * dPR[4];
+    gR[4] = rho_a * dPR[0] + c * dPR[N] + ccr * dPR[4];
+    gR[1] = dPR[0];
+    gR[I::e0] = dPR[I::m0];
+    gR[I::e1] = dPR[I::m1];
+    drho_a = (dPL[0] + cc * dPL[4]) * sL4 + (dPR[0] + cc * dPR[4]) * sR4;
+    dc = dPL[N] * (cL[4] - cL[0]) + dPR[N] * (cR[4] - cR[0]);
+    dcc = dPL[4] * rho_a * sL4 + dPR[4] * rho_a * sR4;
+  }
+  // per window cell: cotangents of the char variables, then of the primitives
+  double dk_m = 0.0, dk_p = 0.0, dk_e = 0.0, dk_s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double dch[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      double d = (k <= 4) ? gL[j] * SL(j, k) : 0.0;
+      if (k >= 1) d += gR[j] * JR(j, 5 - k);
+      dch[j] = d;
+    }
+    const double xn = x(N, k), x4 = x(4, k);
+    dk_m += dch[0] * xn;
+    dk_p += dch[4] * xn;
+    dk_e += (dch[0] + dch[4]) * x4;
+    dk_s -= dch[1] * x4;
+    double dx[5];
+    dx[0] = dch[1];
+    dx[N] = k_m * dch[0] + k_p * dch[4];
+    dx[4] = k_e * (dch[0] + dch[4]) - k_s * dch[1];
+    dx[I::m0] = dch[I::e0];
+    dx[I::m1] = dch[I::e1];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) SL(v, k) = dx[v];
+  }
+  // k_m = -0.5/c, k_p = 0.5/c, k_e = 0.5/(cc rho_a), k_s = 1/cc
+  dc += (dk_m - dk_p) * 0.5 * ic * ic;
+  const double dden = -dk_e * k_e / (cc * rho_a);
+  dcc += dden * rho_a - dk_s * k_s * k_s;
+  drho_a += dden * cc;
+  double dLc[5] = {0, 0, 0, 0, 0}, dRc[5] = {0, 0, 0, 0, 0};
+  frozen_state_vjp(Lc, Rc, fp, drho_a, dc, dcc, dLc, dRc);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    SL(v, 2) += dLc[v];
+    SL(v, 3) += dRc[v];
+  }
+}
+
 template <int AX, int RECON, int RIEMANN>
 __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], const int ext[3],
                                          double* sm_prim, double* sm_slot, double* sm_jr) {
@@ -106,6 +229,9 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         for (int k = 1; k < 5; ++k) sm_slot[(v * K + k) * fvol + f] = gL * jl[k] + gR * jr[5 - k];
         sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
       }
+    } else if constexpr (RECON == RECON_WENO5Z_CHAR) {
+      char_face_vjp<AX, RIEMANN>(p.fp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol,
+                                 sm_jr + tid, nthr);
     } else {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -184,10 +310,196 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
   // pencil primitives | per-thread right-stencil gradients (WENO only) | face slots
   double* sm_prim = smem;
   double* sm_jr = smem + 5 * pmax;
-  double* sm_slot = sm_jr + ((RECON == GBF_RECON_WENO5Z) ? 25 * blockDim.x : 0);
+  double* sm_slot = sm_jr + ((RECON == GBF_RECON_WENO5Z || RECON == RECON_WENO5Z_CHAR) ? 25 * blockDim.x : 0);
   if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
   if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
   if (p.active_mask & 4) vjp_axis<2, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+}
+
+// ---------------------------------------------------------------------------
+// Viscous and heat fluxes (CENTRAL4, periodic boundaries): the flux at a face
+// is a function of the velocity gradient at the face (normal derivatives by
+// the face stencil, tangential ones as face interpolations of centre
+// derivatives), the face-interpolated velocity and the face derivative of T.
+// Pass 1 (one thread per face) turns the face-flux cotangent into the
+// cotangents of those 11 stencil outputs; pass 2 (one thread per cell) applies
+// the transposed stencils, gathers over every face whose stencil reads the
+// cell, pulls dT back through T = p / (rho R) and adds to the primitive
+// cotangent.  Fixed summation order: deterministic.
+// ---------------------------------------------------------------------------
+constexpr int VISC_SLOTS = 11;  // dg[a][AX] (3), tangential (2 x 2), dvf (3), dTn
+
+struct ViscVjpParams {
+  int n[3];
+  int active_mask;
+  double one_dx[3];
+  const double* prims;  // interior primitives [5][N]
+  const double* w;      // rhs cotangent [5][N]
+  double* fc;           // face cotangents [3][VISC_SLOTS][N]; face i-1/2 of axis a stored at cell i
+  double* dP;           // primitive cotangent accumulator [5][N]
+  double mu1, mu2, kappa, R;
+  int viscous, heat, heat_production;
+};
+
+__device__ __forceinline__ long long wrap_off(const ViscVjpParams& p, int g0, int g1, int g2) {
+  g0 = (g0 < 0) ? g0 + p.n[0] : ((g0 >= p.n[0]) ? g0 - p.n[0] : g0);
+  g1 = (g1 < 0) ? g1 + p.n[1] : ((g1 >= p.n[1]) ? g1 - p.n[1] : g1);
+  g2 = (g2 < 0) ? g2 + p.n[2] : ((g2 >= p.n[2]) ? g2 - p.n[2] : g2);
+  return ((long long)g0 * p.n[1] + g1) * p.n[2] + g2;
+}
+
+// tangential axes of AX in ascending order (the ones that are active)
+template <int AX>
+__device__ __forceinline__ int tangential(int t) {
+  return (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
+}
+
+template <int AX>
+__global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams p) {
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= cs) return;
+  const int q2 = (int)(i % p.n[2]);
+  const int q1 = (int)((i / p.n[2]) % p.n[1]);
+  const int q0 = (int)(i / ((long long)p.n[2] * p.n[1]));
+  const int q[3] = {q0, q1, q2};
+  auto cell = [&](int v, int kax, int ax2, int k2) {
+    int g[3] = {q[0], q[1], q[2]};
+    g[AX] += kax;
+    g[ax2] += k2;
+    return __ldg(p.prims + v * cs + wrap_off(p, g[0], g[1], g[2]));
+  };
+  const double odx = p.one_dx[AX];
+  int gl[3] = {q0, q1, q2};
+  gl[AX] -= 1;
+  const long long offL = wrap_off(p, gl[0], gl[1], gl[2]);
+  double dF[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) dF[v] = odx * (__ldg(p.w + v * cs + i) - __ldg(p.w + v * cs + offL));
+  double out[VISC_SLOTS];
+#pragma unroll
+  for (int k = 0; k < VISC_SLOTS; ++k) out[k] = 0.0;
+  if (p.viscous) {
+    double dtau[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dtau[k] = (p.active_mask & (1 << k)) ? -dF[1 + k] : 0.0;
+    if (p.heat_production) {
+      // tau and the face velocity of the forward (energy flux sum_k tau_k vf_k)
+      double gr[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        gr[a][AX] = c4_face_deriv(odx, cell(1 + a, -2, AX, 0), cell(1 + a, -1, AX, 0), cell(1 + a, 0, AX, 0),
+                                  cell(1 + a, 1, AX, 0));
+#pragma unroll
+      for (int ii = 0; ii < 3; ++ii) {
+        if (ii == AX || !(p.active_mask & (1 << ii))) continue;
+        const double odi = p.one_dx[ii];
+#pragma unroll
+        for (int which = 0; which < 2; ++which) {
+          const int a = (which == 0) ? AX : ii;
+          double d[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            d[k] = c4_center_deriv(odi, cell(1 + a, k - 2, ii, -2), cell(1 + a, k - 2, ii, -1),
+                                   cell(1 + a, k - 2, ii, 1), cell(1 + a, k - 2, ii, 2));
+          gr[a][ii] = c4_face_interp(d[0], d[1], d[2], d[3]);
+        }
+      }
+      double tau[3], tr = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const bool act = p.active_mask & (1 << k);
+        tau[k] = act ? p.mu1 * (gr[AX][k] + gr[k][AX]) : 0.0;
+        if (act) tr += gr[k][k];
+      }
+      tau[AX] += p.mu2 * tr;
+      const double dvt = -dF[4];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (!(p.active_mask & (1 << k))) continue;
+        const double vf = c4_face_interp(cell(1 + k, -2, AX, 0), cell(1 + k, -1, AX, 0), cell(1 + k, 0, AX, 0),
+                                         cell(1 + k, 1, AX, 0));
+        dtau[k] += dvt * vf;
+        out[7 + k] = dvt * tau[k];
+      }
+    }
+    const double dtr = p.mu2 * dtau[AX];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (!(p.active_mask & (1 << a))) continue;
+      out[a] = p.mu1 * dtau[a] + ((a == AX) ? p.mu1 * dtau[AX] + dtr : 0.0);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int ii = tangential<AX>(t);
+      if (!(p.active_mask & (1 << ii))) continue;
+      out[3 + 2 * t] = p.mu1 * dtau[ii];  // d u_AX / d x_i
+      out[4 + 2 * t] = dtr;               // d u_i / d x_i
+    }
+  }
+  if (p.heat) out[10] = -p.kappa * dF[4];
+  double* fc = p.fc + (long long)AX * VISC_SLOTS * cs;
+#pragma unroll
+  for (int k = 0; k < VISC_SLOTS; ++k) fc[k * cs + i] = out[k];
+}
+
+__global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpParams p) {
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= cs) return;
+  const int c2 = (int)(i % p.n[2]);
+  const int c1 = (int)((i / p.n[2]) % p.n[1]);
+  const int c0 = (int)(i / ((long long)p.n[2] * p.n[1]));
+  constexpr double fd[4] = {1.0 / 24.0, -27.0 / 24.0, 27.0 / 24.0, -1.0 / 24.0};
+  constexpr double fi[4] = {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0};
+  constexpr double cd[4] = {1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};  // offsets -2, -1, +1, +2
+  constexpr int cj[4] = {-2, -1, 1, 2};
+  double du[3] = {0.0, 0.0, 0.0}, dT = 0.0;
+#pragma unroll
+  for (int AX = 0; AX < 3; ++AX) {
+    if (!(p.active_mask & (1 << AX))) continue;
+    const double* fc = p.fc + (long long)AX * VISC_SLOTS * cs;
+    const double odx = p.one_dx[AX];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      // this cell is stencil point k (offset k-2) of the face at q = c - (k-2) along AX
+      int g[3] = {c0, c1, c2};
+      g[AX] -= k - 2;
+      const long long f = wrap_off(p, g[0], g[1], g[2]);
+      const double wd = odx * fd[k];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * cs + f] + fi[k] * fc[(7 + a) * cs + f];
+      dT += wd * fc[10 * cs + f];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int ii = (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
+        if (!(p.active_mask & (1 << ii))) continue;
+        const double odi = p.one_dx[ii];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          int h[3] = {g[0], g[1], g[2]};
+          h[ii] -= cj[jj];
+          const long long ff = wrap_off(p, h[0], h[1], h[2]);
+          const double wt = fi[k] * odi * cd[jj];
+          du[AX] += wt * fc[(3 + 2 * t) * cs + ff];
+          du[ii] += wt * fc[(4 + 2 * t) * cs + ff];
+        }
+      }
+    }
+  }
+  const double rho = __ldg(p.prims + i);
+  const double pr = __ldg(p.prims + 4 * cs + i);
+  // T = p / (rho R)
+  const double iden = 1.0 / (rho * p.R);
+  p.dP[i] += -dT * pr * iden / rho;
+  p.dP[cs + i] += du[0];
+  p.dP[2 * cs + i] += du[1];
+  p.dP[3 * cs + i] += du[2];
+  p.dP[4 * cs + i] += dT * iden;
 }
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
@@ -237,17 +549,25 @@ inline int grid_for(long long n) {
 }
 
 int vjp_check(const gbf_case* c) {
-  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var != GBF_RECVAR_PRIMITIVE) return GBF_ERR_UNSUPPORTED;
   if (c->recon != GBF_RECON_WENO5Z && c->recon != GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
   if (c->riemann == GBF_RIEMANN_HLLC && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
+}
+
+inline bool vjp_dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0; }
+
+// doubles of rhs-VJP scratch beyond the primitive cotangent: interior
+// primitives and the viscous face cotangents of every active axis
+long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
+  if (!vjp_dissipative(c)) return 0;
+  return 5 * ci.cells + 3LL * VISC_SLOTS * ci.cells;
 }
 
 // VJP of the rhs at state U (interior): out = J(U)^T w.  dP: zeroed scratch of 5 n doubles
 // (left zeroed on return).
 int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const double* U,
-                   const double* w, double* out, double* dP, cudaStream_t s) {
+                   const double* w, double* out, double* dP, double* extra, cudaStream_t s) {
   VjpParams vp;
   int threads;
   size_t smem;
@@ -256,6 +576,7 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
   // shared memory: pencil primitives + 2R x 5 slots per face (replaces the
   // flux slots) + 25 doubles per thread for WENO's right-stencil gradients
+  // (primitive or characteristic)
   long long pmax = 0, fmax = 0;
   for (int a = 0; a < 3; ++a) {
     if (!(ci.active_mask & (1 << a))) continue;
@@ -281,13 +602,42 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     k<<<grid, threads, smem, s>>>(vp);                                                               \
   }
   const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
-  if (c->recon == GBF_RECON_WENO5Z) {
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE) {
+    if (hllc) GBF_VJP(RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC) else GBF_VJP(RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV)
+  } else if (c->recon == GBF_RECON_WENO5Z) {
     if (hllc) GBF_VJP(GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC) else GBF_VJP(GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV)
   } else {
     if (hllc) GBF_VJP(GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC) else GBF_VJP(GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV)
   }
 #undef GBF_VJP
   if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
+  if (vjp_dissipative(c)) {
+    ViscVjpParams q;
+    for (int a = 0; a < 3; ++a) {
+      q.n[a] = ci.n[a];
+      q.one_dx[a] = vp.sp.one_dx[a];
+    }
+    q.active_mask = ci.active_mask;
+    double* P = extra;
+    q.prims = P;
+    q.w = w;
+    q.fc = P + 5 * ci.cells;
+    q.dP = dP;
+    q.mu1 = vp.sp.mu1;
+    q.mu2 = vp.sp.mu2;
+    q.kappa = vp.sp.kappa;
+    q.R = vp.sp.R;
+    q.viscous = vp.sp.viscous;
+    q.heat = vp.sp.heat;
+    q.heat_production = vp.sp.heat_production;
+    if ((st = launch_convert(c, U, P, ci.cells, 1, s)) != GBF_OK) return st;
+    const unsigned g = (unsigned)((ci.cells + 255) / 256);
+    if (ci.active_mask & 1) visc_face_vjp_kernel<0><<<g, 256, 0, s>>>(q);
+    if (ci.active_mask & 2) visc_face_vjp_kernel<1><<<g, 256, 0, s>>>(q);
+    if (ci.active_mask & 4) visc_face_vjp_kernel<2><<<g, 256, 0, s>>>(q);
+    visc_cell_gather_kernel<<<g, 256, 0, s>>>(q);
+    if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
+  }
   dp_to_du_kernel<<<grid_for(ci.cells), 256, 0, s>>>(U, dP, out, ci.cells, ci.fp.gm1);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
@@ -301,8 +651,9 @@ using namespace gbf;
 extern "C" size_t gbf_vjp_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
   if (make_case_info(c, &ci) != GBF_OK) return 0;
-  // step VJP: U1, U2, lam2, lam1, j, dP (6 interior states)
-  return (size_t)6 * 5 * (size_t)ci.cells * sizeof(double);
+  // step VJP: U1, U2, lam2, lam1, j, dP (6 interior states); dissipative
+  // cases add the primitives and the viscous face cotangents
+  return ((size_t)6 * 5 * (size_t)ci.cells + (size_t)vjp_extra_doubles(c, ci)) * sizeof(double);
 }
 
 extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out,
@@ -316,7 +667,7 @@ extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* 
   cudaStream_t s = (cudaStream_t)stream;
   double* dP = (double*)workspace;
   zero_kernel<<<grid_for(5 * ci.cells), 256, 0, s>>>(dP, 5 * ci.cells);
-  return launch_rhs_vjp(c, ci, tile, cons, w, out, dP, s);
+  return launch_rhs_vjp(c, ci, tile, cons, w, out, dP, dP + 5 * ci.cells, s);
 }
 
 static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, const double* u2_in,
@@ -336,6 +687,7 @@ static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, 
   double* lam1 = lam2 + m;
   double* j = lam1 + m;
   double* dP = j + m;
+  double* extra = dP + m;
   const double* S1 = u1_in;
   const double* S2 = u2_in;
   if (!S1 || !S2) {
@@ -347,22 +699,27 @@ static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, 
     // the forward kernels read dt from dt_state[0]; dt points at a device scalar
     p.dt_state = const_cast<double*>(dt);
     p.reduce_dt = 0;
+    const bool diss = vjp_dissipative(c);
+    const int mode = diss ? MODE_STAGE_P : MODE_STAGE;
+    p.prims = extra;  // dissipative stages read the stage primitives
+    if (diss && (st = launch_convert(c, cons, extra, ci.cells, 1, s)) != GBF_OK) return st;
     p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = U1;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
+    if (diss && (st = launch_convert(c, U1, extra, ci.cells, 1, s)) != GBF_OK) return st;
     p.stage = 1; p.cons = U1; p.cons0 = cons; p.out = U2;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
+    if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
     S1 = U1;
     S2 = U2;
   }
   zero_kernel<<<grid_for(m), 256, 0, s>>>(dP, m);
   // stage 3: U3 = 1/3 Un + 2/3 U2 + 2/3 dt L(U2)
-  if ((st = launch_rhs_vjp(c, ci, tile, S2, lam, j, dP, s)) != GBF_OK) return st;
+  if ((st = launch_rhs_vjp(c, ci, tile, S2, lam, j, dP, extra, s)) != GBF_OK) return st;
   axpy_dt_kernel<<<grid_for(m), 256, 0, s>>>(lam2, lam, 2.0 / 3.0, j, 2.0 / 3.0, dt, m);
   // stage 2: U2 = 3/4 Un + 1/4 U1 + 1/4 dt L(U1)
-  if ((st = launch_rhs_vjp(c, ci, tile, S1, lam2, j, dP, s)) != GBF_OK) return st;
+  if ((st = launch_rhs_vjp(c, ci, tile, S1, lam2, j, dP, extra, s)) != GBF_OK) return st;
   axpy_dt_kernel<<<grid_for(m), 256, 0, s>>>(lam1, lam2, 0.25, j, 0.25, dt, m);
   // stage 1: U1 = Un + dt L(Un)
-  if ((st = launch_rhs_vjp(c, ci, tile, cons, lam1, j, dP, s)) != GBF_OK) return st;
+  if ((st = launch_rhs_vjp(c, ci, tile, cons, lam1, j, dP, extra, s)) != GBF_OK) return st;
   step_combine_kernel<<<grid_for(m), 256, 0, s>>>(lam_out, lam, lam2, lam1, j, dt, m);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }

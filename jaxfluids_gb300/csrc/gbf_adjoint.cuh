@@ -420,6 +420,81 @@ __device__ __forceinline__ void rusanov_vjp(const double PL[5], const double PR[
   cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
 
+// Reverse of frozen_state (eigendecomposition.py:120-281) for the single-phase
+// ideal gas: cotangents of (rho_a, c, cc) pulled back onto the primitives of
+// the two cells L, R adjacent to the face (accumulated into dL, dR).
+__device__ __forceinline__ void frozen_state_vjp(const double L[5], const double R[5], const FaceParams& fp,
+                                                 double drho_a, double dc, double dcc, double dL[5],
+                                                 double dR[5]) {
+  if (fp.frozen_state == GBF_FROZEN_ARITHMETIC) {
+    // rho = (L0+R0)/2, p = (L4+R4)/2, c = sqrt(gamma p / rho), cc = c c
+    const double rho = 0.5 * (L[0] + R[0]);
+    const double p = 0.5 * (L[4] + R[4]);
+    const double irho = 1.0 / rho;
+    const double y = fp.gamma * p * irho;
+    const double c = sqrt(y);
+    const double dct = dc + dcc * 2.0 * c;
+    const double dy = dct * 0.5 / c;
+    const double drho = drho_a - dy * y * irho;
+    const double dp = dy * fp.gamma * irho;
+    dL[0] += 0.5 * drho;
+    dR[0] += 0.5 * drho;
+    dL[4] += 0.5 * dp;
+    dR[4] += 0.5 * dp;
+    return;
+  }
+  const double gm1 = fp.gm1;
+  const double rho_a = sqrt(L[0] * R[0]);
+  const double sL = sqrt(L[0]), sR = sqrt(R[0]);
+  const double rho_div = 1.0 / (sL + sR);
+  const double iL0 = 1.0 / L[0], iR0 = 1.0 / R[0];
+  const double qL = L[4] * iL0, qR = R[4] * iR0;
+  const double A = sL * qL + sR * qR;  // psi_a and the first term of p_over_rho
+  const double gr_a = (sL * gm1 + sR * gm1) * rho_div;
+  const double d1 = R[1] - L[1], d2 = R[2] - L[2], d3 = R[3] - L[3];
+  const double sqvd = d1 * d1 + d2 * d2 + d3 * d3;
+  const double p_over_rho = A * rho_div + 0.5 * rho_a * rho_div * rho_div * sqvd;
+  const double cc = A * rho_div + gr_a * p_over_rho;
+  const double c = sqrt(cc);
+  // c = sqrt(cc)
+  const double dcct = dcc + dc * 0.5 / c;
+  // cc = psi_a + gr_a p_over_rho
+  const double dpor = dcct * gr_a;
+  const double dgr = dcct * p_over_rho;
+  double dA = dcct * rho_div + dpor * rho_div;
+  double drho_div = dcct * A + dpor * A + dpor * rho_a * rho_div * sqvd;
+  double drho = drho_a + dpor * 0.5 * rho_div * rho_div * sqvd;
+  const double dsq = dpor * 0.5 * rho_a * rho_div * rho_div;
+  // gr_a = (sL gm1 + sR gm1) rho_div
+  double dsL = dgr * gm1 * rho_div, dsR = dgr * gm1 * rho_div;
+  drho_div += dgr * (sL * gm1 + sR * gm1);
+  // A = sL L4/L0 + sR R4/R0
+  dsL += dA * qL;
+  dsR += dA * qR;
+  const double dqL = dA * sL, dqR = dA * sR;
+  dL[4] += dqL * iL0;
+  dR[4] += dqR * iR0;
+  dL[0] -= dqL * qL * iL0;
+  dR[0] -= dqR * qR * iR0;
+  // sqvd
+  dR[1] += 2.0 * d1 * dsq;
+  dL[1] -= 2.0 * d1 * dsq;
+  dR[2] += 2.0 * d2 * dsq;
+  dL[2] -= 2.0 * d2 * dsq;
+  dR[3] += 2.0 * d3 * dsq;
+  dL[3] -= 2.0 * d3 * dsq;
+  // rho_div = 1/(sL + sR)
+  const double dsum = -drho_div * rho_div * rho_div;
+  dsL += dsum;
+  dsR += dsum;
+  dL[0] += dsL * 0.5 / sL;
+  dR[0] += dsR * 0.5 / sR;
+  // rho_a = sqrt(L0 R0)
+  const double dprod = drho * 0.5 / rho_a;
+  dL[0] += dprod * R[0];
+  dR[0] += dprod * L[0];
+}
+
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
                                                  const double dF[5], double dPL[5], double dPR[5]) {

@@ -109,6 +109,21 @@ VJP_CASES = [
     ("3d-weno-hllc", (20, 12, 18), "PERIODIC", {}, "generic"),
     ("3d-minmodad-rusanov-zg", (12, 10, 20), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "RUSANOV"},
      "generic"),
+    ("2d-char-roe-hllc", (40, 36, 1), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "generic"),
+    ("2d-char-arith-rusanov-zg", (20, 36, 1), "ZEROGRADIENT", {"recon_var": "CHAR-PRIMITIVE", "riemann": "RUSANOV"},
+     "generic"),
+    ("2d-char-roe-sym", (36, 20, 1), {"east": "SYMMETRY", "west": "SYMMETRY", "north": "ZEROGRADIENT",
+                                       "south": "ZEROGRADIENT", "top": "PERIODIC", "bottom": "PERIODIC"},
+     {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "generic"),
+    ("3d-char-roe-hllc", (16, 12, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "generic"),
+    ("2d-viscous-heat", (24, 20, 1), "PERIODIC", {"nh": 4, "viscous": True, "heat": True, "mu": 0.05,
+                                                   "prandtl": 0.71}, "generic"),
+    ("2d-heat-only", (20, 24, 1), "PERIODIC", {"nh": 4, "heat": True, "mu": 0.05, "prandtl": 0.71}, "generic"),
+    ("3d-viscous-noheatprod", (12, 16, 10), "PERIODIC", {"nh": 4, "viscous": True, "mu": 0.02,
+                                                          "viscous_heat_production": False}, "generic"),
+    ("3d-char-roe-viscous-heat", (16, 12, 14), "PERIODIC", {"nh": 4, "recon_var": "CHAR-PRIMITIVE",
+                                                             "frozen_state": "ROE", "viscous": True, "heat": True,
+                                                             "mu": 0.02, "prandtl": 0.71}, "generic"),
 ]
 
 
@@ -149,7 +164,8 @@ def test_checkpoint_schedules_agree_and_match_oracle():
     adj = AdjointRK3(cc, dt=dt)
     tg = target.cuda()
     grads = []
-    for sched, kw in (("uniform", {"every": n}), ("uniform", {"every": 4}), ("binomial", {"slots": 2}),
+    for sched, kw in (("uniform", {"every": n}), ("uniform", {"every": 4}),
+                      ("uniform", {"every": 5, "keep_stages": False}), ("binomial", {"slots": 2}),
                       ("binomial", {"slots": 0}), ("stored", {})):
         UN, g = adj.gradient(U0.cuda(), n, lambda U: torch.stack([U[0] - tg] + [torch.zeros_like(tg)] * 4),
                              schedule=sched, **kw)
