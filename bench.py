@@ -339,6 +339,63 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_viscous_adjoint(args):
+    """Adjoint of the viscous TGV (CHAR-ROE + HLLC + CENTRAL4, Re 1600, Pr 0.71):
+    gradient of the final kinetic energy w.r.t. the initial velocity over a
+    fixed-dt trajectory, reversed with binomial checkpoints whose segments of
+    up to `leaf` steps are replayed keeping their stage states.  Reports the cost
+    of the gradient (forward for the loss + recomputation + reverse sweep)
+    over the cost of the forward run alone."""
+    from jaxfluids_gb300 import FusedRK3, build
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    build.build()
+    device = torch.device("cuda", 0)
+    n = args.n if args.n else 256
+    cfg = viscous_tgv_config(n)
+    U0 = tgv_state(n, device)
+    f = FusedRK3(cfg, device)
+    f.set_state(U0)
+    dt = float(f.dt)
+    del f
+    adj = AdjointRK3(cfg, dt, device)
+    steps = args.adj_steps
+    adj.advance(U0, 2)  # warm-up
+    torch.cuda.synchronize()
+
+    def ke_grad(U):
+        # KE = sum (rho u)^2 / (2 rho): dKE/d(rho u_i) = u_i, dKE/drho = -|u|^2 / 2
+        u = U[1:4] / U[0]
+        return torch.cat([(-0.5 * (u * u).sum(0))[None], u, torch.zeros_like(U[:1])])
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    UN = adj.advance(U0, steps)
+    b.record()
+    b.synchronize()
+    t_fwd = a.elapsed_time(b) / 1e3
+    del UN
+    adj.forward_steps = 0
+    torch.cuda.reset_peak_memory_stats(device)
+    a.record()
+    UN2, grad = adj.gradient(U0, steps, ke_grad, schedule="binomial", slots=args.adj_slots, leaf=args.adj_leaf)
+    b.record()
+    b.synchronize()
+    t_adj = a.elapsed_time(b) / 1e3
+    rho0 = U0[0]
+    gu = torch.stack([grad[1 + i] * rho0 + grad[4] * U0[1 + i] for i in range(3)])
+    ke = float((0.5 * (UN2[1:4] ** 2).sum(0) / UN2[0]).sum())
+    line = {"metric": "adjoint cost / forward cost, 3-D viscous TGV", "value": t_adj / t_fwd, "unit": "x",
+            "higher_is_better": False, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"viscous TGV {n}^3 Re 1600 Pr 0.71, CHAR-ROE WENO5-Z + HLLC + CENTRAL4, "
+                                   f"{steps} fixed-dt RK3 steps (dt {dt:.4e})",
+                       "schedule": "binomial", "slots": args.adj_slots, "leaf": args.adj_leaf,
+                       "cells": n ** 3},
+            "forward_s": t_fwd, "gradient_s": t_adj, "forward_steps_recomputed": adj.forward_steps,
+            "peak_device_gb": torch.cuda.max_memory_allocated(device) / 1e9,
+            "final_ke": ke, "grad_u_norm": float(gu.norm())}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,9 +404,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=None, help="grid side (default 128 inviscid, 256 viscous)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "adjoint"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "adjoint", "viscous-adjoint"])
     ap.add_argument("--adj-n", type=int, default=512)
-    ap.add_argument("--adj-steps", type=int, default=1000)
+    ap.add_argument("--adj-steps", type=int, default=None, help="default 1000 (KH), 200 (viscous TGV)")
+    ap.add_argument("--adj-slots", type=int, default=4, help="binomial checkpoint slots (viscous adjoint)")
+    ap.add_argument("--adj-leaf", type=int, default=50,
+                    help="binomial: longest segment replayed once with its stage states kept (viscous adjoint)")
     ap.add_argument("--adj-every", type=int, default=50)
     ap.add_argument("--adj-schedule", default="stored", choices=["stored", "uniform", "binomial"])
     ap.add_argument("--cases", type=int, default=256)
@@ -357,7 +417,11 @@ def main():
     if args.workload == "batch":
         return run_batch(args)
     if args.workload == "adjoint":
+        args.adj_steps = args.adj_steps or 1000
         return run_adjoint(args)
+    if args.workload == "viscous-adjoint":
+        args.adj_steps = args.adj_steps or 200
+        return run_viscous_adjoint(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -13,7 +13,10 @@ trajectory is replayed from checkpoints kept in device memory:
   they fit in device memory), so nothing is recomputed;
 * binomial: at most ``slots`` stored states, split points chosen by dynamic
   programming to minimise recomputed steps (Griewank-style revolve), so long
-  trajectories of large grids fit in memory.
+  trajectories of large grids fit in memory; the forward run for the loss
+  places the first checkpoints, and segments of up to ``leaf`` steps are
+  replayed once keeping their stage states (3 states per step of leaf memory)
+  instead of recomputing stages inside every step VJP.
 
 ``RK3Trajectory`` wraps both as a ``torch.autograd.Function``.
 """
@@ -91,8 +94,12 @@ class AdjointRK3:
         return self.fwd.cons.clone(), store
 
     def backward_stored(self, store, lam: torch.Tensor) -> torch.Tensor:
-        for Un, U1, U2 in reversed(store):
+        """Reverse the stored steps, releasing each step's states once used
+        (the list is emptied)."""
+        while store:
+            Un, U1, U2 = store.pop()
             lam = self.step_vjp_stages(Un, U1, U2, lam)
+            del Un, U1, U2
         return lam
 
     def rhs_vjp(self, U: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
@@ -139,49 +146,123 @@ class AdjointRK3:
 
     # ---- binomial checkpoints ---------------------------------------------
     @staticmethod
-    @functools.lru_cache(maxsize=None)
-    def _plan(n: int, slots: int) -> Tuple[int, Tuple]:
-        """(cost, split) minimising recomputed steps to reverse n steps from a
-        stored start state with `slots` extra stored states."""
-        if n <= 1:
-            return 0, ()
-        if slots == 0:
-            return n * (n - 1) // 2, ()
-        best = None
-        for m in range(1, n):
-            c = m + AdjointRK3._plan(n - m, slots - 1)[0] + AdjointRK3._plan(m, slots)[0]
-            if best is None or c < best[0]:
-                best = (c, (m,))
-        return best
+    @functools.lru_cache(maxsize=8)
+    def _leaf_plan(n: int, slots: int, leaf: int):
+        """Revolve with stored-stage leaves.  Costs in thirds of a step.  To
+        reverse k steps from a stored state: one step costs 2 (its two stage
+        states are recomputed inside the step VJP), a segment of 2..leaf steps
+        costs 3k (replayed once keeping every stage state, held in 3k states of
+        leaf memory); longer ones split at m: advance m (3m), reverse the tail
+        with one slot fewer, then the head.  Without slots the tail segment is
+        reached by re-advancing from the start.  Returns (cost, choice) tables
+        indexed [s][k]; choice = (kind, m)."""
+        INF = float("inf")
+        cost = [[INF] * (n + 1) for _ in range(slots + 1)]
+        choice = [[None] * (n + 1) for _ in range(slots + 1)]
 
-    def _reverse(self, U: torch.Tensor, n: int, slots: int, lam: torch.Tensor) -> torch.Tensor:
-        if n == 1:
+        def leaf_cost(k):
+            return 2 if k == 1 else 3 * k
+
+        for sl in range(slots + 1):
+            cost[sl][0] = 0
+            for k in range(1, n + 1):
+                if k <= max(leaf, 1):
+                    best, ch = leaf_cost(k), ("step" if k == 1 else "leaf", k)
+                else:
+                    best, ch = INF, None
+                if sl == 0:
+                    for t in range(1, min(k - 1, leaf) + 1):  # last segment of t steps
+                        c = 3 * (k - t) + leaf_cost(t) + cost[0][k - t]
+                        if c < best:
+                            best, ch = c, ("tail", t)
+                else:
+                    for m in range(1, k):
+                        c = 3 * m + cost[sl - 1][k - m] + cost[sl][m]
+                        if c < best:
+                            best, ch = c, ("split", m)
+                cost[sl][k] = best
+                choice[sl][k] = ch
+        return cost, choice
+
+    def _reverse(self, U: torch.Tensor, n: int, slots: int, lam: torch.Tensor, choice) -> torch.Tensor:
+        kind, m = choice[slots][n]
+        if kind == "step":
             return self.step_vjp(U, lam)
-        if slots == 0:
-            for j in range(n - 1, -1, -1):
-                lam = self.step_vjp(self.advance(U, j), lam)
+        if kind == "leaf":
+            _, store = self.forward_stored(U, n)
+            lam = self.backward_stored(store, lam)
+            del store
             return lam
-        m = self._plan(n, slots)[1][0]
+        if kind == "tail":
+            Ut = self.advance(U, n - m)
+            lam = self._reverse(Ut, m, 0, lam, choice)
+            del Ut
+            return self._reverse(U, n - m, 0, lam, choice)
         Um = self.advance(U, m)
-        lam = self._reverse(Um, n - m, slots - 1, lam)
+        lam = self._reverse(Um, n - m, slots - 1, lam, choice)
         del Um
-        return self._reverse(U, m, slots, lam)
+        return self._reverse(U, m, slots, lam, choice)
 
-    def backward_binomial(self, U0: torch.Tensor, nsteps: int, slots: int, lam: torch.Tensor) -> torch.Tensor:
-        return self._reverse(U0, nsteps, slots, lam)
+    def forward_binomial(self, U0: torch.Tensor, nsteps: int, slots: int, leaf: int = 1):
+        """The forward run for the loss, placing the checkpoints the reverse
+        sweep reaches first (the right spine of the plan) and keeping the stage
+        states of the last segment.  Returns (U_N, last-segment store, spine),
+        spine = [(start state, steps, slots)] still to be reversed."""
+        choice = self._leaf_plan(nsteps, slots, leaf)[1]
+        U, n, sl = U0, nsteps, slots
+        spine = []
+        while True:
+            kind, m = choice[sl][n]
+            if kind == "split":
+                Um = self.advance(U, m)
+                spine.append((U, m, sl))
+                U, n, sl = Um, n - m, sl - 1
+            elif kind == "tail":
+                Ut = self.advance(U, n - m)
+                spine.append((U, n - m, 0))
+                U, n = Ut, m
+            else:
+                UN, store = self.forward_stored(U, n)
+                return UN, store, (spine, choice)
+
+    def backward_binomial(self, store, spine, lam: torch.Tensor) -> torch.Tensor:
+        parts, choice = spine
+        lam = self.backward_stored(store, lam)
+        del store
+        while parts:
+            U, m, sl = parts.pop()
+            lam = self._reverse(U, m, sl, lam, choice)
+        return lam
+
+    def binomial_cost(self, nsteps: int, slots: int, leaf: int = 1) -> float:
+        """Forward-step equivalents of the binomial schedule beyond the loss's
+        forward run (stage recomputation inside step VJPs included)."""
+        cost, choice = self._leaf_plan(nsteps, slots, leaf)
+        total, n, sl = 0, nsteps, slots
+        while True:  # the spine's left parts; the spine itself is the loss forward
+            kind, m = choice[sl][n]
+            if kind == "split":
+                total += cost[sl][m]
+                n, sl = n - m, sl - 1
+            elif kind == "tail":
+                total += cost[0][n - m]
+                n = m
+            else:
+                return total / 3.0
 
     # ---- gradient -----------------------------------------------------------
     def gradient(self, U0: torch.Tensor, nsteps: int, loss_grad: Callable[[torch.Tensor], torch.Tensor],
-                 schedule: str = "uniform", every: int = 50, slots: int = 8, keep_stages: bool = True):
+                 schedule: str = "uniform", every: int = 50, slots: int = 8, keep_stages: bool = True,
+                 leaf: int = 1):
         """(U_N, dL/dU_0) for a loss whose gradient w.r.t. U_N is loss_grad(U_N)."""
         if schedule == "uniform":
             UN, ckpt = self.forward_uniform(U0, nsteps, every)
             lam = loss_grad(UN)
             return UN, self.backward_uniform(ckpt, nsteps, every, lam, keep_stages)
         if schedule == "binomial":
-            UN = self.advance(U0, nsteps)
+            UN, store, spine = self.forward_binomial(U0, nsteps, slots, leaf)
             lam = loss_grad(UN)
-            return UN, self.backward_binomial(U0, nsteps, slots, lam)
+            return UN, self.backward_binomial(store, spine, lam)
         if schedule == "stored":
             UN, store = self.forward_stored(U0, nsteps)
             lam = loss_grad(UN)
@@ -194,15 +275,14 @@ class RK3Trajectory(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, U0: torch.Tensor, adj: AdjointRK3, nsteps: int, schedule: str = "uniform",
-                every: int = 50, slots: int = 8):
-        ctx.adj, ctx.nsteps, ctx.schedule, ctx.every, ctx.slots = adj, nsteps, schedule, every, slots
+                every: int = 50, slots: int = 8, leaf: int = 1):
+        ctx.adj, ctx.nsteps, ctx.schedule, ctx.every, ctx.slots, ctx.leaf = adj, nsteps, schedule, every, slots, leaf
         U0c = U0.detach().contiguous()
         if schedule == "uniform":
             UN, ckpt = adj.forward_uniform(U0c, nsteps, every)
             ctx.ckpt = ckpt
         else:
-            UN = adj.advance(U0c, nsteps)
-            ctx.U0 = U0c
+            UN, ctx.store, ctx.spine = adj.forward_binomial(U0c, nsteps, slots, leaf)
         return UN
 
     @staticmethod
@@ -212,5 +292,6 @@ class RK3Trajectory(torch.autograd.Function):
         if ctx.schedule == "uniform":
             dU0 = adj.backward_uniform(ctx.ckpt, ctx.nsteps, ctx.every, lam)
         else:
-            dU0 = adj.backward_binomial(ctx.U0, ctx.nsteps, ctx.slots, lam)
-        return dU0, None, None, None, None, None
+            dU0 = adj.backward_binomial(ctx.store, ctx.spine, lam)
+            ctx.store = ctx.spine = None
+        return dU0, None, None, None, None, None, None

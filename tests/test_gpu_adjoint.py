@@ -166,6 +166,7 @@ def test_checkpoint_schedules_agree_and_match_oracle():
     grads = []
     for sched, kw in (("uniform", {"every": n}), ("uniform", {"every": 4}),
                       ("uniform", {"every": 5, "keep_stages": False}), ("binomial", {"slots": 2}),
+                      ("binomial", {"slots": 2, "leaf": 4}), ("binomial", {"slots": 0, "leaf": 3}),
                       ("binomial", {"slots": 0}), ("stored", {})):
         UN, g = adj.gradient(U0.cuda(), n, lambda U: torch.stack([U[0] - tg] + [torch.zeros_like(tg)] * 4),
                              schedule=sched, **kw)
