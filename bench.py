@@ -230,9 +230,10 @@ def run_batch(args):
     batch = BatchedRK3(cfgs, device)
     batch.set_states([s.to(device) for s in states])
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    tune = autotune(batch, candidates=[((16, 32, 1), 256, 2 * sms), ((32, 16, 1), 256, 2 * sms),
-                                       ((8, 64, 1), 256, 2 * sms), ((16, 16, 1), 128, 3 * sms),
-                                       ((16, 32, 1), 256, sms), ((32, 32, 1), 256, 2 * sms)], steps=1)
+    tune = autotune(batch, candidates=[((15, 32, 1), 256, 2 * sms), ((31, 16, 1), 256, 2 * sms),
+                                       ((15, 32, 1), 256, sms), ((15, 16, 1), 128, 3 * sms),
+                                       ((16, 32, 1), 256, 2 * sms), ((32, 16, 1), 256, 2 * sms),
+                                       ((8, 64, 1), 256, 2 * sms), ((16, 16, 1), 128, 3 * sms)], steps=1)
     graph = batch.capture(args.steps)
     for _ in range(max(1, args.warmup // max(1, args.steps))):
         graph.replay()

@@ -32,7 +32,7 @@ _SCHEME_KEYS = ("nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riema
 
 
 def default_tile(dim: int) -> Tuple[int, int, int]:
-    return {1: (256, 1, 1), 2: (16, 32, 1), 3: (8, 8, 8)}[dim]
+    return {1: (256, 1, 1), 2: (15, 32, 1), 3: (8, 8, 8)}[dim]
 
 
 def build_worklist(cells: Sequence[Tuple[int, int, int]], tile: Tuple[int, int, int]):
@@ -170,9 +170,11 @@ def autotune(batch: BatchedRK3, candidates: Optional[List[Tuple[Tuple[int, int, 
     if candidates is None:
         sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
         if dim == 2:
-            shapes = [(16, 32, 1), (32, 16, 1), (8, 64, 1), (16, 16, 1), (32, 32, 1)]
+            # 15 x 32 and 31 x 16 give 512 / 496 faces per axis: two full
+            # rounds of 256 threads per face sweep, no ragged third round
+            shapes = [(15, 32, 1), (16, 32, 1), (31, 16, 1), (15, 16, 1), (32, 16, 1), (8, 64, 1), (16, 16, 1)]
         elif dim == 3:
-            shapes = [(8, 8, 8), (8, 8, 16), (4, 8, 16), (8, 16, 8)]
+            shapes = [(7, 8, 8), (8, 8, 8), (8, 8, 16), (4, 8, 16), (8, 16, 8)]
         else:
             shapes = [(256, 1, 1), (512, 1, 1), (128, 1, 1)]
         candidates = [(sh, thr, k * sms) for sh in shapes for thr in (256, 128) for k in (1, 2, 3)]

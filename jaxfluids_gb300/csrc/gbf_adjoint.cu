@@ -571,7 +571,7 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   VjpParams vp;
   int threads;
   size_t smem;
-  int st = make_sweep_params(c, ci, tile, &vp.sp, &threads, &smem);
+  int st = make_sweep_params(c, ci, tile, &vp.sp, &threads, &smem, true);
   if (st != GBF_OK) return st;
   const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
   // shared memory: pencil primitives + 2R x 5 slots per face (replaces the

@@ -21,9 +21,10 @@ struct CaseInfo {
 
 int make_case_info(const gbf_case* c, CaseInfo* ci);
 
-// fills p.{n,t,tiles,...} from the case and tile; returns status
+// fills p.{n,t,tiles,...} from the case and tile (tile null or all zero:
+// the default shape, for_vjp picking the adjoint kernel's); returns status
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
-                      int* threads, size_t* smem);
+                      int* threads, size_t* smem, bool for_vjp = false);
 
 // launch the sweep kernel instantiation for (recon, riemann, mode)
 int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem,
