@@ -103,10 +103,13 @@ typedef struct gbf_case {
   double stencil_eps;    /* spatial stencil epsilon (1e-30) */
 } gbf_case;
 
-/* Launch shape of the fused sweep kernels; all-zero picks the built-in default. */
+/* Launch shape of the fused sweep kernels; all-zero picks the built-in default
+ * (2-D 15x32, 3-D 8x8x8 inviscid PRIMITIVE or 7x8x8 CHAR/viscous and adjoint,
+ * 1-D 256).  Cells per tile at most 4 x threads; the staged pencil and face
+ * slots must fit 227 KB of shared memory (GBF_ERR_INVALID_ARGUMENT otherwise). */
 typedef struct gbf_tile {
   int32_t t[3];          /* cells per tile along each axis (1 on inactive axes) */
-  int32_t threads;       /* threads per CTA (multiple of 32, <= 1024) */
+  int32_t threads;       /* threads per CTA (multiple of 32, 32..256) */
 } gbf_tile;
 
 int gbf_abi_version(void);
@@ -176,11 +179,15 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
  * (feed_forward/feed_forward.py:231-524, simulation_manager.py:1296-1412).
  * Follows jax.grad's conventions at non-smooth points (|x|' = +1 at 0, half
  * of the cotangent to each argument of a max/min tie, zero derivative of
- * sign, where() passes the selected branch).  Inviscid, PRIMITIVE
- * reconstruction with WENO5-Z or MINMOD-AD, HLLC (Einfeldt speeds) or Rusanov.
+ * sign, where() passes the selected branch).  PRIMITIVE reconstruction with
+ * WENO5-Z or MINMOD-AD, CHAR-PRIMITIVE (ARITHMETIC or ROE frozen state) with
+ * WENO5-Z, HLLC (Einfeldt speeds) or Rusanov, and the CENTRAL4 viscous and
+ * heat fluxes (source_term_solver.py:188-350); other schemes return
+ * GBF_ERR_UNSUPPORTED.
  *
  * gbf_rhs_vjp: out = J(U)^T w with J = d rhs / d U at the interior state
- *   `cons`; w, out interior [5][N].  workspace >= 5 N doubles.
+ *   `cons`; w, out interior [5][N].  workspace: gbf_vjp_workspace_bytes(c)
+ *   (at least 5 N doubles; dissipative cases 38 N more).
  * gbf_rk3_step_vjp: lam_out = (d U^{n+1} / d U^n)^T lam for one TVD-RK3 step
  *   from U^n = `cons` with the device time step *dt (stage states recomputed).
  *   workspace: gbf_vjp_workspace_bytes(c).  lam_out must not alias lam.
