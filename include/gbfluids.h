@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GBF_ABI_VERSION 1
+#define GBF_ABI_VERSION 2
 
 /* status codes */
 #define GBF_OK 0
@@ -62,10 +62,19 @@ extern "C" {
 #define GBF_SIGNAL_RUSANOV 3
 #define GBF_SIGNAL_TORO 4
 
-/* boundary types (halos/outer/boundary_condition.py:539-604) */
+/* boundary types (halos/outer/boundary_condition.py:539-604,
+ * halos/outer/material.py:140-210): WALL mirrors the interior with
+ * u_halo = 2 u_wall - u (:473-531), DIRICHLET sets the given primitives
+ * (:732-798), NEUMANN adds sign * dx * gradient to the boundary cell
+ * (:825-866; sign +1 at west/south/bottom, -1 at east/north/top).  Values
+ * come from gbf_case.bc_value; spatially or temporally varying callables and
+ * several types on one face are not supported. */
 #define GBF_BC_PERIODIC 0
 #define GBF_BC_ZEROGRADIENT 1
 #define GBF_BC_SYMMETRY 2
+#define GBF_BC_WALL 3
+#define GBF_BC_DIRICHLET 4
+#define GBF_BC_NEUMANN 5
 
 /* face order of gbf_case.bc */
 #define GBF_FACE_WEST 0
@@ -101,6 +110,9 @@ typedef struct gbf_case {
   double fixed_dt;       /* time_integration.fixed_timestep, 0 = CFL time step */
   double eps;            /* precision epsilon (jnp.finfo(float64).eps) */
   double stencil_eps;    /* spatial stencil epsilon (1e-30) */
+  double bc_value[6][5]; /* per face, GBF_FACE_* order: WALL [1..3] = wall velocity
+                            (u, v, w); DIRICHLET [0..4] = (rho, u, v, w, p);
+                            NEUMANN [0..4] = normal derivatives of (rho, u, v, w, p) */
 } gbf_case;
 
 /* Launch shape of the fused sweep kernels; all-zero picks the built-in default

@@ -21,7 +21,8 @@ RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"HLLC": 0, "RUSANOV": 1}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
-BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2}
+ABI_VERSION = 2  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
 FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
 FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION = 1, 2, 4
 
@@ -60,6 +61,7 @@ class GbfCase(ctypes.Structure):
         ("fixed_dt", ctypes.c_double),
         ("eps", ctypes.c_double),
         ("stencil_eps", ctypes.c_double),
+        ("bc_value", (ctypes.c_double * 5) * 6),
     ]
 
 
@@ -114,6 +116,9 @@ def load() -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.gbf_abi_version() != ABI_VERSION:
+        raise GbfError(f"{LIB_PATH} has ABI version {lib.gbf_abi_version()}, this package needs {ABI_VERSION}: "
+                       "rebuild it with jaxfluids_gb300.build.build()")
     _lib = lib
     return lib
 

@@ -47,6 +47,23 @@ def _get(d: dict, path: str, default=None):
     return cur
 
 
+def _constant_callables(spec: dict, names: Tuple[str, ...], face: str) -> Tuple[float, ...]:
+    """Values of the reference's boundary callables (case_setup
+    boundary_conditions.<face>.wall_velocity_callable / primitives_callable)
+    when they are constants: numbers, or strings holding a number.  Functions
+    of the boundary coordinates or time are rejected."""
+    out = []
+    for k in names:
+        v = spec.get(k, 0.0) if k == "w" else spec.get(k)
+        if v is None:
+            raise SetupError(f"boundary at '{face}': '{k}' missing")
+        try:
+            out.append(float(v))
+        except (TypeError, ValueError):
+            raise NotImplementedError(f"boundary at '{face}': only constant '{k}' values are supported, got {v!r}")
+    return tuple(out)
+
+
 @dataclass
 class CaseConfig:
     cells: Tuple[int, int, int]
@@ -71,6 +88,9 @@ class CaseConfig:
     viscous_heat_production: bool = True
     eps: float = EPS
     stencil_eps: float = STENCIL_EPS
+    # constant boundary values per face: WALL (u, v, w), DIRICHLET and
+    # NEUMANN (rho, u, v, w, p) (wall_velocity_callable / primitives_callable)
+    bc_values: Dict[str, Tuple[float, ...]] = field(default_factory=dict)
 
     def __post_init__(self):
         self.cells = tuple(int(n) for n in self.cells)
@@ -85,6 +105,15 @@ class CaseConfig:
                     raise SetupError(f"boundary condition for face '{f}' missing")
                 if self.bc[f] not in _lib.BC:
                     raise NotImplementedError(f"boundary type {self.bc[f]} at {f}")
+        for f in FACES:
+            if FACE_AXIS[f] not in self.active:
+                continue
+            need_values = {"WALL": 3, "DIRICHLET": 5, "NEUMANN": 5}.get(self.bc[f])
+            if need_values is not None:
+                vals = self.bc_values.get(f)
+                if vals is None or len(vals) != need_values:
+                    raise SetupError(f"{self.bc[f]} boundary at '{f}' needs {need_values} values")
+                self.bc_values[f] = tuple(float(v) for v in vals)
         for ax, (lo, hi) in ((0, ("west", "east")), (1, ("south", "north")), (2, ("bottom", "top"))):
             if ax in self.active and (self.bc[lo] == "PERIODIC") != (self.bc[hi] == "PERIODIC"):
                 raise SetupError(f"PERIODIC must be set on both faces of axis {ax}")
@@ -109,8 +138,6 @@ class CaseConfig:
                 raise NotImplementedError("dissipative fluxes are built with WENO5-Z convective fluxes")
             if self.nh < 4:
                 raise SetupError("CENTRAL4 dissipative fluxes need halo_cells >= 4")
-            if any(self.bc[f] != "PERIODIC" for f in FACES if FACE_AXIS[f] in self.active):
-                raise NotImplementedError("dissipative fluxes are built for PERIODIC boundaries")
 
     # domain/domain_information.py:80-206 and mesh_creation/homogenous.py:13
     @property
@@ -152,6 +179,11 @@ class CaseConfig:
         c.signal_speed = _lib.SIGNAL[self.signal_speed]
         for k, f in enumerate(_lib.FACE_ORDER):
             c.bc[k] = _lib.BC[self.bc.get(f, "PERIODIC")]
+            vals = self.bc_values.get(f)
+            if vals is not None:
+                row = [0.0, *vals, 0.0] if len(vals) == 3 else list(vals)
+                for v in range(5):
+                    c.bc_value[k][v] = float(row[v])
         flags = 0
         if self.viscous:
             flags |= _lib.FLAG_VISCOUS
@@ -176,17 +208,23 @@ class CaseConfig:
         """Build from the reference's case_setup / numerical_setup dictionaries."""
         cells = tuple(int(_get(case_setup, f"domain.{a}.cells", 1)) for a in "xyz")
         ranges = tuple(tuple(_get(case_setup, f"domain.{a}.range", [0.0, 1.0])) for a in "xyz")
-        bc = {}
+        bc, bc_values = {}, {}
         for f in FACES:
             t = _get(case_setup, f"boundary_conditions.{f}")
             if isinstance(t, list):
                 if len(t) != 1:
                     raise NotImplementedError("multiple boundary types on one face")
                 t = t[0]
+            spec = t if isinstance(t, dict) else {}
             if isinstance(t, dict):
                 t = t.get("type")
             if t is not None and t != "INACTIVE":
                 bc[f] = t
+                if t == "WALL":
+                    bc_values[f] = _constant_callables(spec.get("wall_velocity_callable", {}), ("u", "v", "w"), f)
+                elif t in ("DIRICHLET", "NEUMANN"):
+                    bc_values[f] = _constant_callables(spec.get("primitives_callable", {}),
+                                                       ("rho", "u", "v", "w", "p"), f)
         eos = _get(case_setup, "material_properties.equation_of_state", {}) or {}
         if eos.get("model", "IdealGas") != "IdealGas":
             raise NotImplementedError(f"equation of state {eos.get('model')}")
@@ -235,6 +273,7 @@ class CaseConfig:
             raise NotImplementedError("single-precision compute")
         return cls(
             cells=cells, ranges=ranges, nh=int(cons.get("halo_cells", 3)), gamma=gamma, R=R, bc=bc,
+            bc_values=bc_values,
             recon=god.get("reconstruction_stencil", "WENO5-Z"),
             recon_var=god.get("reconstruction_variable", "PRIMITIVE"),
             frozen_state=god.get("frozen_state", "ARITHMETIC"),

@@ -279,9 +279,13 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     if (!any) continue;
     int g[3] = {o[0] + i0, o[1] + i1, o[2] + i2};
     g[AX] -= R;
-    bool flip;
-    g[AX] = remap_bc(g[AX], p.n[AX], p.bc[2 * AX], p.bc[2 * AX + 1], flip);
-    if (flip) d[AX + 1] = -d[AX + 1];
+    if (g[AX] < 0 || g[AX] >= p.n[AX]) {
+      // halo cell: transpose of the face rule (DIRICHLET halos are constants)
+      const int t = p.bc[2 * AX + (g[AX] >= 0 ? 1 : 0)];
+      g[AX] = bc_src(g[AX], p.n[AX], t);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] *= bc_apply_grad(t, AX, v);
+    }
     const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
 #pragma unroll
     for (int v = 0; v < 5; ++v)
@@ -552,6 +556,10 @@ int vjp_check(const gbf_case* c) {
   if (c->recon != GBF_RECON_WENO5Z && c->recon != GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
   if (c->riemann == GBF_RIEMANN_HLLC && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
+  // the viscous reverse pass indexes faces periodically (one face per cell)
+  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))
+    for (int f = 0; f < 6; ++f)
+      if (c->n[f >> 1] > 1 && c->bc[f] != GBF_BC_PERIODIC) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
 }
 

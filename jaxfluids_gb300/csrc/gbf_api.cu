@@ -54,13 +54,11 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
   if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) {
-    // CENTRAL4 dissipative fluxes: WENO5-Z convective part, periodic
-    // boundaries (edge halos of periodic faces are plain wraps), and four
-    // halo cells for the centre-derivative ring (spatial_stencil.py:86-96)
+    // CENTRAL4 dissipative fluxes: WENO5-Z convective part and four halo
+    // cells for the centre-derivative ring (spatial_stencil.py:86-96); the
+    // tangential stencils read edge halos (global_prim's edge rule)
     if (c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
     if (c->nh < 4) return GBF_ERR_INVALID_ARGUMENT;
-    for (int f = 0; f < 6; ++f)
-      if ((c->n[f >> 1] > 1) && c->bc[f] != GBF_BC_PERIODIC) return GBF_ERR_UNSUPPORTED;
     if (!(c->mu >= 0.0) || !(c->kappa >= 0.0) || !(c->R > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
   }
   if (!(c->gamma > 1.0)) return GBF_ERR_INVALID_ARGUMENT;
@@ -71,8 +69,7 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
       if (c->n[a] < c->nh) return GBF_ERR_SIZE;  // halo retrieve slices need nh interior cells
       for (int s = 0; s < 2; ++s) {
         const int b = c->bc[2 * a + s];
-        if (b != GBF_BC_PERIODIC && b != GBF_BC_ZEROGRADIENT && b != GBF_BC_SYMMETRY)
-          return GBF_ERR_UNSUPPORTED;
+        if (b < GBF_BC_PERIODIC || b > GBF_BC_NEUMANN) return GBF_ERR_UNSUPPORTED;
       }
       if ((c->bc[2 * a] == GBF_BC_PERIODIC) != (c->bc[2 * a + 1] == GBF_BC_PERIODIC))
         return GBF_ERR_INVALID_ARGUMENT;
@@ -130,9 +127,11 @@ int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) 
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
   if (!prims) return GBF_ERR_INVALID_ARGUMENT;
-  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))  // face, edge and vertex halos (all periodic)
-    return launch_halo_wrap(c, ci, prims, cons, (cudaStream_t)stream);
-  return launch_halo_fill(c, ci, prims, cons, (cudaStream_t)stream);
+  // face halos, then (viscous or heat flux) the edge halos from them
+  // (halo_manager.py:126-129; no vertex halos for a single phase)
+  st = launch_halo_fill(c, ci, prims, cons, (cudaStream_t)stream);
+  if (st != GBF_OK || !(c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))) return st;
+  return launch_halo_edges(c, ci, prims, cons, (cudaStream_t)stream);
 }
 
 int gbf_prims_from_cons(const gbf_case* c, const double* cons, double* prims, int64_t count,

@@ -27,6 +27,7 @@ struct HaloParams {
   long long face_start[6];
   long long total;
   double gm1;
+  double bcv[6][5];  // per-face boundary constants (fill_bc_constants)
 };
 
 // halos/outer/material.py:94-287 (face halos) with the retrieve slices of
@@ -58,24 +59,15 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
     const int n = hp.n[ax];
     const int nh = hp.nh;
     const int bct = hp.bc[face];
-    bool flip = false;
-    if (!hi) {
-      dst[ax] = layer;                                   // [:nh]
-      if (bct == GBF_BC_PERIODIC) src[ax] = n + layer;   // [-2nh:-nh]
-      else if (bct == GBF_BC_ZEROGRADIENT) src[ax] = nh; // [nh:nh+1]
-      else { src[ax] = 2 * nh - 1 - layer; flip = true; }  // [2nh-1:nh-1:-1]
-    } else {
-      dst[ax] = n + nh + layer;                          // [-nh:]
-      if (bct == GBF_BC_PERIODIC) src[ax] = nh + layer;  // [nh:2nh]
-      else if (bct == GBF_BC_ZEROGRADIENT) src[ax] = n + nh - 1;  // [-nh-1:-nh]
-      else { src[ax] = n + nh - 1 - layer; flip = true; }  // [-nh-1:-2nh-1:-1]
-    }
+    // logical halo coordinate of this layer and the interior cell it reads
+    const int g = hi ? n + layer : layer - nh;
+    dst[ax] = g + nh;
+    src[ax] = bc_src(g, n, bct) + nh;
     const long long so = ((long long)src[0] * hp.hs[1] + src[1]) * hp.hs[2] + src[2];
     const long long d = ((long long)dst[0] * hp.hs[1] + dst[1]) * hp.hs[2] + dst[2];
     double P[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) P[v] = prims[v * cs + so];
-    if (flip) P[ax + 1] = -P[ax + 1];
+    for (int v = 0; v < 5; ++v) P[v] = bc_apply(bct, hp.bcv[face], ax, v, prims[v * cs + so]);
 #pragma unroll
     for (int v = 0; v < 5; ++v) prims[v * cs + d] = P[v];
     if (cons) {
@@ -87,32 +79,49 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
   }
 }
 
-// All-periodic halos of every kind (faces, edges, vertices): each halo cell
-// copies the interior cell its coordinates wrap to; the halo conservatives are
-// recomputed from the copied primitives (outer/material.py:248-250, :289-379).
-__global__ void halo_wrap_kernel(const HaloParams hp, double* prims, double* cons) {
+// Edge halos (outer/material.py:289-379) of the halo buffer, after its face
+// halos: one thread per buffer cell outside the interior along exactly two
+// active axes a < b.  Type combination of boundary_condition.py:128-177 and
+// retrieve locations :606-660: the first of the two faces (axis order) that is
+// PERIODIC or SYMMETRY takes the other face's halo cell at its periodic image
+// or mirror (that axis' velocity negated); otherwise (ANY_ANY) the mean of the
+// two face-halo cells nh cells inward ('_10' then '_01' slices,
+// halo_slices.py:77-149).  Halo conservatives from the halo primitives.
+__global__ void halo_edge_kernel(const HaloParams hp, double* prims, double* cons) {
   const long long cs = (long long)hp.hs[0] * hp.hs[1] * hp.hs[2];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
        i += (long long)gridDim.x * blockDim.x) {
     int b[3] = {(int)(i / ((long long)hp.hs[1] * hp.hs[2])), (int)((i / hp.hs[2]) % hp.hs[1]),
                 (int)(i % hp.hs[2])};
-    int src[3];
-    bool halo = false;
+    int out[3], k = 0;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      src[a] = b[a];
-      if (hp.n[a] > 1) {
-        int g = b[a] - hp.nh;
-        if (g < 0) { g += hp.n[a]; halo = true; }
-        else if (g >= hp.n[a]) { g -= hp.n[a]; halo = true; }
-        src[a] = g + hp.nh;
-      }
-    }
-    if (!halo) continue;
-    const long long so = ((long long)src[0] * hp.hs[1] + src[1]) * hp.hs[2] + src[2];
+    for (int a = 0; a < 3; ++a)
+      if (hp.n[a] > 1 && (b[a] < hp.nh || b[a] >= hp.n[a] + hp.nh)) out[k++] = a;
+    if (k != 2) continue;
+    const int a0 = out[0], a1 = out[1];
+    auto lo = [&](int a) { return b[a] < hp.nh; };
+    const int t0 = hp.bc[2 * a0 + (lo(a0) ? 0 : 1)];
+    const int t1 = hp.bc[2 * a1 + (lo(a1) ? 0 : 1)];
+    auto at = [&](const int q[3]) { return ((long long)q[0] * hp.hs[1] + q[1]) * hp.hs[2] + q[2]; };
     double P[5];
+    if (t0 == GBF_BC_PERIODIC || t0 == GBF_BC_SYMMETRY || t1 == GBF_BC_PERIODIC || t1 == GBF_BC_SYMMETRY) {
+      const bool first = (t0 == GBF_BC_PERIODIC || t0 == GBF_BC_SYMMETRY);
+      const int a = first ? a0 : a1;
+      const int t = first ? t0 : t1;
+      int q[3] = {b[0], b[1], b[2]};
+      q[a] = bc_src(b[a] - hp.nh, hp.n[a], t) + hp.nh;
+      const long long so = at(q);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) P[v] = prims[v * cs + so];
+      for (int v = 0; v < 5; ++v) P[v] = prims[v * cs + so];
+      if (t == GBF_BC_SYMMETRY) P[a + 1] = -P[a + 1];
+    } else {
+      int qa[3] = {b[0], b[1], b[2]}, qb[3] = {b[0], b[1], b[2]};
+      qa[a0] += lo(a0) ? hp.nh : -hp.nh;
+      qb[a1] += lo(a1) ? hp.nh : -hp.nh;
+      const long long sa = at(qa), sb = at(qb);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) P[v] = 0.5 * (prims[v * cs + sa] + prims[v * cs + sb]);
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v) prims[v * cs + i] = P[v];
     if (cons) {
@@ -320,7 +329,10 @@ int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, doubl
     hp.hs[a] = ci.hs[a];
   }
   hp.nh = ci.nh;
-  for (int f = 0; f < 6; ++f) hp.bc[f] = c->bc[f];
+  for (int f = 0; f < 6; ++f) {
+    hp.bc[f] = c->bc[f];
+    fill_bc_constants(c, f, hp.bcv[f]);
+  }
   hp.active_mask = ci.active_mask;
   hp.gm1 = ci.fp.gm1;
   long long start = 0;
@@ -342,16 +354,17 @@ int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, doubl
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
-int launch_halo_wrap(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
-                     cudaStream_t s) {
+int launch_halo_edges(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
+                      cudaStream_t s) {
   HaloParams hp{};
   for (int a = 0; a < 3; ++a) {
     hp.n[a] = ci.n[a];
     hp.hs[a] = ci.hs[a];
   }
   hp.nh = ci.nh;
+  for (int f = 0; f < 6; ++f) hp.bc[f] = c->bc[f];
   hp.gm1 = ci.fp.gm1;
-  halo_wrap_kernel<<<grid_for(ci.halo_cells), kThreads, 0, s>>>(hp, prims, cons);
+  halo_edge_kernel<<<grid_for(ci.halo_cells), kThreads, 0, s>>>(hp, prims, cons);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 

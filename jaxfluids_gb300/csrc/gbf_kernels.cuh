@@ -21,6 +21,9 @@ struct CaseInfo {
 
 int make_case_info(const gbf_case* c, CaseInfo* ci);
 
+// per-face boundary constants for the kernels (gbf_sweep.cu)
+void fill_bc_constants(const gbf_case* c, int f, double out[5]);
+
 // fills p.{n,t,tiles,...} from the case and tile (tile null or all zero:
 // the default shape, for_vjp picking the adjoint kernel's); returns status
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
@@ -33,8 +36,9 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
 // auxiliary kernels (gbf_aux.cu)
 int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
                      cudaStream_t s);
-int launch_halo_wrap(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
-                     cudaStream_t s);
+// edge halos from the filled face halos (viscous / heat; no vertex halos)
+int launch_halo_edges(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
+                      cudaStream_t s);
 int launch_convert(const gbf_case* c, const double* in, double* out, long long count, int to_prims,
                    cudaStream_t s);
 int launch_stage_integrate(const gbf_case* c, const CaseInfo& ci, double* cons,

@@ -1,63 +1,36 @@
-// Instantiations and host launch of the sweep kernel.
+// Launch parameters of the sweep kernel and dispatch to the scheme families
+// (gbf_sweep_<family>.cu instantiate the kernels).
 #include <algorithm>
 
-#include "gbf_kernels.cuh"
+#include "gbf_sweep_launch.cuh"
 
 namespace gbf {
 
 namespace {
 
-constexpr int kMaxCellsPerThread = 4;
-
-template <int RECON>
-constexpr int recon_radius() {
-  return ReconTraits<RECON>::R;
-}
-
 int radius_of(int recon) {
   return recon == GBF_RECON_WENO5Z ? 3 : 2;
 }
 
-template <int RECON, int RIEMANN, int MODE, bool VISC>
-int launch_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  auto kern = sweep_kernel<RECON, RIEMANN, MODE, kMaxCellsPerThread, VISC>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return GBF_ERR_CUDA;
-  const int grid = p.tiles[0] * p.tiles[1] * p.tiles[2];
-  kern<<<grid, threads, smem, s>>>(p);
-  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
-}
+}  // namespace
 
-template <int RECON, int MODE, bool VISC>
-int launch_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (riemann == GBF_RIEMANN_HLLC) return launch_one<RECON, GBF_RIEMANN_HLLC, MODE, VISC>(p, threads, smem, s);
-  return launch_one<RECON, GBF_RIEMANN_RUSANOV, MODE, VISC>(p, threads, smem, s);
-}
-
-// inviscid kernels: every reconstruction
-template <int MODE>
-int launch_recon(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
-    return launch_riemann<RECON_WENO5Z_CHAR, MODE, false>(c->riemann, p, threads, smem, s);
-  switch (c->recon) {
-    case GBF_RECON_WENO5Z:
-      return launch_riemann<GBF_RECON_WENO5Z, MODE, false>(c->riemann, p, threads, smem, s);
-    case GBF_RECON_MINMOD:
-      return launch_riemann<GBF_RECON_MINMOD, MODE, false>(c->riemann, p, threads, smem, s);
-    default:
-      return launch_riemann<GBF_RECON_MINMOD_AD, MODE, false>(c->riemann, p, threads, smem, s);
+// Per-face boundary constants of the kernels, rounded as the reference rounds
+// them: WALL 2 u_wall (exact), DIRICHLET the primitives, NEUMANN
+// (gradient * sign) * dx with sign +1 at the low and -1 at the high face
+// (halos/outer/material.py:41-44, :860-861).
+void fill_bc_constants(const gbf_case* c, int f, double out[5]) {
+  const int ax = f >> 1;
+  const double sign = (f & 1) ? -1.0 : 1.0;
+  for (int v = 0; v < 5; ++v) {
+    const double x = c->bc_value[f][v];
+    switch (c->bc[f]) {
+      case GBF_BC_WALL: out[v] = 2.0 * x; break;
+      case GBF_BC_DIRICHLET: out[v] = x; break;
+      case GBF_BC_NEUMANN: out[v] = (x * sign) * c->dx[ax]; break;
+      default: out[v] = 0.0;
+    }
   }
 }
-
-// viscous / heat-conducting kernels: WENO5-Z on primitive or characteristic variables
-template <int MODE>
-int launch_recon_visc(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
-    return launch_riemann<RECON_WENO5Z_CHAR, MODE, true>(c->riemann, p, threads, smem, s);
-  return launch_riemann<GBF_RECON_WENO5Z, MODE, true>(c->riemann, p, threads, smem, s);
-}
-
-}  // namespace
 
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
                       int* threads, size_t* smem, bool for_vjp) {
@@ -100,7 +73,7 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   }
   if (thr % 32 != 0 || thr < 32 || thr > 256) return GBF_ERR_INVALID_ARGUMENT;
   const long long tvol = (long long)t[0] * t[1] * t[2];
-  if (tvol > (long long)kMaxCellsPerThread * thr) return GBF_ERR_INVALID_ARGUMENT;
+  if (tvol > (long long)kSweepMaxCellsPerThread * thr) return GBF_ERR_INVALID_ARGUMENT;
   const int R = radius_of(c->recon);
   long long pmax = 0, fmax = 0;
   for (int a = 0; a < 3; ++a) {
@@ -123,7 +96,10 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
     q.one_dx[a] = 1.0 / c->dx[a];
   }
   q.nh = ci.nh;
-  for (int f = 0; f < 6; ++f) q.bc[f] = c->bc[f];
+  for (int f = 0; f < 6; ++f) {
+    q.bc[f] = c->bc[f];
+    fill_bc_constants(c, f, q.bcv[f]);
+  }
   q.fp = ci.fp;
   q.active_mask = ci.active_mask;
   q.viscous = (c->flags & GBF_FLAG_VISCOUS) ? 1 : 0;
@@ -142,12 +118,17 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
 int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
                  int mode) {
   const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
-  if (mode == MODE_RHS)
-    return visc ? launch_recon_visc<MODE_RHS>(c, p, threads, smem, s)
-                : launch_recon<MODE_RHS>(c, p, threads, smem, s);
-  if (mode == MODE_STAGE_P) return launch_recon_visc<MODE_STAGE_P>(c, p, threads, smem, s);
-  if (visc) return GBF_ERR_UNSUPPORTED;  // dissipative fluxes need the primitive buffer
-  return launch_recon<MODE_STAGE>(c, p, threads, smem, s);
+  const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
+  if (visc) {
+    // dissipative fluxes read the primitive buffer (MODE_STAGE_P) or the halo buffer
+    if (mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
+    return chr ? launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s)
+               : launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
+  }
+  if (mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
+  if (chr) return launch_sweep_char(c->riemann, mode, p, threads, smem, s);
+  if (c->recon == GBF_RECON_WENO5Z) return launch_sweep_weno(c->riemann, mode, p, threads, smem, s);
+  return launch_sweep_muscl(c->recon, c->riemann, mode, p, threads, smem, s);
 }
 
 }  // namespace gbf

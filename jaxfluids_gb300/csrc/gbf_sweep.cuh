@@ -37,6 +37,9 @@ struct SweepParams {
   int nh;            // halo width of the halo buffer (MODE_RHS)
   int hs[3];         // halo buffer extents (MODE_RHS)
   int bc[6];         // boundary types, GBF_FACE_* order (MODE_STAGE)
+  // per-face boundary constants: WALL [1..3] = 2 u_wall, DIRICHLET [0..4] =
+  // primitives, NEUMANN [0..4] = (gradient * sign) * dx
+  double bcv[6][5];
   double one_dx[3];  // 1 / dx per axis
   FaceParams fp;
   const double* prims_halo;  // MODE_RHS input
@@ -58,9 +61,123 @@ struct SweepParams {
   double R;                  // specific gas constant
 };
 
+// Boundary rule of one face (halos/outer/material.py:140-210 with the
+// retrieve slices of halos/outer/boundary_condition.py:539-604): bc_src is
+// the interior index along the face's axis that halo coordinate g reads
+// (PERIODIC image, SYMMETRY/WALL mirror: halo layer j <- interior cell j,
+// ZEROGRADIENT/NEUMANN boundary cell; DIRICHLET reads nothing), bc_apply the
+// value of primitive v from the retrieved value x.
+__device__ __forceinline__ int bc_src(int g, int n, int type) {
+  if (g < 0) {
+    if (type == GBF_BC_PERIODIC) return g + n;
+    if (type == GBF_BC_SYMMETRY || type == GBF_BC_WALL) return -1 - g;
+    return 0;
+  }
+  if (type == GBF_BC_PERIODIC) return g - n;
+  if (type == GBF_BC_SYMMETRY || type == GBF_BC_WALL) return 2 * n - 1 - g;
+  return n - 1;
+}
+
+__device__ __forceinline__ double bc_apply(int type, const double* bcv, int ax, int v, double x) {
+  switch (type) {
+    case GBF_BC_SYMMETRY:
+      return (v == ax + 1) ? -x : x;
+    case GBF_BC_WALL:  // 2 u_wall - u (material.py:511-513), 2 u_wall precomputed exactly
+      return (v >= 1 && v <= 3) ? bcv[v] - x : x;
+    case GBF_BC_DIRICHLET:
+      return bcv[v];
+    case GBF_BC_NEUMANN:  // P + (g sign) dx (material.py:860-862)
+      return x + bcv[v];
+    default:
+      return x;
+  }
+}
+
+// d bc_apply / d x (the adjoint's boundary transpose)
+__device__ __forceinline__ double bc_apply_grad(int type, int ax, int v) {
+  switch (type) {
+    case GBF_BC_SYMMETRY:
+      return (v == ax + 1) ? -1.0 : 1.0;
+    case GBF_BC_WALL:
+      return (v >= 1 && v <= 3) ? -1.0 : 1.0;
+    case GBF_BC_DIRICHLET:
+      return 0.0;
+    default:
+      return 1.0;
+  }
+}
+
+__device__ __forceinline__ int idx3(int i0, int i1, int i2, int e1, int e2) {
+  return (i0 * e1 + i1) * e2 + i2;
+}
+
+// Primitive v of an interior cell of the interior primitive buffer.
+__device__ __forceinline__ double interior_prim(const SweepParams& p, int v, const int g[3]) {
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  return __ldg(p.prims + v * cs + ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2]);
+}
+
+// Primitive v of a cell outside along axis a only: the face rule of that face.
+__device__ __forceinline__ double face_halo_prim(const SweepParams& p, int v, int a, int g[3]) {
+  const int f = 2 * a + (g[a] >= 0 ? 1 : 0);
+  const int t = p.bc[f];
+  const int ga = g[a];
+  g[a] = bc_src(ga, p.n[a], t);
+  const double x = (t == GBF_BC_DIRICHLET) ? 0.0 : interior_prim(p, v, g);
+  g[a] = ga;
+  return bc_apply(t, p.bcv[f], a, v, x);
+}
+
 // Primitive v of the logical cell (g0, g1, g2), which may lie up to nh cells
-// outside the interior: read from the halo buffer (MODE_RHS) or, with
-// periodic wrapping on every axis, from the interior primitive buffer.
+// outside the interior along one or two axes: read from the halo buffer
+// (MODE_RHS), or from the interior primitive buffer through the face rules
+// and, for edge cells, the edge rule of compute_edge_halos
+// (outer/material.py:339-379, type combinations boundary_condition.py:128-177,
+// :606-660): along the edge's faces in axis order the first PERIODIC or
+// SYMMETRY face maps the cell onto the other face's halo (periodic image, or
+// mirror with that axis' velocity negated); otherwise the mean of the two face
+// halos nh cells inward.
+// Primitive v of a logical cell outside the interior along one or two axes,
+// from the interior primitive buffer: the face rule, and for edge cells the
+// edge rule of compute_edge_halos (outer/material.py:339-379, type
+// combinations boundary_condition.py:128-177, :606-660): along the edge's
+// faces in axis order the first PERIODIC or SYMMETRY face maps the cell onto
+// the other face's halo (periodic image, or mirror with that axis' velocity
+// negated); otherwise the mean of the two face halos nh cells inward.  Kept
+// out of line: only tiles on the domain boundary reach it, and inlining it
+// costs the interior path registers.
+static __device__ __noinline__ double halo_prim(const SweepParams& p, int v, int g0, int g1, int g2) {
+  int g[3] = {g0, g1, g2};
+  int out[3], k = 0;
+  for (int a = 0; a < 3; ++a)
+    if (g[a] < 0 || g[a] >= p.n[a]) out[k++] = a;
+  if (k == 1) return face_halo_prim(p, v, out[0], g);
+  const int a = out[0], b = out[1];
+  const int ta = p.bc[2 * a + (g[a] >= 0 ? 1 : 0)];
+  const int tb = p.bc[2 * b + (g[b] >= 0 ? 1 : 0)];
+  if (ta == GBF_BC_PERIODIC || ta == GBF_BC_SYMMETRY) {
+    g[a] = bc_src(g[a], p.n[a], ta);
+    const double x = face_halo_prim(p, v, b, g);
+    return (ta == GBF_BC_SYMMETRY && v == a + 1) ? -x : x;
+  }
+  if (tb == GBF_BC_PERIODIC || tb == GBF_BC_SYMMETRY) {
+    g[b] = bc_src(g[b], p.n[b], tb);
+    const double x = face_halo_prim(p, v, a, g);
+    return (tb == GBF_BC_SYMMETRY && v == b + 1) ? -x : x;
+  }
+  // ANY_ANY: 0.5 * (edge '_10' + edge '_01')
+  int ga[3] = {g[0], g[1], g[2]};
+  ga[a] += (g[a] < 0) ? p.nh : -p.nh;
+  const double A = face_halo_prim(p, v, b, ga);
+  int gb[3] = {g[0], g[1], g[2]};
+  gb[b] += (g[b] < 0) ? p.nh : -p.nh;
+  const double B = face_halo_prim(p, v, a, gb);
+  return 0.5 * (A + B);
+}
+
+// Primitive v of the logical cell (g0, g1, g2), which may lie up to nh cells
+// outside the interior (face or edge halo): read from the halo buffer
+// (MODE_RHS) or from the interior primitive buffer through halo_prim.
 template <int MODE>
 __device__ __forceinline__ double global_prim(const SweepParams& p, int v, int g0, int g1, int g2) {
   if (MODE == MODE_RHS) {
@@ -70,36 +187,14 @@ __device__ __forceinline__ double global_prim(const SweepParams& p, int v, int g
     const long long cs = (long long)p.hs[0] * p.hs[1] * p.hs[2];
     return __ldg(p.prims_halo + v * cs + ((long long)b0 * p.hs[1] + b1) * p.hs[2] + b2);
   } else {
-    g0 = (g0 < 0) ? g0 + p.n[0] : ((g0 >= p.n[0]) ? g0 - p.n[0] : g0);
-    g1 = (g1 < 0) ? g1 + p.n[1] : ((g1 >= p.n[1]) ? g1 - p.n[1] : g1);
-    g2 = (g2 < 0) ? g2 + p.n[2] : ((g2 >= p.n[2]) ? g2 - p.n[2] : g2);
-    const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
-    return __ldg(p.prims + v * cs + ((long long)g0 * p.n[1] + g1) * p.n[2] + g2);
+    const bool inside = (unsigned)g0 < (unsigned)p.n[0] && (unsigned)g1 < (unsigned)p.n[1] &&
+                        (unsigned)g2 < (unsigned)p.n[2];
+    if (inside) {
+      const int g[3] = {g0, g1, g2};
+      return interior_prim(p, v, g);
+    }
+    return halo_prim(p, v, g0, g1, g2);
   }
-}
-
-__device__ __forceinline__ int idx3(int i0, int i1, int i2, int e1, int e2) {
-  return (i0 * e1 + i1) * e2 + i2;
-}
-
-// Boundary index remap along one axis for a logical cell coordinate g that may
-// lie in the halo (g < 0 or g >= n); returns the interior cell and whether the
-// normal velocity flips sign (halos/outer/boundary_condition.py:539-604).
-__device__ __forceinline__ int remap_bc(int g, int n, int bc_lo, int bc_hi, bool& flip) {
-  flip = false;
-  if (g < 0) {
-    if (bc_lo == GBF_BC_PERIODIC) return g + n;
-    if (bc_lo == GBF_BC_ZEROGRADIENT) return 0;
-    flip = true;           // SYMMETRY: halo layer j mirrors interior cell j
-    return -1 - g;
-  }
-  if (g >= n) {
-    if (bc_hi == GBF_BC_PERIODIC) return g - n;
-    if (bc_hi == GBF_BC_ZEROGRADIENT) return n - 1;
-    flip = true;
-    return 2 * n - 1 - g;
-  }
-  return g;
 }
 
 // Orders non-negative doubles as unsigned integers (for atomicMax).
@@ -224,8 +319,14 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
 #pragma unroll
       for (int v = 0; v < 5; ++v) P[v] = __ldg(p.prims_halo + v * cs + off);
     } else {
-      bool flip;
-      g[AX] = remap_bc(g[AX], p.n[AX], p.bc[2 * AX], p.bc[2 * AX + 1], flip);
+      // halo cells along AX: the face rule applied to the primitives of the
+      // retrieved interior cell (halo prims from interior prims, as the
+      // reference's halo update after prims_from_cons over the buffer)
+      const int ga = g[AX];
+      const bool halo = ga < 0 || ga >= p.n[AX];
+      const int f = 2 * AX + (ga >= 0 ? 1 : 0);
+      const int t = halo ? p.bc[f] : -1;
+      if (halo) g[AX] = bc_src(ga, p.n[AX], t);
       const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
       const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
       if (MODE == MODE_STAGE_P) {
@@ -237,7 +338,10 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
         for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
         prims_from_cons(U, P, p.fp.gm1);
       }
-      if (flip) P[AX + 1] = -P[AX + 1];
+      if (halo) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) P[v] = bc_apply(t, p.bcv[f], AX, v, P[v]);
+      }
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_prim[v * pvol + i] = P[v];

@@ -1,0 +1,37 @@
+// Host launch templates of the sweep kernel, shared by the translation units
+// that instantiate one scheme family each (compiled in parallel).
+#pragma once
+
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+constexpr int kSweepMaxCellsPerThread = 4;
+
+template <int RECON, int RIEMANN, int MODE, bool VISC>
+int launch_sweep_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  auto kern = sweep_kernel<RECON, RIEMANN, MODE, kSweepMaxCellsPerThread, VISC>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return GBF_ERR_CUDA;
+  const int grid = p.tiles[0] * p.tiles[1] * p.tiles[2];
+  kern<<<grid, threads, smem, s>>>(p);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+template <int RECON, int MODE, bool VISC>
+int launch_sweep_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  if (riemann == GBF_RIEMANN_HLLC) return launch_sweep_one<RECON, GBF_RIEMANN_HLLC, MODE, VISC>(p, threads, smem, s);
+  return launch_sweep_one<RECON, GBF_RIEMANN_RUSANOV, MODE, VISC>(p, threads, smem, s);
+}
+
+// One entry per scheme family (gbf_sweep_<family>.cu); mode is MODE_RHS or
+// MODE_STAGE for the inviscid families, MODE_RHS or MODE_STAGE_P for the
+// viscous ones.
+int launch_sweep_weno(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_weno_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_char(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_char_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_muscl(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                       cudaStream_t s);
+
+}  // namespace gbf

@@ -68,6 +68,10 @@ class OracleCase:
     bulk_viscosity: float = 0.0
     prandtl: Optional[float] = None
     viscous_heat_production: bool = True
+    # constant boundary values per face: WALL (u, v, w) wall velocity
+    # (wall_velocity_callable), DIRICHLET (rho, u, v, w, p)
+    # (primitives_callable), NEUMANN (rho, u, v, w, p) normal derivatives
+    bc_values: Dict[str, Tuple[float, ...]] = field(default_factory=dict)
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -601,9 +605,9 @@ def _face_retrieve_slice(case: OracleCase, face: str, btype: str) -> Tuple[slice
     hi = face in ("east", "north", "top")
     if btype == "PERIODIC":
         s = slice(nh, 2 * nh) if hi else slice(-2 * nh, -nh)
-    elif btype == "ZEROGRADIENT":
+    elif btype in ("ZEROGRADIENT", "NEUMANN"):
         s = slice(-nh - 1, -nh) if hi else slice(nh, nh + 1)
-    elif btype == "SYMMETRY":
+    elif btype in ("SYMMETRY", "WALL"):
         # reference: [-nh-1:-2nh-1:-1] (hi) and [2nh-1:nh-1:-1] (lo); torch has no
         # negative steps, so return the forward slice and let the caller flip it
         s = slice(-2 * nh, -nh) if hi else slice(nh, 2 * nh)
@@ -612,12 +616,48 @@ def _face_retrieve_slice(case: OracleCase, face: str, btype: str) -> Tuple[slice
     return _axis_slice(case, axis, s)
 
 
+# UPWIND DIRECTION FOR NEUMANN DERIVATIVE STENCIL (outer/material.py:41-44)
+NEUMANN_SIGN = {"east": -1, "west": 1, "north": -1, "south": 1, "top": -1, "bottom": 1}
+
+
+def _face_halo(P: Tensor, case: OracleCase, face: str, btype: str) -> Tensor:
+    """Halo primitives of one face (outer/material.py:140-210): miscellaneous
+    (:868-894) for PERIODIC / SYMMETRY / ZEROGRADIENT, wall (:473-531),
+    dirichlet (:732-798, constant callables), neumann (:825-866)."""
+    axis = FACE_AXIS[face]
+    fill_shape = P[_face_fill_slice(case, face)].shape
+    if btype == "DIRICHLET":
+        vals = torch.tensor([float(x) for x in case.bc_values[face]], dtype=P.dtype).reshape(5, 1, 1, 1)
+        return vals.expand(fill_shape).clone()
+    h = P[_face_retrieve_slice(case, face, btype)].clone()
+    if btype in ("SYMMETRY", "WALL"):
+        h = torch.flip(h, dims=(axis + 1,))
+    if btype == "SYMMETRY":
+        sign = torch.ones(5, dtype=P.dtype).reshape(5, 1, 1, 1)
+        sign[axis + 1] = -1.0
+        h = h * sign
+    elif btype == "WALL":
+        # u_halo = 2 u_wall - u_mirror for every velocity component (:511-513)
+        uw = [2 * float(x) for x in case.bc_values[face]]
+        h = torch.cat([h[0:1], uw[0] - h[1:2], uw[1] - h[2:3], uw[2] - h[3:4], h[4:5]])
+    elif btype == "NEUMANN":
+        # neumann_value *= sign; neumann_value *= dx; halo = P + neumann_value (:860-862)
+        dx = case.cell_size(axis)
+        off = torch.tensor([(float(g) * NEUMANN_SIGN[face]) * dx for g in case.bc_values[face]],
+                           dtype=P.dtype).reshape(5, 1, 1, 1)
+        h = h + off
+    if h.shape != fill_shape:  # one retrieved layer fills all nh layers
+        h = h.expand(fill_shape).clone()
+    return h
+
+
 def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tensor, Optional[Tensor]]:
     """HaloManager.perform_halo_update_material, face halos (outer/material.py:94-287).
 
-    Halo primitives are copied (or mirrored) from the interior; halo
-    conservatives are recomputed from the halo primitives (:248-250).  The
-    reference writes them as ``x.at[fill].mul(0).add(h)``, i.e. a plain set.
+    Halo primitives follow each face's boundary rule; halo conservatives are
+    recomputed from the halo primitives (:248-250).  The reference writes
+    them as ``x.at[fill].mul(0).add(h)``, i.e. a plain set.  Edge halos
+    follow when viscous or heat fluxes are on (halo_manager.py:126-129).
     """
     P = P.clone()
     U = U.clone() if U is not None else None
@@ -625,17 +665,7 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
         axis = FACE_AXIS[face]
         if axis not in case.active:
             continue
-        btype = case.bc[face]
-        h = P[_face_retrieve_slice(case, face, btype)].clone()
-        if btype == "ZEROGRADIENT":
-            reps = [1] * 4
-            reps[axis + 1] = case.nh
-            h = h.repeat(*reps)
-        if btype == "SYMMETRY":
-            h = torch.flip(h, dims=(axis + 1,))
-            sign = torch.ones(5, dtype=P.dtype).reshape(5, 1, 1, 1)
-            sign[axis + 1] = -1.0
-            h = h * sign
+        h = _face_halo(P, case, face, case.bc[face])
         fill = _face_fill_slice(case, face)
         P[fill] = h
         if U is not None:
@@ -645,37 +675,75 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
     return P, U
 
 
-def edge_halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase):
-    """Edge halos for all-PERIODIC boundaries (outer/material.py:289-379).
+def _rows(case: OracleCase, axis: int, kind: str, hi: bool) -> slice:
+    """Buffer rows along `axis` (halo_slices.py:77-149 edge slices, in
+    logical terms): the halo layers of one side, their periodic images, the
+    interior rows a symmetry mirrors them from (forward order; the caller
+    flips), or the interior rows nh cells inward (the '_10' / '_01' slices)."""
+    n, nh = case.cells[axis], case.nh
+    if kind == "halo":
+        return slice(n + nh, n + 2 * nh) if hi else slice(0, nh)
+    if kind == "wrap":
+        return slice(nh, 2 * nh) if hi else slice(n, n + nh)
+    if kind in ("mirror", "shift"):
+        return slice(n, n + nh) if hi else slice(nh, 2 * nh)
+    raise ValueError(kind)
 
-    For PERIODIC_PERIODIC edges the retrieve location is the opposite edge, which
-    is the same as wrapping each index independently.
+
+def edge_halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase):
+    """MaterialBoundaryCondition.edge_halo_update / compute_edge_halos
+    (outer/material.py:289-379) with the type combinations of
+    boundary_condition.py:128-177 and :606-660: along the edge's faces in
+    axis order, the first PERIODIC or SYMMETRY face decides (its periodic
+    image, or its mirror with that axis' velocity negated, of the other
+    face's halo); otherwise (ANY_ANY) the mean of the two face halos nh
+    cells inward.  Vertex halos are not filled (single phase,
+    halo_manager.py:131-143); conservatives are recomputed for the edge
+    cells only.
     """
-    for f in FACES:
-        if FACE_AXIS[f] in case.active and case.bc[f] != "PERIODIC":
-            raise NotImplementedError("edge halos are restated for PERIODIC boundaries only")
-    nh = case.nh
     P = P.clone()
-    for axis in case.active:
-        n = case.cells[axis]
-        # wrap along axis over the full extent of the other axes
-        sl_lo = [slice(None)] * 4
-        sl_hi = [slice(None)] * 4
-        src_lo = [slice(None)] * 4
-        src_hi = [slice(None)] * 4
-        sl_lo[axis + 1] = slice(0, nh)
-        src_lo[axis + 1] = slice(n, n + nh)
-        sl_hi[axis + 1] = slice(n + nh, n + 2 * nh)
-        src_hi[axis + 1] = slice(nh, 2 * nh)
-        P[tuple(sl_lo)] = P[tuple(src_lo)]
-        P[tuple(sl_hi)] = P[tuple(src_hi)]
-    if U is not None:
-        U = U.clone()
-        # recompute conservatives in every halo cell (interior untouched)
-        full = cons_from_prims(P, case.gamma)
-        mask = torch.ones(P.shape[1:], dtype=torch.bool)
-        mask[tuple(case.inner(i) for i in range(3))] = False
-        U[:, mask] = full[:, mask]
+    U = U.clone() if U is not None else None
+    act = case.active
+    for ia in range(len(act)):
+        for ib in range(ia + 1, len(act)):
+            a, b = act[ia], act[ib]
+            c = [i for i in range(3) if i not in (a, b)][0]
+            for hia in (False, True):
+                for hib in (False, True):
+                    fa = AXIS_FACES[a][1 if hia else 0]
+                    fb = AXIS_FACES[b][1 if hib else 0]
+                    ta, tb = case.bc[fa], case.bc[fb]
+
+                    def block(ra, rb):
+                        sl = [slice(None)] * 4
+                        sl[a + 1], sl[b + 1], sl[c + 1] = ra, rb, case.inner(c)
+                        return tuple(sl)
+
+                    target = block(_rows(case, a, "halo", hia), _rows(case, b, "halo", hib))
+                    if ta in ("PERIODIC", "SYMMETRY"):
+                        ax, t, hi_ = a, ta, hia
+                        src_blk = block(_rows(case, a, "wrap" if ta == "PERIODIC" else "mirror", hia),
+                                        _rows(case, b, "halo", hib))
+                    elif tb in ("PERIODIC", "SYMMETRY"):
+                        ax, t, hi_ = b, tb, hib
+                        src_blk = block(_rows(case, a, "halo", hia),
+                                        _rows(case, b, "wrap" if tb == "PERIODIC" else "mirror", hib))
+                    else:
+                        t = "ANY"
+                    if t == "ANY":
+                        A = P[block(_rows(case, a, "shift", hia), _rows(case, b, "halo", hib))]
+                        B = P[block(_rows(case, a, "halo", hia), _rows(case, b, "shift", hib))]
+                        h = 0.5 * (A + B)
+                    else:
+                        h = P[src_blk].clone()
+                        if t == "SYMMETRY":
+                            h = torch.flip(h, dims=(ax + 1,))
+                            sign = torch.ones(5, dtype=P.dtype).reshape(5, 1, 1, 1)
+                            sign[ax + 1] = -1.0
+                            h = h * sign
+                    P[target] = h
+                    if U is not None:
+                        U[target] = cons_from_prims(h, case.gamma)
     return P, U
 
 

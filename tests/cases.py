@@ -14,7 +14,8 @@ def both(cells, bc, **kw):
     oc = O.OracleCase(cells=cells, bc=bcd, **kw)
     fields = {k: v for k, v in kw.items() if k in (
         "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
-        "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "viscous_heat_production")}
+        "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "viscous_heat_production",
+        "bc_values")}
     cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
     return oc, cc
 

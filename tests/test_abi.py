@@ -30,7 +30,8 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_version_and_status_strings(lib):
-    assert lib.gbf_abi_version() == 1
+    from jaxfluids_gb300 import _lib
+    assert lib.gbf_abi_version() == _lib.ABI_VERSION == 2
     assert lib.gbf_status_string(0) == b"ok"
     assert lib.gbf_status_string(-2) == b"unsupported setup"
 

@@ -1,0 +1,72 @@
+"""Boundary conditions read from the reference's case_setup dictionaries
+(input/case_setup/read_boundary_conditions.py layout) into the C descriptor."""
+import pytest
+
+from jaxfluids_gb300 import _lib
+from jaxfluids_gb300.config import CaseConfig, SetupError
+
+
+def _setup(bcs, cells=(32, 24, 1)):
+    case = {
+        "domain": {a: {"cells": n, "range": [0.0, 1.0]} for a, n in zip("xyz", cells)},
+        "boundary_conditions": bcs,
+        "material_properties": {"equation_of_state": {"model": "IdealGas", "specific_heat_ratio": 1.4,
+                                                      "specific_gas_constant": 1.0}},
+    }
+    num = {"conservatives": {"halo_cells": 4, "time_integration": {"integrator": "RK3", "CFL": 0.5}}}
+    return case, num
+
+
+def test_cavity_walls_and_lid_velocity():
+    wall = {"type": "WALL", "wall_velocity_callable": {"u": 0.0, "v": 0.0, "w": 0.0}}
+    lid = {"type": "WALL", "wall_velocity_callable": {"u": 5e-1, "v": 0.0, "w": 0.0}}
+    case, num = _setup({"east": wall, "west": wall, "north": lid, "south": wall,
+                        "top": {"type": "INACTIVE"}, "bottom": {"type": "INACTIVE"}})
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.bc["north"] == "WALL" and cfg.bc_values["north"] == (0.5, 0.0, 0.0)
+    c = cfg.to_c()
+    k = _lib.FACE_ORDER.index("north")
+    assert c.bc[k] == _lib.BC["WALL"]
+    assert list(c.bc_value[k]) == [0.0, 0.5, 0.0, 0.0, 0.0]
+
+
+def test_dirichlet_inflow_and_neumann_outflow():
+    inflow = {"type": "DIRICHLET", "primitives_callable": {"rho": 8.0, "u": 7.144709581221618, "v": -4.125,
+                                                           "w": 0.0, "p": 116.5}}
+    outflow = {"type": "NEUMANN", "primitives_callable": {"rho": 0.0, "u": "0.5", "v": 0.0, "w": 0.0, "p": 0.0}}
+    case, num = _setup({"west": inflow, "east": outflow, "north": {"type": "ZEROGRADIENT"},
+                        "south": [{"type": "SYMMETRY"}], "top": {"type": "INACTIVE"},
+                        "bottom": {"type": "INACTIVE"}})
+    cfg = CaseConfig.from_setups(case, num)
+    c = cfg.to_c()
+    w, e = _lib.FACE_ORDER.index("west"), _lib.FACE_ORDER.index("east")
+    assert list(c.bc_value[w]) == [8.0, 7.144709581221618, -4.125, 0.0, 116.5]
+    assert c.bc[e] == _lib.BC["NEUMANN"] and list(c.bc_value[e]) == [0.0, 0.5, 0.0, 0.0, 0.0]
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
+
+
+def test_varying_callables_and_mixed_faces_are_rejected():
+    f = {"type": "DIRICHLET", "primitives_callable": {"rho": "lambda x, t: 1.0 + x", "u": 0.0, "v": 0.0,
+                                                      "w": 0.0, "p": 1.0}}
+    case, num = _setup({"west": f, "east": {"type": "ZEROGRADIENT"}, "north": {"type": "ZEROGRADIENT"},
+                        "south": {"type": "ZEROGRADIENT"}})
+    with pytest.raises(NotImplementedError, match="constant"):
+        CaseConfig.from_setups(case, num)
+    mixed = [{"type": "DIRICHLET", "primitives_callable": {"rho": 1.0, "u": 0.0, "v": 0.0, "w": 0.0, "p": 1.0},
+              "bounding_domain": "lambda x: x < 0.5"}, {"type": "SYMMETRY", "bounding_domain": "lambda x: x >= 0.5"}]
+    case, num = _setup({"west": {"type": "ZEROGRADIENT"}, "east": {"type": "ZEROGRADIENT"},
+                        "north": {"type": "ZEROGRADIENT"}, "south": mixed})
+    with pytest.raises(NotImplementedError, match="multiple"):
+        CaseConfig.from_setups(case, num)
+
+
+def test_wall_needs_its_velocity():
+    with pytest.raises(SetupError):
+        CaseConfig(cells=(16, 1, 1), bc={"west": "WALL", "east": "ZEROGRADIENT"})
+
+
+def test_viscous_walls_accepted_by_the_library():
+    cfg = CaseConfig(cells=(16, 16, 1), nh=4, viscous=True, heat=True, mu=0.01, prandtl=0.71,
+                     bc={f: "WALL" for f in ("east", "west", "north", "south")},
+                     bc_values={f: (0.0, 0.0, 0.0) for f in ("east", "west", "north", "south")})
+    assert _lib.load().gbf_case_check(cfg.to_c()) == _lib.GBF_OK

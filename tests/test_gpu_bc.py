@@ -1,0 +1,174 @@
+"""WALL, DIRICHLET and NEUMANN boundaries (halos/outer/material.py:473-866) and
+the edge halos of the dissipative fluxes (:289-379) on the CUDA path against
+the oracle: right-hand side bitwise, halo buffers bitwise, RK3 steps through
+the drop-in and fused paths, and the inviscid adjoint."""
+import math
+
+import pytest
+import torch
+
+from oracle import jf_oracle as O
+from tests.cases import both, quadrant_prims, rel_err, sod_prims, tgv_prims
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+STEP_TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from jaxfluids_gb300 import build
+    build.build()
+
+
+def _faces(x=None, y=None, z=None):
+    bc = {}
+    for (lo, hi), t in ((("west", "east"), x), (("south", "north"), y), (("bottom", "top"), z)):
+        if t is None:
+            t = ("PERIODIC", "PERIODIC")
+        bc[lo], bc[hi] = t
+    return bc
+
+
+IN_STATE = (1.2, 0.3, 0.1, 0.0, 1.1)
+GRAD = (0.1, -0.2, 0.05, 0.0, 0.3)
+VISC = {"nh": 4, "viscous": True, "heat": True, "mu": 0.02, "prandtl": 0.71}
+
+# (name, cells, bc, bc_values, scheme keywords, initial condition)
+BC_CASES = [
+    ("1d-dirichlet-neumann", (100, 1, 1), _faces(x=("DIRICHLET", "NEUMANN")),
+     {"west": (1.0, 0.0, 0.0, 0.0, 1.0), "east": GRAD}, {}, "sod"),
+    ("2d-dirichlet-neumann-wall", (40, 32, 1), _faces(x=("DIRICHLET", "NEUMANN"), y=("WALL", "WALL")),
+     {"west": IN_STATE, "east": GRAD, "south": (0.0, 0.0, 0.0), "north": (0.4, 0.0, 0.0)}, {}, "quad"),
+    ("2d-wall-sym-minmod-rusanov", (36, 28, 1), _faces(x=("WALL", "WALL"), y=("SYMMETRY", "SYMMETRY")),
+     {"west": (0.0, 0.2, 0.0), "east": (0.0, -0.1, 0.0)}, {"nh": 4, "recon": "MINMOD", "riemann": "RUSANOV"},
+     "quad"),
+    ("2d-char-roe-dirichlet-wall", (32, 36, 1), _faces(x=("NEUMANN", "DIRICHLET"), y=("WALL", "ZEROGRADIENT")),
+     {"west": GRAD, "east": IN_STATE, "south": (0.1, 0.0, 0.0)},
+     {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "quad"),
+    ("2d-cavity-viscous-heat", (32, 32, 1), _faces(x=("WALL", "WALL"), y=("WALL", "WALL")),
+     {"west": (0.0, 0.0, 0.0), "east": (0.0, 0.0, 0.0), "south": (0.0, 0.0, 0.0), "north": (0.5, 0.0, 0.0)},
+     dict(VISC), "quad"),
+    ("3d-viscous-periodic-wall-zg", (16, 12, 14), _faces(y=("WALL", "WALL"), z=("ZEROGRADIENT", "ZEROGRADIENT")),
+     {"south": (0.0, 0.0, 0.0), "north": (0.3, 0.0, 0.1)}, dict(VISC), "tgv"),
+    ("3d-char-roe-viscous-sym-neumann-dirichlet-wall", (12, 14, 16),
+     _faces(x=("SYMMETRY", "SYMMETRY"), y=("NEUMANN", "DIRICHLET"), z=("WALL", "WALL")),
+     {"south": GRAD, "north": (1.0, 0.1, 0.0, 0.05, 72.0), "bottom": (0.0, 0.0, 0.0), "top": (0.2, -0.1, 0.0)},
+     dict(VISC, recon_var="CHAR-PRIMITIVE", frozen_state="ROE", mu=1.0 / 1600), "tgv"),
+    ("3d-viscous-noheatprod-wall-neumann", (14, 12, 12),
+     _faces(x=("WALL", "NEUMANN"), y=("ZEROGRADIENT", "WALL"), z=("SYMMETRY", "SYMMETRY")),
+     {"west": (0.0, 0.1, 0.0), "east": GRAD, "north": (0.2, 0.0, 0.0)},
+     dict(VISC, viscous_heat_production=False), "tgv"),
+]
+
+
+def _prims(kind, cells):
+    if kind == "sod":
+        return sod_prims(cells[0])
+    if kind == "quad":
+        return quadrant_prims(cells[0], cells[1], seed=cells[0] + 1)
+    n = max(cells)
+    full = tgv_prims(n)
+    return full[:, :cells[0], :cells[1], :cells[2]].contiguous()
+
+
+def _case(name):
+    for c in BC_CASES:
+        if c[0] == name:
+            return c
+    raise KeyError(name)
+
+
+IDS = [c[0] for c in BC_CASES]
+
+
+@pytest.mark.parametrize("name", IDS)
+def test_bc_rhs_bitwise(name):
+    from jaxfluids_gb300 import SimulationManager
+    _, cells, bc, vals, kw, kind = _case(name)
+    oc, cc = both(cells, bc, bc_values=vals, **kw)
+    U, P = O.initialize(_prims(kind, cells), oc)
+    ref = O.compute_rhs(U, P, oc)
+    sim = SimulationManager(cc)
+    rhs = sim.space_solver.compute_rhs(U.cuda(), P.cuda(), None, 0.0, 0.0)[0].euler_buffers.conservatives
+    assert rel_err(rhs, ref) <= RHS_TOL
+    assert torch.equal(rhs.cpu(), ref)
+
+
+@pytest.mark.parametrize("name", IDS)
+def test_bc_halo_fill_bitwise(name):
+    """Face halos of every face (and edge halos of the dissipative cases)."""
+    from jaxfluids_gb300 import SimulationManager
+    _, cells, bc, vals, kw, kind = _case(name)
+    oc, cc = both(cells, bc, bc_values=vals, **kw)
+    prims = _prims(kind, cells)
+    U, P = O.initialize(prims, oc)
+    Ug, Pg = SimulationManager(cc).initialize(prims.cuda())
+    assert torch.equal(Pg.cpu(), P)
+    assert torch.equal(Ug.cpu(), U)
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["drop-in", "fused"])
+@pytest.mark.parametrize("name", IDS)
+def test_bc_steps(name, fused):
+    from jaxfluids_gb300 import FusedRK3, SimulationManager
+    _, cells, bc, vals, kw, kind = _case(name)
+    oc, cc = both(cells, bc, bc_values=vals, **kw)
+    U, P = O.initialize(_prims(kind, cells), oc)
+    steps = 5
+    Ur, Pr = U, P
+    for _ in range(steps):
+        Ur, Pr = O.rk3_step(Ur, Pr, O.compute_dt(Pr, oc), oc)
+    inner = oc.interior()
+    if fused:
+        f = FusedRK3(cc)
+        f.set_state(U[inner].contiguous().cuda())
+        f.advance(steps)
+        out = f.cons
+    else:
+        sim = SimulationManager(cc)
+        Ug, Pg = U.cuda(), P.cuda()
+        for _ in range(steps):
+            Ug, Pg = sim.do_integration_step(Ug, Pg, sim.compute_time_step_size(Pg))
+        out = Ug[inner]
+    assert rel_err(out, Ur[inner]) <= STEP_TOL
+
+
+ADJ_CASES = [c for c in IDS if not c.startswith(("2d-cavity", "3d-viscous", "3d-char-roe-viscous"))]
+
+
+@pytest.mark.parametrize("name", ADJ_CASES)
+def test_bc_rhs_vjp_matches_oracle_autograd(name):
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    _, cells, bc, vals, kw, kind = _case(name)
+    oc, cc = both(cells, bc, bc_values=vals, **kw)
+    if cc.recon == "MINMOD":
+        pytest.skip("the adjoint is built for MINMOD-AD, not MINMOD")
+    U, P = O.initialize(_prims(kind, cells), oc)
+    Ui = U[oc.interior()].clone()
+    g = torch.Generator().manual_seed(21)
+    Ui = Ui * (1 + 1e-2 * torch.rand(Ui.shape, generator=g, dtype=torch.float64))
+    if cells[1] == 1:
+        Ui[2] = 0.0
+    if cells[2] == 1:
+        Ui[3] = 0.0
+    w = torch.randn(Ui.shape, generator=torch.Generator().manual_seed(22), dtype=torch.float64)
+    x = Ui.clone().requires_grad_(True)
+    (O.rhs_of_interior_cons(x, oc) * w).sum().backward()
+    adj = AdjointRK3(cc, dt=1e-3)
+    gv = adj.rhs_vjp(Ui.cuda().contiguous(), w.cuda().contiguous())
+    assert rel_err(gv, x.grad) <= 1e-11
+
+
+def test_viscous_adjoint_rejects_non_periodic_boundaries():
+    from jaxfluids_gb300 import _lib
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    _, cells, bc, vals, kw, kind = _case("2d-cavity-viscous-heat")
+    oc, cc = both(cells, bc, bc_values=vals, **kw)
+    adj = AdjointRK3(cc, dt=1e-3)
+    U = torch.ones((5,) + cells, dtype=torch.float64, device="cuda")
+    with pytest.raises(_lib.GbfError, match="unsupported"):
+        adj.rhs_vjp(U, U)
