@@ -408,8 +408,8 @@ def main():
     ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "adjoint", "viscous-adjoint"])
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=None, help="default 1000 (KH), 200 (viscous TGV)")
-    ap.add_argument("--adj-slots", type=int, default=4, help="binomial checkpoint slots (viscous adjoint)")
-    ap.add_argument("--adj-leaf", type=int, default=50,
+    ap.add_argument("--adj-slots", type=int, default=2, help="binomial checkpoint slots (viscous adjoint)")
+    ap.add_argument("--adj-leaf", type=int, default=100,
                     help="binomial: longest segment replayed once with its stage states kept (viscous adjoint)")
     ap.add_argument("--adj-every", type=int, default=50)
     ap.add_argument("--adj-schedule", default="stored", choices=["stored", "uniform", "binomial"])
