@@ -42,6 +42,9 @@ extern "C" {
 #define GBF_RECON_WENO5Z 0
 #define GBF_RECON_MINMOD 1
 #define GBF_RECON_MINMOD_AD 2
+#define GBF_RECON_WENO5JS 3   /* weno/weno5_js.py */
+#define GBF_RECON_WENO3JS 4   /* weno/weno3_js.py */
+#define GBF_RECON_WENO3Z 5    /* weno/weno3_z.py */
 
 /* reconstruction_variable (solvers/__init__.py:5-12) */
 #define GBF_RECVAR_PRIMITIVE 0
@@ -54,6 +57,7 @@ extern "C" {
 /* riemann_solver (solvers/riemann_solvers/__init__.py:16) */
 #define GBF_RIEMANN_HLLC 0
 #define GBF_RIEMANN_RUSANOV 1
+#define GBF_RIEMANN_HLL 2     /* riemann_solvers/HLL.py */
 
 /* signal_speed (solvers/riemann_solvers/__init__.py:27) */
 #define GBF_SIGNAL_EINFELDT 0

@@ -16,10 +16,10 @@ GBF_OK = 0
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported setup", -3: "CUDA launch error",
           -4: "invalid or unsupported size", -5: "misaligned pointer"}
 
-RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2}
+RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2, "WENO5-JS": 3, "WENO3-JS": 4, "WENO3-Z": 5}
 RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
-RIEMANN = {"HLLC": 0, "RUSANOV": 1}
+RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
 ABI_VERSION = 2  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}

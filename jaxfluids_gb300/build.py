@@ -65,7 +65,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1, len(srcs)))) as ex:
         results = list(ex.map(compile_one, srcs))
     for obj, log in results:
         if verbose and log:

@@ -555,6 +555,7 @@ inline int grid_for(long long n) {
 int vjp_check(const gbf_case* c) {
   if (c->recon != GBF_RECON_WENO5Z && c->recon != GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
+  if (c->riemann != GBF_RIEMANN_HLLC && c->riemann != GBF_RIEMANN_RUSANOV) return GBF_ERR_UNSUPPORTED;
   if (c->riemann == GBF_RIEMANN_HLLC && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   // the viscous reverse pass indexes faces periodically (one face per cell)
   if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))
@@ -581,7 +582,7 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   size_t smem;
   int st = make_sweep_params(c, ci, tile, &vp.sp, &threads, &smem, true);
   if (st != GBF_OK) return st;
-  const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
+  const int R = recon_radius(c->recon);
   // shared memory: pencil primitives + 2R x 5 slots per face (replaces the
   // flux slots) + 25 doubles per thread for WENO's right-stencil gradients
   // (primitive or characteristic)

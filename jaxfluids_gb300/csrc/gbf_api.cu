@@ -35,6 +35,7 @@ int make_case_info(const gbf_case* c, CaseInfo* ci) {
   ci->fp.gamma = c->gamma;
   ci->fp.gm1 = c->gamma - 1.0;
   ci->fp.stencil_eps = c->stencil_eps;
+  ci->fp.eps = c->eps;
   ci->fp.signal_speed = c->signal_speed;
   ci->fp.frozen_state = c->frozen_state;
   return GBF_OK;
@@ -43,14 +44,14 @@ int make_case_info(const gbf_case* c, CaseInfo* ci) {
 static int check_case(const gbf_case* c, CaseInfo* ci) {
   int st = make_case_info(c, ci);
   if (st != GBF_OK) return st;
-  if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
+  if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_WENO3Z) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var != GBF_RECVAR_PRIMITIVE && c->recon_var != GBF_RECVAR_CHAR_PRIMITIVE)
     return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE &&
       (c->recon != GBF_RECON_WENO5Z ||
        (c->frozen_state != GBF_FROZEN_ARITHMETIC && c->frozen_state != GBF_FROZEN_ROE)))
     return GBF_ERR_UNSUPPORTED;
-  if (c->riemann != GBF_RIEMANN_HLLC && c->riemann != GBF_RIEMANN_RUSANOV) return GBF_ERR_UNSUPPORTED;
+  if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_HLL) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
   if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) {
@@ -62,7 +63,7 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
     if (!(c->mu >= 0.0) || !(c->kappa >= 0.0) || !(c->R > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
   }
   if (!(c->gamma > 1.0)) return GBF_ERR_INVALID_ARGUMENT;
-  const int R = (c->recon == GBF_RECON_WENO5Z) ? 3 : 2;
+  const int R = recon_radius(c->recon);
   if (c->nh < R) return GBF_ERR_INVALID_ARGUMENT;
   for (int a = 0; a < 3; ++a) {
     if (c->n[a] > 1) {

@@ -149,6 +149,8 @@ int launch_batch_sweep(const gbf_case* c, const BatchParams& bp, int threads, si
     k<<<grid, threads, smem, s>>>(bp);                                                              \
     return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;                               \
   }
+  // the batched kernels are built for WENO5-Z / MUSCL with HLLC or Rusanov
+  if (c->riemann == GBF_RIEMANN_HLL || c->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
   const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE) {
     if (hllc) GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC) else GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV)
@@ -171,6 +173,7 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                 int* threads, size_t* smem) {
   if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
   if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) return GBF_ERR_UNSUPPORTED;
+  if (scheme->riemann == GBF_RIEMANN_HLL || scheme->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
   // validate the scheme on a case of the tile's size (sizes vary per case)
   gbf_case rep = *scheme;
   int st = gbf_case_check(&rep);

@@ -18,6 +18,7 @@ struct FaceParams {
   double gamma;        // specific heat ratio
   double gm1;          // gamma - 1.0 (computed once on the host, like ideal_gas.py)
   double stencil_eps;  // WENO / MUSCL epsilon (precision.py:53, 1e-30)
+  double eps;          // precision epsilon (float64 machine epsilon; HLL denominator)
   int signal_speed;    // GBF_SIGNAL_*
   int frozen_state;    // GBF_FROZEN_*
 };
@@ -82,20 +83,66 @@ __device__ __forceinline__ void physical_flux(const double P[5], const double U[
 // Products by powers of two (2 u, 4 u, 1/4 t^2) are exact, so fusing them with
 // the following addition (explicit fma) rounds exactly like the reference's
 // separate multiply and add; the build forbids every other contraction.
-__device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
-                                         double eps) {
-  const double b0 = fma(0.25, sq(fma(-4.0, u1, u0) + 3.0 * u2), (13.0 / 12.0) * sq(fma(-2.0, u1, u0) + u2));
-  const double b1 = fma(0.25, sq(u1 - u3), (13.0 / 12.0) * sq(fma(-2.0, u2, u1) + u3));
-  const double b2 = fma(0.25, sq(fma(-4.0, u3, 3.0 * u2) + u4), (13.0 / 12.0) * sq(fma(-2.0, u3, u2) + u4));
-  const double tau5 = fabs(b0 - b2);
-  const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
-  const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
-  const double a2 = 0.3 * (1.0 + tau5 / (b2 + eps));
+// Smoothness indicators and candidate polynomials of the five-point stencils
+// (weno5_base.py:34-51).
+__device__ __forceinline__ void weno5_smoothness(double u0, double u1, double u2, double u3, double u4,
+                                                 double& b0, double& b1, double& b2) {
+  b0 = fma(0.25, sq(fma(-4.0, u1, u0) + 3.0 * u2), (13.0 / 12.0) * sq(fma(-2.0, u1, u0) + u2));
+  b1 = fma(0.25, sq(u1 - u3), (13.0 / 12.0) * sq(fma(-2.0, u2, u1) + u3));
+  b2 = fma(0.25, sq(fma(-4.0, u3, 3.0 * u2) + u4), (13.0 / 12.0) * sq(fma(-2.0, u3, u2) + u4));
+}
+
+__device__ __forceinline__ double weno5_combine(double a0, double a1, double a2, double u0, double u1,
+                                                double u2, double u3, double u4) {
   const double one_a = 1.0 / (a0 + a1 + a2);
   const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
   const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
   const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
   return (a0 * one_a) * p0 + (a1 * one_a) * p1 + (a2 * one_a) * p2;
+}
+
+__device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
+                                         double eps) {
+  double b0, b1, b2;
+  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  const double tau5 = fabs(b0 - b2);
+  const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
+  const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
+  const double a2 = 0.3 * (1.0 + tau5 / (b2 + eps));
+  return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
+}
+
+// WENO5-JS (shock_capturing/weno/weno5_js.py:33-70): alpha_k = d_k / (beta_k^2 + eps).
+__device__ __forceinline__ double weno5js(double u0, double u1, double u2, double u3, double u4,
+                                          double eps) {
+  double b0, b1, b2;
+  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  const double a0 = 0.1 * (1.0 / (b0 * b0 + eps));
+  const double a1 = 0.6 * (1.0 / (b1 * b1 + eps));
+  const double a2 = 0.3 * (1.0 / (b2 * b2 + eps));
+  return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
+}
+
+// WENO3-JS (weno/weno3_js.py:22-45) and WENO3-Z (weno/weno3_z.py:24-46) on
+// (u_im, u_i, u_ip), weno3_base.py:20-44: d = (1/3, 2/3),
+// p0 = -u_im/2 + 3 u_i / 2, p1 = (u_i + u_ip) / 2.
+template <bool Z>
+__device__ __forceinline__ double weno3(double u0, double u1, double u2, double eps) {
+  const double b0 = sq(u1 - u0);
+  const double b1 = sq(u2 - u1);
+  double a0, a1;
+  if (Z) {
+    const double tau3 = fabs(b0 - b1);
+    a0 = (1.0 / 3.0) * (1.0 + tau3 / (b0 + eps));
+    a1 = (2.0 / 3.0) * (1.0 + tau3 / (b1 + eps));
+  } else {
+    a0 = (1.0 / 3.0) * (1.0 / (b0 * b0 + eps));
+    a1 = (2.0 / 3.0) * (1.0 / (b1 * b1 + eps));
+  }
+  const double one_a = 1.0 / (a0 + a1);
+  const double p0 = fma(-0.5, u0, 1.5 * u1);   // -0.5 u exact
+  const double p1 = fma(0.5, u1, 0.5 * u2);    // both products exact
+  return (a0 * one_a) * p0 + (a1 * one_a) * p1;
 }
 
 // MUSCL3 with the MINMOD limiter (shock_capturing/muscl/muscl3.py:53-75, limiter.py:9-10).
@@ -118,9 +165,15 @@ __device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, dou
   return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : fma(-0.5, b0, 1.5 * b1));
 }
 
-// Internal reconstruction id: WENO5-Z on Roe-characteristic variables
-// (reconstruction_variable CHAR-PRIMITIVE); same six-cell window as WENO5-Z.
-constexpr int RECON_WENO5Z_CHAR = 3;
+// Internal reconstruction id (outside the GBF_RECON_* range): WENO5-Z on
+// Roe-characteristic variables (reconstruction_variable CHAR-PRIMITIVE); same
+// six-cell window as WENO5-Z.
+constexpr int RECON_WENO5Z_CHAR = 100;
+
+// Halo radius of a GBF_RECON_* stencil (host and device).
+__host__ __device__ constexpr int recon_radius(int recon) {
+  return (recon == GBF_RECON_WENO5Z || recon == GBF_RECON_WENO5JS || recon == RECON_WENO5Z_CHAR) ? 3 : 2;
+}
 
 // Halo radius (cells each side of a face) of each reconstruction stencil.
 template <int RECON>
@@ -139,6 +192,18 @@ struct ReconTraits<GBF_RECON_MINMOD> {
 };
 template <>
 struct ReconTraits<GBF_RECON_MINMOD_AD> {
+  static constexpr int R = 2;
+};
+template <>
+struct ReconTraits<GBF_RECON_WENO5JS> {
+  static constexpr int R = 3;
+};
+template <>
+struct ReconTraits<GBF_RECON_WENO3JS> {
+  static constexpr int R = 2;
+};
+template <>
+struct ReconTraits<GBF_RECON_WENO3Z> {
   static constexpr int R = 2;
 };
 
@@ -169,6 +234,28 @@ __device__ __forceinline__ void reconstruct_pair<GBF_RECON_MINMOD_AD>(const doub
                                                                        double& L, double& R) {
   L = minmod_ad<0>(w[0], w[1], w[2], eps);
   R = minmod_ad<1>(w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO5JS>(const double* w, double eps,
+                                                                     double& L, double& R) {
+  L = weno5js(w[0], w[1], w[2], w[3], w[4], eps);
+  R = weno5js(w[5], w[4], w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO3JS>(const double* w, double eps,
+                                                                     double& L, double& R) {
+  // j=0 offsets (-2,-1,0) -> w[0],w[1],w[2]; j=1 offsets (1,0,-1) -> w[3],w[2],w[1]
+  L = weno3<false>(w[0], w[1], w[2], eps);
+  R = weno3<false>(w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO3Z>(const double* w, double eps,
+                                                                    double& L, double& R) {
+  L = weno3<true>(w[0], w[1], w[2], eps);
+  R = weno3<true>(w[3], w[2], w[1], eps);
 }
 
 // ---------------------------------------------------------------------------
@@ -398,12 +485,38 @@ __device__ __forceinline__ void rusanov(const double PL[5], const double PR[5], 
   for (int v = 0; v < 5; ++v) F[v] = fma(0.5, FL[v] + FR[v], -(0.5 * alpha * (UR[v] - UL[v])));
 }
 
+// HLL._solve_riemann_problem_xi_single_phase (HLL.py:28-58):
+// F = (S_R F_L - S_L F_R + S_L S_R (U_R - U_L)) / (S_R - S_L + eps) with
+// S_L = min(s_L, 0), S_R = max(s_R, 0) from the configured signal speeds.
+template <int AX>
+__device__ __forceinline__ void hll(const double PL[5], const double PR[5], const double UL[5],
+                                    const double UR[5], const FaceParams& fp, double F[5]) {
+  constexpr int N = AX + 1;
+  const double cL = speed_of_sound(PL[4], PL[0], fp);
+  const double cR = speed_of_sound(PR[4], PR[0], fp);
+  double sL, sR;
+  signal_speeds(fp.signal_speed, PL[N], PR[N], cL, cR, PL[0], PR[0], PL[4], PR[4], fp.gamma, sL, sR);
+  const double SL = fmin(sL, 0.0);
+  const double SR = fmax(sR, 0.0);
+  double FL[5], FR[5];
+  physical_flux<AX>(PL, UL, FL);
+  physical_flux<AX>(PR, UR, FR);
+  const double SLR = SL * SR;
+  const double den = (SR - SL) + fp.eps;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F[v] = ((SR * FL[v] - SL * FR[v]) + SLR * (UR[v] - UL[v])) / den;
+}
+
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux(const double PL[5], const double PR[5],
                                              const FaceParams& fp, double F[5]) {
   double UL[5], UR[5];
   if (RIEMANN == GBF_RIEMANN_HLLC) {
     hllc<AX>(PL, PR, fp, F);  // forms the conservatives of the side(s) it uses
+  } else if (RIEMANN == GBF_RIEMANN_HLL) {
+    cons_from_prims(PL, UL, fp.gm1);
+    cons_from_prims(PR, UR, fp.gm1);
+    hll<AX>(PL, PR, UL, UR, fp, F);
   } else {
     cons_from_prims(PL, UL, fp.gm1);
     cons_from_prims(PR, UR, fp.gm1);

@@ -9,7 +9,7 @@ namespace gbf {
 namespace {
 
 int radius_of(int recon) {
-  return recon == GBF_RECON_WENO5Z ? 3 : 2;
+  return recon_radius(recon);
 }
 
 }  // namespace
@@ -128,7 +128,9 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
   if (mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
   if (chr) return launch_sweep_char(c->riemann, mode, p, threads, smem, s);
   if (c->recon == GBF_RECON_WENO5Z) return launch_sweep_weno(c->riemann, mode, p, threads, smem, s);
-  return launch_sweep_muscl(c->recon, c->riemann, mode, p, threads, smem, s);
+  if (c->recon == GBF_RECON_MINMOD || c->recon == GBF_RECON_MINMOD_AD)
+    return launch_sweep_muscl(c->recon, c->riemann, mode, p, threads, smem, s);
+  return launch_sweep_weno_family(c->recon, c->riemann, mode, p, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -21,6 +21,7 @@ int launch_sweep_one(const SweepParams& p, int threads, size_t smem, cudaStream_
 template <int RECON, int MODE, bool VISC>
 int launch_sweep_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   if (riemann == GBF_RIEMANN_HLLC) return launch_sweep_one<RECON, GBF_RIEMANN_HLLC, MODE, VISC>(p, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLL) return launch_sweep_one<RECON, GBF_RIEMANN_HLL, MODE, VISC>(p, threads, smem, s);
   return launch_sweep_one<RECON, GBF_RIEMANN_RUSANOV, MODE, VISC>(p, threads, smem, s);
 }
 
@@ -33,5 +34,8 @@ int launch_sweep_char(int riemann, int mode, const SweepParams& p, int threads, 
 int launch_sweep_char_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 int launch_sweep_muscl(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                        cudaStream_t s);
+int launch_sweep_weno5js(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                             cudaStream_t s);
 
 }  // namespace gbf

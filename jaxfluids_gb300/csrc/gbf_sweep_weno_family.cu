@@ -1,0 +1,27 @@
+// Sweep kernels: WENO3-JS and WENO3-Z on primitive variables, inviscid (and
+// the dispatch of the WENO5-JS / WENO3 family).
+#include "gbf_sweep_launch.cuh"
+
+namespace gbf {
+
+namespace {
+
+template <int RECON>
+int launch_modes(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
+  if (mode == MODE_RHS) return launch_sweep_riemann<RECON, MODE_RHS, false>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<RECON, MODE_STAGE, false>(riemann, p, threads, smem, s);
+}
+
+}  // namespace
+
+int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                             cudaStream_t s) {
+  switch (recon) {
+    case GBF_RECON_WENO5JS: return launch_sweep_weno5js(riemann, mode, p, threads, smem, s);
+    case GBF_RECON_WENO3JS: return launch_modes<GBF_RECON_WENO3JS>(riemann, mode, p, threads, smem, s);
+    case GBF_RECON_WENO3Z: return launch_modes<GBF_RECON_WENO3Z>(riemann, mode, p, threads, smem, s);
+    default: return GBF_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace gbf

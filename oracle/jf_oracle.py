@@ -55,10 +55,10 @@ class OracleCase:
     gamma: float = 1.4
     R: float = 1.0
     bc: Dict[str, str] = field(default_factory=dict)
-    recon: str = "WENO5-Z"                 # WENO5-Z | MINMOD | MINMOD-AD
+    recon: str = "WENO5-Z"                 # WENO5-Z | WENO5-JS | WENO3-JS | WENO3-Z | MINMOD | MINMOD-AD
     recon_var: str = "PRIMITIVE"           # PRIMITIVE | CHAR-PRIMITIVE
     frozen_state: str = "ARITHMETIC"       # ARITHMETIC | ROE
-    riemann: str = "HLLC"                  # HLLC | RUSANOV
+    riemann: str = "HLLC"                  # HLLC | HLL | RUSANOV
     signal_speed: str = "EINFELDT"
     cfl: float = 0.5
     fixed_dt: Optional[float] = None
@@ -233,8 +233,56 @@ def weno5z_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
     return w0 * p0 + w1 * p1 + w2 * p2
 
 
+def _weno5_smoothness(u0, u1, u2, u3, u4):
+    # weno5_base.py:34-41
+    b0 = 13.0 / 12.0 * torch.square(u0 - 2 * u1 + u2) + 1.0 / 4.0 * torch.square(u0 - 4 * u1 + 3 * u2)
+    b1 = 13.0 / 12.0 * torch.square(u1 - 2 * u2 + u3) + 1.0 / 4.0 * torch.square(u1 - u3)
+    b2 = 13.0 / 12.0 * torch.square(u2 - 2 * u3 + u4) + 1.0 / 4.0 * torch.square(3 * u2 - 4 * u3 + u4)
+    return b0, b1, b2
+
+
+def weno5js_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
+                    eps: float = STENCIL_EPS) -> Tensor:
+    """WENO5-JS (shock_capturing/weno/weno5_js.py:33-70, weno5_base.py:34-51)."""
+    b0, b1, b2 = _weno5_smoothness(u0, u1, u2, u3, u4)
+    a0 = _WENO_DR[0] * (1.0 / (b0 * b0 + eps))
+    a1 = _WENO_DR[1] * (1.0 / (b1 * b1 + eps))
+    a2 = _WENO_DR[2] * (1.0 / (b2 * b2 + eps))
+    one_a = 1.0 / (a0 + a1 + a2)
+    c = _WENO_CR
+    p0 = c[0][0] * u0 + c[0][1] * u1 + c[0][2] * u2
+    p1 = c[1][0] * u1 + c[1][1] * u2 + c[1][2] * u3
+    p2 = c[2][0] * u2 + c[2][1] * u3 + c[2][2] * u4
+    return (a0 * one_a) * p0 + (a1 * one_a) * p1 + (a2 * one_a) * p2
+
+
+_WENO3_DR = (1 / 3, 2 / 3)                    # weno3_base.py:24
+_WENO3_CR = ((-0.5, 1.5), (0.5, 0.5))          # weno3_base.py:25
+
+
+def weno3_stencil(u0: Tensor, u1: Tensor, u2: Tensor, z: bool, eps: float = STENCIL_EPS) -> Tensor:
+    """WENO3-JS (weno/weno3_js.py:22-45) and WENO3-Z (weno/weno3_z.py:24-46) on
+    (u_im, u_i, u_ip), weno3_base.py:31-44."""
+    b0 = torch.square(u1 - u0)
+    b1 = torch.square(u2 - u1)
+    if z:
+        tau3 = jabs(b0 - b1)
+        a0 = _WENO3_DR[0] * (1.0 + tau3 / (b0 + eps))
+        a1 = _WENO3_DR[1] * (1.0 + tau3 / (b1 + eps))
+    else:
+        a0 = _WENO3_DR[0] * (1.0 / (b0 * b0 + eps))
+        a1 = _WENO3_DR[1] * (1.0 / (b1 * b1 + eps))
+    one_a = 1.0 / (a0 + a1)
+    p0 = _WENO3_CR[0][0] * u0 + _WENO3_CR[0][1] * u1
+    p1 = _WENO3_CR[1][0] * u1 + _WENO3_CR[1][1] * u2
+    return (a0 * one_a) * p0 + (a1 * one_a) * p1
+
+
 def _recon_offsets(recon: str, j: int) -> Tuple[int, ...]:
-    if recon == "WENO5-Z":
+    if recon in ("WENO3-JS", "WENO3-Z"):
+        # weno3_base.py:29 array_slices([range(-2, 1, 1), range(1, -2, -1)])
+        return (-2, -1, 0) if j == 0 else (1, 0, -1)
+    if recon in ("WENO5-Z", "WENO5-JS"):
         # weno5_base.py:30 array_slices([range(-3, 2, 1), range(2, -3, -1)])
         return (-3, -2, -1, 0, 1) if j == 0 else (2, 1, 0, -1, -2)
     if recon in ("MINMOD", "MINMOD-AD"):
@@ -247,6 +295,10 @@ def recon_stencil(recon: str, j: int, vals: List[Tensor], eps: float = STENCIL_E
     """Face value from the stencil values ordered as the reference's slices."""
     if recon == "WENO5-Z":
         return weno5z_stencil(*vals, eps=eps)
+    if recon == "WENO5-JS":
+        return weno5js_stencil(*vals, eps=eps)
+    if recon in ("WENO3-JS", "WENO3-Z"):
+        return weno3_stencil(*vals, z=(recon == "WENO3-Z"), eps=eps)
     b0, b1, b2 = vals
     if recon == "MINMOD":
         # muscl3.py:53-75, limiter.py:9-10
@@ -422,6 +474,14 @@ def riemann(PL, PR, UL, UR, case: OracleCase, axis: int) -> Tensor:
         FR = _hllc_star_flux(PR, UR, SR, Ss, axis, "R")
         sg = torch.sign(Ss)
         return 0.5 * (1 + sg) * FL + 0.5 * (1 - sg) * FR
+    if case.riemann == "HLL":
+        # HLL.py:28-58 (eps = precision epsilon, riemann_solver.py:28)
+        SLs, SRs = signal_speeds(case.signal_speed, PL[n], PR[n], cL, cR, PL[0], PR[0], PL[4], PR[4], g)
+        SL = torch.minimum(SLs, torch.zeros_like(SLs))
+        SR = torch.maximum(SRs, torch.zeros_like(SRs))
+        FL = fluxes_xi(PL, UL, axis)
+        FR = fluxes_xi(PR, UR, axis)
+        return (SR * FL - SL * FR + SL * SR * (UR - UL)) / (SR - SL + EPS)
     if case.riemann == "RUSANOV":
         # Rusanov.py:25-47
         alpha = torch.maximum(jabs(PL[n]) + cL, jabs(PR[n]) + cR)

@@ -75,6 +75,25 @@ RHS_CASES = [
     ("tgv-3d-mixed", dict(cells=(20, 12, 18), bc={"east": ZG, "west": ZG, "north": "SYMMETRY", "south": "SYMMETRY",
                                                   "top": "PERIODIC", "bottom": "PERIODIC"},
                           ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    # WENO5-JS, WENO3-JS, WENO3-Z and HLL (with every signal speed)
+    ("sod-weno5js-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="WENO5-JS"), "sod"),
+    ("sod-weno3js-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="WENO3-JS"), "sod"),
+    ("sod-weno3z-rusanov", dict(cells=(200, 1, 1), bc=ZG, recon="WENO3-Z", riemann="RUSANOV"), "sod"),
+    ("sod-hll-einfeldt", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL"), "sod"),
+    ("sod-hll-davis", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL", signal_speed="DAVIS"), "sod"),
+    ("sod-hll-arith", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL", signal_speed="ARITHMETIC"), "sod"),
+    ("sod-hll-rusanov-speed", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL", signal_speed="RUSANOV"), "sod"),
+    ("sod-hll-toro", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL", signal_speed="TORO"), "sod"),
+    ("quad-2d-weno5js-hll", dict(cells=(48, 40, 1), bc=ZG, recon="WENO5-JS", riemann="HLL"), "quad"),
+    ("quad-2d-weno3z-hllc-sym", dict(cells=(36, 44, 1), bc={"east": ZG, "west": ZG, "north": "SYMMETRY",
+                                                           "south": "SYMMETRY", "top": "PERIODIC",
+                                                           "bottom": "PERIODIC"}, recon="WENO3-Z"), "quad"),
+    ("tgv-3d-weno3js-hll", dict(cells=(20, 16, 24), bc="PERIODIC", recon="WENO3-JS", riemann="HLL",
+                                ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-char-roe-hll", dict(cells=(20, 16, 24), bc="PERIODIC", recon_var="CHAR-PRIMITIVE", frozen_state="ROE",
+                                 riemann="HLL", ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-viscous-hll", dict(cells=(16, 20, 12), bc="PERIODIC", nh=4, viscous=True, heat=True, mu=1e-2,
+                                prandtl=0.71, riemann="HLL", ranges=((0, 2 * math.pi),) * 3), "tgv"),
 ]
 
 
@@ -158,7 +177,9 @@ def test_steps_match_oracle(fused):
              ((16, 16, 16), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3, "nh": 4,
                                                 "recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
                                                 "viscous": True, "heat": True, "mu": 1.0 / 1600, "prandtl": 0.71}),
-             ((24, 20, 1), "PERIODIC", "quad", {"nh": 4, "viscous": True, "mu": 0.05})]
+             ((24, 20, 1), "PERIODIC", "quad", {"nh": 4, "viscous": True, "mu": 0.05}),
+             ((48, 40, 1), ZG, "quad", {"recon": "WENO5-JS", "riemann": "HLL"}),
+             ((40, 36, 1), ZG, "quad", {"recon": "WENO3-Z", "riemann": "HLL", "signal_speed": "DAVIS"})]
     for cells, bc, kind, kw in cases:
         oc, cc = both(cells, bc, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
