@@ -129,6 +129,10 @@ typedef struct gbf_tile {
 } gbf_tile;
 
 int gbf_abi_version(void);
+/* Status returned by the most recent int-returning entry point called on this
+ * host thread (GBF_OK before any call).  No reference counterpart: the
+ * reference raises Python exceptions instead of returning codes. */
+int gbf_last_status(void);
 const char* gbf_status_string(int status);
 
 /* Checks a descriptor; returns GBF_OK or the reason it cannot run. */
@@ -190,6 +194,36 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
                     const gbf_tile* tile, void* stream);
 
 /*
+ * One fused TVD-RK3 stage, for callers that drive the stage loop themselves
+ * (SimulationManager.do_runge_kutta_stages, simulation_manager.py:770-1042,
+ * one iteration: RHS of the stage state and TimeIntegrator.integrate, RK3.py:31-62).
+ * stage 0: out = U^n + dt L(U^n) with cons_k == cons_n == U^n;
+ * stage 1: out = 3/4 U^n + 1/4 U^1 + 1/4 dt L(U^1);
+ * stage 2: out = 1/3 U^n + 2/3 U^2 + 2/3 dt L(U^2), then the next time step of
+ * out is reduced into dt_state and the time advanced (three calls equal one
+ * step of gbf_rk3_advance, bitwise).  out must not alias cons_k; at stage 2 it
+ * may alias cons_n.  dt from dt_state[0] on the device.  prims_ws: 5 N doubles
+ * of device memory for the stage primitives (viscous / heat cases; else may be
+ * NULL).
+ */
+int gbf_rk3_stage(const gbf_case* c, int stage, const double* cons_k, const double* cons_n, double* out,
+                  double* dt_state, double* prims_ws, const gbf_tile* tile, void* stream);
+
+/*
+ * Solver handle: the fused path with its workspace and time-step state owned
+ * by the library (allocated on the current device by gbf_create, freed by
+ * gbf_destroy).  No reference counterpart as a C object: it plays the part of
+ * the SimulationManager instance (simulation_manager.py:94-138) for C callers.
+ * gbf_solver_time copies {dt, t} to host memory and synchronises the stream.
+ */
+typedef struct gbf_solver gbf_solver;
+int gbf_create(const gbf_case* c, const gbf_tile* tile, gbf_solver** out);
+int gbf_destroy(gbf_solver* s);
+int gbf_solver_init(gbf_solver* s, const double* cons, double t0, void* stream);
+int gbf_solver_advance(gbf_solver* s, double* cons, int steps, void* stream);
+int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
+
+/*
  * Adjoint (reverse mode) of the fused path, replacing jax.grad through
  * SimulationManager._feed_forward with a fixed time step
  * (feed_forward/feed_forward.py:231-524, simulation_manager.py:1296-1412).
@@ -218,6 +252,13 @@ int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, co
 int gbf_rk3_step_vjp_stages(const gbf_case* c, const double* cons, const double* u1, const double* u2,
                             const double* dt, const double* lam, double* lam_out, void* workspace,
                             const gbf_tile* tile, void* stream);
+/* Reverse of one gbf_rk3_stage, U_out = a U_k + b U^n + c dt L(U_k) (stage 0:
+ * a = 1, b = 0, c = 1; stage 1: 1/4, 3/4, 1/4; stage 2: 2/3, 1/3, 2/3):
+ * lam_k = a lam + c dt J(U_k)^T lam; lam_n += b lam (stages 1 and 2; at stage 0,
+ * where U_k is U^n, the caller adds lam_k to its U^n cotangent).  workspace:
+ * gbf_vjp_workspace_bytes(c). */
+int gbf_rk3_stage_vjp(const gbf_case* c, int stage, const double* cons_k, const double* dt, const double* lam,
+                      double* lam_k, double* lam_n, void* workspace, const gbf_tile* tile, void* stream);
 
 /*
  * Batched fused TVD-RK3 of many independent cases of uneven size sharing one
@@ -243,6 +284,15 @@ typedef struct gbf_batch_case {
   double dx[3];          /* cell sizes */
 } gbf_batch_case;
 
+/* Host-side case table and work list of a batch (no device work): cells and
+ * dx are 3 per case; cases receives n, tiles (for the tile shape; 1 on axes no
+ * case uses), offset (packed in the given order) and dx; worklist receives
+ * (case, tile) pairs, largest cases first.  *nitems and *total_doubles are set
+ * even when worklist is NULL or capacity (pairs) is too small, which returns
+ * GBF_ERR_SIZE: call once to size the list. */
+int gbf_batch_worklist(const int32_t* cells, const double* dx, int ncases, const gbf_tile* tile,
+                       gbf_batch_case* cases, int32_t* worklist, int64_t capacity, int64_t* nitems,
+                       int64_t* total_doubles);
 size_t gbf_batch_workspace_bytes(int64_t total_doubles);
 int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                    const int32_t* worklist, int ntiles, const gbf_tile* tile, const double* cons,

@@ -13,6 +13,11 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libgbfluids.so")
 
 GBF_OK = 0
+GBF_ERR_INVALID_ARGUMENT = -1
+GBF_ERR_UNSUPPORTED = -2
+GBF_ERR_CUDA = -3
+GBF_ERR_SIZE = -4
+GBF_ERR_ALIGNMENT = -5
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported setup", -3: "CUDA launch error",
           -4: "invalid or unsupported size", -5: "misaligned pointer"}
 
@@ -28,12 +33,14 @@ FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION = 1, 2, 4
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (
-    "gbf_abi_version", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill",
+    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
     "gbf_batch_workspace_bytes", "gbf_batch_init", "gbf_batch_advance",
     "gbf_vjp_workspace_bytes", "gbf_rhs_vjp", "gbf_rk3_step_vjp", "gbf_rk3_step_vjp_stages",
+    "gbf_rk3_stage", "gbf_rk3_stage_vjp", "gbf_batch_worklist",
+    "gbf_create", "gbf_destroy", "gbf_solver_init", "gbf_solver_advance", "gbf_solver_time",
 )
 
 # interior cells the allocation-free entry point's built-in scratch holds
@@ -90,6 +97,7 @@ def load() -> ctypes.CDLL:
     T = ctypes.POINTER(GbfTile)
     sig = {
         "gbf_abi_version": (I, []),
+        "gbf_last_status": (I, []),
         "gbf_status_string": (ctypes.c_char_p, [I]),
         "gbf_case_check": (I, [C]),
         "gbf_rhs": (I, [C, P, P, T, P]),
@@ -111,6 +119,14 @@ def load() -> ctypes.CDLL:
         "gbf_rk3_step_vjp_stages": (I, [C, P, P, P, P, P, P, P, T, P]),
         "gbf_batch_init": (I, [C, P, I, P, I, T, P, P, ctypes.c_double, P]),
         "gbf_batch_advance": (I, [C, P, I, P, I, T, I, P, P, P, ctypes.c_int64, I, P]),
+        "gbf_rk3_stage": (I, [C, I, P, P, P, P, P, T, P]),
+        "gbf_rk3_stage_vjp": (I, [C, I, P, P, P, P, P, P, T, P]),
+        "gbf_batch_worklist": (I, [P, P, I, T, P, P, ctypes.c_int64, P, P]),
+        "gbf_create": (I, [C, T, ctypes.POINTER(ctypes.c_void_p)]),
+        "gbf_destroy": (I, [P]),
+        "gbf_solver_init": (I, [P, P, ctypes.c_double, P]),
+        "gbf_solver_advance": (I, [P, P, I, P]),
+        "gbf_solver_time": (I, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

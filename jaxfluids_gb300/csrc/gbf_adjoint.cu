@@ -541,6 +541,13 @@ __global__ void step_combine_kernel(double* out, const double* lam3, const doubl
     out[i] = ((1.0 / 3.0) * lam3[i] + 0.75 * lam2[i]) + lam1[i] + dt * j1[i];
 }
 
+// y += b x (elementwise)
+__global__ void add_scaled_kernel(double* y, const double* x, double b, long long m) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] += b * x[i];
+}
+
 __global__ void zero_kernel(double* x, long long m) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
        i += (long long)gridDim.x * blockDim.x)
@@ -665,7 +672,7 @@ extern "C" size_t gbf_vjp_workspace_bytes(const gbf_case* c) {
   return ((size_t)6 * 5 * (size_t)ci.cells + (size_t)vjp_extra_doubles(c, ci)) * sizeof(double);
 }
 
-extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out,
+static int gbf_rhs_vjp_impl(const gbf_case* c, const double* cons, const double* w, double* out,
                            void* workspace, const gbf_tile* tile, void* stream) {
   int st = gbf_case_check(c);
   if (st != GBF_OK) return st;
@@ -677,6 +684,11 @@ extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* 
   double* dP = (double*)workspace;
   zero_kernel<<<grid_for(5 * ci.cells), 256, 0, s>>>(dP, 5 * ci.cells);
   return launch_rhs_vjp(c, ci, tile, cons, w, out, dP, dP + 5 * ci.cells, s);
+}
+
+extern "C" int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out,
+                           void* workspace, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rhs_vjp_impl(c, cons, w, out, workspace, tile, stream));
 }
 
 static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, const double* u2_in,
@@ -733,14 +745,61 @@ static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, 
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
-extern "C" int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
+static int gbf_rk3_step_vjp_impl(const gbf_case* c, const double* cons, const double* dt, const double* lam,
                                 double* lam_out, void* workspace, const gbf_tile* tile, void* stream) {
   return step_vjp(c, cons, nullptr, nullptr, dt, lam, lam_out, workspace, tile, stream);
+}
+
+// Reverse of one fused stage U_out = a U_k + b U^n + c dt L(U_k)
+// (RK3.py:27-29: stage 0 a = 1, b = 0, c = 1 with U_k = U^n; stage 1
+// a = 1/4, b = 3/4, c = 1/4; stage 2 a = 2/3, b = 1/3, c = 2/3):
+// lam_k = a lam + c dt J(U_k)^T lam, lam_n += b lam (stages 1 and 2).
+static int gbf_rk3_stage_vjp_impl(const gbf_case* c, int stage, const double* cons_k, const double* dt,
+                                  const double* lam, double* lam_k, double* lam_n, void* workspace,
+                                  const gbf_tile* tile, void* stream) {
+  int st = gbf_case_check(c);
+  if (st != GBF_OK) return st;
+  if ((st = vjp_check(c)) != GBF_OK) return st;
+  if (stage < 0 || stage > 2 || !cons_k || !dt || !lam || !lam_k || !workspace || lam_k == lam)
+    return GBF_ERR_INVALID_ARGUMENT;
+  if (stage > 0 && (!lam_n || lam_n == lam || lam_n == lam_k)) return GBF_ERR_INVALID_ARGUMENT;
+  CaseInfo ci;
+  make_case_info(c, &ci);
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long m = 5 * ci.cells;
+  double* dP = (double*)workspace;
+  double* j = dP + m;
+  double* extra = j + m;
+  static const double kA[3] = {1.0, 0.25, 2.0 / 3.0};
+  static const double kB[3] = {0.0, 0.75, 1.0 / 3.0};
+  static const double kC[3] = {1.0, 0.25, 2.0 / 3.0};
+  zero_kernel<<<grid_for(m), 256, 0, s>>>(dP, m);
+  if ((st = launch_rhs_vjp(c, ci, tile, cons_k, lam, j, dP, extra, s)) != GBF_OK) return st;
+  axpy_dt_kernel<<<grid_for(m), 256, 0, s>>>(lam_k, lam, kA[stage], j, kC[stage], dt, m);
+  if (stage > 0) add_scaled_kernel<<<grid_for(m), 256, 0, s>>>(lam_n, lam, kB[stage], m);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+extern "C" int gbf_rk3_stage_vjp(const gbf_case* c, int stage, const double* cons_k, const double* dt,
+                                 const double* lam, double* lam_k, double* lam_n, void* workspace,
+                                 const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_stage_vjp_impl(c, stage, cons_k, dt, lam, lam_k, lam_n, workspace, tile, stream));
+}
+
+extern "C" int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,
+                                double* lam_out, void* workspace, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_step_vjp_impl(c, cons, dt, lam, lam_out, workspace, tile, stream));
+}
+
+static int gbf_rk3_step_vjp_stages_impl(const gbf_case* c, const double* cons, const double* u1,
+                                       const double* u2, const double* dt, const double* lam, double* lam_out,
+                                       void* workspace, const gbf_tile* tile, void* stream) {
+  if (!u1 || !u2) return GBF_ERR_INVALID_ARGUMENT;
+  return step_vjp(c, cons, u1, u2, dt, lam, lam_out, workspace, tile, stream);
 }
 
 extern "C" int gbf_rk3_step_vjp_stages(const gbf_case* c, const double* cons, const double* u1,
                                        const double* u2, const double* dt, const double* lam, double* lam_out,
                                        void* workspace, const gbf_tile* tile, void* stream) {
-  if (!u1 || !u2) return GBF_ERR_INVALID_ARGUMENT;
-  return step_vjp(c, cons, u1, u2, dt, lam, lam_out, workspace, tile, stream);
+  return record_status(gbf_rk3_step_vjp_stages_impl(c, cons, u1, u2, dt, lam, lam_out, workspace, tile, stream));
 }

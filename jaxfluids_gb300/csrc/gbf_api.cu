@@ -80,11 +80,23 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   return GBF_OK;
 }
 
+namespace {
+thread_local int g_last_status = GBF_OK;
+}  // namespace
+
+int record_status(int status) {
+  g_last_status = status;
+  return status;
+}
+
 }  // namespace gbf
 
 using namespace gbf;
 
 extern "C" {
+
+int gbf_last_status(void) { return g_last_status; }
+
 
 int gbf_abi_version(void) { return GBF_ABI_VERSION; }
 
@@ -100,14 +112,18 @@ const char* gbf_status_string(int status) {
   }
 }
 
-int gbf_case_check(const gbf_case* c) {
+static int gbf_case_check_impl(const gbf_case* c) {
   CaseInfo ci;
   return check_case(c, &ci);
 }
 
+int gbf_case_check(const gbf_case* c) {
+  return record_status(gbf_case_check_impl(c));
+}
+
 static bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
 
-int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
+static int gbf_rhs_impl(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
@@ -123,7 +139,11 @@ int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile*
   return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS);
 }
 
-int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) {
+int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rhs_impl(c, prims, rhs, tile, stream));
+}
+
+static int gbf_halo_fill_impl(const gbf_case* c, double* prims, double* cons, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
@@ -135,19 +155,33 @@ int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) 
   return launch_halo_edges(c, ci, prims, cons, (cudaStream_t)stream);
 }
 
-int gbf_prims_from_cons(const gbf_case* c, const double* cons, double* prims, int64_t count,
+int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream) {
+  return record_status(gbf_halo_fill_impl(c, prims, cons, stream));
+}
+
+static int gbf_prims_from_cons_impl(const gbf_case* c, const double* cons, double* prims, int64_t count,
                         void* stream) {
   if (!c || !cons || !prims || count < 0) return GBF_ERR_INVALID_ARGUMENT;
   return launch_convert(c, cons, prims, count, 1, (cudaStream_t)stream);
 }
 
-int gbf_cons_from_prims(const gbf_case* c, const double* prims, double* cons, int64_t count,
+int gbf_prims_from_cons(const gbf_case* c, const double* cons, double* prims, int64_t count,
+                        void* stream) {
+  return record_status(gbf_prims_from_cons_impl(c, cons, prims, count, stream));
+}
+
+static int gbf_cons_from_prims_impl(const gbf_case* c, const double* prims, double* cons, int64_t count,
                         void* stream) {
   if (!c || !cons || !prims || count < 0) return GBF_ERR_INVALID_ARGUMENT;
   return launch_convert(c, prims, cons, count, 0, (cudaStream_t)stream);
 }
 
-int gbf_stage_integrate(const gbf_case* c, double* cons, const double* cons0, const double* rhs,
+int gbf_cons_from_prims(const gbf_case* c, const double* prims, double* cons, int64_t count,
+                        void* stream) {
+  return record_status(gbf_cons_from_prims_impl(c, prims, cons, count, stream));
+}
+
+static int gbf_stage_integrate_impl(const gbf_case* c, double* cons, const double* cons0, const double* rhs,
                         const double* dt, int stage, void* stream) {
   CaseInfo ci;
   int st = make_case_info(c, &ci);
@@ -157,9 +191,14 @@ int gbf_stage_integrate(const gbf_case* c, double* cons, const double* cons0, co
   return launch_stage_integrate(c, ci, cons, cons0, rhs, dt, stage, (cudaStream_t)stream);
 }
 
+int gbf_stage_integrate(const gbf_case* c, double* cons, const double* cons0, const double* rhs,
+                        const double* dt, int stage, void* stream) {
+  return record_status(gbf_stage_integrate_impl(c, cons, cons0, rhs, dt, stage, stream));
+}
+
 size_t gbf_dt_workspace_bytes(void) { return 2 * sizeof(unsigned long long); }
 
-int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream) {
+static int gbf_dt_impl(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream) {
   CaseInfo ci;
   int st = make_case_info(c, &ci);
   if (st != GBF_OK) return st;
@@ -170,6 +209,10 @@ int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspa
   if ((st = launch_reduce_init(red, s)) != GBF_OK) return st;
   if ((st = launch_reduce_halo_prims(ci, prims, red, s)) != GBF_OK) return st;
   return launch_dt_finalize(c, ci, red, dt_out, nullptr, 0, s);
+}
+
+int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream) {
+  return record_status(gbf_dt_impl(c, prims, dt_out, workspace, stream));
 }
 
 static bool dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0; }
@@ -183,7 +226,7 @@ size_t gbf_rk3_workspace_bytes(const gbf_case* c) {
 }
 
 // dt_state = {dt, t, max signal speed bits, min density bits}
-int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
+static int gbf_rk3_init_impl(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
@@ -196,7 +239,11 @@ int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double
   return launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 0, s);
 }
 
-int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
+int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
+  return record_status(gbf_rk3_init_impl(c, cons, dt_state, t0, stream));
+}
+
+static int gbf_rk3_advance_impl(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
                     const gbf_tile* tile, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
@@ -246,6 +293,51 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
     if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
   }
   return GBF_OK;
+}
+
+int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
+                    const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_advance_impl(c, cons, dt_state, workspace, steps, tile, stream));
+}
+
+static int gbf_rk3_stage_impl(const gbf_case* c, int stage, const double* cons_k, const double* cons_n,
+                              double* out, double* dt_state, double* prims_ws, const gbf_tile* tile,
+                              void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (stage < 0 || stage > 2 || !cons_k || !cons_n || !out || !dt_state) return GBF_ERR_INVALID_ARGUMENT;
+  if (out == cons_k) return GBF_ERR_INVALID_ARGUMENT;  // the sweep reads neighbours of U^k
+  if (stage == 0 && cons_k != cons_n) return GBF_ERR_INVALID_ARGUMENT;
+  if (dissipative(c) && !prims_ws) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(cons_k) || !aligned8(cons_n) || !aligned8(out) || !aligned8(dt_state)) return GBF_ERR_ALIGNMENT;
+  SweepParams p;
+  int threads;
+  size_t smem;
+  if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  p.dt_state = dt_state;
+  p.stage = stage;
+  p.cons = cons_k;
+  p.cons0 = cons_n;
+  p.out = out;
+  p.reduce_dt = (stage == 2);
+  int mode = MODE_STAGE;
+  if (dissipative(c)) {
+    if ((st = launch_convert(c, cons_k, prims_ws, ci.cells, 1, s)) != GBF_OK) return st;
+    p.prims = prims_ws;
+    mode = MODE_STAGE_P;
+  }
+  if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
+  if (stage != 2) return GBF_OK;
+  // the step is complete: next time step from the new state, time advanced
+  unsigned long long* red = (unsigned long long*)(dt_state + 2);
+  return launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s);
+}
+
+int gbf_rk3_stage(const gbf_case* c, int stage, const double* cons_k, const double* cons_n, double* out,
+                  double* dt_state, double* prims_ws, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_stage_impl(c, stage, cons_k, cons_n, out, dt_state, prims_ws, tile, stream));
 }
 
 }  // extern "C"

@@ -7,6 +7,7 @@
 // share one launch, and the whole step (3 stage launches + 1 time-step
 // launch) has a fixed launch sequence that can be captured in a CUDA graph.
 #include <algorithm>
+#include <vector>
 
 #include "gbf_kernels.cuh"
 
@@ -200,11 +201,67 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
 
 using namespace gbf;
 
+// Host-side case table and (case, tile) work list of a batch, largest cases
+// first (the layout jaxfluids_gb300.batch.build_worklist builds).
+static int batch_worklist(const int32_t* cells, const double* dx, int ncases, const gbf_tile* tile,
+                          gbf_batch_case* cases, int32_t* worklist, int64_t capacity, int64_t* nitems,
+                          int64_t* total_doubles) {
+  if (!cells || !dx || ncases <= 0 || !tile || !cases || !nitems || !total_doubles) return GBF_ERR_INVALID_ARGUMENT;
+  int t[3];
+  for (int a = 0; a < 3; ++a) {
+    bool active = false;
+    for (int c = 0; c < ncases; ++c) {
+      if (cells[3 * c + a] < 1) return GBF_ERR_INVALID_ARGUMENT;
+      active |= cells[3 * c + a] > 1;
+    }
+    t[a] = active ? std::max(1, (int)tile->t[a]) : 1;
+  }
+  std::vector<long long> cellcount(ncases);
+  long long offset = 0, items = 0;
+  for (int c = 0; c < ncases; ++c) {
+    gbf_batch_case& bc = cases[c];
+    long long nc = 1, nt = 1;
+    for (int a = 0; a < 3; ++a) {
+      bc.n[a] = cells[3 * c + a];
+      bc.tiles[a] = (cells[3 * c + a] + t[a] - 1) / t[a];
+      bc.dx[a] = dx[3 * c + a];
+      nc *= bc.n[a];
+      nt *= bc.tiles[a];
+    }
+    bc.offset = offset;
+    offset += 5 * nc;
+    cellcount[c] = nc;
+    items += nt;
+  }
+  *total_doubles = offset;
+  *nitems = items;
+  if (!worklist || capacity < items) return GBF_ERR_SIZE;
+  std::vector<int> order(ncases);
+  for (int c = 0; c < ncases; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cellcount[x] > cellcount[y]; });
+  long long k = 0;
+  for (int c : order) {
+    const long long nt = (long long)cases[c].tiles[0] * cases[c].tiles[1] * cases[c].tiles[2];
+    for (long long i = 0; i < nt; ++i) {
+      worklist[2 * k] = c;
+      worklist[2 * k + 1] = (int32_t)i;
+      ++k;
+    }
+  }
+  return GBF_OK;
+}
+
+extern "C" int gbf_batch_worklist(const int32_t* cells, const double* dx, int ncases, const gbf_tile* tile,
+                                  gbf_batch_case* cases, int32_t* worklist, int64_t capacity, int64_t* nitems,
+                                  int64_t* total_doubles) {
+  return record_status(batch_worklist(cells, dx, ncases, tile, cases, worklist, capacity, nitems, total_doubles));
+}
+
 extern "C" size_t gbf_batch_workspace_bytes(int64_t total_doubles) {
   return total_doubles > 0 ? (size_t)2 * (size_t)total_doubles * sizeof(double) : 0;
 }
 
-extern "C" int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+static int gbf_batch_init_impl(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                               const int32_t* worklist, int ntiles, const gbf_tile* tile,
                               const double* cons, double* dt_states, double t0, void* stream) {
   BatchParams bp;
@@ -224,7 +281,13 @@ extern "C" int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* case
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
-extern "C" int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+extern "C" int gbf_batch_init(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                              const int32_t* worklist, int ntiles, const gbf_tile* tile,
+                              const double* cons, double* dt_states, double t0, void* stream) {
+  return record_status(gbf_batch_init_impl(scheme, cases, ncases, worklist, ntiles, tile, cons, dt_states, t0, stream));
+}
+
+static int gbf_batch_advance_impl(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                                  const int32_t* worklist, int ntiles, const gbf_tile* tile, int ctas,
                                  double* cons, double* dt_states, void* workspace,
                                  int64_t total_doubles, int steps, void* stream) {
@@ -256,4 +319,11 @@ extern "C" int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* c
     if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
   }
   return GBF_OK;
+}
+
+extern "C" int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
+                                 const int32_t* worklist, int ntiles, const gbf_tile* tile, int ctas,
+                                 double* cons, double* dt_states, void* workspace,
+                                 int64_t total_doubles, int steps, void* stream) {
+  return record_status(gbf_batch_advance_impl(scheme, cases, ncases, worklist, ntiles, tile, ctas, cons, dt_states, workspace, total_doubles, steps, stream));
 }

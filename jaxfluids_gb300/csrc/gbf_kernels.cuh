@@ -21,6 +21,10 @@ struct CaseInfo {
 
 int make_case_info(const gbf_case* c, CaseInfo* ci);
 
+// Records the status an entry point returns for gbf_last_status (per host
+// thread) and passes it through.
+int record_status(int status);
+
 // per-face boundary constants for the kernels (gbf_sweep.cu)
 void fill_bc_constants(const gbf_case* c, int f, double out[5]);
 

@@ -48,7 +48,7 @@ int scratch_on_current_device(double** out) {
 
 using namespace gbf;
 
-extern "C" int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* dt_state, int steps,
+static int gbf_rk3_advance_noalloc_impl(const gbf_case* c, double* cons, double* dt_state, int steps,
                                        const gbf_tile* tile, void* stream) {
   int st = gbf_case_check(c);
   if (st != GBF_OK) return st;
@@ -81,4 +81,9 @@ extern "C" int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* 
     if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
   }
   return GBF_OK;
+}
+
+extern "C" int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* dt_state, int steps,
+                                       const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_advance_noalloc_impl(c, cons, dt_state, steps, tile, stream));
 }

@@ -3,7 +3,7 @@
 // chains per thread, results stored so nothing is optimised away.
 #include <cuda_runtime.h>
 
-#include "gbfluids.h"
+#include "gbf_kernels.cuh"
 
 namespace {
 
@@ -48,7 +48,7 @@ __global__ void probe_ffma_kernel(double* out, int iters, double seed) {
 
 }  // namespace
 
-extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream) {
+static int gbf_probe_arith_impl(int mode, double* out, int blocks, int threads, int iters, void* stream) {
   if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) return GBF_ERR_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
   switch (mode) {
@@ -59,4 +59,8 @@ extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, i
     default: return GBF_ERR_INVALID_ARGUMENT;
   }
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream) {
+  return gbf::record_status(gbf_probe_arith_impl(mode, out, blocks, threads, iters, stream));
 }

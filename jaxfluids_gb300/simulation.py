@@ -119,6 +119,27 @@ class FusedRK3:
         _lib.check(self.lib.gbf_rk3_advance(ctypes.byref(self.case), _ptr(self.cons), _ptr(self.dt_state),
                                             _ptr(self.workspace), int(steps), tile, _stream()), "rk3 advance")
 
+    def capture(self, steps: int) -> torch.cuda.CUDAGraph:
+        """A CUDA graph of `steps` fused steps on this object's buffers: each
+        replay() advances the state, time step and time by `steps` steps with
+        one host call (the multi-step loop of SimulationManager.simulate,
+        simulation_manager.py:296-401, without its per-step host work).  The
+        state is left as it was; one warm-up step sets the kernel attributes
+        outside the capture and is undone."""
+        saved = (self.cons.clone(), self.dt_state.clone())
+        self.advance(1)
+        torch.cuda.synchronize(self.device)
+        self.cons.copy_(saved[0])
+        self.dt_state.copy_(saved[1])
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.advance(steps)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        return g
+
     @property
     def dt(self) -> torch.Tensor:
         return self.dt_state[0]

@@ -1,0 +1,88 @@
+"""Host-side entry points of the C ABI that need no GPU: the per-thread last
+status, the batch work-list builder (against the Python builder), and
+argument validation of the stage entry points (which returns before any
+CUDA call)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from jaxfluids_gb300 import _lib
+from jaxfluids_gb300.batch import BATCH_CASE_DTYPE, build_worklist
+from jaxfluids_gb300.config import CaseConfig
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from jaxfluids_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def _case(**kw):
+    base = dict(cells=(32, 24, 1), bc={f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")})
+    base.update(kw)
+    return CaseConfig(**base).to_c()
+
+
+def test_last_status_follows_the_latest_call(lib):
+    bad = _case()
+    bad.nh = 1
+    assert lib.gbf_case_check(ctypes.byref(bad)) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_last_status() == _lib.GBF_ERR_INVALID_ARGUMENT
+    good = _case()
+    assert lib.gbf_case_check(ctypes.byref(good)) == _lib.GBF_OK
+    assert lib.gbf_last_status() == _lib.GBF_OK
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_batch_worklist_matches_python_builder(lib, seed):
+    rng = np.random.default_rng(seed)
+    ncases = int(rng.integers(1, 40))
+    cells = np.stack([rng.choice([64, 96, 128, 192, 256], size=ncases), rng.choice([32, 64, 160], size=ncases),
+                      np.ones(ncases, dtype=np.int64)], axis=1).astype(np.int32)
+    dx = rng.uniform(0.001, 0.1, size=(ncases, 3))
+    tile = (15, 32, 1)
+    n, tiles, offsets, worklist, total = build_worklist([tuple(c) for c in cells], tile)
+    gt = _lib.GbfTile()
+    gt.t[0], gt.t[1], gt.t[2] = tile
+    table = np.zeros(ncases, dtype=BATCH_CASE_DTYPE)
+    nitems, tot = ctypes.c_int64(), ctypes.c_int64()
+    cells_c = np.ascontiguousarray(cells)
+    dx_c = np.ascontiguousarray(dx)
+    # size query first
+    st = lib.gbf_batch_worklist(cells_c.ctypes.data, dx_c.ctypes.data, ncases, ctypes.byref(gt),
+                                table.ctypes.data, None, 0, ctypes.byref(nitems), ctypes.byref(tot))
+    assert st == _lib.GBF_ERR_SIZE and nitems.value == worklist.shape[0] and tot.value == total
+    wl = np.zeros((nitems.value, 2), dtype=np.int32)
+    st = lib.gbf_batch_worklist(cells_c.ctypes.data, dx_c.ctypes.data, ncases, ctypes.byref(gt),
+                                table.ctypes.data, wl.ctypes.data, nitems.value, ctypes.byref(nitems),
+                                ctypes.byref(tot))
+    assert st == _lib.GBF_OK
+    assert np.array_equal(wl, worklist)
+    assert np.array_equal(table["n"], n) and np.array_equal(table["tiles"], tiles)
+    assert np.array_equal(table["offset"], offsets) and np.array_equal(table["dx"], dx)
+
+
+def test_stage_entry_points_validate_before_any_device_call(lib):
+    c = _case()
+    buf = ctypes.c_void_p(8)  # never dereferenced: validation fails first
+    # stage out of range, aliasing output, stage 0 with distinct states
+    assert lib.gbf_rk3_stage(ctypes.byref(c), 3, buf, buf, ctypes.c_void_p(16), buf, None, None, None) \
+        == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_rk3_stage(ctypes.byref(c), 1, buf, buf, buf, buf, None, None, None) \
+        == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_rk3_stage(ctypes.byref(c), 0, buf, ctypes.c_void_p(24), ctypes.c_void_p(16), buf, None, None,
+                             None) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_last_status() == _lib.GBF_ERR_INVALID_ARGUMENT
+    # the stage VJP rejects schemes the adjoint does not cover
+    hll = _case(riemann="HLL")
+    assert lib.gbf_rk3_stage_vjp(ctypes.byref(hll), 1, buf, buf, buf, ctypes.c_void_p(16), ctypes.c_void_p(24),
+                                 buf, None, None) == _lib.GBF_ERR_UNSUPPORTED
+    # a solver handle needs a valid case
+    bad = _case()
+    bad.nh = 1
+    out = ctypes.c_void_p()
+    assert lib.gbf_create(ctypes.byref(bad), None, ctypes.byref(out)) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert out.value is None
+    assert lib.gbf_destroy(None) == _lib.GBF_OK
