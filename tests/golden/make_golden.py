@@ -8,9 +8,10 @@ the reference at run time.
   reference's own run of notebooks/basics/101/01_tutorial (linear advection,
   50 cells, MINMOD + HLLC/Einfeldt, PRIMITIVE, periodic, RK3, CFL 0.9,
   JAX CPU backend), parsed from the notebook's stored output.
-* ``tut02_grad.json``: the loss and the first gradient-descent update printed
-  by notebooks/basics/101/02_tutorial (Sod, 100 cells, MINMOD-AD + Rusanov,
-  fixed dt 1e-3, 200 steps, jax.value_and_grad through _feed_forward).
+* ``tut02_grad.json``: the losses and parameters printed every 25 iterations of
+  the gradient-descent run of notebooks/basics/101/02_tutorial (Sod, 100 cells,
+  MINMOD-AD + Rusanov, fixed dt 1e-3, 200 steps, jax.value_and_grad through
+  _feed_forward), with the first update's gradient.
 * ``sod_exact.npz``: the reference's exact Riemann solver
   (src/jaxfluids_thirdparty/exact_riemann_solver) for Sod at t = 0.2 sampled
   on 4001 points of x in [0, 1] (W = rho, u, p rows).
@@ -62,13 +63,23 @@ def tut02():
     theta0 = [1.0, 1.0, 0.0, 0.0, 1.0, 1.0]
     lr = 0.2
     grad = [(a - b) / lr for a, b in zip(theta0, params1)]
+    # every printed line: iteration, loss (3 digits) and the parameters after
+    # that iteration's update (numpy's 8 decimals); plain gradient descent with
+    # lr_schedule of cell 6 (0.2 below 50, 0.1 below 200, else 0.01)
+    traj = []
+    for line in txt.splitlines():
+        mm = re.match(r"(\d{4}), ([0-9.e+-]+), \[(.*)\]", line.strip())
+        if mm:
+            traj.append({"itr": int(mm.group(1)), "loss": float(mm.group(2)),
+                         "params": [float(x) for x in mm.group(3).split()]})
     return {
-        "source": "notebooks/basics/101/02_tutorial/02_tutorial.ipynb cell 7 output, first line",
+        "source": "notebooks/basics/101/02_tutorial/02_tutorial.ipynb cell 7 output",
         "case": {"cells": 100, "range": [0.0, 1.0], "bc": "ZEROGRADIENT", "recon": "MINMOD-AD",
                  "riemann": "RUSANOV", "signal_speed": "EINFELDT", "fixed_dt": 1e-3, "nh": 4,
                  "steps": 200, "end_time_ref": 0.2, "gamma": 1.4},
         "theta0": theta0, "lr": lr, "loss": loss, "loss_digits": 3,
         "params_after_first_update": params1, "params_decimals": 8, "grad": grad,
+        "lr_schedule": [[50, 0.2], [200, 0.1], [None, 0.01]], "trajectory": traj,
     }
 
 

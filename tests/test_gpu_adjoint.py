@@ -210,6 +210,44 @@ def test_tutorial02_gradient_trace_on_gpu():
         assert abs(a - b) <= 0.6e-8
 
 
+def test_tutorial02_optimisation_trajectory_on_gpu():
+    """The reference's whole gradient-descent run (976 iterations, each a
+    jax.value_and_grad through 200 fixed-dt steps), printed every 25
+    iterations to 3 digits (loss) and 8 decimals (parameters), replayed with
+    the hand-written adjoint."""
+    from jaxfluids_gb300 import FusedRK3
+    from jaxfluids_gb300.adjoint import AdjointRK3, RK3Trajectory
+    g = json.load(open(os.path.join(GOLDEN, "tut02_grad.json")))
+    oc, cc = both((100, 1, 1), "ZEROGRADIENT", nh=4, recon="MINMOD-AD", riemann="RUSANOV", fixed_dt=1e-3)
+    U, P = O.initialize(sod_prims(100), oc)
+    f = FusedRK3(cc)
+    f.set_state(U[oc.interior()].contiguous().cuda())
+    f.advance(200)
+    rho_ref = f.primitives()[0].reshape(-1)
+    x = oc.cell_centers(0).cuda()
+    adj = AdjointRK3(cc, dt=1e-3)
+    printed = {row["itr"]: row for row in g["trajectory"]}
+    theta = torch.tensor(g["theta0"], dtype=torch.float64, device="cuda")
+    for itr in range(max(printed) + 1):
+        th = theta.clone().requires_grad_(True)
+        d0 = torch.where(x < 0.5, th[0], th[1])
+        u0 = torch.where(x < 0.5, th[2], th[3])
+        p0 = torch.where(x < 0.5, th[4], th[5])
+        z = torch.zeros_like(u0)
+        U0 = O.cons_from_prims(torch.stack([d0, u0, z, z, p0]).reshape(5, 100, 1, 1), 1.4)
+        # one stored-stage leaf over the whole 200-step trajectory
+        UN = RK3Trajectory.apply(U0, adj, 200, "binomial", 50, 0, 200)
+        loss = torch.mean((UN[0].reshape(-1) - rho_ref) ** 2)
+        loss.backward()
+        lr = next(v for lim, v in g["lr_schedule"] if lim is None or itr < lim)
+        theta = theta - lr * th.grad
+        if itr in printed:
+            row = printed[itr]
+            assert "%.2e" % loss.item() == "%.2e" % row["loss"], itr
+            for a, b in zip(theta.tolist(), row["params"]):
+                assert abs(a - b) <= 0.6e-8, (itr, theta.tolist(), row["params"])
+
+
 def test_gradient_matches_central_differences():
     from jaxfluids_gb300.adjoint import AdjointRK3
     oc, cc = both((40, 36, 1), "PERIODIC")
