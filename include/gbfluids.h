@@ -210,6 +210,15 @@ int gbf_rk3_stage(const gbf_case* c, int stage, const double* cons_k, const doub
                   double* dt_state, double* prims_ws, const gbf_tile* tile, void* stream);
 
 /*
+ * Numerical health of an interior conservative state [5][N]: counts[0] cells
+ * with a non-finite value, counts[1] cells with rho <= 0, counts[2] cells with
+ * p <= 0 (device uint64[3], overwritten; no host synchronisation).  The
+ * reference propagates NaN silently at run time; this is the positive-count
+ * warning channel of this library (a host reads counts when it wants to).
+ */
+int gbf_state_check(const gbf_case* c, const double* cons, uint64_t* counts, void* stream);
+
+/*
  * Solver handle: the fused path with its workspace and time-step state owned
  * by the library (allocated on the current device by gbf_create, freed by
  * gbf_destroy).  No reference counterpart as a C object: it plays the part of

@@ -39,7 +39,7 @@ EXPORTS = (
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
     "gbf_batch_workspace_bytes", "gbf_batch_init", "gbf_batch_advance",
     "gbf_vjp_workspace_bytes", "gbf_rhs_vjp", "gbf_rk3_step_vjp", "gbf_rk3_step_vjp_stages",
-    "gbf_rk3_stage", "gbf_rk3_stage_vjp", "gbf_batch_worklist",
+    "gbf_rk3_stage", "gbf_rk3_stage_vjp", "gbf_batch_worklist", "gbf_state_check",
     "gbf_create", "gbf_destroy", "gbf_solver_init", "gbf_solver_advance", "gbf_solver_time",
 )
 
@@ -120,6 +120,7 @@ def load() -> ctypes.CDLL:
         "gbf_batch_init": (I, [C, P, I, P, I, T, P, P, ctypes.c_double, P]),
         "gbf_batch_advance": (I, [C, P, I, P, I, T, I, P, P, P, ctypes.c_int64, I, P]),
         "gbf_rk3_stage": (I, [C, I, P, P, P, P, P, T, P]),
+        "gbf_state_check": (I, [C, P, P, P]),
         "gbf_rk3_stage_vjp": (I, [C, I, P, P, P, P, P, P, T, P]),
         "gbf_batch_worklist": (I, [P, P, I, T, P, P, ctypes.c_int64, P, P]),
         "gbf_create": (I, [C, T, ctypes.POINTER(ctypes.c_void_p)]),

@@ -300,6 +300,21 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
   return record_status(gbf_rk3_advance_impl(c, cons, dt_state, workspace, steps, tile, stream));
 }
 
+static int gbf_state_check_impl(const gbf_case* c, const double* cons, uint64_t* counts, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!cons || !counts) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(cons) || !aligned8(counts)) return GBF_ERR_ALIGNMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(counts, 0, 3 * sizeof(uint64_t), s) != cudaSuccess) return GBF_ERR_CUDA;
+  return launch_state_check(ci, cons, (unsigned long long*)counts, s);
+}
+
+int gbf_state_check(const gbf_case* c, const double* cons, uint64_t* counts, void* stream) {
+  return record_status(gbf_state_check_impl(c, cons, counts, stream));
+}
+
 static int gbf_rk3_stage_impl(const gbf_case* c, int stage, const double* cons_k, const double* cons_n,
                               double* out, double* dt_state, double* prims_ws, const gbf_tile* tile,
                               void* stream) {

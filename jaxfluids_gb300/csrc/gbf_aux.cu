@@ -425,6 +425,42 @@ int launch_reduce_halo_prims(const CaseInfo& ci, const double* prims, unsigned l
   return launch_reduce(ci, prims, red, 0, s);
 }
 
+// Numerical health of an interior conservative state: cells with a
+// non-finite conservative, with rho <= 0, and with p <= 0 (p from the ideal-gas
+// EOS, equation_manager.py:164-171), counted into counts[0..2] (accumulated).
+__global__ void state_check_kernel(const double* cons, long long n, double gm1, unsigned long long* counts) {
+  unsigned long long bad = 0, neg_rho = 0, neg_p = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double U[5], P[5];
+    bool finite = true;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      U[v] = cons[v * n + i];
+      finite &= isfinite(U[v]);
+    }
+    prims_from_cons(U, P, gm1);
+    bad += finite ? 0 : 1;
+    neg_rho += (U[0] <= 0.0) ? 1 : 0;
+    neg_p += (P[4] <= 0.0) ? 1 : 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bad += __shfl_down_sync(0xffffffffu, bad, o);
+    neg_rho += __shfl_down_sync(0xffffffffu, neg_rho, o);
+    neg_p += __shfl_down_sync(0xffffffffu, neg_p, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (bad | neg_rho | neg_p)) {
+    atomicAdd(counts + 0, bad);
+    atomicAdd(counts + 1, neg_rho);
+    atomicAdd(counts + 2, neg_p);
+  }
+}
+
+int launch_state_check(const CaseInfo& ci, const double* cons, unsigned long long* counts, cudaStream_t s) {
+  state_check_kernel<<<grid_for(ci.cells), kThreads, 0, s>>>(cons, ci.cells, ci.fp.gm1, counts);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
 int launch_reduce_cons(const CaseInfo& ci, const double* cons, unsigned long long* red,
                        cudaStream_t s) {
   return launch_reduce(ci, cons, red, 1, s);

@@ -53,6 +53,8 @@ int launch_set_scalar(double* dst, double v, cudaStream_t s);
 int launch_reduce_init(unsigned long long* red, cudaStream_t s);
 int launch_reduce_halo_prims(const CaseInfo& ci, const double* prims, unsigned long long* red,
                              cudaStream_t s);
+// cells with non-finite values, rho <= 0, p <= 0 added to counts[0..2]
+int launch_state_check(const CaseInfo& ci, const double* cons, unsigned long long* counts, cudaStream_t s);
 int launch_reduce_cons(const CaseInfo& ci, const double* cons, unsigned long long* red,
                        cudaStream_t s);
 // dt from reduction slots; when advance_time, dt_state[1] += previous dt first

@@ -148,6 +148,15 @@ class FusedRK3:
     def t(self) -> torch.Tensor:
         return self.dt_state[1]
 
+    def state_health(self) -> dict:
+        """Counts of cells with non-finite values, rho <= 0 and p <= 0 in the
+        current state (synchronises the stream to read them)."""
+        counts = torch.zeros(3, dtype=torch.int64, device=self.device)
+        _lib.check(self.lib.gbf_state_check(ctypes.byref(self.case), _ptr(self.cons), _ptr(counts), _stream()),
+                   "state check")
+        nonfinite, rho, p = counts.tolist()
+        return {"nonfinite": nonfinite, "rho_nonpositive": rho, "p_nonpositive": p}
+
     def primitives(self) -> torch.Tensor:
         out = torch.empty_like(self.cons)
         _lib.check(self.lib.gbf_prims_from_cons(ctypes.byref(self.case), _ptr(self.cons), _ptr(out),

@@ -139,3 +139,18 @@ def test_captured_steps_equal_launched_steps():
     torch.cuda.synchronize()
     assert torch.equal(a.cons, b.cons)
     assert torch.equal(a.dt_state[:2], b.dt_state[:2])
+
+
+def test_state_health_counts_planted_faults():
+    from jaxfluids_gb300 import FusedRK3
+    oc, cc = both((32, 24, 1), "ZEROGRADIENT")
+    U0 = _state((32, 24, 1), "quad", oc)
+    f = FusedRK3(cc)
+    f.set_state(U0)
+    assert f.state_health() == {"nonfinite": 0, "rho_nonpositive": 0, "p_nonpositive": 0}
+    bad = U0.clone()
+    bad[4, 3, 5, 0] = float("nan")                       # non-finite energy
+    bad[:, 10, 2, 0] = torch.tensor([-1.0, 0.0, 0.0, 0.0, 1.0], dtype=torch.float64)   # rho < 0, p > 0
+    bad[:, 20, 7, 0] = torch.tensor([1.0, 0.0, 0.0, 0.0, -1.0], dtype=torch.float64)   # p < 0
+    f.cons.copy_(bad)
+    assert f.state_health() == {"nonfinite": 1, "rho_nonpositive": 1, "p_nonpositive": 1}
