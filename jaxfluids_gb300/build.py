@@ -35,7 +35,7 @@ def _nvcc() -> str:
 # Translation units whose results need not round like the reference's
 # forward graph (the adjoint: jax.grad's own backward pass rounds differently,
 # and the adjoint is checked to a tolerance), compiled with contraction on.
-FMAD_ON = {"gbf_adjoint.cu"}
+FMAD_ON_PREFIXES = ("gbf_adjoint", "gbf_vjp_")
 
 
 def sources():
@@ -58,7 +58,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        flags = [f for f in FLAGS if not (os.path.basename(src) in FMAD_ON and f == "-fmad=false")]
+        fmad_on = os.path.basename(src).startswith(FMAD_ON_PREFIXES)
+        flags = [f for f in FLAGS if not (fmad_on and f == "-fmad=false")]
         cmd = [nvcc, *ARCH, *flags, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -76,6 +76,96 @@ __device__ __forceinline__ void weno5z_jac(double u0, double u1, double u2, doub
   J[4] += dt4 + dt5;
 }
 
+// weno5js(u0..u4) and its gradient (weno/weno5_js.py:33-70): as weno5z_jac
+// with alpha_k = d_k / (beta_k^2 + eps), d alpha_k / d beta_k = -2 alpha_k beta_k / (beta_k^2 + eps).
+__device__ __forceinline__ void weno5js_jac(double u0, double u1, double u2, double u3, double u4,
+                                            double eps, double& out, double J[5]) {
+  constexpr double c13 = 13.0 / 12.0;
+  const double t0 = u0 - 2.0 * u1 + u2;
+  const double t1 = u0 - 4.0 * u1 + 3.0 * u2;
+  const double t2 = u1 - 2.0 * u2 + u3;
+  const double t3 = u1 - u3;
+  const double t4 = u2 - 2.0 * u3 + u4;
+  const double t5 = 3.0 * u2 - 4.0 * u3 + u4;
+  const double b0 = c13 * (t0 * t0) + 0.25 * (t1 * t1);
+  const double b1 = c13 * (t2 * t2) + 0.25 * (t3 * t3);
+  const double b2 = c13 * (t4 * t4) + 0.25 * (t5 * t5);
+  const double ie0 = 1.0 / (b0 * b0 + eps), ie1 = 1.0 / (b1 * b1 + eps), ie2 = 1.0 / (b2 * b2 + eps);
+  const double a0 = 0.1 * ie0, a1 = 0.6 * ie1, a2 = 0.3 * ie2;
+  const double r = 1.0 / (a0 + a1 + a2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  const double w0 = a0 * r, w1 = a1 * r, w2 = a2 * r;
+  out = w0 * p0 + w1 * p1 + w2 * p2;
+  J[0] = (1.0 / 3.0) * w0;
+  J[1] = (-7.0 / 6.0) * w0 + (-1.0 / 6.0) * w1;
+  J[2] = (11.0 / 6.0) * w0 + (5.0 / 6.0) * w1 + (1.0 / 3.0) * w2;
+  J[3] = (1.0 / 3.0) * w1 + (5.0 / 6.0) * w2;
+  J[4] = (-1.0 / 6.0) * w2;
+  const double db0 = -2.0 * r * (p0 - out) * a0 * b0 * ie0;
+  const double db1 = -2.0 * r * (p1 - out) * a1 * b1 * ie1;
+  const double db2 = -2.0 * r * (p2 - out) * a2 * b2 * ie2;
+  const double dt0 = db0 * (2.0 * c13) * t0, dt1 = db0 * 0.5 * t1;
+  const double dt2 = db1 * (2.0 * c13) * t2, dt3 = db1 * 0.5 * t3;
+  const double dt4 = db2 * (2.0 * c13) * t4, dt5 = db2 * 0.5 * t5;
+  J[0] += dt0 + dt1;
+  J[1] += -2.0 * dt0 - 4.0 * dt1 + dt2 + dt3;
+  J[2] += dt0 + 3.0 * dt1 - 2.0 * dt2 + dt4 + 3.0 * dt5;
+  J[3] += dt2 - dt3 - 2.0 * dt4 - 4.0 * dt5;
+  J[4] += dt4 + dt5;
+}
+
+// weno3<Z>(u0, u1, u2) and its gradient (weno/weno3_js.py:22-45,
+// weno/weno3_z.py:24-46, weno3_base.py:20-44).
+template <bool Z>
+__device__ __forceinline__ void weno3_jac(double u0, double u1, double u2, double eps, double& out, double J[3]) {
+  const double e0 = u1 - u0, e1 = u2 - u1;
+  const double b0 = e0 * e0, b1 = e1 * e1;
+  double a0, a1, da0_db0, da1_db1, tau = 0.0, ie0 = 0.0, ie1 = 0.0;
+  if (Z) {
+    tau = fabs(b0 - b1);
+    ie0 = 1.0 / (b0 + eps);
+    ie1 = 1.0 / (b1 + eps);
+    a0 = (1.0 / 3.0) * (1.0 + tau * ie0);
+    a1 = (2.0 / 3.0) * (1.0 + tau * ie1);
+    da0_db0 = da1_db1 = 0.0;
+  } else {
+    ie0 = 1.0 / (b0 * b0 + eps);
+    ie1 = 1.0 / (b1 * b1 + eps);
+    a0 = (1.0 / 3.0) * ie0;
+    a1 = (2.0 / 3.0) * ie1;
+    da0_db0 = -2.0 * a0 * b0 * ie0;
+    da1_db1 = -2.0 * a1 * b1 * ie1;
+  }
+  const double r = 1.0 / (a0 + a1);
+  const double p0 = -0.5 * u0 + 1.5 * u1, p1 = 0.5 * u1 + 0.5 * u2;
+  const double w0 = a0 * r, w1 = a1 * r;
+  out = w0 * p0 + w1 * p1;
+  J[0] = -0.5 * w0;
+  J[1] = 1.5 * w0 + 0.5 * w1;
+  J[2] = 0.5 * w1;
+  const double da0 = r * (p0 - out), da1 = r * (p1 - out);
+  double db0, db1;
+  if (Z) {
+    // a_k = d_k (1 + tau / (b_k + eps))
+    const double dq0 = (1.0 / 3.0) * da0 * ie0, dq1 = (2.0 / 3.0) * da1 * ie1;
+    const double dtau = dq0 + dq1;
+    db0 = -dq0 * tau * ie0;
+    db1 = -dq1 * tau * ie1;
+    const double sg = jabs_grad(b0 - b1);
+    db0 += dtau * sg;
+    db1 -= dtau * sg;
+  } else {
+    db0 = da0 * da0_db0;
+    db1 = da1 * da1_db1;
+  }
+  const double de0 = 2.0 * e0 * db0, de1 = 2.0 * e1 * db1;
+  J[0] -= de0;
+  J[1] += de0 - de1;
+  J[2] += de1;
+}
+
 // Reverse of minmod_ad<J>(b0, b1, b2): the ratio only selects a branch.
 template <int J>
 __device__ __forceinline__ void minmod_ad_vjp(double b0, double b1, double b2, double eps, double g,
@@ -108,6 +198,42 @@ __device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5Z>(const dou
 #pragma unroll
   for (int k = 1; k < 5; ++k) dw[k] = gL * jl[k] + gR * jr[5 - k];
   dw[5] = gR * jr[0];
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5JS>(const double* w, double eps,
+                                                                         double gL, double gR, double* dw) {
+  double jl[5], jr[5], vl, vr;
+  weno5js_jac(w[0], w[1], w[2], w[3], w[4], eps, vl, jl);
+  weno5js_jac(w[5], w[4], w[3], w[2], w[1], eps, vr, jr);
+  dw[0] = gL * jl[0];
+#pragma unroll
+  for (int k = 1; k < 5; ++k) dw[k] = gL * jl[k] + gR * jr[5 - k];
+  dw[5] = gR * jr[0];
+}
+
+template <bool Z>
+__device__ __forceinline__ void weno3_pair_vjp(const double* w, double eps, double gL, double gR, double* dw) {
+  // j=0 (w0, w1, w2), j=1 (w3, w2, w1)
+  double jl[3], jr[3], vl, vr;
+  weno3_jac<Z>(w[0], w[1], w[2], eps, vl, jl);
+  weno3_jac<Z>(w[3], w[2], w[1], eps, vr, jr);
+  dw[0] = gL * jl[0];
+  dw[1] = gL * jl[1] + gR * jr[2];
+  dw[2] = gL * jl[2] + gR * jr[1];
+  dw[3] = gR * jr[0];
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO3JS>(const double* w, double eps,
+                                                                         double gL, double gR, double* dw) {
+  weno3_pair_vjp<false>(w, eps, gL, gR, dw);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO3Z>(const double* w, double eps,
+                                                                        double gL, double gR, double* dw) {
+  weno3_pair_vjp<true>(w, eps, gL, gR, dw);
 }
 
 template <>
@@ -269,6 +395,86 @@ __device__ __forceinline__ void hllc_star_flux_vjp(const double P[5], const doub
   dP[N] += du;
 }
 
+// Einfeldt wave speeds (signal_speeds.py:109-133) recomputed for a reverse
+// pass, with 1/sqrt(rho) and 1/dbar from rsqrt.
+struct Einfeldt {
+  double isL, isR, sL, sR, od, eta2, ubar, duu, Wn, idbar, X1, X2, Y1, Y2, SL, SR;
+};
+
+__device__ __forceinline__ void einfeldt_fwd(double uL, double uR, double rL, double rR, double cL, double cR,
+                                             Einfeldt& e) {
+  e.isL = rsqrt(rL);
+  e.isR = rsqrt(rR);
+  e.sL = rL * e.isL;
+  e.sR = rR * e.isR;
+  e.od = 1.0 / (e.sL + e.sR);
+  e.eta2 = 0.5 * e.sL * e.sR * e.od * e.od;
+  e.ubar = (e.sL * uL + e.sR * uR) * e.od;
+  e.duu = uR - uL;
+  e.Wn = e.sL * cL * cL + e.sR * cR * cR;
+  const double Z = e.Wn * e.od + e.eta2 * (e.duu * e.duu);
+  e.idbar = rsqrt(Z);
+  const double dbar = Z * e.idbar;
+  e.X1 = e.ubar - dbar;
+  e.X2 = uL - cL;
+  e.Y1 = e.ubar + dbar;
+  e.Y2 = uR + cR;
+  e.SL = fmin(e.X1, e.X2);
+  e.SR = fmax(e.Y1, e.Y2);
+}
+
+// Reverse of einfeldt_fwd: cotangents dSL, dSR of the wave speeds added to
+// those of the normal velocities, densities and sounds speeds of both sides.
+__device__ __forceinline__ void einfeldt_vjp(const Einfeldt& e, double uL, double uR, double cL, double cR,
+                                             double dSL, double dSR, double& duL, double& duR, double& drL,
+                                             double& drR, double& dcL, double& dcR) {
+  // SL = min(X1, X2), SR = max(Y1, Y2)
+  const double wx = min_weight_a(e.X1, e.X2), wy = max_weight_a(e.Y1, e.Y2);
+  const double dX1 = dSL * wx, dX2 = dSL * (1.0 - wx);
+  const double dY1 = dSR * wy, dY2 = dSR * (1.0 - wy);
+  const double dubar = dX1 + dY1;
+  const double ddbar = -dX1 + dY1;
+  duL += dX2;
+  dcL -= dX2;
+  duR += dY2;
+  dcR += dY2;
+  // dbar = sqrt(Z), Z = Wn od + eta2 du^2
+  const double dZ = ddbar * 0.5 * e.idbar;
+  const double dWn = dZ * e.od;
+  double dod = dZ * e.Wn;
+  const double deta2 = dZ * (e.duu * e.duu);
+  const double dduu = dZ * e.eta2 * 2.0 * e.duu;
+  duR += dduu;
+  duL -= dduu;
+  double dsL = dWn * cL * cL, dsR = dWn * cR * cR;
+  dcL += dWn * e.sL * 2.0 * cL;
+  dcR += dWn * e.sR * 2.0 * cR;
+  // eta2 = 0.5 sL sR od od
+  const double od2 = e.od * e.od;
+  dsL += deta2 * 0.5 * e.sR * od2;
+  dsR += deta2 * 0.5 * e.sL * od2;
+  dod += deta2 * e.sL * e.sR * e.od;
+  // ubar = (sL uL + sR uR) od
+  dsL += dubar * uL * e.od;
+  dsR += dubar * uR * e.od;
+  duL += dubar * e.sL * e.od;
+  duR += dubar * e.sR * e.od;
+  dod += dubar * (e.sL * uL + e.sR * uR);
+  // od = 1 / (sL + sR)
+  const double dsum = -dod * od2;
+  dsL += dsum;
+  dsR += dsum;
+  drL += dsL * 0.5 * e.isL;
+  drR += dsR * 0.5 * e.isR;
+}
+
+// Reverse of c = sqrt(y), y = gamma p / rho for one side: dc onto dP[0], dP[4].
+__device__ __forceinline__ void sound_speed_vjp(const FaceSide& S, double gamma, double dc, double dP[5]) {
+  const double dy = dc * 0.5 * S.ic;
+  dP[0] -= dy * S.y * S.ir;
+  dP[4] += dy * S.ir * gamma;
+}
+
 // Reverse of hllc<AX> with Einfeldt wave speeds (HLLC.py:80-126,
 // signal_speeds.py:109-133, :159-199); the cons of the face states are
 // recomputed and reversed too.  dPL, dPR are accumulated.
@@ -282,19 +488,9 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   face_side(PL, gamma, igm1, L);
   face_side(PR, gamma, igm1, R);
   const double uL = PL[N], uR = PR[N], rL = PL[0], rR = PR[0], pL = PL[4], pR = PR[4];
-  const double cL = L.c, cR = R.c;
-  const double isL = rsqrt(rL), isR = rsqrt(rR);
-  const double sL = rL * isL, sR = rR * isR;
-  const double od = 1.0 / (sL + sR);
-  const double eta2 = 0.5 * sL * sR * od * od;
-  const double ubar = (sL * uL + sR * uR) * od;
-  const double duu = uR - uL;
-  const double Wn = sL * cL * cL + sR * cR * cR;
-  const double Z = Wn * od + eta2 * (duu * duu);
-  const double idbar = rsqrt(Z);
-  const double dbar = Z * idbar;
-  const double X1 = ubar - dbar, X2 = uL - cL, Y1 = ubar + dbar, Y2 = uR + cR;
-  const double SL = fmin(X1, X2), SR = fmax(Y1, Y2);
+  Einfeldt e;
+  einfeldt_fwd(uL, uR, rL, rR, L.c, R.c, e);
+  const double SL = e.SL, SR = e.SR;
   const double rdL = rL * (SL - uL), rdR = rR * (SR - uR);
   const double num = (pR - pL) + (uL * rdL - uR * rdR);
   const double den = rdL - rdR;
@@ -329,55 +525,68 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   duL -= drdL * rL;
   dSR += drdR * rR;
   duR -= drdR * rR;
-  // SL = min(X1, X2), SR = max(Y1, Y2)
-  const double wx = min_weight_a(X1, X2), wy = max_weight_a(Y1, Y2);
-  const double dX1 = dSL * wx, dX2 = dSL * (1.0 - wx);
-  const double dY1 = dSR * wy, dY2 = dSR * (1.0 - wy);
-  const double dubar = dX1 + dY1;
-  const double ddbar = -dX1 + dY1;
-  duL += dX2;
-  double dcL = -dX2;
-  duR += dY2;
-  double dcR = dY2;
-  // dbar = sqrt(Z), Z = Wn od + eta2 du^2
-  const double dZ = ddbar * 0.5 * idbar;
-  const double dWn = dZ * od;
-  double dod = dZ * Wn;
-  const double deta2 = dZ * (duu * duu);
-  const double dduu = dZ * eta2 * 2.0 * duu;
-  duR += dduu;
-  duL -= dduu;
-  double dsL = dWn * cL * cL, dsR = dWn * cR * cR;
-  dcL += dWn * sL * 2.0 * cL;
-  dcR += dWn * sR * 2.0 * cR;
-  // eta2 = 0.5 sL sR od od
-  const double od2 = od * od;
-  dsL += deta2 * 0.5 * sR * od2;
-  dsR += deta2 * 0.5 * sL * od2;
-  dod += deta2 * sL * sR * od;
-  // ubar = (sL uL + sR uR) od
-  dsL += dubar * uL * od;
-  dsR += dubar * uR * od;
-  duL += dubar * sL * od;
-  duR += dubar * sR * od;
-  dod += dubar * (sL * uL + sR * uR);
-  // od = 1 / (sL + sR)
-  const double dsum = -dod * od2;
-  dsL += dsum;
-  dsR += dsum;
-  drL += dsL * 0.5 * isL;
-  drR += dsR * 0.5 * isR;
-  // c = sqrt(y), y = gamma p / rho
-  const double dyL = dcL * 0.5 * L.ic, dyR = dcR * 0.5 * R.ic;
-  drL -= dyL * L.y * L.ir;
-  drR -= dyR * R.y * R.ir;
-  dPL[4] += dyL * L.ir * gamma;
-  dPR[4] += dyR * R.ir * gamma;
+  double dcL = 0.0, dcR = 0.0;
+  einfeldt_vjp(e, uL, uR, L.c, R.c, dSL, dSR, duL, duR, drL, drR, dcL, dcR);
+  sound_speed_vjp(L, gamma, dcL, dPL);
+  sound_speed_vjp(R, gamma, dcR, dPR);
   dPL[0] += drL;
   dPR[0] += drR;
   dPL[N] += duL;
   dPR[N] += duR;
   // U = cons(P)
+  cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
+  cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
+}
+
+// Reverse of hll<AX> with Einfeldt wave speeds (HLL.py:28-58):
+// F = N / den, N = SR FL - SL FR + SL SR (UR - UL), den = SR - SL + eps,
+// SL = min(sL, 0), SR = max(sR, 0).
+template <int AX>
+__device__ __forceinline__ void hll_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
+                                        const double dF[5], double dPL[5], double dPR[5]) {
+  constexpr int N = AX + 1;
+  const double gamma = fp.gamma;
+  const double igm1 = 1.0 / fp.gm1;
+  FaceSide L, R;
+  face_side(PL, gamma, igm1, L);
+  face_side(PR, gamma, igm1, R);
+  const double uL = PL[N], uR = PR[N];
+  Einfeldt e;
+  einfeldt_fwd(uL, uR, PL[0], PR[0], L.c, R.c, e);
+  const double SL = fmin(e.SL, 0.0), SR = fmax(e.SR, 0.0);
+  double FL[5], FR[5];
+  physical_flux<AX>(PL, L.U, FL);
+  physical_flux<AX>(PR, R.U, FR);
+  const double iden = 1.0 / ((SR - SL) + fp.eps);
+  double dSL = 0.0, dSR = 0.0, dden = 0.0;
+  double dFL[5], dFR[5], dUL[5], dUR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double dU = R.U[v] - L.U[v];
+    const double Fv = ((SR * FL[v] - SL * FR[v]) + (SL * SR) * dU) * iden;
+    const double dN = dF[v] * iden;
+    dden -= dF[v] * Fv * iden;
+    dSR += dN * (FL[v] + SL * dU);
+    dSL += dN * (SR * dU - FR[v]);
+    dFL[v] = dN * SR;
+    dFR[v] = -dN * SL;
+    dUR[v] = dN * SL * SR;
+    dUL[v] = -dUR[v];
+  }
+  dSR += dden;
+  dSL -= dden;
+  const double dsL = dSL * min_weight_a(e.SL, 0.0);
+  const double dsR = dSR * max_weight_a(e.SR, 0.0);
+  physical_flux_vjp<AX>(PL, L.U, dFL, dPL, dUL);
+  physical_flux_vjp<AX>(PR, R.U, dFR, dPR, dUR);
+  double duL = 0.0, duR = 0.0, drL = 0.0, drR = 0.0, dcL = 0.0, dcR = 0.0;
+  einfeldt_vjp(e, uL, uR, L.c, R.c, dsL, dsR, duL, duR, drL, drR, dcL, dcR);
+  sound_speed_vjp(L, gamma, dcL, dPL);
+  sound_speed_vjp(R, gamma, dcR, dPR);
+  dPL[0] += drL;
+  dPR[0] += drR;
+  dPL[N] += duL;
+  dPR[N] += duR;
   cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
   cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
@@ -500,6 +709,8 @@ __device__ __forceinline__ void riemann_flux_vjp(const double PL[5], const doubl
                                                  const double dF[5], double dPL[5], double dPR[5]) {
   if (RIEMANN == GBF_RIEMANN_HLLC)
     hllc_vjp<AX>(PL, PR, fp, dF, dPL, dPR);
+  else if (RIEMANN == GBF_RIEMANN_HLL)
+    hll_vjp<AX>(PL, PR, fp, dF, dPL, dPR);
   else
     rusanov_vjp<AX>(PL, PR, fp, dF, dPL, dPR);
 }

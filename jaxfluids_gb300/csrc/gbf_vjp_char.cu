@@ -1,0 +1,10 @@
+// Right-hand-side VJP kernels: WENO5-Z on characteristic variables (CHAR-PRIMITIVE).
+#include "gbf_vjp_kernels.cuh"
+
+namespace gbf {
+
+int launch_vjp_char(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s) {
+  return launch_vjp_riemann<RECON_WENO5Z_CHAR>(riemann, vp, grid, threads, smem, s);
+}
+
+}  // namespace gbf

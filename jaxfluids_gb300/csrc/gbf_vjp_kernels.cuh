@@ -1,0 +1,338 @@
+// Tile kernel of the right-hand-side VJP (the inviscid part), shared by the
+// translation units that instantiate one scheme family each
+// (gbf_vjp_<family>.cu, compiled in parallel); launched by gbf_adjoint.cu.
+#pragma once
+
+#include "gbf_adjoint.cuh"
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+struct VjpParams {
+  SweepParams sp;       // state U (sp.cons), sizes, tile, scheme
+  const double* w;      // cotangent of the rhs, interior [5][N]
+  double* dP;           // primitive cotangent accumulator, interior [5][N]
+};
+
+// CHAR-PRIMITIVE face (char_reconstruct of the forward): frozen state of the
+// two cells adjacent to the face, characteristic variables of the six window
+// cells, WENO5-Z with its gradients on each, back-projection, Riemann VJP, and
+// the reverse of all of it onto the window cells' primitives.  win points at
+// window cell 0 of variable 0 in the staged pencil (variable stride pvol, cell
+// stride ps); slot(v, k) = slot[(v * 6 + k) * fvol] receives the cotangent of
+// primitive v of window cell k; jr is this thread's private row block.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void char_face_vjp(const FaceParams& fp, const double* win, int pvol, int ps,
+                                              const double dF[5], double* slot, int fvol, double* jr_rows,
+                                              int nthr) {
+  constexpr int N = AX + 1;
+  using I = CharIds<AX>;
+  auto x = [&](int v, int k) { return win[v * pvol + k * ps]; };
+  auto SL = [&](int j, int k) -> double& { return slot[(j * 6 + k) * fvol]; };
+  auto JR = [&](int j, int i) -> double& { return jr_rows[(j * 5 + i) * nthr]; };
+  double Lc[5], Rc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    Lc[v] = x(v, 2);
+    Rc[v] = x(v, 3);
+  }
+  double rho_a, c, cc;
+  frozen_state(Lc, Rc, fp, rho_a, c, cc);
+  const double ic = 1.0 / c;
+  const double k_m = -0.5 * ic, k_p = 0.5 * ic;
+  const double k_e = 0.5 / (cc * rho_a);
+  const double k_s = 1.0 / cc;
+  const double eps = fp.stencil_eps;
+  // characteristic face values cL[j], cR[j]; gradients of char var j: left in
+  // slot(j, 0..4), right in the private rows
+  double cL[5], cR[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    double ch[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      if (j == 0) ch[k] = k_m * x(N, k) + k_e * x(4, k);
+      else if (j == 1) ch[k] = x(0, k) - k_s * x(4, k);
+      else if (j == 4) ch[k] = k_p * x(N, k) + k_e * x(4, k);
+      else ch[k] = x(j == I::e0 ? I::m0 : I::m1, k);
+    }
+    double jl[5], jr[5];
+    weno5z_jac(ch[0], ch[1], ch[2], ch[3], ch[4], eps, cL[j], jl);
+    weno5z_jac(ch[5], ch[4], ch[3], ch[2], ch[1], eps, cR[j], jr);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      SL(j, k) = jl[k];
+      JR(j, k) = jr[k];
+    }
+  }
+  double PL[5], PR[5];
+  PL[0] = rho_a * (cL[0] + cL[4]) + cL[1];
+  PL[N] = c * (-cL[0] + cL[4]);
+  PL[I::m0] = cL[I::e0];
+  PL[I::m1] = cL[I::e1];
+  PL[4] = cc * rho_a * (cL[0] + cL[4]);
+  PR[0] = rho_a * (cR[0] + cR[4]) + cR[1];
+  PR[N] = c * (-cR[0] + cR[4]);
+  PR[I::m0] = cR[I::e0];
+  PR[I::m1] = cR[I::e1];
+  PR[4] = cc * rho_a * (cR[0] + cR[4]);
+  double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+  riemann_flux_vjp<AX, RIEMANN>(PL, PR, fp, dF, dPL, dPR);
+  // back-projection reverse
+  double drho_a = 0.0, dc = 0.0, dcc = 0.0;
+  double gL[5], gR[5];
+  {
+    const double sL4 = cL[0] + cL[4], sR4 = cR[0] + cR[4];
+    const double ccr = cc * rho_a;
+    gL[0] = rho_a * dPL[0] - c * dPL[N] + ccr * dPL[4];
+    gL[4] = rho_a * dPL[0] + c * dPL[N] + ccr * dPL[4];
+    gL[1] = dPL[0];
+    gL[I::e0] = dPL[I::m0];
+    gL[I::e1] = dPL[I::m1];
+    gR[0] = rho_a * dPR[0] - c * dPR[N] + ccr * dPR[4];
+    gR[4] = rho_a * dPR[0] + c * dPR[N] + ccr * dPR[4];
+    gR[1] = dPR[0];
+    gR[I::e0] = dPR[I::m0];
+    gR[I::e1] = dPR[I::m1];
+    drho_a = (dPL[0] + cc * dPL[4]) * sL4 + (dPR[0] + cc * dPR[4]) * sR4;
+    dc = dPL[N] * (cL[4] - cL[0]) + dPR[N] * (cR[4] - cR[0]);
+    dcc = dPL[4] * rho_a * sL4 + dPR[4] * rho_a * sR4;
+  }
+  // per window cell: cotangents of the char variables, then of the primitives
+  double dk_m = 0.0, dk_p = 0.0, dk_e = 0.0, dk_s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double dch[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      double d = (k <= 4) ? gL[j] * SL(j, k) : 0.0;
+      if (k >= 1) d += gR[j] * JR(j, 5 - k);
+      dch[j] = d;
+    }
+    const double xn = x(N, k), x4 = x(4, k);
+    dk_m += dch[0] * xn;
+    dk_p += dch[4] * xn;
+    dk_e += (dch[0] + dch[4]) * x4;
+    dk_s -= dch[1] * x4;
+    double dx[5];
+    dx[0] = dch[1];
+    dx[N] = k_m * dch[0] + k_p * dch[4];
+    dx[4] = k_e * (dch[0] + dch[4]) - k_s * dch[1];
+    dx[I::m0] = dch[I::e0];
+    dx[I::m1] = dch[I::e1];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) SL(v, k) = dx[v];
+  }
+  // k_m = -0.5/c, k_p = 0.5/c, k_e = 0.5/(cc rho_a), k_s = 1/cc
+  dc += (dk_m - dk_p) * 0.5 * ic * ic;
+  const double dden = -dk_e * k_e / (cc * rho_a);
+  dcc += dden * rho_a - dk_s * k_s * k_s;
+  drho_a += dden * cc;
+  double dLc[5] = {0, 0, 0, 0, 0}, dRc[5] = {0, 0, 0, 0, 0};
+  frozen_state_vjp(Lc, Rc, fp, drho_a, dc, dcc, dLc, dRc);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    SL(v, 2) += dLc[v];
+    SL(v, 3) += dRc[v];
+  }
+}
+
+template <int AX, int RECON, int RIEMANN>
+__device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], const int ext[3],
+                                         double* sm_prim, double* sm_slot, double* sm_jr) {
+  constexpr int R = ReconTraits<RECON>::R;
+  constexpr int K = 2 * R;
+  const SweepParams& p = vp.sp;
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  int pe[3] = {ext[0], ext[1], ext[2]};
+  pe[AX] += 2 * R;
+  const int pvol = pe[0] * pe[1] * pe[2];
+  stage_pencil<AX, R, MODE_STAGE>(p, o, pe, pvol, sm_prim);
+  __syncthreads();
+
+  int fe[3] = {ext[0], ext[1], ext[2]};
+  fe[AX] += 1;
+  const int fvol = fe[0] * fe[1] * fe[2];
+  const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const double odx = p.one_dx[AX];
+  for (int f = tid; f < fvol; f += nthr) {
+    const int f2 = f % fe[2];
+    const int r = f / fe[2];
+    const int f1 = r % fe[1];
+    const int f0 = r / fe[1];
+    // cotangent of the face flux: rhs_i = odx (F_i - F_{i+1}).  A face on a
+    // tile boundary is computed by both tiles, and each tile's forward uses
+    // it only for its own cell, so each tile pulls back only the share of
+    // its own cells (this also drops cells outside the domain).
+    int gc[3] = {o[0] + f0, o[1] + f1, o[2] + f2};  // cell right of the face
+    const long long offR = ((long long)gc[0] * p.n[1] + gc[1]) * p.n[2] + gc[2];
+    gc[AX] -= 1;
+    const long long offL = ((long long)gc[0] * p.n[1] + gc[1]) * p.n[2] + gc[2];
+    const int fl = (AX == 0) ? f0 : ((AX == 1) ? f1 : f2);  // tile-local face index
+    const bool hasR = fl < ext[AX];
+    const bool hasL = fl >= 1;
+    double dF[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double wr = hasR ? __ldg(vp.w + v * cs + offR) : 0.0;
+      const double wl = hasL ? __ldg(vp.w + v * cs + offL) : 0.0;
+      dF[v] = odx * (wr - wl);
+    }
+    const int base = idx3(f0, f1, f2, pe[1], pe[2]);
+    double PL[5], PR[5];
+    if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS) {
+      // one pass gives the face states and the stencil gradients; the left
+      // gradient waits in the face's slots 0..4, the right one in this
+      // thread's private rows, until the Riemann cotangents are known
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K], jl[5], jr[5];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        if constexpr (RECON == GBF_RECON_WENO5Z) {
+          weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
+          weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
+        } else {
+          weno5js_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
+          weno5js_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          sm_slot[(v * K + k) * fvol + f] = jl[k];
+          sm_jr[(v * 5 + k) * nthr + tid] = jr[k];
+        }
+      }
+      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double gL = dPL[v], gR = dPR[v];
+        double jl[5], jr[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          jl[k] = sm_slot[(v * K + k) * fvol + f];
+          jr[k] = sm_jr[(v * 5 + k) * nthr + tid];
+        }
+        sm_slot[(v * K + 0) * fvol + f] = gL * jl[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) sm_slot[(v * K + k) * fvol + f] = gL * jl[k] + gR * jr[5 - k];
+        sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
+      }
+    } else if constexpr (RECON == RECON_WENO5Z_CHAR) {
+      char_face_vjp<AX, RIEMANN>(p.fp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol,
+                                 sm_jr + tid, nthr);
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        reconstruct_pair<RECON>(wv, p.fp.stencil_eps, PL[v], PR[v]);
+      }
+      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K], dw[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
+        reconstruct_pair_vjp<RECON>(wv, p.fp.stencil_eps, dPL[v], dPR[v], dw);
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm_slot[(v * K + k) * fvol + f] = dw[k];
+      }
+    }
+  }
+  __syncthreads();
+
+  // gather per pencil cell (fixed order), map back through the boundary
+  // remap and accumulate into the primitive cotangent
+  for (int i = tid; i < pvol; i += nthr) {
+    const int i2 = i % pe[2];
+    const int r = i / pe[2];
+    const int i1 = r % pe[1];
+    const int i0 = r / pe[1];
+    const int ia = (AX == 0) ? i0 : ((AX == 1) ? i1 : i2);
+    double d[5] = {0, 0, 0, 0, 0};
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int fa = ia - k;  // face whose stencil slot k is this cell
+      if (fa < 0 || fa >= fe[AX]) continue;
+      int fi[3] = {i0, i1, i2};
+      fi[AX] = fa;
+      const int f = idx3(fi[0], fi[1], fi[2], fe[1], fe[2]);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] += sm_slot[(v * K + k) * fvol + f];
+      any = true;
+    }
+    if (!any) continue;
+    int g[3] = {o[0] + i0, o[1] + i1, o[2] + i2};
+    g[AX] -= R;
+    if (g[AX] < 0 || g[AX] >= p.n[AX]) {
+      // halo cell: transpose of the face rule (DIRICHLET halos are constants)
+      const int t = p.bc[2 * AX + (g[AX] >= 0 ? 1 : 0)];
+      g[AX] = bc_src(g[AX], p.n[AX], t);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] *= bc_apply_grad(t, AX, v);
+    }
+    const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (d[v] != 0.0) atomicAdd(vp.dP + v * cs + off, d[v]);
+  }
+  __syncthreads();
+}
+
+template <int RECON, int RIEMANN>
+__global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
+  extern __shared__ double smem[];
+  const SweepParams& p = vp.sp;
+  const int b = blockIdx.x;
+  const int b2 = b % p.tiles[2];
+  const int b1 = (b / p.tiles[2]) % p.tiles[1];
+  const int b0 = b / (p.tiles[2] * p.tiles[1]);
+  const int o[3] = {b0 * p.t[0], b1 * p.t[1], b2 * p.t[2]};
+  const int ext[3] = {min(p.t[0], p.n[0] - o[0]), min(p.t[1], p.n[1] - o[1]), min(p.t[2], p.n[2] - o[2])};
+  constexpr int R = ReconTraits<RECON>::R;
+  int pmax = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    if (p.active_mask & (1 << a))
+      pmax = max(pmax, (p.t[0] + (a == 0 ? 2 * R : 0)) * (p.t[1] + (a == 1 ? 2 * R : 0)) *
+                           (p.t[2] + (a == 2 ? 2 * R : 0)));
+  // pencil primitives | per-thread right-stencil gradients (WENO only) | face slots
+  double* sm_prim = smem;
+  double* sm_jr = smem + 5 * pmax;
+  double* sm_slot = sm_jr + (ReconTraits<RECON>::R == 3 ? 25 * blockDim.x : 0);
+  if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+  if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+  if (p.active_mask & 4) vjp_axis<2, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
+}
+
+// Launch of rhs_vjp_kernel for one reconstruction family (mode of the
+// gbf_vjp_<family>.cu units): recon and riemann select the instantiation.
+int launch_vjp_weno5(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
+                     cudaStream_t s);
+int launch_vjp_char(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
+int launch_vjp_short(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
+                     cudaStream_t s);
+
+template <int RECON, int RIEMANN>
+int launch_vjp_one(const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s) {
+  auto k = rhs_vjp_kernel<RECON, RIEMANN>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return GBF_ERR_CUDA;
+  k<<<grid, threads, smem, s>>>(vp);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+template <int RECON>
+int launch_vjp_riemann(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s) {
+  if (riemann == GBF_RIEMANN_HLLC) return launch_vjp_one<RECON, GBF_RIEMANN_HLLC>(vp, grid, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLL) return launch_vjp_one<RECON, GBF_RIEMANN_HLL>(vp, grid, threads, smem, s);
+  return launch_vjp_one<RECON, GBF_RIEMANN_RUSANOV>(vp, grid, threads, smem, s);
+}
+
+}  // namespace gbf

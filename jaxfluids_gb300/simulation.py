@@ -152,8 +152,8 @@ class FusedRK3:
         """Counts of cells with non-finite values, rho <= 0 and p <= 0 in the
         current state (synchronises the stream to read them)."""
         counts = torch.zeros(3, dtype=torch.int64, device=self.device)
-        _lib.check(self.lib.gbf_state_check(ctypes.byref(self.case), _ptr(self.cons), _ptr(counts), _stream()),
-                   "state check")
+        _lib.check(self.lib.gbf_state_check(ctypes.byref(self.case), _ptr(self.cons),
+                                            ctypes.c_void_p(counts.data_ptr()), _stream()), "state check")
         nonfinite, rho, p = counts.tolist()
         return {"nonfinite": nonfinite, "rho_nonpositive": rho, "p_nonpositive": p}
 

@@ -75,8 +75,8 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     assert lib.gbf_rk3_stage(ctypes.byref(c), 0, buf, ctypes.c_void_p(24), ctypes.c_void_p(16), buf, None, None,
                              None) == _lib.GBF_ERR_INVALID_ARGUMENT
     assert lib.gbf_last_status() == _lib.GBF_ERR_INVALID_ARGUMENT
-    # the stage VJP rejects schemes the adjoint does not cover
-    hll = _case(riemann="HLL")
+    # the stage VJP rejects schemes the adjoint does not cover (HLL with Davis speeds)
+    hll = _case(riemann="HLL", signal_speed="DAVIS")
     assert lib.gbf_rk3_stage_vjp(ctypes.byref(hll), 1, buf, buf, buf, ctypes.c_void_p(16), ctypes.c_void_p(24),
                                  buf, None, None) == _lib.GBF_ERR_UNSUPPORTED
     # a solver handle needs a valid case

@@ -121,6 +121,13 @@ VJP_CASES = [
     ("2d-heat-only", (20, 24, 1), "PERIODIC", {"nh": 4, "heat": True, "mu": 0.05, "prandtl": 0.71}, "generic"),
     ("3d-viscous-noheatprod", (12, 16, 10), "PERIODIC", {"nh": 4, "viscous": True, "mu": 0.02,
                                                           "viscous_heat_production": False}, "generic"),
+    ("2d-weno5js-hll", (40, 36, 1), "PERIODIC", {"recon": "WENO5-JS", "riemann": "HLL"}, "generic"),
+    ("2d-weno3js-hllc", (40, 36, 1), "PERIODIC", {"recon": "WENO3-JS"}, "generic"),
+    ("2d-weno3z-rusanov-zg", (20, 36, 1), "ZEROGRADIENT", {"recon": "WENO3-Z", "riemann": "RUSANOV"}, "generic"),
+    ("3d-weno5z-hll", (12, 14, 10), "PERIODIC", {"riemann": "HLL"}, "generic"),
+    ("3d-char-roe-hll", (16, 12, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
+                                                   "riemann": "HLL"}, "generic"),
+    ("sod-minmodad-hll", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "HLL"}, "sod"),
     ("3d-char-roe-viscous-heat", (16, 12, 14), "PERIODIC", {"nh": 4, "recon_var": "CHAR-PRIMITIVE",
                                                              "frozen_state": "ROE", "viscous": True, "heat": True,
                                                              "mu": 0.02, "prandtl": 0.71}, "generic"),
