@@ -22,35 +22,57 @@ namespace gbf {
 namespace {
 
 // ---------------------------------------------------------------------------
-// Viscous and heat fluxes (CENTRAL4, periodic boundaries): the flux at a face
+// Viscous and heat fluxes (CENTRAL4, any boundary types): the flux at a face
 // is a function of the velocity gradient at the face (normal derivatives by
 // the face stencil, tangential ones as face interpolations of centre
 // derivatives), the face-interpolated velocity and the face derivative of T.
-// Pass 1 (one thread per face) turns the face-flux cotangent into the
-// cotangents of those 11 stencil outputs; pass 2 (one thread per cell) applies
-// the transposed stencils, gathers over every face whose stencil reads the
-// cell, pulls dT back through T = p / (rho R) and adds to the primitive
-// cotangent.  Fixed summation order: deterministic.
+// Every axis has N+1 faces (face i-1/2 at index i; the end faces take the
+// one-sided cotangent of their single interior cell, which is exact for
+// periodic axes too).  Pass 1 (one thread per face) turns the face-flux
+// cotangent into the cotangents of the 11 stencil outputs; pass 2 (one thread
+// per interior cell) applies the transposed stencils to every face whose
+// stencil reads the cell, pulls dT back through T = p / (rho R) and adds to
+// the primitive cotangent in a fixed order; pass 3 (one thread per face, only
+// faces whose stencil leaves the domain) sends the cotangents of halo cells
+// back through the transposed boundary rules (face rule, and the edge rule of
+// compute_edge_halos) with atomics.
 // ---------------------------------------------------------------------------
 constexpr int VISC_SLOTS = 11;  // dg[a][AX] (3), tangential (2 x 2), dvf (3), dTn
 
 struct ViscVjpParams {
-  int n[3];
-  int active_mask;
-  double one_dx[3];
-  const double* prims;  // interior primitives [5][N]
+  SweepParams sp;       // sizes, boundary rules, transport, interior primitives (sp.prims)
   const double* w;      // rhs cotangent [5][N]
-  double* fc;           // face cotangents [3][VISC_SLOTS][N]; face i-1/2 of axis a stored at cell i
+  double* fc;           // face cotangents: axis a at fc + foff[a], [VISC_SLOTS][faces of axis a]
+  long long foff[3];
   double* dP;           // primitive cotangent accumulator [5][N]
-  double mu1, mu2, kappa, R;
-  int viscous, heat, heat_production;
 };
 
-__device__ __forceinline__ long long wrap_off(const ViscVjpParams& p, int g0, int g1, int g2) {
-  g0 = (g0 < 0) ? g0 + p.n[0] : ((g0 >= p.n[0]) ? g0 - p.n[0] : g0);
-  g1 = (g1 < 0) ? g1 + p.n[1] : ((g1 >= p.n[1]) ? g1 - p.n[1] : g1);
-  g2 = (g2 < 0) ? g2 + p.n[2] : ((g2 >= p.n[2]) ? g2 - p.n[2] : g2);
-  return ((long long)g0 * p.n[1] + g1) * p.n[2] + g2;
+__device__ __forceinline__ long long cell_off(const SweepParams& p, const int g[3]) {
+  return ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+}
+
+__device__ __forceinline__ bool cell_inside(const SweepParams& p, const int g[3]) {
+  return (unsigned)g[0] < (unsigned)p.n[0] && (unsigned)g[1] < (unsigned)p.n[1] &&
+         (unsigned)g[2] < (unsigned)p.n[2];
+}
+
+// faces of axis AX: index q[AX] in [0, n], the others in [0, n)
+template <int AX>
+__device__ __forceinline__ long long face_count(const SweepParams& p) {
+  return (long long)(p.n[0] + (AX == 0)) * (p.n[1] + (AX == 1)) * (p.n[2] + (AX == 2));
+}
+
+template <int AX>
+__device__ __forceinline__ bool face_valid(const SweepParams& p, const int q[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    if (q[a] < 0 || q[a] > p.n[a] - (a == AX ? 0 : 1)) return false;
+  return true;
+}
+
+template <int AX>
+__device__ __forceinline__ long long face_off(const SweepParams& p, const int q[3]) {
+  return ((long long)q[0] * (p.n[1] + (AX == 1)) + q[1]) * (p.n[2] + (AX == 2)) + q[2];
 }
 
 // tangential axes of AX in ascending order (the ones that are active)
@@ -59,28 +81,93 @@ __device__ __forceinline__ int tangential(int t) {
   return (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
 }
 
-template <int AX>
-__global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams p) {
+// Transpose of the face rule of the face beyond which g lies along axis a
+// (bc_src / bc_apply): the cotangent d of the halo primitives goes to the
+// retrieved interior cell, scaled by d bc_apply / d x (DIRICHLET: nothing).
+__device__ __forceinline__ void face_halo_transpose(const SweepParams& p, int a, int g[3], const double d[5],
+                                                    double* dP) {
+  const int f = 2 * a + (g[a] >= 0 ? 1 : 0);
+  const int t = p.bc[f];
+  if (t == GBF_BC_DIRICHLET) return;
+  const int ga = g[a];
+  g[a] = bc_src(ga, p.n[a], t);
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const long long off = cell_off(p, g);
+  g[a] = ga;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double x = d[v] * bc_apply_grad(t, a, v);
+    if (x != 0.0) atomicAdd(dP + v * cs + off, x);
+  }
+}
+
+// Transpose of halo_prim: the cotangent d of the primitives of halo cell g
+// (outside along one or two axes) onto interior cells.
+__device__ __noinline__ void scatter_halo_cotangent(const SweepParams& p, int g0, int g1, int g2, double d0,
+                                                    double d1, double d2, double d3, double d4, double* dP) {
+  int g[3] = {g0, g1, g2};
+  double d[5] = {d0, d1, d2, d3, d4};
+  int out[3], k = 0;
+  for (int a = 0; a < 3; ++a)
+    if (g[a] < 0 || g[a] >= p.n[a]) out[k++] = a;
+  if (k == 1) {
+    face_halo_transpose(p, out[0], g, d, dP);
+    return;
+  }
+  const int a = out[0], b = out[1];
+  const int ta = p.bc[2 * a + (g[a] >= 0 ? 1 : 0)];
+  const int tb = p.bc[2 * b + (g[b] >= 0 ? 1 : 0)];
+  if (ta == GBF_BC_PERIODIC || ta == GBF_BC_SYMMETRY) {
+    g[a] = bc_src(g[a], p.n[a], ta);
+    if (ta == GBF_BC_SYMMETRY) d[a + 1] = -d[a + 1];
+    face_halo_transpose(p, b, g, d, dP);
+    return;
+  }
+  if (tb == GBF_BC_PERIODIC || tb == GBF_BC_SYMMETRY) {
+    g[b] = bc_src(g[b], p.n[b], tb);
+    if (tb == GBF_BC_SYMMETRY) d[b + 1] = -d[b + 1];
+    face_halo_transpose(p, a, g, d, dP);
+    return;
+  }
+  // ANY_ANY: 0.5 (edge '_10' + edge '_01')
+  double h[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) h[v] = 0.5 * d[v];
+  int ga[3] = {g[0], g[1], g[2]};
+  ga[a] += (g[a] < 0) ? p.nh : -p.nh;
+  face_halo_transpose(p, b, ga, h, dP);
+  int gb[3] = {g[0], g[1], g[2]};
+  gb[b] += (g[b] < 0) ? p.nh : -p.nh;
+  face_halo_transpose(p, a, gb, h, dP);
+}
+
+template <int AX>
+__global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams vp) {
+  const SweepParams& p = vp.sp;
+  const long long nf = face_count<AX>(p);
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= cs) return;
-  const int q2 = (int)(i % p.n[2]);
-  const int q1 = (int)((i / p.n[2]) % p.n[1]);
-  const int q0 = (int)(i / ((long long)p.n[2] * p.n[1]));
-  const int q[3] = {q0, q1, q2};
+  if (i >= nf) return;
+  const int e1 = p.n[1] + (AX == 1), e2 = p.n[2] + (AX == 2);
+  const int q[3] = {(int)(i / ((long long)e2 * e1)), (int)((i / e2) % e1), (int)(i % e2)};
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
   auto cell = [&](int v, int kax, int ax2, int k2) {
     int g[3] = {q[0], q[1], q[2]};
     g[AX] += kax;
     g[ax2] += k2;
-    return __ldg(p.prims + v * cs + wrap_off(p, g[0], g[1], g[2]));
+    return global_prim<MODE_STAGE_P>(p, v, g[0], g[1], g[2]);
   };
   const double odx = p.one_dx[AX];
-  int gl[3] = {q0, q1, q2};
+  // face cotangent: rhs_c = odx (F_{c-1/2} - F_{c+1/2}) over interior cells c
+  int gl[3] = {q[0], q[1], q[2]};
   gl[AX] -= 1;
-  const long long offL = wrap_off(p, gl[0], gl[1], gl[2]);
+  const bool hasR = q[AX] < p.n[AX], hasL = q[AX] >= 1;
   double dF[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) dF[v] = odx * (__ldg(p.w + v * cs + i) - __ldg(p.w + v * cs + offL));
+  for (int v = 0; v < 5; ++v) {
+    const double wr = hasR ? __ldg(vp.w + v * cs + cell_off(p, q)) : 0.0;
+    const double wl = hasL ? __ldg(vp.w + v * cs + cell_off(p, gl)) : 0.0;
+    dF[v] = odx * (wr - wl);
+  }
   double out[VISC_SLOTS];
 #pragma unroll
   for (int k = 0; k < VISC_SLOTS; ++k) out[k] = 0.0;
@@ -147,38 +234,43 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
     }
   }
   if (p.heat) out[10] = -p.kappa * dF[4];
-  double* fc = p.fc + (long long)AX * VISC_SLOTS * cs;
+  double* fc = vp.fc + vp.foff[AX];
 #pragma unroll
-  for (int k = 0; k < VISC_SLOTS; ++k) fc[k * cs + i] = out[k];
+  for (int k = 0; k < VISC_SLOTS; ++k) fc[k * nf + i] = out[k];
 }
 
-__global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpParams p) {
+// CENTRAL4 weights: face derivative (offsets -2..1), face interpolation,
+// centre derivative (offsets -2, -1, +1, +2)
+__device__ __constant__ double kFd[4] = {1.0 / 24.0, -27.0 / 24.0, 27.0 / 24.0, -1.0 / 24.0};
+__device__ __constant__ double kFi[4] = {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0};
+__device__ __constant__ double kCd[4] = {1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};
+__device__ __constant__ int kCj[4] = {-2, -1, 1, 2};
+
+__global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpParams vp) {
+  const SweepParams& p = vp.sp;
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= cs) return;
-  const int c2 = (int)(i % p.n[2]);
-  const int c1 = (int)((i / p.n[2]) % p.n[1]);
-  const int c0 = (int)(i / ((long long)p.n[2] * p.n[1]));
-  constexpr double fd[4] = {1.0 / 24.0, -27.0 / 24.0, 27.0 / 24.0, -1.0 / 24.0};
-  constexpr double fi[4] = {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0};
-  constexpr double cd[4] = {1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};  // offsets -2, -1, +1, +2
-  constexpr int cj[4] = {-2, -1, 1, 2};
+  const int c[3] = {(int)(i / ((long long)p.n[2] * p.n[1])), (int)((i / p.n[2]) % p.n[1]), (int)(i % p.n[2])};
   double du[3] = {0.0, 0.0, 0.0}, dT = 0.0;
 #pragma unroll
   for (int AX = 0; AX < 3; ++AX) {
     if (!(p.active_mask & (1 << AX))) continue;
-    const double* fc = p.fc + (long long)AX * VISC_SLOTS * cs;
+    const long long nf = (long long)(p.n[0] + (AX == 0)) * (p.n[1] + (AX == 1)) * (p.n[2] + (AX == 2));
+    const double* fc = vp.fc + vp.foff[AX];
+    const int e1 = p.n[1] + (AX == 1), e2 = p.n[2] + (AX == 2);
     const double odx = p.one_dx[AX];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       // this cell is stencil point k (offset k-2) of the face at q = c - (k-2) along AX
-      int g[3] = {c0, c1, c2};
-      g[AX] -= k - 2;
-      const long long f = wrap_off(p, g[0], g[1], g[2]);
-      const double wd = odx * fd[k];
+      int q[3] = {c[0], c[1], c[2]};
+      q[AX] -= k - 2;
+      if (q[AX] < 0 || q[AX] > p.n[AX]) continue;
+      const long long f = ((long long)q[0] * e1 + q[1]) * e2 + q[2];
+      const double wd = odx * kFd[k];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * cs + f] + fi[k] * fc[(7 + a) * cs + f];
-      dT += wd * fc[10 * cs + f];
+      for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * nf + f] + kFi[k] * fc[(7 + a) * nf + f];
+      dT += wd * fc[10 * nf + f];
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         const int ii = (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
@@ -186,12 +278,13 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
         const double odi = p.one_dx[ii];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          int h[3] = {g[0], g[1], g[2]};
-          h[ii] -= cj[jj];
-          const long long ff = wrap_off(p, h[0], h[1], h[2]);
-          const double wt = fi[k] * odi * cd[jj];
-          du[AX] += wt * fc[(3 + 2 * t) * cs + ff];
-          du[ii] += wt * fc[(4 + 2 * t) * cs + ff];
+          int h[3] = {q[0], q[1], q[2]};
+          h[ii] -= kCj[jj];
+          if (h[ii] < 0 || h[ii] >= p.n[ii]) continue;
+          const long long ff = ((long long)h[0] * e1 + h[1]) * e2 + h[2];
+          const double wt = kFi[k] * odi * kCd[jj];
+          du[AX] += wt * fc[(3 + 2 * t) * nf + ff];
+          du[ii] += wt * fc[(4 + 2 * t) * nf + ff];
         }
       }
     }
@@ -200,11 +293,70 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
   const double pr = __ldg(p.prims + 4 * cs + i);
   // T = p / (rho R)
   const double iden = 1.0 / (rho * p.R);
-  p.dP[i] += -dT * pr * iden / rho;
-  p.dP[cs + i] += du[0];
-  p.dP[2 * cs + i] += du[1];
-  p.dP[3 * cs + i] += du[2];
-  p.dP[4 * cs + i] += dT * iden;
+  vp.dP[i] += -dT * pr * iden / rho;
+  vp.dP[cs + i] += du[0];
+  vp.dP[2 * cs + i] += du[1];
+  vp.dP[3 * cs + i] += du[2];
+  vp.dP[4 * cs + i] += dT * iden;
+}
+
+// Pass 3: the stencil cells of face q (axis AX) that lie outside the domain.
+template <int AX>
+__global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpParams vp) {
+  const SweepParams& p = vp.sp;
+  const long long nf = face_count<AX>(p);
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  const int e1 = p.n[1] + (AX == 1), e2 = p.n[2] + (AX == 2);
+  const int q[3] = {(int)(i / ((long long)e2 * e1)), (int)((i / e2) % e1), (int)(i % e2)};
+  // faces whose whole stencil is interior have nothing to send
+  bool reaches_out = q[AX] < 2 || q[AX] > p.n[AX] - 2;
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const int ii = tangential<AX>(t);
+    if (p.viscous && (p.active_mask & (1 << ii)) && (q[ii] < 2 || q[ii] > p.n[ii] - 3)) reaches_out = true;
+  }
+  if (!reaches_out) return;
+  const double* fc = vp.fc + vp.foff[AX];
+  double s[VISC_SLOTS];
+#pragma unroll
+  for (int k = 0; k < VISC_SLOTS; ++k) s[k] = fc[k * nf + i];
+  const double odx = p.one_dx[AX];
+  for (int k = 0; k < 4; ++k) {
+    int g[3] = {q[0], q[1], q[2]};
+    g[AX] += k - 2;
+    if (g[AX] < 0 || g[AX] >= p.n[AX]) {
+      // normal stencil cell in the halo: velocity and temperature cotangents
+      const double wd = odx * kFd[k];
+      double d[5];
+      d[1] = wd * s[0] + kFi[k] * s[7];
+      d[2] = wd * s[1] + kFi[k] * s[8];
+      d[3] = wd * s[2] + kFi[k] * s[9];
+      const double dT = wd * s[10];
+      const double rho = global_prim<MODE_STAGE_P>(p, 0, g[0], g[1], g[2]);
+      const double pr = global_prim<MODE_STAGE_P>(p, 4, g[0], g[1], g[2]);
+      const double iden = 1.0 / (rho * p.R);
+      d[0] = -dT * pr * iden / rho;
+      d[4] = dT * iden;
+      scatter_halo_cotangent(p, g[0], g[1], g[2], d[0], d[1], d[2], d[3], d[4], vp.dP);
+    }
+    if (!p.viscous) continue;
+    for (int t = 0; t < 2; ++t) {
+      const int ii = tangential<AX>(t);
+      if (!(p.active_mask & (1 << ii))) continue;
+      const double odi = p.one_dx[ii];
+      for (int jj = 0; jj < 4; ++jj) {
+        int h[3] = {g[0], g[1], g[2]};
+        h[ii] += kCj[jj];
+        if (cell_inside(p, h)) continue;
+        const double wt = kFi[k] * odi * kCd[jj];
+        double d[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        d[1 + AX] = wt * s[3 + 2 * t];
+        d[1 + ii] = wt * s[4 + 2 * t];
+        scatter_halo_cotangent(p, h[0], h[1], h[2], d[0], d[1], d[2], d[3], d[4], vp.dP);
+      }
+    }
+  }
 }
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
@@ -266,10 +418,6 @@ int vjp_check(const gbf_case* c) {
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
-  // the viscous reverse pass indexes faces periodically (one face per cell)
-  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT))
-    for (int f = 0; f < 6; ++f)
-      if (c->n[f >> 1] > 1 && c->bc[f] != GBF_BC_PERIODIC) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
 }
 
@@ -277,9 +425,15 @@ inline bool vjp_dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VI
 
 // doubles of rhs-VJP scratch beyond the primitive cotangent: interior
 // primitives and the viscous face cotangents of every active axis
+// faces of axis a: N_a + 1 along a
+long long visc_faces(const CaseInfo& ci, int a) { return ci.cells / ci.n[a] * (ci.n[a] + 1); }
+
 long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
   if (!vjp_dissipative(c)) return 0;
-  return 5 * ci.cells + 3LL * VISC_SLOTS * ci.cells;
+  long long faces = 0;
+  for (int a = 0; a < 3; ++a)
+    if (ci.active_mask & (1 << a)) faces += visc_faces(ci, a);
+  return 5 * ci.cells + VISC_SLOTS * faces;
 }
 
 // VJP of the rhs at state U (interior): out = J(U)^T w.  dP: zeroed scratch of 5 n doubles
@@ -322,29 +476,27 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
   if (vjp_dissipative(c)) {
     ViscVjpParams q;
-    for (int a = 0; a < 3; ++a) {
-      q.n[a] = ci.n[a];
-      q.one_dx[a] = vp.sp.one_dx[a];
-    }
-    q.active_mask = ci.active_mask;
+    q.sp = vp.sp;
     double* P = extra;
-    q.prims = P;
+    q.sp.prims = P;
     q.w = w;
     q.fc = P + 5 * ci.cells;
     q.dP = dP;
-    q.mu1 = vp.sp.mu1;
-    q.mu2 = vp.sp.mu2;
-    q.kappa = vp.sp.kappa;
-    q.R = vp.sp.R;
-    q.viscous = vp.sp.viscous;
-    q.heat = vp.sp.heat;
-    q.heat_production = vp.sp.heat_production;
+    long long off = 0, nface[3];
+    for (int a = 0; a < 3; ++a) {
+      nface[a] = (ci.active_mask & (1 << a)) ? visc_faces(ci, a) : 0;
+      q.foff[a] = off;
+      off += VISC_SLOTS * nface[a];
+    }
     if ((st = launch_convert(c, U, P, ci.cells, 1, s)) != GBF_OK) return st;
-    const unsigned g = (unsigned)((ci.cells + 255) / 256);
-    if (ci.active_mask & 1) visc_face_vjp_kernel<0><<<g, 256, 0, s>>>(q);
-    if (ci.active_mask & 2) visc_face_vjp_kernel<1><<<g, 256, 0, s>>>(q);
-    if (ci.active_mask & 4) visc_face_vjp_kernel<2><<<g, 256, 0, s>>>(q);
-    visc_cell_gather_kernel<<<g, 256, 0, s>>>(q);
+    auto blocks = [](long long n) { return (unsigned)((n + 255) / 256); };
+    if (nface[0]) visc_face_vjp_kernel<0><<<blocks(nface[0]), 256, 0, s>>>(q);
+    if (nface[1]) visc_face_vjp_kernel<1><<<blocks(nface[1]), 256, 0, s>>>(q);
+    if (nface[2]) visc_face_vjp_kernel<2><<<blocks(nface[2]), 256, 0, s>>>(q);
+    visc_cell_gather_kernel<<<blocks(ci.cells), 256, 0, s>>>(q);
+    if (nface[0]) visc_halo_scatter_kernel<0><<<blocks(nface[0]), 256, 0, s>>>(q);
+    if (nface[1]) visc_halo_scatter_kernel<1><<<blocks(nface[1]), 256, 0, s>>>(q);
+    if (nface[2]) visc_halo_scatter_kernel<2><<<blocks(nface[2]), 256, 0, s>>>(q);
     if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
   }
   dp_to_du_kernel<<<grid_for(ci.cells), 256, 0, s>>>(U, dP, out, ci.cells, ci.fp.gm1);

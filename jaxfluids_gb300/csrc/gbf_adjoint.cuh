@@ -23,6 +23,12 @@ __device__ __forceinline__ double max_weight_a(double a, double b) {
   return (a > b) ? 1.0 : ((a == b) ? 0.5 : 0.0);
 }
 
+// Contraction is on in the reverse pass, except where the forward's rounding
+// decides a branch of the derivative: the smoothness terms (flat stencils give
+// exact zeros, |b0 - b2| ties) and the HLLC contact-speed numerator (mirrored
+// wall states give S* = 0 exactly, where jnp.sign blends both star fluxes)
+// use non-fusable products (__dmul_rn) to round like the forward.
+//
 // weno5z(u0..u4) and its gradient J[k] = d out / d u_k (the reverse pass with
 // unit cotangent), so a caller can scale J by the cotangent once it is known
 // without recomputing the stencil.  One reciprocal per denominator serves the
@@ -32,11 +38,11 @@ __device__ __forceinline__ void weno5z_jac(double u0, double u1, double u2, doub
                                            double eps, double& out, double J[5]) {
   constexpr double c13 = 13.0 / 12.0;
   const double t0 = u0 - 2.0 * u1 + u2;
-  const double t1 = u0 - 4.0 * u1 + 3.0 * u2;
+  const double t1 = (u0 - 4.0 * u1) + __dmul_rn(3.0, u2);
   const double t2 = u1 - 2.0 * u2 + u3;
   const double t3 = u1 - u3;
   const double t4 = u2 - 2.0 * u3 + u4;
-  const double t5 = 3.0 * u2 - 4.0 * u3 + u4;
+  const double t5 = fma(-4.0, u3, __dmul_rn(3.0, u2)) + u4;
   const double b0 = c13 * (t0 * t0) + 0.25 * (t1 * t1);
   const double b1 = c13 * (t2 * t2) + 0.25 * (t3 * t3);
   const double b2 = c13 * (t4 * t4) + 0.25 * (t5 * t5);
@@ -82,11 +88,11 @@ __device__ __forceinline__ void weno5js_jac(double u0, double u1, double u2, dou
                                             double eps, double& out, double J[5]) {
   constexpr double c13 = 13.0 / 12.0;
   const double t0 = u0 - 2.0 * u1 + u2;
-  const double t1 = u0 - 4.0 * u1 + 3.0 * u2;
+  const double t1 = (u0 - 4.0 * u1) + __dmul_rn(3.0, u2);
   const double t2 = u1 - 2.0 * u2 + u3;
   const double t3 = u1 - u3;
   const double t4 = u2 - 2.0 * u3 + u4;
-  const double t5 = 3.0 * u2 - 4.0 * u3 + u4;
+  const double t5 = fma(-4.0, u3, __dmul_rn(3.0, u2)) + u4;
   const double b0 = c13 * (t0 * t0) + 0.25 * (t1 * t1);
   const double b1 = c13 * (t2 * t2) + 0.25 * (t3 * t3);
   const double b2 = c13 * (t4 * t4) + 0.25 * (t5 * t5);
@@ -492,7 +498,7 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   einfeldt_fwd(uL, uR, rL, rR, L.c, R.c, e);
   const double SL = e.SL, SR = e.SR;
   const double rdL = rL * (SL - uL), rdR = rR * (SR - uR);
-  const double num = (pR - pL) + (uL * rdL - uR * rdR);
+  const double num = (pR - pL) + (__dmul_rn(uL, rdL) - __dmul_rn(uR, rdR));
   const double den = rdL - rdR;
   const double iden = 1.0 / den;
   const double Ss = num * iden;

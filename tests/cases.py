@@ -65,3 +65,29 @@ def rel_err(a: torch.Tensor, b: torch.Tensor) -> float:
         num = (a[v] - b[v]).abs().max().item()
         worst = max(worst, num / den if den > 0 else num)
     return worst
+
+
+def smooth_field(cells, seed, mean, amp):
+    """Sum of random-phase cosines varying along every active axis (no flat
+    directions, where WENO-Z's derivative is not numerically meaningful)."""
+    rng = np.random.default_rng(seed)
+    axes = [(np.arange(n) + 0.5) / n for n in cells]
+    X = np.meshgrid(*axes, indexing="ij")
+    f = np.full(X[0].shape, mean, dtype=np.float64)
+    for _ in range(3):
+        k = rng.integers(1, 3, size=3)
+        ph = rng.uniform(0, 2 * np.pi, size=3)
+        term = np.ones_like(f)
+        for a in range(3):
+            if cells[a] > 1:
+                term = term * np.cos(2 * np.pi * k[a] * X[a] + ph[a])
+        f = f + amp * rng.uniform(0.3, 1.0) * term
+    return f
+
+
+def generic_cons(cells, seed=0):
+    P = np.stack([smooth_field(cells, seed, 1.0, 0.2), smooth_field(cells, seed + 1, 0.0, 0.3),
+                  smooth_field(cells, seed + 2, 0.0, 0.3) if cells[1] > 1 else np.zeros(cells),
+                  smooth_field(cells, seed + 3, 0.0, 0.3) if cells[2] > 1 else np.zeros(cells),
+                  smooth_field(cells, seed + 4, 1.0, 0.2)])
+    return O.cons_from_prims(torch.from_numpy(P), 1.4)

@@ -1,14 +1,14 @@
 """WALL, DIRICHLET and NEUMANN boundaries (halos/outer/material.py:473-866) and
 the edge halos of the dissipative fluxes (:289-379) on the CUDA path against
 the oracle: right-hand side bitwise, halo buffers bitwise, RK3 steps through
-the drop-in and fused paths, and the inviscid adjoint."""
+the drop-in and fused paths, and the adjoint (viscous and inviscid)."""
 import math
 
 import pytest
 import torch
 
 from oracle import jf_oracle as O
-from tests.cases import both, quadrant_prims, rel_err, sod_prims, tgv_prims
+from tests.cases import both, generic_cons, quadrant_prims, rel_err, sod_prims, tgv_prims
 
 pytestmark = pytest.mark.gpu
 
@@ -137,7 +137,7 @@ def test_bc_steps(name, fused):
     assert rel_err(out, Ur[inner]) <= STEP_TOL
 
 
-ADJ_CASES = [c for c in IDS if not c.startswith(("2d-cavity", "3d-viscous", "3d-char-roe-viscous"))]
+ADJ_CASES = IDS
 
 
 @pytest.mark.parametrize("name", ADJ_CASES)
@@ -147,14 +147,10 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     oc, cc = both(cells, bc, bc_values=vals, **kw)
     if cc.recon == "MINMOD":
         pytest.skip("the adjoint is built for MINMOD-AD, not MINMOD")
-    U, P = O.initialize(_prims(kind, cells), oc)
-    Ui = U[oc.interior()].clone()
-    g = torch.Generator().manual_seed(21)
-    Ui = Ui * (1 + 1e-2 * torch.rand(Ui.shape, generator=g, dtype=torch.float64))
-    if cells[1] == 1:
-        Ui[2] = 0.0
-    if cells[2] == 1:
-        Ui[3] = 0.0
+    # smooth random-phase fields: WENO-Z's derivative amplifies rounding by
+    # up to 1/eps where stencils are flat, e.g. zero-gradient halos of a
+    # piecewise-constant state, so the comparison uses fields with none
+    Ui = generic_cons(cells, seed=3)
     w = torch.randn(Ui.shape, generator=torch.Generator().manual_seed(22), dtype=torch.float64)
     x = Ui.clone().requires_grad_(True)
     (O.rhs_of_interior_cons(x, oc) * w).sum().backward()
@@ -163,12 +159,18 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     assert rel_err(gv, x.grad) <= 1e-11
 
 
-def test_viscous_adjoint_rejects_non_periodic_boundaries():
-    from jaxfluids_gb300 import _lib
+@pytest.mark.parametrize("name", ["2d-cavity-viscous-heat", "3d-char-roe-viscous-sym-neumann-dirichlet-wall"])
+def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
-    _, cells, bc, vals, kw, kind = _case("2d-cavity-viscous-heat")
+    _, cells, bc, vals, kw, kind = _case(name)
     oc, cc = both(cells, bc, bc_values=vals, **kw)
-    adj = AdjointRK3(cc, dt=1e-3)
-    U = torch.ones((5,) + cells, dtype=torch.float64, device="cuda")
-    with pytest.raises(_lib.GbfError, match="unsupported"):
-        adj.rhs_vjp(U, U)
+    Ui = generic_cons(cells, seed=4)
+    dt = 0.2 * float(O.compute_dt(O.buffers_from_interior_cons(Ui, oc)[1], oc))
+    lam = torch.randn(Ui.shape, generator=torch.Generator().manual_seed(23), dtype=torch.float64)
+    if cells[2] == 1:
+        lam[3] = 0.0
+    x = Ui.clone().requires_grad_(True)
+    (O.rk3_step_interior(x, torch.tensor(dt, dtype=torch.float64), oc) * lam).sum().backward()
+    adj = AdjointRK3(cc, dt=dt)
+    g = adj.step_vjp(Ui.cuda().contiguous(), lam.cuda().contiguous())
+    assert rel_err(g, x.grad) <= 1e-11
