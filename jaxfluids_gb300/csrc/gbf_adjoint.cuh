@@ -190,33 +190,13 @@ __device__ __forceinline__ void minmod_ad_vjp(double b0, double b1, double b2, d
   }
 }
 
+// Reverse of reconstruct_pair<RECON> for the four-cell stencils (WENO3-JS,
+// WENO3-Z, MINMOD-AD): dw[k] = gL dL/dw_k + gR dR/dw_k.  The five-point WENO
+// stencils take the single-pass value-and-gradient route (weno5z_jac,
+// weno5js_jac) in the tile kernel instead.
 template <int RECON>
 __device__ __forceinline__ void reconstruct_pair_vjp(const double* w, double eps, double gL, double gR,
                                                      double* dw);
-
-template <>
-__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5Z>(const double* w, double eps,
-                                                                        double gL, double gR, double* dw) {
-  double jl[5], jr[5], vl, vr;
-  weno5z_jac(w[0], w[1], w[2], w[3], w[4], eps, vl, jl);
-  weno5z_jac(w[5], w[4], w[3], w[2], w[1], eps, vr, jr);
-  dw[0] = gL * jl[0];
-#pragma unroll
-  for (int k = 1; k < 5; ++k) dw[k] = gL * jl[k] + gR * jr[5 - k];
-  dw[5] = gR * jr[0];
-}
-
-template <>
-__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO5JS>(const double* w, double eps,
-                                                                         double gL, double gR, double* dw) {
-  double jl[5], jr[5], vl, vr;
-  weno5js_jac(w[0], w[1], w[2], w[3], w[4], eps, vl, jl);
-  weno5js_jac(w[5], w[4], w[3], w[2], w[1], eps, vr, jr);
-  dw[0] = gL * jl[0];
-#pragma unroll
-  for (int k = 1; k < 5; ++k) dw[k] = gL * jl[k] + gR * jr[5 - k];
-  dw[5] = gR * jr[0];
-}
 
 template <bool Z>
 __device__ __forceinline__ void weno3_pair_vjp(const double* w, double eps, double gL, double gR, double* dw) {
