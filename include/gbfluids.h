@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GBF_ABI_VERSION 2
+#define GBF_ABI_VERSION 3
 
 /* status codes */
 #define GBF_OK 0
@@ -80,6 +80,11 @@ extern "C" {
 #define GBF_BC_DIRICHLET 4
 #define GBF_BC_NEUMANN 5
 
+/* dissipative-flux stencils (stencils/reconstruction/central/central_{2,4}.py,
+ * stencils/derivative/deriv_{center,face}_{2,4}.py) */
+#define GBF_CENTRAL4 0
+#define GBF_CENTRAL2 1
+
 /* face order of gbf_case.bc */
 #define GBF_FACE_WEST 0
 #define GBF_FACE_EAST 1
@@ -117,6 +122,10 @@ typedef struct gbf_case {
   double bc_value[6][5]; /* per face, GBF_FACE_* order: WALL [1..3] = wall velocity
                             (u, v, w); DIRICHLET [0..4] = (rho, u, v, w, p);
                             NEUMANN [0..4] = normal derivatives of (rho, u, v, w, p) */
+  int32_t dissipative_stencil[3]; /* dissipative_fluxes.{reconstruction_stencil,
+                            derivative_stencil_center, derivative_stencil_face}: GBF_CENTRAL4 or
+                            GBF_CENTRAL2 (read_conservatives.py:374-445) */
+  int32_t reserved;
 } gbf_case;
 
 /* Launch shape of the fused sweep kernels; all-zero picks the built-in default

@@ -26,7 +26,8 @@ RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
-ABI_VERSION = 2  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+ABI_VERSION = 3  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
 FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
 FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION = 1, 2, 4
@@ -69,6 +70,8 @@ class GbfCase(ctypes.Structure):
         ("eps", ctypes.c_double),
         ("stencil_eps", ctypes.c_double),
         ("bc_value", (ctypes.c_double * 5) * 6),
+        ("dissipative_stencil", ctypes.c_int32 * 3),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -91,6 +91,11 @@ class CaseConfig:
     # constant boundary values per face: WALL (u, v, w), DIRICHLET and
     # NEUMANN (rho, u, v, w, p) (wall_velocity_callable / primitives_callable)
     bc_values: Dict[str, Tuple[float, ...]] = field(default_factory=dict)
+    # dissipative_fluxes.{reconstruction_stencil, derivative_stencil_center,
+    # derivative_stencil_face}: CENTRAL4 or CENTRAL2
+    diss_recon: str = "CENTRAL4"
+    diss_deriv_center: str = "CENTRAL4"
+    diss_deriv_face: str = "CENTRAL4"
 
     def __post_init__(self):
         self.cells = tuple(int(n) for n in self.cells)
@@ -136,8 +141,15 @@ class CaseConfig:
         if self.viscous or self.heat:
             if self.recon != "WENO5-Z":
                 raise NotImplementedError("dissipative fluxes are built with WENO5-Z convective fluxes")
-            if self.nh < 4:
-                raise SetupError("CENTRAL4 dissipative fluxes need halo_cells >= 4")
+            for key in ("diss_recon", "diss_deriv_center", "diss_deriv_face"):
+                if getattr(self, key) not in _lib.CENTRAL:
+                    raise NotImplementedError(f"dissipative stencil {getattr(self, key)}")
+            # centre derivatives on a ring of the reconstruction's halo width
+            # (source_term_solver.py:63-71): nh >= both halo widths together
+            halos = {"CENTRAL4": 2, "CENTRAL2": 1}
+            need_d = halos[self.diss_recon] + halos[self.diss_deriv_center] if self.viscous else 2
+            if self.nh < need_d:
+                raise SetupError(f"the dissipative stencils need halo_cells >= {need_d}")
 
     # domain/domain_information.py:80-206 and mesh_creation/homogenous.py:13
     @property
@@ -201,6 +213,9 @@ class CaseConfig:
         c.fixed_dt = float(self.fixed_dt) if self.fixed_dt else 0.0
         c.eps = self.eps
         c.stencil_eps = self.stencil_eps
+        c.dissipative_stencil[0] = _lib.CENTRAL[self.diss_recon]
+        c.dissipative_stencil[1] = _lib.CENTRAL[self.diss_deriv_center]
+        c.dissipative_stencil[2] = _lib.CENTRAL[self.diss_deriv_face]
         return c
 
     @classmethod
@@ -267,6 +282,9 @@ class CaseConfig:
                 kappa = float(tc.get("value", 0.0))
             else:
                 raise NotImplementedError("thermal conductivity model")
+        diss = cons.get("dissipative_fluxes", {}) or {}
+        if diss.get("is_laplacian", False):
+            raise NotImplementedError("dissipative_fluxes.is_laplacian")
         fixed = ti.get("fixed_timestep")
         prec = _get(numerical_setup, "precision", {}) or {}
         if prec.get("is_double_precision_compute", True) is False:
@@ -283,6 +301,9 @@ class CaseConfig:
             viscous=viscous, heat=heat, mu=mu, kappa=kappa,
             bulk_viscosity=float(transport.get("bulk_viscosity", 0.0) or 0.0),
             viscous_heat_production=bool(phys.get("is_viscous_heat_production", True)),
+            diss_recon=diss.get("reconstruction_stencil", "CENTRAL4"),
+            diss_deriv_center=diss.get("derivative_stencil_center", "CENTRAL4"),
+            diss_deriv_face=diss.get("derivative_stencil_face", "CENTRAL4"),
             eps=float(prec.get("epsilon", EPS)) if isinstance(prec.get("epsilon"), float) else EPS,
             stencil_eps=float(prec.get("spatial_stencil_epsilon", STENCIL_EPS))
             if isinstance(prec.get("spatial_stencil_epsilon"), float) else STENCIL_EPS,

@@ -178,29 +178,7 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
     if (p.heat_production) {
       // tau and the face velocity of the forward (energy flux sum_k tau_k vf_k)
       double gr[3][3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        gr[a][AX] = c4_face_deriv(odx, cell(1 + a, -2, AX, 0), cell(1 + a, -1, AX, 0), cell(1 + a, 0, AX, 0),
-                                  cell(1 + a, 1, AX, 0));
-#pragma unroll
-      for (int ii = 0; ii < 3; ++ii) {
-        if (ii == AX || !(p.active_mask & (1 << ii))) continue;
-        const double odi = p.one_dx[ii];
-#pragma unroll
-        for (int which = 0; which < 2; ++which) {
-          const int a = (which == 0) ? AX : ii;
-          double d[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            d[k] = c4_center_deriv(odi, cell(1 + a, k - 2, ii, -2), cell(1 + a, k - 2, ii, -1),
-                                   cell(1 + a, k - 2, ii, 1), cell(1 + a, k - 2, ii, 2));
-          gr[a][ii] = c4_face_interp(d[0], d[1], d[2], d[3]);
-        }
-      }
+      face_velocity_gradient<AX>(p, cell, gr);
       double tau[3], tr = 0.0;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -213,8 +191,7 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         if (!(p.active_mask & (1 << k))) continue;
-        const double vf = c4_face_interp(cell(1 + k, -2, AX, 0), cell(1 + k, -1, AX, 0), cell(1 + k, 0, AX, 0),
-                                         cell(1 + k, 1, AX, 0));
+        const double vf = face_interp_along<AX>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
         dtau[k] += dvt * vf;
         out[7 + k] = dvt * tau[k];
       }
@@ -239,11 +216,15 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
   for (int k = 0; k < VISC_SLOTS; ++k) fc[k * nf + i] = out[k];
 }
 
-// CENTRAL4 weights: face derivative (offsets -2..1), face interpolation,
-// centre derivative (offsets -2, -1, +1, +2)
-__device__ __constant__ double kFd[4] = {1.0 / 24.0, -27.0 / 24.0, 27.0 / 24.0, -1.0 / 24.0};
-__device__ __constant__ double kFi[4] = {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0};
-__device__ __constant__ double kCd[4] = {1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};
+// Weights of the dissipative stencils, [CENTRAL4, CENTRAL2]: face derivative
+// and face interpolation at normal offsets -2..1, centre derivative at offsets
+// -2, -1, +1, +2 (CENTRAL2 zero at the outer points)
+__device__ __constant__ double kFd[2][4] = {{1.0 / 24.0, -27.0 / 24.0, 27.0 / 24.0, -1.0 / 24.0},
+                                            {0.0, -1.0, 1.0, 0.0}};
+__device__ __constant__ double kFi[2][4] = {{-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0},
+                                            {0.0, 0.5, 0.5, 0.0}};
+__device__ __constant__ double kCd[2][4] = {{1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0},
+                                            {0.0, -0.5, 0.5, 0.0}};
 __device__ __constant__ int kCj[4] = {-2, -1, 1, 2};
 
 __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpParams vp) {
@@ -253,6 +234,9 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
   if (i >= cs) return;
   const int c[3] = {(int)(i / ((long long)p.n[2] * p.n[1])), (int)((i / p.n[2]) % p.n[1]), (int)(i % p.n[2])};
   double du[3] = {0.0, 0.0, 0.0}, dT = 0.0;
+  const double* Fd = kFd[p.diss_face];
+  const double* Fi = kFi[p.diss_recon];
+  const double* Cd = kCd[p.diss_center];
 #pragma unroll
   for (int AX = 0; AX < 3; ++AX) {
     if (!(p.active_mask & (1 << AX))) continue;
@@ -267,10 +251,13 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
       q[AX] -= k - 2;
       if (q[AX] < 0 || q[AX] > p.n[AX]) continue;
       const long long f = ((long long)q[0] * e1 + q[1]) * e2 + q[2];
-      const double wd = odx * kFd[k];
+      const double wd = odx * Fd[k];
+      if (wd != 0.0 || Fi[k] != 0.0) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * nf + f] + kFi[k] * fc[(7 + a) * nf + f];
-      dT += wd * fc[10 * nf + f];
+        for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * nf + f] + Fi[k] * fc[(7 + a) * nf + f];
+        dT += wd * fc[10 * nf + f];
+      }
+      if (Fi[k] == 0.0) continue;
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         const int ii = (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
@@ -278,11 +265,12 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
         const double odi = p.one_dx[ii];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
+          if (Cd[jj] == 0.0) continue;
           int h[3] = {q[0], q[1], q[2]};
           h[ii] -= kCj[jj];
           if (h[ii] < 0 || h[ii] >= p.n[ii]) continue;
           const long long ff = ((long long)h[0] * e1 + h[1]) * e2 + h[2];
-          const double wt = kFi[k] * odi * kCd[jj];
+          const double wt = Fi[k] * odi * Cd[jj];
           du[AX] += wt * fc[(3 + 2 * t) * nf + ff];
           du[ii] += wt * fc[(4 + 2 * t) * nf + ff];
         }
@@ -322,16 +310,20 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
 #pragma unroll
   for (int k = 0; k < VISC_SLOTS; ++k) s[k] = fc[k * nf + i];
   const double odx = p.one_dx[AX];
+  const double* Fd = kFd[p.diss_face];
+  const double* Fi = kFi[p.diss_recon];
+  const double* Cd = kCd[p.diss_center];
   for (int k = 0; k < 4; ++k) {
+    if (Fd[k] == 0.0 && Fi[k] == 0.0) continue;
     int g[3] = {q[0], q[1], q[2]};
     g[AX] += k - 2;
     if (g[AX] < 0 || g[AX] >= p.n[AX]) {
       // normal stencil cell in the halo: velocity and temperature cotangents
-      const double wd = odx * kFd[k];
+      const double wd = odx * Fd[k];
       double d[5];
-      d[1] = wd * s[0] + kFi[k] * s[7];
-      d[2] = wd * s[1] + kFi[k] * s[8];
-      d[3] = wd * s[2] + kFi[k] * s[9];
+      d[1] = wd * s[0] + Fi[k] * s[7];
+      d[2] = wd * s[1] + Fi[k] * s[8];
+      d[3] = wd * s[2] + Fi[k] * s[9];
       const double dT = wd * s[10];
       const double rho = global_prim<MODE_STAGE_P>(p, 0, g[0], g[1], g[2]);
       const double pr = global_prim<MODE_STAGE_P>(p, 4, g[0], g[1], g[2]);
@@ -340,16 +332,17 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
       d[4] = dT * iden;
       scatter_halo_cotangent(p, g[0], g[1], g[2], d[0], d[1], d[2], d[3], d[4], vp.dP);
     }
-    if (!p.viscous) continue;
+    if (!p.viscous || Fi[k] == 0.0) continue;
     for (int t = 0; t < 2; ++t) {
       const int ii = tangential<AX>(t);
       if (!(p.active_mask & (1 << ii))) continue;
       const double odi = p.one_dx[ii];
       for (int jj = 0; jj < 4; ++jj) {
+        if (Cd[jj] == 0.0) continue;
         int h[3] = {g[0], g[1], g[2]};
         h[ii] += kCj[jj];
         if (cell_inside(p, h)) continue;
-        const double wt = kFi[k] * odi * kCd[jj];
+        const double wt = Fi[k] * odi * Cd[jj];
         double d[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         d[1 + AX] = wt * s[3 + 2 * t];
         d[1 + ii] = wt * s[4 + 2 * t];

@@ -59,7 +59,16 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
     // cells for the centre-derivative ring (spatial_stencil.py:86-96); the
     // tangential stencils read edge halos (global_prim's edge rule)
     if (c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-    if (c->nh < 4) return GBF_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 3; ++k)
+      if (c->dissipative_stencil[k] != GBF_CENTRAL4 && c->dissipative_stencil[k] != GBF_CENTRAL2)
+        return GBF_ERR_UNSUPPORTED;
+    // centre derivatives on a ring of the reconstruction's halo width
+    // (source_term_solver.py:63-71): CENTRAL4 needs 2 cells, CENTRAL2 1
+    auto halos = [](int st) { return st == GBF_CENTRAL4 ? 2 : 1; };
+    const int need = (c->flags & GBF_FLAG_VISCOUS)
+                         ? halos(c->dissipative_stencil[0]) + halos(c->dissipative_stencil[1])
+                         : 2;
+    if (c->nh < need) return GBF_ERR_INVALID_ARGUMENT;
     if (!(c->mu >= 0.0) || !(c->kappa >= 0.0) || !(c->R > 0.0)) return GBF_ERR_INVALID_ARGUMENT;
   }
   if (!(c->gamma > 1.0)) return GBF_ERR_INVALID_ARGUMENT;

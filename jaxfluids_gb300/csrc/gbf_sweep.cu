@@ -109,6 +109,9 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   q.mu2 = c->bulk_mu - 2.0 / 3.0 * c->mu;  // compute_tau: bulk - 2/3 mu
   q.kappa = c->kappa;
   q.R = c->R;
+  q.diss_recon = c->dissipative_stencil[0];
+  q.diss_center = c->dissipative_stencil[1];
+  q.diss_face = c->dissipative_stencil[2];
   *p = q;
   *threads = thr;
   *smem = bytes;

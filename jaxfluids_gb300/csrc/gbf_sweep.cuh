@@ -59,6 +59,9 @@ struct SweepParams {
   double mu2;                // bulk viscosity - 2/3 mu
   double kappa;              // thermal conductivity
   double R;                  // specific gas constant
+  // dissipative stencils: 0 CENTRAL4, 1 CENTRAL2 (reconstruction, centre
+  // derivative, face derivative)
+  int diss_recon, diss_center, diss_face;
 };
 
 // Boundary rule of one face (halos/outer/material.py:140-210 with the
@@ -212,6 +215,60 @@ __device__ __forceinline__ double c4_face_deriv(double one_dx, double m2, double
 __device__ __forceinline__ double c4_face_interp(double m2, double m1, double c0, double p1) {
   return fma(-1.0 / 16.0, m2 + p1, (9.0 / 16.0) * (m1 + c0));  // -1/16 x exact
 }
+// CENTRAL2 stencils: deriv_center_2.py:33-44 ((1/dx) 1/2 (u[i+1] - u[i-1])),
+// deriv_face_2.py:30-45 ((1/dx) (u[i] - u[i-1])), central_2.py:30-41 (1/2 (u[i-1] + u[i]))
+__device__ __forceinline__ double c2_center_deriv(double one_dx, double m1, double p1) {
+  return (one_dx * 0.5) * (p1 - m1);
+}
+__device__ __forceinline__ double c2_face_deriv(double one_dx, double m1, double c0) {
+  return one_dx * (c0 - m1);
+}
+__device__ __forceinline__ double c2_face_interp(double m1, double c0) { return 0.5 * (m1 + c0); }
+
+// The dissipative face stencils of one face along AX (CENTRAL4 or CENTRAL2 by
+// SweepParams::diss_*).  at(k) is the value at normal offset k (cells k = -2..1
+// around face q - 1/2), cell(v, kax, ax2, k2) primitive v at normal offset kax
+// and offset k2 along axis ax2.
+template <class At>
+__device__ __forceinline__ double face_deriv_along(const SweepParams& p, double odx, const At& at) {
+  return (p.diss_face == 0) ? c4_face_deriv(odx, at(-2), at(-1), at(0), at(1)) : c2_face_deriv(odx, at(-1), at(0));
+}
+
+template <int AX, class At>
+__device__ __forceinline__ double face_interp_along(const SweepParams& p, const At& at) {
+  return (p.diss_recon == 0) ? c4_face_interp(at(-2), at(-1), at(0), at(1)) : c2_face_interp(at(-1), at(0));
+}
+
+// gr[a][b] = d u_a / d x_b at the face (zero for inactive axes and for the
+// tangential derivatives tau does not use): normal derivatives by the face
+// stencil, tangential ones as face reconstructions of centre derivatives
+// (source_term_solver.py compute_velocity_gradient :414-448 and
+// compute_xi_derivatives_at_xj :538-580, stencils chosen at :57-118).
+template <int AX, class Cell>
+__device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, const Cell& cell, double gr[3][3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
+  const double odx = p.one_dx[AX];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) gr[a][AX] = face_deriv_along(p, odx, [&](int k) { return cell(1 + a, k, AX, 0); });
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (i == AX || !(p.active_mask & (1 << i))) continue;
+    const double odi = p.one_dx[i];
+    // d u_AX / d x_i and d u_i / d x_i
+#pragma unroll
+    for (int which = 0; which < 2; ++which) {
+      const int a = (which == 0) ? AX : i;
+      gr[a][i] = face_interp_along<AX>(p, [&](int kax) {
+        return (p.diss_center == 0) ? c4_center_deriv(odi, cell(1 + a, kax, i, -2), cell(1 + a, kax, i, -1),
+                                                      cell(1 + a, kax, i, 1), cell(1 + a, kax, i, 2))
+                                    : c2_center_deriv(odi, cell(1 + a, kax, i, -1), cell(1 + a, kax, i, 1));
+      });
+    }
+  }
+}
 
 // Viscous and heat fluxes at the face of axis AX with logical face coordinates
 // q (the face lies between cells q[AX]-1 and q[AX]); source_term_solver.py
@@ -230,32 +287,8 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   };
   const double odx = p.one_dx[AX];
   if (p.viscous) {
-    // g_[a][b] = d u_a / d x_b at the face (zero for inactive axes)
     double gr[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-      gr[a][AX] = c4_face_deriv(odx, cell(1 + a, -2, AX, 0), cell(1 + a, -1, AX, 0),
-                                cell(1 + a, 0, AX, 0), cell(1 + a, 1, AX, 0));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      if (i == AX || !(p.active_mask & (1 << i))) continue;
-      const double odi = p.one_dx[i];
-      // tangential derivatives needed by tau: d u_AX / d x_i and d u_i / d x_i
-#pragma unroll
-      for (int which = 0; which < 2; ++which) {
-        const int a = (which == 0) ? AX : i;
-        double d[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          d[k] = c4_center_deriv(odi, cell(1 + a, k - 2, i, -2), cell(1 + a, k - 2, i, -1),
-                                 cell(1 + a, k - 2, i, 1), cell(1 + a, k - 2, i, 2));
-        gr[a][i] = c4_face_interp(d[0], d[1], d[2], d[3]);
-      }
-    }
+    face_velocity_gradient<AX>(p, cell, gr);
     double tau[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -275,8 +308,7 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         if (!(p.active_mask & (1 << k))) continue;
-        const double vf = c4_face_interp(cell(1 + k, -2, AX, 0), cell(1 + k, -1, AX, 0),
-                                         cell(1 + k, 0, AX, 0), cell(1 + k, 1, AX, 0));
+        const double vf = face_interp_along<AX>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
         vt = first ? tau[k] * vf : vt + tau[k] * vf;
         first = false;
       }
@@ -286,10 +318,9 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
     F[4] = F[4] + (-vt);
   }
   if (p.heat) {
-    double T[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) T[k] = cell(4, k - 2, AX, 0) / (cell(0, k - 2, AX, 0) * p.R);
-    F[4] = F[4] + (-p.kappa) * c4_face_deriv(odx, T[0], T[1], T[2], T[3]);
+    const double dT =
+        face_deriv_along(p, odx, [&](int k) { return cell(4, k, AX, 0) / (cell(0, k, AX, 0) * p.R); });
+    F[4] = F[4] + (-p.kappa) * dT;
   }
 }
 

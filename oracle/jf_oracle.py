@@ -72,6 +72,10 @@ class OracleCase:
     # (wall_velocity_callable), DIRICHLET (rho, u, v, w, p)
     # (primitives_callable), NEUMANN (rho, u, v, w, p) normal derivatives
     bc_values: Dict[str, Tuple[float, ...]] = field(default_factory=dict)
+    # dissipative_fluxes stencils: CENTRAL4 | CENTRAL2
+    diss_recon: str = "CENTRAL4"
+    diss_deriv_center: str = "CENTRAL4"
+    diss_deriv_face: str = "CENTRAL4"
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -533,38 +537,56 @@ def _ring_slices(case: OracleCase, n: int, axis: int, lo: int, hi: Optional[int]
     return tuple(sl)
 
 
-def _deriv_center_ring(buf: Tensor, case: OracleCase, axis_i: int, offset: int = 2) -> Tensor:
-    """DerivativeFourthOrderCenter.derivative_xi with offset (deriv_center_4.py:37-49).
+def _recon_halos(case: OracleCase) -> int:
+    # required_halos of the reconstruction stencil (central_4.py / central_2.py)
+    return 2 if case.diss_recon == "CENTRAL4" else 1
 
-    Built with offset = 2 (source_term_solver.py:63-71): the result covers the
-    interior plus a ring of two cells on every active axis.
+
+def _deriv_center_ring(buf: Tensor, case: OracleCase, axis_i: int) -> Tensor:
+    """Centre derivative with offset (deriv_center_4.py:37-49, deriv_center_2.py:33-44).
+
+    Built with offset = the reconstruction stencil's required halos
+    (source_term_solver.py:63-71): the result covers the interior plus a ring
+    of that many cells on every active axis.
     """
-    n = case.nh - offset
+    n = case.nh - _recon_halos(case)
 
     def sl(k):
         hi = -n + k   # nhi = -n + k + 1 - at_cell_center
         return _ring_slices(case, n, axis_i, n + k, hi if hi != 0 else None)
+    if case.diss_deriv_center == "CENTRAL2":
+        # 1.0 / dxi * coeffs[0] * (u[i+1] - u[i-1]), coeffs = (1/2,)
+        return 1.0 / case.cell_size(axis_i) * 0.5 * (buf[sl(1)] - buf[sl(-1)])
     return 1.0 / case.cell_size(axis_i) * (_C12[0] * (buf[sl(-2)] - buf[sl(2)]) + _C12[1] * (buf[sl(1)] - buf[sl(-1)]))
 
 
 def _recon4_from_ring(ring: Tensor, case: OracleCase, axis_j: int) -> Tensor:
-    """CentralFourthOrderReconstruction built with nh = 2 on the ring array (central_4.py:39-50)."""
-    n = 2
+    """Reconstruction stencil built with nh = its halo width on the ring array
+    (central_4.py:39-50, central_2.py:30-41)."""
+    n = _recon_halos(case)
 
     def sl(k):
         hi = -n + k + 1
         return _ring_slices(case, n, axis_j, n + k, hi if hi != 0 else None)
+    if case.diss_recon == "CENTRAL2":
+        return 0.5 * (ring[sl(-1)] + ring[sl(0)])
     return _C16[0] * (ring[sl(-2)] + ring[sl(1)]) + _C16[1] * (ring[sl(-1)] + ring[sl(0)])
 
 
 def _recon4(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
-    # reconstruct_stencil_ui (central_4.py:39-50) on the halo buffer
+    # reconstruct_stencil_ui (central_4.py:39-50, central_2.py:30-41) on the halo buffer
+    if case.diss_recon == "CENTRAL2":
+        s = [buf[_stencil_slice(case, axis, k)] for k in (-1, 0)]
+        return 0.5 * (s[0] + s[1])
     s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
     return _C16[0] * (s[0] + s[3]) + _C16[1] * (s[1] + s[2])
 
 
 def _deriv_face(buf: Tensor, case: OracleCase, axis: int) -> Tensor:
-    # DerivativeFourthOrderFace.derivative_xi (deriv_face_4.py:37-50)
+    # derivative_stencil_face (deriv_face_4.py:37-50, deriv_face_2.py:30-45)
+    if case.diss_deriv_face == "CENTRAL2":
+        s = [buf[_stencil_slice(case, axis, k)] for k in (-1, 0)]
+        return (1.0 / case.cell_size(axis)) * (s[1] - s[0])
     s = [buf[_stencil_slice(case, axis, k)] for k in (-2, -1, 0, 1)]
     return 1.0 / case.cell_size(axis) * (_C24[0] * (s[0] - s[3]) + _C24[1] * (s[2] - s[1]))
 

@@ -15,7 +15,7 @@ def both(cells, bc, **kw):
     fields = {k: v for k, v in kw.items() if k in (
         "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
         "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "viscous_heat_production",
-        "bc_values")}
+        "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face")}
     cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
     return oc, cc
 

@@ -70,3 +70,48 @@ def test_viscous_walls_accepted_by_the_library():
                      bc={f: "WALL" for f in ("east", "west", "north", "south")},
                      bc_values={f: (0.0, 0.0, 0.0) for f in ("east", "west", "north", "south")})
     assert _lib.load().gbf_case_check(cfg.to_c()) == _lib.GBF_OK
+
+
+@pytest.mark.parametrize("recon,center,nh,ok", [
+    ("CENTRAL4", "CENTRAL4", 4, True), ("CENTRAL4", "CENTRAL4", 3, False),
+    ("CENTRAL2", "CENTRAL4", 3, True), ("CENTRAL4", "CENTRAL2", 3, True), ("CENTRAL2", "CENTRAL2", 3, True)])
+def test_dissipative_stencil_halos(recon, center, nh, ok):
+    """Centre derivatives cover a ring as wide as the reconstruction's halos
+    (source_term_solver.py:57-79): the case needs nh >= both halo widths."""
+    kw = dict(cells=(16, 16, 1), bc={f: "PERIODIC" for f in ("east", "west", "north", "south", "top", "bottom")},
+              viscous=True, mu=0.01, diss_recon=recon, diss_deriv_center=center,
+              diss_deriv_face="CENTRAL2")
+    if ok:
+        cfg = CaseConfig(nh=nh, **kw)
+        assert _lib.load().gbf_case_check(cfg.to_c()) == _lib.GBF_OK
+        c = cfg.to_c()
+        c.nh = nh - 1
+        assert _lib.load().gbf_case_check(c) == _lib.GBF_ERR_INVALID_ARGUMENT
+    else:
+        with pytest.raises(SetupError):
+            CaseConfig(nh=nh, **kw)
+        c = CaseConfig(nh=4, **kw).to_c()
+        c.nh = nh
+        assert _lib.load().gbf_case_check(c) == _lib.GBF_ERR_INVALID_ARGUMENT
+
+
+def test_dissipative_stencils_from_setup():
+    case = {"domain": {"x": {"cells": 16, "range": [0, 1]}, "y": {"cells": 16, "range": [0, 1]},
+                       "z": {"cells": 1, "range": [0, 1]}},
+            "boundary_conditions": {f: {"type": "PERIODIC"} for f in ("east", "west", "north", "south",
+                                                                      "top", "bottom")},
+            "material_properties": {"equation_of_state": {"model": "IdealGas", "specific_heat_ratio": 1.4,
+                                                          "specific_gas_constant": 1.0},
+                                    "transport": {"dynamic_viscosity": {"model": "CUSTOM", "value": 0.01},
+                                                  "bulk_viscosity": 0.0,
+                                                  "thermal_conductivity": {"model": "PRANDTL", "prandtl_number": 0.72}}}}
+    num = {"conservatives": {"halo_cells": 3,
+                             "dissipative_fluxes": {"reconstruction_stencil": "CENTRAL2",
+                                                    "derivative_stencil_center": "CENTRAL2",
+                                                    "derivative_stencil_face": "CENTRAL2"}},
+           "active_physics": {"is_convective_flux": True, "is_viscous_flux": True, "is_heat_flux": True}}
+    cfg = CaseConfig.from_setups(case, num)
+    assert (cfg.diss_recon, cfg.diss_deriv_center, cfg.diss_deriv_face) == ("CENTRAL2",) * 3
+    c = cfg.to_c()
+    assert list(c.dissipative_stencil) == [_lib.CENTRAL["CENTRAL2"]] * 3
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_OK

@@ -1,5 +1,6 @@
 """WALL, DIRICHLET and NEUMANN boundaries (halos/outer/material.py:473-866) and
-the edge halos of the dissipative fluxes (:289-379) on the CUDA path against
+the edge halos of the dissipative fluxes (:289-379), with CENTRAL4 and CENTRAL2
+dissipative stencils, on the CUDA path against
 the oracle: right-hand side bitwise, halo buffers bitwise, RK3 steps through
 the drop-in and fused paths, and the adjoint (viscous and inviscid)."""
 import math
@@ -62,6 +63,18 @@ BC_CASES = [
      _faces(x=("WALL", "NEUMANN"), y=("ZEROGRADIENT", "WALL"), z=("SYMMETRY", "SYMMETRY")),
      {"west": (0.0, 0.1, 0.0), "east": GRAD, "north": (0.2, 0.0, 0.0)},
      dict(VISC, viscous_heat_production=False), "tgv"),
+    # CENTRAL2 dissipative stencils (reconstruction, centre and face derivative)
+    ("2d-cavity-viscous-heat-central2", (30, 26, 1), _faces(x=("WALL", "WALL"), y=("WALL", "WALL")),
+     {"west": (0.0, 0.0, 0.0), "east": (0.0, 0.0, 0.0), "south": (0.0, 0.0, 0.0), "north": (0.5, 0.0, 0.0)},
+     dict(VISC, nh=3, diss_recon="CENTRAL2", diss_deriv_center="CENTRAL2", diss_deriv_face="CENTRAL2"), "quad"),
+    ("3d-viscous-mixed-stencils-wall-neumann", (14, 12, 10),
+     _faces(y=("WALL", "NEUMANN"), z=("ZEROGRADIENT", "SYMMETRY")),
+     {"south": (0.2, 0.0, -0.1), "north": GRAD},
+     dict(VISC, nh=3, diss_recon="CENTRAL2", diss_deriv_center="CENTRAL4", diss_deriv_face="CENTRAL2"), "tgv"),
+    ("3d-char-roe-viscous-c4recon-c2deriv", (12, 12, 12), _faces(x=("WALL", "DIRICHLET")),
+     {"west": (0.0, 0.0, 0.1), "east": (1.0, 0.1, 0.0, 0.05, 72.0)},
+     dict(VISC, recon_var="CHAR-PRIMITIVE", frozen_state="ROE", diss_recon="CENTRAL4", diss_deriv_center="CENTRAL2",
+          diss_deriv_face="CENTRAL4"), "tgv"),
 ]
 
 
@@ -159,7 +172,8 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     assert rel_err(gv, x.grad) <= 1e-11
 
 
-@pytest.mark.parametrize("name", ["2d-cavity-viscous-heat", "3d-char-roe-viscous-sym-neumann-dirichlet-wall"])
+@pytest.mark.parametrize("name", ["2d-cavity-viscous-heat", "3d-char-roe-viscous-sym-neumann-dirichlet-wall",
+                                  "2d-cavity-viscous-heat-central2", "3d-viscous-mixed-stencils-wall-neumann"])
 def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
