@@ -97,6 +97,10 @@ extern "C" {
 #define GBF_FLAG_VISCOUS 1u
 #define GBF_FLAG_HEAT 2u
 #define GBF_FLAG_VISCOUS_HEAT_PRODUCTION 4u
+/* active_physics.is_convective_flux = false: the face flux starts at zero and
+   carries only the dissipative fluxes (space_solver.py:512-529); needs
+   GBF_FLAG_VISCOUS or GBF_FLAG_HEAT */
+#define GBF_FLAG_NO_CONVECTIVE 8u
 
 /* Case descriptor: the numerical_setup / case_setup keys the path reads. */
 typedef struct gbf_case {

@@ -30,7 +30,7 @@ ABI_VERSION = 3  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
 FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
-FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION = 1, 2, 4
+FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION, FLAG_NO_CONVECTIVE = 1, 2, 4, 8
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (

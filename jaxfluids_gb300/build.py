@@ -66,8 +66,12 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
         return obj, r.stderr
 
+    # the instantiation units of the large kernels start first, so that the
+    # small units fill in beside them
+    heavy = ("visc", "char", "vjp", "weno")
+    order = sorted(srcs, key=lambda p: (not any(h in os.path.basename(p) for h in heavy), p))
     with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1, len(srcs)))) as ex:
-        results = list(ex.map(compile_one, srcs))
+        results = list(ex.map(compile_one, order))
     for obj, log in results:
         if verbose and log:
             print(log, file=sys.stderr)

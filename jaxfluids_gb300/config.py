@@ -96,6 +96,8 @@ class CaseConfig:
     diss_recon: str = "CENTRAL4"
     diss_deriv_center: str = "CENTRAL4"
     diss_deriv_face: str = "CENTRAL4"
+    # active_physics.is_convective_flux: False leaves only the dissipative fluxes
+    convective: bool = True
 
     def __post_init__(self):
         self.cells = tuple(int(n) for n in self.cells)
@@ -138,9 +140,9 @@ class CaseConfig:
         if self.heat and self.prandtl is not None and not self.kappa:
             # PRANDTL model (materials/single_materials/material.py:115-116)
             self.kappa = self.gamma / (self.gamma - 1.0) * self.R * self.mu / self.prandtl
+        if not self.convective and not (self.viscous or self.heat):
+            raise SetupError("no convective, viscous or heat flux is active")
         if self.viscous or self.heat:
-            if self.recon != "WENO5-Z":
-                raise NotImplementedError("dissipative fluxes are built with WENO5-Z convective fluxes")
             for key in ("diss_recon", "diss_deriv_center", "diss_deriv_face"):
                 if getattr(self, key) not in _lib.CENTRAL:
                     raise NotImplementedError(f"dissipative stencil {getattr(self, key)}")
@@ -203,6 +205,8 @@ class CaseConfig:
             flags |= _lib.FLAG_HEAT
         if self.viscous_heat_production:
             flags |= _lib.FLAG_VISCOUS_HEAT_PRODUCTION
+        if not self.convective:
+            flags |= _lib.FLAG_NO_CONVECTIVE
         c.flags = flags
         c.gamma = self.gamma
         c.R = self.R
@@ -257,8 +261,6 @@ class CaseConfig:
         for key in ("is_volume_force", "is_geometric_source", "is_surface_tension"):
             if phys.get(key, False):
                 raise NotImplementedError(key)
-        if not phys.get("is_convective_flux", True):
-            raise NotImplementedError("is_convective_flux = false")
         transport = _get(case_setup, "material_properties.transport", {}) or {}
         mu = 0.0
         if viscous:
@@ -304,6 +306,7 @@ class CaseConfig:
             diss_recon=diss.get("reconstruction_stencil", "CENTRAL4"),
             diss_deriv_center=diss.get("derivative_stencil_center", "CENTRAL4"),
             diss_deriv_face=diss.get("derivative_stencil_face", "CENTRAL4"),
+            convective=bool(phys.get("is_convective_flux", True)),
             eps=float(prec.get("epsilon", EPS)) if isinstance(prec.get("epsilon"), float) else EPS,
             stencil_eps=float(prec.get("spatial_stencil_epsilon", STENCIL_EPS))
             if isinstance(prec.get("spatial_stencil_epsilon"), float) else STENCIL_EPS,

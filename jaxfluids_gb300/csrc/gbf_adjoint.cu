@@ -406,6 +406,7 @@ inline int grid_for(long long n) {
 }
 
 int vjp_check(const gbf_case* c) {
+  if (c->flags & GBF_FLAG_NO_CONVECTIVE) return GBF_OK;  // no convective scheme to reverse
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
@@ -459,7 +460,9 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   vp.w = w;
   vp.dP = dP;
   const int grid = vp.sp.tiles[0] * vp.sp.tiles[1] * vp.sp.tiles[2];
-  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+  if (c->flags & GBF_FLAG_NO_CONVECTIVE)
+    st = GBF_OK;  // dissipative fluxes only
+  else if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
     st = launch_vjp_char(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
     st = launch_vjp_weno5(c->recon, c->riemann, vp, grid, threads, smem, s);

@@ -54,11 +54,13 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_HLL) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
+  if (c->flags & ~(GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_VISCOUS_HEAT_PRODUCTION | GBF_FLAG_NO_CONVECTIVE))
+    return GBF_ERR_INVALID_ARGUMENT;
+  if ((c->flags & GBF_FLAG_NO_CONVECTIVE) && !(c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)))
+    return GBF_ERR_INVALID_ARGUMENT;  // nothing to compute
   if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) {
-    // CENTRAL4 dissipative fluxes: WENO5-Z convective part and four halo
-    // cells for the centre-derivative ring (spatial_stencil.py:86-96); the
-    // tangential stencils read edge halos (global_prim's edge rule)
-    if (c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
+    // dissipative fluxes beside any convective scheme; the tangential
+    // stencils read edge halos (global_prim's edge rule)
     for (int k = 0; k < 3; ++k)
       if (c->dissipative_stencil[k] != GBF_CENTRAL4 && c->dissipative_stencil[k] != GBF_CENTRAL2)
         return GBF_ERR_UNSUPPORTED;

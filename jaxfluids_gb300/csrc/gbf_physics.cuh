@@ -507,11 +507,18 @@ __device__ __forceinline__ void hll(const double PL[5], const double PR[5], cons
   for (int v = 0; v < 5; ++v) F[v] = ((SR * FL[v] - SL * FR[v]) + SLR * (UR[v] - UL[v])) / den;
 }
 
+// Face flux without a convective part (GBF_FLAG_NO_CONVECTIVE): flux_xi =
+// zeros, the dissipative fluxes are added to it.
+constexpr int RIEMANN_NONE = 100;
+
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux(const double PL[5], const double PR[5],
                                              const FaceParams& fp, double F[5]) {
   double UL[5], UR[5];
-  if (RIEMANN == GBF_RIEMANN_HLLC) {
+  if (RIEMANN == RIEMANN_NONE) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = 0.0;
+  } else if (RIEMANN == GBF_RIEMANN_HLLC) {
     hllc<AX>(PL, PR, fp, F);  // forms the conservatives of the side(s) it uses
   } else if (RIEMANN == GBF_RIEMANN_HLL) {
     cons_from_prims(PL, UL, fp.gm1);

@@ -125,8 +125,11 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
   if (visc) {
     // dissipative fluxes read the primitive buffer (MODE_STAGE_P) or the halo buffer
     if (mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
-    return chr ? launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s)
-               : launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
+    if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_sweep_dissipative(mode, p, threads, smem, s);
+    if (chr) return launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s);
+    if (c->recon == GBF_RECON_WENO5Z) return launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
+    if (c->recon == GBF_RECON_WENO5JS) return launch_sweep_weno5js_visc(c->riemann, mode, p, threads, smem, s);
+    return launch_sweep_short_visc(c->recon, c->riemann, mode, p, threads, smem, s);
   }
   if (mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
   if (chr) return launch_sweep_char(c->riemann, mode, p, threads, smem, s);

@@ -392,8 +392,10 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
   pe[AX] += 2 * R;
   const int pvol = pe[0] * pe[1] * pe[2];
 
-  stage_pencil<AX, R, MODE>(p, o, pe, pvol, sm_prim);
-  __syncthreads();
+  if (RIEMANN != RIEMANN_NONE) {
+    stage_pencil<AX, R, MODE>(p, o, pe, pvol, sm_prim);
+    __syncthreads();
+  }
 
   // ---- face fluxes, one face per thread --------------------------------
   int fe[3] = {ext[0], ext[1], ext[2]};
@@ -409,7 +411,9 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
-    if (RECON == RECON_WENO5Z_CHAR) {
+    if (RIEMANN == RIEMANN_NONE) {
+      // no convective flux: nothing to reconstruct
+    } else if (RECON == RECON_WENO5Z_CHAR) {
       const double* b = sm_prim + base;
       auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
       char_reconstruct<AX>(w, p.fp, PL, PR);

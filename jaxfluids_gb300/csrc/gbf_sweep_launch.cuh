@@ -37,5 +37,11 @@ int launch_sweep_muscl(int recon, int riemann, int mode, const SweepParams& p, i
 int launch_sweep_weno5js(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                              cudaStream_t s);
+// viscous / heat fluxes with the other PRIMITIVE reconstructions, and the
+// dissipative fluxes alone (no convective flux)
+int launch_sweep_weno5js_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_short_visc(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                            cudaStream_t s);
+int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 
 }  // namespace gbf

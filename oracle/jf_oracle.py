@@ -76,6 +76,10 @@ class OracleCase:
     diss_recon: str = "CENTRAL4"
     diss_deriv_center: str = "CENTRAL4"
     diss_deriv_face: str = "CENTRAL4"
+    # active_physics.is_convective_flux
+    convective: bool = True
+    # thermal_conductivity CUSTOM value (None: PRANDTL model from prandtl)
+    thermal_conductivity: Optional[float] = None
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -122,7 +126,10 @@ class OracleCase:
         return self.gamma / (self.gamma - 1.0) * self.R
 
     def kappa(self) -> float:
-        # PRANDTL model (materials/single_materials/material.py:115-116): cp mu / Pr
+        # CUSTOM constant value, else the PRANDTL model
+        # (materials/single_materials/material.py:115-116): cp mu / Pr
+        if self.thermal_conductivity is not None:
+            return self.thermal_conductivity
         return self.cp() * self.mu / self.prandtl
 
 
@@ -655,7 +662,11 @@ def compute_rhs(U: Tensor, P: Tensor, case: OracleCase) -> Tensor:
     """
     rhs = None
     for axis in case.active:
-        flux = convective_flux_xi(P, case, axis)
+        if case.convective:
+            flux = convective_flux_xi(P, case, axis)
+        else:
+            # space_solver.py:510: flux_xi = zeros(flux_shapes[axis])
+            flux = torch.zeros((5,) + _deriv_face(P[:1], case, axis).shape[1:], dtype=P.dtype)
         if case.viscous:
             # space_solver.py:565-573: flux.at[1:5].add(-visc)
             visc = viscous_flux_xi(P, case, axis)

@@ -11,11 +11,14 @@ def both(cells, bc, **kw):
     """(OracleCase, CaseConfig) for the same setup."""
     from jaxfluids_gb300.config import CaseConfig
     bcd = {f: bc[f] if isinstance(bc, dict) else bc for f in O.FACES}
-    oc = O.OracleCase(cells=cells, bc=bcd, **kw)
+    okw = {k: v for k, v in kw.items() if k != "kappa"}
+    if "kappa" in kw:
+        okw["thermal_conductivity"] = kw["kappa"]
+    oc = O.OracleCase(cells=cells, bc=bcd, **okw)
     fields = {k: v for k, v in kw.items() if k in (
         "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
-        "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "viscous_heat_production",
-        "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face")}
+        "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "kappa", "viscous_heat_production",
+        "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face", "convective")}
     cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
     return oc, cc
 

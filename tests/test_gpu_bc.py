@@ -75,6 +75,29 @@ BC_CASES = [
      {"west": (0.0, 0.0, 0.1), "east": (1.0, 0.1, 0.0, 0.05, 72.0)},
      dict(VISC, recon_var="CHAR-PRIMITIVE", frozen_state="ROE", diss_recon="CENTRAL4", diss_deriv_center="CENTRAL2",
           diss_deriv_face="CENTRAL4"), "tgv"),
+    # dissipative fluxes beside the other reconstructions (lid-driven cavity:
+    # WENO5-JS + HLLC + CENTRAL4 viscous, no heat production)
+    ("2d-cavity-weno5js-viscous", (28, 30, 1), _faces(x=("WALL", "WALL"), y=("WALL", "WALL")),
+     {"west": (0.0, 0.0, 0.0), "east": (0.0, 0.0, 0.0), "south": (0.0, 0.0, 0.0), "north": (0.5, 0.0, 0.0)},
+     dict(nh=4, recon="WENO5-JS", viscous=True, mu=0.01, viscous_heat_production=False), "quad"),
+    ("3d-weno3z-rusanov-viscous-heat", (12, 10, 14), _faces(y=("WALL", "ZEROGRADIENT")),
+     {"south": (0.1, 0.0, 0.0)}, dict(VISC, recon="WENO3-Z", riemann="RUSANOV"), "tgv"),
+    ("2d-minmod-ad-hll-viscous-heat-c2", (26, 24, 1), _faces(x=("DIRICHLET", "NEUMANN"), y=("SYMMETRY", "WALL")),
+     {"west": IN_STATE, "east": GRAD, "north": (0.2, 0.0, 0.0)},
+     dict(VISC, nh=3, recon="MINMOD-AD", riemann="HLL", diss_recon="CENTRAL2", diss_deriv_center="CENTRAL2",
+          diss_deriv_face="CENTRAL2"), "quad"),
+    # no convective flux (active_physics.is_convective_flux = false): Couette
+    # flow, and heat conduction alone with a constant CUSTOM conductivity
+    ("2d-couette-viscous-only", (16, 24, 1), _faces(y=("WALL", "WALL")),
+     {"south": (0.0, 0.0, 0.0), "north": (0.1, 0.0, 0.0)},
+     dict(nh=4, recon="WENO5-JS", viscous=True, mu=0.1, convective=False), "quad"),
+    ("1d-heat-only-dirichlet", (64, 1, 1), _faces(x=("DIRICHLET", "DIRICHLET")),
+     {"west": (1.0, 0.0, 0.0, 0.0, 1.0), "east": (0.5, 0.0, 0.0, 0.0, 1.0)},
+     dict(nh=4, recon="WENO5-JS", heat=True, kappa=0.1, convective=False), "sod"),
+    ("3d-heat-viscous-only-c2", (10, 12, 8), _faces(x=("DIRICHLET", "WALL"), z=("NEUMANN", "ZEROGRADIENT")),
+     {"west": (1.0, 0.0, 0.1, 0.0, 1.2), "east": (0.0, 0.1, 0.0), "bottom": GRAD},
+     dict(VISC, nh=3, convective=False, diss_recon="CENTRAL2", diss_deriv_center="CENTRAL2",
+          diss_deriv_face="CENTRAL4"), "tgv"),
 ]
 
 
@@ -173,7 +196,9 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
 
 
 @pytest.mark.parametrize("name", ["2d-cavity-viscous-heat", "3d-char-roe-viscous-sym-neumann-dirichlet-wall",
-                                  "2d-cavity-viscous-heat-central2", "3d-viscous-mixed-stencils-wall-neumann"])
+                                  "2d-cavity-viscous-heat-central2", "3d-viscous-mixed-stencils-wall-neumann",
+                                  "2d-cavity-weno5js-viscous", "2d-couette-viscous-only",
+                                  "3d-heat-viscous-only-c2"])
 def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
