@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GBF_ABI_VERSION 3
+#define GBF_ABI_VERSION 4
 
 /* status codes */
 #define GBF_OK 0
@@ -71,14 +71,20 @@ extern "C" {
  * u_halo = 2 u_wall - u (:473-531), DIRICHLET sets the given primitives
  * (:732-798), NEUMANN adds sign * dx * gradient to the boundary cell
  * (:825-866; sign +1 at west/south/bottom, -1 at east/north/top).  Values
- * come from gbf_case.bc_value; spatially or temporally varying callables and
- * several types on one face are not supported. */
+ * come from gbf_case.bc_value, or per boundary cell from
+ * gbf_case.bc_field_values (callables of the boundary coordinates).
+ * GBF_BC_MIXED marks a face of several types (bounding_domain masks,
+ * material.py:252-266): gbf_case.bc_field_types gives the type of each
+ * boundary cell, and the edges of such a face take the mean rule
+ * (boundary_condition.py:128-177, "ANY").  Values varying in time are not
+ * supported. */
 #define GBF_BC_PERIODIC 0
 #define GBF_BC_ZEROGRADIENT 1
 #define GBF_BC_SYMMETRY 2
 #define GBF_BC_WALL 3
 #define GBF_BC_DIRICHLET 4
 #define GBF_BC_NEUMANN 5
+#define GBF_BC_MIXED 6
 
 /* dissipative-flux stencils (stencils/reconstruction/central/central_{2,4}.py,
  * stencils/derivative/deriv_{center,face}_{2,4}.py) */
@@ -101,6 +107,13 @@ extern "C" {
    carries only the dissipative fluxes (space_solver.py:512-529); needs
    GBF_FLAG_VISCOUS or GBF_FLAG_HEAT */
 #define GBF_FLAG_NO_CONVECTIVE 8u
+/* conservatives.positivity.is_interpolation_limiter: reconstructed face
+   states with density < 1e-12 or pressure < 1e-10 fall back to the cell
+   beside the face (limiter_interpolation.py:82-210, precision.py:54) for
+   density and pressure, or for every primitive with GBF_FLAG_LIMIT_VELOCITY
+   (positivity.limit_velocity) */
+#define GBF_FLAG_INTERPOLATION_LIMITER 16u
+#define GBF_FLAG_LIMIT_VELOCITY 32u
 
 /* Case descriptor: the numerical_setup / case_setup keys the path reads. */
 typedef struct gbf_case {
@@ -130,6 +143,16 @@ typedef struct gbf_case {
                             derivative_stencil_center, derivative_stencil_face}: GBF_CENTRAL4 or
                             GBF_CENTRAL2 (read_conservatives.py:374-445) */
   int32_t reserved;
+  /* Boundary values along a face, device memory, NULL where the face uses
+     bc_value: per face nt = the product of the interior extents of its two
+     other axes (axis order, the later one fastest); bc_field_values[f] holds
+     5 x nt doubles, variable-major, laid out as bc_value (WALL velocity in
+     1..3), the callables' values at the boundary cells' centres;
+     bc_field_types[f] (only with bc[f] = GBF_BC_MIXED, required there) holds
+     nt GBF_BC_* types other than PERIODIC and MIXED.  Read by every launch;
+     they must stay valid and unchanged while work of this case runs. */
+  const double* bc_field_values[6];
+  const int8_t* bc_field_types[6];
 } gbf_case;
 
 /* Launch shape of the fused sweep kernels; all-zero picks the built-in default
@@ -264,7 +287,7 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  *   from U^n = `cons` with the device time step *dt (stage states recomputed).
  *   workspace: gbf_vjp_workspace_bytes(c).  lam_out must not alias lam.
  */
-size_t gbf_vjp_workspace_bytes(const gbf_case* c);
+size_t gbf_vjp_workspace_bytes(const gbf_case* c);  /* 0: invalid case, or no adjoint for it */
 int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out, void* workspace,
                 const gbf_tile* tile, void* stream);
 int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,

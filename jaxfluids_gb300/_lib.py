@@ -26,11 +26,13 @@ RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
-ABI_VERSION = 3  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+ABI_VERSION = 4  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
+BC_MIXED = 6  # a face of several types, per-cell types in bc_field_types
 FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
 FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION, FLAG_NO_CONVECTIVE = 1, 2, 4, 8
+FLAG_INTERPOLATION_LIMITER, FLAG_LIMIT_VELOCITY = 16, 32
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (
@@ -72,6 +74,8 @@ class GbfCase(ctypes.Structure):
         ("bc_value", (ctypes.c_double * 5) * 6),
         ("dissipative_stencil", ctypes.c_int32 * 3),
         ("reserved", ctypes.c_int32),
+        ("bc_field_values", ctypes.c_void_p * 6),
+        ("bc_field_types", ctypes.c_void_p * 6),
     ]
 
 

@@ -24,6 +24,8 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 from typing import Dict, Optional, Tuple
 
+import numpy as np
+
 from . import _lib
 
 FACES = ("east", "west", "north", "south", "top", "bottom")
@@ -32,6 +34,10 @@ FACE_AXIS = {"east": 0, "west": 0, "north": 1, "south": 1, "top": 2, "bottom": 2
 # precision.py:50 and :53
 EPS = 2.220446049250313e-16
 STENCIL_EPS = 1e-30
+
+
+# values per boundary type: WALL (u, v, w), DIRICHLET / NEUMANN (rho, u, v, w, p)
+_VALUE_COUNT = {"WALL": 3, "DIRICHLET": 5, "NEUMANN": 5}
 
 
 class SetupError(AssertionError):
@@ -47,20 +53,36 @@ def _get(d: dict, path: str, default=None):
     return cur
 
 
-def _constant_callables(spec: dict, names: Tuple[str, ...], face: str) -> Tuple[float, ...]:
-    """Values of the reference's boundary callables (case_setup
-    boundary_conditions.<face>.wall_velocity_callable / primitives_callable)
-    when they are constants: numbers, or strings holding a number.  Functions
-    of the boundary coordinates or time are rejected."""
+def _callable(v, what: str):
+    """A number, or a function: a Python callable or a "lambda ..." string
+    (the reference evaluates these with jax.numpy as ``jnp``,
+    input/setup_reader.py:123-230; here numpy stands in)."""
+    if callable(v):
+        return v
+    if isinstance(v, str):
+        try:
+            return float(v)
+        except ValueError:
+            pass
+        if not v.strip().startswith("lambda"):
+            raise SetupError(f"{what}: {v!r} is neither a number nor a lambda")
+        return eval(v, {"jnp": np, "np": np, "numpy": np})  # noqa: S307 (setup files are trusted input)
+    try:
+        return float(v)
+    except (TypeError, ValueError):
+        raise SetupError(f"{what}: {v!r} is neither a number nor a function")
+
+
+def _boundary_callables(spec: dict, names: Tuple[str, ...], face: str):
+    """The reference's boundary callables (case_setup boundary_conditions.<face>.
+    wall_velocity_callable / primitives_callable): numbers, or functions of
+    the active tangential boundary coordinates and time."""
     out = []
     for k in names:
         v = spec.get(k, 0.0) if k == "w" else spec.get(k)
         if v is None:
             raise SetupError(f"boundary at '{face}': '{k}' missing")
-        try:
-            out.append(float(v))
-        except (TypeError, ValueError):
-            raise NotImplementedError(f"boundary at '{face}': only constant '{k}' values are supported, got {v!r}")
+        out.append(_callable(v, f"boundary at '{face}', '{k}'"))
     return tuple(out)
 
 
@@ -88,8 +110,13 @@ class CaseConfig:
     viscous_heat_production: bool = True
     eps: float = EPS
     stencil_eps: float = STENCIL_EPS
-    # constant boundary values per face: WALL (u, v, w), DIRICHLET and
-    # NEUMANN (rho, u, v, w, p) (wall_velocity_callable / primitives_callable)
+    # boundary values per face: WALL (u, v, w), DIRICHLET and NEUMANN
+    # (rho, u, v, w, p) (wall_velocity_callable / primitives_callable), each a
+    # number or a function of the active tangential coordinates and time
+    # (constant in time); normalised to a tuple of constants or an array
+    # [k, boundary cells].  A face of several types has bc[face] =
+    # [(type, values, bounding_domain), ...] (bounding_domain: function of
+    # the coordinates, or a boolean per boundary cell).
     bc_values: Dict[str, Tuple[float, ...]] = field(default_factory=dict)
     # dissipative_fluxes.{reconstruction_stencil, derivative_stencil_center,
     # derivative_stencil_face}: CENTRAL4 or CENTRAL2
@@ -98,6 +125,11 @@ class CaseConfig:
     diss_deriv_face: str = "CENTRAL4"
     # active_physics.is_convective_flux: False leaves only the dissipative fluxes
     convective: bool = True
+    # conservatives.positivity.{is_interpolation_limiter, limit_velocity}
+    interpolation_limiter: bool = False
+    limit_velocity: bool = False
+    # device copies of the boundary value fields, per device
+    _fields: dict = field(default_factory=dict, init=False, repr=False, compare=False)
 
     def __post_init__(self):
         self.cells = tuple(int(n) for n in self.cells)
@@ -107,20 +139,18 @@ class CaseConfig:
         if not self.active:
             raise SetupError("at least one axis needs more than one cell")
         for f in FACES:
-            if FACE_AXIS[f] in self.active:
-                if f not in self.bc:
-                    raise SetupError(f"boundary condition for face '{f}' missing")
-                if self.bc[f] not in _lib.BC:
-                    raise NotImplementedError(f"boundary type {self.bc[f]} at {f}")
-        for f in FACES:
             if FACE_AXIS[f] not in self.active:
                 continue
-            need_values = {"WALL": 3, "DIRICHLET": 5, "NEUMANN": 5}.get(self.bc[f])
-            if need_values is not None:
-                vals = self.bc_values.get(f)
-                if vals is None or len(vals) != need_values:
-                    raise SetupError(f"{self.bc[f]} boundary at '{f}' needs {need_values} values")
-                self.bc_values[f] = tuple(float(v) for v in vals)
+            if f not in self.bc:
+                raise SetupError(f"boundary condition for face '{f}' missing")
+            spec = self.bc[f]
+            if isinstance(spec, (list, tuple)):
+                self.bc[f] = self._face_segments(f, spec)
+                continue
+            if spec not in _lib.BC:
+                raise NotImplementedError(f"boundary type {spec} at {f}")
+            if spec in _VALUE_COUNT:
+                self.bc_values[f] = self._face_values(f, spec, self.bc_values.get(f))
         for ax, (lo, hi) in ((0, ("west", "east")), (1, ("south", "north")), (2, ("bottom", "top"))):
             if ax in self.active and (self.bc[lo] == "PERIODIC") != (self.bc[hi] == "PERIODIC"):
                 raise SetupError(f"PERIODIC must be set on both faces of axis {ax}")
@@ -153,6 +183,153 @@ class CaseConfig:
             if self.nh < need_d:
                 raise SetupError(f"the dissipative stencils need halo_cells >= {need_d}")
 
+    # ---- boundary values along a face --------------------------------------
+
+    def face_axes(self, face: str) -> Tuple[int, int]:
+        """The two other axes of a face, in axis order (boundary cells are
+        numbered with the later one fastest)."""
+        a = FACE_AXIS[face]
+        return tuple(i for i in range(3) if i != a)
+
+    def face_cells(self, face: str) -> int:
+        b, c = self.face_axes(face)
+        return self.cells[b] * self.cells[c]
+
+    def cell_centers(self, axis: int) -> np.ndarray:
+        # mesh_creation/homogenous.py:13-14
+        lo, hi = self.ranges[axis]
+        dx = (hi - lo) / self.cells[axis]
+        return np.linspace(lo + dx / 2, hi - dx / 2, self.cells[axis])
+
+    def boundary_coordinates(self, face: str):
+        """Cell-centre coordinates of the boundary cells along the face's
+        active axes, flattened in boundary-cell order
+        (get_boundary_coordinates_at_location, boundary_condition.py:105-126)."""
+        b, c = self.face_axes(face)
+        xb, xc = np.meshgrid(self.cell_centers(b), self.cell_centers(c), indexing="ij")
+        return [x.reshape(-1) for x, ax in ((xb, b), (xc, c)) if ax in self.active]
+
+    def _eval_on_face(self, face: str, fn, with_time: bool, what: str) -> np.ndarray:
+        nt = self.face_cells(face)
+        coords = self.boundary_coordinates(face)
+        if not callable(fn):
+            return np.full(nt, float(fn))
+        r0 = fn(*coords, 0.0) if with_time else fn(*coords)
+        out = np.broadcast_to(np.asarray(r0, dtype=np.float64 if with_time else bool), (nt,)).copy()
+        if with_time:
+            r1 = np.broadcast_to(np.asarray(fn(*coords, 1.0), dtype=np.float64), (nt,))
+            if not np.array_equal(out, r1):
+                raise NotImplementedError(f"{what}: boundary values varying in time")
+        return out
+
+    def _face_values(self, face: str, btype: str, vals):
+        """Values of a face's type: a tuple of constants, or an array
+        [k, boundary cells] where a value varies along the face (k = 3 wall
+        velocities for WALL, 5 primitives or derivatives for DIRICHLET and
+        NEUMANN)."""
+        k = _VALUE_COUNT.get(btype)
+        if k is None:
+            return None
+        if vals is None:
+            raise SetupError(f"{btype} boundary at '{face}' needs {k} values")
+        if isinstance(vals, np.ndarray) or hasattr(vals, "numpy"):
+            arr = np.asarray(vals, dtype=np.float64)
+            if arr.shape == (k,):
+                return tuple(float(v) for v in arr)
+            if arr.shape != (k, self.face_cells(face)):
+                raise SetupError(f"{btype} boundary at '{face}': values of shape {arr.shape}, "
+                                 f"expected ({k}, {self.face_cells(face)})")
+            return arr.copy()
+        vals = tuple(vals)
+        if len(vals) != k:
+            raise SetupError(f"{btype} boundary at '{face}' needs {k} values")
+        fns = [_callable(v, f"boundary at '{face}'") for v in vals]
+        if not any(callable(fn) for fn in fns):
+            return tuple(float(fn) for fn in fns)
+        return np.stack([self._eval_on_face(face, fn, True, f"boundary at '{face}'") for fn in fns])
+
+    def _face_segments(self, face: str, spec):
+        """A face of several types (bounding_domain masks, material.py:252-266):
+        [(type, values, mask)] with the mask a boolean per boundary cell."""
+        segs = []
+        for seg in spec:
+            if isinstance(seg, dict):
+                seg = (seg.get("type"), seg.get("values"), seg.get("bounding_domain"))
+            btype, vals, mask = seg
+            if btype not in _lib.BC or btype == "PERIODIC":
+                raise NotImplementedError(f"boundary type {btype} on a face of several types at '{face}'")
+            if isinstance(mask, np.ndarray) or hasattr(mask, "numpy"):
+                m = np.asarray(mask).astype(bool).reshape(-1)
+                if m.shape != (self.face_cells(face),):
+                    raise SetupError(f"bounding domain at '{face}': {m.shape} cells")
+            else:
+                m = self._eval_on_face(face, _callable(mask, f"bounding domain at '{face}'"), False,
+                                       f"bounding domain at '{face}'")
+            segs.append((btype, self._face_values(face, btype, vals), m))
+        cover = np.zeros(self.face_cells(face), dtype=bool)
+        for _, _, m in segs:
+            cover |= m
+        if not cover.all():
+            raise SetupError(f"the bounding domains at '{face}' leave boundary cells uncovered")
+        return segs
+
+    def face_is_mixed(self, face: str) -> bool:
+        return isinstance(self.bc.get(face), list)
+
+    def face_fields(self, face: str):
+        """(values [5, nt] float64 or None, types [nt] int8 or None) of a face
+        for gbf_case.bc_field_values / bc_field_types: per boundary cell the
+        raw values laid out like bc_value, and for a face of several types the
+        type of the last segment covering the cell (the reference's masked
+        writes in face order, material.py:268-276)."""
+        nt = self.face_cells(face)
+
+        def rows(btype, vals):
+            out = np.zeros((5, nt))
+            if vals is None:
+                return out
+            arr = np.broadcast_to(np.asarray(vals, dtype=np.float64).reshape(len(vals), -1), (len(vals), nt))
+            if btype == "WALL":
+                out[1:4] = arr
+            else:
+                out[:] = arr
+            return out
+
+        if self.face_is_mixed(face):
+            types = np.zeros(nt, dtype=np.int8)
+            values = np.zeros((5, nt))
+            any_values = False
+            for btype, vals, m in self.bc[face]:
+                types[m] = _lib.BC[btype]
+                values[:, m] = rows(btype, vals)[:, m]
+                any_values |= vals is not None
+            return (values if any_values else None), types
+        vals = self.bc_values.get(face)
+        if isinstance(vals, np.ndarray):
+            return rows(self.bc[face], vals), None
+        return None, None
+
+    @property
+    def has_bc_fields(self) -> bool:
+        return any(FACE_AXIS[f] in self.active and (self.face_is_mixed(f) or
+                                                    isinstance(self.bc_values.get(f), np.ndarray))
+                   for f in FACES)
+
+    def _device_fields(self, device):
+        """The face fields as tensors on `device`, kept alive by this object."""
+        import torch
+        key = str(device)
+        if key not in self._fields:
+            d = {}
+            for f in FACES:
+                if FACE_AXIS[f] not in self.active:
+                    continue
+                vals, types = self.face_fields(f)
+                d[f] = (None if vals is None else torch.from_numpy(np.ascontiguousarray(vals)).to(device),
+                        None if types is None else torch.from_numpy(types).to(device))
+            self._fields[key] = d
+        return self._fields[key]
+
     # domain/domain_information.py:80-206 and mesh_creation/homogenous.py:13
     @property
     def active(self):
@@ -180,7 +357,10 @@ class CaseConfig:
         return (slice(None),) + tuple(slice(self.nh, -self.nh) if n > 1 else slice(None)
                                       for n in self.cells)
 
-    def to_c(self) -> _lib.GbfCase:
+    def to_c(self, device=None) -> _lib.GbfCase:
+        """The gbf_case of this setup.  Boundary value fields go to `device`
+        (default: the current CUDA device, or host memory without one, which
+        only the host-side checks read)."""
         c = _lib.GbfCase()
         for i in range(3):
             c.n[i] = self.cells[i]
@@ -191,13 +371,26 @@ class CaseConfig:
         c.frozen_state = _lib.FROZEN[self.frozen_state]
         c.riemann = _lib.RIEMANN[self.riemann]
         c.signal_speed = _lib.SIGNAL[self.signal_speed]
+        fields = None
+        if self.has_bc_fields:
+            import torch
+            if device is None:
+                device = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else "cpu"
+            fields = self._device_fields(device)
         for k, f in enumerate(_lib.FACE_ORDER):
-            c.bc[k] = _lib.BC[self.bc.get(f, "PERIODIC")]
+            if self.face_is_mixed(f):
+                c.bc[k] = _lib.BC_MIXED
+            else:
+                c.bc[k] = _lib.BC[self.bc.get(f, "PERIODIC")]
             vals = self.bc_values.get(f)
-            if vals is not None:
+            if isinstance(vals, tuple) and not self.face_is_mixed(f):
                 row = [0.0, *vals, 0.0] if len(vals) == 3 else list(vals)
                 for v in range(5):
                     c.bc_value[k][v] = float(row[v])
+            if fields is not None and f in fields:
+                fv, ft = fields[f]
+                c.bc_field_values[k] = fv.data_ptr() if fv is not None else None
+                c.bc_field_types[k] = ft.data_ptr() if ft is not None else None
         flags = 0
         if self.viscous:
             flags |= _lib.FLAG_VISCOUS
@@ -207,6 +400,10 @@ class CaseConfig:
             flags |= _lib.FLAG_VISCOUS_HEAT_PRODUCTION
         if not self.convective:
             flags |= _lib.FLAG_NO_CONVECTIVE
+        if self.interpolation_limiter:
+            flags |= _lib.FLAG_INTERPOLATION_LIMITER
+            if self.limit_velocity:
+                flags |= _lib.FLAG_LIMIT_VELOCITY
         c.flags = flags
         c.gamma = self.gamma
         c.R = self.R
@@ -228,22 +425,36 @@ class CaseConfig:
         cells = tuple(int(_get(case_setup, f"domain.{a}.cells", 1)) for a in "xyz")
         ranges = tuple(tuple(_get(case_setup, f"domain.{a}.range", [0.0, 1.0])) for a in "xyz")
         bc, bc_values = {}, {}
+
+        def values_of(spec, t, f):
+            if t == "WALL":
+                return _boundary_callables(spec.get("wall_velocity_callable", {}), ("u", "v", "w"), f)
+            if t in ("DIRICHLET", "NEUMANN"):
+                if spec.get("primitives_callable") is None:
+                    raise NotImplementedError(f"{t} boundary at '{f}' without primitives_callable")
+                return _boundary_callables(spec["primitives_callable"], ("rho", "u", "v", "w", "p"), f)
+            return None
+
         for f in FACES:
             t = _get(case_setup, f"boundary_conditions.{f}")
+            if isinstance(t, list) and len(t) == 1 and "bounding_domain" not in t[0]:
+                t = t[0]  # a one-type list reads as that type
             if isinstance(t, list):
-                if len(t) != 1:
-                    raise NotImplementedError("multiple boundary types on one face")
-                t = t[0]
+                # several types on the face (read_boundary_conditions.py:66-96)
+                segs = []
+                for spec in t:
+                    st = spec.get("type")
+                    segs.append((st, values_of(spec, st, f), spec.get("bounding_domain")))
+                bc[f] = segs
+                continue
             spec = t if isinstance(t, dict) else {}
             if isinstance(t, dict):
                 t = t.get("type")
             if t is not None and t != "INACTIVE":
                 bc[f] = t
-                if t == "WALL":
-                    bc_values[f] = _constant_callables(spec.get("wall_velocity_callable", {}), ("u", "v", "w"), f)
-                elif t in ("DIRICHLET", "NEUMANN"):
-                    bc_values[f] = _constant_callables(spec.get("primitives_callable", {}),
-                                                       ("rho", "u", "v", "w", "p"), f)
+                vals = values_of(spec, t, f)
+                if vals is not None:
+                    bc_values[f] = vals
         eos = _get(case_setup, "material_properties.equation_of_state", {}) or {}
         if eos.get("model", "IdealGas") != "IdealGas":
             raise NotImplementedError(f"equation of state {eos.get('model')}")
@@ -284,6 +495,9 @@ class CaseConfig:
                 kappa = float(tc.get("value", 0.0))
             else:
                 raise NotImplementedError("thermal conductivity model")
+        pos = cons.get("positivity", {}) or {}
+        if pos.get("flux_limiter", False):
+            raise NotImplementedError(f"positivity.flux_limiter = {pos['flux_limiter']}")
         diss = cons.get("dissipative_fluxes", {}) or {}
         if diss.get("is_laplacian", False):
             raise NotImplementedError("dissipative_fluxes.is_laplacian")
@@ -307,6 +521,8 @@ class CaseConfig:
             diss_deriv_center=diss.get("derivative_stencil_center", "CENTRAL4"),
             diss_deriv_face=diss.get("derivative_stencil_face", "CENTRAL4"),
             convective=bool(phys.get("is_convective_flux", True)),
+            interpolation_limiter=bool(pos.get("is_interpolation_limiter", False)),
+            limit_velocity=bool(pos.get("limit_velocity", False)),
             eps=float(prec.get("epsilon", EPS)) if isinstance(prec.get("epsilon"), float) else EPS,
             stencil_eps=float(prec.get("spatial_stencil_epsilon", STENCIL_EPS))
             if isinstance(prec.get("spatial_stencil_epsilon"), float) else STENCIL_EPS,

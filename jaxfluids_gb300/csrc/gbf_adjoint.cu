@@ -87,7 +87,7 @@ __device__ __forceinline__ int tangential(int t) {
 __device__ __forceinline__ void face_halo_transpose(const SweepParams& p, int a, int g[3], const double d[5],
                                                     double* dP) {
   const int f = 2 * a + (g[a] >= 0 ? 1 : 0);
-  const int t = p.bc[f];
+  const int t = face_type_at(p.bc, p.bf, f, face_pos(p.n, a, g));
   if (t == GBF_BC_DIRICHLET) return;
   const int ga = g[a];
   g[a] = bc_src(ga, p.n[a], t);
@@ -407,6 +407,9 @@ inline int grid_for(long long n) {
 
 int vjp_check(const gbf_case* c) {
   if (c->flags & GBF_FLAG_NO_CONVECTIVE) return GBF_OK;  // no convective scheme to reverse
+  // the interpolation limiter is reversed on the PRIMITIVE paths
+  if ((c->flags & GBF_FLAG_INTERPOLATION_LIMITER) && c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+    return GBF_ERR_UNSUPPORTED;
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
@@ -507,7 +510,7 @@ using namespace gbf;
 
 extern "C" size_t gbf_vjp_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
-  if (make_case_info(c, &ci) != GBF_OK) return 0;
+  if (make_case_info(c, &ci) != GBF_OK || vjp_check(c) != GBF_OK) return 0;  // no adjoint for this case
   // step VJP: U1, U2, lam2, lam1, j, dP (6 interior states); dissipative
   // cases add the primitives and the viscous face cotangents
   return ((size_t)6 * 5 * (size_t)ci.cells + (size_t)vjp_extra_doubles(c, ci)) * sizeof(double);

@@ -54,7 +54,10 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_HLL) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
-  if (c->flags & ~(GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_VISCOUS_HEAT_PRODUCTION | GBF_FLAG_NO_CONVECTIVE))
+  if (c->flags & ~(GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_VISCOUS_HEAT_PRODUCTION | GBF_FLAG_NO_CONVECTIVE |
+                   GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_LIMIT_VELOCITY))
+    return GBF_ERR_INVALID_ARGUMENT;
+  if ((c->flags & GBF_FLAG_LIMIT_VELOCITY) && !(c->flags & GBF_FLAG_INTERPOLATION_LIMITER))
     return GBF_ERR_INVALID_ARGUMENT;
   if ((c->flags & GBF_FLAG_NO_CONVECTIVE) && !(c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)))
     return GBF_ERR_INVALID_ARGUMENT;  // nothing to compute
@@ -80,8 +83,14 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
     if (c->n[a] > 1) {
       if (c->n[a] < c->nh) return GBF_ERR_SIZE;  // halo retrieve slices need nh interior cells
       for (int s = 0; s < 2; ++s) {
-        const int b = c->bc[2 * a + s];
-        if (b < GBF_BC_PERIODIC || b > GBF_BC_NEUMANN) return GBF_ERR_UNSUPPORTED;
+        const int f = 2 * a + s;
+        const int b = c->bc[f];
+        if (b < GBF_BC_PERIODIC || b > GBF_BC_MIXED) return GBF_ERR_UNSUPPORTED;
+        // per-cell types exactly on MIXED faces; no value fields on PERIODIC
+        // faces; values 8-byte aligned
+        if ((b == GBF_BC_MIXED) != (c->bc_field_types[f] != nullptr)) return GBF_ERR_INVALID_ARGUMENT;
+        if (b == GBF_BC_PERIODIC && c->bc_field_values[f]) return GBF_ERR_INVALID_ARGUMENT;
+        if ((uintptr_t)c->bc_field_values[f] & 7u) return GBF_ERR_ALIGNMENT;
       }
       if ((c->bc[2 * a] == GBF_BC_PERIODIC) != (c->bc[2 * a + 1] == GBF_BC_PERIODIC))
         return GBF_ERR_INVALID_ARGUMENT;

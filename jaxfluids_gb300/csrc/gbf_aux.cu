@@ -28,6 +28,8 @@ struct HaloParams {
   long long total;
   double gm1;
   double bcv[6][5];  // per-face boundary constants (fill_bc_constants)
+  BcFields bf;       // boundary values varying along a face
+  double dx[3];
 };
 
 // halos/outer/material.py:94-287 (face halos) with the retrieve slices of
@@ -58,7 +60,8 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
     src[ob] = dst[ob];
     const int n = hp.n[ax];
     const int nh = hp.nh;
-    const int bct = hp.bc[face];
+    const long long k = (long long)ia * eb + ib;  // boundary cell along the face
+    const int bct = face_type_at(hp.bc, hp.bf, face, k);
     // logical halo coordinate of this layer and the interior cell it reads
     const int g = hi ? n + layer : layer - nh;
     dst[ax] = g + nh;
@@ -67,7 +70,8 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
     const long long d = ((long long)dst[0] * hp.hs[1] + dst[1]) * hp.hs[2] + dst[2];
     double P[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) P[v] = bc_apply(bct, hp.bcv[face], ax, v, prims[v * cs + so]);
+    for (int v = 0; v < 5; ++v)
+      P[v] = bc_apply_at(bct, hp.bcv[face], hp.bf, face, k, (long long)ea * eb, hp.dx[ax], ax, v, prims[v * cs + so]);
 #pragma unroll
     for (int v = 0; v < 5; ++v) prims[v * cs + d] = P[v];
     if (cons) {
@@ -86,7 +90,8 @@ __global__ void halo_fill_kernel(const HaloParams hp, double* prims, double* con
 // PERIODIC or SYMMETRY takes the other face's halo cell at its periodic image
 // or mirror (that axis' velocity negated); otherwise (ANY_ANY) the mean of the
 // two face-halo cells nh cells inward ('_10' then '_01' slices,
-// halo_slices.py:77-149).  Halo conservatives from the halo primitives.
+// halo_slices.py:77-149); a face of several types counts as neither.  Halo
+// conservatives from the halo primitives.
 __global__ void halo_edge_kernel(const HaloParams hp, double* prims, double* cons) {
   const long long cs = (long long)hp.hs[0] * hp.hs[1] * hp.hs[2];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
@@ -333,6 +338,8 @@ int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, doubl
     hp.bc[f] = c->bc[f];
     fill_bc_constants(c, f, hp.bcv[f]);
   }
+  fill_bc_fields(c, &hp.bf);
+  for (int a = 0; a < 3; ++a) hp.dx[a] = c->dx[a];
   hp.active_mask = ci.active_mask;
   hp.gm1 = ci.fp.gm1;
   long long start = 0;

@@ -27,6 +27,8 @@ int record_status(int status);
 
 // per-face boundary constants for the kernels (gbf_sweep.cu)
 void fill_bc_constants(const gbf_case* c, int f, double out[5]);
+// Boundary value fields of the case (null where a face is uniform).
+void fill_bc_fields(const gbf_case* c, BcFields* bf);
 
 // fills p.{n,t,tiles,...} from the case and tile (tile null or all zero:
 // the default shape, for_vjp picking the adjoint kernel's); returns status

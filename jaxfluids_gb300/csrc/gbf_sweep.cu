@@ -32,6 +32,13 @@ void fill_bc_constants(const gbf_case* c, int f, double out[5]) {
   }
 }
 
+void fill_bc_fields(const gbf_case* c, BcFields* bf) {
+  for (int f = 0; f < 6; ++f) {
+    bf->val[f] = c->bc_field_values[f];
+    bf->type[f] = reinterpret_cast<const signed char*>(c->bc_field_types[f]);
+  }
+}
+
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
                       int* threads, size_t* smem, bool for_vjp) {
   SweepParams q{};
@@ -100,6 +107,8 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
     q.bc[f] = c->bc[f];
     fill_bc_constants(c, f, q.bcv[f]);
   }
+  fill_bc_fields(c, &q.bf);
+  for (int a = 0; a < 3; ++a) q.dx[a] = c->dx[a];
   q.fp = ci.fp;
   q.active_mask = ci.active_mask;
   q.viscous = (c->flags & GBF_FLAG_VISCOUS) ? 1 : 0;
@@ -112,6 +121,7 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   q.diss_recon = c->dissipative_stencil[0];
   q.diss_center = c->dissipative_stencil[1];
   q.diss_face = c->dissipative_stencil[2];
+  q.limiter = (c->flags & GBF_FLAG_INTERPOLATION_LIMITER) ? ((c->flags & GBF_FLAG_LIMIT_VELOCITY) ? 2 : 1) : 0;
   *p = q;
   *threads = thr;
   *smem = bytes;

@@ -30,6 +30,16 @@ namespace gbf {
 //   and heat-conduction path, whose face stencils reach across the tile).
 enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_STAGE_P = 2 };
 
+// Boundary values that vary along a face (gbf_case::bc_field_values /
+// bc_field_types): per face the raw boundary values of every boundary cell
+// (5 x nt, variable-major; WALL velocity in 1..3, DIRICHLET primitives,
+// NEUMANN normal derivatives) and, for faces of several types, the type of
+// every boundary cell; null where the face is uniform.
+struct BcFields {
+  const double* val[6];
+  const signed char* type[6];
+};
+
 struct SweepParams {
   int n[3];          // interior cells per axis (1 = inactive)
   int t[3];          // tile extents
@@ -40,6 +50,8 @@ struct SweepParams {
   // per-face boundary constants: WALL [1..3] = 2 u_wall, DIRICHLET [0..4] =
   // primitives, NEUMANN [0..4] = (gradient * sign) * dx
   double bcv[6][5];
+  BcFields bf;       // boundary values varying along a face
+  double dx[3];      // cell size per axis (NEUMANN fields)
   double one_dx[3];  // 1 / dx per axis
   FaceParams fp;
   const double* prims_halo;  // MODE_RHS input
@@ -62,6 +74,8 @@ struct SweepParams {
   // dissipative stencils: 0 CENTRAL4, 1 CENTRAL2 (reconstruction, centre
   // derivative, face derivative)
   int diss_recon, diss_center, diss_face;
+  // interpolation limiter: 0 off, 1 density and pressure, 2 every primitive
+  int limiter;
 };
 
 // Boundary rule of one face (halos/outer/material.py:140-210 with the
@@ -110,6 +124,43 @@ __device__ __forceinline__ double bc_apply_grad(int type, int ax, int v) {
   }
 }
 
+// Tangential position of cell g on a face of axis a (the other two axes in
+// axis order, interior coordinates) and the number of such positions.
+__device__ __forceinline__ long long face_pos(const int n[3], int a, const int g[3]) {
+  const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+  return (long long)g[b] * n[c] + g[c];
+}
+__device__ __forceinline__ long long face_npos(const int n[3], int a) {
+  const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+  return (long long)n[b] * n[c];
+}
+
+// Boundary type of face f at tangential position k: per boundary cell on a
+// face of several types (bounding_domain masks, outer/material.py:252-266),
+// else the face's type.
+__device__ __forceinline__ int face_type_at(const int bc[6], const BcFields& bf, int f, long long k) {
+  return bf.type[f] ? (int)bf.type[f][k] : bc[f];
+}
+
+// bc_apply with the values of boundary cell k where face f carries a value
+// field, transformed as the reference transforms the callables' values:
+// 2 u_wall - u (material.py:511-513), P + (g sign) dx (material.py:860-862).
+__device__ __forceinline__ double bc_apply_at(int type, const double* bcv, const BcFields& bf, int f, long long k,
+                                              long long nk, double dx, int ax, int v, double x) {
+  const double* fv = bf.val[f];
+  if (!fv) return bc_apply(type, bcv, ax, v, x);
+  switch (type) {
+    case GBF_BC_WALL:
+      return (v >= 1 && v <= 3) ? 2.0 * __ldg(fv + v * nk + k) - x : x;
+    case GBF_BC_DIRICHLET:
+      return __ldg(fv + v * nk + k);
+    case GBF_BC_NEUMANN:
+      return x + __dmul_rn(__ldg(fv + v * nk + k) * ((f & 1) ? -1.0 : 1.0), dx);
+    default:
+      return bc_apply(type, bcv, ax, v, x);
+  }
+}
+
 __device__ __forceinline__ int idx3(int i0, int i1, int i2, int e1, int e2) {
   return (i0 * e1 + i1) * e2 + i2;
 }
@@ -123,31 +174,23 @@ __device__ __forceinline__ double interior_prim(const SweepParams& p, int v, con
 // Primitive v of a cell outside along axis a only: the face rule of that face.
 __device__ __forceinline__ double face_halo_prim(const SweepParams& p, int v, int a, int g[3]) {
   const int f = 2 * a + (g[a] >= 0 ? 1 : 0);
-  const int t = p.bc[f];
+  const long long k = face_pos(p.n, a, g);
+  const int t = face_type_at(p.bc, p.bf, f, k);
   const int ga = g[a];
   g[a] = bc_src(ga, p.n[a], t);
   const double x = (t == GBF_BC_DIRICHLET) ? 0.0 : interior_prim(p, v, g);
   g[a] = ga;
-  return bc_apply(t, p.bcv[f], a, v, x);
+  return bc_apply_at(t, p.bcv[f], p.bf, f, k, face_npos(p.n, a), p.dx[a], a, v, x);
 }
 
-// Primitive v of the logical cell (g0, g1, g2), which may lie up to nh cells
-// outside the interior along one or two axes: read from the halo buffer
-// (MODE_RHS), or from the interior primitive buffer through the face rules
-// and, for edge cells, the edge rule of compute_edge_halos
-// (outer/material.py:339-379, type combinations boundary_condition.py:128-177,
-// :606-660): along the edge's faces in axis order the first PERIODIC or
-// SYMMETRY face maps the cell onto the other face's halo (periodic image, or
-// mirror with that axis' velocity negated); otherwise the mean of the two face
-// halos nh cells inward.
 // Primitive v of a logical cell outside the interior along one or two axes,
 // from the interior primitive buffer: the face rule, and for edge cells the
 // edge rule of compute_edge_halos (outer/material.py:339-379, type
 // combinations boundary_condition.py:128-177, :606-660): along the edge's
 // faces in axis order the first PERIODIC or SYMMETRY face maps the cell onto
 // the other face's halo (periodic image, or mirror with that axis' velocity
-// negated); otherwise the mean of the two face halos nh cells inward.  Kept
-// out of line: only tiles on the domain boundary reach it, and inlining it
+// negated); otherwise (also where a face has several types) the mean of the
+// two face halos nh cells inward.  Kept out of line: only tiles on the domain boundary reach it, and inlining it
 // costs the interior path registers.
 static __device__ __noinline__ double halo_prim(const SweepParams& p, int v, int g0, int g1, int g2) {
   int g[3] = {g0, g1, g2};
@@ -324,6 +367,34 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   }
 }
 
+// Interpolation limiter of one reconstructed face state
+// (limiter_interpolation.py:82-125, :170-188, SINGLE-PHASE): where the density
+// is below 1e-12, then where the pressure (+ the ideal gas' zero background
+// pressure) is below 1e-10 (precision.py:54), the first-order state w (the cell
+// beside the face, weno1_js.py; w[v * stride]) replaces density and pressure
+// (mode 1) or every primitive (mode 2, limit_velocity).  The reference's
+// x (1 - mask) + w mask with mask 0 or 1 is this selection.  Returns the
+// replaced primitives as bits (bit v), for the adjoint.
+__device__ __forceinline__ unsigned positivity_limit(double P[5], const double* w, int stride, int mode) {
+  unsigned replaced = 0;
+#pragma unroll
+  for (int check = 0; check < 2; ++check) {
+    const bool m = (check == 0) ? (P[0] < 1e-12) : (P[4] < 1e-10);
+    if (m) {
+      if (mode == 2) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) P[v] = w[v * stride];
+        replaced = 31u;
+      } else {
+        P[0] = w[0];
+        P[4] = w[4 * stride];
+        replaced |= 17u;
+      }
+    }
+  }
+  return replaced;
+}
+
 // Primitives of the pencil box (tile extended by R cells along AX) into
 // shared memory, variable-major: from the halo buffer (MODE_RHS), from the
 // interior primitive buffer (MODE_STAGE_P) or derived from the interior
@@ -356,7 +427,8 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
       const int ga = g[AX];
       const bool halo = ga < 0 || ga >= p.n[AX];
       const int f = 2 * AX + (ga >= 0 ? 1 : 0);
-      const int t = halo ? p.bc[f] : -1;
+      const long long k = halo ? face_pos(p.n, AX, g) : 0;
+      const int t = halo ? face_type_at(p.bc, p.bf, f, k) : -1;
       if (halo) g[AX] = bc_src(ga, p.n[AX], t);
       const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
       const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
@@ -371,7 +443,8 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
       }
       if (halo) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) P[v] = bc_apply(t, p.bcv[f], AX, v, P[v]);
+        for (int v = 0; v < 5; ++v)
+          P[v] = bc_apply_at(t, p.bcv[f], p.bf, f, k, face_npos(p.n, AX), p.dx[AX], AX, v, P[v]);
       }
     }
 #pragma unroll
@@ -426,6 +499,11 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
         reconstruct_pair<(RECON == RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
                                                                                   PL[v], PR[v]);
       }
+    }
+    if (RIEMANN != RIEMANN_NONE && p.limiter) {
+      const double* c = sm_prim + base + (R - 1) * pstride;  // the cell left of the face
+      positivity_limit(PL, c, pvol, p.limiter);
+      positivity_limit(PR, c + pstride, pvol, p.limiter);
     }
     double F[5];
     riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);

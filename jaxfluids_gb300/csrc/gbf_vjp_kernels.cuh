@@ -204,6 +204,20 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
           sm_jr[(v * 5 + k) * nthr + tid] = jr[k];
         }
       }
+      if (p.limiter) {
+        // limited primitives are the cells beside the face (slot R - 1 on
+        // the left, R on the right): unit stencil gradients
+        const double* c = sm_prim + base + (R - 1) * pstride;
+        const unsigned mL = positivity_limit(PL, c, pvol, p.limiter);
+        const unsigned mR = positivity_limit(PR, c + pstride, pvol, p.limiter);
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            if (mL & (1u << v)) sm_slot[(v * K + k) * fvol + f] = (k == R - 1) ? 1.0 : 0.0;
+            if (mR & (1u << v)) sm_jr[(v * 5 + k) * nthr + tid] = (k == R - 1) ? 1.0 : 0.0;
+          }
+      }
       double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
       riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
 #pragma unroll
@@ -231,6 +245,12 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
         reconstruct_pair<RECON>(wv, p.fp.stencil_eps, PL[v], PR[v]);
       }
+      unsigned mL = 0, mR = 0;
+      if (p.limiter) {
+        const double* c = sm_prim + base + (R - 1) * pstride;
+        mL = positivity_limit(PL, c, pvol, p.limiter);
+        mR = positivity_limit(PR, c + pstride, pvol, p.limiter);
+      }
       double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
       riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
 #pragma unroll
@@ -238,7 +258,12 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         double wv[K], dw[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) wv[k] = sm_prim[v * pvol + base + k * pstride];
-        reconstruct_pair_vjp<RECON>(wv, p.fp.stencil_eps, dPL[v], dPR[v], dw);
+        // limited primitives take the cell beside the face (slot R - 1 left, R right)
+        const double gL = (mL & (1u << v)) ? 0.0 : dPL[v];
+        const double gR = (mR & (1u << v)) ? 0.0 : dPR[v];
+        reconstruct_pair_vjp<RECON>(wv, p.fp.stencil_eps, gL, gR, dw);
+        if (mL & (1u << v)) dw[R - 1] += dPL[v];
+        if (mR & (1u << v)) dw[R] += dPR[v];
 #pragma unroll
         for (int k = 0; k < K; ++k) sm_slot[(v * K + k) * fvol + f] = dw[k];
       }
@@ -272,7 +297,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     g[AX] -= R;
     if (g[AX] < 0 || g[AX] >= p.n[AX]) {
       // halo cell: transpose of the face rule (DIRICHLET halos are constants)
-      const int t = p.bc[2 * AX + (g[AX] >= 0 ? 1 : 0)];
+      const int t = face_type_at(p.bc, p.bf, 2 * AX + (g[AX] >= 0 ? 1 : 0), face_pos(p.n, AX, g));
       g[AX] = bc_src(g[AX], p.n[AX], t);
 #pragma unroll
       for (int v = 0; v < 5; ++v) d[v] *= bc_apply_grad(t, AX, v);

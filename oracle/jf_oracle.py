@@ -80,6 +80,9 @@ class OracleCase:
     convective: bool = True
     # thermal_conductivity CUSTOM value (None: PRANDTL model from prandtl)
     thermal_conductivity: Optional[float] = None
+    # conservatives.positivity.{is_interpolation_limiter, limit_velocity}
+    interpolation_limiter: bool = False
+    limit_velocity: bool = False
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -523,9 +526,38 @@ def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
         PR = torch.stack(prims_from_chars(cR, rho_a, c, cc, axis), 0)
     else:
         raise NotImplementedError(case.recon_var)
+    if case.interpolation_limiter:
+        # high_order_godunov.py:163-175
+        PL = limit_interpolation(P, PL, case, axis, 0)
+        PR = limit_interpolation(P, PR, case, axis, 1)
     UL = cons_from_prims(PL, g)
     UR = cons_from_prims(PR, g)
     return riemann(PL, PR, UL, UR, case, axis)
+
+
+# precision.py:54 (double precision): interpolation limiter epsilons
+LIMITER_EPS_DENSITY = 1e-12
+LIMITER_EPS_PRESSURE = 1e-10
+
+
+def limit_interpolation(P: Tensor, Pj: Tensor, case: OracleCase, axis: int, j: int) -> Tensor:
+    """PositivityLimiterInterpolation.limit_interpolation_xi, SINGLE-PHASE
+    (limiter_interpolation.py:82-125, :170-188, apply_limiter :66-74): where
+    the reconstructed density is below eps, then where the pressure (+ the
+    ideal gas' zero background pressure) is below eps, the first-order value
+    (WENO1, weno1_js.py: the cell left of the face for j = 0, right for
+    j = 1) replaces density and pressure, or every primitive with
+    limit_velocity, as x (1 - mask) + x1 mask."""
+    w1 = P[_stencil_slice(case, axis, -1 if j == 0 else 0)]
+    ids = list(range(5)) if case.limit_velocity else [0, 4]
+    for check in range(2):
+        if check == 0:
+            mask = (Pj[0] < LIMITER_EPS_DENSITY).to(P.dtype)
+        else:
+            mask = (Pj[4] + 0.0 < LIMITER_EPS_PRESSURE).to(P.dtype)
+        rows = [Pj[v] * (1 - mask) + w1[v] * mask if v in ids else Pj[v] for v in range(5)]
+        Pj = torch.stack(rows, 0)
+    return Pj
 
 
 # ---------------------------------------------------------------------------
@@ -713,15 +745,29 @@ def _face_retrieve_slice(case: OracleCase, face: str, btype: str) -> Tuple[slice
 NEUMANN_SIGN = {"east": -1, "west": 1, "north": -1, "south": 1, "top": -1, "bottom": 1}
 
 
-def _face_halo(P: Tensor, case: OracleCase, face: str, btype: str) -> Tensor:
+def _face_value_tensor(case: OracleCase, face: str, vals, dtype) -> Tensor:
+    """Boundary values as a tensor [k, 1 along the face's axis, tangential
+    extents]: constants, or an array [k, boundary cells] of the callables'
+    values at the boundary cells (the later tangential axis fastest)."""
+    axis = FACE_AXIS[face]
+    if isinstance(vals, (tuple, list)):
+        return torch.tensor([float(x) for x in vals], dtype=dtype).reshape(len(vals), 1, 1, 1)
+    arr = torch.as_tensor(vals, dtype=dtype)
+    dims = [case.cells[i] if i != axis else 1 for i in range(3)]
+    return arr.reshape([arr.shape[0]] + dims)
+
+
+def _face_halo(P: Tensor, case: OracleCase, face: str, btype: str, vals=None) -> Tensor:
     """Halo primitives of one face (outer/material.py:140-210): miscellaneous
     (:868-894) for PERIODIC / SYMMETRY / ZEROGRADIENT, wall (:473-531),
-    dirichlet (:732-798, constant callables), neumann (:825-866)."""
+    dirichlet (:732-798), neumann (:825-866); values constant or per
+    boundary cell."""
     axis = FACE_AXIS[face]
     fill_shape = P[_face_fill_slice(case, face)].shape
+    if vals is None:
+        vals = case.bc_values.get(face)
     if btype == "DIRICHLET":
-        vals = torch.tensor([float(x) for x in case.bc_values[face]], dtype=P.dtype).reshape(5, 1, 1, 1)
-        return vals.expand(fill_shape).clone()
+        return _face_value_tensor(case, face, vals, P.dtype).expand(fill_shape).clone()
     h = P[_face_retrieve_slice(case, face, btype)].clone()
     if btype in ("SYMMETRY", "WALL"):
         h = torch.flip(h, dims=(axis + 1,))
@@ -731,13 +777,12 @@ def _face_halo(P: Tensor, case: OracleCase, face: str, btype: str) -> Tensor:
         h = h * sign
     elif btype == "WALL":
         # u_halo = 2 u_wall - u_mirror for every velocity component (:511-513)
-        uw = [2 * float(x) for x in case.bc_values[face]]
-        h = torch.cat([h[0:1], uw[0] - h[1:2], uw[1] - h[2:3], uw[2] - h[3:4], h[4:5]])
+        uw = 2 * _face_value_tensor(case, face, vals, P.dtype)
+        h = torch.cat([h[0:1], uw[0:1] - h[1:2], uw[1:2] - h[2:3], uw[2:3] - h[3:4], h[4:5]])
     elif btype == "NEUMANN":
         # neumann_value *= sign; neumann_value *= dx; halo = P + neumann_value (:860-862)
-        dx = case.cell_size(axis)
-        off = torch.tensor([(float(g) * NEUMANN_SIGN[face]) * dx for g in case.bc_values[face]],
-                           dtype=P.dtype).reshape(5, 1, 1, 1)
+        off = _face_value_tensor(case, face, vals, P.dtype) * NEUMANN_SIGN[face]
+        off = off * case.cell_size(axis)
         h = h + off
     if h.shape != fill_shape:  # one retrieved layer fills all nh layers
         h = h.expand(fill_shape).clone()
@@ -758,8 +803,20 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
         axis = FACE_AXIS[face]
         if axis not in case.active:
             continue
-        h = _face_halo(P, case, face, case.bc[face])
         fill = _face_fill_slice(case, face)
+        if isinstance(case.bc[face], (list, tuple)):
+            # several types on the face: each type's halos written through its
+            # bounding-domain mask, x.at[fill].mul(1 - mask).add(h * mask)
+            # (material.py:252-276)
+            for btype, vals, mask in case.bc[face]:
+                h = _face_halo(P, case, face, btype, vals)
+                m = torch.as_tensor(mask, dtype=P.dtype)
+                m = m.reshape([1] + [case.cells[i] if i != axis else 1 for i in range(3)])
+                P[fill] = P[fill] * (1 - m) + h * m
+                if U is not None:
+                    U[fill] = U[fill] * (1 - m) + cons_from_prims(h, case.gamma) * m
+            continue
+        h = _face_halo(P, case, face, case.bc[face])
         P[fill] = h
         if U is not None:
             U[fill] = cons_from_prims(h, case.gamma)

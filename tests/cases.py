@@ -18,8 +18,13 @@ def both(cells, bc, **kw):
     fields = {k: v for k, v in kw.items() if k in (
         "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
         "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "kappa", "viscous_heat_production",
-        "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face", "convective")}
+        "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face", "convective",
+        "interpolation_limiter", "limit_velocity")}
     cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
+    # boundary callables, strings and bounding domains reach the oracle as the
+    # values CaseConfig evaluated at the boundary cells
+    oc.bc = {f: cc.bc.get(f, oc.bc[f]) for f in O.FACES}
+    oc.bc_values = dict(cc.bc_values)
     return oc, cc
 
 

@@ -1,5 +1,6 @@
 """Boundary conditions read from the reference's case_setup dictionaries
 (input/case_setup/read_boundary_conditions.py layout) into the C descriptor."""
+import numpy as np
 import pytest
 
 from jaxfluids_gb300 import _lib
@@ -45,18 +46,84 @@ def test_dirichlet_inflow_and_neumann_outflow():
     assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
 
 
-def test_varying_callables_and_mixed_faces_are_rejected():
-    f = {"type": "DIRICHLET", "primitives_callable": {"rho": "lambda x, t: 1.0 + x", "u": 0.0, "v": 0.0,
+def test_callables_of_the_boundary_coordinates():
+    """Lambda strings are evaluated at the boundary cells' centres
+    (get_boundary_coordinates_at_location, boundary_condition.py:105-126;
+    homogenous.py:13-14) with numpy in place of jax.numpy."""
+    f = {"type": "DIRICHLET", "primitives_callable": {"rho": "lambda y, t: 1.0 + y", "u": 0.0, "v": 0.0,
+                                                      "w": 0.0, "p": "lambda y,t: 1.0 + jnp.sin(jnp.pi * y)"}}
+    case, num = _setup({"west": f, "east": {"type": "ZEROGRADIENT"}, "north": {"type": "ZEROGRADIENT"},
+                        "south": {"type": "ZEROGRADIENT"}})
+    cfg = CaseConfig.from_setups(case, num)
+    ny = cfg.cells[1]
+    lo, hi = cfg.ranges[1]
+    dy = (hi - lo) / ny
+    y = np.linspace(lo + dy / 2, hi - dy / 2, ny)
+    vals = cfg.bc_values["west"]
+    assert vals.shape == (5, ny)
+    np.testing.assert_array_equal(vals[0], 1.0 + y)
+    np.testing.assert_array_equal(vals[4], 1.0 + np.sin(np.pi * y))
+    np.testing.assert_array_equal(vals[1:4], 0.0)
+    fv, ft = cfg.face_fields("west")
+    assert ft is None and fv.shape == (5, ny)
+    c = cfg.to_c()
+    w = _lib.FACE_ORDER.index("west")
+    assert c.bc[w] == _lib.BC["DIRICHLET"] and c.bc_field_values[w] and not c.bc_field_types[w]
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
+
+
+def test_time_varying_callables_are_rejected():
+    f = {"type": "DIRICHLET", "primitives_callable": {"rho": "lambda y, t: 1.0 + t * y", "u": 0.0, "v": 0.0,
                                                       "w": 0.0, "p": 1.0}}
     case, num = _setup({"west": f, "east": {"type": "ZEROGRADIENT"}, "north": {"type": "ZEROGRADIENT"},
                         "south": {"type": "ZEROGRADIENT"}})
-    with pytest.raises(NotImplementedError, match="constant"):
+    with pytest.raises(NotImplementedError, match="time"):
         CaseConfig.from_setups(case, num)
+
+
+def test_face_of_several_types():
+    """bounding_domain masks (material.py:252-276): per boundary cell the type
+    of the last segment covering it, its values in the value field."""
     mixed = [{"type": "DIRICHLET", "primitives_callable": {"rho": 1.0, "u": 0.0, "v": 0.0, "w": 0.0, "p": 1.0},
               "bounding_domain": "lambda x: x < 0.5"}, {"type": "SYMMETRY", "bounding_domain": "lambda x: x >= 0.5"}]
     case, num = _setup({"west": {"type": "ZEROGRADIENT"}, "east": {"type": "ZEROGRADIENT"},
                         "north": {"type": "ZEROGRADIENT"}, "south": mixed})
-    with pytest.raises(NotImplementedError, match="multiple"):
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.face_is_mixed("south")
+    nx = cfg.cells[0]
+    x = (np.arange(nx) + 0.5) / nx
+    fv, ft = cfg.face_fields("south")
+    np.testing.assert_array_equal(ft, np.where(x < 0.5, _lib.BC["DIRICHLET"], _lib.BC["SYMMETRY"]))
+    np.testing.assert_array_equal(fv[0], np.where(x < 0.5, 1.0, 0.0))
+    c = cfg.to_c()
+    s = _lib.FACE_ORDER.index("south")
+    assert c.bc[s] == _lib.BC_MIXED and c.bc_field_types[s] and c.bc_field_values[s]
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
+    # the library wants per-cell types exactly on MIXED faces
+    c.bc_field_types[s] = None
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_ERR_INVALID_ARGUMENT
+    # uncovered boundary cells and PERIODIC segments are rejected
+    gap = [dict(mixed[0]), {"type": "SYMMETRY", "bounding_domain": "lambda x: x >= 0.75"}]
+    case, num = _setup({"west": {"type": "ZEROGRADIENT"}, "east": {"type": "ZEROGRADIENT"},
+                        "north": {"type": "ZEROGRADIENT"}, "south": gap})
+    with pytest.raises(SetupError, match="uncovered"):
+        CaseConfig.from_setups(case, num)
+    per = [dict(mixed[0]), {"type": "PERIODIC", "bounding_domain": "lambda x: x >= 0.5"}]
+    case, num = _setup({"west": {"type": "ZEROGRADIENT"}, "east": {"type": "ZEROGRADIENT"},
+                        "north": {"type": "ZEROGRADIENT"}, "south": per})
+    with pytest.raises(NotImplementedError):
+        CaseConfig.from_setups(case, num)
+
+
+def test_positivity_setup():
+    case, num = _setup({"west": {"type": "ZEROGRADIENT"}, "east": {"type": "ZEROGRADIENT"},
+                        "north": {"type": "ZEROGRADIENT"}, "south": {"type": "ZEROGRADIENT"}})
+    num["conservatives"]["positivity"] = {"is_interpolation_limiter": True}
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.interpolation_limiter and not cfg.limit_velocity
+    assert cfg.to_c().flags & _lib.FLAG_INTERPOLATION_LIMITER
+    num["conservatives"]["positivity"] = {"flux_limiter": "NASA"}
+    with pytest.raises(NotImplementedError, match="flux_limiter"):
         CaseConfig.from_setups(case, num)
 
 

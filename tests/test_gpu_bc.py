@@ -35,6 +35,8 @@ def _faces(x=None, y=None, z=None):
 
 
 IN_STATE = (1.2, 0.3, 0.1, 0.0, 1.1)
+# double Mach reflection: post-shock state of the Mach 10 shock
+POST_SHOCK = (8.0, 7.144709581221618, -4.125, 0.0, 116.5)
 GRAD = (0.1, -0.2, 0.05, 0.0, 0.3)
 VISC = {"nh": 4, "viscous": True, "heat": True, "mu": 0.02, "prandtl": 0.71}
 
@@ -98,10 +100,48 @@ BC_CASES = [
      {"west": (1.0, 0.0, 0.1, 0.0, 1.2), "east": (0.0, 0.1, 0.0), "bottom": GRAD},
      dict(VISC, nh=3, convective=False, diss_recon="CENTRAL2", diss_deriv_center="CENTRAL2",
           diss_deriv_face="CENTRAL4"), "tgv"),
+    # boundary values varying along a face (callables of the boundary
+    # coordinates) and faces of several types (bounding_domain masks)
+    ("2d-heat-equation-sine-dirichlet", (24, 20, 1), _faces(x=("DIRICHLET", "DIRICHLET"), y=("DIRICHLET", "DIRICHLET")),
+     {"west": (1.0, 0.0, 0.0, 0.0, 1.0), "east": (1.0, 0.0, 0.0, 0.0, 1.0), "south": (1.0, 0.0, 0.0, 0.0, 1.0),
+      "north": (1.0, 0.0, 0.0, 0.0, "lambda x,t: 1.0 + jnp.sin(jnp.pi * x)")},
+     dict(nh=4, recon="WENO5-JS", heat=True, kappa=0.1, convective=False), "quad"),
+    ("2d-double-mach-mixed-south", (48, 12, 1),
+     _faces(x=("DIRICHLET", "ZEROGRADIENT"),
+            y=([("DIRICHLET", POST_SHOCK, "lambda x: x < 1.0 / 6.0"),
+                ("SYMMETRY", None, "lambda x: x >= 1.0 / 6.0")], "ZEROGRADIENT")),
+     {"west": POST_SHOCK}, dict(ranges=((0.0, 4.0), (0.0, 1.0), (0.0, 1.0)), interpolation_limiter=True), "dmr"),
+    ("3d-viscous-mixed-wall-neumann-fields", (12, 10, 8),
+     _faces(y=([("WALL", ("lambda x,z,t: 0.1 * jnp.sin(2 * jnp.pi * x)", 0.0, "lambda x,z,t: 0.05 * z"),
+                 "lambda x,z: x < 0.5"),
+                ("NEUMANN", GRAD, "lambda x,z: x >= 0.5")], ("WALL")),
+            z=("DIRICHLET", "ZEROGRADIENT")),
+     {"north": ("lambda x,z,t: 0.2 + 0.05 * z", 0.0, 0.0),
+      "bottom": ("lambda x,y,t: 1.0 + 0.1 * x * y", 0.05, 0.0, 0.0, 1.1)}, dict(VISC), "tgv"),
+    ("2d-char-roe-neumann-wall-fields", (30, 28, 1),
+     _faces(x=("SYMMETRY", "NEUMANN"), y=("ZEROGRADIENT", "WALL")),
+     {"east": (0.0, "lambda y,t: 0.2 * y", 0.0, 0.0, "lambda y,t: -0.1 + 0.3 * y * y"),
+      "north": ("lambda x,t: 0.3 * x * (1.0 - x)", 0.0, 0.0)},
+     {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "quad"),
 ]
 
 
+def _dmr_prims(cells, ranges=((0.0, 4.0), (0.0, 1.0))):
+    """Mach 10 shock at 60 degrees through x = 1/6 (the double Mach
+    reflection's initial condition)."""
+    x = [torch.linspace(lo + (hi - lo) / n / 2, hi - (hi - lo) / n / 2, n, dtype=torch.float64)
+         for (lo, hi), n in zip(ranges, cells[:2])]
+    X, Y = torch.meshgrid(x[0], x[1], indexing="ij")
+    post = Y > math.sqrt(3.0) * (X - 1.0 / 6.0)
+    P = torch.zeros(5, cells[0], cells[1], 1, dtype=torch.float64)
+    for v, (a, b) in enumerate(zip(POST_SHOCK, (1.4, 0.0, 0.0, 0.0, 1.0))):
+        P[v, :, :, 0] = torch.where(post, torch.full_like(X, a), torch.full_like(X, b))
+    return P
+
+
 def _prims(kind, cells):
+    if kind == "dmr":
+        return _dmr_prims(cells)
     if kind == "sod":
         return sod_prims(cells[0])
     if kind == "quad":
@@ -198,7 +238,8 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
 @pytest.mark.parametrize("name", ["2d-cavity-viscous-heat", "3d-char-roe-viscous-sym-neumann-dirichlet-wall",
                                   "2d-cavity-viscous-heat-central2", "3d-viscous-mixed-stencils-wall-neumann",
                                   "2d-cavity-weno5js-viscous", "2d-couette-viscous-only",
-                                  "3d-heat-viscous-only-c2"])
+                                  "3d-heat-viscous-only-c2", "2d-heat-equation-sine-dirichlet",
+                                  "3d-viscous-mixed-wall-neumann-fields"])
 def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
