@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GBF_ABI_VERSION 4
+#define GBF_ABI_VERSION 5
 
 /* status codes */
 #define GBF_OK 0
@@ -114,6 +114,11 @@ extern "C" {
    (positivity.limit_velocity) */
 #define GBF_FLAG_INTERPOLATION_LIMITER 16u
 #define GBF_FLAG_LIMIT_VELOCITY 32u
+/* active_physics.is_volume_force: gravity (gbf_case.gravity, forcings.gravity)
+   adds rho g to the momentum and g . (rho u) to the energy right-hand side
+   after the flux divergence (space_solver.py:377-384,
+   source_term_solver.py:165-186) */
+#define GBF_FLAG_GRAVITY 64u
 
 /* Case descriptor: the numerical_setup / case_setup keys the path reads. */
 typedef struct gbf_case {
@@ -153,6 +158,7 @@ typedef struct gbf_case {
      they must stay valid and unchanged while work of this case runs. */
   const double* bc_field_values[6];
   const int8_t* bc_field_types[6];
+  double gravity[3];     /* forcings.gravity, with GBF_FLAG_GRAVITY */
 } gbf_case;
 
 /* Launch shape of the fused sweep kernels; all-zero picks the built-in default
@@ -190,6 +196,11 @@ int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile*
  * (halos/halo_manager.py:146-234, halos/outer/material.py:94-287).
  */
 int gbf_halo_fill(const gbf_case* c, double* prims, double* cons, void* stream);
+
+/* SpaceSolver.compute_rhs volume forces (space_solver.py:377-384): with
+ * GBF_FLAG_GRAVITY, rhs[1:5] (interior [5][N]) += the gravity forces of the
+ * halo-buffer conservatives `cons`; nothing without the flag. */
+int gbf_volume_force(const gbf_case* c, const double* cons, double* rhs, void* stream);
 
 /* Primitive <-> conservative conversion over `count` cells of SoA buffers with
  * a variable stride of `count` (equation_manager.py:44-171). */

@@ -26,17 +26,17 @@ RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
-ABI_VERSION = 4  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+ABI_VERSION = 5  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
 BC_MIXED = 6  # a face of several types, per-cell types in bc_field_types
 FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
 FLAG_VISCOUS, FLAG_HEAT, FLAG_VISCOUS_HEAT_PRODUCTION, FLAG_NO_CONVECTIVE = 1, 2, 4, 8
-FLAG_INTERPOLATION_LIMITER, FLAG_LIMIT_VELOCITY = 16, 32
+FLAG_INTERPOLATION_LIMITER, FLAG_LIMIT_VELOCITY, FLAG_GRAVITY = 16, 32, 64
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (
-    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill",
+    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill", "gbf_volume_force",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
@@ -76,6 +76,7 @@ class GbfCase(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("bc_field_values", ctypes.c_void_p * 6),
         ("bc_field_types", ctypes.c_void_p * 6),
+        ("gravity", ctypes.c_double * 3),
     ]
 
 
@@ -109,6 +110,7 @@ def load() -> ctypes.CDLL:
         "gbf_case_check": (I, [C]),
         "gbf_rhs": (I, [C, P, P, T, P]),
         "gbf_halo_fill": (I, [C, P, P, P]),
+        "gbf_volume_force": (I, [C, P, P, P]),
         "gbf_prims_from_cons": (I, [C, P, P, ctypes.c_int64, P]),
         "gbf_cons_from_prims": (I, [C, P, P, ctypes.c_int64, P]),
         "gbf_stage_integrate": (I, [C, P, P, P, P, I, P]),

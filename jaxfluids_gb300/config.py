@@ -128,6 +128,8 @@ class CaseConfig:
     # conservatives.positivity.{is_interpolation_limiter, limit_velocity}
     interpolation_limiter: bool = False
     limit_velocity: bool = False
+    # active_physics.is_volume_force with forcings.gravity: the gravity vector
+    gravity: Optional[Tuple[float, float, float]] = None
     # device copies of the boundary value fields, per device
     _fields: dict = field(default_factory=dict, init=False, repr=False, compare=False)
 
@@ -400,6 +402,10 @@ class CaseConfig:
             flags |= _lib.FLAG_VISCOUS_HEAT_PRODUCTION
         if not self.convective:
             flags |= _lib.FLAG_NO_CONVECTIVE
+        if self.gravity is not None:
+            flags |= _lib.FLAG_GRAVITY
+            for i in range(3):
+                c.gravity[i] = float(self.gravity[i])
         if self.interpolation_limiter:
             flags |= _lib.FLAG_INTERPOLATION_LIMITER
             if self.limit_velocity:
@@ -469,9 +475,22 @@ class CaseConfig:
         phys = _get(numerical_setup, "active_physics", {}) or {}
         viscous = bool(phys.get("is_viscous_flux", False))
         heat = bool(phys.get("is_heat_flux", False))
-        for key in ("is_volume_force", "is_geometric_source", "is_surface_tension"):
+        for key in ("is_geometric_source", "is_surface_tension"):
             if phys.get(key, False):
                 raise NotImplementedError(key)
+        gravity = None
+        if phys.get("is_volume_force", False):
+            # forcings.gravity (read_forcings / source_term_solver.py:165-186)
+            g = _get(case_setup, "forcings.gravity")
+            if g is None or len(g) != 3:
+                raise SetupError("is_volume_force needs forcings.gravity = [gx, gy, gz]")
+            gravity = tuple(float(x) for x in g)
+        forcings = _get(numerical_setup, "active_forcings", {}) or {}
+        for key, on in forcings.items():
+            if on:
+                raise NotImplementedError(f"active_forcings.{key}")
+        if (_get(numerical_setup, "precision", {}) or {}).get("is_consistent_summation", False):
+            raise NotImplementedError("precision.is_consistent_summation")
         transport = _get(case_setup, "material_properties.transport", {}) or {}
         mu = 0.0
         if viscous:
@@ -521,6 +540,7 @@ class CaseConfig:
             diss_deriv_center=diss.get("derivative_stencil_center", "CENTRAL4"),
             diss_deriv_face=diss.get("derivative_stencil_face", "CENTRAL4"),
             convective=bool(phys.get("is_convective_flux", True)),
+            gravity=gravity,
             interpolation_limiter=bool(pos.get("is_interpolation_limiter", False)),
             limit_velocity=bool(pos.get("limit_velocity", False)),
             eps=float(prec.get("epsilon", EPS)) if isinstance(prec.get("epsilon"), float) else EPS,

@@ -353,7 +353,10 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
 }
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
-__global__ void dp_to_du_kernel(const double* U, double* dP, double* out, long long n, double gm1) {
+// With gravity (g non-null) the transpose of add_gravity joins: d rho += g . w[1:4],
+// d m_j += g_j w[4], w the right-hand side's cotangent.
+__global__ void dp_to_du_kernel(const double* U, double* dP, double* out, long long n, double gm1,
+                                const double* w, double g0, double g1, double g2) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     double u[5], d[5], o[5] = {0, 0, 0, 0, 0};
@@ -364,6 +367,13 @@ __global__ void dp_to_du_kernel(const double* U, double* dP, double* out, long l
       dP[v * n + i] = 0.0;
     }
     prims_from_cons_vjp(u, d, gm1, o);
+    if (w) {
+      const double w1 = w[n + i], w2 = w[2 * n + i], w3 = w[3 * n + i], w4 = w[4 * n + i];
+      o[0] += (g0 * w1 + g1 * w2) + g2 * w3;
+      o[1] += g0 * w4;
+      o[2] += g1 * w4;
+      o[3] += g2 * w4;
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + i] = o[v];
   }
@@ -498,7 +508,9 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     if (nface[2]) visc_halo_scatter_kernel<2><<<blocks(nface[2]), 256, 0, s>>>(q);
     if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
   }
-  dp_to_du_kernel<<<grid_for(ci.cells), 256, 0, s>>>(U, dP, out, ci.cells, ci.fp.gm1);
+  const bool grav = (c->flags & GBF_FLAG_GRAVITY) != 0;
+  dp_to_du_kernel<<<grid_for(ci.cells), 256, 0, s>>>(U, dP, out, ci.cells, ci.fp.gm1, grav ? w : nullptr,
+                                                     c->gravity[0], c->gravity[1], c->gravity[2]);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 

@@ -55,7 +55,7 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
   if (c->flags & ~(GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_VISCOUS_HEAT_PRODUCTION | GBF_FLAG_NO_CONVECTIVE |
-                   GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_LIMIT_VELOCITY))
+                   GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_LIMIT_VELOCITY | GBF_FLAG_GRAVITY))
     return GBF_ERR_INVALID_ARGUMENT;
   if ((c->flags & GBF_FLAG_LIMIT_VELOCITY) && !(c->flags & GBF_FLAG_INTERPOLATION_LIMITER))
     return GBF_ERR_INVALID_ARGUMENT;
@@ -161,6 +161,20 @@ static int gbf_rhs_impl(const gbf_case* c, const double* prims, double* rhs, con
 
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
   return record_status(gbf_rhs_impl(c, prims, rhs, tile, stream));
+}
+
+static int gbf_volume_force_impl(const gbf_case* c, const double* cons, double* rhs, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!cons || !rhs) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(cons) || !aligned8(rhs)) return GBF_ERR_ALIGNMENT;
+  if (!(c->flags & GBF_FLAG_GRAVITY)) return GBF_OK;
+  return launch_volume_force(c, ci, cons, rhs, (cudaStream_t)stream);
+}
+
+int gbf_volume_force(const gbf_case* c, const double* cons, double* rhs, void* stream) {
+  return record_status(gbf_volume_force_impl(c, cons, rhs, stream));
 }
 
 static int gbf_halo_fill_impl(const gbf_case* c, double* prims, double* cons, void* stream) {

@@ -326,6 +326,42 @@ __global__ void dt_finalize_kernel(const DtParams dp, unsigned long long* red, d
 
 }  // namespace
 
+namespace {
+
+// Gravity forces of the drop-in right-hand side: one thread per interior
+// cell, conservatives read from the halo buffer.
+__global__ void volume_force_kernel(const double* cons, double* rhs, int n0, int n1, int n2, int hs1, int hs2,
+                                    int h0, int h1, int h2, long long hcs, double g0, double g1, double g2) {
+  const long long cs = (long long)n0 * n1 * n2;
+  const double g[3] = {g0, g1, g2};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int i2 = (int)(i % n2), i1 = (int)((i / n2) % n1), i0 = (int)(i / ((long long)n2 * n1));
+    const long long hoff = ((long long)(i0 + h0) * hs1 + (i1 + h1)) * hs2 + (i2 + h2);
+    double U[5], r[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      U[v] = cons[v * hcs + hoff];
+      r[v] = rhs[v * cs + i];
+    }
+    add_gravity(r, U, g);
+#pragma unroll
+    for (int v = 1; v < 5; ++v) rhs[v * cs + i] = r[v];
+  }
+}
+
+}  // namespace
+
+int launch_volume_force(const gbf_case* c, const CaseInfo& ci, const double* cons, double* rhs, cudaStream_t s) {
+  int h[3];
+  for (int a = 0; a < 3; ++a) h[a] = (ci.n[a] > 1) ? ci.nh : 0;
+  const long long hcs = (long long)ci.hs[0] * ci.hs[1] * ci.hs[2];
+  volume_force_kernel<<<grid_for(ci.cells), kThreads, 0, s>>>(cons, rhs, ci.n[0], ci.n[1], ci.n[2], ci.hs[1],
+                                                               ci.hs[2], h[0], h[1], h[2], hcs, c->gravity[0],
+                                                               c->gravity[1], c->gravity[2]);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
 int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
                      cudaStream_t s) {
   HaloParams hp;

@@ -40,6 +40,8 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
                  cudaStream_t s, int mode);
 
 // auxiliary kernels (gbf_aux.cu)
+// rhs[1:5] += gravity forces of the interior of the halo-buffer conservatives
+int launch_volume_force(const gbf_case* c, const CaseInfo& ci, const double* cons, double* rhs, cudaStream_t s);
 int launch_halo_fill(const gbf_case* c, const CaseInfo& ci, double* prims, double* cons,
                      cudaStream_t s);
 // edge halos from the filled face halos (viscous / heat; no vertex halos)

@@ -122,6 +122,8 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   q.diss_center = c->dissipative_stencil[1];
   q.diss_face = c->dissipative_stencil[2];
   q.limiter = (c->flags & GBF_FLAG_INTERPOLATION_LIMITER) ? ((c->flags & GBF_FLAG_LIMIT_VELOCITY) ? 2 : 1) : 0;
+  q.gravity = (c->flags & GBF_FLAG_GRAVITY) ? 1 : 0;
+  for (int a = 0; a < 3; ++a) q.g[a] = q.gravity ? c->gravity[a] : 0.0;
   *p = q;
   *threads = thr;
   *smem = bytes;

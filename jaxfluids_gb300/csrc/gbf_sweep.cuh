@@ -76,7 +76,19 @@ struct SweepParams {
   int diss_recon, diss_center, diss_face;
   // interpolation limiter: 0 off, 1 density and pressure, 2 every primitive
   int limiter;
+  int gravity;               // volume force on
+  double g[3];               // gravity vector
 };
+
+// Gravity forces added to a cell's right-hand side (source_term_solver.py:165-186,
+// space_solver.py:377-384): rhs[1 + i] += g_i rho, rhs[4] += (g_0 m_0 + g_1 m_1) + g_2 m_2
+// from the cell's conservatives U.
+__device__ __forceinline__ void add_gravity(double rhs[5], const double U[5], const double g[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) rhs[1 + i] = __dadd_rn(rhs[1 + i], __dmul_rn(g[i], U[0]));
+  const double e = __dadd_rn(__dadd_rn(__dmul_rn(g[0], U[1]), __dmul_rn(g[1], U[2])), __dmul_rn(g[2], U[3]));
+  rhs[4] = __dadd_rn(rhs[4], e);
+}
 
 // Boundary rule of one face (halos/outer/material.py:140-210 with the
 // retrieve slices of halos/outer/boundary_condition.py:539-604): bc_src is
@@ -617,12 +629,14 @@ __device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* 
 #pragma unroll
         for (int v = 0; v < 5; ++v) p.out[v * cs + off] = acc[k][v];
       } else {  // MODE_STAGE, MODE_STAGE_P
-        double Un[5];
+        double U[5], Un[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
+        if (p.gravity) add_gravity(acc[k], U, p.g);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-          const double U = p.cons[v * cs + off];
-          const double U0 = (p.stage == 0) ? U : p.cons0[v * cs + off];
-          Un[v] = rk3_combine(p.stage, U, U0, acc[k][v], dt);
+          const double U0 = (p.stage == 0) ? U[v] : p.cons0[v * cs + off];
+          Un[v] = rk3_combine(p.stage, U[v], U0, acc[k][v], dt);
         }
 #pragma unroll
         for (int v = 0; v < 5; ++v) p.out[v * cs + off] = Un[v];

@@ -129,6 +129,10 @@ class SpaceSolver(_Base):
         tile = ctypes.byref(self.tile) if self.tile is not None else None
         _lib.check(self.lib.gbf_rhs(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
                                     _ptr(rhs), tile, _stream()), "compute_rhs")
+        if self.config.gravity is not None:
+            # volume forces from the conservatives (space_solver.py:377-384)
+            _lib.check(self.lib.gbf_volume_force(ctypes.byref(self.case), _ptr(conservatives, shape, "conservatives"),
+                                                 _ptr(rhs), _stream()), "volume forces")
         return (IntegrationBuffers(EulerIntegrationBuffers(rhs)), PositivityCounter(),
                 DiscretizationCounter())
 

@@ -83,6 +83,8 @@ class OracleCase:
     # conservatives.positivity.{is_interpolation_limiter, limit_velocity}
     interpolation_limiter: bool = False
     limit_velocity: bool = False
+    # forcings.gravity with active_physics.is_volume_force
+    gravity: Optional[Tuple[float, float, float]] = None
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -712,7 +714,19 @@ def compute_rhs(U: Tensor, P: Tensor, case: OracleCase) -> Tensor:
         sl_hi[axis + 1] = slice(1, None)
         rhs_xi = case.one_cell_size(axis) * (flux[tuple(sl_lo)] - flux[tuple(sl_hi)])
         rhs = rhs_xi if rhs is None else rhs + rhs_xi
+    if case.gravity is not None:
+        rhs = rhs + gravity_forces(U[case.interior()], case)
     return rhs
+
+
+def gravity_forces(Ui: Tensor, case: OracleCase) -> Tensor:
+    """compute_gravity_forces (source_term_solver.py:165-186) added to
+    rhs[1:5] (space_solver.py:377-384): momentum g_i rho, energy g . (rho u)
+    summed in axis order; zero for the density."""
+    g = [float(x) for x in case.gravity]
+    mom = [g[i] * Ui[0] for i in range(3)]
+    energy = (g[0] * Ui[1] + g[1] * Ui[2]) + g[2] * Ui[3]
+    return torch.stack([torch.zeros_like(Ui[0])] + mom + [energy], 0)
 
 
 def _face_fill_slice(case: OracleCase, face: str) -> Tuple[slice, ...]:

@@ -19,7 +19,7 @@ def both(cells, bc, **kw):
         "ranges", "nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riemann", "signal_speed",
         "cfl", "fixed_dt", "viscous", "heat", "mu", "bulk_viscosity", "prandtl", "kappa", "viscous_heat_production",
         "bc_values", "diss_recon", "diss_deriv_center", "diss_deriv_face", "convective",
-        "interpolation_limiter", "limit_velocity")}
+        "interpolation_limiter", "limit_velocity", "gravity")}
     cc = CaseConfig(cells=cells, bc={f: bcd[f] for f in O.FACES}, **fields)
     # boundary callables, strings and bounding domains reach the oracle as the
     # values CaseConfig evaluated at the boundary cells

@@ -31,7 +31,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_version_and_status_strings(lib):
     from jaxfluids_gb300 import _lib
-    assert lib.gbf_abi_version() == _lib.ABI_VERSION == 4
+    assert lib.gbf_abi_version() == _lib.ABI_VERSION == 5
     assert lib.gbf_status_string(0) == b"ok"
     assert lib.gbf_status_string(-2) == b"unsupported setup"
 

@@ -182,3 +182,24 @@ def test_dissipative_stencils_from_setup():
     c = cfg.to_c()
     assert list(c.dissipative_stencil) == [_lib.CENTRAL["CENTRAL2"]] * 3
     assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
+
+
+def test_gravity_from_setup():
+    """active_physics.is_volume_force with forcings.gravity (the Rayleigh-Taylor
+    example's keys); other forcings and consistent summation are rejected."""
+    case, num = _setup({"west": {"type": "SYMMETRY"}, "east": {"type": "SYMMETRY"},
+                        "north": {"type": "ZEROGRADIENT"}, "south": {"type": "ZEROGRADIENT"}})
+    case["forcings"] = {"gravity": [0.0, 1.0, 0.0]}
+    num["active_physics"] = {"is_convective_flux": True, "is_volume_force": True}
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.gravity == (0.0, 1.0, 0.0)
+    c = cfg.to_c()
+    assert c.flags & _lib.FLAG_GRAVITY and list(c.gravity) == [0.0, 1.0, 0.0]
+    assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
+    num["active_forcings"] = {"is_mass_flow_forcing": True}
+    with pytest.raises(NotImplementedError, match="mass_flow"):
+        CaseConfig.from_setups(case, num)
+    del num["active_forcings"]
+    num["precision"] = {"is_consistent_summation": True}
+    with pytest.raises(NotImplementedError, match="consistent"):
+        CaseConfig.from_setups(case, num)

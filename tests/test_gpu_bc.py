@@ -123,6 +123,13 @@ BC_CASES = [
      {"east": (0.0, "lambda y,t: 0.2 * y", 0.0, 0.0, "lambda y,t: -0.1 + 0.3 * y * y"),
       "north": ("lambda x,t: 0.3 * x * (1.0 - x)", 0.0, 0.0)},
      {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE"}, "quad"),
+    # gravity (active_physics.is_volume_force): Rayleigh-Taylor-like walls of
+    # fixed states, and a 3-D viscous case with every component
+    ("2d-rayleigh-taylor-gravity", (16, 40, 1), _faces(x=("SYMMETRY", "SYMMETRY"), y=("DIRICHLET", "DIRICHLET")),
+     {"south": (2.0, 0.0, 0.0, 0.0, 1.0), "north": (1.0, 0.0, 0.0, 0.0, 2.5)},
+     dict(gravity=(0.0, 1.0, 0.0), ranges=((0.0, 0.25), (0.0, 1.0), (0.0, 1.0))), "quad"),
+    ("3d-viscous-gravity-wall", (10, 12, 8), _faces(y=("WALL", "WALL")),
+     {"south": (0.0, 0.0, 0.0), "north": (0.1, 0.0, 0.0)}, dict(VISC, gravity=(0.3, -0.5, 0.2)), "tgv"),
 ]
 
 
@@ -239,7 +246,8 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
                                   "2d-cavity-viscous-heat-central2", "3d-viscous-mixed-stencils-wall-neumann",
                                   "2d-cavity-weno5js-viscous", "2d-couette-viscous-only",
                                   "3d-heat-viscous-only-c2", "2d-heat-equation-sine-dirichlet",
-                                  "3d-viscous-mixed-wall-neumann-fields"])
+                                  "3d-viscous-mixed-wall-neumann-fields", "2d-rayleigh-taylor-gravity",
+                                  "3d-viscous-gravity-wall"])
 def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
