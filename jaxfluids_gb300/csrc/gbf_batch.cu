@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) batch_sweep_kernel(const BatchParams bp) 
     const int tile = bp.worklist[2 * item + 1];
     SweepParams p;
     case_params(bp, c, p);
-    sweep_tile<RECON, RIEMANN, MODE_STAGE, kMaxCellsPerThread, false>(p, tile, smem);
+    sweep_tile<RECON, RIEMANN, MODE_STAGE, kMaxCellsPerThread, 0>(p, tile, smem);
   }
 }
 

@@ -138,8 +138,14 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
     // dissipative fluxes read the primitive buffer (MODE_STAGE_P) or the halo buffer
     if (mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
     if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_sweep_dissipative(mode, p, threads, smem, s);
-    if (chr) return launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s);
-    if (c->recon == GBF_RECON_WENO5Z) return launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
+    const bool c4 = c->dissipative_stencil[0] == GBF_CENTRAL4 && c->dissipative_stencil[1] == GBF_CENTRAL4 &&
+                    c->dissipative_stencil[2] == GBF_CENTRAL4;
+    if (chr)
+      return c4 ? launch_sweep_char_visc_c4(c->riemann, mode, p, threads, smem, s)
+                : launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s);
+    if (c->recon == GBF_RECON_WENO5Z)
+      return c4 ? launch_sweep_weno_visc_c4(c->riemann, mode, p, threads, smem, s)
+                : launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
     if (c->recon == GBF_RECON_WENO5JS) return launch_sweep_weno5js_visc(c->riemann, mode, p, threads, smem, s);
     return launch_sweep_short_visc(c->recon, c->riemann, mode, p, threads, smem, s);
   }

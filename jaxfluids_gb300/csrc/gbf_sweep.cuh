@@ -284,14 +284,14 @@ __device__ __forceinline__ double c2_face_interp(double m1, double c0) { return 
 // SweepParams::diss_*).  at(k) is the value at normal offset k (cells k = -2..1
 // around face q - 1/2), cell(v, kax, ax2, k2) primitive v at normal offset kax
 // and offset k2 along axis ax2.
-template <class At>
+template <bool C4 = false, class At>
 __device__ __forceinline__ double face_deriv_along(const SweepParams& p, double odx, const At& at) {
-  return (p.diss_face == 0) ? c4_face_deriv(odx, at(-2), at(-1), at(0), at(1)) : c2_face_deriv(odx, at(-1), at(0));
+  return (C4 || p.diss_face == 0) ? c4_face_deriv(odx, at(-2), at(-1), at(0), at(1)) : c2_face_deriv(odx, at(-1), at(0));
 }
 
-template <int AX, class At>
+template <int AX, bool C4 = false, class At>
 __device__ __forceinline__ double face_interp_along(const SweepParams& p, const At& at) {
-  return (p.diss_recon == 0) ? c4_face_interp(at(-2), at(-1), at(0), at(1)) : c2_face_interp(at(-1), at(0));
+  return (C4 || p.diss_recon == 0) ? c4_face_interp(at(-2), at(-1), at(0), at(1)) : c2_face_interp(at(-1), at(0));
 }
 
 // gr[a][b] = d u_a / d x_b at the face (zero for inactive axes and for the
@@ -299,7 +299,7 @@ __device__ __forceinline__ double face_interp_along(const SweepParams& p, const 
 // stencil, tangential ones as face reconstructions of centre derivatives
 // (source_term_solver.py compute_velocity_gradient :414-448 and
 // compute_xi_derivatives_at_xj :538-580, stencils chosen at :57-118).
-template <int AX, class Cell>
+template <int AX, bool C4 = false, class Cell>
 __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, const Cell& cell, double gr[3][3]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -307,7 +307,7 @@ __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, con
     for (int b = 0; b < 3; ++b) gr[a][b] = 0.0;
   const double odx = p.one_dx[AX];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) gr[a][AX] = face_deriv_along(p, odx, [&](int k) { return cell(1 + a, k, AX, 0); });
+  for (int a = 0; a < 3; ++a) gr[a][AX] = face_deriv_along<C4>(p, odx, [&](int k) { return cell(1 + a, k, AX, 0); });
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     if (i == AX || !(p.active_mask & (1 << i))) continue;
@@ -316,8 +316,8 @@ __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, con
 #pragma unroll
     for (int which = 0; which < 2; ++which) {
       const int a = (which == 0) ? AX : i;
-      gr[a][i] = face_interp_along<AX>(p, [&](int kax) {
-        return (p.diss_center == 0) ? c4_center_deriv(odi, cell(1 + a, kax, i, -2), cell(1 + a, kax, i, -1),
+      gr[a][i] = face_interp_along<AX, C4>(p, [&](int kax) {
+        return (C4 || p.diss_center == 0) ? c4_center_deriv(odi, cell(1 + a, kax, i, -2), cell(1 + a, kax, i, -1),
                                                       cell(1 + a, kax, i, 1), cell(1 + a, kax, i, 2))
                                     : c2_center_deriv(odi, cell(1 + a, kax, i, -1), cell(1 + a, kax, i, 1));
       });
@@ -332,7 +332,8 @@ __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, con
 // compute_heat_flux_xi (:188-254).  Adds them to the convective flux F the
 // way compute_rhs_xi does: F[1:5] += -visc, then F[4] += heat
 // (space_solver.py:565-585).
-template <int AX, int MODE>
+// C4: the stencils are CENTRAL4 at compile time (else chosen by p.diss_*).
+template <int AX, int MODE, bool C4>
 __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const int q[3], double F[5]) {
   auto cell = [&](int v, int kax, int ax2, int k2) {
     int g[3] = {q[0], q[1], q[2]};
@@ -343,7 +344,7 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   const double odx = p.one_dx[AX];
   if (p.viscous) {
     double gr[3][3];
-    face_velocity_gradient<AX>(p, cell, gr);
+    face_velocity_gradient<AX, C4>(p, cell, gr);
     double tau[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -363,7 +364,7 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         if (!(p.active_mask & (1 << k))) continue;
-        const double vf = face_interp_along<AX>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
+        const double vf = face_interp_along<AX, C4>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
         vt = first ? tau[k] * vf : vt + tau[k] * vf;
         first = false;
       }
@@ -374,7 +375,7 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   }
   if (p.heat) {
     const double dT =
-        face_deriv_along(p, odx, [&](int k) { return cell(4, k, AX, 0) / (cell(0, k, AX, 0) * p.R); });
+        face_deriv_along<C4>(p, odx, [&](int k) { return cell(4, k, AX, 0) / (cell(0, k, AX, 0) * p.R); });
     F[4] = F[4] + (-p.kappa) * dT;
   }
 }
@@ -464,7 +465,9 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
   }
 }
 
-template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
+// VISC: 0 no dissipative fluxes, 1 dissipative fluxes with the stencils of
+// p.diss_*, 2 dissipative fluxes with CENTRAL4 stencils fixed at compile time
+template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
 __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
                                            double* sm_prim, double* sm_flux,
                                            double (&acc)[MAXC][5], bool first) {
@@ -521,7 +524,7 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
     if (VISC) {
       int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
-      add_dissipative_flux<AX, MODE>(p, q, F);
+      add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F);
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
@@ -567,7 +570,7 @@ __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, do
 }
 
 // One tile (index b of the case described by p) of the fused sweep.
-template <int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
+template <int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
 __device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* smem) {
   const int b2 = b % p.tiles[2];
   const int b1 = (b / p.tiles[2]) % p.tiles[1];
@@ -691,7 +694,7 @@ __device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* 
 // Two CTAs per SM: the register cap (128) costs the CHAR and viscous variants
 // a few spilled values but doubles their resident warps (viscous CHAR-ROE TGV
 // 128^3: 3.15e7 -> 3.31e7 cell-updates/s); the others fit 128 registers anyway.
-template <int RECON, int RIEMANN, int MODE, int MAXC, bool VISC>
+template <int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
 __global__ void __launch_bounds__(256, 2) sweep_kernel(const SweepParams p) {
   extern __shared__ double smem[];
   sweep_tile<RECON, RIEMANN, MODE, MAXC, VISC>(p, blockIdx.x, smem);

@@ -6,8 +6,8 @@ namespace gbf {
 
 int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   // the reconstruction parameter only sizes the (unused) pencil box
-  if (mode == MODE_RHS) return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_RHS, true>(p, threads, smem, s);
-  return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_STAGE_P, true>(p, threads, smem, s);
+  if (mode == MODE_RHS) return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_RHS, 1>(p, threads, smem, s);
+  return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_STAGE_P, 1>(p, threads, smem, s);
 }
 
 }  // namespace gbf

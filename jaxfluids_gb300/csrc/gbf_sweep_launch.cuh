@@ -8,7 +8,7 @@ namespace gbf {
 
 constexpr int kSweepMaxCellsPerThread = 4;
 
-template <int RECON, int RIEMANN, int MODE, bool VISC>
+template <int RECON, int RIEMANN, int MODE, int VISC>
 int launch_sweep_one(const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   auto kern = sweep_kernel<RECON, RIEMANN, MODE, kSweepMaxCellsPerThread, VISC>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -18,7 +18,7 @@ int launch_sweep_one(const SweepParams& p, int threads, size_t smem, cudaStream_
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
-template <int RECON, int MODE, bool VISC>
+template <int RECON, int MODE, int VISC>
 int launch_sweep_riemann(int riemann, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   if (riemann == GBF_RIEMANN_HLLC) return launch_sweep_one<RECON, GBF_RIEMANN_HLLC, MODE, VISC>(p, threads, smem, s);
   if (riemann == GBF_RIEMANN_HLL) return launch_sweep_one<RECON, GBF_RIEMANN_HLL, MODE, VISC>(p, threads, smem, s);
@@ -43,5 +43,11 @@ int launch_sweep_weno5js_visc(int riemann, int mode, const SweepParams& p, int t
 int launch_sweep_short_visc(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                             cudaStream_t s);
 int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+// WENO5-Z (PRIMITIVE and CHAR-PRIMITIVE) with CENTRAL4 dissipative stencils fixed
+// at compile time (VISC = 2), the default setups
+int launch_sweep_weno_visc_c4(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                              cudaStream_t s);
+int launch_sweep_char_visc_c4(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                              cudaStream_t s);
 
 }  // namespace gbf

@@ -4,8 +4,8 @@
 namespace gbf {
 
 int launch_sweep_visc_weno3js(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO3JS, MODE_RHS, true>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<GBF_RECON_WENO3JS, MODE_STAGE_P, true>(riemann, p, threads, smem, s);
+  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO3JS, MODE_RHS, 1>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<GBF_RECON_WENO3JS, MODE_STAGE_P, 1>(riemann, p, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -4,8 +4,8 @@
 namespace gbf {
 
 int launch_sweep_weno(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_RHS, false>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_STAGE, false>(riemann, p, threads, smem, s);
+  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_RHS, 0>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_STAGE, 0>(riemann, p, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -8,8 +8,8 @@ namespace {
 
 template <int RECON>
 int launch_modes(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<RECON, MODE_RHS, false>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<RECON, MODE_STAGE, false>(riemann, p, threads, smem, s);
+  if (mode == MODE_RHS) return launch_sweep_riemann<RECON, MODE_RHS, 0>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<RECON, MODE_STAGE, 0>(riemann, p, threads, smem, s);
 }
 
 }  // namespace

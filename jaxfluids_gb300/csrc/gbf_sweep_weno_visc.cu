@@ -1,12 +1,13 @@
-// Sweep kernels: WENO5-Z on primitive variables with CENTRAL4 viscous / heat fluxes.
+// Sweep kernels: WENO5-Z on primitive variables with viscous / heat fluxes on the
+// stencils chosen per case (CENTRAL2 in any of the three).
 #include "gbf_sweep_launch.cuh"
 
 namespace gbf {
 
 int launch_sweep_weno_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                            cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_RHS, true>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_STAGE_P, true>(riemann, p, threads, smem, s);
+  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_RHS, 1>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_STAGE_P, 1>(riemann, p, threads, smem, s);
 }
 
 }  // namespace gbf
