@@ -45,10 +45,13 @@ extern "C" {
 #define GBF_RECON_WENO5JS 3   /* weno/weno5_js.py */
 #define GBF_RECON_WENO3JS 4   /* weno/weno3_js.py */
 #define GBF_RECON_WENO3Z 5    /* weno/weno3_z.py */
+#define GBF_RECON_TENO5 6     /* teno/teno5.py */
 
 /* reconstruction_variable (solvers/__init__.py:5-12) */
 #define GBF_RECVAR_PRIMITIVE 0
 #define GBF_RECVAR_CHAR_PRIMITIVE 1
+#define GBF_RECVAR_CONSERVATIVE 2       /* high_order_godunov.py:282-296 (WENO5-Z) */
+#define GBF_RECVAR_CHAR_CONSERVATIVE 3  /* high_order_godunov.py:404-416 (WENO5-Z) */
 
 /* frozen_state (input/numerical_setup/read_conservatives.py:162-166) */
 #define GBF_FROZEN_ARITHMETIC 0
@@ -188,6 +191,13 @@ int gbf_case_check(const gbf_case* c);
  * the active axes in x, y, z order.  prims: halo buffer; rhs: interior buffer.
  */
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream);
+
+/* As gbf_rhs with the halo-buffer conservatives `cons` beside the primitives
+ * (SpaceSolver.compute_rhs receives both): required by the CONSERVATIVE and
+ * CHAR-CONSERVATIVE reconstructions, which reconstruct the conservatives
+ * (gbf_rhs returns GBF_ERR_INVALID_ARGUMENT for them); read by no other case. */
+int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
+                 void* stream);
 
 /*
  * Face halos (and, for viscous cases, edge halos) of the primitive buffer and,

@@ -21,8 +21,8 @@ GBF_ERR_ALIGNMENT = -5
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported setup", -3: "CUDA launch error",
           -4: "invalid or unsupported size", -5: "misaligned pointer"}
 
-RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2, "WENO5-JS": 3, "WENO3-JS": 4, "WENO3-Z": 5}
-RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1}
+RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2, "WENO5-JS": 3, "WENO3-JS": 4, "WENO3-Z": 5, "TENO5": 6}
+RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1, "CONSERVATIVE": 2, "CHAR-CONSERVATIVE": 3}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
@@ -36,7 +36,7 @@ FLAG_INTERPOLATION_LIMITER, FLAG_LIMIT_VELOCITY, FLAG_GRAVITY = 16, 32, 64
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (
-    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_halo_fill", "gbf_volume_force",
+    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_rhs_cons", "gbf_halo_fill", "gbf_volume_force",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
@@ -109,6 +109,7 @@ def load() -> ctypes.CDLL:
         "gbf_status_string": (ctypes.c_char_p, [I]),
         "gbf_case_check": (I, [C]),
         "gbf_rhs": (I, [C, P, P, T, P]),
+        "gbf_rhs_cons": (I, [C, P, P, P, T, P]),
         "gbf_halo_fill": (I, [C, P, P, P]),
         "gbf_volume_force": (I, [C, P, P, P]),
         "gbf_prims_from_cons": (I, [C, P, P, ctypes.c_int64, P]),

@@ -161,7 +161,9 @@ class CaseConfig:
                            ("signal_speed", _lib.SIGNAL)):
             if getattr(self, key) not in table:
                 raise NotImplementedError(f"{key} = {getattr(self, key)}")
-        need = 3 if self.recon in ("WENO5-Z", "WENO5-JS") else 2
+        if self.recon_var != "PRIMITIVE" and self.recon != "WENO5-Z":
+            raise NotImplementedError(f"{self.recon_var} is built with WENO5-Z")
+        need = 3 if self.recon in ("WENO5-Z", "WENO5-JS", "TENO5") else 2
         if self.nh < need:
             raise SetupError(f"halo_cells = {self.nh} < {need} required by {self.recon}")
         for i in self.active:

@@ -423,6 +423,9 @@ int vjp_check(const gbf_case* c) {
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
+  // the conservative reconstructions have no reverse
+  if (c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE)
+    return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
@@ -479,6 +482,8 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     st = launch_vjp_char(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
     st = launch_vjp_weno5(c->recon, c->riemann, vp, grid, threads, smem, s);
+  else if (c->recon == GBF_RECON_TENO5)
+    st = launch_vjp_teno5(c->riemann, vp, grid, threads, smem, s);
   else
     st = launch_vjp_short(c->recon, c->riemann, vp, grid, threads, smem, s);
   if (st != GBF_OK) return st;

@@ -122,6 +122,24 @@ __device__ __forceinline__ void weno5js_jac(double u0, double u1, double u2, dou
   J[4] += dt4 + dt5;
 }
 
+// teno5(u0..u4) and its gradient (teno/teno5.py): the cutoff weights are
+// piecewise constant (jnp.where), so d out / d u = sum_k omega_k d p_k / d u.
+__device__ __forceinline__ void teno5_jac(double u0, double u1, double u2, double u3, double u4, double eps,
+                                          double& out, double J[5]) {
+  double b0, b1, b2, o0, o1, o2;
+  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  teno5_weights(b0, b1, b2, eps, o0, o1, o2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  out = o0 * p0 + o1 * p1 + o2 * p2;
+  J[0] = (1.0 / 3.0) * o0;
+  J[1] = (-7.0 / 6.0) * o0 + (-1.0 / 6.0) * o1;
+  J[2] = (11.0 / 6.0) * o0 + (5.0 / 6.0) * o1 + (1.0 / 3.0) * o2;
+  J[3] = (1.0 / 3.0) * o1 + (5.0 / 6.0) * o2;
+  J[4] = (-1.0 / 6.0) * o2;
+}
+
 // weno3<Z>(u0, u1, u2) and its gradient (weno/weno3_js.py:22-45,
 // weno/weno3_z.py:24-46, weno3_base.py:20-44).
 template <bool Z>

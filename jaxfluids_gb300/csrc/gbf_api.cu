@@ -44,12 +44,13 @@ int make_case_info(const gbf_case* c, CaseInfo* ci) {
 static int check_case(const gbf_case* c, CaseInfo* ci) {
   int st = make_case_info(c, ci);
   if (st != GBF_OK) return st;
-  if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_WENO3Z) return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var != GBF_RECVAR_PRIMITIVE && c->recon_var != GBF_RECVAR_CHAR_PRIMITIVE)
+  if (c->recon < GBF_RECON_WENO5Z || c->recon > GBF_RECON_TENO5) return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var < GBF_RECVAR_PRIMITIVE || c->recon_var > GBF_RECVAR_CHAR_CONSERVATIVE)
     return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE &&
-      (c->recon != GBF_RECON_WENO5Z ||
-       (c->frozen_state != GBF_FROZEN_ARITHMETIC && c->frozen_state != GBF_FROZEN_ROE)))
+  // the characteristic and conservative reconstructions are built with WENO5-Z
+  if (c->recon_var != GBF_RECVAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
+  if ((c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) &&
+      c->frozen_state != GBF_FROZEN_ARITHMETIC && c->frozen_state != GBF_FROZEN_ROE)
     return GBF_ERR_UNSUPPORTED;
   if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_HLL) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
@@ -161,6 +162,29 @@ static int gbf_rhs_impl(const gbf_case* c, const double* prims, double* rhs, con
 
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
   return record_status(gbf_rhs_impl(c, prims, rhs, tile, stream));
+}
+
+static int gbf_rhs_cons_impl(const gbf_case* c, const double* prims, const double* cons, double* rhs,
+                             const gbf_tile* tile, void* stream) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!prims || !rhs || !cons) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(prims) || !aligned8(rhs) || !aligned8(cons)) return GBF_ERR_ALIGNMENT;
+  SweepParams p;
+  int threads;
+  size_t smem;
+  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
+  if (st != GBF_OK) return st;
+  p.prims_halo = prims;
+  p.cons_halo = cons;
+  p.out = rhs;
+  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS);
+}
+
+int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
+                 void* stream) {
+  return record_status(gbf_rhs_cons_impl(c, prims, cons, rhs, tile, stream));
 }
 
 static int gbf_volume_force_impl(const gbf_case* c, const double* cons, double* rhs, void* stream) {

@@ -123,6 +123,41 @@ __device__ __forceinline__ double weno5js(double u0, double u1, double u2, doubl
   return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
 }
 
+// TENO5 (teno/teno5.py, Fu et al. 2016) weights: gamma_k = (1 + tau5 / (beta_k
+// + eps))^6 (jnp.power with an integer exponent: x^2 (x^2)^2, the square-and-
+// multiply of lax.integer_pow), sharp cutoff (gamma_k / sum gamma < 1e-5 drops
+// stencil k), weights d_k = (0.05, 0.55, 0.40) of the kept stencils divided by
+// their sum + eps.  Unfused products: the adjoint units recompute the cutoff
+// with the forward's rounding.
+__device__ __forceinline__ void teno5_weights(double b0, double b1, double b2, double eps, double& o0,
+                                              double& o1, double& o2) {
+  const double tau5 = fabs(__dsub_rn(b0, b2));
+  auto gamma = [&](double b) {
+    const double x = __dadd_rn(1.0, __ddiv_rn(tau5, __dadd_rn(b, eps)));
+    const double x2 = __dmul_rn(x, x);
+    return __dmul_rn(x2, __dmul_rn(x2, x2));
+  };
+  const double g0 = gamma(b0), g1 = gamma(b1), g2 = gamma(b2);
+  const double one_gamma_sum = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(g0, g1), g2));
+  const double w0 = (__dmul_rn(g0, one_gamma_sum) < 1e-5) ? 0.0 : 0.05;
+  const double w1 = (__dmul_rn(g1, one_gamma_sum) < 1e-5) ? 0.0 : 0.55;
+  const double w2 = (__dmul_rn(g2, one_gamma_sum) < 1e-5) ? 0.0 : 0.40;
+  const double one_dk = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(__dadd_rn(w0, w1), w2), eps));
+  o0 = __dmul_rn(w0, one_dk);
+  o1 = __dmul_rn(w1, one_dk);
+  o2 = __dmul_rn(w2, one_dk);
+}
+
+__device__ __forceinline__ double teno5(double u0, double u1, double u2, double u3, double u4, double eps) {
+  double b0, b1, b2, o0, o1, o2;
+  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  teno5_weights(b0, b1, b2, eps, o0, o1, o2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  return o0 * p0 + o1 * p1 + o2 * p2;
+}
+
 // WENO3-JS (weno/weno3_js.py:22-45) and WENO3-Z (weno/weno3_z.py:24-46) on
 // (u_im, u_i, u_ip), weno3_base.py:20-44: d = (1/3, 2/3),
 // p0 = -u_im/2 + 3 u_i / 2, p1 = (u_i + u_ip) / 2.
@@ -169,10 +204,18 @@ __device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, dou
 // Roe-characteristic variables (reconstruction_variable CHAR-PRIMITIVE); same
 // six-cell window as WENO5-Z.
 constexpr int RECON_WENO5Z_CHAR = 100;
+// WENO5-Z on the conservatives (reconstruction_variable CONSERVATIVE) and on
+// their characteristic variables (CHAR-CONSERVATIVE); the pencil carries the
+// conservatives behind the primitives.
+constexpr int RECON_WENO5Z_CONS = 101;
+constexpr int RECON_WENO5Z_CHARCONS = 102;
 
 // Halo radius of a GBF_RECON_* stencil (host and device).
 __host__ __device__ constexpr int recon_radius(int recon) {
-  return (recon == GBF_RECON_WENO5Z || recon == GBF_RECON_WENO5JS || recon == RECON_WENO5Z_CHAR) ? 3 : 2;
+  return (recon == GBF_RECON_WENO5Z || recon == GBF_RECON_WENO5JS || recon == GBF_RECON_TENO5 ||
+          recon == RECON_WENO5Z_CHAR)
+             ? 3
+             : 2;
 }
 
 // Halo radius (cells each side of a face) of each reconstruction stencil.
@@ -180,6 +223,14 @@ template <int RECON>
 struct ReconTraits;
 template <>
 struct ReconTraits<RECON_WENO5Z_CHAR> {
+  static constexpr int R = 3;
+};
+template <>
+struct ReconTraits<RECON_WENO5Z_CONS> {
+  static constexpr int R = 3;
+};
+template <>
+struct ReconTraits<RECON_WENO5Z_CHARCONS> {
   static constexpr int R = 3;
 };
 template <>
@@ -196,6 +247,10 @@ struct ReconTraits<GBF_RECON_MINMOD_AD> {
 };
 template <>
 struct ReconTraits<GBF_RECON_WENO5JS> {
+  static constexpr int R = 3;
+};
+template <>
+struct ReconTraits<GBF_RECON_TENO5> {
   static constexpr int R = 3;
 };
 template <>
@@ -241,6 +296,13 @@ __device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO5JS>(const double
                                                                      double& L, double& R) {
   L = weno5js(w[0], w[1], w[2], w[3], w[4], eps);
   R = weno5js(w[5], w[4], w[3], w[2], w[1], eps);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair<GBF_RECON_TENO5>(const double* w, double eps,
+                                                                   double& L, double& R) {
+  L = teno5(w[0], w[1], w[2], w[3], w[4], eps);
+  R = teno5(w[5], w[4], w[3], w[2], w[1], eps);
 }
 
 template <>
@@ -292,6 +354,56 @@ __device__ __forceinline__ void frozen_state(const double L[5], const double R[5
   }
 }
 
+// Every output of compute_frozen_state (eigendecomposition.py:120-281), single
+// phase, for the conservative eigenvectors: averaged primitives (ROE:
+// compute_roe_cons :283-294, density sqrt(rho_L rho_R)), total enthalpy,
+// Grueneisen coefficient (gamma - 1 for the ideal gas), speed of sound, its
+// square and the squared averaged velocity.
+struct FrozenFull {
+  double pa[5];
+  double H, gr, c, cc, vsq;
+};
+
+// ideal_gas.py:90-110: (p / (gamma - 1) + 0.5 rho (u^2 + v^2 + w^2) + p) / rho
+__device__ __forceinline__ double total_enthalpy(double p, double rho, double u0, double u1, double u2,
+                                                 double gm1) {
+  const double E = p / gm1 + 0.5 * rho * (u0 * u0 + u1 * u1 + u2 * u2);
+  return (E + p) / rho;
+}
+
+__device__ __forceinline__ void frozen_state_full(const double L[5], const double R[5], const FaceParams& fp,
+                                                  FrozenFull& z) {
+  if (fp.frozen_state == GBF_FROZEN_ARITHMETIC) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) z.pa[v] = 0.5 * (L[v] + R[v]);
+    z.gr = fp.gm1;
+    z.H = total_enthalpy(z.pa[4], z.pa[0], z.pa[1], z.pa[2], z.pa[3], fp.gm1);
+    z.c = sqrt(fp.gamma * z.pa[4] / z.pa[0]);
+    z.cc = z.c * z.c;
+  } else {
+    const double sL = sqrt(L[0]);
+    const double sR = sqrt(R[0]);
+#pragma unroll
+    for (int v = 1; v < 5; ++v) z.pa[v] = (sL * L[v] + sR * R[v]) / (sL + sR);
+    z.pa[0] = sqrt(L[0] * R[0]);
+    const double rho_div = 1.0 / (sL + sR);
+    const double HL = total_enthalpy(L[4], L[0], L[1], L[2], L[3], fp.gm1);
+    const double HR = total_enthalpy(R[4], R[0], R[1], R[2], R[3], fp.gm1);
+    z.H = (sL * HL + sR * HR) * rho_div;
+    const double psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div;
+    z.gr = (sL * fp.gm1 + sR * fp.gm1) * rho_div;
+    const double d1 = R[1] - L[1];
+    const double d2 = R[2] - L[2];
+    const double d3 = R[3] - L[3];
+    const double sqvd = d1 * d1 + d2 * d2 + d3 * d3;
+    const double p_over_rho =
+        (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div + 0.5 * z.pa[0] * rho_div * rho_div * sqvd;
+    z.cc = psi_a + z.gr * p_over_rho;
+    z.c = sqrt(z.cc);
+  }
+  z.vsq = z.pa[1] * z.pa[1] + z.pa[2] * z.pa[2] + z.pa[3] * z.pa[3];
+}
+
 // velocity_minor_axes (equation_information.py:110) and vel_id_eigs
 // (eigendecomposition.py:67-71) for each sweep axis
 template <int AX>
@@ -301,6 +413,113 @@ struct CharIds {
   static constexpr int e0 = (AX == 1) ? 3 : 2;
   static constexpr int e1 = (AX == 1) ? 2 : 3;
 };
+
+// Left eigenvectors of the conservative flux Jacobian along AX
+// (eigendecomposition_conservatives, eigendecomposition.py:576-662, Fedkiw et
+// al. 1999), zeros included: the transforms sum over every column in order as
+// jnp.einsum("ij...,j...->i...") does.
+template <int AX>
+__device__ __forceinline__ void left_eigvecs_cons(const FrozenFull& z, double Lm[5][5]) {
+  constexpr int n = AX + 1;
+  using I = CharIds<AX>;
+  constexpr int m0 = I::m0, m1 = I::m1;
+  const double one_cc = 1.0 / z.cc;
+  const double one_rho = 1.0 / z.pa[0];
+  const double h = 0.5 * one_cc;
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) Lm[i][j] = 0.0;
+  Lm[0][0] = h * (z.gr * z.vsq - z.gr * z.H + (z.pa[n] + z.c) * z.c);
+  Lm[0][n] = h * (-z.pa[n] * z.gr - z.c);
+  Lm[0][m0] = h * (-z.pa[m0] * z.gr);
+  Lm[0][m1] = h * (-z.pa[m1] * z.gr);
+  Lm[0][4] = h * z.gr;
+  Lm[n][0] = one_cc * (z.H - z.vsq);
+  Lm[n][1] = z.pa[1] * one_cc;
+  Lm[n][2] = z.pa[2] * one_cc;
+  Lm[n][3] = z.pa[3] * one_cc;
+  Lm[n][4] = -one_cc;
+  Lm[m0][0] = z.pa[m0] * one_rho;
+  Lm[m0][m0] = -one_rho;
+  Lm[m1][0] = -z.pa[m1] * one_rho;
+  Lm[m1][m1] = one_rho;
+  Lm[4][0] = h * (z.gr * z.vsq - z.gr * z.H - (z.pa[n] - z.c) * z.c);
+  Lm[4][n] = h * (-z.pa[n] * z.gr + z.c);
+  Lm[4][m0] = h * (-z.pa[m0] * z.gr);
+  Lm[4][m1] = h * (-z.pa[m1] * z.gr);
+  Lm[4][4] = h * z.gr;
+}
+
+// Right eigenvectors (the same source), zeros included.
+template <int AX>
+__device__ __forceinline__ void right_eigvecs_cons(const FrozenFull& z, double Rm[5][5]) {
+  constexpr int n = AX + 1;
+  using I = CharIds<AX>;
+  constexpr int m0 = I::m0, m1 = I::m1;
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) Rm[i][j] = 0.0;
+  Rm[0][0] = 1.0;
+  Rm[n][0] = z.pa[n] - z.c;
+  Rm[m0][0] = z.pa[m0];
+  Rm[m1][0] = z.pa[m1];
+  Rm[4][0] = z.H - z.pa[n] * z.c;
+  Rm[0][n] = z.gr;
+  Rm[1][n] = z.gr * z.pa[1];
+  Rm[2][n] = z.gr * z.pa[2];
+  Rm[3][n] = z.gr * z.pa[3];
+  Rm[4][n] = z.gr * z.H - z.cc;
+  Rm[m0][m0] = -z.pa[0];
+  Rm[4][m0] = -z.pa[0] * z.pa[m0];
+  Rm[m1][m1] = z.pa[0];
+  Rm[4][m1] = z.pa[0] * z.pa[m1];
+  Rm[0][4] = 1.0;
+  Rm[n][4] = z.pa[n] + z.c;
+  Rm[m0][4] = z.pa[m0];
+  Rm[m1][4] = z.pa[m1];
+  Rm[4][4] = z.H + z.pa[n] * z.c;
+}
+
+// CHAR-CONSERVATIVE face states (high_order_godunov.py:404-416): the window of
+// conservatives u(v, k) (k = 0..5, face between cells 2 and 3) to
+// characteristic variables with the left eigenvectors of the frozen state of
+// the primitives w(v, 2), w(v, 3), WENO5-Z on each, back with the right ones.
+template <int AX, typename WU, typename WP>
+__device__ __forceinline__ void charcons_reconstruct(const WU& u, const WP& w, const FaceParams& fp, double UL[5],
+                                                     double UR[5]) {
+  double L[5], R[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    L[v] = w(v, 2);
+    R[v] = w(v, 3);
+  }
+  FrozenFull z;
+  frozen_state_full(L, R, fp, z);
+  double cL[5], cR[5];
+  {
+    double Lm[5][5];
+    left_eigvecs_cons<AX>(z, Lm);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      double ch[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+        ch[k] = Lm[i][0] * u(0, k) + Lm[i][1] * u(1, k) + Lm[i][2] * u(2, k) + Lm[i][3] * u(3, k) +
+                Lm[i][4] * u(4, k);
+      cL[i] = weno5z(ch[0], ch[1], ch[2], ch[3], ch[4], fp.stencil_eps);
+      cR[i] = weno5z(ch[5], ch[4], ch[3], ch[2], ch[1], fp.stencil_eps);
+    }
+  }
+  double Rm[5][5];
+  right_eigvecs_cons<AX>(z, Rm);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    UL[i] = Rm[i][0] * cL[0] + Rm[i][1] * cL[1] + Rm[i][2] * cL[2] + Rm[i][3] * cL[3] + Rm[i][4] * cL[4];
+    UR[i] = Rm[i][0] * cR[0] + Rm[i][1] * cR[1] + Rm[i][2] * cR[2] + Rm[i][3] * cR[3] + Rm[i][4] * cR[4];
+  }
+}
 
 // CHAR-PRIMITIVE face states (high_order_godunov.py:298-316): transform the six
 // window cells to characteristic variables with the face's frozen state
@@ -429,10 +648,12 @@ __device__ __forceinline__ void hllc_star_flux(const double P[5], const double U
   for (int v = 0; v < 5; ++v) F[v] = F[v] + wave * (us[v] - U[v]);
 }
 
-// HLLC._solve_riemann_problem_xi_single_phase (HLLC.py:80-126)
-template <int AX>
-__device__ __forceinline__ void hllc(const double PL[5], const double PR[5], const FaceParams& fp,
-                                     double F[5]) {
+// HLLC._solve_riemann_problem_xi_single_phase (HLLC.py:80-126).  GIVEN: the
+// face conservatives come with the primitives (the conservative
+// reconstructions) instead of being formed from them.
+template <int AX, bool GIVEN = false>
+__device__ __forceinline__ void hllc(const double PL[5], const double PR[5], const FaceParams& fp, double F[5],
+                                     const double* gUL = nullptr, const double* gUR = nullptr) {
   constexpr int N = AX + 1;
   const double cL = speed_of_sound(PL[4], PL[0], fp);
   const double cR = speed_of_sound(PR[4], PR[0], fp);
@@ -448,18 +669,26 @@ __device__ __forceinline__ void hllc(const double PL[5], const double PR[5], con
   // is formed (a finite F* times 0 adds a signed zero, which changes nothing
   // downstream); S* = 0 and NaN take the general blend.
   double UL[5], UR[5];
+  auto side = [&](const double* P, const double* gU, double* U) {
+    if (GIVEN) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) U[v] = gU[v];
+    } else {
+      cons_from_prims(P, U, fp.gm1);
+    }
+  };
   if (Ss > 0.0) {
-    cons_from_prims(PL, UL, fp.gm1);
+    side(PL, gUL, UL);
     hllc_star_flux<AX, 0>(PL, UL, SL, Ss, F);
     return;
   }
   if (Ss < 0.0) {
-    cons_from_prims(PR, UR, fp.gm1);
+    side(PR, gUR, UR);
     hllc_star_flux<AX, 1>(PR, UR, SR, Ss, F);
     return;
   }
-  cons_from_prims(PL, UL, fp.gm1);
-  cons_from_prims(PR, UR, fp.gm1);
+  side(PL, gUL, UL);
+  side(PR, gUR, UR);
   double FL[5], FR[5];
   hllc_star_flux<AX, 0>(PL, UL, SL, Ss, FL);
   hllc_star_flux<AX, 1>(PR, UR, SR, Ss, FR);
@@ -510,6 +739,20 @@ __device__ __forceinline__ void hll(const double PL[5], const double PR[5], cons
 // Face flux without a convective part (GBF_FLAG_NO_CONVECTIVE): flux_xi =
 // zeros, the dissipative fluxes are added to it.
 constexpr int RIEMANN_NONE = 100;
+
+// Face flux from face primitives and the given face conservatives (the
+// conservative reconstructions).
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void riemann_flux_u(const double PL[5], const double PR[5], const double UL[5],
+                                               const double UR[5], const FaceParams& fp, double F[5]) {
+  if (RIEMANN == GBF_RIEMANN_HLLC) {
+    hllc<AX, true>(PL, PR, fp, F, UL, UR);
+  } else if (RIEMANN == GBF_RIEMANN_HLL) {
+    hll<AX>(PL, PR, UL, UR, fp, F);
+  } else {
+    rusanov<AX>(PL, PR, UL, UR, fp, F);
+  }
+}
 
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux(const double PL[5], const double PR[5],

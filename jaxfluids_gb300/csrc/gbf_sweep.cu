@@ -93,7 +93,9 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
     pmax = std::max(pmax, pv);
     fmax = std::max(fmax, fv);
   }
-  const size_t bytes = (size_t)(pmax + fmax) * 5 * sizeof(double);
+  const bool cons_pencil =
+      c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
+  const size_t bytes = (size_t)((cons_pencil ? 2 : 1) * pmax + fmax) * 5 * sizeof(double);
   if (bytes > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
   for (int a = 0; a < 3; ++a) {
     q.n[a] = ci.n[a];
@@ -134,6 +136,15 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
                  int mode) {
   const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
   const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
+  const bool cons = c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
+  if (cons && !(c->flags & GBF_FLAG_NO_CONVECTIVE)) {
+    if (visc && mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
+    if (!visc && mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
+    if (mode == MODE_RHS && !p.cons_halo) return GBF_ERR_INVALID_ARGUMENT;  // needs the conservatives
+    return (c->recon_var == GBF_RECVAR_CONSERVATIVE)
+               ? launch_sweep_cons(visc, c->riemann, mode, p, threads, smem, s)
+               : launch_sweep_charcons(visc, c->riemann, mode, p, threads, smem, s);
+  }
   if (visc) {
     // dissipative fluxes read the primitive buffer (MODE_STAGE_P) or the halo buffer
     if (mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
@@ -147,6 +158,7 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
       return c4 ? launch_sweep_weno_visc_c4(c->riemann, mode, p, threads, smem, s)
                 : launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
     if (c->recon == GBF_RECON_WENO5JS) return launch_sweep_weno5js_visc(c->riemann, mode, p, threads, smem, s);
+    if (c->recon == GBF_RECON_TENO5) return launch_sweep_teno5_visc(c->riemann, mode, p, threads, smem, s);
     return launch_sweep_short_visc(c->recon, c->riemann, mode, p, threads, smem, s);
   }
   if (mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;

@@ -55,6 +55,7 @@ struct SweepParams {
   double one_dx[3];  // 1 / dx per axis
   FaceParams fp;
   const double* prims_halo;  // MODE_RHS input
+  const double* cons_halo;   // MODE_RHS input of the conservative reconstructions
   const double* cons;        // MODE_STAGE: stage state U^k (interior layout)
   const double* cons0;       // MODE_STAGE: step state U^n (interior layout)
   double* out;               // MODE_RHS: rhs; MODE_STAGE: U^{k+1}
@@ -411,8 +412,11 @@ __device__ __forceinline__ unsigned positivity_limit(double P[5], const double* 
 // Primitives of the pencil box (tile extended by R cells along AX) into
 // shared memory, variable-major: from the halo buffer (MODE_RHS), from the
 // interior primitive buffer (MODE_STAGE_P) or derived from the interior
-// conservatives (MODE_STAGE); boundary conditions by index remapping.
-template <int AX, int R, int MODE>
+// conservatives (MODE_STAGE); boundary conditions by index remapping.  CONS
+// also stages the conservatives behind the primitives (sm_prim[(5 + v) pvol]):
+// the halo buffer's (MODE_RHS), the state's in the interior, and in the halos
+// the conservatives of the halo primitives (material.py:248-250).
+template <int AX, int R, int MODE, bool CONS = false>
 __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3], const int pe[3], int pvol,
                                              double* sm_prim) {
   const int tid = threadIdx.x;
@@ -424,7 +428,7 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
     const int i0 = r / pe[1];
     int g[3] = {o[0] + i0, o[1] + i1, o[2] + i2};
     g[AX] -= R;
-    double P[5];
+    double P[5], U[5];
     if (MODE == MODE_RHS) {
       int b[3];
 #pragma unroll
@@ -433,6 +437,10 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
       const long long off = ((long long)b[0] * p.hs[1] + b[1]) * p.hs[2] + b[2];
 #pragma unroll
       for (int v = 0; v < 5; ++v) P[v] = __ldg(p.prims_halo + v * cs + off);
+      if (CONS) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) U[v] = __ldg(p.cons_halo + v * cs + off);
+      }
     } else {
       // halo cells along AX: the face rule applied to the primitives of the
       // retrieved interior cell (halo prims from interior prims, as the
@@ -448,8 +456,11 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
       if (MODE == MODE_STAGE_P) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) P[v] = __ldg(p.prims + v * cs + off);
+        if (CONS && !halo) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
+        }
       } else {
-        double U[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
         prims_from_cons(U, P, p.fp.gm1);
@@ -458,10 +469,15 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
 #pragma unroll
         for (int v = 0; v < 5; ++v)
           P[v] = bc_apply_at(t, p.bcv[f], p.bf, f, k, face_npos(p.n, AX), p.dx[AX], AX, v, P[v]);
+        if (CONS) cons_from_prims(P, U, p.fp.gm1);
       }
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_prim[v * pvol + i] = P[v];
+    if (CONS) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) sm_prim[(5 + v) * pvol + i] = U[v];
+    }
   }
 }
 
@@ -472,6 +488,7 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
                                            double* sm_prim, double* sm_flux,
                                            double (&acc)[MAXC][5], bool first) {
   constexpr int R = ReconTraits<RECON>::R;
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
 
@@ -481,7 +498,7 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
   const int pvol = pe[0] * pe[1] * pe[2];
 
   if (RIEMANN != RIEMANN_NONE) {
-    stage_pencil<AX, R, MODE>(p, o, pe, pvol, sm_prim);
+    stage_pencil<AX, R, MODE, CONS>(p, o, pe, pvol, sm_prim);
     __syncthreads();
   }
 
@@ -499,8 +516,27 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
+    double UL[5], UR[5];  // face conservatives of the conservative reconstructions
     if (RIEMANN == RIEMANN_NONE) {
       // no convective flux: nothing to reconstruct
+    } else if (RECON == RECON_WENO5Z_CONS) {
+      // high_order_godunov.py:282-296
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double w[2 * R];
+#pragma unroll
+        for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[(5 + v) * pvol + base + k * pstride];
+        reconstruct_pair<GBF_RECON_WENO5Z>(w, p.fp.stencil_eps, UL[v], UR[v]);
+      }
+      prims_from_cons(UL, PL, p.fp.gm1);
+      prims_from_cons(UR, PR, p.fp.gm1);
+    } else if (RECON == RECON_WENO5Z_CHARCONS) {
+      const double* b = sm_prim + base;
+      auto wu = [&](int v, int k) { return b[(5 + v) * pvol + k * pstride]; };
+      auto wp = [&](int v, int k) { return b[v * pvol + k * pstride]; };
+      charcons_reconstruct<AX>(wu, wp, p.fp, UL, UR);
+      prims_from_cons(UL, PL, p.fp.gm1);
+      prims_from_cons(UR, PR, p.fp.gm1);
     } else if (RECON == RECON_WENO5Z_CHAR) {
       const double* b = sm_prim + base;
       auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
@@ -511,7 +547,7 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
         double w[2 * R];
 #pragma unroll
         for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
-        reconstruct_pair<(RECON == RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
+        reconstruct_pair<(RECON >= RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
                                                                                   PL[v], PR[v]);
       }
     }
@@ -521,7 +557,13 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
       positivity_limit(PR, c + pstride, pvol, p.limiter);
     }
     double F[5];
-    riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
+    if (CONS && RIEMANN != RIEMANN_NONE && !p.limiter) {
+      riemann_flux_u<AX, RIEMANN>(PL, PR, UL, UR, p.fp, F);
+    } else {
+      // the limiter returns the conservatives of its primitives
+      // (limiter_interpolation.py:206)
+      riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
+    }
     if (VISC) {
       int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
       add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F);
@@ -590,8 +632,10 @@ __device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* 
       pmax = max(pmax, v);
     }
   }
+  // (the conservative reconstructions stage the conservatives too)
+  constexpr int PV = (RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS) ? 10 : 5;
   double* sm_prim = smem;
-  double* sm_flux = smem + 5 * pmax;
+  double* sm_flux = smem + PV * pmax;
 
   double acc[MAXC][5];
 #pragma unroll

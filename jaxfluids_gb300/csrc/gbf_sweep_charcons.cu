@@ -1,0 +1,18 @@
+// Sweep kernels: WENO5-Z on the characteristic variables of the conservatives
+// (reconstruction_variable CHAR-CONSERVATIVE), inviscid.
+#include "gbf_sweep_launch.cuh"
+
+namespace gbf {
+
+int launch_sweep_charcons_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                               cudaStream_t s);
+
+int launch_sweep_charcons(bool visc, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                          cudaStream_t s) {
+  if (visc) return launch_sweep_charcons_visc(riemann, mode, p, threads, smem, s);
+  if (mode == MODE_RHS)
+    return launch_sweep_riemann<RECON_WENO5Z_CHARCONS, MODE_RHS, 0>(riemann, p, threads, smem, s);
+  return launch_sweep_riemann<RECON_WENO5Z_CHARCONS, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+}
+
+}  // namespace gbf

@@ -43,6 +43,16 @@ int launch_sweep_weno5js_visc(int riemann, int mode, const SweepParams& p, int t
 int launch_sweep_short_visc(int recon, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                             cudaStream_t s);
 int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+// WENO5-Z on the conservatives and on their characteristic variables,
+// inviscid (MODE_RHS, MODE_STAGE) and with dissipative fluxes (MODE_RHS,
+// MODE_STAGE_P, stencils per case)
+int launch_sweep_cons(bool visc, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                      cudaStream_t s);
+int launch_sweep_charcons(bool visc, int riemann, int mode, const SweepParams& p, int threads, size_t smem,
+                          cudaStream_t s);
+// TENO5 on primitive variables, inviscid and with viscous / heat fluxes
+int launch_sweep_teno5(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
+int launch_sweep_teno5_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 // WENO5-Z (PRIMITIVE and CHAR-PRIMITIVE) with CENTRAL4 dissipative stencils fixed
 // at compile time (VISC = 2), the default setups
 int launch_sweep_weno_visc_c4(int riemann, int mode, const SweepParams& p, int threads, size_t smem,

@@ -20,6 +20,7 @@ int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams
     case GBF_RECON_WENO5JS: return launch_sweep_weno5js(riemann, mode, p, threads, smem, s);
     case GBF_RECON_WENO3JS: return launch_modes<GBF_RECON_WENO3JS>(riemann, mode, p, threads, smem, s);
     case GBF_RECON_WENO3Z: return launch_modes<GBF_RECON_WENO3Z>(riemann, mode, p, threads, smem, s);
+    case GBF_RECON_TENO5: return launch_sweep_teno5(riemann, mode, p, threads, smem, s);
     default: return GBF_ERR_UNSUPPORTED;
   }
 }

@@ -182,7 +182,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     }
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
-    if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS) {
+    if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5) {
       // one pass gives the face states and the stencil gradients; the left
       // gradient waits in the face's slots 0..4, the right one in this
       // thread's private rows, until the Riemann cotangents are known
@@ -194,6 +194,9 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         if constexpr (RECON == GBF_RECON_WENO5Z) {
           weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
           weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
+        } else if constexpr (RECON == GBF_RECON_TENO5) {
+          teno5_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
+          teno5_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
         } else {
           weno5js_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, PL[v], jl);
           weno5js_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, PR[v], jr);
@@ -341,6 +344,7 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
 int launch_vjp_weno5(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
                      cudaStream_t s);
 int launch_vjp_char(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
+int launch_vjp_teno5(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_short(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
                      cudaStream_t s);
 

@@ -127,8 +127,9 @@ class SpaceSolver(_Base):
         shape = self.config.halo_shape()
         rhs = torch.empty(self.config.interior_shape(), dtype=torch.float64, device=primitives.device)
         tile = ctypes.byref(self.tile) if self.tile is not None else None
-        _lib.check(self.lib.gbf_rhs(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
-                                    _ptr(rhs), tile, _stream()), "compute_rhs")
+        _lib.check(self.lib.gbf_rhs_cons(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
+                                         _ptr(conservatives, shape, "conservatives"), _ptr(rhs), tile, _stream()),
+                   "compute_rhs")
         if self.config.gravity is not None:
             # volume forces from the conservatives (space_solver.py:377-384)
             _lib.check(self.lib.gbf_volume_force(ctypes.byref(self.case), _ptr(conservatives, shape, "conservatives"),

@@ -55,8 +55,8 @@ class OracleCase:
     gamma: float = 1.4
     R: float = 1.0
     bc: Dict[str, str] = field(default_factory=dict)
-    recon: str = "WENO5-Z"                 # WENO5-Z | WENO5-JS | WENO3-JS | WENO3-Z | MINMOD | MINMOD-AD
-    recon_var: str = "PRIMITIVE"           # PRIMITIVE | CHAR-PRIMITIVE
+    recon: str = "WENO5-Z"                 # WENO5-Z | WENO5-JS | TENO5 | WENO3-JS | WENO3-Z | MINMOD | MINMOD-AD
+    recon_var: str = "PRIMITIVE"           # PRIMITIVE | CHAR-PRIMITIVE | CONSERVATIVE | CHAR-CONSERVATIVE
     frozen_state: str = "ARITHMETIC"       # ARITHMETIC | ROE
     riemann: str = "HLLC"                  # HLLC | HLL | RUSANOV
     signal_speed: str = "EINFELDT"
@@ -272,6 +272,40 @@ def weno5js_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
     return (a0 * one_a) * p0 + (a1 * one_a) * p1 + (a2 * one_a) * p2
 
 
+_TENO5_DR = (0.05, 0.55, 0.40)                # teno5.py: coefficients for spectral properties
+_TENO5_CT = 1e-5                               # teno5.py: cutoff
+
+
+def teno5_stencil(u0: Tensor, u1: Tensor, u2: Tensor, u3: Tensor, u4: Tensor,
+                  eps: float = STENCIL_EPS) -> Tensor:
+    """TENO5 (shock_capturing/teno/teno5.py, Fu et al. 2016): gamma_k = (C +
+    tau5 / (beta_k + eps))^q with C = 1, q = 6 (jnp.power with an integer
+    exponent: lax.integer_pow's square-and-multiply, x^2 (x^2 x^2)); stencils
+    with gamma_k / sum gamma < CT are cut; the kept d_k normalised by their sum
+    + eps weight the WENO5 polynomials."""
+    b0, b1, b2 = _weno5_smoothness(u0, u1, u2, u3, u4)
+    tau5 = torch.abs(b0 - b2)
+
+    def gamma(b):
+        x = 1.0 + tau5 / (b + eps)
+        x2 = x * x
+        return x2 * (x2 * x2)
+    g0, g1, g2 = gamma(b0), gamma(b1), gamma(b2)
+    one_gamma_sum = 1.0 / (g0 + g1 + g2)
+    def keep(g):
+        # jnp.where(chi < CT, 0, 1): no derivative
+        return torch.where(g * one_gamma_sum < _TENO5_CT, torch.zeros_like(g), torch.ones_like(g)).detach()
+    w0 = _TENO5_DR[0] * keep(g0)
+    w1 = _TENO5_DR[1] * keep(g1)
+    w2 = _TENO5_DR[2] * keep(g2)
+    one_dk = 1.0 / (w0 + w1 + w2 + eps)
+    c = _WENO_CR
+    p0 = c[0][0] * u0 + c[0][1] * u1 + c[0][2] * u2
+    p1 = c[1][0] * u1 + c[1][1] * u2 + c[1][2] * u3
+    p2 = c[2][0] * u2 + c[2][1] * u3 + c[2][2] * u4
+    return (w0 * one_dk) * p0 + (w1 * one_dk) * p1 + (w2 * one_dk) * p2
+
+
 _WENO3_DR = (1 / 3, 2 / 3)                    # weno3_base.py:24
 _WENO3_CR = ((-0.5, 1.5), (0.5, 0.5))          # weno3_base.py:25
 
@@ -298,7 +332,7 @@ def _recon_offsets(recon: str, j: int) -> Tuple[int, ...]:
     if recon in ("WENO3-JS", "WENO3-Z"):
         # weno3_base.py:29 array_slices([range(-2, 1, 1), range(1, -2, -1)])
         return (-2, -1, 0) if j == 0 else (1, 0, -1)
-    if recon in ("WENO5-Z", "WENO5-JS"):
+    if recon in ("WENO5-Z", "WENO5-JS", "TENO5"):
         # weno5_base.py:30 array_slices([range(-3, 2, 1), range(2, -3, -1)])
         return (-3, -2, -1, 0, 1) if j == 0 else (2, 1, 0, -1, -2)
     if recon in ("MINMOD", "MINMOD-AD"):
@@ -313,6 +347,8 @@ def recon_stencil(recon: str, j: int, vals: List[Tensor], eps: float = STENCIL_E
         return weno5z_stencil(*vals, eps=eps)
     if recon == "WENO5-JS":
         return weno5js_stencil(*vals, eps=eps)
+    if recon == "TENO5":
+        return teno5_stencil(*vals, eps=eps)
     if recon in ("WENO3-JS", "WENO3-Z"):
         return weno3_stencil(*vals, z=(recon == "WENO3-Z"), eps=eps)
     b0, b1, b2 = vals
@@ -386,6 +422,93 @@ def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, Tensor
         cc = psi_a + gr_a * p_over_rho
         return rho_a, torch.sqrt(cc), cc
     raise NotImplementedError(case.frozen_state)
+
+
+def _total_enthalpy(p: Tensor, rho: Tensor, u: Tensor, g: float) -> Tensor:
+    # ideal_gas.py:90-110: (p / (gamma - 1) + 0.5 rho (u^2 + v^2 + w^2) + p) / rho
+    E = p / (g - 1) + 0.5 * rho * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2])
+    return (E + p) / rho
+
+
+def frozen_state_full(P: Tensor, case: OracleCase, axis: int):
+    """compute_frozen_state (eigendecomposition.py:120-281), single phase, with
+    every output the conservative eigenvectors use: averaged primitives (ROE:
+    compute_roe_cons :283-294 with the density sqrt(rho_L rho_R)), total
+    enthalpy, Grueneisen coefficient (gamma - 1 for the ideal gas), speed of
+    sound, its square, and the squared averaged velocity."""
+    g = case.gamma
+    L = P[_stencil_slice(case, axis, -1)]
+    R = P[_stencil_slice(case, axis, 0)]
+    if case.frozen_state == "ARITHMETIC":
+        pa = 0.5 * (L + R)
+        gr = (g - 1) * torch.ones_like(pa[0])
+        H = _total_enthalpy(pa[4], pa[0], pa[1:4], g)
+        c = torch.sqrt(g * pa[4] / pa[0])
+        cc = c * c
+    elif case.frozen_state == "ROE":
+        sL, sR = torch.sqrt(L[0]), torch.sqrt(R[0])
+        pa = (sL * L + sR * R) / (sL + sR)
+        pa = torch.cat([torch.sqrt(L[0] * R[0]).unsqueeze(0), pa[1:]], 0)
+        rho_div = 1.0 / (sL + sR)
+        H = (sL * _total_enthalpy(L[4], L[0], L[1:4], g) + sR * _total_enthalpy(R[4], R[0], R[1:4], g)) * rho_div
+        psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div
+        gr = (sL * (g - 1) + sR * (g - 1)) * rho_div
+        d = R[1:4] - L[1:4]
+        d2 = d * d
+        sqvd = d2[0] + d2[1] + d2[2]
+        p_over_rho = (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div \
+            + 0.5 * pa[0] * rho_div * rho_div * sqvd
+        cc = psi_a + gr * p_over_rho
+        c = torch.sqrt(cc)
+    else:
+        raise NotImplementedError(case.frozen_state)
+    u2 = pa[1:4] * pa[1:4]
+    vsq = u2[0] + u2[1] + u2[2]
+    return pa, H, gr, c, cc, vsq
+
+
+def eigvecs_conservatives(P: Tensor, case: OracleCase, axis: int):
+    """eigendecomposition_conservatives (eigendecomposition.py:576-662), single
+    phase (Fedkiw et al. 1999): right and left eigenvectors of the
+    conservative flux Jacobian at every face, as 5 x 5 nested lists."""
+    pa, H, gr, c, cc, vsq = frozen_state_full(P, case, axis)
+    one_cc = 1.0 / cc
+    one_rho = 1.0 / pa[0]
+    n = axis + 1
+    m0, m1 = VEL_MINORS[axis]
+    z = torch.zeros_like(pa[0])
+    Rm = [[z] * 5 for _ in range(5)]
+    Lm = [[z] * 5 for _ in range(5)]
+    one = torch.ones_like(pa[0])
+    Rm[0][0], Rm[n][0], Rm[m0][0], Rm[m1][0], Rm[4][0] = one, pa[n] - c, pa[m0], pa[m1], H - pa[n] * c
+    Rm[0][n], Rm[1][n], Rm[2][n], Rm[3][n] = gr, gr * pa[1], gr * pa[2], gr * pa[3]
+    Rm[4][n] = gr * H - cc
+    Rm[m0][m0], Rm[4][m0] = -pa[0], -pa[0] * pa[m0]
+    Rm[m1][m1], Rm[4][m1] = pa[0], pa[0] * pa[m1]
+    Rm[0][4], Rm[n][4], Rm[m0][4], Rm[m1][4], Rm[4][4] = one, pa[n] + c, pa[m0], pa[m1], H + pa[n] * c
+    h = 0.5 * one_cc
+    Lm[0][0] = h * (gr * vsq - gr * H + (pa[n] + c) * c)
+    Lm[0][n] = h * (-pa[n] * gr - c)
+    Lm[0][m0] = h * (-pa[m0] * gr)
+    Lm[0][m1] = h * (-pa[m1] * gr)
+    Lm[0][4] = h * gr
+    Lm[n][0] = one_cc * (H - vsq)
+    Lm[n][1], Lm[n][2], Lm[n][3] = pa[1] * one_cc, pa[2] * one_cc, pa[3] * one_cc
+    Lm[n][4] = -one_cc
+    Lm[m0][0], Lm[m0][m0] = pa[m0] * one_rho, -one_rho
+    Lm[m1][0], Lm[m1][m1] = -pa[m1] * one_rho, one_rho
+    Lm[4][0] = h * (gr * vsq - gr * H - (pa[n] - c) * c)
+    Lm[4][n] = h * (-pa[n] * gr + c)
+    Lm[4][m0] = h * (-pa[m0] * gr)
+    Lm[4][m1] = h * (-pa[m1] * gr)
+    Lm[4][4] = h * gr
+    return Rm, Lm
+
+
+def _matvec5(M, x: List[Tensor]) -> List[Tensor]:
+    # jnp.einsum("ij...,j...->i...") as a sum over j in index order
+    return [M[i][0] * x[0] + M[i][1] * x[1] + M[i][2] * x[2] + M[i][3] * x[3] + M[i][4] * x[4]
+            for i in range(5)]
 
 
 def chars_from_prims(x: List[Tensor], rho_a, c, cc, axis: int) -> List[Tensor]:
@@ -507,9 +630,10 @@ def riemann(PL, PR, UL, UR, case: OracleCase, axis: int) -> Tensor:
     raise NotImplementedError(case.riemann)
 
 
-def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
-    """HighOrderGodunov.compute_flux_xi (high_order_godunov.py:117-231, :233-402)."""
+def convective_flux_xi(P: Tensor, case: OracleCase, axis: int, U: Optional[Tensor] = None) -> Tensor:
+    """HighOrderGodunov.compute_flux_xi (high_order_godunov.py:117-231, :233-418)."""
     g = case.gamma
+    UL = UR = None
     if case.recon_var == "PRIMITIVE":
         PL = reconstruct_xi(P, case, axis, 0)
         PR = reconstruct_xi(P, case, axis, 1)
@@ -526,14 +650,38 @@ def convective_flux_xi(P: Tensor, case: OracleCase, axis: int) -> Tensor:
         cR = [weno5z_stencil(*[chars[k][v] for k in (5, 4, 3, 2, 1)]) for v in range(5)]
         PL = torch.stack(prims_from_chars(cL, rho_a, c, cc, axis), 0)
         PR = torch.stack(prims_from_chars(cR, rho_a, c, cc, axis), 0)
+    elif case.recon_var == "CONSERVATIVE":
+        # high_order_godunov.py:282-296: reconstruct the conservatives
+        if case.recon != "WENO5-Z":
+            raise NotImplementedError("CONSERVATIVE is restated for WENO5-Z")
+        UL = reconstruct_xi(U, case, axis, 0)
+        UR = reconstruct_xi(U, case, axis, 1)
+        PL, PR = prims_from_cons(UL, g), prims_from_cons(UR, g)
+    elif case.recon_var == "CHAR-CONSERVATIVE":
+        # high_order_godunov.py:404-416: window of conservatives to
+        # characteristics with the face's left eigenvectors, WENO on each,
+        # back with the right eigenvectors
+        if case.recon != "WENO5-Z":
+            raise NotImplementedError("CHAR-CONSERVATIVE is restated for WENO5-Z")
+        Rm, Lm = eigvecs_conservatives(P, case, axis)
+        win = [U[_stencil_slice(case, axis, k)] for k in range(-3, 3)]
+        chars = [_matvec5(Lm, [w[v] for v in range(5)]) for w in win]
+        cL = [weno5z_stencil(*[chars[k][v] for k in (0, 1, 2, 3, 4)]) for v in range(5)]
+        cR = [weno5z_stencil(*[chars[k][v] for k in (5, 4, 3, 2, 1)]) for v in range(5)]
+        UL = torch.stack(_matvec5(Rm, cL), 0)
+        UR = torch.stack(_matvec5(Rm, cR), 0)
+        PL, PR = prims_from_cons(UL, g), prims_from_cons(UR, g)
     else:
         raise NotImplementedError(case.recon_var)
     if case.interpolation_limiter:
-        # high_order_godunov.py:163-175
+        # high_order_godunov.py:163-175; the limiter returns the conservatives
+        # of its primitives (limiter_interpolation.py:206)
         PL = limit_interpolation(P, PL, case, axis, 0)
         PR = limit_interpolation(P, PR, case, axis, 1)
-    UL = cons_from_prims(PL, g)
-    UR = cons_from_prims(PR, g)
+        UL = UR = None
+    if UL is None:
+        UL = cons_from_prims(PL, g)
+        UR = cons_from_prims(PR, g)
     return riemann(PL, PR, UL, UR, case, axis)
 
 
@@ -697,7 +845,7 @@ def compute_rhs(U: Tensor, P: Tensor, case: OracleCase) -> Tensor:
     rhs = None
     for axis in case.active:
         if case.convective:
-            flux = convective_flux_xi(P, case, axis)
+            flux = convective_flux_xi(P, case, axis, U)
         else:
             # space_solver.py:510: flux_xi = zeros(flux_shapes[axis])
             flux = torch.zeros((5,) + _deriv_face(P[:1], case, axis).shape[1:], dtype=P.dtype)

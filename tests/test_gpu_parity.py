@@ -78,6 +78,28 @@ RHS_CASES = [
     # WENO5-JS, WENO3-JS, WENO3-Z and HLL (with every signal speed)
     ("sod-weno5js-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="WENO5-JS"), "sod"),
     ("sod-weno3js-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="WENO3-JS"), "sod"),
+    # CONSERVATIVE and CHAR-CONSERVATIVE reconstructions (WENO5-Z)
+    ("sod-cons-hllc", dict(cells=(200, 1, 1), bc=ZG, recon_var="CONSERVATIVE"), "sod"),
+    ("sod-charcons-roe-hllc", dict(cells=(200, 1, 1), bc=ZG, recon_var="CHAR-CONSERVATIVE", frozen_state="ROE"),
+     "sod"),
+    ("quad-2d-charcons-arith-hll", dict(cells=(40, 44, 1), bc=ZG, recon_var="CHAR-CONSERVATIVE", riemann="HLL"),
+     "quad"),
+    ("quad-2d-cons-rusanov", dict(cells=(44, 40, 1), bc=ZG, recon_var="CONSERVATIVE", riemann="RUSANOV"), "quad"),
+    ("tgv-3d-charcons-roe-hllc", dict(cells=(20, 16, 24), bc="PERIODIC", recon_var="CHAR-CONSERVATIVE",
+                                      frozen_state="ROE", ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-cons-viscous-heat", dict(cells=(16, 20, 12), bc="PERIODIC", nh=4, recon_var="CONSERVATIVE",
+                                      viscous=True, heat=True, mu=1e-2, prandtl=0.71,
+                                      ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-charcons-roe-viscous", dict(cells=(12, 16, 14), bc="PERIODIC", nh=4, recon_var="CHAR-CONSERVATIVE",
+                                         frozen_state="ROE", viscous=True, heat=True, mu=1e-2, prandtl=0.71,
+                                         ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    # TENO5 (its sharp cutoff drops stencils across the discontinuities)
+    ("sod-teno5-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="TENO5"), "sod"),
+    ("quad-2d-teno5-rusanov", dict(cells=(48, 40, 1), bc=ZG, recon="TENO5", riemann="RUSANOV"), "quad"),
+    ("tgv-3d-teno5-hll", dict(cells=(20, 16, 24), bc="PERIODIC", recon="TENO5", riemann="HLL",
+                              ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-teno5-viscous-heat", dict(cells=(16, 20, 12), bc="PERIODIC", nh=4, recon="TENO5", viscous=True,
+                                       heat=True, mu=1e-2, prandtl=0.71, ranges=((0, 2 * math.pi),) * 3), "tgv"),
     ("sod-weno3z-rusanov", dict(cells=(200, 1, 1), bc=ZG, recon="WENO3-Z", riemann="RUSANOV"), "sod"),
     ("sod-hll-einfeldt", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL"), "sod"),
     ("sod-hll-davis", dict(cells=(200, 1, 1), bc=ZG, riemann="HLL", signal_speed="DAVIS"), "sod"),
@@ -179,7 +201,10 @@ def test_steps_match_oracle(fused):
                                                 "viscous": True, "heat": True, "mu": 1.0 / 1600, "prandtl": 0.71}),
              ((24, 20, 1), "PERIODIC", "quad", {"nh": 4, "viscous": True, "mu": 0.05}),
              ((48, 40, 1), ZG, "quad", {"recon": "WENO5-JS", "riemann": "HLL"}),
-             ((40, 36, 1), ZG, "quad", {"recon": "WENO3-Z", "riemann": "HLL", "signal_speed": "DAVIS"})]
+             ((40, 36, 1), ZG, "quad", {"recon": "WENO3-Z", "riemann": "HLL", "signal_speed": "DAVIS"}),
+             ((44, 40, 1), ZG, "quad", {"recon": "TENO5"}),
+             ((40, 44, 1), ZG, "quad", {"recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE"}),
+             ((44, 40, 1), ZG, "quad", {"recon_var": "CONSERVATIVE", "riemann": "HLL"})]
     for cells, bc, kind, kw in cases:
         oc, cc = both(cells, bc, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
