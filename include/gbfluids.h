@@ -61,6 +61,12 @@ extern "C" {
 #define GBF_RIEMANN_HLLC 0
 #define GBF_RIEMANN_RUSANOV 1
 #define GBF_RIEMANN_HLL 2     /* riemann_solvers/HLL.py */
+/* riemann_solvers/LaxFriedrichs.py: Rusanov's flux with one dissipation speed
+ * per axis, the maximum of |u| + c over every reconstructed face state of the
+ * axis (reduced by an extra reconstruction pass; the pass's scratch is a
+ * per-device array, so Lax-Friedrichs evaluations on concurrent streams of one
+ * device must not overlap) */
+#define GBF_RIEMANN_LAXFRIEDRICHS 3
 
 /* signal_speed (solvers/riemann_solvers/__init__.py:27) */
 #define GBF_SIGNAL_EINFELDT 0

@@ -24,7 +24,7 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported setup", -3: "CUDA la
 RECON = {"WENO5-Z": 0, "MINMOD": 1, "MINMOD-AD": 2, "WENO5-JS": 3, "WENO3-JS": 4, "WENO3-Z": 5, "TENO5": 6}
 RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1, "CONSERVATIVE": 2, "CHAR-CONSERVATIVE": 3}
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
-RIEMANN = {"HLLC": 0, "RUSANOV": 1, "HLL": 2}
+RIEMANN = {"LAX-FRIEDRICHS": 3, "HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
 ABI_VERSION = 5  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}

@@ -423,7 +423,8 @@ int vjp_check(const gbf_case* c) {
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // the conservative reconstructions have no reverse
+  // Lax-Friedrichs' global maximum and the conservative reconstructions have no reverse
+  if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE)
     return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own

@@ -52,7 +52,7 @@ static int check_case(const gbf_case* c, CaseInfo* ci) {
   if ((c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) &&
       c->frozen_state != GBF_FROZEN_ARITHMETIC && c->frozen_state != GBF_FROZEN_ROE)
     return GBF_ERR_UNSUPPORTED;
-  if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_HLL) return GBF_ERR_UNSUPPORTED;
+  if (c->riemann < GBF_RIEMANN_HLLC || c->riemann > GBF_RIEMANN_LAXFRIEDRICHS) return GBF_ERR_UNSUPPORTED;
   if (c->signal_speed < GBF_SIGNAL_EINFELDT || c->signal_speed > GBF_SIGNAL_TORO)
     return GBF_ERR_UNSUPPORTED;
   if (c->flags & ~(GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_VISCOUS_HEAT_PRODUCTION | GBF_FLAG_NO_CONVECTIVE |

@@ -175,7 +175,8 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
   if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
   if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_GRAVITY))
     return GBF_ERR_UNSUPPORTED;
-  if (scheme->riemann == GBF_RIEMANN_HLL || scheme->recon > GBF_RECON_MINMOD_AD ||
+  if (scheme->riemann == GBF_RIEMANN_HLL || scheme->riemann == GBF_RIEMANN_LAXFRIEDRICHS ||
+      scheme->recon > GBF_RECON_MINMOD_AD ||
       scheme->recon_var > GBF_RECVAR_CHAR_PRIMITIVE)
     return GBF_ERR_UNSUPPORTED;
   for (int f = 0; f < 6; ++f)  // boundary value fields are per case size: not batched

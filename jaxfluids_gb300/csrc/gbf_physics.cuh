@@ -699,6 +699,18 @@ __device__ __forceinline__ void hllc(const double PL[5], const double PR[5], con
   for (int v = 0; v < 5; ++v) F[v] = fma(wl, FL[v], wr * FR[v]);  // wl in {0, 1/2, 1}: exact product
 }
 
+// 0.5 (F_L + F_R) - 0.5 alpha (U_R - U_L): Rusanov's flux with its local alpha,
+// Lax-Friedrichs' (LaxFriedrichs.py:25-47) with the axis' global one.
+template <int AX>
+__device__ __forceinline__ void rusanov_alpha(const double PL[5], const double PR[5], const double UL[5],
+                                              const double UR[5], double alpha, double F[5]) {
+  double FL[5], FR[5];
+  physical_flux<AX>(PL, UL, FL);
+  physical_flux<AX>(PR, UR, FR);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F[v] = fma(0.5, FL[v] + FR[v], -(0.5 * alpha * (UR[v] - UL[v])));
+}
+
 // Rusanov._solve_riemann_problem_xi_single_phase (Rusanov.py:25-47)
 template <int AX>
 __device__ __forceinline__ void rusanov(const double PL[5], const double PR[5], const double UL[5],
@@ -707,11 +719,7 @@ __device__ __forceinline__ void rusanov(const double PL[5], const double PR[5], 
   const double cL = speed_of_sound(PL[4], PL[0], fp);
   const double cR = speed_of_sound(PR[4], PR[0], fp);
   const double alpha = fmax(fabs(PL[N]) + cL, fabs(PR[N]) + cR);
-  double FL[5], FR[5];
-  physical_flux<AX>(PL, UL, FL);
-  physical_flux<AX>(PR, UR, FR);
-#pragma unroll
-  for (int v = 0; v < 5; ++v) F[v] = fma(0.5, FL[v] + FR[v], -(0.5 * alpha * (UR[v] - UL[v])));
+  rusanov_alpha<AX>(PL, PR, UL, UR, alpha, F);
 }
 
 // HLL._solve_riemann_problem_xi_single_phase (HLL.py:28-58):

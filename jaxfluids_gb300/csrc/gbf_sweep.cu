@@ -132,8 +132,57 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   return GBF_OK;
 }
 
-int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
-                 int mode) {
+namespace {
+
+// Lax-Friedrichs dissipation speeds (bits of three non-negative doubles), one
+// array per device; its address is looked up once per device, before any
+// graph capture (the first launch of a case).
+__device__ unsigned long long g_lf_alpha[3];
+constexpr int kLfMaxDevices = 64;
+double* g_lf_alpha_ptr[kLfMaxDevices] = {};
+
+int lf_alpha_on_current_device(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GBF_ERR_CUDA;
+  if (dev < 0 || dev >= kLfMaxDevices) return GBF_ERR_UNSUPPORTED;
+  if (!g_lf_alpha_ptr[dev]) {
+    void* a = nullptr;
+    if (cudaGetSymbolAddress(&a, g_lf_alpha) != cudaSuccess || !a) return GBF_ERR_CUDA;
+    g_lf_alpha_ptr[dev] = static_cast<double*>(a);
+  }
+  *out = g_lf_alpha_ptr[dev];
+  return GBF_OK;
+}
+
+int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
+                         int mode);
+
+}  // namespace
+
+// Lax-Friedrichs (LaxFriedrichs.py:25-47) runs the Rusanov instantiation twice:
+// a pass reducing the axis' max |u| + c over the face states, then the flux
+// pass with that speed.
+int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s, int mode) {
+  if (c->riemann != GBF_RIEMANN_LAXFRIEDRICHS || (c->flags & GBF_FLAG_NO_CONVECTIVE))
+    return launch_sweep_schemes(c, p, threads, smem, s, mode);
+  double* alpha = nullptr;
+  int st = lf_alpha_on_current_device(&alpha);
+  if (st != GBF_OK) return st;
+  if (cudaMemsetAsync(alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
+  SweepParams q = p;
+  q.lf_alpha = alpha;
+  q.speed_pass = 1;
+  q.reduce_dt = 0;
+  if ((st = launch_sweep_schemes(c, q, threads, smem, s, mode)) != GBF_OK) return st;
+  q.speed_pass = 0;
+  q.reduce_dt = p.reduce_dt;
+  return launch_sweep_schemes(c, q, threads, smem, s, mode);
+}
+
+namespace {
+
+int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
+                         int mode) {
   const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
   const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
   const bool cons = c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
@@ -168,5 +217,7 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
     return launch_sweep_muscl(c->recon, c->riemann, mode, p, threads, smem, s);
   return launch_sweep_weno_family(c->recon, c->riemann, mode, p, threads, smem, s);
 }
+
+}  // namespace
 
 }  // namespace gbf

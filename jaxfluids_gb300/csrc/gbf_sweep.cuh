@@ -79,6 +79,11 @@ struct SweepParams {
   int limiter;
   int gravity;               // volume force on
   double g[3];               // gravity vector
+  // Lax-Friedrichs (Rusanov instantiations): the per-axis dissipation speeds;
+  // speed_pass reduces them (max of |u| + c over the face states, as bits)
+  // instead of computing fluxes
+  double* lf_alpha;
+  int speed_pass;
 };
 
 // Gravity forces added to a cell's right-hand side (source_term_solver.py:165-186,
@@ -507,6 +512,7 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
   fe[AX] += 1;
   const int fvol = fe[0] * fe[1] * fe[2];
   const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
+  double smax_faces = 0.0;  // Lax-Friedrichs speed pass
   for (int f = tid; f < fvol; f += nthr) {
     const int f2 = f % fe[2];
     const int r = f / fe[2];
@@ -556,8 +562,28 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
       positivity_limit(PL, c, pvol, p.limiter);
       positivity_limit(PR, c + pstride, pvol, p.limiter);
     }
+    if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
+      // LaxFriedrichs.py:35-38: max(max |u_L| + c_L, max |u_R| + c_R) over the axis
+      const double cL = speed_of_sound(PL[4], PL[0], p.fp);
+      const double cR = speed_of_sound(PR[4], PR[0], p.fp);
+      smax_faces = fmax(smax_faces, fmax(fabs(PL[AX + 1]) + cL, fabs(PR[AX + 1]) + cR));
+      continue;
+    }
     double F[5];
-    if (CONS && RIEMANN != RIEMANN_NONE && !p.limiter) {
+    if (RIEMANN == GBF_RIEMANN_RUSANOV && p.lf_alpha) {
+      double uL[5], uR[5];
+      if (CONS && !p.limiter) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          uL[v] = UL[v];
+          uR[v] = UR[v];
+        }
+      } else {
+        cons_from_prims(PL, uL, p.fp.gm1);
+        cons_from_prims(PR, uR, p.fp.gm1);
+      }
+      rusanov_alpha<AX>(PL, PR, uL, uR, p.lf_alpha[AX], F);
+    } else if (CONS && RIEMANN != RIEMANN_NONE && !p.limiter) {
       riemann_flux_u<AX, RIEMANN>(PL, PR, UL, UR, p.fp, F);
     } else {
       // the limiter returns the conservatives of its primitives
@@ -570,6 +596,17 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
+  }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
+    // warp maximum, one atomic per warp on the order-preserving bits of the
+    // non-negative speeds
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) smax_faces = fmax(smax_faces, __shfl_xor_sync(0xffffffffu, smax_faces, off));
+    if ((tid & 31) == 0)
+      atomicMax(reinterpret_cast<unsigned long long*>(p.lf_alpha) + AX,
+                (unsigned long long)__double_as_longlong(smax_faces));
+    __syncthreads();  // the pencil is restaged by the next axis
+    return;
   }
   __syncthreads();
 
@@ -655,6 +692,7 @@ __device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* 
   if (p.active_mask & 4) {
     sweep_axis<2, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
   }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) return;  // speeds only, nothing to store
 
   // ---- epilogue ---------------------------------------------------------
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];

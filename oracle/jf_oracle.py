@@ -58,7 +58,7 @@ class OracleCase:
     recon: str = "WENO5-Z"                 # WENO5-Z | WENO5-JS | TENO5 | WENO3-JS | WENO3-Z | MINMOD | MINMOD-AD
     recon_var: str = "PRIMITIVE"           # PRIMITIVE | CHAR-PRIMITIVE | CONSERVATIVE | CHAR-CONSERVATIVE
     frozen_state: str = "ARITHMETIC"       # ARITHMETIC | ROE
-    riemann: str = "HLLC"                  # HLLC | HLL | RUSANOV
+    riemann: str = "HLLC"                  # HLLC | HLL | RUSANOV | LAX-FRIEDRICHS
     signal_speed: str = "EINFELDT"
     cfl: float = 0.5
     fixed_dt: Optional[float] = None
@@ -624,6 +624,12 @@ def riemann(PL, PR, UL, UR, case: OracleCase, axis: int) -> Tensor:
     if case.riemann == "RUSANOV":
         # Rusanov.py:25-47
         alpha = torch.maximum(jabs(PL[n]) + cL, jabs(PR[n]) + cR)
+        FL = fluxes_xi(PL, UL, axis)
+        FR = fluxes_xi(PR, UR, axis)
+        return 0.5 * (FL + FR) - 0.5 * alpha * (UR - UL)
+    if case.riemann == "LAX-FRIEDRICHS":
+        # LaxFriedrichs.py:25-47: one alpha for the axis, the maxima over every face
+        alpha = torch.maximum(torch.max(jabs(PL[n]) + cL), torch.max(jabs(PR[n]) + cR))
         FL = fluxes_xi(PL, UL, axis)
         FR = fluxes_xi(PR, UR, axis)
         return 0.5 * (FL + FR) - 0.5 * alpha * (UR - UL)

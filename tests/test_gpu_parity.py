@@ -93,6 +93,19 @@ RHS_CASES = [
     ("tgv-3d-charcons-roe-viscous", dict(cells=(12, 16, 14), bc="PERIODIC", nh=4, recon_var="CHAR-CONSERVATIVE",
                                          frozen_state="ROE", viscous=True, heat=True, mu=1e-2, prandtl=0.71,
                                          ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    # Lax-Friedrichs: one dissipation speed per axis, the maximum over every face
+    ("sod-lax-friedrichs", dict(cells=(200, 1, 1), bc=ZG, riemann="LAX-FRIEDRICHS"), "sod"),
+    ("quad-2d-teno5-lax-friedrichs", dict(cells=(44, 40, 1), bc=ZG, recon="TENO5", riemann="LAX-FRIEDRICHS"),
+     "quad"),
+    ("tgv-3d-char-roe-lax-friedrichs", dict(cells=(20, 16, 24), bc="PERIODIC", recon_var="CHAR-PRIMITIVE",
+                                            frozen_state="ROE", riemann="LAX-FRIEDRICHS",
+                                            ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("tgv-3d-charcons-lax-friedrichs-viscous", dict(cells=(12, 16, 14), bc="PERIODIC", nh=4,
+                                                    recon_var="CHAR-CONSERVATIVE", riemann="LAX-FRIEDRICHS",
+                                                    viscous=True, heat=True, mu=1e-2, prandtl=0.71,
+                                                    ranges=((0, 2 * math.pi),) * 3), "tgv"),
+    ("quad-2d-lax-friedrichs-limiter", dict(cells=(40, 36, 1), bc=ZG, riemann="LAX-FRIEDRICHS",
+                                            interpolation_limiter=True, recon_var="CONSERVATIVE"), "quad"),
     # TENO5 (its sharp cutoff drops stencils across the discontinuities)
     ("sod-teno5-hllc", dict(cells=(200, 1, 1), bc=ZG, recon="TENO5"), "sod"),
     ("quad-2d-teno5-rusanov", dict(cells=(48, 40, 1), bc=ZG, recon="TENO5", riemann="RUSANOV"), "quad"),
@@ -204,7 +217,10 @@ def test_steps_match_oracle(fused):
              ((40, 36, 1), ZG, "quad", {"recon": "WENO3-Z", "riemann": "HLL", "signal_speed": "DAVIS"}),
              ((44, 40, 1), ZG, "quad", {"recon": "TENO5"}),
              ((40, 44, 1), ZG, "quad", {"recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE"}),
-             ((44, 40, 1), ZG, "quad", {"recon_var": "CONSERVATIVE", "riemann": "HLL"})]
+             ((44, 40, 1), ZG, "quad", {"recon_var": "CONSERVATIVE", "riemann": "HLL"}),
+             ((40, 36, 1), ZG, "quad", {"riemann": "LAX-FRIEDRICHS"}),
+             ((12, 16, 14), "PERIODIC", "tgv", {"ranges": ((0, 2 * math.pi),) * 3, "nh": 4,
+                                                "riemann": "LAX-FRIEDRICHS", "viscous": True, "mu": 1e-2})]
     for cells, bc, kind, kw in cases:
         oc, cc = both(cells, bc, **kw)
         U, P = O.initialize(_prims_for(kind, cells), oc)
