@@ -86,3 +86,34 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     assert lib.gbf_create(ctypes.byref(bad), None, ctypes.byref(out)) == _lib.GBF_ERR_INVALID_ARGUMENT
     assert out.value is None
     assert lib.gbf_destroy(None) == _lib.GBF_OK
+
+
+@pytest.mark.parametrize("kw,has_adjoint", [
+    (dict(), True),
+    (dict(recon="TENO5"), True),
+    (dict(riemann="LAX-FRIEDRICHS"), False),
+    (dict(recon_var="CONSERVATIVE"), False),
+    (dict(recon_var="CHAR-CONSERVATIVE", frozen_state="ROE"), False),
+    (dict(recon_var="CHAR-PRIMITIVE", interpolation_limiter=True), False),
+    (dict(interpolation_limiter=True), True),
+    (dict(nh=4, viscous=True, mu=0.01, convective=False), True),
+])
+def test_adjoint_coverage_is_reported_without_a_device(lib, kw, has_adjoint):
+    """gbf_vjp_workspace_bytes is 0 exactly for the setups without an adjoint."""
+    c = _case(**kw)
+    assert lib.gbf_case_check(ctypes.byref(c)) == _lib.GBF_OK
+    assert (lib.gbf_vjp_workspace_bytes(ctypes.byref(c)) > 0) == has_adjoint
+
+
+def test_conservative_reconstructions_need_the_conservatives(lib):
+    c = _case(recon_var="CONSERVATIVE")
+    buf = ctypes.c_void_p(8)
+    assert lib.gbf_rhs_cons(ctypes.byref(c), buf, None, buf, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_rhs_cons(ctypes.byref(c), buf, ctypes.c_void_p(12), buf, None, None) == _lib.GBF_ERR_ALIGNMENT
+    # the characteristic and conservative variables are built with WENO5-Z only
+    bad = _case(recon_var="CONSERVATIVE")
+    bad.recon = _lib.RECON["WENO5-JS"]
+    assert lib.gbf_case_check(ctypes.byref(bad)) == _lib.GBF_ERR_UNSUPPORTED
+    # gravity: the drop-in volume force validates before any device call
+    g = _case(gravity=(0.0, -1.0, 0.0))
+    assert lib.gbf_volume_force(ctypes.byref(g), None, buf, None) == _lib.GBF_ERR_INVALID_ARGUMENT
