@@ -132,6 +132,8 @@ class CaseConfig:
     gravity: Optional[Tuple[float, float, float]] = None
     # device copies of the boundary value fields, per device
     _fields: dict = field(default_factory=dict, init=False, repr=False, compare=False)
+    # boundary callables that vary in time, per face
+    _time_fns: dict = field(default_factory=dict, init=False, repr=False, compare=False)
 
     def __post_init__(self):
         self.cells = tuple(int(n) for n in self.cells)
@@ -213,18 +215,19 @@ class CaseConfig:
         xb, xc = np.meshgrid(self.cell_centers(b), self.cell_centers(c), indexing="ij")
         return [x.reshape(-1) for x, ax in ((xb, b), (xc, c)) if ax in self.active]
 
-    def _eval_on_face(self, face: str, fn, with_time: bool, what: str) -> np.ndarray:
+    def _eval_on_face(self, face: str, fn, with_time: bool, t: float = 0.0) -> np.ndarray:
         nt = self.face_cells(face)
         coords = self.boundary_coordinates(face)
         if not callable(fn):
             return np.full(nt, float(fn))
-        r0 = fn(*coords, 0.0) if with_time else fn(*coords)
-        out = np.broadcast_to(np.asarray(r0, dtype=np.float64 if with_time else bool), (nt,)).copy()
-        if with_time:
-            r1 = np.broadcast_to(np.asarray(fn(*coords, 1.0), dtype=np.float64), (nt,))
-            if not np.array_equal(out, r1):
-                raise NotImplementedError(f"{what}: boundary values varying in time")
-        return out
+        r = fn(*coords, t) if with_time else fn(*coords)
+        return np.broadcast_to(np.asarray(r, dtype=np.float64 if with_time else bool), (nt,)).copy()
+
+    def _varies_in_time(self, face: str, fn) -> bool:
+        if not callable(fn):
+            return False
+        v0 = self._eval_on_face(face, fn, True, 0.0)
+        return any(not np.array_equal(v0, self._eval_on_face(face, fn, True, t)) for t in (0.37, 1.0))
 
     def _face_values(self, face: str, btype: str, vals):
         """Values of a face's type: a tuple of constants, or an array
@@ -250,7 +253,10 @@ class CaseConfig:
         fns = [_callable(v, f"boundary at '{face}'") for v in vals]
         if not any(callable(fn) for fn in fns):
             return tuple(float(fn) for fn in fns)
-        return np.stack([self._eval_on_face(face, fn, True, f"boundary at '{face}'") for fn in fns])
+        if any(self._varies_in_time(face, fn) for fn in fns):
+            # re-evaluated at every halo update's time (refresh_bc_fields)
+            self._time_fns[face] = fns
+        return np.stack([self._eval_on_face(face, fn, True) for fn in fns])
 
     def _face_segments(self, face: str, spec):
         """A face of several types (bounding_domain masks, material.py:252-266):
@@ -267,9 +273,10 @@ class CaseConfig:
                 if m.shape != (self.face_cells(face),):
                     raise SetupError(f"bounding domain at '{face}': {m.shape} cells")
             else:
-                m = self._eval_on_face(face, _callable(mask, f"bounding domain at '{face}'"), False,
-                                       f"bounding domain at '{face}'")
+                m = self._eval_on_face(face, _callable(mask, f"bounding domain at '{face}'"), False)
             segs.append((btype, self._face_values(face, btype, vals), m))
+            if face in self._time_fns:
+                raise NotImplementedError(f"boundary values varying in time on a face of several types ('{face}')")
         cover = np.zeros(self.face_cells(face), dtype=bool)
         for _, _, m in segs:
             cover |= m
@@ -280,7 +287,7 @@ class CaseConfig:
     def face_is_mixed(self, face: str) -> bool:
         return isinstance(self.bc.get(face), list)
 
-    def face_fields(self, face: str):
+    def face_fields(self, face: str, values=None):
         """(values [5, nt] float64 or None, types [nt] int8 or None) of a face
         for gbf_case.bc_field_values / bc_field_types: per boundary cell the
         raw values laid out like bc_value, and for a face of several types the
@@ -308,10 +315,30 @@ class CaseConfig:
                 values[:, m] = rows(btype, vals)[:, m]
                 any_values |= vals is not None
             return (values if any_values else None), types
-        vals = self.bc_values.get(face)
+        vals = self.bc_values.get(face) if values is None else values
         if isinstance(vals, np.ndarray):
             return rows(self.bc[face], vals), None
         return None, None
+
+    @property
+    def time_varying_faces(self):
+        """Faces whose boundary values are functions of time (the drop-in
+        halo update re-evaluates them at its time; the fused path, which keeps
+        time on the device, rejects them)."""
+        return sorted(self._time_fns)
+
+    def bc_values_at(self, face: str, t: float) -> np.ndarray:
+        """The values [k, boundary cells] of a time-varying face at time t."""
+        return np.stack([self._eval_on_face(face, fn, True, t) for fn in self._time_fns[face]])
+
+    def refresh_bc_fields(self, t: float) -> None:
+        """Boundary values at time t into the device fields (stream-ordered
+        copies on the current stream), for every time-varying face."""
+        import torch
+        for d in self._fields.values():
+            for face in self._time_fns:
+                vals, _ = self.face_fields(face, self.bc_values_at(face, t))
+                d[face][0].copy_(torch.from_numpy(vals))
 
     @property
     def has_bc_fields(self) -> bool:

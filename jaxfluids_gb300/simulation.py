@@ -59,18 +59,25 @@ class SimulationManager:
     def compute_time_step_size(self, primitives: torch.Tensor) -> torch.Tensor:
         return self.time_step_size(primitives)
 
+    # RK3.timestep_increment_factor (RK3.py:28): the halos after stage k are
+    # filled at t + dt * factor[k] (simulation_manager.py:855-857)
+    STAGE_TIME_FACTORS = (1.0, 0.5, 1.0)
+
     def do_integration_step(self, conservatives: torch.Tensor, primitives: torch.Tensor,
                             dt: torch.Tensor, t: float = 0.0):
         """One TVD-RK3 step through the drop-in kernels (do_runge_kutta_stages)."""
         init = conservatives
         cons, prims = conservatives, primitives
+        # host time of the stage halos: only boundary values varying in time read it
+        dt_host = float(dt) if self.config.time_varying_faces else 0.0
         for stage in range(3):
             (rhs_buf, _, _) = self.space_solver.compute_rhs(cons, prims, None, t, dt)
             rhs = rhs_buf.euler_buffers.conservatives
             cons = self.time_integrator.perform_stage_integration(
                 cons, rhs, init if stage > 0 else None, dt, stage)
             prims = self.equation_manager.get_primitives_from_conservatives(cons)
-            prims, cons = self.halo_manager.perform_halo_update_material(prims, t, False, False, cons)
+            t_stage = t + dt_host * self.STAGE_TIME_FACTORS[stage]
+            prims, cons = self.halo_manager.perform_halo_update_material(prims, t_stage, False, False, cons)
         return cons, prims
 
     def simulate(self, conservatives, primitives, end_time: float = math.inf,
@@ -94,6 +101,9 @@ class FusedRK3:
     """Fused TVD-RK3 stepping of interior conservatives (gbf_rk3_advance)."""
 
     def __init__(self, config: CaseConfig, device="cuda", tile: Optional[_lib.GbfTile] = None):
+        if config.time_varying_faces:
+            raise NotImplementedError("boundary values varying in time need the host time of every stage: "
+                                      "use SimulationManager (the fused path keeps time on the device)")
         self.config = config
         self.lib = _lib.load()
         self.case = config.to_c()

@@ -97,8 +97,11 @@ class HaloManager(_Base):
     def perform_halo_update_material(self, primitives: torch.Tensor, physical_simulation_time: float = 0.0,
                                      fill_edge_halos: bool = False, fill_vertex_halos: bool = False,
                                      conservatives: Optional[torch.Tensor] = None, **kwargs):
-        """Fills halos in place of copies of the inputs; returns (prims, cons) or prims."""
+        """Fills halos in place of copies of the inputs; returns (prims, cons) or prims.
+        Boundary values that vary in time are taken at physical_simulation_time."""
         shape = self.config.halo_shape()
+        if self.config.time_varying_faces:
+            self.config.refresh_bc_fields(float(physical_simulation_time))
         prims = primitives.clone()
         cons = conservatives.clone() if conservatives is not None else None
         _lib.check(self.lib.gbf_halo_fill(ctypes.byref(self.case), _ptr(prims, shape, "primitives"),

@@ -31,7 +31,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional, Tuple
+from typing import Callable, Dict, List, Optional, Tuple
 
 import torch
 
@@ -85,6 +85,9 @@ class OracleCase:
     limit_velocity: bool = False
     # forcings.gravity with active_physics.is_volume_force
     gravity: Optional[Tuple[float, float, float]] = None
+    # boundary values varying in time: face -> function of t giving the
+    # values [k, boundary cells] at t (replaces bc_values[face])
+    bc_time: Dict[str, Callable] = field(default_factory=dict)
 
     # ---- domain information (domain/domain_information.py:80-206) ----
     @property
@@ -957,7 +960,8 @@ def _face_halo(P: Tensor, case: OracleCase, face: str, btype: str, vals=None) ->
     return h
 
 
-def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tensor, Optional[Tensor]]:
+def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase,
+                t: float = 0.0) -> Tuple[Tensor, Optional[Tensor]]:
     """HaloManager.perform_halo_update_material, face halos (outer/material.py:94-287).
 
     Halo primitives follow each face's boundary rule; halo conservatives are
@@ -984,7 +988,9 @@ def halo_update(P: Tensor, U: Optional[Tensor], case: OracleCase) -> Tuple[Tenso
                 if U is not None:
                     U[fill] = U[fill] * (1 - m) + cons_from_prims(h, case.gamma) * m
             continue
-        h = _face_halo(P, case, face, case.bc[face])
+        # callables of time are evaluated at the halo update's time (material.py:740-798)
+        vals = case.bc_time[face](t) if face in case.bc_time else None
+        h = _face_halo(P, case, face, case.bc[face], vals)
         P[fill] = h
         if U is not None:
             U[fill] = cons_from_prims(h, case.gamma)
@@ -1081,14 +1087,18 @@ def rk3_stage_update(U: Tensor, Un: Tensor, rhs: Tensor, dt, stage: int, case: O
     return U
 
 
-def rk3_step(U: Tensor, P: Tensor, dt, case: OracleCase) -> Tuple[Tensor, Tensor]:
-    """One TVD-RK3 step (simulation_manager.py:670-1077)."""
+RK3_TIME_INCREMENT = (1.0, 0.5, 1.0)                 # RK3.py:28
+
+
+def rk3_step(U: Tensor, P: Tensor, dt, case: OracleCase, t: float = 0.0) -> Tuple[Tensor, Tensor]:
+    """One TVD-RK3 step (simulation_manager.py:670-1077); the halos after stage
+    k are filled at t + dt * timestep_increment_factor[k] (:855-857)."""
     Un = U
     for stage in range(3):
         rhs = compute_rhs(U, P, case)
         U = rk3_stage_update(U, Un, rhs, dt, stage, case)
         P = prims_from_cons(U, case.gamma)          # simulation_manager.py:943-944
-        P, U = halo_update(P, U, case)              # :961-970
+        P, U = halo_update(P, U, case, t + float(dt) * RK3_TIME_INCREMENT[stage])  # :961-970
     return U, P
 
 

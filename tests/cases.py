@@ -25,6 +25,7 @@ def both(cells, bc, **kw):
     # values CaseConfig evaluated at the boundary cells
     oc.bc = {f: cc.bc.get(f, oc.bc[f]) for f in O.FACES}
     oc.bc_values = dict(cc.bc_values)
+    oc.bc_time = {f: (lambda t, f=f: cc.bc_values_at(f, t)) for f in cc.time_varying_faces}
     return oc, cc
 
 

@@ -72,10 +72,24 @@ def test_callables_of_the_boundary_coordinates():
     assert _lib.load().gbf_case_check(c) == _lib.GBF_OK
 
 
-def test_time_varying_callables_are_rejected():
+def test_time_varying_callables():
+    """Callables of time are detected, evaluated at the halo update's time,
+    and rejected by the fused path (time lives on the device there)."""
     f = {"type": "DIRICHLET", "primitives_callable": {"rho": "lambda y, t: 1.0 + t * y", "u": 0.0, "v": 0.0,
                                                       "w": 0.0, "p": 1.0}}
     case, num = _setup({"west": f, "east": {"type": "ZEROGRADIENT"}, "north": {"type": "ZEROGRADIENT"},
+                        "south": {"type": "ZEROGRADIENT"}})
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.time_varying_faces == ["west"]
+    ny = cfg.cells[1]
+    y = (np.arange(ny) + 0.5) / ny
+    np.testing.assert_array_equal(cfg.bc_values_at("west", 0.25)[0], 1.0 + 0.25 * y)
+    np.testing.assert_array_equal(cfg.bc_values["west"][0], np.ones(ny))  # t = 0
+    from jaxfluids_gb300 import FusedRK3
+    with pytest.raises(NotImplementedError, match="time"):
+        FusedRK3(cfg, device="cpu")
+    mixed = [dict(f, bounding_domain="lambda y: y < 0.5"), {"type": "SYMMETRY", "bounding_domain": "lambda y: y >= 0.5"}]
+    case, num = _setup({"west": mixed, "east": {"type": "ZEROGRADIENT"}, "north": {"type": "ZEROGRADIENT"},
                         "south": {"type": "ZEROGRADIENT"}})
     with pytest.raises(NotImplementedError, match="time"):
         CaseConfig.from_setups(case, num)

@@ -271,3 +271,28 @@ def test_bc_step_vjp_matches_oracle_autograd(name):
     adj = AdjointRK3(cc, dt=dt)
     g = adj.step_vjp(Ui.cuda().contiguous(), lam.cuda().contiguous())
     assert rel_err(g, x.grad) <= 1e-11
+
+
+def test_time_varying_boundary_values_drop_in_steps():
+    """DIRICHLET and WALL values that are functions of time, filled at each
+    stage's time t + dt (1, 1/2, 1) (simulation_manager.py:855-857), through
+    the drop-in stage loop; 4 steps against the oracle."""
+    from jaxfluids_gb300 import SimulationManager
+    cells = (32, 28, 1)
+    bc = _faces(x=("DIRICHLET", "ZEROGRADIENT"), y=("WALL", "WALL"))
+    vals = {"west": (1.2, "lambda y,t: 0.3 + 2.0 * t * y", 0.0, 0.0, "lambda y,t: 1.1 + 5.0 * t"),
+            "south": (0.0, 0.0, 0.0), "north": ("lambda x,t: 0.4 * jnp.sin(20.0 * t) * x", 0.0, 0.0)}
+    oc, cc = both(cells, bc, bc_values=vals, nh=4, viscous=True, heat=True, mu=0.02, prandtl=0.71)
+    assert cc.time_varying_faces == ["north", "west"]
+    U, P = O.initialize(_prims("quad", cells), oc)
+    sim = SimulationManager(cc)
+    Ug, Pg = sim.initialize(_prims("quad", cells).cuda())
+    assert torch.equal(Pg.cpu(), P)
+    t = 0.0
+    for _ in range(4):
+        dt = O.compute_dt(P, oc)
+        U, P = O.rk3_step(U, P, dt, oc, t)
+        Ug, Pg = sim.do_integration_step(Ug, Pg, dt.cuda(), t)
+        t += float(dt)
+    assert rel_err(Ug[oc.interior()], U[oc.interior()]) <= STEP_TOL
+    assert torch.equal(Pg.cpu()[oc.interior()], P[oc.interior()])
