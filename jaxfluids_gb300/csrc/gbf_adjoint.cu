@@ -141,7 +141,9 @@ __device__ __noinline__ void scatter_halo_cotangent(const SweepParams& p, int g0
   face_halo_transpose(p, a, gb, h, dP);
 }
 
-template <int AX>
+// C4: CENTRAL4 stencils fixed at compile time (the default setups), else the
+// per-case stencils of p.diss_*.
+template <int AX, bool C4>
 __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams vp) {
   const SweepParams& p = vp.sp;
   const long long nf = face_count<AX>(p);
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
     if (p.heat_production) {
       // tau and the face velocity of the forward (energy flux sum_k tau_k vf_k)
       double gr[3][3];
-      face_velocity_gradient<AX>(p, cell, gr);
+      face_velocity_gradient<AX, C4>(p, cell, gr);
       double tau[3], tr = 0.0;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(256) visc_face_vjp_kernel(const ViscVjpParams 
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         if (!(p.active_mask & (1 << k))) continue;
-        const double vf = face_interp_along<AX>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
+        const double vf = face_interp_along<AX, C4>(p, [&](int kax) { return cell(1 + k, kax, AX, 0); });
         dtau[k] += dvt * vf;
         out[7 + k] = dvt * tau[k];
       }
@@ -227,6 +229,25 @@ __device__ __constant__ double kCd[2][4] = {{1.0 / 12.0, -8.0 / 12.0, 8.0 / 12.0
                                             {0.0, -0.5, 0.5, 0.0}};
 __device__ __constant__ int kCj[4] = {-2, -1, 1, 2};
 
+// Stencil weight k of the face derivative, face interpolation and centre
+// derivative: CENTRAL4 as immediates when C4, else the case's row of the tables.
+template <bool C4>
+__device__ __forceinline__ double w_fd(const SweepParams& p, int k) {
+  if (C4) return (k == 0) ? 1.0 / 24.0 : (k == 1) ? -27.0 / 24.0 : (k == 2) ? 27.0 / 24.0 : -1.0 / 24.0;
+  return kFd[p.diss_face][k];
+}
+template <bool C4>
+__device__ __forceinline__ double w_fi(const SweepParams& p, int k) {
+  if (C4) return (k == 0 || k == 3) ? -1.0 / 16.0 : 9.0 / 16.0;
+  return kFi[p.diss_recon][k];
+}
+template <bool C4>
+__device__ __forceinline__ double w_cd(const SweepParams& p, int k) {
+  if (C4) return (k == 0) ? 1.0 / 12.0 : (k == 1) ? -8.0 / 12.0 : (k == 2) ? 8.0 / 12.0 : -1.0 / 12.0;
+  return kCd[p.diss_center][k];
+}
+
+template <bool C4>
 __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpParams vp) {
   const SweepParams& p = vp.sp;
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
@@ -234,9 +255,6 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
   if (i >= cs) return;
   const int c[3] = {(int)(i / ((long long)p.n[2] * p.n[1])), (int)((i / p.n[2]) % p.n[1]), (int)(i % p.n[2])};
   double du[3] = {0.0, 0.0, 0.0}, dT = 0.0;
-  const double* Fd = kFd[p.diss_face];
-  const double* Fi = kFi[p.diss_recon];
-  const double* Cd = kCd[p.diss_center];
 #pragma unroll
   for (int AX = 0; AX < 3; ++AX) {
     if (!(p.active_mask & (1 << AX))) continue;
@@ -251,13 +269,13 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
       q[AX] -= k - 2;
       if (q[AX] < 0 || q[AX] > p.n[AX]) continue;
       const long long f = ((long long)q[0] * e1 + q[1]) * e2 + q[2];
-      const double wd = odx * Fd[k];
-      if (wd != 0.0 || Fi[k] != 0.0) {
+      const double wd = odx * w_fd<C4>(p, k);
+      if (wd != 0.0 || w_fi<C4>(p, k) != 0.0) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * nf + f] + Fi[k] * fc[(7 + a) * nf + f];
+        for (int a = 0; a < 3; ++a) du[a] += wd * fc[a * nf + f] + w_fi<C4>(p, k) * fc[(7 + a) * nf + f];
         dT += wd * fc[10 * nf + f];
       }
-      if (Fi[k] == 0.0) continue;
+      if (w_fi<C4>(p, k) == 0.0) continue;
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         const int ii = (AX == 0) ? 1 + t : ((AX == 1) ? 2 * t : t);
@@ -265,12 +283,12 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
         const double odi = p.one_dx[ii];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          if (Cd[jj] == 0.0) continue;
+          if (w_cd<C4>(p, jj) == 0.0) continue;
           int h[3] = {q[0], q[1], q[2]};
           h[ii] -= kCj[jj];
           if (h[ii] < 0 || h[ii] >= p.n[ii]) continue;
           const long long ff = ((long long)h[0] * e1 + h[1]) * e2 + h[2];
-          const double wt = Fi[k] * odi * Cd[jj];
+          const double wt = w_fi<C4>(p, k) * odi * w_cd<C4>(p, jj);
           du[AX] += wt * fc[(3 + 2 * t) * nf + ff];
           du[ii] += wt * fc[(4 + 2 * t) * nf + ff];
         }
@@ -289,7 +307,7 @@ __global__ void __launch_bounds__(256) visc_cell_gather_kernel(const ViscVjpPara
 }
 
 // Pass 3: the stencil cells of face q (axis AX) that lie outside the domain.
-template <int AX>
+template <int AX, bool C4>
 __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpParams vp) {
   const SweepParams& p = vp.sp;
   const long long nf = face_count<AX>(p);
@@ -310,20 +328,18 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
 #pragma unroll
   for (int k = 0; k < VISC_SLOTS; ++k) s[k] = fc[k * nf + i];
   const double odx = p.one_dx[AX];
-  const double* Fd = kFd[p.diss_face];
-  const double* Fi = kFi[p.diss_recon];
-  const double* Cd = kCd[p.diss_center];
+#pragma unroll
   for (int k = 0; k < 4; ++k) {
-    if (Fd[k] == 0.0 && Fi[k] == 0.0) continue;
+    if (w_fd<C4>(p, k) == 0.0 && w_fi<C4>(p, k) == 0.0) continue;
     int g[3] = {q[0], q[1], q[2]};
     g[AX] += k - 2;
     if (g[AX] < 0 || g[AX] >= p.n[AX]) {
       // normal stencil cell in the halo: velocity and temperature cotangents
-      const double wd = odx * Fd[k];
+      const double wd = odx * w_fd<C4>(p, k);
       double d[5];
-      d[1] = wd * s[0] + Fi[k] * s[7];
-      d[2] = wd * s[1] + Fi[k] * s[8];
-      d[3] = wd * s[2] + Fi[k] * s[9];
+      d[1] = wd * s[0] + w_fi<C4>(p, k) * s[7];
+      d[2] = wd * s[1] + w_fi<C4>(p, k) * s[8];
+      d[3] = wd * s[2] + w_fi<C4>(p, k) * s[9];
       const double dT = wd * s[10];
       const double rho = global_prim<MODE_STAGE_P>(p, 0, g[0], g[1], g[2]);
       const double pr = global_prim<MODE_STAGE_P>(p, 4, g[0], g[1], g[2]);
@@ -332,17 +348,17 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
       d[4] = dT * iden;
       scatter_halo_cotangent(p, g[0], g[1], g[2], d[0], d[1], d[2], d[3], d[4], vp.dP);
     }
-    if (!p.viscous || Fi[k] == 0.0) continue;
+    if (!p.viscous || w_fi<C4>(p, k) == 0.0) continue;
     for (int t = 0; t < 2; ++t) {
       const int ii = tangential<AX>(t);
       if (!(p.active_mask & (1 << ii))) continue;
       const double odi = p.one_dx[ii];
       for (int jj = 0; jj < 4; ++jj) {
-        if (Cd[jj] == 0.0) continue;
+        if (w_cd<C4>(p, jj) == 0.0) continue;
         int h[3] = {g[0], g[1], g[2]};
         h[ii] += kCj[jj];
         if (cell_inside(p, h)) continue;
-        const double wt = Fi[k] * odi * Cd[jj];
+        const double wt = w_fi<C4>(p, k) * odi * w_cd<C4>(p, jj);
         double d[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         d[1 + AX] = wt * s[3 + 2 * t];
         d[1 + ii] = wt * s[4 + 2 * t];
@@ -350,6 +366,19 @@ __global__ void __launch_bounds__(256) visc_halo_scatter_kernel(const ViscVjpPar
       }
     }
   }
+}
+
+// The three passes of the dissipative-flux reverse.
+template <bool C4>
+void launch_visc_vjp(const ViscVjpParams& q, const long long nface[3], long long cells, cudaStream_t s) {
+  auto blocks = [](long long n) { return (unsigned)((n + 255) / 256); };
+  if (nface[0]) visc_face_vjp_kernel<0, C4><<<blocks(nface[0]), 256, 0, s>>>(q);
+  if (nface[1]) visc_face_vjp_kernel<1, C4><<<blocks(nface[1]), 256, 0, s>>>(q);
+  if (nface[2]) visc_face_vjp_kernel<2, C4><<<blocks(nface[2]), 256, 0, s>>>(q);
+  visc_cell_gather_kernel<C4><<<blocks(cells), 256, 0, s>>>(q);
+  if (nface[0]) visc_halo_scatter_kernel<0, C4><<<blocks(nface[0]), 256, 0, s>>>(q);
+  if (nface[1]) visc_halo_scatter_kernel<1, C4><<<blocks(nface[1]), 256, 0, s>>>(q);
+  if (nface[2]) visc_halo_scatter_kernel<2, C4><<<blocks(nface[2]), 256, 0, s>>>(q);
 }
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
@@ -504,14 +533,12 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
       off += VISC_SLOTS * nface[a];
     }
     if ((st = launch_convert(c, U, P, ci.cells, 1, s)) != GBF_OK) return st;
-    auto blocks = [](long long n) { return (unsigned)((n + 255) / 256); };
-    if (nface[0]) visc_face_vjp_kernel<0><<<blocks(nface[0]), 256, 0, s>>>(q);
-    if (nface[1]) visc_face_vjp_kernel<1><<<blocks(nface[1]), 256, 0, s>>>(q);
-    if (nface[2]) visc_face_vjp_kernel<2><<<blocks(nface[2]), 256, 0, s>>>(q);
-    visc_cell_gather_kernel<<<blocks(ci.cells), 256, 0, s>>>(q);
-    if (nface[0]) visc_halo_scatter_kernel<0><<<blocks(nface[0]), 256, 0, s>>>(q);
-    if (nface[1]) visc_halo_scatter_kernel<1><<<blocks(nface[1]), 256, 0, s>>>(q);
-    if (nface[2]) visc_halo_scatter_kernel<2><<<blocks(nface[2]), 256, 0, s>>>(q);
+    const bool c4 = c->dissipative_stencil[0] == GBF_CENTRAL4 && c->dissipative_stencil[1] == GBF_CENTRAL4 &&
+                    c->dissipative_stencil[2] == GBF_CENTRAL4;
+    if (c4)
+      launch_visc_vjp<true>(q, nface, ci.cells, s);
+    else
+      launch_visc_vjp<false>(q, nface, ci.cells, s);
     if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
   }
   const bool grav = (c->flags & GBF_FLAG_GRAVITY) != 0;
