@@ -4,16 +4,24 @@
 dictionaries ``jaxfluids.InputManager`` reads (input/input_manager.py:32-43)
 and keeps the keys the single-phase right-hand side uses:
 
-* case_setup: ``domain.{x,y,z}.{cells,range}``, ``boundary_conditions.<face>.type``,
+* case_setup: ``domain.{x,y,z}.{cells,range}``; ``boundary_conditions.<face>``
+  as one type or a list of types with ``bounding_domain`` masks, with
+  ``wall_velocity_callable`` / ``primitives_callable`` values (numbers, or
+  functions or "lambda" strings of the boundary coordinates and time,
+  input/case_setup/read_boundary_conditions.py:28-393);
   ``material_properties.equation_of_state.{model,specific_heat_ratio,specific_gas_constant}``,
   ``material_properties.transport.dynamic_viscosity`` / ``thermal_conductivity``;
+  ``forcings.gravity``;
 * numerical_setup: ``conservatives.halo_cells``,
   ``conservatives.time_integration.{integrator,CFL,fixed_timestep}``,
   ``conservatives.convective_fluxes.{convective_solver,godunov.{riemann_solver,
   signal_speed,reconstruction_stencil,reconstruction_variable,frozen_state}}``
   (input/numerical_setup/read_conservatives.py:55-203),
-  ``conservatives.dissipative_fluxes.*`` (:374-445) and ``active_physics.*``
-  (data_types/numerical_setup/active_physics.py:3-13).
+  ``conservatives.dissipative_fluxes.*`` (:374-445),
+  ``conservatives.positivity.{is_interpolation_limiter,limit_velocity,flux_limiter}``
+  (read_positivity.py), ``active_physics.*``
+  (data_types/numerical_setup/active_physics.py:3-13), ``active_forcings.*``
+  and ``precision.*``.
 
 Setups the CUDA path does not implement are rejected here, at construction,
 the way the reference rejects invalid setups with assertions; nothing is
