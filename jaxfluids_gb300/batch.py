@@ -64,8 +64,12 @@ class BatchedRK3:
                     raise ValueError(f"all cases of a batch share the scheme; '{k}' differs")
             if c.active != c0.active or c.bc != c0.bc:
                 raise ValueError("all cases of a batch share active axes and boundary types")
-        if c0.viscous or c0.heat:
+        if c0.viscous or c0.heat or not c0.convective:
             raise NotImplementedError("the batched path is built for inviscid cases")
+        if c0.riemann == "LAX-FRIEDRICHS" or c0.recon_var in ("CONSERVATIVE", "CHAR-CONSERVATIVE"):
+            raise NotImplementedError(f"the batched path does not build {c0.riemann} / {c0.recon_var}")
+        if c0.interpolation_limiter or c0.gravity is not None or any(c.has_bc_fields for c in configs):
+            raise NotImplementedError("the batched path has no limiter, gravity or boundary value fields")
         self.configs = configs
         self.lib = _lib.load()
         self.device = torch.device(device)

@@ -68,7 +68,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
 
     # the instantiation units of the large kernels start first, so that the
     # small units fill in beside them
-    heavy = ("visc", "char", "vjp", "weno")
+    heavy = ("visc", "char", "vjp", "weno", "batch")
     order = sorted(srcs, key=lambda p: (not any(h in os.path.basename(p) for h in heavy), p))
     with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1, len(srcs)))) as ex:
         results = list(ex.map(compile_one, order))

@@ -9,55 +9,11 @@
 #include <algorithm>
 #include <vector>
 
-#include "gbf_kernels.cuh"
+#include "gbf_batch.cuh"
 
 namespace gbf {
 
 namespace {
-
-constexpr int kMaxCellsPerThread = 4;
-
-struct BatchParams {
-  SweepParams base;            // scheme and tile shape (sizes are per case)
-  const gbf_batch_case* cases;
-  const int32_t* worklist;
-  int ntiles;
-  int stage;
-  const double* cons;          // stage input (packed)
-  const double* cons0;         // step state U^n (packed)
-  double* out;                 // stage output (packed)
-  double* dt_states;           // 4 per case
-  int reduce_dt;
-};
-
-__device__ __forceinline__ void case_params(const BatchParams& bp, int c, SweepParams& p) {
-  p = bp.base;
-  const gbf_batch_case& cs = bp.cases[c];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    p.n[a] = cs.n[a];
-    p.tiles[a] = cs.tiles[a];
-    p.one_dx[a] = 1.0 / cs.dx[a];
-  }
-  p.cons = bp.cons + cs.offset;
-  p.cons0 = bp.cons0 + cs.offset;
-  p.out = bp.out + cs.offset;
-  p.dt_state = bp.dt_states + 4 * c;
-  p.stage = bp.stage;
-  p.reduce_dt = bp.reduce_dt;
-}
-
-template <int RECON, int RIEMANN>
-__global__ void __launch_bounds__(256) batch_sweep_kernel(const BatchParams bp) {
-  extern __shared__ double smem[];
-  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
-    const int c = bp.worklist[2 * item];
-    const int tile = bp.worklist[2 * item + 1];
-    SweepParams p;
-    case_params(bp, c, p);
-    sweep_tile<RECON, RIEMANN, MODE_STAGE, kMaxCellsPerThread, 0>(p, tile, smem);
-  }
-}
 
 // Per-case maximum signal speed and minimum density of the packed states
 // (time_step_size.py:96-109), one tile per work item.
@@ -141,30 +97,26 @@ __global__ void batch_slot_init_kernel(double* dt_states, int ncases) {
 int launch_batch_sweep(const gbf_case* c, const BatchParams& bp, int threads, size_t smem, int ctas,
                        cudaStream_t s) {
   const int grid = std::max(1, std::min(ctas, bp.ntiles));
-#define GBF_LAUNCH(RC, RM)                                                                          \
-  {                                                                                                 \
-    auto k = batch_sweep_kernel<RC, RM>;                                                            \
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=          \
-        cudaSuccess)                                                                                \
-      return GBF_ERR_CUDA;                                                                          \
-    k<<<grid, threads, smem, s>>>(bp);                                                              \
-    return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;                               \
-  }
-  // the batched kernels are built for WENO5-Z / MUSCL with HLLC or Rusanov
-  if (c->riemann == GBF_RIEMANN_HLL || c->recon > GBF_RECON_MINMOD_AD) return GBF_ERR_UNSUPPORTED;
+  // WENO5-Z / MUSCL / CHAR-ROE with HLLC or Rusanov here, the other inviscid
+  // schemes in gbf_batch_schemes.cu
+  const bool here = (c->riemann == GBF_RIEMANN_HLLC || c->riemann == GBF_RIEMANN_RUSANOV) &&
+                    (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE || c->recon <= GBF_RECON_MINMOD_AD);
+  if (!here) return launch_batch_sweep_schemes(c, bp, grid, threads, smem, s);
   const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
-  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE) {
-    if (hllc) GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC) else GBF_LAUNCH(RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV)
-  }
+  if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+    return hllc ? launch_batch_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                : launch_batch_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
   switch (c->recon) {
     case GBF_RECON_WENO5Z:
-      if (hllc) GBF_LAUNCH(GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV)
+      return hllc ? launch_batch_one<GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_one<GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
     case GBF_RECON_MINMOD:
-      if (hllc) GBF_LAUNCH(GBF_RECON_MINMOD, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV)
+      return hllc ? launch_batch_one<GBF_RECON_MINMOD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_one<GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
     default:
-      if (hllc) GBF_LAUNCH(GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC) else GBF_LAUNCH(GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV)
+      return hllc ? launch_batch_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
   }
-#undef GBF_LAUNCH
 }
 
 // Scheme checks shared by init and advance; fills the base params from a
@@ -175,9 +127,9 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
   if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
   if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_GRAVITY))
     return GBF_ERR_UNSUPPORTED;
-  if (scheme->riemann == GBF_RIEMANN_HLL || scheme->riemann == GBF_RIEMANN_LAXFRIEDRICHS ||
-      scheme->recon > GBF_RECON_MINMOD_AD ||
-      scheme->recon_var > GBF_RECVAR_CHAR_PRIMITIVE)
+  // every inviscid PRIMITIVE and CHAR-PRIMITIVE scheme but Lax-Friedrichs, whose
+  // global speed pass is per case
+  if (scheme->riemann == GBF_RIEMANN_LAXFRIEDRICHS || scheme->recon_var > GBF_RECVAR_CHAR_PRIMITIVE)
     return GBF_ERR_UNSUPPORTED;
   for (int f = 0; f < 6; ++f)  // boundary value fields are per case size: not batched
     if (scheme->bc_field_values[f] || scheme->bc_field_types[f] || scheme->bc[f] == GBF_BC_MIXED)

@@ -21,9 +21,9 @@ def test_worklist_layout_covers_every_tile_once():
     assert wl[0][0] == 2  # largest case first
 
 
-def _configs(sides):
+def _configs(sides, **kw):
     from jaxfluids_gb300 import CaseConfig
-    return [CaseConfig(cells=(a, b, 1), bc={f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")})
+    return [CaseConfig(cells=(a, b, 1), bc={f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")}, **kw)
             for a, b in sides]
 
 
@@ -37,11 +37,17 @@ def _cons(cfg, seed):
 SIDES = [(16, 16), (48, 48), (24, 40), (32, 32), (40, 24), (64, 64)]
 
 
+SCHEMES = [dict(), dict(recon="WENO5-JS", riemann="HLL"), dict(recon="TENO5", riemann="RUSANOV"),
+           dict(recon="WENO3-Z"), dict(recon="WENO3-JS", riemann="HLL"), dict(riemann="HLL", signal_speed="DAVIS"),
+           dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE", riemann="HLL"), dict(recon="MINMOD-AD", riemann="HLL")]
+
+
 @pytest.mark.gpu
-def test_batched_steps_equal_single_case_steps():
+@pytest.mark.parametrize("kw", SCHEMES, ids=["-".join(str(v) for v in s.values()) or "weno5z-hllc" for s in SCHEMES])
+def test_batched_steps_equal_single_case_steps(kw):
     from jaxfluids_gb300 import BatchedRK3, FusedRK3, build
     build.build()
-    cfgs = _configs(SIDES)
+    cfgs = _configs(SIDES, **kw)
     states = [_cons(c, 100 + i) for i, c in enumerate(cfgs)]
     batch = BatchedRK3(cfgs)
     batch.set_states([s.cuda() for s in states])
