@@ -383,9 +383,11 @@ void launch_visc_vjp(const ViscVjpParams& q, const long long nface[3], long long
 
 // out = (dP/dU)^T dP per cell, dP is cleared for the next use.
 // With gravity (g non-null) the transpose of add_gravity joins: d rho += g . w[1:4],
-// d m_j += g_j w[4], w the right-hand side's cotangent.
+// d m_j += g_j w[4], w the right-hand side's cotangent.  dU (non-null: the
+// CONSERVATIVE reconstruction) adds the cotangent that reached the state's
+// conservatives directly, and is cleared.
 __global__ void dp_to_du_kernel(const double* U, double* dP, double* out, long long n, double gm1,
-                                const double* w, double g0, double g1, double g2) {
+                                const double* w, double g0, double g1, double g2, double* dU) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     double u[5], d[5], o[5] = {0, 0, 0, 0, 0};
@@ -402,6 +404,13 @@ __global__ void dp_to_du_kernel(const double* U, double* dP, double* out, long l
       o[1] += g0 * w4;
       o[2] += g1 * w4;
       o[3] += g2 * w4;
+    }
+    if (dU) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        o[v] += dU[v * n + i];
+        dU[v * n + i] = 0.0;
+      }
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + i] = o[v];
@@ -447,15 +456,14 @@ inline int grid_for(long long n) {
 int vjp_check(const gbf_case* c) {
   if (c->flags & GBF_FLAG_NO_CONVECTIVE) return GBF_OK;  // no convective scheme to reverse
   // the interpolation limiter is reversed on the PRIMITIVE paths
-  if ((c->flags & GBF_FLAG_INTERPOLATION_LIMITER) && c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+  if ((c->flags & GBF_FLAG_INTERPOLATION_LIMITER) && c->recon_var != GBF_RECVAR_PRIMITIVE)
     return GBF_ERR_UNSUPPORTED;
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // Lax-Friedrichs' global maximum and the conservative reconstructions have no reverse
+  // Lax-Friedrichs' global maximum and CHAR-CONSERVATIVE have no reverse
   if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS) return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE)
-    return GBF_ERR_UNSUPPORTED;
+  if (c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
@@ -468,7 +476,7 @@ inline bool vjp_dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VI
 // faces of axis a: N_a + 1 along a
 long long visc_faces(const CaseInfo& ci, int a) { return ci.cells / ci.n[a] * (ci.n[a] + 1); }
 
-long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
+long long vjp_visc_doubles(const gbf_case* c, const CaseInfo& ci) {
   if (!vjp_dissipative(c)) return 0;
   long long faces = 0;
   for (int a = 0; a < 3; ++a)
@@ -476,10 +484,26 @@ long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
   return 5 * ci.cells + VISC_SLOTS * faces;
 }
 
+// the CONSERVATIVE reconstruction's conservative cotangent follows the
+// dissipative part
+inline bool vjp_cons(const gbf_case* c) {
+  return c->recon_var == GBF_RECVAR_CONSERVATIVE && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+}
+
+long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
+  return vjp_visc_doubles(c, ci) + (vjp_cons(c) ? 5 * ci.cells : 0);
+}
+
 // VJP of the rhs at state U (interior): out = J(U)^T w.  dP: zeroed scratch of 5 n doubles
 // (left zeroed on return).
 int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const double* U,
                    const double* w, double* out, double* dP, double* extra, cudaStream_t s) {
+  // the CONSERVATIVE pencil carries primitives and conservatives: the 3-D
+  // default tile is one cell shorter (6 x 8 x 8) to stay within 227 KB of
+  // shared memory with the WENO5 gradient rows and face slots
+  gbf_tile cons_tile{{6, 8, 8}, 256};
+  const bool user_tile = tile && (tile->t[0] > 0 || tile->t[1] > 0 || tile->t[2] > 0);
+  if (vjp_cons(c) && !user_tile && ci.active_mask == 7) tile = &cons_tile;
   VjpParams vp;
   int threads;
   size_t smem;
@@ -500,14 +524,19 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     pmax = std::max(pmax, pv);
     fmax = std::max(fmax, fv);
   }
-  smem = (size_t)(5 * pmax + 10 * R * fmax + (R == 3 ? 25 * threads : 0)) * sizeof(double);
+  // (the CONSERVATIVE pencil stages the conservatives too)
+  smem = (size_t)((vjp_cons(c) ? 10 : 5) * pmax + 10 * R * fmax + (R == 3 ? 25 * threads : 0)) * sizeof(double);
   if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
   vp.sp.cons = U;
   vp.w = w;
   vp.dP = dP;
+  vp.dU = vjp_cons(c) ? extra + vjp_visc_doubles(c, ci) : nullptr;
+  if (vp.dU) zero_kernel<<<grid_for(5 * ci.cells), 256, 0, s>>>(vp.dU, 5 * ci.cells);
   const int grid = vp.sp.tiles[0] * vp.sp.tiles[1] * vp.sp.tiles[2];
   if (c->flags & GBF_FLAG_NO_CONVECTIVE)
     st = GBF_OK;  // dissipative fluxes only
+  else if (vjp_cons(c))
+    st = launch_vjp_cons(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
     st = launch_vjp_char(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
@@ -543,7 +572,7 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   }
   const bool grav = (c->flags & GBF_FLAG_GRAVITY) != 0;
   dp_to_du_kernel<<<grid_for(ci.cells), 256, 0, s>>>(U, dP, out, ci.cells, ci.fp.gm1, grav ? w : nullptr,
-                                                     c->gravity[0], c->gravity[1], c->gravity[2]);
+                                                     c->gravity[0], c->gravity[1], c->gravity[2], vp.dU);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 

@@ -1,0 +1,11 @@
+// Right-hand-side VJP kernels: WENO5-Z on the conservative variables
+// (reconstruction_variable CONSERVATIVE).
+#include "gbf_vjp_kernels.cuh"
+
+namespace gbf {
+
+int launch_vjp_cons(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s) {
+  return launch_vjp_riemann<RECON_WENO5Z_CONS>(riemann, vp, grid, threads, smem, s);
+}
+
+}  // namespace gbf

@@ -12,6 +12,7 @@ struct VjpParams {
   SweepParams sp;       // state U (sp.cons), sizes, tile, scheme
   const double* w;      // cotangent of the rhs, interior [5][N]
   double* dP;           // primitive cotangent accumulator, interior [5][N]
+  double* dU;           // conservative cotangent accumulator (CONSERVATIVE reconstruction), interior [5][N]
 };
 
 // CHAR-PRIMITIVE face (char_reconstruct of the forward): frozen state of the
@@ -142,13 +143,15 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
                                          double* sm_prim, double* sm_slot, double* sm_jr) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr int K = 2 * R;
+  // CONSERVATIVE: the stencils read the staged conservatives (pencil rows 5..9)
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS;
   const SweepParams& p = vp.sp;
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   int pe[3] = {ext[0], ext[1], ext[2]};
   pe[AX] += 2 * R;
   const int pvol = pe[0] * pe[1] * pe[2];
-  stage_pencil<AX, R, MODE_STAGE>(p, o, pe, pvol, sm_prim);
+  stage_pencil<AX, R, MODE_STAGE, CONS>(p, o, pe, pvol, sm_prim);
   __syncthreads();
 
   int fe[3] = {ext[0], ext[1], ext[2]};
@@ -182,7 +185,46 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     }
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
-    if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5) {
+    if constexpr (CONS) {
+      // high_order_godunov.py:282-296 reversed: WENO5-Z on the conservatives
+      // with its gradients, primitives of the face conservatives, Riemann VJP,
+      // then the face conservatives' cotangents through the stencil gradients
+      double UL[5], UR[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double wv[K], jl[5], jr[5];
+#pragma unroll
+        for (int k = 0; k < K; ++k) wv[k] = sm_prim[(5 + v) * pvol + base + k * pstride];
+        weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, UL[v], jl);
+        weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, UR[v], jr);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          sm_slot[(v * K + k) * fvol + f] = jl[k];
+          sm_jr[(v * 5 + k) * nthr + tid] = jr[k];
+        }
+      }
+      prims_from_cons(UL, PL, p.fp.gm1);
+      prims_from_cons(UR, PR, p.fp.gm1);
+      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+      double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
+      prims_from_cons_vjp(UL, dPL, p.fp.gm1, dUL);
+      prims_from_cons_vjp(UR, dPR, p.fp.gm1, dUR);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double gL = dUL[v], gR = dUR[v];
+        double jl[5], jr[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          jl[k] = sm_slot[(v * K + k) * fvol + f];
+          jr[k] = sm_jr[(v * 5 + k) * nthr + tid];
+        }
+        sm_slot[(v * K + 0) * fvol + f] = gL * jl[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) sm_slot[(v * K + k) * fvol + f] = gL * jl[k] + gR * jr[5 - k];
+        sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
+      }
+    } else if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5) {
       // one pass gives the face states and the stencil gradients; the left
       // gradient waits in the face's slots 0..4, the right one in this
       // thread's private rows, until the Riemann cotangents are known
@@ -298,7 +340,26 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     if (!any) continue;
     int g[3] = {o[0] + i0, o[1] + i1, o[2] + i2};
     g[AX] -= R;
-    if (g[AX] < 0 || g[AX] >= p.n[AX]) {
+    const bool halo = g[AX] < 0 || g[AX] >= p.n[AX];
+    if constexpr (CONS) {
+      if (!halo) {
+        // an interior cell's conservatives are the state itself
+        const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          if (d[v] != 0.0) atomicAdd(vp.dU + v * cs + off, d[v]);
+        continue;
+      }
+      // a halo cell's conservatives are those of its halo primitives
+      // (material.py:248-250): on to the primitives, then the face rule
+      double P[5], dPh[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+      for (int v = 0; v < 5; ++v) P[v] = sm_prim[v * pvol + i];
+      cons_from_prims_vjp(P, d, 1.0 / P[0], 1.0 / p.fp.gm1, dPh);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] = dPh[v];
+    }
+    if (halo) {
       // halo cell: transpose of the face rule (DIRICHLET halos are constants)
       const int t = face_type_at(p.bc, p.bf, 2 * AX + (g[AX] >= 0 ? 1 : 0), face_pos(p.n, AX, g));
       g[AX] = bc_src(g[AX], p.n[AX], t);
@@ -330,9 +391,10 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
     if (p.active_mask & (1 << a))
       pmax = max(pmax, (p.t[0] + (a == 0 ? 2 * R : 0)) * (p.t[1] + (a == 1 ? 2 * R : 0)) *
                            (p.t[2] + (a == 2 ? 2 * R : 0)));
-  // pencil primitives | per-thread right-stencil gradients (WENO only) | face slots
+  // pencil primitives (and conservatives) | per-thread right-stencil gradients
+  // (WENO only) | face slots
   double* sm_prim = smem;
-  double* sm_jr = smem + 5 * pmax;
+  double* sm_jr = smem + (RECON == RECON_WENO5Z_CONS ? 10 : 5) * pmax;
   double* sm_slot = sm_jr + (ReconTraits<RECON>::R == 3 ? 25 * blockDim.x : 0);
   if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
   if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
@@ -345,6 +407,7 @@ int launch_vjp_weno5(int recon, int riemann, const VjpParams& vp, int grid, int 
                      cudaStream_t s);
 int launch_vjp_char(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_teno5(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
+int launch_vjp_cons(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_short(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
                      cudaStream_t s);
 

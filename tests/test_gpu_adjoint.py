@@ -102,6 +102,10 @@ VJP_CASES = [
     ("3d-char-roe-hll", (16, 12, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
                                                    "riemann": "HLL"}, "generic"),
     ("sod-minmodad-hll", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "HLL"}, "sod"),
+    # CONSERVATIVE: WENO5-Z on the conservatives
+    ("2d-cons-hllc", (32, 28, 1), "PERIODIC", {"recon_var": "CONSERVATIVE"}, "generic"),
+    ("3d-cons-hll-zg", (12, 14, 10), "ZEROGRADIENT", {"recon_var": "CONSERVATIVE", "riemann": "HLL"}, "generic"),
+    ("1d-cons-rusanov", (60, 1, 1), "ZEROGRADIENT", {"recon_var": "CONSERVATIVE", "riemann": "RUSANOV"}, "generic"),
     # TENO5: the cutoff is piecewise constant; quadrant states make it cut
     ("2d-teno5-hllc-quad", (32, 28, 1), "ZEROGRADIENT", {"recon": "TENO5"}, "quad"),
     ("3d-teno5-rusanov-viscous", (12, 14, 10), "PERIODIC", {"nh": 4, "recon": "TENO5", "riemann": "RUSANOV",

@@ -237,8 +237,8 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     oc, cc = both(cells, bc, bc_values=vals, **kw)
     if cc.recon == "MINMOD":
         pytest.skip("the adjoint is built for MINMOD-AD, not MINMOD")
-    if cc.recon_var in ("CONSERVATIVE", "CHAR-CONSERVATIVE"):
-        pytest.skip("the conservative reconstructions have no adjoint")
+    if cc.recon_var == "CHAR-CONSERVATIVE":
+        pytest.skip("CHAR-CONSERVATIVE has no adjoint")
     # smooth random-phase fields: WENO-Z's derivative amplifies rounding by
     # up to 1/eps where stencils are flat, e.g. zero-gradient halos of a
     # piecewise-constant state, so the comparison uses fields with none
@@ -256,7 +256,7 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
                                   "2d-cavity-weno5js-viscous", "2d-couette-viscous-only",
                                   "3d-heat-viscous-only-c2", "2d-heat-equation-sine-dirichlet",
                                   "3d-viscous-mixed-wall-neumann-fields", "2d-rayleigh-taylor-gravity",
-                                  "3d-viscous-gravity-wall"])
+                                  "3d-viscous-gravity-wall", "3d-cons-viscous-wall"])
 def test_bc_step_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
