@@ -91,3 +91,13 @@ def test_autotune_keeps_the_state():
     assert res["best"] in [r[0] for r in res["results"]]
     assert torch.equal(batch.cons, before)
     assert batch.tile == res["best"][0]
+
+
+@pytest.mark.parametrize("kw", [dict(riemann="LAX-FRIEDRICHS"), dict(recon_var="CONSERVATIVE"),
+                                dict(interpolation_limiter=True), dict(gravity=(0.0, -1.0, 0.0)),
+                                dict(nh=4, viscous=True, mu=0.01)])
+def test_batch_rejects_setups_it_does_not_build(kw):
+    """Checked on the host before anything touches a device."""
+    from jaxfluids_gb300 import BatchedRK3
+    with pytest.raises(NotImplementedError):
+        BatchedRK3(_configs([(16, 16), (24, 24)], **kw), device="cpu")
