@@ -347,7 +347,9 @@ int gbf_rk3_stage_vjp(const gbf_case* c, int stage, const double* cons_k, const 
  * (gbf_batch_workspace_bytes).  Each stage is ONE persistent launch of `ctas`
  * CTAs (0 = 2 per SM) looping over the work list; one more launch per step
  * updates every case's dt.  No host synchronisation; graph-capturable.
- * `scheme` supplies everything but the sizes (n, dx are taken per case).
+ * `scheme` supplies everything but the sizes (n, dx are taken per case): any
+ * inviscid PRIMITIVE or CHAR-PRIMITIVE scheme but Lax-Friedrichs, without the
+ * limiter, gravity or boundary value fields (GBF_ERR_UNSUPPORTED otherwise).
  */
 typedef struct gbf_batch_case {
   int32_t n[3];          /* interior cells per axis */
