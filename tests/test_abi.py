@@ -93,3 +93,37 @@ def test_config_from_reference_setup_dicts():
         CaseConfig.from_setups(case, bad)
     with pytest.raises(NotImplementedError):
         CaseConfig.from_setups(case, {"conservatives": {"convective_fluxes": {"convective_solver": "FLUX-SPLITTING"}}})
+
+
+def test_ctypes_mirror_matches_the_c_layout(tmp_path):
+    """Every field of gbf_case / gbf_tile / gbf_batch_case sits at the offset
+    the C compiler gives it (the ctypes mirror in _lib.py is hand-written)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from jaxfluids_gb300 import _lib
+    from jaxfluids_gb300.batch import BATCH_CASE_DTYPE
+
+    def ctypes_layout(ct):
+        return ctypes.sizeof(ct), {f: getattr(ct, f).offset for f, _ in ct._fields_}
+    layouts = {"gbf_case": ctypes_layout(_lib.GbfCase), "gbf_tile": ctypes_layout(_lib.GbfTile),
+               "gbf_batch_case": (BATCH_CASE_DTYPE.itemsize,
+                                  {f: BATCH_CASE_DTYPE.fields[f][1] for f in BATCH_CASE_DTYPE.names})}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbfluids.h"', "int main(void) {"]
+    for cname, (_, offsets) in layouts.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname in offsets:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    for line in filter(None, out):
+        cname, field, value = line.split()
+        size, offsets = layouts[cname]
+        assert int(value) == (size if field == "sizeof" else offsets[field]), (cname, field)
