@@ -1,0 +1,145 @@
+/*
+ * Test infrastructure, not product code: a second CPU restatement, in plain C,
+ * of the single-phase right-hand side for WENO5-Z on primitive variables with
+ * HLLC and Einfeldt signal speeds, on a halo-filled primitive buffer.  It is
+ * written independently of the torch restatement in jf_oracle.py and follows
+ * the same reference operations in the same order, so the two must agree
+ * bitwise; the tests check that (tests/test_oracle_c.py).  Compile without
+ * contraction (-ffp-contract=off): the reference rounds every product.
+ *
+ *   reconstruction   stencils/reconstruction/shock_capturing/weno/weno5_z.py:24-58,
+ *                    weno5_base.py:24-51 (smoothness, polynomials, eps = 1e-30)
+ *   conversions      equation_manager.py:93-101, :164-171; ideal_gas.py:69-88
+ *   physical flux    equation_manager.py:237-252
+ *   HLLC             solvers/riemann_solvers/HLLC.py:41-126,
+ *                    signal_speeds.py:109-133 (Einfeldt), :159-199 (S*)
+ *   divergence       solvers/space_solver.py:266-314, :597-599
+ */
+#include <math.h>
+#include <stddef.h>
+
+static double weno5z(double u0, double u1, double u2, double u3, double u4, double eps) {
+  const double t0 = u0 - 2.0 * u1 + u2, t1 = u0 - 4.0 * u1 + 3.0 * u2;
+  const double t2 = u1 - 2.0 * u2 + u3, t3 = u1 - u3;
+  const double t4 = u2 - 2.0 * u3 + u4, t5 = 3.0 * u2 - 4.0 * u3 + u4;
+  const double b0 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double b1 = 13.0 / 12.0 * (t2 * t2) + 1.0 / 4.0 * (t3 * t3);
+  const double b2 = 13.0 / 12.0 * (t4 * t4) + 1.0 / 4.0 * (t5 * t5);
+  const double tau5 = fabs(b0 - b2);
+  const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
+  const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
+  const double a2 = 0.3 * (1.0 + tau5 / (b2 + eps));
+  const double one_a = 1.0 / (a0 + a1 + a2);
+  const double w0 = a0 * one_a, w1 = a1 * one_a, w2 = a2 * one_a;
+  const double p0 = 1.0 / 3.0 * u0 + -7.0 / 6.0 * u1 + 11.0 / 6.0 * u2;
+  const double p1 = -1.0 / 6.0 * u1 + 5.0 / 6.0 * u2 + 1.0 / 3.0 * u3;
+  const double p2 = 1.0 / 3.0 * u2 + 5.0 / 6.0 * u3 + -1.0 / 6.0 * u4;
+  return w0 * p0 + w1 * p1 + w2 * p2;
+}
+
+static void cons_from_prims(const double P[5], double U[5], double gamma) {
+  const double rho = P[0];
+  const double e = P[4] / (rho * (gamma - 1.0));
+  const double s = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
+  U[0] = rho;
+  U[1] = rho * P[1];
+  U[2] = rho * P[2];
+  U[3] = rho * P[3];
+  U[4] = rho * (0.5 * s + e);
+}
+
+static void physical_flux(const double P[5], const double U[5], int n, double F[5]) {
+  F[0] = U[n];
+  F[1] = U[n] * P[1];
+  F[2] = U[n] * P[2];
+  F[3] = U[n] * P[3];
+  F[4] = P[n] * (U[4] + P[4]);
+  F[n] = F[n] + P[4];
+}
+
+static void hllc_star_flux(const double P[5], const double U[5], double S, double Ss, int n, int left,
+                           double out[5]) {
+  const double pre = (S - P[n]) / (S - Ss) * P[0];
+  const double e_term = pre * (U[4] / U[0] + (Ss - P[n]) * (Ss + P[4] / P[0] / (S - P[n])));
+  double us[5] = {pre, pre, pre, pre, e_term};
+  for (int t = 1; t <= 3; ++t) us[t] = (t == n) ? us[t] * Ss : us[t] * P[t];
+  double F[5];
+  physical_flux(P, U, n, F);
+  const double wave = left ? fmin(S, 0.0) : fmax(S, 0.0);
+  for (int v = 0; v < 5; ++v) out[v] = F[v] + wave * (us[v] - U[v]);
+}
+
+static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double gamma, double F[5]) {
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, gamma);
+  cons_from_prims(PR, UR, gamma);
+  const double cL = sqrt(gamma * PL[4] / PL[0]);
+  const double cR = sqrt(gamma * PR[4] / PR[0]);
+  const double uL = PL[n], uR = PR[n];
+  const double sL = sqrt(PL[0]), sR = sqrt(PR[0]);
+  const double od = 1.0 / (sL + sR);
+  const double eta2 = 0.5 * sL * sR * od * od;
+  const double ubar = (sL * uL + sR * uR) * od;
+  const double du = uR - uL;
+  const double dbar = sqrt((sL * cL * cL + sR * cR * cR) * od + eta2 * (du * du));
+  const double SL = fmin(ubar - dbar, uL - cL);
+  const double SR = fmax(ubar + dbar, uR + cR);
+  const double rdL = PL[0] * (SL - uL);
+  const double rdR = PR[0] * (SR - uR);
+  const double Ss = ((PR[4] - PL[4]) + (uL * rdL - uR * rdR)) / (rdL - rdR);
+  double FL[5], FR[5];
+  hllc_star_flux(PL, UL, SL, Ss, n, 1, FL);
+  hllc_star_flux(PR, UR, SR, Ss, n, 0, FR);
+  const double sg = (Ss > 0.0) ? 1.0 : (Ss < 0.0) ? -1.0 : Ss;  /* sign, 0 and NaN kept */
+  for (int v = 0; v < 5; ++v) F[v] = 0.5 * (1.0 + sg) * FL[v] + 0.5 * (1.0 - sg) * FR[v];
+}
+
+/*
+ * rhs[5][n0][n1][n2] of the primitive halo buffer P[5][h0][h1][h2]
+ * (h_a = n_a + 2 nh on active axes, 1 on inactive ones), axes summed in order
+ * from the first active one.  Returns 0.
+ */
+int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one_dx[3], double gamma,
+                       double eps, double* rhs) {
+  int h[3], lo[3];
+  for (int a = 0; a < 3; ++a) {
+    h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
+    lo[a] = n[a] > 1 ? nh : 0;
+  }
+  const size_t hcs = (size_t)h[0] * h[1] * h[2];
+  const size_t cs = (size_t)n[0] * n[1] * n[2];
+  int first = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] <= 1) continue;
+    const size_t stride = (a == 0) ? (size_t)h[1] * h[2] : (a == 1) ? (size_t)h[2] : 1;
+    for (int i0 = 0; i0 < n[0]; ++i0)
+      for (int i1 = 0; i1 < n[1]; ++i1)
+        for (int i2 = 0; i2 < n[2]; ++i2) {
+          const int idx[3] = {i0, i1, i2};
+          /* fluxes of the faces left (f = c) and right (f = c + 1) of this cell */
+          double F[2][5];
+          for (int side = 0; side < 2; ++side) {
+            int g[3] = {idx[0] + lo[0], idx[1] + lo[1], idx[2] + lo[2]};
+            g[a] += side;  /* face between buffer cells g[a] - 1 and g[a] */
+            const size_t c0 = ((size_t)g[0] * h[1] + g[1]) * h[2] + g[2];
+            double PL[5], PR[5];
+            for (int v = 0; v < 5; ++v) {
+              const double* q = P + v * hcs + c0;
+              const double m3 = q[-3 * (ptrdiff_t)stride], m2 = q[-2 * (ptrdiff_t)stride];
+              const double m1 = q[-(ptrdiff_t)stride], z0 = q[0];
+              const double p1 = q[stride], p2 = q[2 * stride];
+              PL[v] = weno5z(m3, m2, m1, z0, p1, eps);
+              PR[v] = weno5z(p2, p1, z0, m1, m2, eps);
+            }
+            hllc_einfeldt(PL, PR, a + 1, gamma, F[side]);
+          }
+          const size_t o = ((size_t)i0 * n[1] + i1) * n[2] + i2;
+          for (int v = 0; v < 5; ++v) {
+            const double r = one_dx[a] * (F[0][v] - F[1][v]);
+            rhs[v * cs + o] = first ? r : rhs[v * cs + o] + r;
+          }
+        }
+    first = 0;
+  }
+  return 0;
+}
