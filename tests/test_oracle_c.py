@@ -4,8 +4,6 @@ speeds) against the torch oracle, on periodic, zero-gradient and symmetry
 halos in 1-D to 3-D.  Built here with the system C compiler, contraction off."""
 import ctypes
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
@@ -18,13 +16,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
-def crhs(tmp_path_factory):
-    cc = shutil.which("gcc") or shutil.which("cc")
-    if cc is None:
+def crhs():
+    import __graft_entry__
+    so = __graft_entry__.build_oracle_c()  # oracle/_build/jf_rhs.so, rebuilt when the source is newer
+    if not so:
         pytest.skip("no C compiler")
-    so = str(tmp_path_factory.mktemp("c") / "jf_rhs.so")
-    subprocess.run([cc, "-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                    os.path.join(ROOT, "oracle", "jf_rhs.c"), "-o", so, "-lm"], check=True)
     lib = ctypes.CDLL(so)
     f = lib.jf_rhs_weno5z_hllc
     f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
