@@ -33,9 +33,36 @@ import math
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional, Tuple
 
+import numpy as np
 import torch
 
 Tensor = torch.Tensor
+
+
+class _Sqrt(torch.autograd.Function):
+    """Correctly rounded square root with torch's own derivative.
+
+    jnp.sqrt (XLA), libm and CUDA's double sqrt round correctly; torch.sqrt
+    in float64 does not on every CPU build (an x86 build with MKL is one ulp
+    off for about 1% of inputs, sqrt(2.0) among them), so the oracle takes
+    numpy's, which does.  The derivative is torch's: grad / (2 sqrt(x)).
+    """
+
+    @staticmethod
+    def forward(ctx, x):
+        out = torch.from_numpy(np.asarray(np.sqrt(x.detach().numpy())))
+        ctx.save_for_backward(out)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        (out,) = ctx.saved_tensors
+        return grad / (2 * out)
+
+
+def sqrt(x: Tensor) -> Tensor:
+    return _Sqrt.apply(x)
+
 
 # precision.py:50 (jnp.finfo(float64).eps) and :53 (spatial stencil eps)
 EPS = 2.220446049250313e-16
@@ -181,7 +208,7 @@ def jabs(x: Tensor) -> Tensor:
 
 def speed_of_sound(p: Tensor, rho: Tensor, gamma: float) -> Tensor:
     # materials/single_materials/ideal_gas.py:69-71
-    return torch.sqrt(gamma * p / rho)
+    return sqrt(gamma * p / rho)
 
 
 def cons_from_prims(P: Tensor, gamma: float) -> Tensor:
@@ -409,11 +436,11 @@ def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, Tensor
     R = P[_stencil_slice(case, axis, 0)]    # slice_LR[axis][1]: nh : -nh+1
     if case.frozen_state == "ARITHMETIC":
         pa = 0.5 * (L + R)
-        c = torch.sqrt(g * pa[4] / pa[0])
+        c = sqrt(g * pa[4] / pa[0])
         return pa[0], c, c * c
     if case.frozen_state == "ROE":
-        rho_a = torch.sqrt(L[0] * R[0])
-        sL, sR = torch.sqrt(L[0]), torch.sqrt(R[0])
+        rho_a = sqrt(L[0] * R[0])
+        sL, sR = sqrt(L[0]), sqrt(R[0])
         rho_div = 1.0 / (sL + sR)
         psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div
         gr_a = (sL * (g - 1) + sR * (g - 1)) * rho_div
@@ -423,7 +450,7 @@ def frozen_state(P: Tensor, case: OracleCase, axis: int) -> Tuple[Tensor, Tensor
         p_over_rho = (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div \
             + 0.5 * rho_a * rho_div * rho_div * sqvd
         cc = psi_a + gr_a * p_over_rho
-        return rho_a, torch.sqrt(cc), cc
+        return rho_a, sqrt(cc), cc
     raise NotImplementedError(case.frozen_state)
 
 
@@ -446,12 +473,12 @@ def frozen_state_full(P: Tensor, case: OracleCase, axis: int):
         pa = 0.5 * (L + R)
         gr = (g - 1) * torch.ones_like(pa[0])
         H = _total_enthalpy(pa[4], pa[0], pa[1:4], g)
-        c = torch.sqrt(g * pa[4] / pa[0])
+        c = sqrt(g * pa[4] / pa[0])
         cc = c * c
     elif case.frozen_state == "ROE":
-        sL, sR = torch.sqrt(L[0]), torch.sqrt(R[0])
+        sL, sR = sqrt(L[0]), sqrt(R[0])
         pa = (sL * L + sR * R) / (sL + sR)
-        pa = torch.cat([torch.sqrt(L[0] * R[0]).unsqueeze(0), pa[1:]], 0)
+        pa = torch.cat([sqrt(L[0] * R[0]).unsqueeze(0), pa[1:]], 0)
         rho_div = 1.0 / (sL + sR)
         H = (sL * _total_enthalpy(L[4], L[0], L[1:4], g) + sR * _total_enthalpy(R[4], R[0], R[1:4], g)) * rho_div
         psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div
@@ -462,7 +489,7 @@ def frozen_state_full(P: Tensor, case: OracleCase, axis: int):
         p_over_rho = (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div \
             + 0.5 * pa[0] * rho_div * rho_div * sqvd
         cc = psi_a + gr * p_over_rho
-        c = torch.sqrt(cc)
+        c = sqrt(cc)
     else:
         raise NotImplementedError(case.frozen_state)
     u2 = pa[1:4] * pa[1:4]
@@ -549,12 +576,12 @@ def prims_from_chars(x: List[Tensor], rho_a, c, cc, axis: int) -> List[Tensor]:
 def signal_speeds(name: str, uL, uR, aL, aR, rhoL, rhoR, pL, pR, gamma):
     # solvers/riemann_solvers/signal_speeds.py
     if name == "EINFELDT":              # :109-133
-        sL = torch.sqrt(rhoL)
-        sR = torch.sqrt(rhoR)
+        sL = sqrt(rhoL)
+        sR = sqrt(rhoR)
         od = 1.0 / (sL + sR)
         eta2 = 0.5 * sL * sR * od * od
         ubar = (sL * uL + sR * uR) * od
-        dbar = torch.sqrt((sL * aL * aL + sR * aR * aR) * od + eta2 * torch.square(uR - uL))
+        dbar = sqrt((sL * aL * aL + sR * aR * aR) * od + eta2 * torch.square(uR - uL))
         return torch.minimum(ubar - dbar, uL - aL), torch.maximum(ubar + dbar, uR + aR)
     if name == "DAVIS":                 # :51-69
         return torch.minimum(uL - aL, uR - aR), torch.maximum(uL + aL, uR + aR)
@@ -571,8 +598,8 @@ def signal_speeds(name: str, uL, uR, aL, aR, rhoL, rhoR, pL, pR, gamma):
         p_pvrs = 0.5 * (pL + pR) - 0.5 * (uR - uL) * rho_bar * a_bar
         p_star = torch.maximum(torch.zeros_like(p_pvrs), p_pvrs)
         g_ = (gamma + 1) * 0.5 / gamma
-        qL = 1.0 * (p_star <= pL) + torch.sqrt(1 + g_ * (p_star / pL - 1)) * (p_star > pL)
-        qR = 1.0 * (p_star <= pR) + torch.sqrt(1 + g_ * (p_star / pR - 1)) * (p_star > pR)
+        qL = 1.0 * (p_star <= pL) + sqrt(1 + g_ * (p_star / pL - 1)) * (p_star > pL)
+        qR = 1.0 * (p_star <= pR) + sqrt(1 + g_ * (p_star / pR - 1)) * (p_star > pR)
         return uL - aL * qL, uR + aR * qR
     raise NotImplementedError(name)
 

@@ -9,6 +9,9 @@
  *
  *   reconstruction   stencils/reconstruction/shock_capturing/weno/weno5_z.py:24-58,
  *                    weno5_base.py:24-51 (smoothness, polynomials, eps = 1e-30)
+ *   CHAR-PRIMITIVE   high_order_godunov.py:298-316; eigendecomposition.py:120-281
+ *                    (frozen state, ARITHMETIC and ROE), :402-433 and :499-523
+ *                    (primitive <-> characteristic transforms)
  *   conversions      equation_manager.py:93-101, :164-171; ideal_gas.py:69-88
  *   physical flux    equation_manager.py:237-252
  *   HLLC             solvers/riemann_solvers/HLLC.py:41-126,
@@ -94,13 +97,86 @@ static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double 
   for (int v = 0; v < 5; ++v) F[v] = 0.5 * (1.0 + sg) * FL[v] + 0.5 * (1.0 - sg) * FR[v];
 }
 
+/* velocity_minor_axes and vel_id_eigs per axis (equation_information.py:110,
+   eigendecomposition.py:67-71) */
+static const int kMinor[3][2] = {{2, 3}, {3, 1}, {1, 2}};
+static const int kEig[3][2] = {{2, 3}, {3, 2}, {2, 3}};
+
+/* Frozen density, speed of sound and its square between cells L and R:
+   frozen 1 ARITHMETIC, 2 ROE (eigendecomposition.py:120-281). */
+static void frozen_state(const double L[5], const double R[5], int frozen, double gamma, double* rho_a,
+                         double* c, double* cc) {
+  if (frozen == 1) {
+    double pa[5];
+    for (int v = 0; v < 5; ++v) pa[v] = 0.5 * (L[v] + R[v]);
+    *rho_a = pa[0];
+    *c = sqrt(gamma * pa[4] / pa[0]);
+    *cc = *c * *c;
+    return;
+  }
+  const double ra = sqrt(L[0] * R[0]);
+  const double sL = sqrt(L[0]), sR = sqrt(R[0]);
+  const double rho_div = 1.0 / (sL + sR);
+  const double psi_a = (sL * (L[4] / L[0]) + sR * (R[4] / R[0])) * rho_div;
+  const double gr_a = (sL * (gamma - 1) + sR * (gamma - 1)) * rho_div;
+  const double d1 = R[1] - L[1], d2 = R[2] - L[2], d3 = R[3] - L[3];
+  const double sqvd = d1 * d1 + d2 * d2 + d3 * d3;
+  const double p_over_rho = (sL * L[4] / L[0] + sR * R[4] / R[0]) * rho_div + 0.5 * ra * rho_div * rho_div * sqvd;
+  *rho_a = ra;
+  *cc = psi_a + gr_a * p_over_rho;
+  *c = sqrt(*cc);
+}
+
+/* Face states of the six window cells w[k][v] (k = 0..5, face between 2 and 3):
+   mode 0 WENO5-Z on the primitives, 1 / 2 on the characteristic variables of
+   the ARITHMETIC / ROE frozen state. */
+static void face_states(double w[6][5], int axis, int mode, double gamma, double eps, double PL[5],
+                        double PR[5]) {
+  if (mode == 0) {
+    for (int v = 0; v < 5; ++v) {
+      PL[v] = weno5z(w[0][v], w[1][v], w[2][v], w[3][v], w[4][v], eps);
+      PR[v] = weno5z(w[5][v], w[4][v], w[3][v], w[2][v], w[1][v], eps);
+    }
+    return;
+  }
+  const int n = axis + 1, m0 = kMinor[axis][0], m1 = kMinor[axis][1];
+  const int e0 = kEig[axis][0], e1 = kEig[axis][1];
+  double rho_a, c, cc;
+  frozen_state(w[2], w[3], mode, gamma, &rho_a, &c, &cc);
+  double ch[6][5];
+  for (int k = 0; k < 6; ++k) {
+    const double* x = w[k];
+    ch[k][0] = -0.5 / c * x[n] + 0.5 / (cc * rho_a) * x[4];
+    ch[k][1] = x[0] - 1.0 / cc * x[4];
+    ch[k][e0] = x[m0];
+    ch[k][e1] = x[m1];
+    ch[k][4] = 0.5 / c * x[n] + 0.5 / (cc * rho_a) * x[4];
+  }
+  double cL[5], cR[5];
+  for (int v = 0; v < 5; ++v) {
+    cL[v] = weno5z(ch[0][v], ch[1][v], ch[2][v], ch[3][v], ch[4][v], eps);
+    cR[v] = weno5z(ch[5][v], ch[4][v], ch[3][v], ch[2][v], ch[1][v], eps);
+  }
+  const double* xs[2] = {cL, cR};
+  double* outs[2] = {PL, PR};
+  for (int side = 0; side < 2; ++side) {
+    const double* x = xs[side];
+    double* o = outs[side];
+    o[0] = rho_a * (x[0] + x[4]) + x[1];
+    o[n] = c * (-x[0] + x[4]);
+    o[m0] = x[e0];
+    o[m1] = x[e1];
+    o[4] = cc * rho_a * (x[0] + x[4]);
+  }
+}
+
 /*
  * rhs[5][n0][n1][n2] of the primitive halo buffer P[5][h0][h1][h2]
  * (h_a = n_a + 2 nh on active axes, 1 on inactive ones), axes summed in order
- * from the first active one.  Returns 0.
+ * from the first active one; mode as face_states.  Returns 0.
  */
 int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one_dx[3], double gamma,
-                       double eps, double* rhs) {
+                       double eps, int mode, double* rhs) {
   int h[3], lo[3];
   for (int a = 0; a < 3; ++a) {
     h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
@@ -122,15 +198,10 @@ int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one
             int g[3] = {idx[0] + lo[0], idx[1] + lo[1], idx[2] + lo[2]};
             g[a] += side;  /* face between buffer cells g[a] - 1 and g[a] */
             const size_t c0 = ((size_t)g[0] * h[1] + g[1]) * h[2] + g[2];
-            double PL[5], PR[5];
-            for (int v = 0; v < 5; ++v) {
-              const double* q = P + v * hcs + c0;
-              const double m3 = q[-3 * (ptrdiff_t)stride], m2 = q[-2 * (ptrdiff_t)stride];
-              const double m1 = q[-(ptrdiff_t)stride], z0 = q[0];
-              const double p1 = q[stride], p2 = q[2 * stride];
-              PL[v] = weno5z(m3, m2, m1, z0, p1, eps);
-              PR[v] = weno5z(p2, p1, z0, m1, m2, eps);
-            }
+            double w[6][5], PL[5], PR[5];
+            for (int v = 0; v < 5; ++v)
+              for (int k = 0; k < 6; ++k) w[k][v] = P[v * hcs + c0 + (ptrdiff_t)(k - 3) * (ptrdiff_t)stride];
+            face_states(w, a, mode, gamma, eps, PL, PR);
             hllc_einfeldt(PL, PR, a + 1, gamma, F[side]);
           }
           const size_t o = ((size_t)i0 * n[1] + i1) * n[2] + i2;
@@ -143,3 +214,4 @@ int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one
   }
   return 0;
 }
+

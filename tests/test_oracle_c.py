@@ -1,6 +1,7 @@
 """Two independent CPU restatements of the reference agree bitwise: the plain-C
-right-hand side (oracle/jf_rhs.c: WENO5-Z on primitives, HLLC with Einfeldt
-speeds) against the torch oracle, on periodic, zero-gradient and symmetry
+right-hand side (oracle/jf_rhs.c: WENO5-Z on primitives or on their
+characteristic variables with the ARITHMETIC or ROE frozen state, HLLC with
+Einfeldt speeds) against the torch oracle, on periodic, zero-gradient and symmetry
 halos in 1-D to 3-D.  Built here with the system C compiler, contraction off."""
 import ctypes
 import os
@@ -24,7 +25,7 @@ def crhs():
     lib = ctypes.CDLL(so)
     f = lib.jf_rhs_weno5z_hllc
     f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
-                  ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+                  ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
     f.restype = ctypes.c_int
     return f
 
@@ -37,9 +38,14 @@ CASES = [
 ]
 
 
+MODES = {0: {}, 1: dict(recon_var="CHAR-PRIMITIVE", frozen_state="ARITHMETIC"),
+         2: dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE")}
+
+
+@pytest.mark.parametrize("mode", list(MODES), ids=["primitive", "char-arithmetic", "char-roe"])
 @pytest.mark.parametrize("name,cells,bc,kind", CASES, ids=[c[0] for c in CASES])
-def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind):
-    oc, _ = both(cells, bc)
+def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode):
+    oc, _ = both(cells, bc, **MODES[mode])
     if kind == "sod":
         prims = sod_prims(cells[0])
     elif kind == "quad":
@@ -52,5 +58,18 @@ def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind):
     out = np.empty(ref.shape, dtype=np.float64)
     n = (ctypes.c_int * 3)(*cells)
     odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
-    assert crhs(Pn.ctypes.data, n, oc.nh, odx, oc.gamma, O.STENCIL_EPS, out.ctypes.data) == 0
+    assert crhs(Pn.ctypes.data, n, oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, out.ctypes.data) == 0
     assert torch.equal(torch.from_numpy(out), ref)
+
+
+def test_oracle_sqrt_is_correctly_rounded():
+    """The oracle's square root rounds like jnp.sqrt, libm and CUDA, whatever
+    the host's torch build does, and keeps torch's derivative."""
+    import math
+    x = torch.from_numpy(np.random.default_rng(3).uniform(0.01, 10.0, 20000))
+    assert torch.equal(O.sqrt(x), torch.from_numpy(np.sqrt(x.numpy())))
+    assert [O.sqrt(torch.tensor(v, dtype=torch.float64)).item() for v in (2.0, 0.125, 1.12)] == \
+        [math.sqrt(v) for v in (2.0, 0.125, 1.12)]
+    xg = x[:64].clone().requires_grad_(True)
+    O.sqrt(xg).sum().backward()
+    assert torch.allclose(xg.grad, 0.5 / torch.from_numpy(np.sqrt(x[:64].numpy())), rtol=1e-15, atol=0)
