@@ -100,3 +100,21 @@ def generic_cons(cells, seed=0):
                   smooth_field(cells, seed + 3, 0.0, 0.3) if cells[2] > 1 else np.zeros(cells),
                   smooth_field(cells, seed + 4, 1.0, 0.2)])
     return O.cons_from_prims(torch.from_numpy(P), 1.4)
+
+
+def reflect_xy(U: torch.Tensor) -> torch.Tensor:
+    """Cells (i, j, k) -> (j, i, k) with the x and y velocity (or momentum)
+    components swapped: the mirror image of a field in the plane x = y."""
+    return U.transpose(1, 2)[[0, 2, 1, 3, 4]].contiguous()
+
+
+def assert_conserved(U0: torch.Tensor, UK: torch.Tensor, tol: float = 1e-12) -> None:
+    """Domain totals of mass, momentum and energy unchanged to `tol` relative to
+    the total of |rho|, of |rho u_i| over all components, and of |E|."""
+    t0 = U0.reshape(5, -1).sum(1)
+    tk = UK.reshape(5, -1).sum(1)
+    a0 = U0.reshape(5, -1).abs().sum(1)
+    mom = a0[1] + a0[2] + a0[3]
+    scale = [a0[0], mom, mom, mom, a0[4]]
+    for v in range(5):
+        assert abs((tk[v] - t0[v]).item()) <= tol * scale[v].item(), (v, tk[v].item(), t0[v].item())
