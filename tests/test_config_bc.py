@@ -217,3 +217,60 @@ def test_gravity_from_setup():
     num["precision"] = {"is_consistent_summation": True}
     with pytest.raises(NotImplementedError, match="consistent"):
         CaseConfig.from_setups(case, num)
+
+
+def _zg_setup():
+    return _setup({f: {"type": "ZEROGRADIENT"} for f in ("west", "east", "north", "south")})
+
+
+def _set(d, path, value):
+    keys = path.split(".")
+    for k in keys[:-1]:
+        d = d.setdefault(k, {})
+    d[keys[-1]] = value
+
+
+# (which dictionary, key path, value): settings of the reference's setups
+# outside the single-phase path this package builds
+NOT_BUILT = [
+    ("case", "boundary_conditions.east", {"type": "ISOTHERMALWALL"}),
+    ("case", "boundary_conditions.east", {"type": "LINEAREXTRAPOLATION"}),
+    ("case", "boundary_conditions.west", {"type": "SIMPLE_INFLOW"}),
+    ("case", "material_properties.equation_of_state", {"model": "StiffenedGas"}),
+    ("num", "conservatives.convective_fluxes.godunov.reconstruction_stencil", "WENO7"),
+    ("num", "conservatives.convective_fluxes.godunov.reconstruction_stencil", "ALDM"),
+    ("num", "conservatives.convective_fluxes.godunov.riemann_solver", "HLLC-LM"),
+    ("num", "conservatives.convective_fluxes.godunov.riemann_solver", "AUSMP"),
+    ("num", "conservatives.convective_fluxes.convective_solver", "FLUX-SPLITTING"),
+    ("num", "conservatives.time_integration.integrator", "RK2"),
+    ("num", "active_physics.is_geometric_source", True),
+    ("num", "active_physics.is_surface_tension", True),
+    ("num", "conservatives.dissipative_fluxes.is_laplacian", True),
+    ("num", "precision.is_double_precision_compute", False),
+    ("num", "active_forcings.is_turb_hit_forcing", True),
+]
+
+
+@pytest.mark.parametrize("where,path,value", NOT_BUILT, ids=[f"{p}={v}" for _, p, v in NOT_BUILT])
+def test_settings_outside_the_path_are_rejected(where, path, value):
+    """Raised while reading the setups, before any device work."""
+    case, num = _zg_setup()
+    _set(case if where == "case" else num, path, value)
+    with pytest.raises(NotImplementedError):
+        CaseConfig.from_setups(case, num)
+
+
+def test_viscosity_and_conductivity_models_outside_the_path_are_rejected():
+    case, num = _zg_setup()
+    num["active_physics"] = {"is_viscous_flux": True}
+    case["material_properties"]["transport"] = {"dynamic_viscosity": {"model": "SUTHERLAND"}}
+    with pytest.raises(NotImplementedError):
+        CaseConfig.from_setups(case, num)
+    num["active_physics"] = {"is_viscous_flux": True, "is_heat_flux": True}
+    case["material_properties"]["transport"] = {"dynamic_viscosity": {"model": "CUSTOM", "value": 1e-3},
+                                                "thermal_conductivity": {"model": "SUTHERLAND"}}
+    with pytest.raises(NotImplementedError):
+        CaseConfig.from_setups(case, num)
+    case["material_properties"]["transport"]["thermal_conductivity"] = {"model": "PRANDTL", "prandtl_number": 0.72}
+    cfg = CaseConfig.from_setups(case, num)
+    assert cfg.viscous and cfg.heat and abs(cfg.kappa - 3.5 * 1e-3 / 0.72) <= 1e-18
