@@ -179,6 +179,8 @@ typedef struct gbf_tile {
   int32_t threads;       /* threads per CTA (multiple of 32, 32..256) */
 } gbf_tile;
 
+/* GBF_ABI_VERSION the library was built with: a binding compares it with the
+ * gbf_case layout it mirrors before the first call.  No reference counterpart. */
 int gbf_abi_version(void);
 /* Status returned by the most recent int-returning entry point called on this
  * host thread (GBF_OK before any call).  No reference counterpart: the
@@ -186,7 +188,11 @@ int gbf_abi_version(void);
 int gbf_last_status(void);
 const char* gbf_status_string(int status);
 
-/* Checks a descriptor; returns GBF_OK or the reason it cannot run. */
+/* Checks a descriptor without device work; returns GBF_OK or the reason it
+ * cannot run (GBF_ERR_UNSUPPORTED for a setup the CUDA path does not build).
+ * Takes the place of the setup readers' checks for this path
+ * (input/numerical_setup/read_conservatives.py, halo count :361-365;
+ * input/input_manager.py:116 sanity_check), which raise instead. */
 int gbf_case_check(const gbf_case* c);
 
 /*
@@ -199,8 +205,9 @@ int gbf_case_check(const gbf_case* c);
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream);
 
 /* As gbf_rhs with the halo-buffer conservatives `cons` beside the primitives
- * (SpaceSolver.compute_rhs receives both): required by the CONSERVATIVE and
- * CHAR-CONSERVATIVE reconstructions, which reconstruct the conservatives
+ * (SpaceSolver.compute_rhs, solvers/space_solver.py:151-453, receives both):
+ * required by the CONSERVATIVE and CHAR-CONSERVATIVE reconstructions
+ * (high_order_godunov.py:282-296, :404-416), which reconstruct the conservatives
  * (gbf_rhs returns GBF_ERR_INVALID_ARGUMENT for them); read by no other case. */
 int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
                  void* stream);
@@ -241,7 +248,10 @@ size_t gbf_dt_workspace_bytes(void);
 int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspace, void* stream);
 
 /*
- * Fused TVD-RK3 steps on interior conservatives (the hot path).
+ * Fused TVD-RK3 steps on interior conservatives (the hot path).  Replaces the
+ * step loop of SimulationManager (do_runge_kutta_stages,
+ * simulation_manager.py:536-1077, with compute_time_step_size,
+ * time_integration/time_step_size.py:15-157, for the next step).
  * cons: double[5][Nx][Ny][Nz], advanced in place by `steps` steps.  Each
  * stage is one kernel: it builds the primitives of a tile plus its halo from
  * the conservatives (boundary conditions applied by index remapping), sweeps
