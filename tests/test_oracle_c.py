@@ -73,3 +73,9 @@ def test_oracle_sqrt_is_correctly_rounded():
     xg = x[:64].clone().requires_grad_(True)
     O.sqrt(xg).sum().backward()
     assert torch.allclose(xg.grad, 0.5 / torch.from_numpy(np.sqrt(x[:64].numpy())), rtol=1e-15, atol=0)
+
+
+def test_oracle_takes_every_root_from_its_own_sqrt():
+    src = open(os.path.join(ROOT, "oracle", "jf_oracle.py")).read()
+    code = "\n".join(line.split("#")[0] for line in src.splitlines())
+    assert "torch.sqrt(" not in code and ".sqrt()" not in code and "** 0.5" not in code
