@@ -1,7 +1,8 @@
 /*
  * Test infrastructure, not product code: a second CPU restatement, in plain C,
- * of the single-phase right-hand side for WENO5-Z on primitive variables with
- * HLLC and Einfeldt signal speeds, on a halo-filled primitive buffer.  It is
+ * of the single-phase right-hand side for WENO5-Z on primitive or characteristic
+ * variables with HLLC, HLL (Einfeldt signal speeds) or Rusanov fluxes, on a
+ * halo-filled primitive buffer.  It is
  * written independently of the torch restatement in jf_oracle.py and follows
  * the same reference operations in the same order, so the two must agree
  * bitwise; the tests check that (tests/test_oracle_c.py).  Compile without
@@ -16,6 +17,9 @@
  *   physical flux    equation_manager.py:237-252
  *   HLLC             solvers/riemann_solvers/HLLC.py:41-126,
  *                    signal_speeds.py:109-133 (Einfeldt), :159-199 (S*)
+ *   HLL              solvers/riemann_solvers/HLL.py:28-58 (eps = machine
+ *                    epsilon, riemann_solver.py:28)
+ *   Rusanov          solvers/riemann_solvers/Rusanov.py:25-47
  *   divergence       solvers/space_solver.py:266-314, :597-599
  */
 #include <math.h>
@@ -72,12 +76,10 @@ static void hllc_star_flux(const double P[5], const double U[5], double S, doubl
   for (int v = 0; v < 5; ++v) out[v] = F[v] + wave * (us[v] - U[v]);
 }
 
-static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double gamma, double F[5]) {
-  double UL[5], UR[5];
-  cons_from_prims(PL, UL, gamma);
-  cons_from_prims(PR, UR, gamma);
-  const double cL = sqrt(gamma * PL[4] / PL[0]);
-  const double cR = sqrt(gamma * PR[4] / PR[0]);
+/* Einfeldt's wave-speed estimates (signal_speeds.py:109-133) from the face
+   states' normal velocities uL, uR and speeds of sound cL, cR. */
+static void einfeldt(const double PL[5], const double PR[5], int n, double cL, double cR, double* SL,
+                     double* SR) {
   const double uL = PL[n], uR = PR[n];
   const double sL = sqrt(PL[0]), sR = sqrt(PR[0]);
   const double od = 1.0 / (sL + sR);
@@ -85,8 +87,19 @@ static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double 
   const double ubar = (sL * uL + sR * uR) * od;
   const double du = uR - uL;
   const double dbar = sqrt((sL * cL * cL + sR * cR * cR) * od + eta2 * (du * du));
-  const double SL = fmin(ubar - dbar, uL - cL);
-  const double SR = fmax(ubar + dbar, uR + cR);
+  *SL = fmin(ubar - dbar, uL - cL);
+  *SR = fmax(ubar + dbar, uR + cR);
+}
+
+static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double gamma, double F[5]) {
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, gamma);
+  cons_from_prims(PR, UR, gamma);
+  const double cL = sqrt(gamma * PL[4] / PL[0]);
+  const double cR = sqrt(gamma * PR[4] / PR[0]);
+  const double uL = PL[n], uR = PR[n];
+  double SL, SR;
+  einfeldt(PL, PR, n, cL, cR, &SL, &SR);
   const double rdL = PL[0] * (SL - uL);
   const double rdR = PR[0] * (SR - uR);
   const double Ss = ((PR[4] - PL[4]) + (uL * rdL - uR * rdR)) / (rdL - rdR);
@@ -95,6 +108,49 @@ static void hllc_einfeldt(const double PL[5], const double PR[5], int n, double 
   hllc_star_flux(PR, UR, SR, Ss, n, 0, FR);
   const double sg = (Ss > 0.0) ? 1.0 : (Ss < 0.0) ? -1.0 : Ss;  /* sign, 0 and NaN kept */
   for (int v = 0; v < 5; ++v) F[v] = 0.5 * (1.0 + sg) * FL[v] + 0.5 * (1.0 - sg) * FR[v];
+}
+
+/* Physical fluxes of both face states (equation_manager.py:237-252). */
+static void both_fluxes(const double PL[5], const double PR[5], int n, double gamma, double UL[5], double UR[5],
+                        double FL[5], double FR[5]) {
+  cons_from_prims(PL, UL, gamma);
+  cons_from_prims(PR, UR, gamma);
+  physical_flux(PL, UL, n, FL);
+  physical_flux(PR, UR, n, FR);
+}
+
+/* HLL with Einfeldt speeds clipped at 0: (SR FL - SL FR + SL SR (UR - UL)) /
+   (SR - SL + eps), eps the double-precision machine epsilon. */
+static void hll_einfeldt(const double PL[5], const double PR[5], int n, double gamma, double F[5]) {
+  double UL[5], UR[5], FL[5], FR[5];
+  both_fluxes(PL, PR, n, gamma, UL, UR, FL, FR);
+  const double cL = sqrt(gamma * PL[4] / PL[0]);
+  const double cR = sqrt(gamma * PR[4] / PR[0]);
+  double SLs, SRs;
+  einfeldt(PL, PR, n, cL, cR, &SLs, &SRs);
+  const double SL = fmin(SLs, 0.0), SR = fmax(SRs, 0.0);
+  const double den = SR - SL + 2.220446049250313e-16;
+  for (int v = 0; v < 5; ++v) F[v] = (SR * FL[v] - SL * FR[v] + SL * SR * (UR[v] - UL[v])) / den;
+}
+
+/* Rusanov: 0.5 (FL + FR) - 0.5 alpha (UR - UL), alpha the larger |u| + c. */
+static void rusanov(const double PL[5], const double PR[5], int n, double gamma, double F[5]) {
+  double UL[5], UR[5], FL[5], FR[5];
+  both_fluxes(PL, PR, n, gamma, UL, UR, FL, FR);
+  const double cL = sqrt(gamma * PL[4] / PL[0]);
+  const double cR = sqrt(gamma * PR[4] / PR[0]);
+  const double alpha = fmax(fabs(PL[n]) + cL, fabs(PR[n]) + cR);
+  for (int v = 0; v < 5; ++v) F[v] = 0.5 * (FL[v] + FR[v]) - 0.5 * alpha * (UR[v] - UL[v]);
+}
+
+/* riemann 0 HLLC, 1 Rusanov, 2 HLL (the ABI's numbering). */
+static void riemann_flux(const double PL[5], const double PR[5], int n, double gamma, int riemann, double F[5]) {
+  if (riemann == 1)
+    rusanov(PL, PR, n, gamma, F);
+  else if (riemann == 2)
+    hll_einfeldt(PL, PR, n, gamma, F);
+  else
+    hllc_einfeldt(PL, PR, n, gamma, F);
 }
 
 /* velocity_minor_axes and vel_id_eigs per axis (equation_information.py:110,
@@ -173,10 +229,11 @@ static void face_states(double w[6][5], int axis, int mode, double gamma, double
 /*
  * rhs[5][n0][n1][n2] of the primitive halo buffer P[5][h0][h1][h2]
  * (h_a = n_a + 2 nh on active axes, 1 on inactive ones), axes summed in order
- * from the first active one; mode as face_states.  Returns 0.
+ * from the first active one; mode as face_states, riemann as riemann_flux.
+ * Returns 0.
  */
-int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one_dx[3], double gamma,
-                       double eps, int mode, double* rhs) {
+int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
+                  int mode, int riemann, double* rhs) {
   int h[3], lo[3];
   for (int a = 0; a < 3; ++a) {
     h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
@@ -202,7 +259,7 @@ int jf_rhs_weno5z_hllc(const double* P, const int n[3], int nh, const double one
             for (int v = 0; v < 5; ++v)
               for (int k = 0; k < 6; ++k) w[k][v] = P[v * hcs + c0 + (ptrdiff_t)(k - 3) * (ptrdiff_t)stride];
             face_states(w, a, mode, gamma, eps, PL, PR);
-            hllc_einfeldt(PL, PR, a + 1, gamma, F[side]);
+            riemann_flux(PL, PR, a + 1, gamma, riemann, F[side]);
           }
           const size_t o = ((size_t)i0 * n[1] + i1) * n[2] + i2;
           for (int v = 0; v < 5; ++v) {

@@ -1,7 +1,7 @@
 """Two independent CPU restatements of the reference agree bitwise: the plain-C
 right-hand side (oracle/jf_rhs.c: WENO5-Z on primitives or on their
 characteristic variables with the ARITHMETIC or ROE frozen state, HLLC with
-Einfeldt speeds) against the torch oracle, on periodic, zero-gradient and symmetry
+Einfeldt speeds, HLL or Rusanov) against the torch oracle, on periodic, zero-gradient and symmetry
 halos in 1-D to 3-D.  Built here with the system C compiler, contraction off."""
 import ctypes
 import os
@@ -23,9 +23,9 @@ def crhs():
     if not so:
         pytest.skip("no C compiler")
     lib = ctypes.CDLL(so)
-    f = lib.jf_rhs_weno5z_hllc
+    f = lib.jf_rhs_weno5z
     f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
-                  ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+                  ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     f.restype = ctypes.c_int
     return f
 
@@ -42,10 +42,14 @@ MODES = {0: {}, 1: dict(recon_var="CHAR-PRIMITIVE", frozen_state="ARITHMETIC"),
          2: dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE")}
 
 
+RIEMANN = {0: "HLLC", 1: "RUSANOV", 2: "HLL"}
+
+
+@pytest.mark.parametrize("riemann", list(RIEMANN), ids=[v.lower() for v in RIEMANN.values()])
 @pytest.mark.parametrize("mode", list(MODES), ids=["primitive", "char-arithmetic", "char-roe"])
 @pytest.mark.parametrize("name,cells,bc,kind", CASES, ids=[c[0] for c in CASES])
-def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode):
-    oc, _ = both(cells, bc, **MODES[mode])
+def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode, riemann):
+    oc, _ = both(cells, bc, riemann=RIEMANN[riemann], **MODES[mode])
     if kind == "sod":
         prims = sod_prims(cells[0])
     elif kind == "quad":
@@ -58,7 +62,7 @@ def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode):
     out = np.empty(ref.shape, dtype=np.float64)
     n = (ctypes.c_int * 3)(*cells)
     odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
-    assert crhs(Pn.ctypes.data, n, oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, out.ctypes.data) == 0
+    assert crhs(Pn.ctypes.data, n, oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, riemann, out.ctypes.data) == 0
     assert torch.equal(torch.from_numpy(out), ref)
 
 
