@@ -272,3 +272,52 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
   return 0;
 }
 
+
+/*
+ * Face halos of the primitive halo buffer P[5][h0][h1][h2] (as jf_rhs_weno5z)
+ * from its interior, for PERIODIC (0), ZEROGRADIENT (1) and SYMMETRY (2)
+ * faces (halos/outer/material.py:868-894 with the retrieve slices of
+ * halos/outer/boundary_condition.py:539-604): halo layer g = 1..nh outside a
+ * face takes interior cell n - g + 1 counted from the opposite face
+ * (periodic), the boundary cell (zero gradient), or interior cell g with the
+ * face-normal velocity negated (symmetry).  bc[2 a + hi]: faces west, east,
+ * south, north, bottom, top.  Edge and corner halos are left as they are (the
+ * inviscid right-hand side reads none).  Returns 0, or -1 for another type.
+ */
+int jf_fill_face_halos(double* P, const int n[3], int nh, const int bc[6]) {
+  int h[3];
+  for (int a = 0; a < 3; ++a) h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
+  const size_t hcs = (size_t)h[0] * h[1] * h[2];
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] <= 1) continue;
+    const int b = (a + 1) % 3, c = (a + 2) % 3;  /* the two tangential axes */
+    for (int hi = 0; hi < 2; ++hi) {
+      const int type = bc[2 * a + hi];
+      if (type < 0 || type > 2) return -1;
+      for (int g = 1; g <= nh; ++g) {
+        const int dst = hi ? nh + n[a] + g - 1 : nh - g;
+        int src;
+        if (type == 0)
+          src = hi ? nh + g - 1 : nh + n[a] - g;
+        else if (type == 1)
+          src = hi ? nh + n[a] - 1 : nh;
+        else
+          src = hi ? nh + n[a] - g : nh + g - 1;
+        for (int ib = 0; ib < h[b]; ++ib)
+          for (int ic = 0; ic < h[c]; ++ic) {
+            int id[3], is[3];
+            id[a] = dst; is[a] = src;
+            id[b] = is[b] = ib;
+            id[c] = is[c] = ic;
+            const size_t od = ((size_t)id[0] * h[1] + id[1]) * h[2] + id[2];
+            const size_t os = ((size_t)is[0] * h[1] + is[1]) * h[2] + is[2];
+            for (int v = 0; v < 5; ++v) {
+              const double x = P[v * hcs + os];
+              P[v * hcs + od] = (type == 2 && v == a + 1) ? -1.0 * x : x;
+            }
+          }
+      }
+    }
+  }
+  return 0;
+}

@@ -2,7 +2,8 @@
 right-hand side (oracle/jf_rhs.c: WENO5-Z on primitives or on their
 characteristic variables with the ARITHMETIC or ROE frozen state, HLLC with
 Einfeldt speeds, HLL or Rusanov) against the torch oracle, on periodic, zero-gradient and symmetry
-halos in 1-D to 3-D.  Built here with the system C compiler, contraction off."""
+halos in 1-D to 3-D, each side filling its own halos from the same interior.
+Built here with the system C compiler, contraction off."""
 import ctypes
 import os
 
@@ -12,6 +13,9 @@ import torch
 
 from oracle import jf_oracle as O
 from tests.cases import both, quadrant_prims, sod_prims, tgv_prims
+
+BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2}
+FACE_ORDER = ("west", "east", "south", "north", "bottom", "top")
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -26,6 +30,15 @@ def crhs():
     f = lib.jf_rhs_weno5z
     f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    return f
+
+
+@pytest.fixture(scope="module")
+def halos(crhs):
+    import __graft_entry__
+    f = ctypes.CDLL(__graft_entry__.build_oracle_c()).jf_fill_face_halos
+    f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     f.restype = ctypes.c_int
     return f
 
@@ -48,7 +61,7 @@ RIEMANN = {0: "HLLC", 1: "RUSANOV", 2: "HLL"}
 @pytest.mark.parametrize("riemann", list(RIEMANN), ids=[v.lower() for v in RIEMANN.values()])
 @pytest.mark.parametrize("mode", list(MODES), ids=["primitive", "char-arithmetic", "char-roe"])
 @pytest.mark.parametrize("name,cells,bc,kind", CASES, ids=[c[0] for c in CASES])
-def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode, riemann):
+def test_c_restatement_matches_torch_oracle(crhs, halos, name, cells, bc, kind, mode, riemann):
     oc, _ = both(cells, bc, riemann=RIEMANN[riemann], **MODES[mode])
     if kind == "sod":
         prims = sod_prims(cells[0])
@@ -58,7 +71,15 @@ def test_c_restatement_matches_torch_oracle(crhs, name, cells, bc, kind, mode, r
         prims = tgv_prims(max(cells))[:, :cells[0], :cells[1], :cells[2]].contiguous()
     U, P = O.initialize(prims, oc)
     ref = O.compute_rhs(U, P, oc)
-    Pn = np.ascontiguousarray(P.numpy())
+    # the C side fills its own face halos from the interior
+    Pn = np.zeros(P.shape, dtype=np.float64)
+    Pn[(slice(None),) + oc.interior()[1:]] = P[oc.interior()].numpy()
+    codes = (ctypes.c_int * 6)(*[BC[oc.bc[f]] for f in FACE_ORDER])
+    assert halos(Pn.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, codes) == 0
+    for a in range(3):
+        if cells[a] > 1:
+            face_rows = [slice(None)] + [slice(None) if b == a else oc.interior()[b + 1] for b in range(3)]
+            assert np.array_equal(Pn[tuple(face_rows)], P[tuple(face_rows)].numpy()), a
     out = np.empty(ref.shape, dtype=np.float64)
     n = (ctypes.c_int * 3)(*cells)
     odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
