@@ -64,6 +64,14 @@ def sqrt(x: Tensor) -> Tensor:
     return _Sqrt.apply(x)
 
 
+def rdiv(a: float, t: Tensor) -> Tensor:
+    """a / t rounded once, as jnp's true_divide of a Python scalar by an array.
+    torch evaluates ``float / tensor`` as ``float * (1 / tensor)``, two
+    roundings, which differs for about a quarter of the inputs unless the
+    numerator is a power of two (``1.0 / x``, ``0.5 / x`` stay exact)."""
+    return torch.full_like(t, a) / t
+
+
 # precision.py:50 (jnp.finfo(float64).eps) and :53 (spatial stencil eps)
 EPS = 2.220446049250313e-16
 STENCIL_EPS = 1e-30
@@ -1139,14 +1147,14 @@ def compute_dt(P: Tensor, case: OracleCase) -> Tensor:
     abs_vel = 0.0
     for i in case.active:
         abs_vel = abs_vel + (torch.abs(Pi[i + 1]) + c)
-    dt = case.min_cell_size / (torch.max(abs_vel) + EPS)
+    dt = rdiv(case.min_cell_size, torch.max(abs_vel) + EPS)
     if case.viscous:
-        nu = case.mu / rho
-        dt_v = 3.0 / 14.0 * (case.min_cell_size * case.min_cell_size) / (torch.max(nu) + EPS)
+        nu = rdiv(case.mu, rho)
+        dt_v = rdiv(3.0 / 14.0 * (case.min_cell_size * case.min_cell_size), torch.max(nu) + EPS)
         dt = torch.minimum(dt, dt_v)
     if case.heat:
-        alpha = case.kappa() / (rho * case.cp())
-        dt_h = 0.1 * (case.min_cell_size * case.min_cell_size) / (torch.max(alpha) + EPS)
+        alpha = rdiv(case.kappa(), rho * case.cp())
+        dt_h = rdiv(0.1 * (case.min_cell_size * case.min_cell_size), torch.max(alpha) + EPS)
         dt = torch.minimum(dt, dt_h)
     return dt * case.cfl
 

@@ -24,6 +24,8 @@
  */
 #include <math.h>
 #include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
 
 static double weno5z(double u0, double u1, double u2, double u3, double u4, double eps) {
   const double t0 = u0 - 2.0 * u1 + u2, t1 = u0 - 4.0 * u1 + 3.0 * u2;
@@ -320,4 +322,91 @@ int jf_fill_face_halos(double* P, const int n[3], int nh, const int bc[6]) {
     }
   }
   return 0;
+}
+
+/* Primitives of one cell's conservatives (equation_manager.py:164-171,
+   ideal_gas.py:73-75: p = (gamma - 1) e rho). */
+static void prims_from_cons(const double U[5], double P[5], double gamma) {
+  const double rho = U[0];
+  const double one_rho = 1.0 / rho;
+  const double u = U[1] * one_rho, v = U[2] * one_rho, w = U[3] * one_rho;
+  const double e = U[4] * one_rho - 0.5 * (u * u + v * v + w * w);
+  P[0] = rho; P[1] = u; P[2] = v; P[3] = w;
+  P[4] = (gamma - 1.0) * e * rho;
+}
+
+/*
+ * `steps` TVD-RK3 steps with the CFL time step (simulation_manager.py:670-1077;
+ * time_integration/RK3.py:27-62; time_step_size.py:15-157 for inviscid cases).
+ * U, P: interior conservatives and primitives [5][n0][n1][n2]; P is used for
+ * the first stage (as the reference's initial primitive buffer) and both are
+ * advanced in place.  After each stage the primitives are recomputed from the
+ * conservatives and the face halos refilled (bc as jf_fill_face_halos).  dt of
+ * each step: min_cell_size / (max over cells of the sum over active axes of
+ * |u_i| + c, plus eps) times cfl.  *t is advanced by the dts.  Returns 0, -1
+ * for a boundary type it does not fill, -2 when out of memory.
+ */
+int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
+                 double cfl, double gamma, double eps, int mode, int riemann, const int bc[6], int steps,
+                 double* t) {
+  int h[3], lo[3];
+  for (int a = 0; a < 3; ++a) {
+    h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
+    lo[a] = n[a] > 1 ? nh : 0;
+  }
+  const size_t hcs = (size_t)h[0] * h[1] * h[2];
+  const size_t cs = (size_t)n[0] * n[1] * n[2];
+  double* Ph = (double*)calloc(5 * hcs, sizeof(double));
+  double* Un = (double*)malloc(5 * cs * sizeof(double));
+  double* rhs = (double*)malloc(5 * cs * sizeof(double));
+  int st = 0;
+  if (!Ph || !Un || !rhs) st = -2;
+  /* interior primitives -> halo buffer, then its face halos */
+#define JF_LOAD_HALO()                                                                    \
+  for (int i0 = 0; i0 < n[0]; ++i0)                                                       \
+    for (int i1 = 0; i1 < n[1]; ++i1)                                                     \
+      for (int i2 = 0; i2 < n[2]; ++i2) {                                                 \
+        const size_t o = ((size_t)i0 * n[1] + i1) * n[2] + i2;                             \
+        const size_t q = ((size_t)(i0 + lo[0]) * h[1] + (i1 + lo[1])) * h[2] + (i2 + lo[2]); \
+        for (int v = 0; v < 5; ++v) Ph[v * hcs + q] = P[v * cs + o];                       \
+      }                                                                                   \
+  if (st == 0 && jf_fill_face_halos(Ph, n, nh, bc) != 0) st = -1;
+  if (st == 0) { JF_LOAD_HALO() }
+  static const double kDtMult[3] = {1.0, 0.25, 2.0 / 3.0};
+  static const double kCons[2][2] = {{0.25, 0.75}, {2.0 / 3.0, 1.0 / 3.0}};
+  for (int step = 0; st == 0 && step < steps; ++step) {
+    double amax = 0.0;
+    int first = 1;
+    for (size_t o = 0; o < cs; ++o) {
+      const double c = sqrt(gamma * P[4 * cs + o] / P[o]);
+      double s = 0.0;
+      for (int a = 0; a < 3; ++a)
+        if (n[a] > 1) s = s + (fabs(P[(a + 1) * cs + o]) + c);
+      if (first || s > amax) amax = s;
+      first = 0;
+    }
+    const double dt = min_cell_size / (amax + 2.220446049250313e-16) * cfl;
+    memcpy(Un, U, 5 * cs * sizeof(double));
+    for (int stage = 0; stage < 3; ++stage) {
+      jf_rhs_weno5z(Ph, n, nh, one_dx, gamma, eps, mode, riemann, rhs);
+      const double ts = dt * kDtMult[stage];
+      for (size_t k = 0; k < 5 * cs; ++k) {
+        const double base = stage > 0 ? kCons[stage - 1][0] * U[k] + kCons[stage - 1][1] * Un[k] : U[k];
+        U[k] = base + ts * rhs[k];
+      }
+      for (size_t o = 0; o < cs; ++o) {
+        double u5[5], p5[5];
+        for (int v = 0; v < 5; ++v) u5[v] = U[v * cs + o];
+        prims_from_cons(u5, p5, gamma);
+        for (int v = 0; v < 5; ++v) P[v * cs + o] = p5[v];
+      }
+      JF_LOAD_HALO()
+    }
+    *t += dt;
+  }
+#undef JF_LOAD_HALO
+  free(Ph);
+  free(Un);
+  free(rhs);
+  return st;
 }

@@ -104,3 +104,46 @@ def test_oracle_takes_every_root_from_its_own_sqrt():
     src = open(os.path.join(ROOT, "oracle", "jf_oracle.py")).read()
     code = "\n".join(line.split("#")[0] for line in src.splitlines())
     assert "torch.sqrt(" not in code and ".sqrt()" not in code and "** 0.5" not in code
+
+
+STEP_SCHEMES = [(0, 0), (1, 1), (2, 2)]  # (reconstruction mode, Riemann solver)
+
+
+@pytest.mark.parametrize("mode,riemann", STEP_SCHEMES, ids=["primitive-hllc", "char-arithmetic-rusanov",
+                                                            "char-roe-hll"])
+@pytest.mark.parametrize("name,cells,bc,kind", CASES, ids=[c[0] for c in CASES])
+def test_c_rk3_steps_match_torch_oracle(crhs, name, cells, bc, kind, mode, riemann):
+    """CFL time step, three stages, primitives and halos after every stage:
+    the states and the time agree bitwise after the steps."""
+    import __graft_entry__
+    lib = ctypes.CDLL(__graft_entry__.build_oracle_c())
+    f = lib.jf_rk3_steps
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_double)]
+    f.restype = ctypes.c_int
+    oc, _ = both(cells, bc, riemann=RIEMANN[riemann], **MODES[mode])
+    if kind == "sod":
+        prims, steps = sod_prims(cells[0]), 12
+    elif kind == "quad":
+        prims, steps = quadrant_prims(cells[0], cells[1], seed=4), 4
+    else:
+        prims, steps = tgv_prims(max(cells))[:, :cells[0], :cells[1], :cells[2]].contiguous(), 3
+    U, P = O.initialize(prims, oc)
+    inner = oc.interior()
+    Uc = np.ascontiguousarray(U[inner].numpy())
+    Pc = np.ascontiguousarray(P[inner].numpy())
+    t = 0.0
+    for _ in range(steps):
+        dt = O.compute_dt(P, oc)
+        U, P = O.rk3_step(U, P, dt, oc)
+        t += dt.item()
+    tc = ctypes.c_double(0.0)
+    odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
+    codes = (ctypes.c_int * 6)(*[BC[oc.bc[f_]] for f_ in FACE_ORDER])
+    assert f(Uc.ctypes.data, Pc.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, odx, oc.min_cell_size, oc.cfl,
+             oc.gamma, O.STENCIL_EPS, mode, riemann, codes, steps, ctypes.byref(tc)) == 0
+    assert tc.value == t
+    assert torch.equal(torch.from_numpy(Uc), U[inner])
+    assert torch.equal(torch.from_numpy(Pc), P[inner])
