@@ -2,8 +2,9 @@
  * Test infrastructure, not product code: a second CPU restatement, in plain C,
  * of the single-phase right-hand side for WENO5-Z on primitive or characteristic
  * variables with HLLC, HLL (Einfeldt signal speeds) or Rusanov fluxes, on a
- * halo-filled primitive buffer.  It is
- * written independently of the torch restatement in jf_oracle.py and follows
+ * halo-filled primitive buffer, with its own face halos, CFL time step and
+ * TVD-RK3 steps.  It is written independently of the torch restatement in
+ * jf_oracle.py and follows
  * the same reference operations in the same order, so the two must agree
  * bitwise; the tests check that (tests/test_oracle_c.py).  Compile without
  * contraction (-ffp-contract=off): the reference rounds every product.
@@ -21,6 +22,10 @@
  *                    epsilon, riemann_solver.py:28)
  *   Rusanov          solvers/riemann_solvers/Rusanov.py:25-47
  *   divergence       solvers/space_solver.py:266-314, :597-599
+ *   face halos       halos/outer/material.py:868-894,
+ *                    halos/outer/boundary_condition.py:539-604
+ *   time step        time_integration/time_step_size.py:15-157 (inviscid)
+ *   TVD-RK3          time_integration/RK3.py:27-62, simulation_manager.py:670-1077
  */
 #include <math.h>
 #include <stddef.h>

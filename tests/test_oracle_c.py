@@ -147,3 +147,9 @@ def test_c_rk3_steps_match_torch_oracle(crhs, name, cells, bc, kind, mode, riema
     assert tc.value == t
     assert torch.equal(torch.from_numpy(Uc), U[inner])
     assert torch.equal(torch.from_numpy(Pc), P[inner])
+
+
+def test_oracle_rdiv_rounds_once():
+    x = torch.from_numpy(np.random.default_rng(5).uniform(0.01, 10.0, 20000))
+    for a in (0.1, 3.0 / 14.0, 1.0 / 120.0):
+        assert torch.equal(O.rdiv(a, x), torch.from_numpy(a / x.numpy()))
