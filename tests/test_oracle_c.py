@@ -153,3 +153,33 @@ def test_oracle_rdiv_rounds_once():
     x = torch.from_numpy(np.random.default_rng(5).uniform(0.01, 10.0, 20000))
     for a in (0.1, 3.0 / 14.0, 1.0 / 120.0):
         assert torch.equal(O.rdiv(a, x), torch.from_numpy(a / x.numpy()))
+
+
+def test_c_and_torch_oracles_agree_on_sod_200_to_end_time(crhs):
+    """The 1-D Sod workload at its full size (200 cells, WENO5-Z + HLLC, CFL
+    0.5, zero-gradient) to t = 0.2: both restatements step to the same state
+    and time, bitwise."""
+    import __graft_entry__
+    f = ctypes.CDLL(__graft_entry__.build_oracle_c()).jf_rk3_steps
+    f.restype = ctypes.c_int
+    cells = (200, 1, 1)
+    oc, _ = both(cells, "ZEROGRADIENT", cfl=0.5)
+    U, P = O.initialize(sod_prims(200), oc)
+    inner = oc.interior()
+    Uc = np.ascontiguousarray(U[inner].numpy())
+    Pc = np.ascontiguousarray(P[inner].numpy())
+    t, steps = 0.0, 0
+    while t < 0.2:
+        dt = O.compute_dt(P, oc)
+        U, P = O.rk3_step(U, P, dt, oc)
+        t += dt.item()
+        steps += 1
+    tc = ctypes.c_double(0.0)
+    odx = (ctypes.c_double * 3)(oc.one_cell_size(0), 0.0, 0.0)
+    codes = (ctypes.c_int * 6)(*[BC["ZEROGRADIENT"]] * 6)
+    assert f(ctypes.c_void_p(Uc.ctypes.data), ctypes.c_void_p(Pc.ctypes.data), (ctypes.c_int * 3)(*cells),
+             ctypes.c_int(oc.nh), odx, ctypes.c_double(oc.min_cell_size), ctypes.c_double(oc.cfl),
+             ctypes.c_double(oc.gamma), ctypes.c_double(O.STENCIL_EPS), ctypes.c_int(0), ctypes.c_int(0), codes,
+             ctypes.c_int(steps), ctypes.byref(tc)) == 0
+    assert steps > 50 and tc.value == t
+    assert torch.equal(torch.from_numpy(Uc), U[inner])
