@@ -8,8 +8,9 @@ kernel) of the whole grid; cell-updates/s = cells x steps / time.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm
-(the oracle, torch on all host threads) on a bounded sample of the same
-workload; the reference itself (JAX) is not installed on these machines.
+(the oracle, torch on all host threads) on the same TGV 128^3 workload with
+the same warm-up and step counts; the reference itself (JAX) is installed on
+neither machine.
 Under torchrun each rank advances its own replica (replicas only: the path
 has no multi-GPU exchange), and rank 0 prints one JSON line.
 """
@@ -121,12 +122,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def fp64_peak_tflops(lib, device):
-    """DFMA-chain rate of this GPU (8 chains/thread, 152 x 8 CTAs of 256 threads)."""
+def fp64_peak_tflops(device):
+    """DFMA-chain rate of this GPU (8 chains/thread, 152 x 8 CTAs of 256 threads),
+    timed with the arithmetic-rate probe library (libgbfprobe.so)."""
+    import ctypes
+    from jaxfluids_gb300 import build
+    lib = ctypes.CDLL(build.build_probe())
+    lib.gbf_probe_arith.restype = ctypes.c_int
+    lib.gbf_probe_arith.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p]
     blocks, threads, iters = 152 * 8, 256, 2048
     out = torch.empty(blocks * threads, dtype=torch.float64, device=device)
     s = torch.cuda.current_stream()
-    import ctypes
     st = ctypes.c_void_p(s.cuda_stream)
     lib.gbf_probe_arith(0, ctypes.c_void_p(out.data_ptr()), blocks, threads, 64, st)
     torch.cuda.synchronize()
@@ -143,53 +150,74 @@ def fp64_peak_tflops(lib, device):
     return flops / best / 1e12
 
 
-def cpu_oracle_rate(n=24, steps=2, threads=None):
-    """Oracle (torch CPU, float64) TVD-RK3 rate on a TGV n^3 sample."""
-    from oracle import jf_oracle as O
-    if threads:
+def cpu_model():
+    """CPU model string of this host (lscpu's Model name, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for key in ("Model name:", "Vendor ID:"):
+            for line in out.splitlines():
+                if line.strip().startswith(key):
+                    return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+class OracleRun:
+    """The CPU restatement of the reference (oracle, torch float64 on `threads`
+    host threads) advancing the TGV n^3 workload step by step: the same
+    initial condition, scheme and CFL time step as the GPU run."""
+
+    def __init__(self, n, threads):
+        from oracle import jf_oracle as O
+        self.O = O
         torch.set_num_threads(threads)
-    case = O.OracleCase(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=3,
-                        bc={f: "PERIODIC" for f in O.FACES}, recon="WENO5-Z", riemann="HLLC",
-                        signal_speed="EINFELDT", cfl=0.5)
-    U = tgv_state(n, "cpu")
-    P = O.prims_from_cons(U, 1.4)
-    Ub, Pb = O.initialize(P, case)
-    dt = O.compute_dt(Pb, case)
-    Ub, Pb = O.rk3_step(Ub, Pb, dt, case)  # warm-up
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        dt = O.compute_dt(Pb, case)
-        Ub, Pb = O.rk3_step(Ub, Pb, dt, case)
-    el = time.perf_counter() - t0
-    return n ** 3 * steps / el, el
+        self.case = O.OracleCase(cells=(n, n, n), ranges=((0.0, 2 * math.pi),) * 3, nh=3,
+                                 bc={f: "PERIODIC" for f in O.FACES}, recon="WENO5-Z", riemann="HLLC",
+                                 signal_speed="EINFELDT", cfl=0.5)
+        U = tgv_state(n, "cpu")
+        self.U, self.P = O.initialize(O.prims_from_cons(U, 1.4), self.case)
+        self.dt = O.compute_dt(self.P, self.case)
+        self.cells = n ** 3
+
+    def step(self):
+        """One RK3 step and the next CFL time step; returns its wall time (s)."""
+        t0 = time.perf_counter()
+        self.U, self.P = self.O.rk3_step(self.U, self.P, self.dt, self.case)
+        self.dt = self.O.compute_dt(self.P, self.case)
+        return time.perf_counter() - t0
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference's algorithm
+    (JAX is installed on neither machine, so the reference itself cannot run)
+    on the same TGV 128^3 workload, all host threads, W warm-up + K timed steps."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    n = 48
-    from oracle import jf_oracle as O  # noqa: F401
-    # warm-up steps
+    n = args.n if args.n else N_TGV
+    run = OracleRun(n, threads)
     for _ in range(max(0, args.warmup)):
-        cpu_oracle_rate(n, 1, threads)
-    total_cells, total_t = 0, 0.0
-    for _ in range(args.steps):
-        rate, el = cpu_oracle_rate(n, 1, threads)
-        total_cells += n ** 3
-        total_t += el
-    value = total_cells / total_t
+        run.step()
+    total_t = sum(run.step() for _ in range(args.steps))
+    value = run.cells * args.steps / total_t
+    sample = (f"TGV {n}^3, {args.warmup} warm-up + {args.steps} timed RK3 steps, CPU restatement of the "
+              f"reference (torch float64, {threads} threads on {cpu_model()}); the JAX reference is not installed")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"TGV {n}^3 sample of the 128^3 case (same scheme, periodic)",
+        "config": {"workload": f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4",
                    "cells": n ** 3, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"TGV {n}^3, {args.steps} RK3 steps, CPU restatement (torch float64, "
-                                   f"{threads} threads); the JAX reference is not installed"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -501,12 +529,12 @@ def main():
     except Exception:
         peak_src = "fallback"
     achieved = bytes_per_launch / launch_s / 1e9
-    fp64_peak = fp64_peak_tflops(lib, device)
+    fp64_peak = fp64_peak_tflops(device)
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_source": peak_src,
         "traffic": DRAM_BYTES_PER_LAUNCH,
-        "kernel": "sweep_kernel<WENO5Z,HLLC,STAGE> (one launch per RK stage)",
+        "kernel": "RK stage: face_flux_kernel<x,y,z; WENO5Z,HLLC> + stage_epilogue_kernel",
         "fp64": {"peak_tflops_measured": fp64_peak,
                  "achieved_tflops": (FP64_FLOP_PER_CELL_UPDATE * cells / 3.0 / launch_s / 1e12)
                  if FP64_FLOP_PER_CELL_UPDATE else None,
@@ -536,9 +564,13 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, el = cpu_oracle_rate(64, 3, threads)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"TGV 64^3, 3 RK3 steps ({el:.1f} s), CPU restatement (torch float64)"}
+        run = OracleRun(n, threads)
+        run.step()  # warm-up
+        el = sum(run.step() for _ in range(3))
+        cpu = {"value": run.cells * 3 / el, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"TGV {n}^3 (the same workload), 1 warm-up + 3 timed RK3 steps ({el:.1f} s), CPU "
+                         f"restatement of the reference (torch float64, {threads} threads)",
+               "cpu_model": cpu_model()}
 
     if viscous:
         roofline["fp64"]["flop_per_cell_update"] = None
@@ -560,7 +592,9 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "l2": "256 MiB buffer written between timed steps (per-step CUDA events)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": (7 if viscous else 4) * args.steps, "clocks": clocks, "wall_s": wall,
+            # per advance(1): the stage primitives of U^n, three stages of one face
+            # kernel per axis and one epilogue, the time-step kernel
+            "gpu_launches": (1 + 3 * (3 + 1) + 1) * args.steps, "clocks": clocks, "wall_s": wall,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         }
         print(json.dumps(line), flush=True)

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GBF_ABI_VERSION 5
+#define GBF_ABI_VERSION 6
 
 /* status codes */
 #define GBF_OK 0
@@ -253,18 +253,27 @@ int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspa
  * simulation_manager.py:536-1077, with compute_time_step_size,
  * time_integration/time_step_size.py:15-157, for the next step).
  * cons: double[5][Nx][Ny][Nz], advanced in place by `steps` steps.  Each
- * stage is one kernel: it builds the primitives of a tile plus its halo from
- * the conservatives (boundary conditions applied by index remapping), sweeps
- * x, y, z faces and applies the RK combination; the last stage also reduces
- * the next CFL time step.  dt_state: device double[4] = {dt, t, max_a, max_b}
- * (dt of the next step, simulation time, reduction slots); initialise with
- * gbf_rk3_init.  workspace: gbf_rk3_workspace_bytes(c) bytes of device memory
- * (two stage buffers).  No host synchronisation; graph-capturable.
+ * stage runs one face kernel per active axis (every face flux of the grid
+ * once, from the stage primitives, boundary conditions applied by index
+ * remapping) and one cell kernel (divergence, RK combination, the primitives
+ * of the new state; in the last stage the next CFL time step's reductions).
+ * prims: the interior primitives of cons (double[5][Nx][Ny][Nz]) for the first
+ * stage of this call, as the reference's first stage reads the primitives the
+ * state was initialised from (initialization/material_fields_initializer.py:
+ * 148-210); NULL derives them from cons.  dt_state: device double[4] = {dt, t,
+ * max_a, max_b} (dt of the next step, simulation time, reduction slots);
+ * initialise with gbf_rk3_init (prims as for gbf_rk3_advance: the initial
+ * time step from the initial primitives, time_control_initializer.py:34-70).
+ * workspace: gbf_rk3_workspace_bytes(c) bytes of device memory (the stage
+ * states U^1 and U^2 first, then two primitive buffers, the face fluxes of a
+ * stage and the Lax-Friedrichs speed slots).  No host synchronisation;
+ * graph-capturable.
  */
 size_t gbf_rk3_workspace_bytes(const gbf_case* c);
-int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream);
-int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
-                    const gbf_tile* tile, void* stream);
+int gbf_rk3_init(const gbf_case* c, const double* cons, const double* prims, double* dt_state, double t0,
+                 void* stream);
+int gbf_rk3_advance(const gbf_case* c, double* cons, const double* prims, double* dt_state, void* workspace,
+                    int steps, const gbf_tile* tile, void* stream);
 
 /*
  * One fused TVD-RK3 stage, for callers that drive the stage loop themselves
@@ -274,13 +283,13 @@ int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* wor
  * stage 1: out = 3/4 U^n + 1/4 U^1 + 1/4 dt L(U^1);
  * stage 2: out = 1/3 U^n + 2/3 U^2 + 2/3 dt L(U^2), then the next time step of
  * out is reduced into dt_state and the time advanced (three calls equal one
- * step of gbf_rk3_advance, bitwise).  out must not alias cons_k; at stage 2 it
- * may alias cons_n.  dt from dt_state[0] on the device.  prims_ws: 5 N doubles
- * of device memory for the stage primitives (viscous / heat cases; else may be
- * NULL).
+ * step of gbf_rk3_advance with prims NULL, bitwise).  out must not alias
+ * cons_k; at stage 2 it may alias cons_n.  dt from dt_state[0] on the device.
+ * workspace: gbf_rk3_workspace_bytes(c) bytes (the stage primitives and face
+ * fluxes are kept there).
  */
 int gbf_rk3_stage(const gbf_case* c, int stage, const double* cons_k, const double* cons_n, double* out,
-                  double* dt_state, double* prims_ws, const gbf_tile* tile, void* stream);
+                  double* dt_state, void* workspace, const gbf_tile* tile, void* stream);
 
 /*
  * Numerical health of an interior conservative state [5][N]: counts[0] cells
@@ -392,32 +401,23 @@ int gbf_batch_advance(const gbf_case* scheme, const gbf_batch_case* cases, int n
  * cudaMalloc: an XLA custom call, whose device memory must come from XLA's
  * allocator (which reserves most of the GPU up front); host code with a fixed
  * device-memory budget; loops that must not stall on cudaFree, which
- * synchronises the device.  The two stage buffers live in a fixed 32 MiB
- * device array inside the library (held by every GPU that loads it until the
- * process exits), so cases are limited to GBF_NOALLOC_MAX_CELLS interior
- * cells; larger cases return GBF_ERR_SIZE.  Same arguments and results as
- * gbf_rk3_advance without the workspace; cons and dt_state are the caller's
- * (initialise dt_state with gbf_rk3_init).  The first call on each device looks
- * up the array's device address with that device current; make that first
- * call before any stream capture.  All calls share the one array: calls whose
- * work overlaps on the GPU (other streams, other threads) race on it.
+ * synchronises the device.  The workspace of gbf_rk3_advance lives in a fixed
+ * GBF_NOALLOC_SCRATCH_BYTES (32 MiB) device array inside the library (held by
+ * every GPU that loads it until the process exits), so only cases with
+ * gbf_rk3_workspace_bytes(c) <= GBF_NOALLOC_SCRATCH_BYTES run (about 120 000
+ * interior cells in 3-D); larger cases return GBF_ERR_SIZE before any CUDA
+ * call.  Same arguments and results as gbf_rk3_advance with prims NULL and
+ * without the workspace; cons and dt_state are the caller's (initialise
+ * dt_state with gbf_rk3_init).  The first call on each device looks up the
+ * array's device address with that device current and caches it per device
+ * index; make that first call before any stream capture, and do not call it
+ * again on a device after cudaDeviceReset there (the cached address is stale).
+ * All calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other threads) race on it.
  */
-#define GBF_NOALLOC_MAX_CELLS 419430
+#define GBF_NOALLOC_SCRATCH_BYTES 33554432
 int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* dt_state, int steps,
                             const gbf_tile* tile, void* stream);
-
-/*
- * Measurement helper with no counterpart in the reference: runs `iters`
- * iterations of 8 independent dependency chains of one operation per thread
- * (blocks x threads threads) and stores one value per thread in out, so the
- * caller can time this GPU's arithmetic rates (FP64 fused multiply-add,
- * division, square root; FP32 fused multiply-add) for the roofline.
- */
-#define GBF_PROBE_DFMA 0
-#define GBF_PROBE_DDIV 1
-#define GBF_PROBE_DSQRT 2
-#define GBF_PROBE_FFMA 3
-int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ RECVAR = {"PRIMITIVE": 0, "CHAR-PRIMITIVE": 1, "CONSERVATIVE": 2, "CHAR-CONSERVA
 FROZEN = {"ARITHMETIC": 0, "ROE": 1}
 RIEMANN = {"LAX-FRIEDRICHS": 3, "HLLC": 0, "RUSANOV": 1, "HLL": 2}
 SIGNAL = {"EINFELDT": 0, "DAVIS": 1, "ARITHMETIC": 2, "RUSANOV": 3, "TORO": 4}
-ABI_VERSION = 5  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
+ABI_VERSION = 6  # GBF_ABI_VERSION of include/gbfluids.h (gbf_case layout)
 CENTRAL = {"CENTRAL4": 0, "CENTRAL2": 1}
 BC = {"PERIODIC": 0, "ZEROGRADIENT": 1, "SYMMETRY": 2, "WALL": 3, "DIRICHLET": 4, "NEUMANN": 5}
 BC_MIXED = 6  # a face of several types, per-cell types in bc_field_types
@@ -39,15 +39,16 @@ EXPORTS = (
     "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_rhs_cons", "gbf_halo_fill", "gbf_volume_force",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
-    "gbf_rk3_advance", "gbf_rk3_advance_noalloc", "gbf_probe_arith",
+    "gbf_rk3_advance", "gbf_rk3_advance_noalloc",
     "gbf_batch_workspace_bytes", "gbf_batch_init", "gbf_batch_advance",
     "gbf_vjp_workspace_bytes", "gbf_rhs_vjp", "gbf_rk3_step_vjp", "gbf_rk3_step_vjp_stages",
     "gbf_rk3_stage", "gbf_rk3_stage_vjp", "gbf_batch_worklist", "gbf_state_check",
     "gbf_create", "gbf_destroy", "gbf_solver_init", "gbf_solver_advance", "gbf_solver_time",
 )
 
-# interior cells the allocation-free entry point's built-in scratch holds
-NOALLOC_MAX_CELLS = 419430
+# bytes of the allocation-free entry point's built-in scratch
+# (GBF_NOALLOC_SCRATCH_BYTES): cases whose gbf_rk3_workspace_bytes fit run there
+NOALLOC_SCRATCH_BYTES = 33554432
 
 
 class GbfCase(ctypes.Structure):
@@ -118,10 +119,9 @@ def load() -> ctypes.CDLL:
         "gbf_dt_workspace_bytes": (ctypes.c_size_t, []),
         "gbf_dt": (I, [C, P, P, P, P]),
         "gbf_rk3_workspace_bytes": (ctypes.c_size_t, [C]),
-        "gbf_rk3_init": (I, [C, P, P, ctypes.c_double, P]),
-        "gbf_rk3_advance": (I, [C, P, P, P, I, T, P]),
+        "gbf_rk3_init": (I, [C, P, P, P, ctypes.c_double, P]),
+        "gbf_rk3_advance": (I, [C, P, P, P, P, I, T, P]),
         "gbf_rk3_advance_noalloc": (I, [C, P, P, I, T, P]),
-        "gbf_probe_arith": (I, [I, P, I, I, I, P]),
         "gbf_batch_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
         "gbf_vjp_workspace_bytes": (ctypes.c_size_t, [C]),
         "gbf_rhs_vjp": (I, [C, P, P, P, P, T, P]),

@@ -17,6 +17,10 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbfluids.so")
+# the benchmark's arithmetic-rate probe, a library of its own (not part of
+# the product library)
+PROBE_SRC = os.path.join(CSRC, "probe", "gbf_probe.cu")
+PROBE_LIB = os.path.join(PKG, "libgbfprobe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every FP64 operation rounds
@@ -43,8 +47,22 @@ def sources():
 
 
 def _deps():
-    return ([os.path.join(CSRC, f) for f in os.listdir(CSRC)] +
+    return ([os.path.join(CSRC, f) for f in os.listdir(CSRC) if os.path.isfile(os.path.join(CSRC, f))] +
             [os.path.join(ROOT, "include", "gbfluids.h"), os.path.abspath(__file__)])
+
+
+def build_probe(force: bool = False) -> str:
+    """libgbfprobe.so: the FP64 / FP32 rate probe the benchmark times."""
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= max(
+            os.path.getmtime(PROBE_SRC), os.path.getmtime(os.path.abspath(__file__))):
+        return PROBE_LIB
+    tmp = PROBE_LIB + ".tmp"
+    cmd = [_nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", tmp, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {PROBE_SRC}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
 
 
 def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:

@@ -586,8 +586,10 @@ extern "C" size_t gbf_vjp_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
   if (make_case_info(c, &ci) != GBF_OK || vjp_check(c) != GBF_OK) return 0;  // no adjoint for this case
   // step VJP: U1, U2, lam2, lam1, j, dP (6 interior states); dissipative
-  // cases add the primitives and the viscous face cotangents
-  return ((size_t)6 * 5 * (size_t)ci.cells + (size_t)vjp_extra_doubles(c, ci)) * sizeof(double);
+  // cases add the primitives and the viscous face cotangents; the forward
+  // recomputation of U1, U2 adds two primitive buffers and the face buffers
+  return ((size_t)8 * 5 * (size_t)ci.cells + (size_t)vjp_extra_doubles(c, ci) +
+          (size_t)stage_face_doubles(c, ci)) * sizeof(double);
 }
 
 static int gbf_rhs_vjp_impl(const gbf_case* c, const double* cons, const double* w, double* out,
@@ -630,23 +632,24 @@ static int step_vjp(const gbf_case* c, const double* cons, const double* u1_in, 
   const double* S1 = u1_in;
   const double* S2 = u2_in;
   if (!S1 || !S2) {
-    // recompute the stage states U1, U2 from U^n with the forward stage kernels
+    // recompute the stage states U1, U2 from U^n with the forward stage
+    // kernels (gbf_rk3_advance's stages 0 and 1)
     SweepParams p;
     int threads;
     size_t smem;
     if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
+    double* Pa = extra + vjp_extra_doubles(c, ci);
+    double* Pb = Pa + m;
+    FaceBuffers fb;
+    stage_face_buffers(c, ci, Pb + m, &fb);
     // the forward kernels read dt from dt_state[0]; dt points at a device scalar
     p.dt_state = const_cast<double*>(dt);
     p.reduce_dt = 0;
-    const bool diss = vjp_dissipative(c);
-    const int mode = diss ? MODE_STAGE_P : MODE_STAGE;
-    p.prims = extra;  // dissipative stages read the stage primitives
-    if (diss && (st = launch_convert(c, cons, extra, ci.cells, 1, s)) != GBF_OK) return st;
-    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = U1;
-    if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
-    if (diss && (st = launch_convert(c, U1, extra, ci.cells, 1, s)) != GBF_OK) return st;
-    p.stage = 1; p.cons = U1; p.cons0 = cons; p.out = U2;
-    if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
+    if ((st = launch_convert(c, cons, Pa, ci.cells, 1, s)) != GBF_OK) return st;
+    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = U1; p.prims = Pa;
+    if ((st = launch_rk3_stage(c, ci, tile, p, fb, Pb, s)) != GBF_OK) return st;
+    p.stage = 1; p.cons = U1; p.cons0 = cons; p.out = U2; p.prims = Pb;
+    if ((st = launch_rk3_stage(c, ci, tile, p, fb, nullptr, s)) != GBF_OK) return st;
     S1 = U1;
     S2 = U2;
   }

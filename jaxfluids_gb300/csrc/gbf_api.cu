@@ -112,6 +112,62 @@ int record_status(int status) {
 
 }  // namespace gbf
 
+namespace gbf {
+
+bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+
+// The fused steps on a workspace of gbf_rk3_workspace_bytes(c) bytes (shared
+// with the allocation-free entry point, gbf_noalloc.cu).  prims: the
+// primitives of cons for the first stage, or null (derived from cons).
+int rk3_advance_on(const gbf_case* c, double* cons, const double* prims, double* dt_state, double* workspace,
+                   int steps, const gbf_tile* tile, cudaStream_t s) {
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!cons || !dt_state || !workspace || steps < 0) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(cons) || !aligned8(workspace) || !aligned8(dt_state) || !aligned8(prims)) return GBF_ERR_ALIGNMENT;
+  SweepParams p;
+  int threads;
+  size_t smem;
+  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
+  if (st != GBF_OK) return st;
+  double* A = workspace;
+  double* B = A + 5 * ci.cells;
+  double* W[2] = {B + 5 * ci.cells, B + 10 * ci.cells};
+  FaceBuffers fb;
+  stage_face_buffers(c, ci, B + 15 * ci.cells, &fb);
+  unsigned long long* red = (unsigned long long*)(dt_state + 2);
+  p.dt_state = dt_state;
+  if (steps == 0) return GBF_OK;
+  // the primitives of U^n: the caller's, or derived once per call (every
+  // stage after that writes the primitives of its new state)
+  const double* Pn = prims;
+  int wn = -1;  // index of the W buffer holding Pn (-1: the caller's)
+  if (!Pn) {
+    if ((st = launch_convert(c, cons, W[0], ci.cells, 1, s)) != GBF_OK) return st;
+    Pn = W[0];
+    wn = 0;
+  }
+  for (int step = 0; step < steps; ++step) {
+    const int w1 = (wn == 1) ? 0 : 1, w2 = 1 - w1;
+    // U1 = U^n + dt L(U^n)
+    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = A; p.prims = Pn; p.reduce_dt = 0;
+    if ((st = launch_rk3_stage(c, ci, tile, p, fb, W[w1], s)) != GBF_OK) return st;
+    // U2 = 3/4 U^n + 1/4 U1 + 1/4 dt L(U1)
+    p.stage = 1; p.cons = A; p.out = B; p.prims = W[w1];
+    if ((st = launch_rk3_stage(c, ci, tile, p, fb, W[w2], s)) != GBF_OK) return st;
+    // U^{n+1} = 1/3 U^n + 2/3 U2 + 2/3 dt L(U2), written over U^n (read pointwise)
+    p.stage = 2; p.cons = B; p.out = cons; p.prims = W[w2]; p.reduce_dt = 1;
+    if ((st = launch_rk3_stage(c, ci, tile, p, fb, W[w1], s)) != GBF_OK) return st;
+    if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
+    Pn = W[w1];
+    wn = w1;
+  }
+  return GBF_OK;
+}
+
+}  // namespace gbf
+
 using namespace gbf;
 
 extern "C" {
@@ -142,7 +198,6 @@ int gbf_case_check(const gbf_case* c) {
   return record_status(gbf_case_check_impl(c));
 }
 
-static bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
 
 static int gbf_rhs_impl(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
   CaseInfo ci;
@@ -273,18 +328,17 @@ int gbf_dt(const gbf_case* c, const double* prims, double* dt_out, void* workspa
   return record_status(gbf_dt_impl(c, prims, dt_out, workspace, stream));
 }
 
-static bool dissipative(const gbf_case* c) { return (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0; }
-
+// Fused-path workspace: the stage buffers A, B (U^1, U^2), two primitive
+// buffers (the stage primitives, alternating) and the face buffers of a stage.
 size_t gbf_rk3_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
   if (make_case_info(c, &ci) != GBF_OK) return 0;
-  // two stage buffers, plus the stage primitives for the dissipative fluxes
-  const size_t states = dissipative(c) ? 3 : 2;
-  return states * 5 * (size_t)ci.cells * sizeof(double);
+  return ((size_t)4 * 5 * (size_t)ci.cells + (size_t)stage_face_doubles(c, ci)) * sizeof(double);
 }
 
 // dt_state = {dt, t, max signal speed bits, min density bits}
-static int gbf_rk3_init_impl(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
+static int gbf_rk3_init_impl(const gbf_case* c, const double* cons, const double* prims, double* dt_state,
+                             double t0, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
@@ -293,69 +347,28 @@ static int gbf_rk3_init_impl(const gbf_case* c, const double* cons, double* dt_s
   if ((st = launch_set_scalar(dt_state + 1, t0, s)) != GBF_OK) return st;
   unsigned long long* red = (unsigned long long*)(dt_state + 2);
   if ((st = launch_reduce_init(red, s)) != GBF_OK) return st;
-  if ((st = launch_reduce_cons(ci, cons, red, s)) != GBF_OK) return st;
+  // the initial time step from the primitives the state was built from
+  // (time_control_initializer.py:34-70), else from the conservatives
+  st = prims ? launch_reduce_prims(ci, prims, red, s) : launch_reduce_cons(ci, cons, red, s);
+  if (st != GBF_OK) return st;
   return launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 0, s);
 }
 
-int gbf_rk3_init(const gbf_case* c, const double* cons, double* dt_state, double t0, void* stream) {
-  return record_status(gbf_rk3_init_impl(c, cons, dt_state, t0, stream));
+int gbf_rk3_init(const gbf_case* c, const double* cons, const double* prims, double* dt_state, double t0,
+                 void* stream) {
+  return record_status(gbf_rk3_init_impl(c, cons, prims, dt_state, t0, stream));
 }
 
-static int gbf_rk3_advance_impl(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
-                    const gbf_tile* tile, void* stream) {
-  CaseInfo ci;
-  int st = check_case(c, &ci);
-  if (st != GBF_OK) return st;
-  if (!cons || !dt_state || !workspace || steps < 0) return GBF_ERR_INVALID_ARGUMENT;
-  if (!aligned8(cons) || !aligned8(workspace) || !aligned8(dt_state)) return GBF_ERR_ALIGNMENT;
-  SweepParams p;
-  int threads;
-  size_t smem;
-  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
-  if (st != GBF_OK) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  double* A = (double*)workspace;
-  double* B = A + 5 * ci.cells;
-  unsigned long long* red = (unsigned long long*)(dt_state + 2);
-  p.dt_state = dt_state;
-  if (dissipative(c)) {
-    // per stage: primitives of the stage state once, then the fused sweep
-    double* Pk = B + 5 * ci.cells;
-    p.prims = Pk;
-    const double* stage_in[3] = {cons, A, B};
-    double* stage_out[3] = {A, B, cons};
-    for (int step = 0; step < steps; ++step) {
-      for (int stage = 0; stage < 3; ++stage) {
-        if ((st = launch_convert(c, stage_in[stage], Pk, ci.cells, 1, s)) != GBF_OK) return st;
-        p.stage = stage;
-        p.cons = stage_in[stage];
-        p.cons0 = cons;
-        p.out = stage_out[stage];
-        p.reduce_dt = (stage == 2);
-        if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE_P)) != GBF_OK) return st;
-      }
-      if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
-    }
-    return GBF_OK;
-  }
-  for (int step = 0; step < steps; ++step) {
-    // U1 = U^n + dt L(U^n)
-    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = A; p.reduce_dt = 0;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    // U2 = 3/4 U^n + 1/4 U1 + 1/4 dt L(U1)
-    p.stage = 1; p.cons = A; p.cons0 = cons; p.out = B;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    // U^{n+1} = 1/3 U^n + 2/3 U2 + 2/3 dt L(U2), written over U^n (read pointwise)
-    p.stage = 2; p.cons = B; p.cons0 = cons; p.out = cons; p.reduce_dt = 1;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
-  }
-  return GBF_OK;
+
+static int gbf_rk3_advance_impl(const gbf_case* c, double* cons, const double* prims, double* dt_state,
+                                void* workspace, int steps, const gbf_tile* tile, void* stream) {
+  if (!c || !workspace) return GBF_ERR_INVALID_ARGUMENT;
+  return rk3_advance_on(c, cons, prims, dt_state, (double*)workspace, steps, tile, (cudaStream_t)stream);
 }
 
-int gbf_rk3_advance(const gbf_case* c, double* cons, double* dt_state, void* workspace, int steps,
-                    const gbf_tile* tile, void* stream) {
-  return record_status(gbf_rk3_advance_impl(c, cons, dt_state, workspace, steps, tile, stream));
+int gbf_rk3_advance(const gbf_case* c, double* cons, const double* prims, double* dt_state, void* workspace,
+                    int steps, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_advance_impl(c, cons, prims, dt_state, workspace, steps, tile, stream));
 }
 
 static int gbf_state_check_impl(const gbf_case* c, const double* cons, uint64_t* counts, void* stream) {
@@ -374,34 +387,36 @@ int gbf_state_check(const gbf_case* c, const double* cons, uint64_t* counts, voi
 }
 
 static int gbf_rk3_stage_impl(const gbf_case* c, int stage, const double* cons_k, const double* cons_n,
-                              double* out, double* dt_state, double* prims_ws, const gbf_tile* tile,
+                              double* out, double* dt_state, void* workspace, const gbf_tile* tile,
                               void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
-  if (stage < 0 || stage > 2 || !cons_k || !cons_n || !out || !dt_state) return GBF_ERR_INVALID_ARGUMENT;
-  if (out == cons_k) return GBF_ERR_INVALID_ARGUMENT;  // the sweep reads neighbours of U^k
+  if (stage < 0 || stage > 2 || !cons_k || !cons_n || !out || !dt_state || !workspace)
+    return GBF_ERR_INVALID_ARGUMENT;
+  if (out == cons_k) return GBF_ERR_INVALID_ARGUMENT;  // the faces read neighbours of U^k
   if (stage == 0 && cons_k != cons_n) return GBF_ERR_INVALID_ARGUMENT;
-  if (dissipative(c) && !prims_ws) return GBF_ERR_INVALID_ARGUMENT;
-  if (!aligned8(cons_k) || !aligned8(cons_n) || !aligned8(out) || !aligned8(dt_state)) return GBF_ERR_ALIGNMENT;
+  if (!aligned8(cons_k) || !aligned8(cons_n) || !aligned8(out) || !aligned8(dt_state) || !aligned8(workspace))
+    return GBF_ERR_ALIGNMENT;
   SweepParams p;
   int threads;
   size_t smem;
   if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  // workspace as gbf_rk3_advance's: the stage primitives in the first
+  // primitive buffer, the face buffers behind them
+  double* Pk = (double*)workspace + 10 * ci.cells;
+  FaceBuffers fb;
+  stage_face_buffers(c, ci, (double*)workspace + 20 * ci.cells, &fb);
+  if ((st = launch_convert(c, cons_k, Pk, ci.cells, 1, s)) != GBF_OK) return st;
   p.dt_state = dt_state;
   p.stage = stage;
   p.cons = cons_k;
   p.cons0 = cons_n;
   p.out = out;
+  p.prims = Pk;
   p.reduce_dt = (stage == 2);
-  int mode = MODE_STAGE;
-  if (dissipative(c)) {
-    if ((st = launch_convert(c, cons_k, prims_ws, ci.cells, 1, s)) != GBF_OK) return st;
-    p.prims = prims_ws;
-    mode = MODE_STAGE_P;
-  }
-  if ((st = launch_sweep(c, p, threads, smem, s, mode)) != GBF_OK) return st;
+  if ((st = launch_rk3_stage(c, ci, tile, p, fb, nullptr, s)) != GBF_OK) return st;
   if (stage != 2) return GBF_OK;
   // the step is complete: next time step from the new state, time advanced
   unsigned long long* red = (unsigned long long*)(dt_state + 2);
@@ -409,8 +424,8 @@ static int gbf_rk3_stage_impl(const gbf_case* c, int stage, const double* cons_k
 }
 
 int gbf_rk3_stage(const gbf_case* c, int stage, const double* cons_k, const double* cons_n, double* out,
-                  double* dt_state, double* prims_ws, const gbf_tile* tile, void* stream) {
-  return record_status(gbf_rk3_stage_impl(c, stage, cons_k, cons_n, out, dt_state, prims_ws, tile, stream));
+                  double* dt_state, void* workspace, const gbf_tile* tile, void* stream) {
+  return record_status(gbf_rk3_stage_impl(c, stage, cons_k, cons_n, out, dt_state, workspace, tile, stream));
 }
 
 }  // extern "C"

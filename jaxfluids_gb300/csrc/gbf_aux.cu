@@ -242,7 +242,7 @@ struct ReduceParams {
   long long cells;
   double gamma;
   double gm1;
-  int from_cons;  // 1: interior conservative buffer, 0: halo primitive buffer
+  int from_cons;  // 1: interior conservative buffer, 0: halo primitive buffer, 2: interior primitives
 };
 
 // time_step_size.py:96-109: max over interior cells of sum_active(|u_i| + c);
@@ -254,7 +254,10 @@ __global__ void reduce_kernel(const ReduceParams rp, const double* buf, unsigned
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rp.cells;
        i += (long long)gridDim.x * blockDim.x) {
     double P[5];
-    if (rp.from_cons) {
+    if (rp.from_cons == 2) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) P[v] = buf[v * rp.cells + i];
+    } else if (rp.from_cons) {
       double U[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) U[v] = buf[v * rp.cells + i];
@@ -507,6 +510,10 @@ int launch_state_check(const CaseInfo& ci, const double* cons, unsigned long lon
 int launch_reduce_cons(const CaseInfo& ci, const double* cons, unsigned long long* red,
                        cudaStream_t s) {
   return launch_reduce(ci, cons, red, 1, s);
+}
+
+int launch_reduce_prims(const CaseInfo& ci, const double* prims, unsigned long long* red, cudaStream_t s) {
+  return launch_reduce(ci, prims, red, 2, s);
 }
 
 int launch_dt_finalize(const gbf_case* c, const CaseInfo& ci, unsigned long long* red,

@@ -1,0 +1,124 @@
+// The fused TVD-RK3 stage as per-axis face kernels plus one cell epilogue.
+//
+// A stage of the hot path computes every face flux of the grid exactly once.
+// For each active axis a face kernel covers the faces along that axis with
+// tiles of faces (16 along the axis, the rest across it; the contiguous axis
+// widest), stages the primitives of the tile's stencil cells in shared memory
+// (from the stage's primitive buffer, boundary conditions by index remap) and
+// writes the face fluxes to a face buffer of that axis.  The epilogue kernel
+// (stage_epilogue_kernel, gbf_stage.cu) then forms, per cell, the divergence
+// in the reference's axis order, the RK stage combination, the primitives of
+// the new state (the next stage's input, simulation_manager.py:943-944) and,
+// in the last stage, the next CFL time step's reductions.
+//
+// Against a fused 3-D tile that sweeps all axes in shared memory, this drops
+// the duplicated faces on tile boundaries ((T + 1) / T per axis, 12.5 % of
+// the face work of 8^3 tiles) and the per-pencil conservative-to-primitive
+// conversions (about five per cell and stage): the path is bound by FP64
+// arithmetic, and the face buffers cost HBM bytes, which are not the bound.
+// The face and cell arithmetic is the tile kernel's (face_flux, the same
+// divergence and RK expressions), so both give bitwise equal results.
+//
+// Faces of an axis: N + 1 per line, N on a PERIODIC axis, whose face N - 1/2
+// has the stencil of face -1/2 after the periodic wrap (the epilogue reads
+// face 0 for it).
+#pragma once
+
+#include "gbf_sweep.cuh"
+
+namespace gbf {
+
+// Face tile of one face kernel: t[AX] faces along the axis, t[b] cells across
+// it; tiles[] per axis; nf faces along AX per line.
+struct FaceTile {
+  int t[3];
+  int tiles[3];
+  int nf;
+};
+
+// Face buffers of a stage: flux[a][v * faces_a + face], faces of axis a laid
+// out [E0][E1][E2] with E_a = nf[a] and the other extents the cell counts;
+// lf_alpha: the Lax-Friedrichs speed slots (3 doubles of the same workspace).
+struct FaceBuffers {
+  double* flux[3];
+  int nf[3];
+  double* lf_alpha;
+};
+
+// One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
+// Reads the stage primitives p.prims (and, for the conservative
+// reconstructions, the stage conservatives p.cons), MODE_STAGE_P semantics.
+template <int AX, int RECON, int RIEMANN, int VISC>
+__global__ void __launch_bounds__(256, 2) face_flux_kernel(const SweepParams p, const FaceTile ft,
+                                                           const FaceBuffers fb) {
+  extern __shared__ double smem[];
+  constexpr int R = ReconTraits<RECON>::R;
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
+  const int b = blockIdx.x;
+  const int b2 = b % ft.tiles[2];
+  const int b1 = (b / ft.tiles[2]) % ft.tiles[1];
+  const int b0 = b / (ft.tiles[2] * ft.tiles[1]);
+  const int o[3] = {b0 * ft.t[0], b1 * ft.t[1], b2 * ft.t[2]};
+  int fe[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) fe[a] = min(ft.t[a], ((a == AX) ? ft.nf : p.n[a]) - o[a]);
+  // pencil: the stencil cells of the tile's faces, o[AX] - R .. o[AX] + fe[AX] - 2 + R
+  int pe[3] = {fe[0], fe[1], fe[2]};
+  pe[AX] += 2 * R - 1;
+  const int pvol = pe[0] * pe[1] * pe[2];
+  if (RIEMANN != RIEMANN_NONE) {
+    stage_pencil<AX, R, MODE_STAGE_P, CONS>(p, o, pe, pvol, smem);
+    __syncthreads();
+  }
+  const int fvol = fe[0] * fe[1] * fe[2];
+  const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
+  int ext[3] = {p.n[0], p.n[1], p.n[2]};
+  ext[AX] = ft.nf;
+  const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
+  double* out = fb.flux[AX];
+  double smax_faces = 0.0;
+  for (int f = threadIdx.x; f < fvol; f += blockDim.x) {
+    const int f2 = f % fe[2];
+    const int r = f / fe[2];
+    const int f1 = r % fe[1];
+    const int f0 = r / fe[1];
+    const int base = idx3(f0, f1, f2, pe[1], pe[2]);
+    const int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
+    double F[5];
+    if (!face_flux<AX, RECON, RIEMANN, MODE_STAGE_P, VISC>(p, smem, pvol, pstride, base, q, F, smax_faces))
+      continue;
+    const long long g = ((long long)q[0] * ext[1] + q[1]) * ext[2] + q[2];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v * nfaces + g] = F[v];
+  }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) lf_speed_reduce<AX>(p, smax_faces);
+}
+
+// Host side ------------------------------------------------------------------
+
+// Launch the face kernel of axis `axis` for one scheme (instantiated per
+// scheme family in gbf_faces_<family>.cu).
+template <int RECON, int RIEMANN, int VISC>
+int launch_faces_one(int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb, int threads,
+                     size_t smem, cudaStream_t s) {
+  const int grid = ft.tiles[0] * ft.tiles[1] * ft.tiles[2];
+  auto go = [&](auto kern) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return GBF_ERR_CUDA;
+    kern<<<grid, threads, smem, s>>>(p, ft, fb);
+    return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+  };
+  if (axis == 0) return go(face_flux_kernel<0, RECON, RIEMANN, VISC>);
+  if (axis == 1) return go(face_flux_kernel<1, RECON, RIEMANN, VISC>);
+  return go(face_flux_kernel<2, RECON, RIEMANN, VISC>);
+}
+
+template <int RECON, int VISC>
+int launch_faces_riemann(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+                         int threads, size_t smem, cudaStream_t s) {
+  if (riemann == GBF_RIEMANN_HLLC) return launch_faces_one<RECON, GBF_RIEMANN_HLLC, VISC>(axis, p, ft, fb, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLL) return launch_faces_one<RECON, GBF_RIEMANN_HLL, VISC>(axis, p, ft, fb, threads, smem, s);
+  return launch_faces_one<RECON, GBF_RIEMANN_RUSANOV, VISC>(axis, p, ft, fb, threads, smem, s);
+}
+
+}  // namespace gbf

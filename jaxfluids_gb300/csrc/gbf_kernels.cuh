@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "gbf_faces.cuh"
 #include "gbf_sweep.cuh"
 
 namespace gbf {
@@ -39,6 +40,26 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
 int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem,
                  cudaStream_t s, int mode);
 
+// The Lax-Friedrichs speed slots of the current device (gbf_sweep.cu).
+int lf_alpha_on_current_device(double** out);
+
+// The fused RK stage (gbf_stage.cu): doubles of the three face buffers (and
+// the Lax-Friedrichs speed slots), their layout in a block of that size, and
+// one stage (p: prims, cons, cons0, out,
+// stage, reduce_dt, dt_state; prims_out, may be null, receives the primitives
+// of the new state).
+long long stage_face_doubles(const gbf_case* c, const CaseInfo& ci);
+void stage_face_buffers(const gbf_case* c, const CaseInfo& ci, double* base, FaceBuffers* fb);
+int launch_rk3_stage(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
+                     const FaceBuffers& fb, double* prims_out, cudaStream_t s);
+
+// The fused RK3 steps on a caller-provided workspace of
+// gbf_rk3_workspace_bytes(c) bytes (gbf_api.cu); prims: the primitives of
+// cons for the first stage, or null.
+int rk3_advance_on(const gbf_case* c, double* cons, const double* prims, double* dt_state, double* workspace,
+                   int steps, const gbf_tile* tile, cudaStream_t s);
+bool aligned8(const void* p);
+
 // auxiliary kernels (gbf_aux.cu)
 // rhs[1:5] += gravity forces of the interior of the halo-buffer conservatives
 int launch_volume_force(const gbf_case* c, const CaseInfo& ci, const double* cons, double* rhs, cudaStream_t s);
@@ -61,6 +82,8 @@ int launch_reduce_halo_prims(const CaseInfo& ci, const double* prims, unsigned l
 int launch_state_check(const CaseInfo& ci, const double* cons, unsigned long long* counts, cudaStream_t s);
 int launch_reduce_cons(const CaseInfo& ci, const double* cons, unsigned long long* red,
                        cudaStream_t s);
+// the same reduction from an interior primitive buffer
+int launch_reduce_prims(const CaseInfo& ci, const double* prims, unsigned long long* red, cudaStream_t s);
 // dt from reduction slots; when advance_time, dt_state[1] += previous dt first
 int launch_dt_finalize(const gbf_case* c, const CaseInfo& ci, unsigned long long* red,
                        double* dt_out, double* t_inout, int advance_time, cudaStream_t s);

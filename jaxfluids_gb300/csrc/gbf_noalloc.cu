@@ -9,19 +9,21 @@
 //   * host code with a fixed device-memory budget (a solver embedded in a
 //     larger application) that forbids allocations it does not account for;
 //   * host loops that must not stall: cudaFree synchronises the whole device.
-// For them, the two RK3 stage buffers live in a fixed device array compiled
-// into this library.  The array is modest (GBF_NOALLOC_MAX_CELLS cells, 32 MiB)
-// and every GPU that loads the library holds it until the process exits.
+// For them, the RK3 workspace (stage states, stage primitives, face fluxes)
+// lives in a fixed device array compiled into this library.  The array is
+// modest (GBF_NOALLOC_SCRATCH_BYTES, 32 MiB) and every GPU that loads the
+// library holds it until the process exits.
 #include <mutex>
 
 #include "gbf_kernels.cuh"
 
 namespace {
 
-constexpr size_t kStateDoubles = (size_t)5 * GBF_NOALLOC_MAX_CELLS;
+constexpr size_t kScratchDoubles = (size_t)GBF_NOALLOC_SCRATCH_BYTES / sizeof(double);
 
-// Two stage buffers of up to GBF_NOALLOC_MAX_CELLS cells (5 doubles each).
-static __device__ __align__(256) double g_rk3_stage_scratch[2 * kStateDoubles];
+// The workspace of gbf_rk3_advance for cases whose gbf_rk3_workspace_bytes
+// fits in GBF_NOALLOC_SCRATCH_BYTES.
+static __device__ __align__(256) double g_rk3_stage_scratch[kScratchDoubles];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
@@ -52,35 +54,18 @@ static int gbf_rk3_advance_noalloc_impl(const gbf_case* c, double* cons, double*
                                        const gbf_tile* tile, void* stream) {
   int st = gbf_case_check(c);
   if (st != GBF_OK) return st;
-  CaseInfo ci;
-  if ((st = make_case_info(c, &ci)) != GBF_OK) return st;
-  if (ci.cells > (long long)GBF_NOALLOC_MAX_CELLS) return GBF_ERR_SIZE;  // beyond the built-in scratch
+  // beyond the built-in scratch: refused before any CUDA call
+  if (gbf_rk3_workspace_bytes(c) > (size_t)GBF_NOALLOC_SCRATCH_BYTES) return GBF_ERR_SIZE;
   if (!cons || !dt_state || steps < 0) return GBF_ERR_INVALID_ARGUMENT;
   if (((uintptr_t)cons & 7u) || ((uintptr_t)dt_state & 7u)) return GBF_ERR_ALIGNMENT;
-  SweepParams p;
-  int threads;
-  size_t smem;
-  if ((st = make_sweep_params(c, ci, tile, &p, &threads, &smem)) != GBF_OK) return st;
   double* scratch = nullptr;
   if ((st = scratch_on_current_device(&scratch)) != GBF_OK) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  // Stage buffers packed at the start of the array for this case's size.  Each
-  // stage writes its whole buffer before the next stage reads it, so nothing
-  // left over from an earlier call is ever read and nothing needs clearing.
-  double* A = scratch;
-  double* B = scratch + 5 * ci.cells;
-  unsigned long long* red = (unsigned long long*)(dt_state + 2);
-  p.dt_state = dt_state;
-  for (int step = 0; step < steps; ++step) {
-    p.stage = 0; p.cons = cons; p.cons0 = cons; p.out = A; p.reduce_dt = 0;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    p.stage = 1; p.cons = A; p.cons0 = cons; p.out = B;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    p.stage = 2; p.cons = B; p.cons0 = cons; p.out = cons; p.reduce_dt = 1;
-    if ((st = launch_sweep(c, p, threads, smem, s, MODE_STAGE)) != GBF_OK) return st;
-    if ((st = launch_dt_finalize(c, ci, red, dt_state, dt_state + 1, 1, s)) != GBF_OK) return st;
-  }
-  return GBF_OK;
+  // The workspace is packed at the start of the array for this case's size.
+  // Every buffer in it is written before it is read within a call (the stage
+  // primitives are derived from cons first, each stage writes its whole state,
+  // primitives and face fluxes, the Lax-Friedrichs slots are cleared per
+  // stage), so nothing left over from an earlier call is ever read.
+  return rk3_advance_on(c, cons, nullptr, dt_state, scratch, steps, tile, (cudaStream_t)stream);
 }
 
 extern "C" int gbf_rk3_advance_noalloc(const gbf_case* c, double* cons, double* dt_state, int steps,

@@ -59,12 +59,12 @@ int solver_destroy(gbf_solver* s) {
 
 int solver_init(gbf_solver* s, const double* cons, double t0, void* stream) {
   if (!s) return GBF_ERR_INVALID_ARGUMENT;
-  return gbf_rk3_init(&s->c, cons, s->dt_state, t0, stream);
+  return gbf_rk3_init(&s->c, cons, nullptr, s->dt_state, t0, stream);
 }
 
 int solver_advance(gbf_solver* s, double* cons, int steps, void* stream) {
   if (!s) return GBF_ERR_INVALID_ARGUMENT;
-  return gbf_rk3_advance(&s->c, cons, s->dt_state, s->workspace, steps, s->has_tile ? &s->tile : nullptr,
+  return gbf_rk3_advance(&s->c, cons, nullptr, s->dt_state, s->workspace, steps, s->has_tile ? &s->tile : nullptr,
                          stream);
 }
 

@@ -1,0 +1,269 @@
+// One fused TVD-RK3 stage on interior buffers: the face kernels of every
+// active axis (gbf_faces.cuh), then the cell epilogue.  Used by the fused
+// stepping (gbf_rk3_advance, gbf_rk3_stage, the allocation-free variant) and
+// by the adjoint's recomputation of stage states.
+#include <algorithm>
+
+#include "gbf_sweep_launch.cuh"
+
+namespace gbf {
+
+namespace {
+
+// The cell epilogue of a stage: rhs = ((0 + d_x) + d_y) + d_z with
+// d_a = (1/dx_a)(F[i - 1/2] - F[i + 1/2]) (space_solver.py:266-314, :597-599),
+// gravity (space_solver.py:377-384), the RK combination (RK3.py:27-62,
+// time_integrator.py:34-58) into p.out, the primitives of the new state into
+// prims_out, and (p.reduce_dt) the maximum signal speed and minimum density
+// of the new state (time_step_size.py:96-109).
+__global__ void __launch_bounds__(256) stage_epilogue_kernel(const SweepParams p, const FaceBuffers fb,
+                                                             double* prims_out) {
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const double dt = p.dt_state[0];
+  double smax = 0.0;
+  double rmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int c2 = (int)(i % p.n[2]);
+    const long long r = i / p.n[2];
+    const int c1 = (int)(r % p.n[1]);
+    const int c0 = (int)(r / p.n[1]);
+    const int c[3] = {c0, c1, c2};
+    double acc[5];
+    bool first = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (!(p.active_mask & (1 << a))) continue;
+      int ext[3] = {p.n[0], p.n[1], p.n[2]};
+      ext[a] = fb.nf[a];
+      const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
+      int lo[3] = {c0, c1, c2};
+      const long long flo = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
+      lo[a] = (c[a] + 1 == fb.nf[a]) ? 0 : c[a] + 1;  // periodic: face N - 1/2 is face -1/2
+      const long long fhi = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
+      const double* F = fb.flux[a];
+      const double odx = p.one_dx[a];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double d = odx * (F[v * nfaces + flo] - F[v * nfaces + fhi]);
+        acc[v] = first ? d : __dadd_rn(acc[v], d);
+      }
+      first = false;
+    }
+    double U[5], Un[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + i];
+    if (p.gravity) add_gravity(acc, U, p.g);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double U0 = (p.stage == 0) ? U[v] : p.cons0[v * cs + i];
+      Un[v] = rk3_combine(p.stage, U[v], U0, acc[v], dt);
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) p.out[v * cs + i] = Un[v];
+    if (!prims_out && !p.reduce_dt) continue;
+    double P[5];
+    prims_from_cons(Un, P, p.fp.gm1);
+    if (prims_out) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) prims_out[v * cs + i] = P[v];
+    }
+    if (p.reduce_dt) {
+      const double cc = speed_of_sound(P[4], P[0], p.fp);
+      double s = 0.0;
+      if (p.active_mask & 1) s = s + (fabs(P[1]) + cc);
+      if (p.active_mask & 2) s = s + (fabs(P[2]) + cc);
+      if (p.active_mask & 4) s = s + (fabs(P[3]) + cc);
+      smax = fmax(smax, s);
+      rmin = fmin(rmin, P[0]);
+    }
+  }
+  if (!p.reduce_dt) return;
+  // warp shuffle -> shared -> one atomic per CTA; max/min are exact
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+    rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+  }
+  __shared__ double red[2][32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = smax;
+    red[1][w] = rmin;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = blockDim.x >> 5;
+    smax = (threadIdx.x < nw) ? red[0][threadIdx.x] : 0.0;
+    rmin = (threadIdx.x < nw) ? red[1][threadIdx.x] : __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+    }
+    if (threadIdx.x == 0) {
+      atomicMax(reinterpret_cast<unsigned long long*>(p.dt_state + 2), ordered_bits(smax));
+      atomicMin(reinterpret_cast<unsigned long long*>(p.dt_state + 3), ordered_bits(rmin));
+    }
+  }
+}
+
+bool periodic_axis(const gbf_case* c, int a) { return c->bc[2 * a] == GBF_BC_PERIODIC; }
+
+// Face tile of the face kernel of `axis`: 16 faces along the axis and, across
+// it, 32 cells (2-D) or 2 x 16 cells with the contiguous axis widest (3-D);
+// 256 faces along the axis in 1-D.  A user tile (gbf_tile) gives the extents
+// of every face kernel directly.
+int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, FaceTile* ft, int* threads) {
+  int t[3] = {1, 1, 1};
+  int thr = 256;
+  const bool user = tile && (tile->t[0] > 0 || tile->t[1] > 0 || tile->t[2] > 0);
+  if (user) {
+    for (int a = 0; a < 3; ++a) t[a] = std::max(1, tile->t[a]);
+    if (tile->threads > 0) thr = tile->threads;
+  } else {
+    int others[2], k = 0;
+    for (int a = 0; a < 3; ++a)
+      if (a != axis && (ci.active_mask & (1 << a))) others[k++] = a;
+    t[axis] = (k == 0) ? 256 : 16;
+    if (k == 1) t[others[0]] = 32;
+    if (k == 2) {
+      t[others[0]] = 2;
+      t[others[1]] = 16;
+    }
+  }
+  if (thr % 32 != 0 || thr < 32 || thr > 256) return GBF_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; ++a) {
+    const int ext = (a == axis) ? nf : ci.n[a];
+    if (ci.n[a] == 1) t[a] = 1;
+    t[a] = std::min(t[a], ext);
+    ft->t[a] = t[a];
+    ft->tiles[a] = (ext + t[a] - 1) / t[a];
+  }
+  ft->nf = nf;
+  *threads = thr;
+  return GBF_OK;
+}
+
+size_t face_smem(const gbf_case* c, const FaceTile& ft, int axis) {
+  const int R = recon_radius(c->recon);
+  long long pv = 1;
+  for (int b = 0; b < 3; ++b) pv *= ft.t[b] + (b == axis ? 2 * R - 1 : 0);
+  const bool cons_pencil =
+      c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
+  return (size_t)(cons_pencil ? 10 : 5) * pv * sizeof(double);
+}
+
+// The face kernel of the case's scheme family (as launch_sweep_schemes picks
+// the tile kernel's).
+int launch_faces(const gbf_case* c, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+                 int threads, size_t smem, cudaStream_t s) {
+  const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
+  const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
+  const bool cons = c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
+  const int r = c->riemann;
+  if (cons && !(c->flags & GBF_FLAG_NO_CONVECTIVE)) {
+    if (c->recon_var == GBF_RECVAR_CONSERVATIVE)
+      return visc ? launch_faces_cons_visc(r, axis, p, ft, fb, threads, smem, s)
+                  : launch_faces_cons(r, axis, p, ft, fb, threads, smem, s);
+    return visc ? launch_faces_charcons_visc(r, axis, p, ft, fb, threads, smem, s)
+                : launch_faces_charcons(r, axis, p, ft, fb, threads, smem, s);
+  }
+  if (visc) {
+    if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_faces_dissipative(axis, p, ft, fb, threads, smem, s);
+    const bool c4 = c->dissipative_stencil[0] == GBF_CENTRAL4 && c->dissipative_stencil[1] == GBF_CENTRAL4 &&
+                    c->dissipative_stencil[2] == GBF_CENTRAL4;
+    if (chr)
+      return c4 ? launch_faces_char_visc_c4(r, axis, p, ft, fb, threads, smem, s)
+                : launch_faces_char_visc(r, axis, p, ft, fb, threads, smem, s);
+    switch (c->recon) {
+      case GBF_RECON_WENO5Z:
+        return c4 ? launch_faces_weno_visc_c4(r, axis, p, ft, fb, threads, smem, s)
+                  : launch_faces_weno_visc(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO5JS: return launch_faces_weno5js_visc(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_TENO5: return launch_faces_teno5_visc(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO3JS: return launch_faces_visc_weno3js(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO3Z: return launch_faces_visc_weno3z(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_MINMOD: return launch_faces_visc_minmod(r, axis, p, ft, fb, threads, smem, s);
+      case GBF_RECON_MINMOD_AD: return launch_faces_visc_minmod_ad(r, axis, p, ft, fb, threads, smem, s);
+      default: return GBF_ERR_UNSUPPORTED;
+    }
+  }
+  if (chr) return launch_faces_char(r, axis, p, ft, fb, threads, smem, s);
+  switch (c->recon) {
+    case GBF_RECON_WENO5Z: return launch_faces_weno(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO5JS: return launch_faces_weno5js(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_TENO5: return launch_faces_teno5(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO3JS: return launch_faces_weno3js(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO3Z: return launch_faces_weno3z(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_MINMOD: return launch_faces_minmod(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_MINMOD_AD: return launch_faces_minmod_ad(r, axis, p, ft, fb, threads, smem, s);
+    default: return GBF_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace
+
+// The face buffers plus 4 doubles: the Lax-Friedrichs speed slots (3) and padding.
+long long stage_face_doubles(const gbf_case* c, const CaseInfo& ci) {
+  long long total = 4;
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a))) continue;
+    long long f = periodic_axis(c, a) ? ci.n[a] : ci.n[a] + 1;
+    for (int b = 0; b < 3; ++b)
+      if (b != a) f *= ci.n[b];
+    total += 5 * f;
+  }
+  return total;
+}
+
+void stage_face_buffers(const gbf_case* c, const CaseInfo& ci, double* base, FaceBuffers* fb) {
+  for (int a = 0; a < 3; ++a) {
+    fb->flux[a] = nullptr;
+    fb->nf[a] = 0;
+    if (!(ci.active_mask & (1 << a))) continue;
+    fb->nf[a] = periodic_axis(c, a) ? ci.n[a] : ci.n[a] + 1;
+    long long f = fb->nf[a];
+    for (int b = 0; b < 3; ++b)
+      if (b != a) f *= ci.n[b];
+    fb->flux[a] = base;
+    base += 5 * f;
+  }
+  fb->lf_alpha = base;
+}
+
+// p carries the stage: prims (primitives of p.cons), cons, cons0, out, stage,
+// reduce_dt, dt_state.  prims_out (may be null) receives the primitives of
+// the new state.  Lax-Friedrichs runs a speed pass of each axis' face kernel
+// before its flux pass (LaxFriedrichs.py:25-47).
+int launch_rk3_stage(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
+                     const FaceBuffers& fb, double* prims_out, cudaStream_t s) {
+  const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+  SweepParams q = p;
+  int st;
+  if (lf) {
+    q.lf_alpha = fb.lf_alpha;
+    if (!q.lf_alpha) return GBF_ERR_INVALID_ARGUMENT;
+    if (cudaMemsetAsync(q.lf_alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
+  }
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a))) continue;
+    FaceTile ft;
+    int threads;
+    if ((st = make_face_tile(ci, tile, a, fb.nf[a], &ft, &threads)) != GBF_OK) return st;
+    const size_t smem = face_smem(c, ft, a);
+    if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+    if (lf) {
+      q.speed_pass = 1;
+      if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
+      q.speed_pass = 0;
+    }
+    if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
+  }
+  long long grid = (ci.cells + 255) / 256;
+  grid = std::min<long long>(grid, 152 * 8);
+  stage_epilogue_kernel<<<(int)grid, 256, 0, s>>>(q, fb, prims_out);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+}  // namespace gbf

@@ -141,6 +141,8 @@ __device__ unsigned long long g_lf_alpha[3];
 constexpr int kLfMaxDevices = 64;
 double* g_lf_alpha_ptr[kLfMaxDevices] = {};
 
+}  // namespace
+
 int lf_alpha_on_current_device(double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GBF_ERR_CUDA;
@@ -153,6 +155,8 @@ int lf_alpha_on_current_device(double** out) {
   *out = g_lf_alpha_ptr[dev];
   return GBF_OK;
 }
+
+namespace {
 
 int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
                          int mode);

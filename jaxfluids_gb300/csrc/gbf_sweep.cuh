@@ -486,8 +486,102 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
   }
 }
 
+// Flux of one face along AX from a staged pencil (sm_prim, variable stride
+// pvol, stride pstride along AX); `base` is the pencil index of the face's
+// first stencil cell (R cells left of the face) and q the logical face
+// coordinates (the face lies between cells q[AX] - 1 and q[AX]).  In a
+// Lax-Friedrichs speed pass (p.speed_pass) it folds max(|u| + c) of the two
+// face states into smax_faces and returns false without a flux.
 // VISC: 0 no dissipative fluxes, 1 dissipative fluxes with the stencils of
 // p.diss_*, 2 dissipative fluxes with CENTRAL4 stencils fixed at compile time
+template <int AX, int RECON, int RIEMANN, int MODE, int VISC>
+__device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm_prim, int pvol, int pstride,
+                                          int base, const int q[3], double F[5], double& smax_faces) {
+  constexpr int R = ReconTraits<RECON>::R;
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
+  double PL[5], PR[5];
+  double UL[5], UR[5];  // face conservatives of the conservative reconstructions
+  if (RIEMANN == RIEMANN_NONE) {
+    // no convective flux: nothing to reconstruct
+  } else if (RECON == RECON_WENO5Z_CONS) {
+    // high_order_godunov.py:282-296
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double w[2 * R];
+#pragma unroll
+      for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[(5 + v) * pvol + base + k * pstride];
+      reconstruct_pair<GBF_RECON_WENO5Z>(w, p.fp.stencil_eps, UL[v], UR[v]);
+    }
+    prims_from_cons(UL, PL, p.fp.gm1);
+    prims_from_cons(UR, PR, p.fp.gm1);
+  } else if (RECON == RECON_WENO5Z_CHARCONS) {
+    const double* b = sm_prim + base;
+    auto wu = [&](int v, int k) { return b[(5 + v) * pvol + k * pstride]; };
+    auto wp = [&](int v, int k) { return b[v * pvol + k * pstride]; };
+    charcons_reconstruct<AX>(wu, wp, p.fp, UL, UR);
+    prims_from_cons(UL, PL, p.fp.gm1);
+    prims_from_cons(UR, PR, p.fp.gm1);
+  } else if (RECON == RECON_WENO5Z_CHAR) {
+    const double* b = sm_prim + base;
+    auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
+    char_reconstruct<AX>(w, p.fp, PL, PR);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double w[2 * R];
+#pragma unroll
+      for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
+      reconstruct_pair<(RECON >= RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
+                                                                                PL[v], PR[v]);
+    }
+  }
+  if (RIEMANN != RIEMANN_NONE && p.limiter) {
+    const double* c = sm_prim + base + (R - 1) * pstride;  // the cell left of the face
+    positivity_limit(PL, c, pvol, p.limiter);
+    positivity_limit(PR, c + pstride, pvol, p.limiter);
+  }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
+    // LaxFriedrichs.py:35-38: max(max |u_L| + c_L, max |u_R| + c_R) over the axis
+    const double cL = speed_of_sound(PL[4], PL[0], p.fp);
+    const double cR = speed_of_sound(PR[4], PR[0], p.fp);
+    smax_faces = fmax(smax_faces, fmax(fabs(PL[AX + 1]) + cL, fabs(PR[AX + 1]) + cR));
+    return false;
+  }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.lf_alpha) {
+    double uL[5], uR[5];
+    if (CONS && !p.limiter) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        uL[v] = UL[v];
+        uR[v] = UR[v];
+      }
+    } else {
+      cons_from_prims(PL, uL, p.fp.gm1);
+      cons_from_prims(PR, uR, p.fp.gm1);
+    }
+    rusanov_alpha<AX>(PL, PR, uL, uR, p.lf_alpha[AX], F);
+  } else if (CONS && RIEMANN != RIEMANN_NONE && !p.limiter) {
+    riemann_flux_u<AX, RIEMANN>(PL, PR, UL, UR, p.fp, F);
+  } else {
+    // the limiter returns the conservatives of its primitives
+    // (limiter_interpolation.py:206)
+    riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
+  }
+  if (VISC) add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F);
+  return true;
+}
+
+// Warp maximum of the Lax-Friedrichs face speeds, one atomic per warp on the
+// order-preserving bits of the non-negative speeds.
+template <int AX>
+__device__ __forceinline__ void lf_speed_reduce(const SweepParams& p, double smax_faces) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) smax_faces = fmax(smax_faces, __shfl_xor_sync(0xffffffffu, smax_faces, off));
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(reinterpret_cast<unsigned long long*>(p.lf_alpha) + AX,
+              (unsigned long long)__double_as_longlong(smax_faces));
+}
+
 template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
 __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
                                            double* sm_prim, double* sm_flux,
@@ -521,90 +615,14 @@ __device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3],
     // face f_AX lies between pencil cells f_AX + R - 1 and f_AX + R; the
     // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
-    double PL[5], PR[5];
-    double UL[5], UR[5];  // face conservatives of the conservative reconstructions
-    if (RIEMANN == RIEMANN_NONE) {
-      // no convective flux: nothing to reconstruct
-    } else if (RECON == RECON_WENO5Z_CONS) {
-      // high_order_godunov.py:282-296
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        double w[2 * R];
-#pragma unroll
-        for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[(5 + v) * pvol + base + k * pstride];
-        reconstruct_pair<GBF_RECON_WENO5Z>(w, p.fp.stencil_eps, UL[v], UR[v]);
-      }
-      prims_from_cons(UL, PL, p.fp.gm1);
-      prims_from_cons(UR, PR, p.fp.gm1);
-    } else if (RECON == RECON_WENO5Z_CHARCONS) {
-      const double* b = sm_prim + base;
-      auto wu = [&](int v, int k) { return b[(5 + v) * pvol + k * pstride]; };
-      auto wp = [&](int v, int k) { return b[v * pvol + k * pstride]; };
-      charcons_reconstruct<AX>(wu, wp, p.fp, UL, UR);
-      prims_from_cons(UL, PL, p.fp.gm1);
-      prims_from_cons(UR, PR, p.fp.gm1);
-    } else if (RECON == RECON_WENO5Z_CHAR) {
-      const double* b = sm_prim + base;
-      auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
-      char_reconstruct<AX>(w, p.fp, PL, PR);
-    } else {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        double w[2 * R];
-#pragma unroll
-        for (int k = 0; k < 2 * R; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
-        reconstruct_pair<(RECON >= RECON_WENO5Z_CHAR) ? GBF_RECON_WENO5Z : RECON>(w, p.fp.stencil_eps,
-                                                                                  PL[v], PR[v]);
-      }
-    }
-    if (RIEMANN != RIEMANN_NONE && p.limiter) {
-      const double* c = sm_prim + base + (R - 1) * pstride;  // the cell left of the face
-      positivity_limit(PL, c, pvol, p.limiter);
-      positivity_limit(PR, c + pstride, pvol, p.limiter);
-    }
-    if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
-      // LaxFriedrichs.py:35-38: max(max |u_L| + c_L, max |u_R| + c_R) over the axis
-      const double cL = speed_of_sound(PL[4], PL[0], p.fp);
-      const double cR = speed_of_sound(PR[4], PR[0], p.fp);
-      smax_faces = fmax(smax_faces, fmax(fabs(PL[AX + 1]) + cL, fabs(PR[AX + 1]) + cR));
-      continue;
-    }
+    const int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
     double F[5];
-    if (RIEMANN == GBF_RIEMANN_RUSANOV && p.lf_alpha) {
-      double uL[5], uR[5];
-      if (CONS && !p.limiter) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          uL[v] = UL[v];
-          uR[v] = UR[v];
-        }
-      } else {
-        cons_from_prims(PL, uL, p.fp.gm1);
-        cons_from_prims(PR, uR, p.fp.gm1);
-      }
-      rusanov_alpha<AX>(PL, PR, uL, uR, p.lf_alpha[AX], F);
-    } else if (CONS && RIEMANN != RIEMANN_NONE && !p.limiter) {
-      riemann_flux_u<AX, RIEMANN>(PL, PR, UL, UR, p.fp, F);
-    } else {
-      // the limiter returns the conservatives of its primitives
-      // (limiter_interpolation.py:206)
-      riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
-    }
-    if (VISC) {
-      int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
-      add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F);
-    }
+    if (!face_flux<AX, RECON, RIEMANN, MODE, VISC>(p, sm_prim, pvol, pstride, base, q, F, smax_faces)) continue;
 #pragma unroll
     for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
   }
   if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
-    // warp maximum, one atomic per warp on the order-preserving bits of the
-    // non-negative speeds
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) smax_faces = fmax(smax_faces, __shfl_xor_sync(0xffffffffu, smax_faces, off));
-    if ((tid & 31) == 0)
-      atomicMax(reinterpret_cast<unsigned long long*>(p.lf_alpha) + AX,
-                (unsigned long long)__double_as_longlong(smax_faces));
+    lf_speed_reduce<AX>(p, smax_faces);
     __syncthreads();  // the pencil is restaged by the next axis
     return;
   }

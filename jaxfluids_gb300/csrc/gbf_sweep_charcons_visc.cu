@@ -8,7 +8,12 @@ int launch_sweep_charcons_visc(int riemann, int mode, const SweepParams& p, int 
                                cudaStream_t s) {
   if (mode == MODE_RHS)
     return launch_sweep_riemann<RECON_WENO5Z_CHARCONS, MODE_RHS, 1>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<RECON_WENO5Z_CHARCONS, MODE_STAGE_P, 1>(riemann, p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
+}
+
+int launch_faces_charcons_visc(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<RECON_WENO5Z_CHARCONS, 1>(riemann, axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

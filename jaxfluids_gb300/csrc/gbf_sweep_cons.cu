@@ -11,7 +11,12 @@ int launch_sweep_cons(bool visc, int riemann, int mode, const SweepParams& p, in
                       cudaStream_t s) {
   if (visc) return launch_sweep_cons_visc(riemann, mode, p, threads, smem, s);
   if (mode == MODE_RHS) return launch_sweep_riemann<RECON_WENO5Z_CONS, MODE_RHS, 0>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<RECON_WENO5Z_CONS, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
+}
+
+int launch_faces_cons(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<RECON_WENO5Z_CONS, 0>(riemann, axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -7,7 +7,12 @@ namespace gbf {
 int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   // the reconstruction parameter only sizes the (unused) pencil box
   if (mode == MODE_RHS) return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_RHS, 1>(p, threads, smem, s);
-  return launch_sweep_one<GBF_RECON_MINMOD, RIEMANN_NONE, MODE_STAGE_P, 1>(p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
+}
+
+int launch_faces_dissipative(int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+                             int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_one<GBF_RECON_MINMOD, RIEMANN_NONE, 1>(axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

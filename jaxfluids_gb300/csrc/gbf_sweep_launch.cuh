@@ -2,6 +2,7 @@
 // that instantiate one scheme family each (compiled in parallel).
 #pragma once
 
+#include "gbf_faces.cuh"
 #include "gbf_kernels.cuh"
 
 namespace gbf {
@@ -25,9 +26,9 @@ int launch_sweep_riemann(int riemann, const SweepParams& p, int threads, size_t 
   return launch_sweep_one<RECON, GBF_RIEMANN_RUSANOV, MODE, VISC>(p, threads, smem, s);
 }
 
-// One entry per scheme family (gbf_sweep_<family>.cu); mode is MODE_RHS or
-// MODE_STAGE for the inviscid families, MODE_RHS or MODE_STAGE_P for the
-// viscous ones.
+// One entry per scheme family (gbf_sweep_<family>.cu): the tile kernel of the
+// drop-in right-hand side (mode MODE_RHS; other modes return
+// GBF_ERR_UNSUPPORTED: the fused stages run the face kernels below).
 int launch_sweep_weno(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 int launch_sweep_weno_visc(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
 int launch_sweep_char(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s);
@@ -59,5 +60,35 @@ int launch_sweep_weno_visc_c4(int riemann, int mode, const SweepParams& p, int t
                               cudaStream_t s);
 int launch_sweep_char_visc_c4(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
                               cudaStream_t s);
+
+
+// Face kernels of the fused stages, one entry per scheme family
+// (gbf_sweep_<family>.cu): the faces of one axis.
+#define GBF_FACES_ARGS \
+  int axis, const SweepParams &p, const FaceTile &ft, const FaceBuffers &fb, int threads, size_t smem, cudaStream_t s
+int launch_faces_weno(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno_visc_c4(int riemann, GBF_FACES_ARGS);
+int launch_faces_char(int riemann, GBF_FACES_ARGS);
+int launch_faces_char_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_char_visc_c4(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno5js(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno5js_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_teno5(int riemann, GBF_FACES_ARGS);
+int launch_faces_teno5_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno3js(int riemann, GBF_FACES_ARGS);
+int launch_faces_weno3z(int riemann, GBF_FACES_ARGS);
+int launch_faces_visc_weno3js(int riemann, GBF_FACES_ARGS);
+int launch_faces_visc_weno3z(int riemann, GBF_FACES_ARGS);
+int launch_faces_minmod(int riemann, GBF_FACES_ARGS);
+int launch_faces_minmod_ad(int riemann, GBF_FACES_ARGS);
+int launch_faces_visc_minmod(int riemann, GBF_FACES_ARGS);
+int launch_faces_visc_minmod_ad(int riemann, GBF_FACES_ARGS);
+int launch_faces_cons(int riemann, GBF_FACES_ARGS);
+int launch_faces_cons_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_charcons(int riemann, GBF_FACES_ARGS);
+int launch_faces_charcons_visc(int riemann, GBF_FACES_ARGS);
+int launch_faces_dissipative(GBF_FACES_ARGS);
+#undef GBF_FACES_ARGS
 
 }  // namespace gbf

@@ -7,10 +7,20 @@ int launch_sweep_muscl(int recon, int riemann, int mode, const SweepParams& p, i
                        cudaStream_t s) {
   if (recon == GBF_RECON_MINMOD) {
     if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_MINMOD, MODE_RHS, 0>(riemann, p, threads, smem, s);
-    return launch_sweep_riemann<GBF_RECON_MINMOD, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+    return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
   }
   if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_MINMOD_AD, MODE_RHS, 0>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<GBF_RECON_MINMOD_AD, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
+}
+
+int launch_faces_minmod(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<GBF_RECON_MINMOD, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+}
+
+int launch_faces_minmod_ad(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<GBF_RECON_MINMOD_AD, 0>(riemann, axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -5,7 +5,12 @@ namespace gbf {
 
 int launch_sweep_teno5(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_TENO5, MODE_RHS, 0>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<GBF_RECON_TENO5, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
+}
+
+int launch_faces_teno5(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<GBF_RECON_TENO5, 0>(riemann, axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

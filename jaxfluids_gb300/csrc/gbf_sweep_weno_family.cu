@@ -9,7 +9,7 @@ namespace {
 template <int RECON>
 int launch_modes(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
   if (mode == MODE_RHS) return launch_sweep_riemann<RECON, MODE_RHS, 0>(riemann, p, threads, smem, s);
-  return launch_sweep_riemann<RECON, MODE_STAGE, 0>(riemann, p, threads, smem, s);
+  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
 }
 
 }  // namespace
@@ -23,6 +23,16 @@ int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams
     case GBF_RECON_TENO5: return launch_sweep_teno5(riemann, mode, p, threads, smem, s);
     default: return GBF_ERR_UNSUPPORTED;
   }
+}
+
+int launch_faces_weno3js(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<GBF_RECON_WENO3JS, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+}
+
+int launch_faces_weno3z(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+    int threads, size_t smem, cudaStream_t s) {
+  return launch_faces_riemann<GBF_RECON_WENO3Z, 0>(riemann, axis, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -1,9 +1,15 @@
 // Arithmetic-rate probes used by the benchmark to measure this GPU's FP64
 // roofline (no FP64 peak is published for the part): independent dependency
-// chains per thread, results stored so nothing is optimised away.
+// chains per thread, results stored so nothing is optimised away.  Built as
+// its own library (libgbfprobe.so), apart from the product library; only the
+// benchmark loads it.
 #include <cuda_runtime.h>
 
-#include "gbf_kernels.cuh"
+// modes of gbf_probe_arith
+#define GBF_PROBE_DFMA 0
+#define GBF_PROBE_DDIV 1
+#define GBF_PROBE_DSQRT 2
+#define GBF_PROBE_FFMA 3
 
 namespace {
 
@@ -48,19 +54,18 @@ __global__ void probe_ffma_kernel(double* out, int iters, double seed) {
 
 }  // namespace
 
-static int gbf_probe_arith_impl(int mode, double* out, int blocks, int threads, int iters, void* stream) {
-  if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) return GBF_ERR_INVALID_ARGUMENT;
+// Runs `iters` iterations of 8 independent dependency chains of one operation
+// per thread (blocks x threads threads) and stores one value per thread in
+// out.  Returns 0, or -1 for invalid arguments, -3 for a launch error.
+extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream) {
+  if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) return -1;
   cudaStream_t s = (cudaStream_t)stream;
   switch (mode) {
     case GBF_PROBE_DFMA: probe_kernel<GBF_PROBE_DFMA><<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
     case GBF_PROBE_DDIV: probe_kernel<GBF_PROBE_DDIV><<<blocks, threads, 0, s>>>(out, iters, 1.5); break;
     case GBF_PROBE_DSQRT: probe_kernel<GBF_PROBE_DSQRT><<<blocks, threads, 0, s>>>(out, iters, 2.0); break;
     case GBF_PROBE_FFMA: probe_ffma_kernel<<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
-    default: return GBF_ERR_INVALID_ARGUMENT;
+    default: return -1;
   }
-  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
-}
-
-extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, int iters, void* stream) {
-  return gbf::record_status(gbf_probe_arith_impl(mode, out, blocks, threads, iters, stream));
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }

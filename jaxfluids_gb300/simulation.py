@@ -118,16 +118,33 @@ class FusedRK3:
         # {dt, t, reduction slot (max signal speed), reduction slot (min density)}
         self.dt_state = torch.zeros(4, dtype=torch.float64, device=self.device)
         self.cons = torch.empty(config.interior_shape(), dtype=torch.float64, device=self.device)
+        # primitives of the state for the first stage of the next advance (None:
+        # derived from the conservatives)
+        self._prims0: Optional[torch.Tensor] = None
 
-    def set_state(self, cons_interior: torch.Tensor, t0: float = 0.0) -> None:
+    def set_state(self, cons_interior: torch.Tensor, t0: float = 0.0,
+                  prims: Optional[torch.Tensor] = None) -> None:
+        """Set the interior conservatives; `prims`, the interior primitives the
+        state was built from (all five components), feed the initial time step
+        and the first stage, as in the reference, where the first stage reads
+        the initial primitives rather than primitives recomputed from the
+        conservatives."""
         self.cons.copy_(cons_interior.reshape(self.config.interior_shape()))
-        _lib.check(self.lib.gbf_rk3_init(ctypes.byref(self.case), _ptr(self.cons), _ptr(self.dt_state),
-                                         float(t0), _stream()), "rk3 init")
+        self._prims0 = None
+        if prims is not None:
+            self._prims0 = torch.empty_like(self.cons)
+            self._prims0.copy_(prims.reshape(self.config.interior_shape()))
+        _lib.check(self.lib.gbf_rk3_init(ctypes.byref(self.case), _ptr(self.cons),
+                                         _ptr(self._prims0) if self._prims0 is not None else None,
+                                         _ptr(self.dt_state), float(t0), _stream()), "rk3 init")
 
     def advance(self, steps: int) -> None:
         tile = ctypes.byref(self.tile) if self.tile is not None else None
-        _lib.check(self.lib.gbf_rk3_advance(ctypes.byref(self.case), _ptr(self.cons), _ptr(self.dt_state),
+        prims = _ptr(self._prims0) if self._prims0 is not None else None
+        _lib.check(self.lib.gbf_rk3_advance(ctypes.byref(self.case), _ptr(self.cons), prims, _ptr(self.dt_state),
                                             _ptr(self.workspace), int(steps), tile, _stream()), "rk3 advance")
+        if steps > 0:
+            self._prims0 = None  # the state has moved on
 
     def capture(self, steps: int) -> torch.cuda.CUDAGraph:
         """A CUDA graph of `steps` fused steps on this object's buffers: each

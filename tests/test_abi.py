@@ -31,7 +31,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_version_and_status_strings(lib):
     from jaxfluids_gb300 import _lib
-    assert lib.gbf_abi_version() == _lib.ABI_VERSION == 5
+    assert lib.gbf_abi_version() == _lib.ABI_VERSION == 6
     assert lib.gbf_status_string(0) == b"ok"
     assert lib.gbf_status_string(-2) == b"unsupported setup"
 
@@ -63,8 +63,12 @@ def test_null_pointers_are_rejected_without_a_gpu(lib):
     c = _cfg().to_c()
     assert lib.gbf_rhs(ctypes.byref(c), None, None, None, None) == -1
     assert lib.gbf_halo_fill(ctypes.byref(c), None, None, None) == -1
-    assert lib.gbf_rk3_advance(ctypes.byref(c), None, None, None, 1, None, None) == -1
-    assert lib.gbf_rk3_workspace_bytes(ctypes.byref(c)) == 2 * 5 * 64 * 8
+    assert lib.gbf_rk3_advance(ctypes.byref(c), None, None, None, None, 1, None, None) == -1
+    # U1, U2, two primitive buffers, the x faces (65 on a zero-gradient axis)
+    # and the Lax-Friedrichs speed slots (4 doubles)
+    assert lib.gbf_rk3_workspace_bytes(ctypes.byref(c)) == (4 * 5 * 64 + 5 * 65 + 4) * 8
+    p = _cfg(bc={f: "PERIODIC" for f in ("east", "west")}).to_c()
+    assert lib.gbf_rk3_workspace_bytes(ctypes.byref(p)) == (4 * 5 * 64 + 5 * 64 + 4) * 8
 
 
 def test_config_from_reference_setup_dicts():

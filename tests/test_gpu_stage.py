@@ -63,10 +63,10 @@ def test_three_stages_equal_one_fused_step(name, cells, bc, kw, kind):
     c = cc.to_c()
     U = U0.clone()
     A, B = torch.empty_like(U), torch.empty_like(U)
-    P = torch.empty_like(U)
+    ws = torch.empty(int(lib.gbf_rk3_workspace_bytes(ctypes.byref(c))) // 8, dtype=torch.float64, device="cuda")
     for _ in range(2):
         for stage, (k, n, out) in enumerate(((U, U, A), (A, U, B), (B, U, U))):
-            st = lib.gbf_rk3_stage(ctypes.byref(c), stage, _ptr(k), _ptr(n), _ptr(out), _ptr(dt_state), _ptr(P),
+            st = lib.gbf_rk3_stage(ctypes.byref(c), stage, _ptr(k), _ptr(n), _ptr(out), _ptr(dt_state), _ptr(ws),
                                    None, _stream())
             assert st == _lib.GBF_OK, st
     torch.cuda.synchronize()
