@@ -37,13 +37,17 @@ UNIT = "cell-updates/s"
 # Algorithmic HBM bytes per cell-update: stage 1 reads U^n and writes U^1
 # (80 B); stages 2 and 3 read U^k and U^n and write (120 B each) -> 320 B.
 BYTES_PER_CELL_UPDATE = 320.0
-# FP64 operations per cell-update of the stage kernels (double-precision add,
-# mul and fma thread instructions, fma counted twice) from the ncu capture of
-# the sweep kernel on this workload (summary kept in the profiles directory).
-FP64_FLOP_PER_CELL_UPDATE = 15798.0
-# DRAM bytes (read + write) of one stage launch at 128^3 from the same capture
-# (the captured launch is the second RK stage: 120 B/cell algorithmic).
-DRAM_BYTES_PER_LAUNCH = 233.8e6
+# Algorithmic FP64 operations per cell-update (add, multiply, division and
+# square root, one FLOP each): the oracle's count of one RK3 step of the
+# reference's algorithm (oracle/flop_count.py; pinned by tests/test_flop_count.py).
+FP64_FLOP_ALGORITHMIC = {"tgv": 8280.0, "viscous": 11190.0}
+# FP64 thread instructions (DADD + DMUL + DFMA) executed per cell and stage
+# by the three face kernels, from the ncu capture of TGV 128^3 (summary in the
+# profiles directory); the epilogue adds the primitives of the new state.
+FP64_INST_FACES_PER_CELL_STAGE = 3216.6
+# DRAM bytes (read + write) of one RK stage at 128^3 (three face kernels and
+# the epilogue) from the same capture; 120 B/cell algorithmic for stages 2, 3.
+DRAM_BYTES_PER_STAGE = 964.7e6
 
 
 def tgv_state(n, device, dtype=torch.float64):
@@ -223,13 +227,15 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def batch_cases(ncases=256, seed=0):
+def batch_cases(ncases=256, seed=0, sides=None):
     """Batched 2-D four-quadrant Riemann problems: sides from {64,...,512}
-    (default_rng(0)), per-case quadrant states from default_rng(1000 + i):
-    rho, u, v, p drawn per quadrant from U[0.1,2], U[-1,1], U[-1,1], U[0.1,2]."""
+    (default_rng(0)), or the given sides; per-case quadrant states from
+    default_rng(1000 + i): rho, u, v, p drawn per quadrant from U[0.1,2],
+    U[-1,1], U[-1,1], U[0.1,2]."""
     import numpy as np
     from jaxfluids_gb300 import CaseConfig
-    sides = np.random.default_rng(seed).choice([64, 128, 192, 256, 384, 512], size=ncases)
+    if sides is None:
+        sides = np.random.default_rng(seed).choice([64, 128, 192, 256, 384, 512], size=ncases)
     cfgs, states = [], []
     for i, n in enumerate(sides):
         n = int(n)
@@ -253,7 +259,8 @@ def run_batch(args):
     from jaxfluids_gb300 import BatchedRK3, FusedRK3, autotune, build
     build.build()
     device = torch.device("cuda", 0)
-    cfgs, states = batch_cases(args.cases)
+    small = args.workload == "batch-small"
+    cfgs, states = batch_cases(args.cases, sides=[64] * args.cases if small else None)
     cells = sum(c.n_cells for c in cfgs)
     batch = BatchedRK3(cfgs, device)
     batch.set_states([s.to(device) for s in states])
@@ -291,15 +298,32 @@ def run_batch(args):
     b.synchronize()
     t_single = a.elapsed_time(b) / 1e3
     single = cells * n_single / t_single
+    # one case at a time with each case's steps captured in its own CUDA graph
+    # (no host launch overhead; each case still runs alone on the GPU)
+    graphs = [f.capture(n_single) for f in singles]
+    for g in graphs:
+        g.replay()
+    torch.cuda.synchronize()
+    a.record()
+    for g in graphs:
+        g.replay()
+    b.record()
+    b.synchronize()
+    t_single_g = a.elapsed_time(b) / 1e3
+    single_g = cells * n_single / t_single_g
+    mix = "all 64^2" if small else "sides from {64..512}"
     line = {"metric": "FP64 cell-updates/s, batched 2-D four-quadrant Riemann problems", "value": batched,
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": f"{len(cfgs)} cases, sides from {{64..512}}, {cells} cells, WENO5-Z+HLLC, ZG",
+            "config": {"workload": f"{len(cfgs)} cases, {mix}, {cells} cells, WENO5-Z+HLLC, ZG",
                        "autotuned": {"tile": tune["best"][0], "threads": tune["best"][1], "ctas": tune["best"][2]},
                        "graph_steps": args.steps},
             "one_case_at_a_time": {"value": single, "steps": n_single, "ms_per_step": 1e3 * t_single / n_single},
+            "one_case_at_a_time_graphs": {"value": single_g, "steps": n_single,
+                                          "ms_per_step": 1e3 * t_single_g / n_single},
             "speedup_vs_one_at_a_time": batched / single,
+            "speedup_vs_one_at_a_time_graphs": batched / single_g,
             "autotune_ms_per_step": [[list(c[0]), c[1], c[2], ms] for c, ms in tune["results"]]}
     print(json.dumps(line), flush=True)
 
@@ -433,7 +457,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=None, help="grid side (default 128 inviscid, 256 viscous)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "adjoint", "viscous-adjoint"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "batch-small", "adjoint", "viscous-adjoint"])
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=None, help="default 1000 (KH), 200 (viscous TGV)")
     ap.add_argument("--adj-slots", type=int, default=2, help="binomial checkpoint slots (viscous adjoint)")
@@ -443,7 +467,7 @@ def main():
     ap.add_argument("--adj-schedule", default="stored", choices=["stored", "uniform", "binomial"])
     ap.add_argument("--cases", type=int, default=256)
     args = ap.parse_args()
-    if args.workload == "batch":
+    if args.workload in ("batch", "batch-small"):
         return run_batch(args)
     if args.workload == "adjoint":
         args.adj_steps = args.adj_steps or 1000
@@ -510,7 +534,7 @@ def main():
         t_dev = tt.item()
     value = world * cells * args.steps / t_dev
 
-    # ---- per-kernel time of the stage kernels (same stream, CUDA events) ----
+    # ---- per-stage time (three face kernels + epilogue; same stream, CUDA events) ----
     ka = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     kb = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     for k in range(3):
@@ -519,26 +543,33 @@ def main():
         kb[k].record(stream)
     torch.cuda.synchronize()
     per_step_s = min(a.elapsed_time(b) for a, b in zip(ka, kb)) / 1e3
-    # a step = 3 stage launches + 1 one-thread time-step launch (~microseconds)
-    launch_s = per_step_s / 3.0
-    bytes_per_launch = BYTES_PER_CELL_UPDATE / 3.0 * cells
-    hbm_peak = 6795.1
+    # a step = 3 stages (+ the primitives of U^n and the one-thread time-step
+    # kernel, ~0.2 % of the step)
+    stage_s = per_step_s / 3.0
+    bytes_per_stage = BYTES_PER_CELL_UPDATE / 3.0 * cells
+    hbm_peak, peak_src = 6800.0, "fallback (6.8 TB/s)"
     try:
         hbm_peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
         peak_src = "measured"
     except Exception:
-        peak_src = "fallback"
-    achieved = bytes_per_launch / launch_s / 1e9
+        pass
+    achieved = bytes_per_stage / stage_s / 1e9
     fp64_peak = fp64_peak_tflops(device)
+    flop_alg = FP64_FLOP_ALGORITHMIC["viscous" if viscous else "tgv"]
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_source": peak_src,
-        "traffic": DRAM_BYTES_PER_LAUNCH,
-        "kernel": "RK stage: face_flux_kernel<x,y,z; WENO5Z,HLLC> + stage_epilogue_kernel",
-        "fp64": {"peak_tflops_measured": fp64_peak,
-                 "achieved_tflops": (FP64_FLOP_PER_CELL_UPDATE * cells / 3.0 / launch_s / 1e12)
-                 if FP64_FLOP_PER_CELL_UPDATE else None,
-                 "flop_per_cell_update": FP64_FLOP_PER_CELL_UPDATE},
+        "traffic": None if viscous else DRAM_BYTES_PER_STAGE,
+        "launch": "one RK stage: face_flux_kernel x, y, z + stage_epilogue_kernel",
+        "fp64": {
+            "peak_tflops_measured": fp64_peak,  # DFMA chains, 2 FLOP per instruction
+            "flop_per_cell_update_algorithmic": flop_alg,
+            "achieved_tflops_algorithmic": flop_alg * cells / per_step_s / 1e12,
+            "frac_algorithmic": flop_alg * cells / per_step_s / 1e12 / fp64_peak,
+            "inst_per_cell_stage_faces": None if viscous else FP64_INST_FACES_PER_CELL_STAGE,
+            "frac_issue_faces": None if viscous else
+            FP64_INST_FACES_PER_CELL_STAGE * cells / stage_s / (fp64_peak * 1e12 / 2.0),
+        },
     }
 
     # ---- end to end through the public API with host buffers ----
@@ -572,11 +603,6 @@ def main():
                          f"restatement of the reference (torch float64, {threads} threads)",
                "cpu_model": cpu_model()}
 
-    if viscous:
-        roofline["fp64"]["flop_per_cell_update"] = None
-        roofline["fp64"]["achieved_tflops"] = None
-        roofline["traffic"] = None
-        roofline["kernel"] = "sweep_kernel<WENO5Z-CHAR,HLLC,STAGE_P,VISC> + prims conversion"
     if rank == 0:
         metric = METRIC if not viscous else \
             f"FP64 cell-updates/s (viscous TGV {n}^3 Re 1600, WENO5-Z CHAR-ROE+HLLC+CENTRAL4, TVD-RK3)"

@@ -48,9 +48,13 @@ struct FaceBuffers {
 // One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
 // Reads the stage primitives p.prims (and, for the conservative
 // reconstructions, the stage conservatives p.cons), MODE_STAGE_P semantics.
+// Two CTAs per SM (at most 128 registers; the inviscid kernels use about 95
+// and spill nothing).  The kernels issue FP64 instructions at the rate of a
+// pure DFMA chain on this part; a third CTA (at most 85 registers, spilling)
+// measured the same time on TGV 128^3.
 template <int AX, int RECON, int RIEMANN, int VISC>
-__global__ void __launch_bounds__(256, 2) face_flux_kernel(const SweepParams p, const FaceTile ft,
-                                                           const FaceBuffers fb) {
+__global__ void __launch_bounds__(256, 2)
+    face_flux_kernel(const SweepParams p, const FaceTile ft, const FaceBuffers fb) {
   extern __shared__ double smem[];
   constexpr int R = ReconTraits<RECON>::R;
   constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;

@@ -1,0 +1,169 @@
+"""The headline workloads at their stated sizes against the oracle.
+
+* TGV 128^3 (WENO5-Z + HLLC, PRIMITIVE, periodic): one right-hand side through
+  the drop-in path (<= 1e-12 relative) and 20 fused CFL steps (<= 1e-10),
+  every time step equal.
+* Viscous TGV 256^3 (Re 1600, Pr 0.71, WENO5-Z on Roe-characteristic variables
+  + HLLC + CENTRAL4 viscous and heat fluxes): one right-hand side and one fused
+  step.
+* Kelvin-Helmholtz 512^2 (periodic, noise from default_rng(7)): the
+  right-hand-side VJP against the oracle's autograd (<= 1e-11) and a 5-step
+  fixed-dt gradient of 1/2 ||rho(T) - rho_target||^2 with respect to the
+  initial v field, the workload's control (<= 1e-10).  The gradient with
+  respect to rho, rho u and E is rounding-dominated on this piecewise-constant
+  initial state (WENO-Z's weights on nearly flat stencils): a one-ulp change
+  of the initial rho v moves the oracle's own gradient by 1.5e-3 (max norm)
+  there, while its v-field gradient moves by 1.4e-11; that part is held to
+  1e-2.
+* The batched path on four quadrant problems with sides 64, 128, 192 and 512
+  (states from default_rng(1000 + i)), 10 steps, against the oracle case by case.
+
+The kernels follow the reference's operation order, so the forward results are
+also asserted bitwise equal.  The oracle runs on the host's cores: these tests
+take a few minutes; the 256^3 one needs about 45 GB of host memory and is
+skipped on a host with less available.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import jf_oracle as O
+from tests.cases import both, quadrant_prims, rel_err, tgv_prims
+
+pytestmark = pytest.mark.gpu
+TWO_PI = ((0.0, 2 * math.pi),) * 3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from jaxfluids_gb300 import build
+    build.build()
+    torch.set_num_threads(max(1, __import__("os").cpu_count() or 1))
+
+
+def _available_host_bytes():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def _rhs_and_steps(oc, cc, prims, steps):
+    from jaxfluids_gb300 import FusedRK3, SimulationManager
+    U, P = O.initialize(prims, oc)
+    ref_rhs = O.compute_rhs(U, P, oc)
+    sim = SimulationManager(cc)
+    rhs = sim.space_solver.compute_rhs(U.cuda(), P.cuda(), None, 0.0, 0.0)[0].euler_buffers.conservatives.cpu()
+    del sim
+    assert rel_err(rhs, ref_rhs) <= 1e-12
+    assert torch.equal(rhs, ref_rhs)
+    del rhs, ref_rhs
+    inner = oc.interior()
+    f = FusedRK3(cc)
+    f.set_state(U[inner].contiguous().cuda(), prims=P[inner].contiguous().cuda())
+    dts_gpu = [float(f.dt)]
+    for _ in range(steps):
+        f.advance(1)
+        dts_gpu.append(float(f.dt))
+    dt = O.compute_dt(P, oc)
+    dts = [float(dt)]
+    for _ in range(steps):
+        U, P = O.rk3_step(U, P, dt, oc)
+        dt = O.compute_dt(P, oc)
+        dts.append(float(dt))
+    cons = f.cons.cpu()
+    assert dts_gpu == dts
+    assert rel_err(cons, U[inner]) <= 1e-10
+    assert torch.equal(cons, U[inner])
+
+
+def test_tgv_128_rhs_and_20_steps():
+    oc, cc = both((128, 128, 128), "PERIODIC", ranges=TWO_PI)
+    _rhs_and_steps(oc, cc, tgv_prims(128), 20)
+
+
+def test_viscous_tgv_256_char_roe_rhs_and_one_step():
+    if _available_host_bytes() < 120e9:
+        pytest.skip("the oracle's 256^3 viscous step needs about 45 GB of host memory")
+    oc, cc = both((256, 256, 256), "PERIODIC", ranges=TWO_PI, nh=4, recon_var="CHAR-PRIMITIVE",
+                  frozen_state="ROE", viscous=True, heat=True, mu=1.0 / 1600, prandtl=0.71)
+    _rhs_and_steps(oc, cc, tgv_prims(256), 1)
+
+
+def _kh_cons(n, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    inner = np.abs(Y - 0.5) < 0.25
+    P = np.stack([np.where(inner, 2.0, 1.0), np.where(inner, 0.5, -0.5),
+                  0.01 * np.sin(4 * np.pi * X) + rng.normal(0.0, 1e-3, X.shape), np.zeros_like(X),
+                  np.full_like(X, 2.5)]).reshape(5, n, n, 1)
+    return O.cons_from_prims(torch.from_numpy(P), 1.4)
+
+
+def test_kh_512_rhs_vjp_and_5_step_gradient():
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    n = 512
+    oc, cc = both((n, n, 1), "PERIODIC")
+    U0 = _kh_cons(n, 7)
+    target = _kh_cons(n, 8)[0]
+    dt = float(O.compute_dt(O.buffers_from_interior_cons(U0, oc)[1], oc))
+    adj = AdjointRK3(cc, dt=dt)
+    # right-hand-side VJP
+    w = torch.randn(U0.shape, generator=torch.Generator().manual_seed(11), dtype=torch.float64)
+    x = U0.clone().requires_grad_(True)
+    (O.rhs_of_interior_cons(x, oc) * w).sum().backward()
+    g = adj.rhs_vjp(U0.cuda().contiguous(), w.cuda().contiguous())
+    assert rel_err(g, x.grad) <= 1e-11
+    # 5-step fixed-dt gradient of 1/2 ||rho(T) - target||^2
+    steps = 5
+    tg = target.cuda()
+    UN, grad = adj.gradient(U0.cuda(), steps, lambda U: torch.stack([U[0] - tg] + [torch.zeros_like(tg)] * 4),
+                            schedule="uniform", every=2)
+    x = U0.clone().requires_grad_(True)
+    U = x
+    for _ in range(steps):
+        U = O.rk3_step_interior(U, torch.tensor(dt, dtype=torch.float64), oc)
+    (0.5 * ((U[0] - target) ** 2).sum()).backward()
+    assert torch.equal(UN.cpu(), U.detach())
+    # d loss / d v0 = (d loss / d rho v) rho + (d loss / d E) rho v, with U = cons(P)
+    dv_gpu = grad[2].cpu() * U0[0] + grad[4].cpu() * U0[2]
+    dv_ref = x.grad[2] * U0[0] + x.grad[4] * U0[2]
+    assert rel_err(dv_gpu[None], dv_ref[None]) <= 1e-10
+    assert rel_err(grad, x.grad) <= 1e-2
+
+
+def test_batch_with_a_512_case_against_the_oracle():
+    from jaxfluids_gb300 import BatchedRK3, CaseConfig
+    sides = (64, 128, 192, 512)
+    zg = {f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")}
+    cfgs = [CaseConfig(cells=(s, s, 1), bc=dict(zg)) for s in sides]
+    states, refs = [], []
+    steps = 10
+    for i, s in enumerate(sides):
+        oc, _ = both((s, s, 1), "ZEROGRADIENT")
+        q = quadrant_prims(s, s, seed=1000 + i)
+        U, P = O.initialize(q, oc)
+        Ui = U[oc.interior()].contiguous()
+        states.append(Ui)
+        # the batch takes conservatives: its first stage reads their
+        # primitives, so the oracle starts from those too
+        U, P = O.buffers_from_interior_cons(Ui, oc)
+        Ur, _, _, k = O.simulate(U, P, oc, end_step=steps)
+        assert k == steps
+        refs.append(Ur[oc.interior()])
+    batch = BatchedRK3(cfgs)
+    batch.set_states([u.cuda() for u in states])
+    batch.advance(steps)
+    torch.cuda.synchronize()
+    for i in range(len(sides)):
+        got = batch.case_view(i).cpu()
+        assert rel_err(got, refs[i]) <= 1e-10, sides[i]
+        assert torch.equal(got, refs[i]), sides[i]
