@@ -51,6 +51,36 @@ def _deps():
             [os.path.join(ROOT, "include", "gbfluids.h"), os.path.abspath(__file__)])
 
 
+FFI_SRC = os.path.join(PKG, "ffi", "gbf_ffi.cc")
+FFI_LIB = os.path.join(PKG, "libgbfluids_ffi.so")
+
+
+def build_ffi(force: bool = False):
+    """libgbfluids_ffi.so: the XLA FFI handlers of ffi/gbf_ffi.cc, compiled
+    against jax.ffi.include_dir() and linked to libgbfluids.so.  Returns its
+    path, or None (with the reason printed) where jaxlib is not installed."""
+    try:
+        import jax.ffi  # noqa: F401
+        include = jax.ffi.include_dir()
+    except Exception as e:  # no jaxlib: the binding cannot be compiled here
+        print(f"XLA FFI handlers not built: jax.ffi unavailable ({type(e).__name__}: {e})", file=sys.stderr)
+        return None
+    lib = build()
+    deps = [FFI_SRC, os.path.join(PKG, "ffi", "gbf_ffi_desc.h"), lib]
+    if not force and os.path.exists(FFI_LIB) and os.path.getmtime(FFI_LIB) >= max(map(os.path.getmtime, deps)):
+        return FFI_LIB
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    tmp = FFI_LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", f"-I{include}", f"-I{os.path.join(ROOT, 'include')}",
+           f"-I{os.path.join(PKG, 'ffi')}", f"-I{os.path.join(cuda, 'include')}", FFI_SRC, "-o", tmp,
+           f"-L{PKG}", "-lgbfluids", f"-L{os.path.join(cuda, 'lib64')}", "-lcudart", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for {FFI_SRC}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, FFI_LIB)
+    return FFI_LIB
+
+
 def build_probe(force: bool = False) -> str:
     """libgbfprobe.so: the FP64 / FP32 rate probe the benchmark times."""
     if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= max(

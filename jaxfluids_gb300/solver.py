@@ -111,9 +111,26 @@ class HaloManager(_Base):
 
 
 class SpaceSolver(_Base):
-    """Drop-in for jaxfluids.solvers.space_solver.SpaceSolver (single phase)."""
+    """Drop-in for jaxfluids.solvers.space_solver.SpaceSolver (single phase).
 
-    def __init__(self, config: CaseConfig, tile: Optional[_lib.GbfTile] = None):
+    Constructed either from a CaseConfig, or with the reference's own
+    constructor arguments (solvers/space_solver.py:45-57: domain_information,
+    material_manager, equation_manager, halo_manager, numerical_setup, gravity,
+    geometric_source, handlers), from which the setup is read
+    (jax_binding.case_config_from_reference)."""
+
+    def __init__(self, config, material_manager=None, equation_manager=None, halo_manager=None,
+                 numerical_setup=None, gravity=None, geometric_source=None, levelset_handler=None,
+                 diffuse_interface_handler=None, positivity_handler=None, *, tile: Optional[_lib.GbfTile] = None):
+        if not isinstance(config, CaseConfig):
+            from .jax_binding import case_config_from_reference
+            if material_manager is None or halo_manager is None or numerical_setup is None:
+                raise TypeError("SpaceSolver takes a CaseConfig or the reference's constructor arguments")
+            if levelset_handler is not None or diffuse_interface_handler is not None:
+                raise NotImplementedError("two-phase handlers are not on the GB300 path")
+            config = case_config_from_reference(config, material_manager, numerical_setup, halo_manager, gravity)
+        elif isinstance(material_manager, _lib.GbfTile):  # SpaceSolver(config, tile)
+            tile = material_manager
         super().__init__(config)
         self.tile = tile
 

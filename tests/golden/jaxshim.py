@@ -212,13 +212,13 @@ def _make_jnp():
 
         return f
 
-    jnp.__getattr__ = _getattr
+    jnp.__getattr__ = _attr_only(_getattr)
     for n in ("float32", "float64", "int32", "int64", "bool_", "uint8", "finfo", "iinfo", "dtype"):
         setattr(jnp, n, getattr(np, n))
     for n, v in special.items():
         setattr(jnp, n, v)
     linalg = types.ModuleType("jax.numpy.linalg")
-    linalg.__getattr__ = lambda name: (lambda *a, **k: _wrap(getattr(np.linalg, name)(*a, **k)))
+    linalg.__getattr__ = _attr_only(lambda name: (lambda *a, **k: _wrap(getattr(np.linalg, name)(*a, **k))))
     jnp.linalg = linalg
     return jnp
 
@@ -364,6 +364,16 @@ def pmap(fun=None, **kw):
     return f
 
 
+def _attr_only(fn):
+    """Module __getattr__ answering ordinary names only: dunder lookups
+    (__file__, __path__, ...) raise AttributeError as for a real module."""
+    def getattr_(name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return fn(name)
+    return getattr_
+
+
 def _no(name):
     def f(*a, **k):
         raise NotImplementedError(f"jax.{name} is not available in the numpy stand-in")
@@ -401,7 +411,7 @@ class _StubFinder:
     def create_module(self, spec):
         m = types.ModuleType(spec.name)
         m.__path__ = []
-        m.__getattr__ = lambda k: _Anything
+        m.__getattr__ = _attr_only(lambda k: _Anything)
         return m
 
     def exec_module(self, m):
@@ -463,7 +473,7 @@ def install():
     jax.random = random
     scipy = types.ModuleType("jax.scipy")
     special = types.ModuleType("jax.scipy.special")
-    special.__getattr__ = _no
+    special.__getattr__ = _attr_only(_no)
     scipy.special = special
     jax.scipy = scipy
     experimental = types.ModuleType("jax.experimental")
