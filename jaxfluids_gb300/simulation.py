@@ -96,6 +96,22 @@ class SimulationManager:
                 log.append((t, float(dt), float(primitives[self.config.interior_slices()][0].min())))
         return conservatives, primitives, t, step
 
+    def write(self, path: str, primitives: torch.Tensor, t: float) -> str:
+        """Output of the interior primitives of a halo buffer and the time in the
+        reference's field layout (restart.py; hdf5_writer.py:79-265 writes the
+        same datasets with h5py)."""
+        from .restart import write_fields
+        return write_fields(path, self.config, primitives[self.config.interior_slices()], t)
+
+    def restart(self, path: str, device="cuda") -> Tuple[torch.Tensor, torch.Tensor, float]:
+        """(conservatives, primitives, time) from a file of write(): the halo
+        buffers rebuilt from the primitives, as the reference restarts
+        (material_fields_initializer.py:212-340, create_material_fields)."""
+        from .restart import read_fields
+        P, t = read_fields(path, self.config)
+        U, Pb = self.initialize(torch.from_numpy(P).to(device))
+        return U, Pb, t
+
 
 class FusedRK3:
     """Fused TVD-RK3 stepping of interior conservatives (gbf_rk3_advance)."""
@@ -166,6 +182,26 @@ class FusedRK3:
                 self.advance(steps)
         torch.cuda.current_stream(self.device).wait_stream(s)
         return g
+
+    def write(self, path: str) -> str:
+        """Output of the current state (its primitives) and time in the
+        reference's field layout (restart.py)."""
+        from .restart import write_fields
+        return write_fields(path, self.config, self.primitives(), float(self.t))
+
+    @classmethod
+    def from_restart(cls, config: CaseConfig, path: str, device="cuda",
+                     tile: Optional[_lib.GbfTile] = None) -> "FusedRK3":
+        """A FusedRK3 continuing from a file of write(): conservatives rebuilt
+        from the primitives, which also feed the first stage, as a reference
+        restart does (material_fields_initializer.py:212-340)."""
+        from .restart import read_fields
+        P, t = read_fields(path, config)
+        f = cls(config, device, tile)
+        Pd = torch.from_numpy(P).to(f.device)
+        U = EquationManager(config).get_conservatives_from_primitives(Pd)
+        f.set_state(U, t0=t, prims=Pd)
+        return f
 
     @property
     def dt(self) -> torch.Tensor:
