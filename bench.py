@@ -44,7 +44,7 @@ FP64_FLOP_ALGORITHMIC = {"tgv": 8280.0, "viscous": 11190.0}
 # FP64 thread instructions (DADD + DMUL + DFMA) executed per cell and stage
 # by the three face kernels, from the ncu capture of TGV 128^3 (summary in the
 # profiles directory); the epilogue adds the primitives of the new state.
-FP64_INST_FACES_PER_CELL_STAGE = 3216.6
+FP64_INST_FACES_PER_CELL_STAGE = 2974.8
 # DRAM bytes (read + write) of one RK stage at 128^3 (three face kernels and
 # the epilogue) from the same capture; 120 B/cell algorithmic for stages 2, 3.
 DRAM_BYTES_PER_STAGE = 964.7e6

@@ -48,6 +48,17 @@ struct FaceBuffers {
 // One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
 // Reads the stage primitives p.prims (and, for the conservative
 // reconstructions, the stage conservatives p.cons), MODE_STAGE_P semantics.
+// Whether a face kernel shares the smoothness indicators' window terms
+// between faces (reconstruct_pair_shared): the WENO5 family on primitive
+// variables without dissipative fluxes (whose stencils read the primitive
+// buffer through L1, which the larger shared-memory footprint would shrink).
+// The host sizes shared memory by the same rule (gbf_stage.cu, face_smem).
+template <int RECON, int RIEMANN, int VISC>
+struct FaceShare {
+  static constexpr bool value = VISC == 0 && RIEMANN != RIEMANN_NONE &&
+                                (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5);
+};
+
 // Two CTAs per SM (at most 128 registers; the inviscid kernels use about 95
 // and spill nothing).  The kernels issue FP64 instructions at the rate of a
 // pure DFMA chain on this part; a third CTA (at most 85 registers, spilling)
@@ -76,6 +87,30 @@ __global__ void __launch_bounds__(256, 2)
   }
   const int fvol = fe[0] * fe[1] * fe[2];
   const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
+  // the smoothness indicators' window terms, once per pencil cell (cells with
+  // both neighbours along AX in the pencil) instead of three times per face side
+  constexpr bool SHARE = FaceShare<RECON, RIEMANN, VISC>::value;
+  double* sm_win = smem + 5 * pvol;
+  if constexpr (SHARE) {
+    for (int i = threadIdx.x; i < pvol; i += blockDim.x) {
+      const int i2 = i % pe[2];
+      const int r = i / pe[2];
+      const int i1 = r % pe[1];
+      const int i0 = r / pe[1];
+      const int k = (AX == 0) ? i0 : ((AX == 1) ? i1 : i2);
+      if (k == 0 || k == pe[AX] - 1) continue;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double dl, dr, e;
+        weno5_window_terms(smem[v * pvol + i - pstride], smem[v * pvol + i], smem[v * pvol + i + pstride], dl, dr,
+                           e);
+        sm_win[v * pvol + i] = dl;
+        sm_win[(5 + v) * pvol + i] = dr;
+        sm_win[(10 + v) * pvol + i] = e;
+      }
+    }
+    __syncthreads();
+  }
   int ext[3] = {p.n[0], p.n[1], p.n[2]};
   ext[AX] = ft.nf;
   const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
@@ -89,7 +124,8 @@ __global__ void __launch_bounds__(256, 2)
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     const int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
     double F[5];
-    if (!face_flux<AX, RECON, RIEMANN, MODE_STAGE_P, VISC>(p, smem, pvol, pstride, base, q, F, smax_faces))
+    if (!face_flux<AX, RECON, RIEMANN, MODE_STAGE_P, VISC, SHARE>(p, smem, pvol, pstride, base, q, F, smax_faces,
+                                                                   sm_win))
       continue;
     const long long g = ((long long)q[0] * ext[1] + q[1]) * ext[2] + q[2];
 #pragma unroll

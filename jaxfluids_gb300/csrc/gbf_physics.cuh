@@ -101,10 +101,22 @@ __device__ __forceinline__ double weno5_combine(double a0, double a1, double a2,
   return (a0 * one_a) * p0 + (a1 * one_a) * p1 + (a2 * one_a) * p2;
 }
 
-__device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
-                                         double eps) {
-  double b0, b1, b2;
-  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+// The smoothness indicators of weno5_smoothness from window terms computed
+// once per cell and shared by the three faces whose stencils hold the window:
+// d0, d1, d2 = (13/12) (fma(-2, u_c, u_prev) + u_next)^2 of the windows centred
+// on u1, u2, u3, and e1 = (u1 - u3)^2, each formed by the same operations on
+// the same operands in the same order as weno5_smoothness forms it, so the
+// indicators are bitwise equal.
+__device__ __forceinline__ void weno5_smoothness_shared(double u0, double u1, double u2, double u3, double u4,
+                                                        double d0, double d1, double d2, double e1, double& b0,
+                                                        double& b1, double& b2) {
+  b0 = fma(0.25, sq(fma(-4.0, u1, u0) + 3.0 * u2), d0);
+  b1 = fma(0.25, e1, d1);
+  b2 = fma(0.25, sq(fma(-4.0, u3, 3.0 * u2) + u4), d2);
+}
+
+__device__ __forceinline__ double weno5z_from_beta(double b0, double b1, double b2, double u0, double u1,
+                                                   double u2, double u3, double u4, double eps) {
   const double tau5 = fabs(b0 - b2);
   const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
   const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
@@ -112,15 +124,27 @@ __device__ __forceinline__ double weno5z(double u0, double u1, double u2, double
   return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
 }
 
-// WENO5-JS (shock_capturing/weno/weno5_js.py:33-70): alpha_k = d_k / (beta_k^2 + eps).
-__device__ __forceinline__ double weno5js(double u0, double u1, double u2, double u3, double u4,
-                                          double eps) {
+__device__ __forceinline__ double weno5z(double u0, double u1, double u2, double u3, double u4,
+                                         double eps) {
   double b0, b1, b2;
   weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  return weno5z_from_beta(b0, b1, b2, u0, u1, u2, u3, u4, eps);
+}
+
+// WENO5-JS (shock_capturing/weno/weno5_js.py:33-70): alpha_k = d_k / (beta_k^2 + eps).
+__device__ __forceinline__ double weno5js_from_beta(double b0, double b1, double b2, double u0, double u1,
+                                                    double u2, double u3, double u4, double eps) {
   const double a0 = 0.1 * (1.0 / (b0 * b0 + eps));
   const double a1 = 0.6 * (1.0 / (b1 * b1 + eps));
   const double a2 = 0.3 * (1.0 / (b2 * b2 + eps));
   return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
+}
+
+__device__ __forceinline__ double weno5js(double u0, double u1, double u2, double u3, double u4,
+                                          double eps) {
+  double b0, b1, b2;
+  weno5_smoothness(u0, u1, u2, u3, u4, b0, b1, b2);
+  return weno5js_from_beta(b0, b1, b2, u0, u1, u2, u3, u4, eps);
 }
 
 // TENO5 (teno/teno5.py, Fu et al. 2016) weights: gamma_k = (1 + tau5 / (beta_k
@@ -146,6 +170,16 @@ __device__ __forceinline__ void teno5_weights(double b0, double b1, double b2, d
   o0 = __dmul_rn(w0, one_dk);
   o1 = __dmul_rn(w1, one_dk);
   o2 = __dmul_rn(w2, one_dk);
+}
+
+__device__ __forceinline__ double teno5_from_beta(double b0, double b1, double b2, double u0, double u1,
+                                                  double u2, double u3, double u4, double eps) {
+  double o0, o1, o2;
+  teno5_weights(b0, b1, b2, eps, o0, o1, o2);
+  const double p0 = (1.0 / 3.0) * u0 + (-7.0 / 6.0) * u1 + (11.0 / 6.0) * u2;
+  const double p1 = (-1.0 / 6.0) * u1 + (5.0 / 6.0) * u2 + (1.0 / 3.0) * u3;
+  const double p2 = (1.0 / 3.0) * u2 + (5.0 / 6.0) * u3 + (-1.0 / 6.0) * u4;
+  return o0 * p0 + o1 * p1 + o2 * p2;
 }
 
 __device__ __forceinline__ double teno5(double u0, double u1, double u2, double u3, double u4, double eps) {
@@ -274,6 +308,37 @@ __device__ __forceinline__ void reconstruct_pair<GBF_RECON_WENO5Z>(const double*
   // j=0 offsets (-3..1) -> w[0..4]; j=1 offsets (2..-2) -> w[5..1]
   L = weno5z(w[0], w[1], w[2], w[3], w[4], eps);
   R = weno5z(w[5], w[4], w[3], w[2], w[1], eps);
+}
+
+// The WENO5 family (WENO5-Z, WENO5-JS, TENO5) on primitive variables with the
+// window terms of weno5_smoothness_shared read from per-cell arrays: for the
+// six cells w[0..5] around the face, dl[k] / dr[k] / e[k] are the terms of the
+// window centred on w[k] (k = 1..4) in the left-state / right-state operand
+// order.  Equal bitwise to reconstruct_pair<RECON>.
+template <int RECON>
+__device__ __forceinline__ void reconstruct_pair_shared(const double* w, const double* dl, const double* dr,
+                                                        const double* e, double eps, double& L, double& R) {
+  double b0, b1, b2;
+  // left: (w0 .. w4), windows centred on w1, w2, w3
+  weno5_smoothness_shared(w[0], w[1], w[2], w[3], w[4], dl[1], dl[2], dl[3], e[2], b0, b1, b2);
+  if (RECON == GBF_RECON_WENO5Z) L = weno5z_from_beta(b0, b1, b2, w[0], w[1], w[2], w[3], w[4], eps);
+  if (RECON == GBF_RECON_WENO5JS) L = weno5js_from_beta(b0, b1, b2, w[0], w[1], w[2], w[3], w[4], eps);
+  if (RECON == GBF_RECON_TENO5) L = teno5_from_beta(b0, b1, b2, w[0], w[1], w[2], w[3], w[4], eps);
+  // right: (w5 .. w1), windows centred on w4, w3, w2
+  weno5_smoothness_shared(w[5], w[4], w[3], w[2], w[1], dr[4], dr[3], dr[2], e[3], b0, b1, b2);
+  if (RECON == GBF_RECON_WENO5Z) R = weno5z_from_beta(b0, b1, b2, w[5], w[4], w[3], w[2], w[1], eps);
+  if (RECON == GBF_RECON_WENO5JS) R = weno5js_from_beta(b0, b1, b2, w[5], w[4], w[3], w[2], w[1], eps);
+  if (RECON == GBF_RECON_TENO5) R = teno5_from_beta(b0, b1, b2, w[5], w[4], w[3], w[2], w[1], eps);
+}
+
+// The window terms of the cell u_c between u_prev and u_next (along the axis):
+// dl = (13/12) (fma(-2, u_c, u_prev) + u_next)^2, dr = (13/12) (fma(-2, u_c,
+// u_next) + u_prev)^2, e = (u_prev - u_next)^2 (weno5_smoothness_shared).
+__device__ __forceinline__ void weno5_window_terms(double up, double uc, double un, double& dl, double& dr,
+                                                   double& e) {
+  dl = (13.0 / 12.0) * sq(fma(-2.0, uc, up) + un);
+  dr = (13.0 / 12.0) * sq(fma(-2.0, uc, un) + up);
+  e = sq(up - un);
 }
 
 template <>

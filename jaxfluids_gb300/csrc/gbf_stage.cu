@@ -163,13 +163,19 @@ int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, F
   return GBF_OK;
 }
 
+// Shared memory of a face kernel: the pencil (primitives; conservatives too for
+// the conservative reconstructions) and, for the kernels of FaceShare
+// (gbf_faces.cuh), the three window-term arrays of the smoothness indicators.
 size_t face_smem(const gbf_case* c, const FaceTile& ft, int axis) {
   const int R = recon_radius(c->recon);
   long long pv = 1;
   for (int b = 0; b < 3; ++b) pv *= ft.t[b] + (b == axis ? 2 * R - 1 : 0);
   const bool cons_pencil =
       c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
-  return (size_t)(cons_pencil ? 10 : 5) * pv * sizeof(double);
+  const bool share = !(c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_NO_CONVECTIVE)) &&
+                     c->recon_var == GBF_RECVAR_PRIMITIVE &&
+                     (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS || c->recon == GBF_RECON_TENO5);
+  return (size_t)(cons_pencil ? 10 : (share ? 20 : 5)) * pv * sizeof(double);
 }
 
 // The face kernel of the case's scheme family (as launch_sweep_schemes picks

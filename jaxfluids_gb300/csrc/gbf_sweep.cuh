@@ -494,9 +494,14 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
 // face states into smax_faces and returns false without a flux.
 // VISC: 0 no dissipative fluxes, 1 dissipative fluxes with the stencils of
 // p.diss_*, 2 dissipative fluxes with CENTRAL4 stencils fixed at compile time
-template <int AX, int RECON, int RIEMANN, int MODE, int VISC>
+// SHARE (the WENO5 family on primitive variables): the smoothness indicators'
+// window terms come from sm_win (weno5_window_terms of every pencil cell,
+// arrays dl, dr, e of 5 x pvol each, in that order) instead of being formed
+// per face.
+template <int AX, int RECON, int RIEMANN, int MODE, int VISC, bool SHARE = false>
 __device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm_prim, int pvol, int pstride,
-                                          int base, const int q[3], double F[5], double& smax_faces) {
+                                          int base, const int q[3], double F[5], double& smax_faces,
+                                          const double* sm_win = nullptr) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
   double PL[5], PR[5];
@@ -525,6 +530,20 @@ __device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm
     const double* b = sm_prim + base;
     auto w = [&](int v, int k) { return b[v * pvol + k * pstride]; };
     char_reconstruct<AX>(w, p.fp, PL, PR);
+  } else if constexpr (SHARE) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double w[6], dl[5], dr[5], e[4];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) w[k] = sm_prim[v * pvol + base + k * pstride];
+#pragma unroll
+      for (int k = 1; k <= 3; ++k) dl[k] = sm_win[v * pvol + base + k * pstride];
+#pragma unroll
+      for (int k = 2; k <= 4; ++k) dr[k] = sm_win[(5 + v) * pvol + base + k * pstride];
+#pragma unroll
+      for (int k = 2; k <= 3; ++k) e[k] = sm_win[(10 + v) * pvol + base + k * pstride];
+      reconstruct_pair_shared<RECON>(w, dl, dr, e, p.fp.stencil_eps, PL[v], PR[v]);
+    }
   } else {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
