@@ -111,6 +111,48 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
   }
+  // the dissipative fluxes' per-cell values (DissShared), once per cell of the
+  // tile's faces' normal stencils (normal offsets -2..1 around each face)
+  // instead of once per face reading them: the temperature and the centre
+  // derivatives of the tangential velocity gradient, with the same reads and
+  // arithmetic as the per-face forms
+  double* sm_vis = smem + (CONS ? 10 : 5) * pvol;
+  int se[3] = {fe[0], fe[1], fe[2]};
+  se[AX] += 3;
+  const int svol = se[0] * se[1] * se[2];
+  const int sstride = (AX == 0) ? se[1] * se[2] : ((AX == 1) ? se[2] : 1);
+  if (VISC > 0 && !(RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass)) {
+    // CENTRAL2 everywhere reads only normal offsets -1 and 0
+    const bool c4any = VISC == 2 || p.diss_face == 0 || p.diss_recon == 0;
+    for (int i = threadIdx.x; i < svol; i += blockDim.x) {
+      const int s2 = i % se[2];
+      const int r = i / se[2];
+      const int s1 = r % se[1];
+      const int s0 = r / se[1];
+      const int k = (AX == 0) ? s0 : ((AX == 1) ? s1 : s2);
+      if (!c4any && (k == 0 || k == se[AX] - 1)) continue;
+      int gc[3] = {o[0] + s0, o[1] + s1, o[2] + s2};
+      gc[AX] -= 2;
+      auto cell = [&](int v, int kax, int ax2, int k2) {
+        int g[3] = {gc[0], gc[1], gc[2]};
+        g[AX] += kax;
+        g[ax2] += k2;
+        return global_prim<MODE_STAGE_P>(p, v, g[0], g[1], g[2]);
+      };
+      if (p.heat) sm_vis[i] = cell(4, 0, AX, 0) / (cell(0, 0, AX, 0) * p.R);
+      if (p.viscous) {
+        int t = 0;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          if (ax == AX || !(p.active_mask & (1 << ax))) continue;
+          sm_vis[(1 + 2 * t) * svol + i] = centre_deriv_at<VISC == 2>(p, cell, AX, ax, 0);
+          sm_vis[(2 + 2 * t) * svol + i] = centre_deriv_at<VISC == 2>(p, cell, ax, ax, 0);
+          ++t;
+        }
+      }
+    }
+    __syncthreads();
+  }
   int ext[3] = {p.n[0], p.n[1], p.n[2]};
   ext[AX] = ft.nf;
   const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
@@ -123,9 +165,12 @@ __global__ void __launch_bounds__(256, 2)
     const int f0 = r / fe[1];
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     const int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
+    int sf[3] = {f0, f1, f2};
+    sf[AX] += 2;
+    const DissShared ds{VISC > 0 ? sm_vis + idx3(sf[0], sf[1], sf[2], se[1], se[2]) : nullptr, svol, sstride};
     double F[5];
     if (!face_flux<AX, RECON, RIEMANN, MODE_STAGE_P, VISC, SHARE>(p, smem, pvol, pstride, base, q, F, smax_faces,
-                                                                   sm_win))
+                                                                   sm_win, ds))
       continue;
     const long long g = ((long long)q[0] * ext[1] + q[1]) * ext[2] + q[2];
 #pragma unroll

@@ -175,7 +175,14 @@ size_t face_smem(const gbf_case* c, const FaceTile& ft, int axis) {
   const bool share = !(c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_NO_CONVECTIVE)) &&
                      c->recon_var == GBF_RECVAR_PRIMITIVE &&
                      (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS || c->recon == GBF_RECON_TENO5);
-  return (size_t)(cons_pencil ? 10 : (share ? 20 : 5)) * pv * sizeof(double);
+  // the dissipative fluxes' per-cell values: 5 doubles per cell of the faces'
+  // normal stencils (face_flux_kernel, DissShared)
+  long long sv = 0;
+  if (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) {
+    sv = 1;
+    for (int b = 0; b < 3; ++b) sv *= ft.t[b] + (b == axis ? 3 : 0);
+  }
+  return (size_t)((cons_pencil ? 10 : (share ? 20 : 5)) * pv + 5 * sv) * sizeof(double);
 }
 
 // The face kernel of the case's scheme family (as launch_sweep_schemes picks

@@ -305,8 +305,30 @@ __device__ __forceinline__ double face_interp_along(const SweepParams& p, const 
 // stencil, tangential ones as face reconstructions of centre derivatives
 // (source_term_solver.py compute_velocity_gradient :414-448 and
 // compute_xi_derivatives_at_xj :538-580, stencils chosen at :57-118).
+// The centre derivative d u_a / d x_i (i != AX) of the cell at normal offset
+// kax from the face (deriv_center_4.py / deriv_center_2.py).
+template <bool C4, class Cell>
+__device__ __forceinline__ double centre_deriv_at(const SweepParams& p, const Cell& cell, int a, int i, int kax) {
+  const double odi = p.one_dx[i];
+  return (C4 || p.diss_center == 0) ? c4_center_deriv(odi, cell(1 + a, kax, i, -2), cell(1 + a, kax, i, -1),
+                                                    cell(1 + a, kax, i, 1), cell(1 + a, kax, i, 2))
+                                  : c2_center_deriv(odi, cell(1 + a, kax, i, -1), cell(1 + a, kax, i, 1));
+}
+
+// Per-cell values of the dissipative fluxes shared by the faces that read
+// them (the face kernels form them once per pencil cell): sv[kax * sstride]
+// is the temperature p / (rho R) of the cell at normal offset kax from the
+// face, sv[(1 + j) * svol + kax * sstride] its centre derivative j, j = 2 t +
+// which over the tangential active axes t in axis order (which 0: d u_AX / d
+// x_t, 1: d u_t / d x_t).  Null: formed per face.
+struct DissShared {
+  const double* sv;
+  int svol, sstride;
+};
+
 template <int AX, bool C4 = false, class Cell>
-__device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, const Cell& cell, double gr[3][3]) {
+__device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, const Cell& cell, double gr[3][3],
+                                                       const DissShared& ds = DissShared{nullptr, 0, 0}) {
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -314,20 +336,20 @@ __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, con
   const double odx = p.one_dx[AX];
 #pragma unroll
   for (int a = 0; a < 3; ++a) gr[a][AX] = face_deriv_along<C4>(p, odx, [&](int k) { return cell(1 + a, k, AX, 0); });
+  int t = 0;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     if (i == AX || !(p.active_mask & (1 << i))) continue;
-    const double odi = p.one_dx[i];
     // d u_AX / d x_i and d u_i / d x_i
 #pragma unroll
     for (int which = 0; which < 2; ++which) {
       const int a = (which == 0) ? AX : i;
+      const double* sj = ds.sv ? ds.sv + (1 + 2 * t + which) * ds.svol : nullptr;
       gr[a][i] = face_interp_along<AX, C4>(p, [&](int kax) {
-        return (C4 || p.diss_center == 0) ? c4_center_deriv(odi, cell(1 + a, kax, i, -2), cell(1 + a, kax, i, -1),
-                                                      cell(1 + a, kax, i, 1), cell(1 + a, kax, i, 2))
-                                    : c2_center_deriv(odi, cell(1 + a, kax, i, -1), cell(1 + a, kax, i, 1));
+        return sj ? sj[kax * ds.sstride] : centre_deriv_at<C4>(p, cell, a, i, kax);
       });
     }
+    ++t;
   }
 }
 
@@ -340,7 +362,8 @@ __device__ __forceinline__ void face_velocity_gradient(const SweepParams& p, con
 // (space_solver.py:565-585).
 // C4: the stencils are CENTRAL4 at compile time (else chosen by p.diss_*).
 template <int AX, int MODE, bool C4>
-__device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const int q[3], double F[5]) {
+__device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const int q[3], double F[5],
+                                                     const DissShared& ds = DissShared{nullptr, 0, 0}) {
   auto cell = [&](int v, int kax, int ax2, int k2) {
     int g[3] = {q[0], q[1], q[2]};
     g[AX] += kax;
@@ -350,7 +373,7 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
   const double odx = p.one_dx[AX];
   if (p.viscous) {
     double gr[3][3];
-    face_velocity_gradient<AX, C4>(p, cell, gr);
+    face_velocity_gradient<AX, C4>(p, cell, gr, ds);
     double tau[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -380,8 +403,9 @@ __device__ __forceinline__ void add_dissipative_flux(const SweepParams& p, const
     F[4] = F[4] + (-vt);
   }
   if (p.heat) {
-    const double dT =
-        face_deriv_along<C4>(p, odx, [&](int k) { return cell(4, k, AX, 0) / (cell(0, k, AX, 0) * p.R); });
+    const double dT = face_deriv_along<C4>(p, odx, [&](int k) {
+      return ds.sv ? ds.sv[k * ds.sstride] : cell(4, k, AX, 0) / (cell(0, k, AX, 0) * p.R);
+    });
     F[4] = F[4] + (-p.kappa) * dT;
   }
 }
@@ -498,10 +522,13 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
 // window terms come from sm_win (weno5_window_terms of every pencil cell,
 // arrays dl, dr, e of 5 x pvol each, in that order) instead of being formed
 // per face.
+// ds: the dissipative fluxes' per-cell values at the face's cells (see
+// DissShared; null pointer: formed per face).
 template <int AX, int RECON, int RIEMANN, int MODE, int VISC, bool SHARE = false>
 __device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm_prim, int pvol, int pstride,
                                           int base, const int q[3], double F[5], double& smax_faces,
-                                          const double* sm_win = nullptr) {
+                                          const double* sm_win = nullptr,
+                                          const DissShared& ds = DissShared{nullptr, 0, 0}) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
   double PL[5], PR[5];
@@ -586,7 +613,7 @@ __device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm
     // (limiter_interpolation.py:206)
     riemann_flux<AX, RIEMANN>(PL, PR, p.fp, F);
   }
-  if (VISC) add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F);
+  if (VISC) add_dissipative_flux<AX, MODE, VISC == 2>(p, q, F, ds);
   return true;
 }
 
