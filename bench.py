@@ -387,6 +387,10 @@ def run_adjoint(args):
             "config": {"workload": f"KH {n}^2 periodic, {steps} fixed-dt RK3 steps (dt {dt:.4e})",
                        "schedule": args.adj_schedule, "checkpoint_every": args.adj_every, "cells": n * n},
             "forward_s": t_fwd, "gradient_s": t_adj, "forward_steps_recomputed": adj.forward_steps,
+            # the gradient's two parts: the forward run that places the
+            # checkpoints, and the reverse sweep (replays + step VJPs)
+            "gradient_forward_s": adj.last_split[0], "gradient_reverse_s": adj.last_split[1],
+            "reverse_over_forward": adj.last_split[1] / t_fwd,
             "forward_cell_updates_per_s": n * n * steps / t_fwd,
             "grad_v_norm": float(dv.norm()), "loss": float(0.5 * ((UN[0] - target) ** 2).sum())}
     print(json.dumps(line), flush=True)
@@ -444,6 +448,8 @@ def run_viscous_adjoint(args):
                        "schedule": "binomial", "slots": args.adj_slots, "leaf": args.adj_leaf,
                        "cells": n ** 3},
             "forward_s": t_fwd, "gradient_s": t_adj, "forward_steps_recomputed": adj.forward_steps,
+            "gradient_forward_s": adj.last_split[0], "gradient_reverse_s": adj.last_split[1],
+            "reverse_over_forward": adj.last_split[1] / t_fwd,
             "peak_device_gb": torch.cuda.max_memory_allocated(device) / 1e9,
             "final_ke": ke, "grad_u_norm": float(gu.norm())}
     print(json.dumps(line), flush=True)

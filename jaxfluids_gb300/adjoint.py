@@ -114,13 +114,21 @@ class AdjointRK3:
         return out
 
     # ---- uniform checkpoints ----------------------------------------------
-    def forward_uniform(self, U0: torch.Tensor, nsteps: int, every: int) -> Tuple[torch.Tensor, Dict[int, torch.Tensor]]:
-        ckpt = {0: U0.clone()}
+    def forward_uniform(self, U0: torch.Tensor, nsteps: int, every: int,
+                        keep_last: bool = False) -> Tuple[torch.Tensor, "UniformCheckpoints"]:
+        """U_N and the states at steps 0, every, 2 every, ...  With keep_last the
+        last segment runs keeping its stage states (ckpt.last = (start, store)),
+        which the reverse sweep then uses instead of replaying that segment."""
+        ckpt = UniformCheckpoints({0: U0.clone()})
         U = U0
         k = 0
         while k < nsteps:
             m = min(every, nsteps - k)
-            U = self.advance(U, m)
+            if keep_last and k + m >= nsteps:
+                U, store = self.forward_stored(U, m)
+                ckpt.last = (k, store)
+            else:
+                U = self.advance(U, m)
             k += m
             if k < nsteps:
                 ckpt[k] = U.clone()
@@ -134,8 +142,14 @@ class AdjointRK3:
         VJPs recompute nothing, otherwise it keeps one state per step and each
         step VJP recomputes its two stage states."""
         starts = sorted(s for s in ckpt if s < nsteps)
+        last = getattr(ckpt, "last", None)
         for s in reversed(starts):
             m = min(every, nsteps - s)
+            if last is not None and last[0] == s:
+                # the forward run kept this segment's stage states
+                lam = self.backward_stored(last[1], lam)
+                ckpt.last = last = None
+                continue
             if keep_stages:
                 _, store = self.forward_stored(ckpt[s], m)
                 lam = self.backward_stored(store, lam)
@@ -258,20 +272,43 @@ class AdjointRK3:
     def gradient(self, U0: torch.Tensor, nsteps: int, loss_grad: Callable[[torch.Tensor], torch.Tensor],
                  schedule: str = "uniform", every: int = 50, slots: int = 8, keep_stages: bool = True,
                  leaf: int = 1):
-        """(U_N, dL/dU_0) for a loss whose gradient w.r.t. U_N is loss_grad(U_N)."""
+        """(U_N, dL/dU_0) for a loss whose gradient w.r.t. U_N is loss_grad(U_N).
+
+        The forward run (checkpoints placed) and the reverse sweep (replays and
+        step VJPs) are timed apart with CUDA events on the current stream:
+        self.last_split = (forward seconds, reverse seconds) after the call."""
+        if schedule not in ("uniform", "binomial", "stored"):
+            raise ValueError(schedule)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if U0.is_cuda else None
+        if ev:
+            ev[0].record()
         if schedule == "uniform":
-            UN, ckpt = self.forward_uniform(U0, nsteps, every)
-            lam = loss_grad(UN)
-            return UN, self.backward_uniform(ckpt, nsteps, every, lam, keep_stages)
-        if schedule == "binomial":
+            UN, ckpt = self.forward_uniform(U0, nsteps, every, keep_last=True)
+        elif schedule == "binomial":
             UN, store, spine = self.forward_binomial(U0, nsteps, slots, leaf)
-            lam = loss_grad(UN)
-            return UN, self.backward_binomial(store, spine, lam)
-        if schedule == "stored":
+        else:
             UN, store = self.forward_stored(U0, nsteps)
-            lam = loss_grad(UN)
-            return UN, self.backward_stored(store, lam)
-        raise ValueError(schedule)
+        if ev:
+            ev[1].record()
+        lam = loss_grad(UN)
+        if schedule == "uniform":
+            dU0 = self.backward_uniform(ckpt, nsteps, every, lam, keep_stages)
+        elif schedule == "binomial":
+            dU0 = self.backward_binomial(store, spine, lam)
+        else:
+            dU0 = self.backward_stored(store, lam)
+        if ev:
+            ev[2].record()
+            ev[2].synchronize()
+            self.last_split = (ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3)
+        return UN, dU0
+
+
+class UniformCheckpoints(dict):
+    """Uniform checkpoints {step: state}; `last` optionally holds the last
+    segment's (start step, stored stage states) from the forward run."""
+
+    last = None
 
 
 class RK3Trajectory(torch.autograd.Function):
@@ -283,7 +320,7 @@ class RK3Trajectory(torch.autograd.Function):
         ctx.adj, ctx.nsteps, ctx.schedule, ctx.every, ctx.slots, ctx.leaf = adj, nsteps, schedule, every, slots, leaf
         U0c = U0.detach().contiguous()
         if schedule == "uniform":
-            UN, ckpt = adj.forward_uniform(U0c, nsteps, every)
+            UN, ckpt = adj.forward_uniform(U0c, nsteps, every, keep_last=True)
             ctx.ckpt = ckpt
         else:
             UN, ctx.store, ctx.spine = adj.forward_binomial(U0c, nsteps, slots, leaf)

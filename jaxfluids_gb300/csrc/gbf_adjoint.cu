@@ -461,8 +461,11 @@ int vjp_check(const gbf_case* c) {
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // Lax-Friedrichs' global maximum and CHAR-CONSERVATIVE have no reverse
-  if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS) return GBF_ERR_UNSUPPORTED;
+  // Lax-Friedrichs' axis speed is reversed on the PRIMITIVE reconstructions;
+  // CHAR-CONSERVATIVE has no reverse
+  if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && c->recon_var != GBF_RECVAR_PRIMITIVE &&
+      !(c->flags & GBF_FLAG_NO_CONVECTIVE))
+    return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
@@ -490,8 +493,30 @@ inline bool vjp_cons(const gbf_case* c) {
   return c->recon_var == GBF_RECVAR_CONSERVATIVE && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
 }
 
+inline bool vjp_lf(const gbf_case* c) {
+  return c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+}
+
+// Lax-Friedrichs tie list: two entries (both face states) per face of the
+// axis with the most faces
+long long lf_ties_cap(const gbf_case* c, const CaseInfo& ci) {
+  long long cap = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a))) continue;
+    const long long nf = c->bc[2 * a] == GBF_BC_PERIODIC ? ci.n[a] : ci.n[a] + 1;
+    cap = std::max(cap, 2 * (ci.cells / ci.n[a]) * nf);
+  }
+  return cap;
+}
+
+// Lax-Friedrichs scratch: the state's primitives, the speeds and their
+// cotangents (8 doubles), the tie counters (4) and list
+long long vjp_lf_doubles(const gbf_case* c, const CaseInfo& ci) {
+  return vjp_lf(c) ? 5 * ci.cells + 8 + 4 + lf_ties_cap(c, ci) : 0;
+}
+
 long long vjp_extra_doubles(const gbf_case* c, const CaseInfo& ci) {
-  return vjp_visc_doubles(c, ci) + (vjp_cons(c) ? 5 * ci.cells : 0);
+  return vjp_visc_doubles(c, ci) + (vjp_cons(c) ? 5 * ci.cells : 0) + vjp_lf_doubles(c, ci);
 }
 
 // VJP of the rhs at state U (interior): out = J(U)^T w.  dP: zeroed scratch of 5 n doubles
@@ -532,6 +557,24 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   vp.dP = dP;
   vp.dU = vjp_cons(c) ? extra + vjp_visc_doubles(c, ci) : nullptr;
   if (vp.dU) zero_kernel<<<grid_for(5 * ci.cells), 256, 0, s>>>(vp.dU, 5 * ci.cells);
+  vp.lf_alpha = nullptr;
+  vp.lf_dalpha = nullptr;
+  // Lax-Friedrichs: the axes' speeds of U from the forward face kernels'
+  // speed pass on U's primitives (the same face states and arithmetic as the
+  // forward, so the ties below are the forward's)
+  double* lfP = nullptr;
+  double* lfa = nullptr;
+  unsigned long long* ties = nullptr;
+  if (vjp_lf(c)) {
+    lfP = extra + vjp_visc_doubles(c, ci) + (vjp_cons(c) ? 5 * ci.cells : 0);
+    lfa = lfP + 5 * ci.cells;
+    ties = reinterpret_cast<unsigned long long*>(lfa + 8);
+    if ((st = launch_convert(c, U, lfP, ci.cells, 1, s)) != GBF_OK) return st;
+    if (cudaMemsetAsync(lfa, 0, 8 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
+    if ((st = launch_lf_face_pass(c, ci, U, lfP, lfa, nullptr, 0, 1, -1, nullptr, s)) != GBF_OK) return st;
+    vp.lf_alpha = lfa;
+    vp.lf_dalpha = lfa + 3;
+  }
   const int grid = vp.sp.tiles[0] * vp.sp.tiles[1] * vp.sp.tiles[2];
   if (c->flags & GBF_FLAG_NO_CONVECTIVE)
     st = GBF_OK;  // dissipative fluxes only
@@ -547,6 +590,27 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
     st = launch_vjp_short(c->recon, c->riemann, vp, grid, threads, smem, s);
   if (st != GBF_OK) return st;
   if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
+  if (vjp_lf(c)) {
+    // the speeds' cotangents to the face states attaining them, axis by axis
+    const long long cap = lf_ties_cap(c, ci);
+    for (int a = 0; a < 3; ++a) {
+      if (!(ci.active_mask & (1 << a))) continue;
+      LfTieParams tp;
+      if (cudaMemsetAsync(ties, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess) return GBF_ERR_CUDA;
+      if ((st = launch_lf_face_pass(c, ci, U, lfP, lfa, ties, cap, 2, a, &tp.sp, s)) != GBF_OK) return st;
+      tp.ties = ties;
+      tp.cap = cap;
+      tp.dalpha = lfa + 3;
+      tp.dP = dP;
+      if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
+        st = launch_lf_ties_weno5(c->recon, a, tp, s);
+      else if (c->recon == GBF_RECON_TENO5)
+        st = launch_lf_ties_teno5(a, tp, s);
+      else
+        st = launch_lf_ties_short(c->recon, a, tp, s);
+      if (st != GBF_OK) return st;
+    }
+  }
   if (vjp_dissipative(c)) {
     ViscVjpParams q;
     q.sp = vp.sp;

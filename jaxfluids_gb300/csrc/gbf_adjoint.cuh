@@ -633,6 +633,44 @@ __device__ __forceinline__ void rusanov_vjp(const double PL[5], const double PR[
   cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
 
+// Lax-Friedrichs flux with the axis' speed alpha held fixed
+// (LaxFriedrichs.py:33-45): F = 0.5 (F_L + F_R) - 0.5 alpha (U_R - U_L).  The
+// face states' cotangents go to dPL, dPR; the cotangent of alpha,
+// -0.5 sum_v dF_v (U_R - U_L)_v, is added to dalpha (the caller reduces it
+// over the axis and hands it to the face states that attain the maximum).
+template <int AX>
+__device__ __forceinline__ void lf_vjp(const double PL[5], const double PR[5], const FaceParams& fp, double alpha,
+                                       const double dF[5], double dPL[5], double dPR[5], double& dalpha) {
+  const double igm1 = 1.0 / fp.gm1;
+  double UL[5], UR[5];
+  cons_from_prims(PL, UL, fp.gm1);
+  cons_from_prims(PR, UR, fp.gm1);
+  double dUL[5], dUR[5], g[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    g[v] = 0.5 * dF[v];
+    dalpha += -0.5 * dF[v] * (UR[v] - UL[v]);
+    dUR[v] = -0.5 * alpha * dF[v];
+    dUL[v] = 0.5 * alpha * dF[v];
+  }
+  physical_flux_vjp<AX>(PL, UL, g, dPL, dUL);
+  physical_flux_vjp<AX>(PR, UR, g, dPR, dUR);
+  cons_from_prims_vjp(PL, dUL, 1.0 / PL[0], igm1, dPL);
+  cons_from_prims_vjp(PR, dUR, 1.0 / PR[0], igm1, dPR);
+}
+
+// Pullback of a cotangent ds on the Lax-Friedrichs speed s = |u_n| + c of a
+// face state P (ideal gas, c = sqrt(gamma p / rho)) onto P: jnp.abs has
+// derivative +-1 (+1 at 0, jabs_grad), dc/dp = c / (2 p), dc/drho = -c / (2 rho).
+template <int AX>
+__device__ __forceinline__ void lf_speed_vjp(const double P[5], const FaceParams& fp, double ds, double dP[5]) {
+  const double c = sqrt(fp.gamma * P[4] / P[0]);
+  dP[AX + 1] += ds * jabs_grad(P[AX + 1]);
+  const double h = 0.5 * ds * c;
+  dP[4] += h / P[4];
+  dP[0] -= h / P[0];
+}
+
 // Reverse of frozen_state (eigendecomposition.py:120-281) for the single-phase
 // ideal gas: cotangents of (rho_a, c, cc) pulled back onto the primitives of
 // the two cells L, R adjacent to the face (accumulated into dL, dR).

@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * nfaces + g] = F[v];
   }
-  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) lf_speed_reduce<AX>(p, smax_faces);
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass == 1) lf_speed_reduce<AX>(p, smax_faces);
 }
 
 // Host side ------------------------------------------------------------------

@@ -43,6 +43,12 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
 // The Lax-Friedrichs speed slots of the current device (gbf_sweep.cu).
 int lf_alpha_on_current_device(double** out);
 
+// Lax-Friedrichs speed (mode 1) and tie (mode 2) passes of the face kernels
+// for the adjoint (gbf_stage.cu).
+int launch_lf_face_pass(const gbf_case* c, const CaseInfo& ci, const double* U, const double* P, double* alpha,
+                        unsigned long long* ties, long long cap, int mode, int axis, SweepParams* out,
+                        cudaStream_t s);
+
 // The fused RK stage (gbf_stage.cu): doubles of the three face buffers (and
 // the Lax-Friedrichs speed slots), their layout in a block of that size, and
 // one stage (p: prims, cons, cons0, out,

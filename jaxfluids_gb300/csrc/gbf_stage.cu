@@ -263,6 +263,44 @@ void stage_face_buffers(const gbf_case* c, const CaseInfo& ci, double* base, Fac
   fb->lf_alpha = base;
 }
 
+// Lax-Friedrichs passes of the face kernels over a state's interior
+// primitives P (U its conservatives), for the adjoint: mode 1 reduces every
+// active axis' speed into alpha[0..2] (zeroed by the caller), mode 2 lists
+// the ties of axis `axis` with alpha[axis] into ties (counters zeroed by the
+// caller, cap entries).  The launch parameters go to *out.
+int launch_lf_face_pass(const gbf_case* c, const CaseInfo& ci, const double* U, const double* P, double* alpha,
+                        unsigned long long* ties, long long cap, int mode, int axis, SweepParams* out,
+                        cudaStream_t s) {
+  SweepParams q;
+  int thr;
+  size_t sm;
+  int st = make_sweep_params(c, ci, nullptr, &q, &thr, &sm);
+  if (st != GBF_OK) return st;
+  q.cons = U;
+  q.cons0 = U;
+  q.prims = P;
+  q.lf_alpha = alpha;
+  q.speed_pass = mode;
+  q.lf_ties = ties;
+  q.lf_ties_cap = cap;
+  q.reduce_dt = 0;
+  FaceBuffers fb{};
+  for (int a = 0; a < 3; ++a)
+    if (ci.active_mask & (1 << a)) fb.nf[a] = periodic_axis(c, a) ? ci.n[a] : ci.n[a] + 1;
+  fb.lf_alpha = alpha;
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a)) || (mode == 2 && a != axis)) continue;
+    FaceTile ft;
+    int threads;
+    if ((st = make_face_tile(ci, nullptr, a, fb.nf[a], &ft, &threads)) != GBF_OK) return st;
+    const size_t smem = face_smem(c, ft, a);
+    if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+    if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
+  }
+  if (out) *out = q;
+  return GBF_OK;
+}
+
 // p carries the stage: prims (primitives of p.cons), cons, cons0, out, stage,
 // reduce_dt, dt_state.  prims_out (may be null) receives the primitives of
 // the new state.  Lax-Friedrichs runs a speed pass of each axis' face kernel

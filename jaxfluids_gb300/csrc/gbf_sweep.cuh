@@ -80,10 +80,29 @@ struct SweepParams {
   int gravity;               // volume force on
   double g[3];               // gravity vector
   // Lax-Friedrichs (Rusanov instantiations): the per-axis dissipation speeds;
-  // speed_pass reduces them (max of |u| + c over the face states, as bits)
-  // instead of computing fluxes
+  // speed_pass 1 reduces them (max of |u| + c over the face states, as bits)
+  // instead of computing fluxes; speed_pass 2 (face kernels, for the
+  // adjoint) lists the face states whose speed equals the reduced one
   double* lf_alpha;
   int speed_pass;
+  // speed_pass 2: lf_ties[0] entries listed, lf_ties[1 + side] ties of the
+  // left (0) and right (1) states counted as the reference's face arrays hold
+  // them, then the entries (LfTie) from lf_ties[4], at most lf_ties_cap
+  unsigned long long* lf_ties;
+  long long lf_ties_cap;
+};
+
+// One listed Lax-Friedrichs tie: bits 3.. the face's index in its axis' face
+// buffer layout, bit 2 the side (0 left state, 1 right state), bits 0..1 its
+// multiplicity in the reference's face arrays (2 for face -1/2 of a PERIODIC
+// axis, which the arrays also hold as face N - 1/2).
+struct LfTie {
+  static __host__ __device__ unsigned long long pack(long long face, int side, int mult) {
+    return ((unsigned long long)face << 3) | ((unsigned long long)side << 2) | (unsigned long long)mult;
+  }
+  static __host__ __device__ long long face(unsigned long long e) { return (long long)(e >> 3); }
+  static __host__ __device__ int side(unsigned long long e) { return (int)((e >> 2) & 1); }
+  static __host__ __device__ int mult(unsigned long long e) { return (int)(e & 3); }
 };
 
 // Gravity forces added to a cell's right-hand side (source_term_solver.py:165-186,
@@ -510,6 +529,29 @@ __device__ __forceinline__ void stage_pencil(const SweepParams& p, const int o[3
   }
 }
 
+// Lax-Friedrichs ties (speed_pass 2): list the face states of face q whose
+// speed equals the axis' reduced speed (p.lf_alpha[AX], bitwise: the same
+// face states and arithmetic as the reducing pass) and count them with their
+// multiplicity in the reference's face arrays (N + 1 faces per line; face
+// -1/2 of a PERIODIC axis is also its face N - 1/2, whose states are the same).
+template <int AX>
+__device__ __forceinline__ void lf_record_ties(const SweepParams& p, const int q[3], double sL, double sR) {
+  const double a = p.lf_alpha[AX];
+  if (sL != a && sR != a) return;
+  const bool periodic = p.bc[2 * AX] == GBF_BC_PERIODIC;
+  int ext[3] = {p.n[0], p.n[1], p.n[2]};
+  ext[AX] = periodic ? p.n[AX] : p.n[AX] + 1;
+  const long long face = ((long long)q[0] * ext[1] + q[1]) * ext[2] + q[2];
+  const int mult = (periodic && q[AX] == 0) ? 2 : 1;
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    if ((side == 0 ? sL : sR) != a) continue;
+    const unsigned long long i = atomicAdd(p.lf_ties, 1ull);
+    if ((long long)i < p.lf_ties_cap) p.lf_ties[4 + i] = LfTie::pack(face, side, mult);
+    atomicAdd(p.lf_ties + 1 + side, (unsigned long long)mult);
+  }
+}
+
 // Flux of one face along AX from a staged pencil (sm_prim, variable stride
 // pvol, stride pstride along AX); `base` is the pencil index of the face's
 // first stencil cell (R cells left of the face) and q the logical face
@@ -590,7 +632,12 @@ __device__ __forceinline__ bool face_flux(const SweepParams& p, const double* sm
     // LaxFriedrichs.py:35-38: max(max |u_L| + c_L, max |u_R| + c_R) over the axis
     const double cL = speed_of_sound(PL[4], PL[0], p.fp);
     const double cR = speed_of_sound(PR[4], PR[0], p.fp);
-    smax_faces = fmax(smax_faces, fmax(fabs(PL[AX + 1]) + cL, fabs(PR[AX + 1]) + cR));
+    const double sL = fabs(PL[AX + 1]) + cL, sR = fabs(PR[AX + 1]) + cR;
+    if (p.speed_pass == 2) {
+      lf_record_ties<AX>(p, q, sL, sR);
+      return false;
+    }
+    smax_faces = fmax(smax_faces, fmax(sL, sR));
     return false;
   }
   if (RIEMANN == GBF_RIEMANN_RUSANOV && p.lf_alpha) {

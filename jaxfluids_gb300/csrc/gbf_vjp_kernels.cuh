@@ -13,7 +13,23 @@ struct VjpParams {
   const double* w;      // cotangent of the rhs, interior [5][N]
   double* dP;           // primitive cotangent accumulator, interior [5][N]
   double* dU;           // conservative cotangent accumulator (CONSERVATIVE reconstruction), interior [5][N]
+  // Lax-Friedrichs (Rusanov instantiations, PRIMITIVE reconstructions): the
+  // axes' speeds of the state (null: Rusanov's local speeds) and the
+  // accumulators of their cotangents
+  const double* lf_alpha;
+  double* lf_dalpha;
 };
+
+// Lax-Friedrichs flux VJP with the axis' speed fixed, or the scheme's own.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void face_riemann_vjp(const VjpParams& vp, const double PL[5], const double PR[5],
+                                                 const double dF[5], double dPL[5], double dPR[5],
+                                                 double& dalpha) {
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && vp.lf_alpha)
+    lf_vjp<AX>(PL, PR, vp.sp.fp, vp.lf_alpha[AX], dF, dPL, dPR, dalpha);
+  else
+    riemann_flux_vjp<AX, RIEMANN>(PL, PR, vp.sp.fp, dF, dPL, dPR);
+}
 
 // CHAR-PRIMITIVE face (char_reconstruct of the forward): frozen state of the
 // two cells adjacent to the face, characteristic variables of the six window
@@ -160,6 +176,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
   const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
   const double odx = p.one_dx[AX];
+  double dalpha = 0.0;  // Lax-Friedrichs: this thread's share of the speed's cotangent
   for (int f = tid; f < fvol; f += nthr) {
     const int f2 = f % fe[2];
     const int r = f / fe[2];
@@ -264,7 +281,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
           }
       }
       double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+      face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const double gL = dPL[v], gR = dPR[v];
@@ -297,7 +314,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         mR = positivity_limit(PR, c + pstride, pvol, p.limiter);
       }
       double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+      face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         double wv[K], dw[K];
@@ -313,6 +330,11 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         for (int k = 0; k < K; ++k) sm_slot[(v * K + k) * fvol + f] = dw[k];
       }
     }
+  }
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && vp.lf_alpha) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) dalpha += __shfl_xor_sync(0xffffffffu, dalpha, off);
+    if ((tid & 31) == 0 && dalpha != 0.0) atomicAdd(vp.lf_dalpha + AX, dalpha);
   }
   __syncthreads();
 
@@ -400,6 +422,139 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
   if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
   if (p.active_mask & 4) vjp_axis<2, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
 }
+
+// Lax-Friedrichs: the cotangent of each axis' speed alpha = max(max s_L,
+// max s_R), s = |u_n| + c of the face states (LaxFriedrichs.py:35-38), goes
+// to the face states that attain it, as jax.grad divides it: jnp.maximum
+// gives half to each side when both maxima are equal, jnp.max equal shares to
+// the ties of a side.  One thread per listed tie (the face kernels' tie pass,
+// speed_pass 2, on the same primitives): the tie's face states and stencil
+// gradients, the speed's pullback, then the stencil cells' cotangents
+// through the boundary remap into dP.  PRIMITIVE reconstructions.
+struct LfTieParams {
+  SweepParams sp;                   // the state's interior primitives (sp.prims), sizes, boundaries, scheme
+  const unsigned long long* ties;   // the tie pass's counters and LfTie entries
+  long long cap;                    // entries the list holds
+  const double* dalpha;             // cotangent of each axis' speed
+  double* dP;                       // primitive cotangent accumulator, interior [5][N]
+};
+
+template <int AX, int RECON>
+__global__ void __launch_bounds__(128) lf_tie_vjp_kernel(const LfTieParams tp) {
+  const SweepParams& p = tp.sp;
+  constexpr int R = ReconTraits<RECON>::R;
+  constexpr int K = 2 * R;
+  const unsigned long long listed = tp.ties[0];
+  const long long n = (long long)listed < tp.cap ? (long long)listed : tp.cap;
+  const double nL = (double)tp.ties[1], nR = (double)tp.ties[2];
+  const double share = tp.dalpha[AX] * ((nL > 0.0 && nR > 0.0) ? 0.5 : 1.0);
+  const bool periodic = p.bc[2 * AX] == GBF_BC_PERIODIC;
+  int ext[3] = {p.n[0], p.n[1], p.n[2]};
+  ext[AX] = periodic ? p.n[AX] : p.n[AX] + 1;
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  const double eps = p.fp.stencil_eps;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long t = tp.ties[4 + e];
+    const long long face = LfTie::face(t);
+    const int side = LfTie::side(t);
+    const double ds = share * LfTie::mult(t) / (side == 0 ? nL : nR);
+    int q[3];
+    q[2] = (int)(face % ext[2]);
+    const long long r = face / ext[2];
+    q[1] = (int)(r % ext[1]);
+    q[0] = (int)(r / ext[1]);
+    // stencil cells q[AX] - R .. q[AX] + R - 1 (face q[AX] - 1/2)
+    double wv[5][K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      int g[3] = {q[0], q[1], q[2]};
+      g[AX] += k - R;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) wv[v][k] = global_prim<MODE_STAGE_P>(p, v, g[0], g[1], g[2]);
+    }
+    double PL[5], PR[5], jl[5][5], jr[5][5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double* w = wv[v];
+      if constexpr (RECON == GBF_RECON_WENO5Z) {
+        weno5z_jac(w[0], w[1], w[2], w[3], w[4], eps, PL[v], jl[v]);
+        weno5z_jac(w[5], w[4], w[3], w[2], w[1], eps, PR[v], jr[v]);
+      } else if constexpr (RECON == GBF_RECON_TENO5) {
+        teno5_jac(w[0], w[1], w[2], w[3], w[4], eps, PL[v], jl[v]);
+        teno5_jac(w[5], w[4], w[3], w[2], w[1], eps, PR[v], jr[v]);
+      } else if constexpr (RECON == GBF_RECON_WENO5JS) {
+        weno5js_jac(w[0], w[1], w[2], w[3], w[4], eps, PL[v], jl[v]);
+        weno5js_jac(w[5], w[4], w[3], w[2], w[1], eps, PR[v], jr[v]);
+      } else {
+        reconstruct_pair<RECON>(w, eps, PL[v], PR[v]);
+      }
+    }
+    unsigned mL = 0, mR = 0;
+    if (p.limiter) {
+      // the limited primitives are those of the cell beside the face
+      mL = positivity_limit(PL, &wv[0][R - 1], K, p.limiter);
+      mR = positivity_limit(PR, &wv[0][R], K, p.limiter);
+    }
+    double dPs[5] = {0, 0, 0, 0, 0};
+    lf_speed_vjp<AX>(side == 0 ? PL : PR, p.fp, ds, dPs);
+    const unsigned m = side == 0 ? mL : mR;
+    double dw[5][K];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) dw[v][k] = 0.0;
+      const double gv = dPs[v];
+      if (m & (1u << v)) {
+        dw[v][side == 0 ? R - 1 : R] = gv;
+      } else if constexpr (R == 3) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          if (side == 0) dw[v][k] += gv * jl[v][k];
+          else dw[v][5 - k] += gv * jr[v][k];
+        }
+      } else {
+        double d[K];
+        reconstruct_pair_vjp<RECON>(wv[v], eps, side == 0 ? gv : 0.0, side == 1 ? gv : 0.0, d);
+#pragma unroll
+        for (int k = 0; k < K; ++k) dw[v][k] = d[k];
+      }
+    }
+    // stencil cells' cotangents, halo cells through the transpose of their face rule
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      int g[3] = {q[0], q[1], q[2]};
+      g[AX] += k - R;
+      double d[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] = dw[v][k];
+      if (g[AX] < 0 || g[AX] >= p.n[AX]) {
+        const int ty = face_type_at(p.bc, p.bf, 2 * AX + (g[AX] >= 0 ? 1 : 0), face_pos(p.n, AX, g));
+        g[AX] = bc_src(g[AX], p.n[AX], ty);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) d[v] *= bc_apply_grad(ty, AX, v);
+      }
+      const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (d[v] != 0.0) atomicAdd(tp.dP + v * cs + off, d[v]);
+    }
+  }
+}
+
+template <int RECON>
+int launch_lf_ties_one(int axis, const LfTieParams& tp, cudaStream_t s) {
+  const int grid = 152 * 4, threads = 128;
+  if (axis == 0) lf_tie_vjp_kernel<0, RECON><<<grid, threads, 0, s>>>(tp);
+  else if (axis == 1) lf_tie_vjp_kernel<1, RECON><<<grid, threads, 0, s>>>(tp);
+  else lf_tie_vjp_kernel<2, RECON><<<grid, threads, 0, s>>>(tp);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+// The tie kernels per reconstruction family (gbf_vjp_<family>.cu).
+int launch_lf_ties_weno5(int recon, int axis, const LfTieParams& tp, cudaStream_t s);
+int launch_lf_ties_teno5(int axis, const LfTieParams& tp, cudaStream_t s);
+int launch_lf_ties_short(int recon, int axis, const LfTieParams& tp, cudaStream_t s);
 
 // Launch of rhs_vjp_kernel for one reconstruction family (mode of the
 // gbf_vjp_<family>.cu units): recon and riemann select the instantiation.

@@ -13,4 +13,13 @@ int launch_vjp_short(int recon, int riemann, const VjpParams& vp, int grid, int 
   }
 }
 
+int launch_lf_ties_short(int recon, int axis, const LfTieParams& tp, cudaStream_t s) {
+  switch (recon) {
+    case GBF_RECON_WENO3JS: return launch_lf_ties_one<GBF_RECON_WENO3JS>(axis, tp, s);
+    case GBF_RECON_WENO3Z: return launch_lf_ties_one<GBF_RECON_WENO3Z>(axis, tp, s);
+    case GBF_RECON_MINMOD_AD: return launch_lf_ties_one<GBF_RECON_MINMOD_AD>(axis, tp, s);
+    default: return GBF_ERR_UNSUPPORTED;
+  }
+}
+
 }  // namespace gbf

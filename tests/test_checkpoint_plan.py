@@ -81,3 +81,20 @@ def test_uniform_reverses_every_step_once(n, every):
     for keep in (True, False):
         lam = a.backward_uniform(ckpt, n, every, [n], keep_stages=keep)
         assert lam == [n] + list(range(n - 1, -1, -1))
+
+
+@pytest.mark.parametrize("n,every", [(12, 12), (12, 4), (13, 5), (1, 3), (1000, 50)])
+def test_uniform_with_the_last_segment_kept_replays_all_but_it(n, every):
+    for keep in (True, False):
+        a = MockAdjoint()
+        UN, ckpt = a.forward_uniform(Step(0), n, every, keep_last=True)
+        assert UN == n and a.forward_steps == n and sorted(ckpt) == list(range(0, n, every))
+        start = (n - 1) // every * every
+        assert ckpt.last[0] == start and len(ckpt.last[1]) == n - start
+        a.forward_steps = 0
+        lam = a.backward_uniform(ckpt, n, every, [n], keep_stages=keep)
+        assert lam == [n] + list(range(n - 1, -1, -1))
+        # every segment but the kept one is replayed once (its last step too
+        # when it keeps its stage states)
+        replayed = start if keep else start - len([s for s in ckpt if s < start])
+        assert a.forward_steps == replayed and ckpt.last is None

@@ -54,9 +54,22 @@ def smooth_kh_cons(nx, ny, gamma=1.4, seed=7):
     return O.cons_from_prims(P, gamma)
 
 
+def square_wave_prims(n):
+    """1-D periodic state of two constant parts, the faster one (|u| + c) over
+    the periodic wrap: its flat faces, face -1/2 among them, all attain the
+    Lax-Friedrichs speed."""
+    x = (np.arange(n) + 0.5) / n
+    fast = (x < 0.25) | (x >= 0.75)
+    P = np.stack([np.where(fast, 1.0, 0.5), np.where(fast, 0.5, -0.2), np.zeros(n), np.zeros(n),
+                  np.where(fast, 1.0, 0.4)])
+    return torch.from_numpy(P.reshape(5, n, 1, 1))
+
+
 def _interior_cons(kind, cells, oc):
     if kind == "generic":
         return generic_cons(cells)
+    if kind == "square":
+        return O.cons_from_prims(square_wave_prims(cells[0]), 1.4)
     if kind == "kh":
         return kh_cons(cells[0], cells[1])
     if kind == "sod":
@@ -113,6 +126,22 @@ VJP_CASES = [
     ("3d-char-roe-viscous-heat", (16, 12, 14), "PERIODIC", {"nh": 4, "recon_var": "CHAR-PRIMITIVE",
                                                              "frozen_state": "ROE", "viscous": True, "heat": True,
                                                              "mu": 0.02, "prandtl": 0.71}, "generic"),
+    # Lax-Friedrichs: one speed per axis, the maximum over every face state;
+    # its cotangent goes to the states attaining it (the flat parts of Sod
+    # and of the square wave: many ties on both sides, and face -1/2 of the
+    # periodic axis counted twice, as the reference's face arrays hold it)
+    ("2d-weno-lf", (40, 36, 1), "PERIODIC", {"riemann": "LAX-FRIEDRICHS"}, "generic"),
+    ("3d-weno5js-lf-zg", (12, 14, 10), "ZEROGRADIENT", {"recon": "WENO5-JS", "riemann": "LAX-FRIEDRICHS"},
+     "generic"),
+    ("sod-minmodad-lf", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "LAX-FRIEDRICHS"},
+     "sod"),
+    ("1d-minmodad-lf-periodic-ties", (48, 1, 1), "PERIODIC", {"nh": 4, "recon": "MINMOD-AD",
+                                                              "riemann": "LAX-FRIEDRICHS"}, "square"),
+    ("2d-weno3z-lf-sym", (36, 20, 1), {"east": "SYMMETRY", "west": "SYMMETRY", "north": "PERIODIC",
+                                       "south": "PERIODIC", "top": "PERIODIC", "bottom": "PERIODIC"},
+     {"recon": "WENO3-Z", "riemann": "LAX-FRIEDRICHS"}, "generic"),
+    ("2d-teno5-lf-viscous", (20, 16, 1), "PERIODIC", {"nh": 4, "recon": "TENO5", "riemann": "LAX-FRIEDRICHS",
+                                                      "viscous": True, "mu": 0.02}, "generic"),
 ]
 
 

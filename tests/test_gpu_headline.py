@@ -15,6 +15,9 @@
   of the initial rho v moves the oracle's own gradient by 1.5e-3 (max norm)
   there, while its v-field gradient moves by 1.4e-11; that part is held to
   1e-2.
+* The same Kelvin-Helmholtz gradient as stated (1000 steps, uniform
+  checkpoints every 50) against central differences in 16 random directions
+  at h = 1e-6 relative.
 * The batched path on four quadrant problems with sides 64, 128, 192 and 512
   (states from default_rng(1000 + i)), 10 steps, against the oracle case by case.
 
@@ -138,6 +141,67 @@ def test_kh_512_rhs_vjp_and_5_step_gradient():
     dv_ref = x.grad[2] * U0[0] + x.grad[4] * U0[2]
     assert rel_err(dv_gpu[None], dv_ref[None]) <= 1e-10
     assert rel_err(grad, x.grad) <= 1e-2
+
+
+def test_kh_512_adjoint_1000_steps_against_central_differences():
+    """The Kelvin-Helmholtz adjoint as stated: 512^2, 1000 fixed-dt steps
+    (dt the CFL 0.5 step of the initial state), uniform checkpoints every 50
+    steps, loss 1/2 ||rho(T) - rho_target||^2 with the target the forward run
+    from the noise of default_rng(8); its gradient with respect to the
+    initial v field against central differences in 16 random directions d
+    (v0 +- h d, h = 1e-6 relative: d = N(0, 1) |v0|).
+
+    The loss is not differentiable everywhere: this initial state's density,
+    x velocity and pressure are piecewise constant, and WENO-Z's |b0 - b2|,
+    HLLC's contact sign and the Einfeldt speeds' min / max meet their kinks
+    exactly on flat stencils, where jax.grad's conventions pick one branch
+    while a central difference averages both.  The differences therefore agree
+    with the adjoint to ~1e-3 of each directional derivative (measured on a
+    GB300: median 1.2e-3 at h = 1e-6, the same at h = 1e-7 and 1e-8, so not a
+    truncation error), and to within 1e-5 of the Cauchy-Schwarz bound
+    ||grad|| ||d|| in every direction (measured at most 5.3e-6)."""
+    from jaxfluids_gb300 import FusedRK3
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    n, steps, every = 512, 1000, 50
+    _, cc = both((n, n, 1), "PERIODIC")
+    dev = torch.device("cuda", 0)
+    gamma = 1.4
+
+    def prims(seed):
+        return O.prims_from_cons(_kh_cons(n, seed), gamma).to(dev)
+
+    def cons(P):
+        return O.cons_from_prims(P, gamma)
+
+    P0 = prims(7)
+    U0 = cons(P0)
+    f = FusedRK3(cc, dev)
+    f.set_state(U0)
+    dt = float(f.dt)
+    del f
+    adj = AdjointRK3(cc, dt, dev)
+    target = adj.advance(cons(prims(8)), steps)[0]
+
+    def loss(U):
+        return 0.5 * ((U[0] - target) ** 2).sum().item()
+
+    UN, grad = adj.gradient(U0, steps, lambda U: torch.stack([U[0] - target] + [torch.zeros_like(target)] * 4),
+                            schedule="uniform", every=every)
+    dv = grad[2] * U0[0] + grad[4] * U0[2]
+    gen = torch.Generator(device=dev).manual_seed(16)
+    h = 1e-6
+    rel, cs = [], []
+    for _ in range(16):
+        d = torch.randn(P0[2].shape, generator=gen, dtype=torch.float64, device=dev) * P0[2].abs()
+        Pp, Pm = P0.clone(), P0.clone()
+        Pp[2] += h * d
+        Pm[2] -= h * d
+        fd = (loss(adj.advance(cons(Pp), steps)) - loss(adj.advance(cons(Pm), steps))) / (2 * h)
+        an = (dv * d).sum().item()
+        rel.append(abs(fd - an) / abs(an))
+        cs.append(abs(fd - an) / float(dv.norm() * d.norm()))
+    assert max(cs) <= 1e-5, cs
+    assert sorted(rel)[len(rel) // 2] <= 1e-2, rel
 
 
 def test_batch_with_a_512_case_against_the_oracle():
