@@ -461,12 +461,10 @@ int vjp_check(const gbf_case* c) {
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // Lax-Friedrichs' axis speed is reversed on the PRIMITIVE reconstructions;
-  // CHAR-CONSERVATIVE has no reverse
+  // Lax-Friedrichs' axis speed is reversed on the PRIMITIVE reconstructions
   if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && c->recon_var != GBF_RECVAR_PRIMITIVE &&
       !(c->flags & GBF_FLAG_NO_CONVECTIVE))
     return GBF_ERR_UNSUPPORTED;
-  if (c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
@@ -487,10 +485,11 @@ long long vjp_visc_doubles(const gbf_case* c, const CaseInfo& ci) {
   return 5 * ci.cells + VISC_SLOTS * faces;
 }
 
-// the CONSERVATIVE reconstruction's conservative cotangent follows the
-// dissipative part
+// the conservative reconstructions' (CONSERVATIVE, CHAR-CONSERVATIVE)
+// conservative cotangent follows the dissipative part
 inline bool vjp_cons(const gbf_case* c) {
-  return c->recon_var == GBF_RECVAR_CONSERVATIVE && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+  return (c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) &&
+         !(c->flags & GBF_FLAG_NO_CONVECTIVE);
 }
 
 inline bool vjp_lf(const gbf_case* c) {
@@ -579,7 +578,8 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   if (c->flags & GBF_FLAG_NO_CONVECTIVE)
     st = GBF_OK;  // dissipative fluxes only
   else if (vjp_cons(c))
-    st = launch_vjp_cons(c->riemann, vp, grid, threads, smem, s);
+    st = (c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE) ? launch_vjp_charcons(c->riemann, vp, grid, threads, smem, s)
+                                                        : launch_vjp_cons(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
     st = launch_vjp_char(c->riemann, vp, grid, threads, smem, s);
   else if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)

@@ -746,6 +746,171 @@ __device__ __forceinline__ void frozen_state_vjp(const double L[5], const double
   dR[0] += dprod * L[0];
 }
 
+// Reverse of total_enthalpy(p, rho, u0, u1, u2): H = (p / gm1 + 0.5 rho |u|^2 + p) / rho.
+// P holds (rho, u0, u1, u2, p); dP += dH dH/dP.
+__device__ __forceinline__ void total_enthalpy_vjp(const double P[5], double H, double gm1, double dH,
+                                                   double dP[5]) {
+  const double ir = 1.0 / P[0];
+  const double dE = dH * ir;
+  dP[4] += dH * ir + dE / gm1;
+  dP[0] += -dH * H * ir + dE * 0.5 * (P[1] * P[1] + P[2] * P[2] + P[3] * P[3]);
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) dP[j] += dE * P[0] * P[j];
+}
+
+// Reverse of frozen_state_full (eigendecomposition.py:120-281, both frozen
+// states): the cotangents dz of every field of the full frozen state pulled
+// back onto the primitives of the two cells L, R beside the face (added to
+// dL, dR).  gm1 enters the ROE average's gamma - 1 as a constant.
+__device__ __forceinline__ void frozen_state_full_vjp(const double L[5], const double R[5], const FaceParams& fp,
+                                                      const FrozenFull& z, const FrozenFull& dz, double dL[5],
+                                                      double dR[5]) {
+  double dpa[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) dpa[v] = dz.pa[v];
+  // vsq = |pa[1..3]|^2
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) dpa[j] += 2.0 * z.pa[j] * dz.vsq;
+  const double gm1 = fp.gm1;
+  if (fp.frozen_state == GBF_FROZEN_ARITHMETIC) {
+    // c = sqrt(gamma pa4 / pa0), cc = c c, H = total_enthalpy(pa), gr = gm1
+    const double dct = dz.c + 2.0 * z.c * dz.cc;
+    const double y = z.c * z.c;
+    const double dy = dct * 0.5 / z.c;
+    dpa[4] += dy * y / z.pa[4];
+    dpa[0] -= dy * y / z.pa[0];
+    total_enthalpy_vjp(z.pa, z.H, gm1, dz.H, dpa);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      dL[v] += 0.5 * dpa[v];
+      dR[v] += 0.5 * dpa[v];
+    }
+    return;
+  }
+  const double sL = sqrt(L[0]), sR = sqrt(R[0]);
+  const double S = sL + sR;
+  const double rho_div = 1.0 / S;
+  const double iL0 = 1.0 / L[0], iR0 = 1.0 / R[0];
+  const double qL = L[4] * iL0, qR = R[4] * iR0;
+  const double A = sL * qL + sR * qR;
+  const double HL = total_enthalpy(L[4], L[0], L[1], L[2], L[3], gm1);
+  const double HR = total_enthalpy(R[4], R[0], R[1], R[2], R[3], gm1);
+  const double d1 = R[1] - L[1], d2 = R[2] - L[2], d3 = R[3] - L[3];
+  const double sqvd = d1 * d1 + d2 * d2 + d3 * d3;
+  const double p_over_rho = A * rho_div + 0.5 * z.pa[0] * rho_div * rho_div * sqvd;
+  // c = sqrt(cc); cc = psi_a + gr p_over_rho, psi_a = A rho_div
+  const double dcct = dz.cc + dz.c * 0.5 / z.c;
+  const double dgr = dz.gr + dcct * p_over_rho;
+  const double dpor = dcct * z.gr;
+  double dA = dcct * rho_div + dpor * rho_div;
+  double drho_div = dcct * A + dpor * (A + z.pa[0] * rho_div * sqvd);
+  dpa[0] += dpor * 0.5 * rho_div * rho_div * sqvd;
+  const double dsq = dpor * 0.5 * z.pa[0] * rho_div * rho_div;
+  // gr = (sL gm1 + sR gm1) rho_div
+  double dsL = dgr * gm1 * rho_div, dsR = dgr * gm1 * rho_div;
+  drho_div += dgr * (sL * gm1 + sR * gm1);
+  // H = (sL HL + sR HR) rho_div
+  dsL += dz.H * HL * rho_div;
+  dsR += dz.H * HR * rho_div;
+  drho_div += dz.H * (sL * HL + sR * HR);
+  total_enthalpy_vjp(L, HL, gm1, dz.H * sL * rho_div, dL);
+  total_enthalpy_vjp(R, HR, gm1, dz.H * sR * rho_div, dR);
+  // pa[v] = (sL L[v] + sR R[v]) / S, v = 1..4
+  double dS = 0.0;
+#pragma unroll
+  for (int v = 1; v < 5; ++v) {
+    const double dn = dpa[v] / S;
+    dL[v] += dn * sL;
+    dR[v] += dn * sR;
+    dsL += dn * L[v];
+    dsR += dn * R[v];
+    dS -= dn * z.pa[v];
+  }
+  // A = sL L4/L0 + sR R4/R0
+  dsL += dA * qL;
+  dsR += dA * qR;
+  dL[4] += dA * sL * iL0;
+  dR[4] += dA * sR * iR0;
+  dL[0] -= dA * sL * qL * iL0;
+  dR[0] -= dA * sR * qR * iR0;
+  // sqvd
+  dR[1] += 2.0 * d1 * dsq;
+  dL[1] -= 2.0 * d1 * dsq;
+  dR[2] += 2.0 * d2 * dsq;
+  dL[2] -= 2.0 * d2 * dsq;
+  dR[3] += 2.0 * d3 * dsq;
+  dL[3] -= 2.0 * d3 * dsq;
+  // rho_div = 1 / S
+  dS -= drho_div * rho_div * rho_div;
+  dsL += dS;
+  dsR += dS;
+  dL[0] += dsL * 0.5 / sL;
+  dR[0] += dsR * 0.5 / sR;
+  // pa0 = sqrt(L0 R0)
+  const double dprod = dpa[0] * 0.5 / z.pa[0];
+  dL[0] += dprod * R[0];
+  dR[0] += dprod * L[0];
+}
+
+// Reverse of left_eigvecs_cons: dz += (d Lm / d z)^T G.
+template <int AX>
+__device__ __forceinline__ void left_eigvecs_cons_vjp(const FrozenFull& z, const double G[5][5], FrozenFull& dz) {
+  constexpr int n = AX + 1;
+  using I = CharIds<AX>;
+  constexpr int m0 = I::m0, m1 = I::m1;
+  const double one_cc = 1.0 / z.cc;
+  const double one_rho = 1.0 / z.pa[0];
+  const double h = 0.5 * one_cc;
+  const double pn = z.pa[n], c = z.c, gr = z.gr;
+  const double t0 = gr * z.vsq - gr * z.H;
+  // rows 0 and 4: h * (...)
+  double dh = G[0][0] * (t0 + (pn + c) * c) + G[0][n] * (-pn * gr - c) + G[0][m0] * (-z.pa[m0] * gr) +
+              G[0][m1] * (-z.pa[m1] * gr) + G[0][4] * gr + G[4][0] * (t0 - (pn - c) * c) +
+              G[4][n] * (-pn * gr + c) + G[4][m0] * (-z.pa[m0] * gr) + G[4][m1] * (-z.pa[m1] * gr) +
+              G[4][4] * gr;
+  const double a0 = h * G[0][0], a1 = h * G[0][n], a2 = h * G[0][m0], a3 = h * G[0][m1], a4 = h * G[0][4];
+  const double b0 = h * G[4][0], b1 = h * G[4][n], b2 = h * G[4][m0], b3 = h * G[4][m1], b4 = h * G[4][4];
+  dz.gr += (a0 + b0) * (z.vsq - z.H) - (a1 + b1) * pn - (a2 + b2) * z.pa[m0] - (a3 + b3) * z.pa[m1] + a4 + b4;
+  dz.vsq += (a0 + b0) * gr;
+  dz.H -= (a0 + b0) * gr;
+  dz.pa[n] += a0 * c - b0 * c - (a1 + b1) * gr;
+  dz.c += a0 * (pn + 2.0 * c) + b0 * (2.0 * c - pn) - a1 + b1;
+  dz.pa[m0] -= (a2 + b2) * gr;
+  dz.pa[m1] -= (a3 + b3) * gr;
+  // row n: one_cc * (...)
+  double done_cc = G[n][0] * (z.H - z.vsq) + G[n][1] * z.pa[1] + G[n][2] * z.pa[2] + G[n][3] * z.pa[3] - G[n][4];
+  dz.H += G[n][0] * one_cc;
+  dz.vsq -= G[n][0] * one_cc;
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) dz.pa[j] += G[n][j] * one_cc;
+  // rows m0, m1: one_rho * (...)
+  const double done_rho = G[m0][0] * z.pa[m0] - G[m0][m0] - G[m1][0] * z.pa[m1] + G[m1][m1];
+  dz.pa[m0] += G[m0][0] * one_rho;
+  dz.pa[m1] -= G[m1][0] * one_rho;
+  done_cc += 0.5 * dh;
+  dz.cc -= done_cc * one_cc * one_cc;
+  dz.pa[0] -= done_rho * one_rho * one_rho;
+}
+
+// Reverse of right_eigvecs_cons: dz += (d Rm / d z)^T G.
+template <int AX>
+__device__ __forceinline__ void right_eigvecs_cons_vjp(const FrozenFull& z, const double G[5][5], FrozenFull& dz) {
+  constexpr int n = AX + 1;
+  using I = CharIds<AX>;
+  constexpr int m0 = I::m0, m1 = I::m1;
+  const double pn = z.pa[n], c = z.c;
+  dz.pa[n] += G[n][0] - G[4][0] * c + G[n][4] + G[4][4] * c;
+  dz.c += -G[n][0] - G[4][0] * pn + G[n][4] + G[4][4] * pn;
+  dz.pa[m0] += G[m0][0] + G[m0][4] - G[4][m0] * z.pa[0];
+  dz.pa[m1] += G[m1][0] + G[m1][4] + G[4][m1] * z.pa[0];
+  dz.H += G[4][0] + G[4][n] * z.gr + G[4][4];
+  dz.gr += G[0][n] + G[1][n] * z.pa[1] + G[2][n] * z.pa[2] + G[3][n] * z.pa[3] + G[4][n] * z.H;
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) dz.pa[j] += G[j][n] * z.gr;
+  dz.cc -= G[4][n];
+  dz.pa[0] += -G[m0][m0] - G[4][m0] * z.pa[m0] + G[m1][m1] + G[4][m1] * z.pa[m1];
+}
+
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void riemann_flux_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
                                                  const double dF[5], double dPL[5], double dPR[5]) {

@@ -154,13 +154,136 @@ __device__ __forceinline__ void char_face_vjp(const FaceParams& fp, const double
   }
 }
 
+// CHAR-CONSERVATIVE face (charcons_reconstruct of the forward,
+// high_order_godunov.py:404-416, eigendecomposition.py:576-742): the full
+// frozen state of the primitives of the two cells beside the face, the
+// window conservatives to characteristic variables with the left
+// eigenvectors, WENO5-Z with its gradients on each, back with the right ones,
+// the face conservatives' primitives, the Riemann VJP, and the reverse of all
+// of it: the window cells' conservative cotangents to slot(v, k) =
+// slot[(v * 6 + k) * fvol] (cells 2 and 3 also receive the frozen state's
+// cotangents, carried from their primitives to their conservatives).  win
+// points at window cell 0 of the staged pencil (primitives in rows 0..4,
+// conservatives in rows 5..9); jr is this thread's private row block.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void charcons_face_vjp(const VjpParams& vp, const double* win, int pvol, int ps,
+                                                  const double dF[5], double* slot, int fvol, double* jr_rows,
+                                                  int nthr, double& dalpha) {
+  const FaceParams& fp = vp.sp.fp;
+  auto w = [&](int v, int k) { return win[v * pvol + k * ps]; };
+  auto u = [&](int v, int k) { return win[(5 + v) * pvol + k * ps]; };
+  auto SL = [&](int j, int k) -> double& { return slot[(j * 6 + k) * fvol]; };
+  auto JR = [&](int j, int i) -> double& { return jr_rows[(j * 5 + i) * nthr]; };
+  double L[5], R[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    L[v] = w(v, 2);
+    R[v] = w(v, 3);
+  }
+  FrozenFull z;
+  frozen_state_full(L, R, fp, z);
+  double Lm[5][5];
+  left_eigvecs_cons<AX>(z, Lm);
+  const double eps = fp.stencil_eps;
+  double cL[5], cR[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    double ch[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+      ch[k] = Lm[i][0] * u(0, k) + Lm[i][1] * u(1, k) + Lm[i][2] * u(2, k) + Lm[i][3] * u(3, k) + Lm[i][4] * u(4, k);
+    double jl[5], jr[5];
+    weno5z_jac(ch[0], ch[1], ch[2], ch[3], ch[4], eps, cL[i], jl);
+    weno5z_jac(ch[5], ch[4], ch[3], ch[2], ch[1], eps, cR[i], jr);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      SL(i, k) = jl[k];
+      JR(i, k) = jr[k];
+    }
+  }
+  double Rm[5][5];
+  right_eigvecs_cons<AX>(z, Rm);
+  double UL[5], UR[5], PL[5], PR[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    UL[i] = Rm[i][0] * cL[0] + Rm[i][1] * cL[1] + Rm[i][2] * cL[2] + Rm[i][3] * cL[3] + Rm[i][4] * cL[4];
+    UR[i] = Rm[i][0] * cR[0] + Rm[i][1] * cR[1] + Rm[i][2] * cR[2] + Rm[i][3] * cR[3] + Rm[i][4] * cR[4];
+  }
+  prims_from_cons(UL, PL, fp.gm1);
+  prims_from_cons(UR, PR, fp.gm1);
+  double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+  double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
+  prims_from_cons_vjp(UL, dPL, fp.gm1, dUL);
+  prims_from_cons_vjp(UR, dPR, fp.gm1, dUR);
+  // U = Rm c: cotangents of the right eigenvectors and of the face chars
+  FrozenFull dz{};
+  double G[5][5];
+  double gL[5], gR[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    gL[j] = 0.0;
+    gR[j] = 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      G[i][j] = dUL[i] * cL[j] + dUR[i] * cR[j];
+      gL[j] += Rm[i][j] * dUL[i];
+      gR[j] += Rm[i][j] * dUR[i];
+    }
+  right_eigvecs_cons_vjp<AX>(z, G, dz);
+  // per window cell: char cotangents, then conservative ones; G collects the
+  // left eigenvectors' cotangent
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) G[i][j] = 0.0;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double dch[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      double d = (k <= 4) ? gL[i] * SL(i, k) : 0.0;
+      if (k >= 1) d += gR[i] * JR(i, 5 - k);
+      dch[i] = d;
+    }
+    double uk[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) uk[j] = u(j, k);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+#pragma unroll
+      for (int j = 0; j < 5; ++j) G[i][j] += dch[i] * uk[j];
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      SL(j, k) = Lm[0][j] * dch[0] + Lm[1][j] * dch[1] + Lm[2][j] * dch[2] + Lm[3][j] * dch[3] + Lm[4][j] * dch[4];
+  }
+  left_eigvecs_cons_vjp<AX>(z, G, dz);
+  double dLp[5] = {0, 0, 0, 0, 0}, dRp[5] = {0, 0, 0, 0, 0};
+  frozen_state_full_vjp(L, R, fp, z, dz, dLp, dRp);
+  // the frozen state reads the primitives of cells 2 and 3: on to their conservatives
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int k = 2 + side;
+    double Uc[5], dUc[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Uc[v] = u(v, k);
+    prims_from_cons_vjp(Uc, side == 0 ? dLp : dRp, fp.gm1, dUc);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) SL(v, k) += dUc[v];
+  }
+}
+
 template <int AX, int RECON, int RIEMANN>
 __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], const int ext[3],
                                          double* sm_prim, double* sm_slot, double* sm_jr) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr int K = 2 * R;
-  // CONSERVATIVE: the stencils read the staged conservatives (pencil rows 5..9)
-  constexpr bool CONS = RECON == RECON_WENO5Z_CONS;
+  // CONSERVATIVE, CHAR-CONSERVATIVE: the stencils read the staged
+  // conservatives (pencil rows 5..9); the face slots hold conservative cotangents
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
   const SweepParams& p = vp.sp;
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
@@ -202,7 +325,10 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
     }
     const int base = idx3(f0, f1, f2, pe[1], pe[2]);
     double PL[5], PR[5];
-    if constexpr (CONS) {
+    if constexpr (RECON == RECON_WENO5Z_CHARCONS) {
+      charcons_face_vjp<AX, RIEMANN>(vp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol, sm_jr + tid, nthr,
+                                     dalpha);
+    } else if constexpr (CONS) {
       // high_order_godunov.py:282-296 reversed: WENO5-Z on the conservatives
       // with its gradients, primitives of the face conservatives, Riemann VJP,
       // then the face conservatives' cotangents through the stencil gradients
@@ -223,7 +349,7 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
       prims_from_cons(UL, PL, p.fp.gm1);
       prims_from_cons(UR, PR, p.fp.gm1);
       double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-      riemann_flux_vjp<AX, RIEMANN>(PL, PR, p.fp, dF, dPL, dPR);
+      face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
       double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
       prims_from_cons_vjp(UL, dPL, p.fp.gm1, dUL);
       prims_from_cons_vjp(UR, dPR, p.fp.gm1, dUR);
@@ -416,7 +542,7 @@ __global__ void __launch_bounds__(256) rhs_vjp_kernel(const VjpParams vp) {
   // pencil primitives (and conservatives) | per-thread right-stencil gradients
   // (WENO only) | face slots
   double* sm_prim = smem;
-  double* sm_jr = smem + (RECON == RECON_WENO5Z_CONS ? 10 : 5) * pmax;
+  double* sm_jr = smem + ((RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS) ? 10 : 5) * pmax;
   double* sm_slot = sm_jr + (ReconTraits<RECON>::R == 3 ? 25 * blockDim.x : 0);
   if (p.active_mask & 1) vjp_axis<0, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
   if (p.active_mask & 2) vjp_axis<1, RECON, RIEMANN>(vp, o, ext, sm_prim, sm_slot, sm_jr);
@@ -563,6 +689,7 @@ int launch_vjp_weno5(int recon, int riemann, const VjpParams& vp, int grid, int 
 int launch_vjp_char(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_teno5(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_cons(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
+int launch_vjp_charcons(int riemann, const VjpParams& vp, int grid, int threads, size_t smem, cudaStream_t s);
 int launch_vjp_short(int recon, int riemann, const VjpParams& vp, int grid, int threads, size_t smem,
                      cudaStream_t s);
 

@@ -126,6 +126,17 @@ VJP_CASES = [
     ("3d-char-roe-viscous-heat", (16, 12, 14), "PERIODIC", {"nh": 4, "recon_var": "CHAR-PRIMITIVE",
                                                              "frozen_state": "ROE", "viscous": True, "heat": True,
                                                              "mu": 0.02, "prandtl": 0.71}, "generic"),
+    # CHAR-CONSERVATIVE: the conservative eigen-transforms of the full frozen
+    # state (ROE and ARITHMETIC)
+    ("2d-charcons-roe-hllc", (32, 28, 1), "PERIODIC", {"recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE"},
+     "generic"),
+    ("2d-charcons-arith-hll-zg", (24, 20, 1), "ZEROGRADIENT", {"recon_var": "CHAR-CONSERVATIVE", "riemann": "HLL"},
+     "generic"),
+    ("3d-charcons-roe-rusanov", (12, 10, 14), "PERIODIC", {"recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE",
+                                                           "riemann": "RUSANOV"}, "generic"),
+    ("2d-charcons-roe-sym-viscous", (20, 24, 1), {"east": "SYMMETRY", "west": "SYMMETRY", "north": "PERIODIC",
+                                                  "south": "PERIODIC", "top": "PERIODIC", "bottom": "PERIODIC"},
+     {"nh": 4, "recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE", "viscous": True, "mu": 0.02}, "generic"),
     # Lax-Friedrichs: one speed per axis, the maximum over every face state;
     # its cotangent goes to the states attaining it (the flat parts of Sod
     # and of the square wave: many ties on both sides, and face -1/2 of the
