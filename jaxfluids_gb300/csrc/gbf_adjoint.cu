@@ -461,10 +461,6 @@ int vjp_check(const gbf_case* c) {
   // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
   if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // Lax-Friedrichs' axis speed is reversed on the PRIMITIVE reconstructions
-  if (c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && c->recon_var != GBF_RECVAR_PRIMITIVE &&
-      !(c->flags & GBF_FLAG_NO_CONVECTIVE))
-    return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
@@ -558,6 +554,8 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
   if (vp.dU) zero_kernel<<<grid_for(5 * ci.cells), 256, 0, s>>>(vp.dU, 5 * ci.cells);
   vp.lf_alpha = nullptr;
   vp.lf_dalpha = nullptr;
+  vp.lf_tie_side = -1;
+  vp.lf_tie_ds = 0.0;
   // Lax-Friedrichs: the axes' speeds of U from the forward face kernels'
   // speed pass on U's primitives (the same face states and arithmetic as the
   // forward, so the ties below are the forward's)
@@ -602,7 +600,14 @@ int launch_rhs_vjp(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, 
       tp.cap = cap;
       tp.dalpha = lfa + 3;
       tp.dP = dP;
-      if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
+      tp.dU = vp.dU;
+      if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
+        st = launch_lf_ties_char(a, tp, s);
+      else if (c->recon_var == GBF_RECVAR_CONSERVATIVE)
+        st = launch_lf_ties_cons(a, tp, s);
+      else if (c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE)
+        st = launch_lf_ties_charcons(a, tp, s);
+      else if (c->recon == GBF_RECON_WENO5Z || c->recon == GBF_RECON_WENO5JS)
         st = launch_lf_ties_weno5(c->recon, a, tp, s);
       else if (c->recon == GBF_RECON_TENO5)
         st = launch_lf_ties_teno5(a, tp, s);

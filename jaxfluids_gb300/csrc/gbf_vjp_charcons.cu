@@ -8,4 +8,8 @@ int launch_vjp_charcons(int riemann, const VjpParams& vp, int grid, int threads,
   return launch_vjp_riemann<RECON_WENO5Z_CHARCONS>(riemann, vp, grid, threads, smem, s);
 }
 
+int launch_lf_ties_charcons(int axis, const LfTieParams& tp, cudaStream_t s) {
+  return launch_lf_ties_window_one<RECON_WENO5Z_CHARCONS>(axis, tp, s);
+}
+
 }  // namespace gbf

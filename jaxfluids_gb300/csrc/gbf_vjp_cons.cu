@@ -8,4 +8,8 @@ int launch_vjp_cons(int riemann, const VjpParams& vp, int grid, int threads, siz
   return launch_vjp_riemann<RECON_WENO5Z_CONS>(riemann, vp, grid, threads, smem, s);
 }
 
+int launch_lf_ties_cons(int axis, const LfTieParams& tp, cudaStream_t s) {
+  return launch_lf_ties_window_one<RECON_WENO5Z_CONS>(axis, tp, s);
+}
+
 }  // namespace gbf

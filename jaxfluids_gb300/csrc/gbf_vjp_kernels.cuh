@@ -18,14 +18,22 @@ struct VjpParams {
   // accumulators of their cotangents
   const double* lf_alpha;
   double* lf_dalpha;
+  // Lax-Friedrichs tie pullback (lf_tie_side 0 / 1, -1 off): the face states'
+  // cotangents are those of the speed of side lf_tie_side, lf_tie_ds, in place
+  // of the flux's
+  int lf_tie_side;
+  double lf_tie_ds;
 };
 
-// Lax-Friedrichs flux VJP with the axis' speed fixed, or the scheme's own.
+// Lax-Friedrichs flux VJP with the axis' speed fixed, or the scheme's own;
+// in a tie pullback, the speed's cotangent on one face state.
 template <int AX, int RIEMANN>
 __device__ __forceinline__ void face_riemann_vjp(const VjpParams& vp, const double PL[5], const double PR[5],
                                                  const double dF[5], double dPL[5], double dPR[5],
                                                  double& dalpha) {
-  if (RIEMANN == GBF_RIEMANN_RUSANOV && vp.lf_alpha)
+  if (RIEMANN == GBF_RIEMANN_RUSANOV && vp.lf_tie_side >= 0)
+    lf_speed_vjp<AX>(vp.lf_tie_side == 0 ? PL : PR, vp.sp.fp, vp.lf_tie_ds, vp.lf_tie_side == 0 ? dPL : dPR);
+  else if (RIEMANN == GBF_RIEMANN_RUSANOV && vp.lf_alpha)
     lf_vjp<AX>(PL, PR, vp.sp.fp, vp.lf_alpha[AX], dF, dPL, dPR, dalpha);
   else
     riemann_flux_vjp<AX, RIEMANN>(PL, PR, vp.sp.fp, dF, dPL, dPR);
@@ -39,9 +47,10 @@ __device__ __forceinline__ void face_riemann_vjp(const VjpParams& vp, const doub
 // stride ps); slot(v, k) = slot[(v * 6 + k) * fvol] receives the cotangent of
 // primitive v of window cell k; jr is this thread's private row block.
 template <int AX, int RIEMANN>
-__device__ __forceinline__ void char_face_vjp(const FaceParams& fp, const double* win, int pvol, int ps,
+__device__ __forceinline__ void char_face_vjp(const VjpParams& vp, const double* win, int pvol, int ps,
                                               const double dF[5], double* slot, int fvol, double* jr_rows,
-                                              int nthr) {
+                                              int nthr, double& dalpha) {
+  const FaceParams& fp = vp.sp.fp;
   constexpr int N = AX + 1;
   using I = CharIds<AX>;
   auto x = [&](int v, int k) { return win[v * pvol + k * ps]; };
@@ -94,7 +103,7 @@ __device__ __forceinline__ void char_face_vjp(const FaceParams& fp, const double
   PR[I::m1] = cR[I::e1];
   PR[4] = cc * rho_a * (cR[0] + cR[4]);
   double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-  riemann_flux_vjp<AX, RIEMANN>(PL, PR, fp, dF, dPL, dPR);
+  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
   // back-projection reverse
   double drho_a = 0.0, dc = 0.0, dcc = 0.0;
   double gL[5], gR[5];
@@ -276,6 +285,56 @@ __device__ __forceinline__ void charcons_face_vjp(const VjpParams& vp, const dou
   }
 }
 
+// CONSERVATIVE face (high_order_godunov.py:282-296 reversed): WENO5-Z on the
+// window conservatives with its gradients, primitives of the face
+// conservatives, Riemann VJP, then the face conservatives' cotangents through
+// the stencil gradients into slot(v, k) = slot[(v * 6 + k) * fvol] (the
+// window cells' conservative cotangents).  win: window cell 0 of the staged
+// pencil (conservatives in rows 5..9); jr: this thread's private row block.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void cons_face_vjp(const VjpParams& vp, const double* win, int pvol, int ps,
+                                              const double dF[5], double* slot, int fvol, double* jr_rows,
+                                              int nthr, double& dalpha) {
+  const FaceParams& fp = vp.sp.fp;
+  auto SL = [&](int v, int k) -> double& { return slot[(v * 6 + k) * fvol]; };
+  auto JR = [&](int v, int i) -> double& { return jr_rows[(v * 5 + i) * nthr]; };
+  double UL[5], UR[5], PL[5], PR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    double wv[6], jl[5], jr[5];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) wv[k] = win[(5 + v) * pvol + k * ps];
+    weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], fp.stencil_eps, UL[v], jl);
+    weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], fp.stencil_eps, UR[v], jr);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      SL(v, k) = jl[k];
+      JR(v, k) = jr[k];
+    }
+  }
+  prims_from_cons(UL, PL, fp.gm1);
+  prims_from_cons(UR, PR, fp.gm1);
+  double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
+  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+  double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
+  prims_from_cons_vjp(UL, dPL, fp.gm1, dUL);
+  prims_from_cons_vjp(UR, dPR, fp.gm1, dUR);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double gL = dUL[v], gR = dUR[v];
+    double jl[5], jr[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      jl[k] = SL(v, k);
+      jr[k] = JR(v, k);
+    }
+    SL(v, 0) = gL * jl[0];
+#pragma unroll
+    for (int k = 1; k < 5; ++k) SL(v, k) = gL * jl[k] + gR * jr[5 - k];
+    SL(v, 5) = gR * jr[0];
+  }
+}
+
 template <int AX, int RECON, int RIEMANN>
 __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], const int ext[3],
                                          double* sm_prim, double* sm_slot, double* sm_jr) {
@@ -329,44 +388,8 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
       charcons_face_vjp<AX, RIEMANN>(vp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol, sm_jr + tid, nthr,
                                      dalpha);
     } else if constexpr (CONS) {
-      // high_order_godunov.py:282-296 reversed: WENO5-Z on the conservatives
-      // with its gradients, primitives of the face conservatives, Riemann VJP,
-      // then the face conservatives' cotangents through the stencil gradients
-      double UL[5], UR[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        double wv[K], jl[5], jr[5];
-#pragma unroll
-        for (int k = 0; k < K; ++k) wv[k] = sm_prim[(5 + v) * pvol + base + k * pstride];
-        weno5z_jac(wv[0], wv[1], wv[2], wv[3], wv[4], p.fp.stencil_eps, UL[v], jl);
-        weno5z_jac(wv[5], wv[4], wv[3], wv[2], wv[1], p.fp.stencil_eps, UR[v], jr);
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          sm_slot[(v * K + k) * fvol + f] = jl[k];
-          sm_jr[(v * 5 + k) * nthr + tid] = jr[k];
-        }
-      }
-      prims_from_cons(UL, PL, p.fp.gm1);
-      prims_from_cons(UR, PR, p.fp.gm1);
-      double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-      face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
-      double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
-      prims_from_cons_vjp(UL, dPL, p.fp.gm1, dUL);
-      prims_from_cons_vjp(UR, dPR, p.fp.gm1, dUR);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const double gL = dUL[v], gR = dUR[v];
-        double jl[5], jr[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          jl[k] = sm_slot[(v * K + k) * fvol + f];
-          jr[k] = sm_jr[(v * 5 + k) * nthr + tid];
-        }
-        sm_slot[(v * K + 0) * fvol + f] = gL * jl[0];
-#pragma unroll
-        for (int k = 1; k < 5; ++k) sm_slot[(v * K + k) * fvol + f] = gL * jl[k] + gR * jr[5 - k];
-        sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
-      }
+      cons_face_vjp<AX, RIEMANN>(vp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol, sm_jr + tid, nthr,
+                                 dalpha);
     } else if constexpr (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5) {
       // one pass gives the face states and the stencil gradients; the left
       // gradient waits in the face's slots 0..4, the right one in this
@@ -423,8 +446,8 @@ __device__ __forceinline__ void vjp_axis(const VjpParams& vp, const int o[3], co
         sm_slot[(v * K + 5) * fvol + f] = gR * jr[0];
       }
     } else if constexpr (RECON == RECON_WENO5Z_CHAR) {
-      char_face_vjp<AX, RIEMANN>(p.fp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol,
-                                 sm_jr + tid, nthr);
+      char_face_vjp<AX, RIEMANN>(vp, sm_prim + base, pvol, pstride, dF, sm_slot + f, fvol, sm_jr + tid, nthr,
+                                 dalpha);
     } else {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -563,6 +586,7 @@ struct LfTieParams {
   long long cap;                    // entries the list holds
   const double* dalpha;             // cotangent of each axis' speed
   double* dP;                       // primitive cotangent accumulator, interior [5][N]
+  double* dU;                       // conservative cotangent accumulator (conservative reconstructions)
 };
 
 template <int AX, int RECON>
@@ -676,6 +700,123 @@ int launch_lf_ties_one(int axis, const LfTieParams& tp, cudaStream_t s) {
   else lf_tie_vjp_kernel<2, RECON><<<grid, threads, 0, s>>>(tp);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
+
+// The ties of the characteristic and conservative reconstructions (WENO5-Z
+// on the six-cell window): the window's primitives (and conservatives, those
+// of a halo cell from its halo primitives, material.py:248-250) in local
+// memory, the scheme's own face VJP with the speed's cotangent on the tie's
+// face state in place of the flux's (VjpParams::lf_tie_side), then the window
+// cells' cotangents as the VJP kernel gathers them.
+template <int AX, int RECON>
+__global__ void __launch_bounds__(128) lf_tie_window_vjp_kernel(const LfTieParams tp) {
+  const SweepParams& p = tp.sp;
+  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
+  const unsigned long long listed = tp.ties[0];
+  const long long n = (long long)listed < tp.cap ? (long long)listed : tp.cap;
+  const double nL = (double)tp.ties[1], nR = (double)tp.ties[2];
+  const double share = tp.dalpha[AX] * ((nL > 0.0 && nR > 0.0) ? 0.5 : 1.0);
+  const bool periodic = p.bc[2 * AX] == GBF_BC_PERIODIC;
+  int ext[3] = {p.n[0], p.n[1], p.n[2]};
+  ext[AX] = periodic ? p.n[AX] : p.n[AX] + 1;
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long t = tp.ties[4 + e];
+    const long long face = LfTie::face(t);
+    const int side = LfTie::side(t);
+    int q[3];
+    q[2] = (int)(face % ext[2]);
+    const long long r = face / ext[2];
+    q[1] = (int)(r % ext[1]);
+    q[0] = (int)(r / ext[1]);
+    // window cells q[AX] - 3 .. q[AX] + 2: primitives in rows 0..4,
+    // conservatives in rows 5..9 (variable stride 6, cell stride 1)
+    double win[60], slot[30], jr[25];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      int g[3] = {q[0], q[1], q[2]};
+      g[AX] += k - 3;
+      double P[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) win[v * 6 + k] = P[v] = global_prim<MODE_STAGE_P>(p, v, g[0], g[1], g[2]);
+      if constexpr (CONS) {
+        double U[5];
+        if (g[AX] >= 0 && g[AX] < p.n[AX]) {
+          const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
+        } else {
+          cons_from_prims(P, U, p.fp.gm1);
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) win[(5 + v) * 6 + k] = U[v];
+      }
+    }
+    VjpParams vt{};
+    vt.sp = p;
+    vt.lf_tie_side = side;
+    vt.lf_tie_ds = share * LfTie::mult(t) / (side == 0 ? nL : nR);
+    const double dF[5] = {0, 0, 0, 0, 0};
+    double dal = 0.0;
+    if constexpr (RECON == RECON_WENO5Z_CHAR)
+      char_face_vjp<AX, GBF_RIEMANN_RUSANOV>(vt, win, 6, 1, dF, slot, 1, jr, 1, dal);
+    else if constexpr (RECON == RECON_WENO5Z_CHARCONS)
+      charcons_face_vjp<AX, GBF_RIEMANN_RUSANOV>(vt, win, 6, 1, dF, slot, 1, jr, 1, dal);
+    else
+      cons_face_vjp<AX, GBF_RIEMANN_RUSANOV>(vt, win, 6, 1, dF, slot, 1, jr, 1, dal);
+    // the window cells' cotangents: primitive ones (CHAR-PRIMITIVE) or
+    // conservative ones (interior cells: the state; halo cells: through the
+    // conservatives of their halo primitives), halo cells through the
+    // transpose of their face rule
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      int g[3] = {q[0], q[1], q[2]};
+      g[AX] += k - 3;
+      double d[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] = slot[v * 6 + k];
+      const bool halo = g[AX] < 0 || g[AX] >= p.n[AX];
+      if (CONS && !halo) {
+        const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          if (d[v] != 0.0) atomicAdd(tp.dU + v * cs + off, d[v]);
+        continue;
+      }
+      if (CONS) {
+        double P[5], dPh[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+        for (int v = 0; v < 5; ++v) P[v] = win[v * 6 + k];
+        cons_from_prims_vjp(P, d, 1.0 / P[0], 1.0 / p.fp.gm1, dPh);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) d[v] = dPh[v];
+      }
+      if (halo) {
+        const int ty = face_type_at(p.bc, p.bf, 2 * AX + (g[AX] >= 0 ? 1 : 0), face_pos(p.n, AX, g));
+        g[AX] = bc_src(g[AX], p.n[AX], ty);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) d[v] *= bc_apply_grad(ty, AX, v);
+      }
+      const long long off = ((long long)g[0] * p.n[1] + g[1]) * p.n[2] + g[2];
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (d[v] != 0.0) atomicAdd(tp.dP + v * cs + off, d[v]);
+    }
+  }
+}
+
+template <int RECON>
+int launch_lf_ties_window_one(int axis, const LfTieParams& tp, cudaStream_t s) {
+  const int grid = 152 * 4, threads = 128;
+  if (axis == 0) lf_tie_window_vjp_kernel<0, RECON><<<grid, threads, 0, s>>>(tp);
+  else if (axis == 1) lf_tie_window_vjp_kernel<1, RECON><<<grid, threads, 0, s>>>(tp);
+  else lf_tie_window_vjp_kernel<2, RECON><<<grid, threads, 0, s>>>(tp);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
+int launch_lf_ties_char(int axis, const LfTieParams& tp, cudaStream_t s);
+int launch_lf_ties_cons(int axis, const LfTieParams& tp, cudaStream_t s);
+int launch_lf_ties_charcons(int axis, const LfTieParams& tp, cudaStream_t s);
 
 // The tie kernels per reconstruction family (gbf_vjp_<family>.cu).
 int launch_lf_ties_weno5(int recon, int axis, const LfTieParams& tp, cudaStream_t s);

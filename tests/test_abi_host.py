@@ -93,8 +93,9 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     (dict(recon="TENO5"), True),
     (dict(riemann="LAX-FRIEDRICHS"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon="MINMOD-AD", nh=4), True),
-    (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-PRIMITIVE"), False),
-    (dict(riemann="LAX-FRIEDRICHS", recon_var="CONSERVATIVE"), False),
+    (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-PRIMITIVE"), True),
+    (dict(riemann="LAX-FRIEDRICHS", recon_var="CONSERVATIVE"), True),
+    (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-CONSERVATIVE"), True),
     (dict(recon_var="CONSERVATIVE"), True),
     (dict(recon_var="CONSERVATIVE", interpolation_limiter=True), False),
     (dict(recon_var="CHAR-CONSERVATIVE", frozen_state="ROE"), True),

@@ -65,9 +65,27 @@ def square_wave_prims(n):
     return torch.from_numpy(P.reshape(5, n, 1, 1))
 
 
+def mirror_prims(n):
+    """1-D periodic smooth state, mirror-symmetric about the domain centre with
+    the velocity odd: a face state and its mirror image have bitwise equal
+    Lax-Friedrichs speeds, so the maximum is attained by a left and a right
+    state at once."""
+    x = (np.arange(n // 2) + 0.5) / n
+    rho = 1.0 + 0.2 * np.cos(2 * np.pi * x)
+    u = 0.3 * np.sin(2 * np.pi * x)
+    p = 1.0 + 0.1 * np.cos(2 * np.pi * x)
+    P = np.zeros((5, n))
+    P[0] = np.concatenate([rho, rho[::-1]])
+    P[1] = np.concatenate([u, -u[::-1]])
+    P[4] = np.concatenate([p, p[::-1]])
+    return torch.from_numpy(P.reshape(5, n, 1, 1))
+
+
 def _interior_cons(kind, cells, oc):
     if kind == "generic":
         return generic_cons(cells)
+    if kind == "mirror":
+        return O.cons_from_prims(mirror_prims(cells[0]), 1.4)
     if kind == "square":
         return O.cons_from_prims(square_wave_prims(cells[0]), 1.4)
     if kind == "kh":
@@ -153,6 +171,20 @@ VJP_CASES = [
      {"recon": "WENO3-Z", "riemann": "LAX-FRIEDRICHS"}, "generic"),
     ("2d-teno5-lf-viscous", (20, 16, 1), "PERIODIC", {"nh": 4, "recon": "TENO5", "riemann": "LAX-FRIEDRICHS",
                                                       "viscous": True, "mu": 0.02}, "generic"),
+    ("2d-char-roe-lf", (32, 28, 1), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
+                                                 "riemann": "LAX-FRIEDRICHS"}, "generic"),
+    ("3d-cons-lf-zg", (12, 10, 14), "ZEROGRADIENT", {"recon_var": "CONSERVATIVE", "riemann": "LAX-FRIEDRICHS"},
+     "generic"),
+    ("2d-charcons-arith-lf-zg", (24, 20, 1), "ZEROGRADIENT", {"recon_var": "CHAR-CONSERVATIVE",
+                                                              "riemann": "LAX-FRIEDRICHS"}, "generic"),
+    # mirror-symmetric states: the speed attained by a left and a right state
+    ("1d-weno-lf-mirror", (48, 1, 1), "PERIODIC", {"riemann": "LAX-FRIEDRICHS"}, "mirror"),
+    ("1d-char-roe-lf-mirror", (48, 1, 1), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
+                                                       "riemann": "LAX-FRIEDRICHS"}, "mirror"),
+    ("1d-cons-lf-mirror", (48, 1, 1), "PERIODIC", {"recon_var": "CONSERVATIVE", "riemann": "LAX-FRIEDRICHS"},
+     "mirror"),
+    ("1d-charcons-roe-lf-mirror", (48, 1, 1), "PERIODIC", {"recon_var": "CHAR-CONSERVATIVE", "frozen_state": "ROE",
+                                                           "riemann": "LAX-FRIEDRICHS"}, "mirror"),
 ]
 
 
