@@ -8,6 +8,9 @@
 
 namespace gbf {
 
+// Streaming multiprocessors of a GB300 (the grid-size rules count waves of them).
+constexpr int kSms = 152;
+
 // Host-side view of a validated case.
 struct CaseInfo {
   int n[3];

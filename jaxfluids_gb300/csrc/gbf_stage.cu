@@ -120,7 +120,6 @@ bool periodic_axis(const gbf_case* c, int a) { return c->bc[2 * a] == GBF_BC_PER
 // the larger tiles coalesce and reuse L1 better, 0.4-1.5 % on the 3-D
 // workloads).  In 1-D the tile runs along the axis.  A user tile (gbf_tile)
 // gives the extents of every face kernel directly.
-constexpr int kSms = 152;
 
 int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, FaceTile* ft, int* threads) {
   int t[3] = {1, 1, 1};

@@ -63,9 +63,29 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
       for (int a = 0; a < 3; ++a)
         if (ci.active_mask & (1 << a)) t[a] = 256;
     } else if (dim == 2) {
-      int k = 0;
+      int ax[2], k = 0;
       for (int a = 0; a < 3; ++a)
-        if (ci.active_mask & (1 << a)) t[a] = (k++ == 0) ? 15 : 32;
+        if (ci.active_mask & (1 << a)) ax[k++] = a;
+      t[ax[0]] = 15;
+      t[ax[1]] = 32;
+      if (for_vjp) {
+        // the adjoint kernel runs one CTA per SM (registers): of shapes with
+        // the same two rounds of faces per axis, take the one whose tile
+        // count fills its last wave of 152 CTAs best (KH 512^2: 16 x 27, 608
+        // tiles = 4 full waves, 7 % faster than 15 x 32's 560)
+        static const int cand[3][2] = {{15, 32}, {16, 27}, {14, 32}};
+        double best = -1.0;
+        for (const auto& cd : cand) {
+          const long long tiles = (long long)((ci.n[ax[0]] + cd[0] - 1) / cd[0]) * ((ci.n[ax[1]] + cd[1] - 1) / cd[1]);
+          const long long waves = (tiles + kSms - 1) / kSms;
+          const double fill = (double)tiles / (double)(waves * kSms);
+          if (fill > best + 1e-9) {
+            best = fill;
+            t[ax[0]] = cd[0];
+            t[ax[1]] = cd[1];
+          }
+        }
+      }
     } else {
       const bool heavy = for_vjp || (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) ||
                          c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
