@@ -320,15 +320,20 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  * (feed_forward/feed_forward.py:231-524, simulation_manager.py:1296-1412).
  * Follows jax.grad's conventions at non-smooth points (|x|' = +1 at 0, half
  * of the cotangent to each argument of a max/min tie, zero derivative of
- * sign, where() passes the selected branch).  PRIMITIVE reconstruction with
- * WENO5-Z or MINMOD-AD, CHAR-PRIMITIVE (ARITHMETIC or ROE frozen state) with
- * WENO5-Z, HLLC (Einfeldt speeds) or Rusanov, and the CENTRAL4 viscous and
- * heat fluxes (source_term_solver.py:188-350); other schemes return
+ * sign, where() passes the selected branch; the Lax-Friedrichs speed's
+ * cotangent to the face states attaining the maximum, shared as jnp.max and
+ * jnp.maximum share it).  Every reconstruction but MINMOD (PRIMITIVE WENO5-Z,
+ * WENO5-JS, TENO5, WENO3-JS, WENO3-Z, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
+ * and CHAR-CONSERVATIVE with WENO5-Z and either frozen state), HLLC and HLL
+ * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter on
+ * the PRIMITIVE reconstructions, gravity, and the CENTRAL4 / CENTRAL2 viscous
+ * and heat fluxes (source_term_solver.py:188-350); other setups return
  * GBF_ERR_UNSUPPORTED.
  *
  * gbf_rhs_vjp: out = J(U)^T w with J = d rhs / d U at the interior state
  *   `cons`; w, out interior [5][N].  workspace: gbf_vjp_workspace_bytes(c)
- *   (at least 5 N doubles; dissipative cases 38 N more).
+ *   (at least 5 N doubles; dissipative, conservative and Lax-Friedrichs
+ *   cases more).
  * gbf_rk3_step_vjp: lam_out = (d U^{n+1} / d U^n)^T lam for one TVD-RK3 step
  *   from U^n = `cons` with the device time step *dt (stage states recomputed).
  *   workspace: gbf_vjp_workspace_bytes(c).  lam_out must not alias lam.
