@@ -23,7 +23,16 @@ custom call.  This module provides:
   swaps it into a constructed ``SimulationManager`` (simulation_manager.py:128-138);
 * ``rk3_step_fn(config, dt)``: a fixed-dt TVD-RK3 step on interior
   conservatives as a ``jax.custom_vjp`` pair (``gbf_rk3_advance_ffi`` /
-  ``gbf_rk3_step_vjp_ffi``), the body of ``_feed_forward``'s scan.
+  ``gbf_rk3_step_vjp_ffi``), the body of ``_feed_forward``'s scan;
+* ``fused_step_fn(config)``: the same step with the first stage's
+  primitives, the time step and the time as arguments
+  (``step(cons, prims, dt, t)``);
+* ``simulation_manager_class()``: ``GB300SimulationManager``, a subclass of
+  the reference's ``SimulationManager`` (simulation_manager.py:49-138) whose
+  ``do_runge_kutta_stages`` (:670-1077) is one fused step, so the
+  reference's own ``simulate`` / ``advance`` loop (:186-426), its next-dt
+  computation and output, and ``_feed_forward`` (:1296-1412, differentiable
+  through the hand-written VJP) run on the GB300 kernels.
 
 Importing this module needs neither jax nor jaxfluids; each function imports
 what it uses.  Descriptors of setups with boundary values that vary along a
@@ -305,3 +314,112 @@ def rk3_step_fn(config: CaseConfig, dt: float):
 
     step.defvjp(fwd, bwd)
     return step
+
+
+def fused_step_fn(config: CaseConfig):
+    """One TVD-RK3 step of interior conservatives [5, Nx, Ny, Nz],
+    step(cons, prims, dt, t): prims are the interior primitives the first
+    stage reads (the reference's first stage reads the primitive buffer, not
+    primitives re-derived from the conservatives), dt the step and t the time.
+    A jax.custom_vjp function: forward gbf_rk3_advance (steps = 1,
+    dt_state = [dt, t, 0, 0], with_prims = 1), reverse gbf_rk3_step_vjp with the
+    same dt.  The reverse treats the primitives as those of the conservatives
+    (the cotangent reaches the conservatives; for prims = p(cons) and
+    cons = c(prims0) that is the whole derivative, p' c' = 1); dt and t get none."""
+    import jax
+    import jax.numpy as jnp
+    register_ffi_targets()
+    c = config.to_c()
+    lib = _lib.load()
+    desc = pack_case(c)
+    shape = (5,) + tuple(config.cells)
+    ws = int(lib.gbf_rk3_workspace_bytes(ctypes.byref(c)))
+    vjp_ws = int(lib.gbf_vjp_workspace_bytes(ctypes.byref(c)))
+    cons_t = jax.ShapeDtypeStruct(shape, jnp.float64)
+
+    @jax.custom_vjp
+    def step(cons, prims, dt, t):
+        zero = jnp.zeros((), jnp.float64)
+        dt_state = jnp.stack([jnp.asarray(dt, jnp.float64), jnp.asarray(t, jnp.float64), zero, zero])
+        out, _, _ = jax.ffi.ffi_call(
+            "gbf_rk3_advance", (cons_t, jax.ShapeDtypeStruct((4,), jnp.float64),
+                                jax.ShapeDtypeStruct((ws,), jnp.uint8)),
+            input_output_aliases={0: 0, 2: 1})(cons, prims, dt_state, desc=desc, steps=np.int64(1),
+                                               with_prims=np.int64(1))
+        return out
+
+    def fwd(cons, prims, dt, t):
+        return step(cons, prims, dt, t), (cons, prims, dt, t)
+
+    def bwd(res, lam):
+        cons, prims, dt, t = res
+        if vjp_ws == 0:
+            raise NotImplementedError("no adjoint for this setup")
+        dU, _ = jax.ffi.ffi_call("gbf_rk3_step_vjp", (cons_t, jax.ShapeDtypeStruct((vjp_ws,), jnp.uint8)))(
+            cons, jnp.asarray(dt, jnp.float64), lam, desc=desc)
+        return dU, jnp.zeros_like(prims), jnp.zeros_like(dt), jnp.zeros_like(t)
+
+    step.defvjp(fwd, bwd)
+    return step
+
+
+# ---------------------------------------------------------------- SimulationManager drop-in
+def simulation_manager_class():
+    """GB300SimulationManager: the reference's SimulationManager with each
+    TVD-RK3 step one fused GB300 call (defined against the installed
+    jaxfluids)."""
+    from jaxfluids.data_types.buffers import MaterialFieldBuffers
+    from jaxfluids.data_types.information import StepInformation
+    from jaxfluids.simulation_manager import SimulationManager
+
+    class GB300SimulationManager(SimulationManager):
+        """The reference's SimulationManager whose RK stages
+        (do_runge_kutta_stages, simulation_manager.py:670-1077) are one fused
+        step of the GB300 kernels on the interior conservatives; the
+        primitives of the new state and the halos are then formed by the
+        reference's own equation and halo managers, as its last stage forms
+        them (:943-974), and time and step advance as at :1046-1047.  The
+        reference's loop (advance, :297-426), next-dt computation
+        (_do_integration_step, :611-628), output and feed-forward
+        (_feed_forward, :1296-1412) run unchanged around it; the space solver
+        is GB300SpaceSolver for the calls that still ask for a right-hand side.
+
+        step: optional replacement of the fused step, step(cons, prims, dt, t)
+        -> cons on interior conservatives and primitives (default
+        fused_step_fn of the case)."""
+
+        def __init__(self, input_manager, callbacks=None, step=None):
+            super().__init__(input_manager, callbacks)
+            install_space_solver(self)
+            cfg = self.space_solver.gb300_config
+            if self.equation_information.levelset_model or self.equation_information.diffuse_interface_model:
+                raise NotImplementedError("two-phase flows are not on the GB300 path")
+            self.gb300_step = step if step is not None else fused_step_fn(cfg)
+
+        def do_runge_kutta_stages(self, material_fields, time_control_variables, levelset_fields=None,
+                                  solid_fields=None, forcing_buffers=None, control_flow_params=None,
+                                  ml_setup=None):
+            if forcing_buffers is not None:
+                raise NotImplementedError("forcings are not on the GB300 path")
+            nhx, nhy, nhz = self.domain_information.domain_slices_conservatives
+            dt = time_control_variables.physical_timestep_size
+            t = time_control_variables.physical_simulation_time
+            cons = self.gb300_step(material_fields.conservatives[..., nhx, nhy, nhz],
+                                   material_fields.primitives[..., nhx, nhy, nhz], dt, t)
+            conservatives = material_fields.conservatives.at[..., nhx, nhy, nhz].set(cons)
+            primitives = self.equation_manager.get_primitives_from_conservatives(conservatives)
+            t_new = t + dt
+            primitives, conservatives = self.halo_manager.perform_halo_update_material(
+                primitives, t_new, self.halo_manager.fill_edge_halos_material,
+                self.halo_manager.fill_vertex_halos_material, conservatives, ml_setup=ml_setup)
+            temperature = material_fields.temperature
+            if self.equation_information.is_compute_temperature:
+                temperature = self.material_manager.get_temperature(primitives)
+                temperature = self.halo_manager.perform_outer_halo_update_temperature(temperature, t_new)
+            time_control_variables = time_control_variables._replace(
+                simulation_step=time_control_variables.simulation_step + 1, physical_simulation_time=t_new)
+            return (MaterialFieldBuffers(conservatives, primitives, temperature), time_control_variables,
+                    levelset_fields, solid_fields, StepInformation((), ()))
+
+    return GB300SimulationManager
+

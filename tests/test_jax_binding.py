@@ -10,6 +10,9 @@
   setup; ``GB300SpaceSolver`` and the host-side ``SpaceSolver`` are constructed
   with the reference's constructor arguments (the reference runs under its
   numpy stand-in, in a subprocess).
+* ``GB300SimulationManager`` reproduces the reference's own runs through the
+  reference's loop and feed-forward (the oracle's step standing in for the
+  fused GPU step).
 * Every FFI target the Python side registers has a handler in ``gbf_ffi.cc``.
 """
 import ctypes
@@ -115,6 +118,28 @@ def test_descriptor_from_the_reference_objects_equals_the_one_from_the_setups():
     for name, v in res.items():
         assert v["desc_equal"] and v["solver_desc_equal"] and v["is_subclass"], (name, v)
         assert v["host_desc_equal"], (name, v)
+
+
+def test_simulation_manager_subclass_reproduces_the_references_own_runs():
+    """GB300SimulationManager (the reference's SimulationManager with each RK3
+    step one fused call) driven through the reference's integration-step loop
+    and _feed_forward, the oracle's step standing in for the GPU's: bitwise the
+    reference's own conservatives, time steps and times (golden fixtures), and
+    its stock feed-forward trajectory."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_ref_fixtures
+    if not os.path.isdir(os.path.join(make_ref_fixtures.REFERENCE, "src", "jaxfluids")):
+        pytest.skip("the reference checkout is not available on this machine")
+    r = subprocess.run([sys.executable, "-B", os.path.join(ROOT, "tests", "reference_simulation_check.py")],
+                       capture_output=True, text=True, timeout=1800, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    ff = res.pop("feed_forward")
+    assert ff["prims_equal"] and ff["times_equal"], ff
+    assert len(res) >= 10
+    for name, v in res.items():
+        assert v["subclass"] and v["space_solver"] == "GB300SpaceSolver", (name, v)
+        assert v["cons_equal"] and v["dts_equal"] and v["t_equal"] and v["steps"] == v["steps_ref"], (name, v)
 
 
 def test_every_registered_target_has_a_handler():
