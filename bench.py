@@ -254,8 +254,9 @@ def batch_cases(ncases=256, seed=0, sides=None):
 
 
 def run_batch(args):
-    """Batched (one persistent launch per stage, graph-captured, autotuned)
-    against one case at a time through the single-case fused path."""
+    """Batched (every stage's face and epilogue launches over one work list of
+    all cases, graph-captured, autotuned) against one case at a time through
+    the single-case fused path."""
     from jaxfluids_gb300 import BatchedRK3, FusedRK3, autotune, build
     build.build()
     device = torch.device("cuda", 0)
@@ -265,10 +266,10 @@ def run_batch(args):
     batch = BatchedRK3(cfgs, device)
     batch.set_states([s.to(device) for s in states])
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    tune = autotune(batch, candidates=[((15, 32, 1), 256, 2 * sms), ((31, 16, 1), 256, 2 * sms),
-                                       ((15, 32, 1), 256, sms), ((15, 16, 1), 128, 3 * sms),
-                                       ((16, 32, 1), 256, 2 * sms), ((32, 16, 1), 256, 2 * sms),
-                                       ((8, 64, 1), 256, 2 * sms), ((16, 16, 1), 128, 3 * sms)], steps=1)
+    tune = autotune(batch, candidates=[((16, 16, 1), 128, 2 * sms), ((16, 16, 1), 128, 4 * sms),
+                                       ((16, 16, 1), 256, 2 * sms), ((16, 8, 1), 128, 4 * sms),
+                                       ((32, 16, 1), 256, 2 * sms), ((16, 32, 1), 256, 2 * sms),
+                                       ((32, 32, 1), 256, 2 * sms), ((16, 16, 1), 128, 8 * sms)], steps=1)
     graph = batch.capture(args.steps)
     for _ in range(max(1, args.warmup // max(1, args.steps))):
         graph.replay()

@@ -367,10 +367,14 @@ int gbf_rk3_stage_vjp(const gbf_case* c, int stage, const double* cons_k, const 
  * every case, tiles of shape `tile`).  States are packed per case: case c
  * occupies doubles [offset, offset + 5 n_c) of `cons`, variable-major with
  * stride n_c = cells of c.  `dt_states`: double[4 ncases] = per case {dt, t,
- * reduction slots}.  `workspace`: two stage buffers of the packed size
- * (gbf_batch_workspace_bytes).  Each stage is ONE persistent launch of `ctas`
- * CTAs (0 = 2 per SM) looping over the work list; one more launch per step
- * updates every case's dt.  No host synchronisation; graph-capturable.
+ * reduction slots}.  `workspace`: two stage buffers and two primitive
+ * buffers of the packed size and the face fluxes of three axes
+ * (gbf_batch_workspace_bytes).  Each stage is the single-case fused stage over
+ * the work list: one face-kernel launch per active axis and one epilogue
+ * launch, each of `ctas` CTAs (0 = 2 per SM) looping over the work list; one
+ * more launch per step updates every case's dt.  A batched case advances
+ * bitwise like the same case through gbf_rk3_advance.  No host
+ * synchronisation; graph-capturable.
  * `scheme` supplies everything but the sizes (n, dx are taken per case): any
  * inviscid PRIMITIVE or CHAR-PRIMITIVE scheme but Lax-Friedrichs, without the
  * limiter, gravity or boundary value fields (GBF_ERR_UNSUPPORTED otherwise).

@@ -4,10 +4,11 @@ JAX-Fluids batches equal-size cases with ``jax.vmap`` over
 ``SimulationManager._feed_forward`` (simulation_manager.py:1248-1294).
 ``BatchedRK3`` advances cases of different grid sizes that share one scheme,
 each with its own CFL time step, through ``gbf_batch_advance``: every RK stage
-is one persistent kernel launch over a (case, tile) work list, so a batch of
-small grids fills the GPU the way one large grid does.  ``capture`` records a
-run of steps in a CUDA graph; ``autotune`` picks the tile shape, threads per
-CTA and persistent grid size by timing candidates on the batch itself.
+is the single-case fused stage (a face-kernel launch per active axis, then the
+cell epilogue) over a (case, tile) work list, so a batch of small grids fills
+the GPU the way one large grid does.  ``capture`` records a run of steps in a
+CUDA graph; ``autotune`` picks the tile shape, threads per CTA and persistent
+grid size by timing candidates on the batch itself.
 """
 from __future__ import annotations
 
@@ -32,7 +33,7 @@ _SCHEME_KEYS = ("nh", "gamma", "R", "recon", "recon_var", "frozen_state", "riema
 
 
 def default_tile(dim: int) -> Tuple[int, int, int]:
-    return {1: (256, 1, 1), 2: (15, 32, 1), 3: (8, 8, 8)}[dim]
+    return {1: (256, 1, 1), 2: (16, 16, 1), 3: (8, 8, 8)}[dim]
 
 
 def build_worklist(cells: Sequence[Tuple[int, int, int]], tile: Tuple[int, int, int]):
@@ -78,7 +79,8 @@ class BatchedRK3:
         self._layout(tile or default_tile(c0.dim))
         self.cons = torch.zeros(self.total, dtype=torch.float64, device=self.device)
         self.dt_states = torch.zeros(4 * len(configs), dtype=torch.float64, device=self.device)
-        self.workspace = torch.empty(2 * self.total, dtype=torch.float64, device=self.device)
+        nb = int(self.lib.gbf_batch_workspace_bytes(self.total))
+        self.workspace = torch.empty(nb // 8, dtype=torch.float64, device=self.device)
 
     # ---- layout -----------------------------------------------------------
     def _layout(self, tile):
@@ -174,9 +176,9 @@ def autotune(batch: BatchedRK3, candidates: Optional[List[Tuple[Tuple[int, int, 
     if candidates is None:
         sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
         if dim == 2:
-            # 15 x 32 and 31 x 16 give 512 / 496 faces per axis: two full
-            # rounds of 256 threads per face sweep, no ragged third round
-            shapes = [(15, 32, 1), (16, 32, 1), (31, 16, 1), (15, 16, 1), (32, 16, 1), (8, 64, 1), (16, 16, 1)]
+            # cell tiles whose faces along either axis fill whole rounds of
+            # 128 or 256 threads
+            shapes = [(16, 16, 1), (16, 8, 1), (8, 16, 1), (32, 16, 1), (16, 32, 1), (32, 32, 1)]
         elif dim == 3:
             shapes = [(7, 8, 8), (8, 8, 8), (8, 8, 16), (4, 8, 16), (8, 16, 8)]
         else:

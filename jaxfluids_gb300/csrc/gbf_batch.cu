@@ -1,11 +1,12 @@
 // Batched fused TVD-RK3 over many independent cases of uneven size.
 //
-// One persistent kernel per RK stage walks a work list of (case, tile)
-// pairs; each tile runs the same fused sweep as the single-case path with the
+// Each RK stage walks a work list of (case, tile) pairs: one face-kernel
+// launch per active axis and one epilogue launch (gbf_batch.cuh), with the
 // case's sizes, cell widths, state offsets and time-step slots.  Small cases
-// that would each leave most of the GPU idle (a 64^2 case is 8 tiles) thereby
-// share one launch, and the whole step (3 stage launches + 1 time-step
-// launch) has a fixed launch sequence that can be captured in a CUDA graph.
+// that would each leave most of the GPU idle (a 64^2 case is 16 tiles of
+// 16 x 16) thereby share every launch, and the whole step (per stage the face
+// launches and the epilogue, then one time-step launch) has a fixed launch
+// sequence that can be captured in a CUDA graph.
 #include <algorithm>
 #include <vector>
 
@@ -86,6 +87,65 @@ __global__ void batch_dt_kernel(const gbf_batch_case* cases, int ncases, double*
   red[1] = (unsigned long long)0x7ff0000000000000ull;
 }
 
+// The primitives of the packed states (per work item, its tile's cells).
+__global__ void batch_prims_kernel(const BatchParams bp, double gm1, double* prims) {
+  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
+    const int c = bp.worklist[2 * item];
+    const int tile = bp.worklist[2 * item + 1];
+    SweepParams p;
+    batch_case_params(bp, c, p);
+    const gbf_batch_case& cs = bp.cases[c];
+    int b[3], o[3], e[3];
+    batch_tile(p, cs, tile, b, o, e);
+    const long long ncs = (long long)cs.n[0] * cs.n[1] * cs.n[2];
+    for (int j = threadIdx.x; j < e[0] * e[1] * e[2]; j += blockDim.x) {
+      const int j2 = j % e[2], j1 = (j / e[2]) % e[1], j0 = j / (e[2] * e[1]);
+      const long long off = ((long long)(o[0] + j0) * cs.n[1] + (o[1] + j1)) * cs.n[2] + (o[2] + j2);
+      double U[5], P[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) U[v] = bp.cons[cs.offset + v * ncs + off];
+      prims_from_cons(U, P, gm1);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) prims[cs.offset + v * ncs + off] = P[v];
+    }
+  }
+}
+
+// The stage epilogue of every work item's cells (epilogue_cell): divergence of
+// the case's face fluxes, RK combination, primitives of the new state, and in
+// the last stage the case's time-step reductions.
+__global__ void __launch_bounds__(256) batch_epilogue_kernel(const BatchParams bp) {
+  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
+    const int c = bp.worklist[2 * item];
+    const int tile = bp.worklist[2 * item + 1];
+    SweepParams p;
+    batch_case_params(bp, c, p);
+    const gbf_batch_case& cs = bp.cases[c];
+    FaceBuffers fb;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const bool active = (p.active_mask >> a) & 1;
+      fb.nf[a] = active ? batch_faces_per_line(p, a) : 0;
+      fb.flux[a] = active ? bp.faces[a] + 2 * cs.offset : nullptr;
+    }
+    fb.lf_alpha = nullptr;
+    double* prims_out = bp.prims_out ? bp.prims_out + cs.offset : nullptr;
+    int b[3], o[3], e[3];
+    batch_tile(p, cs, tile, b, o, e);
+    const long long ncs = (long long)cs.n[0] * cs.n[1] * cs.n[2];
+    const double dt = p.dt_state[0];
+    double smax = 0.0;
+    double rmin = __longlong_as_double(0x7ff0000000000000LL);
+    for (int j = threadIdx.x; j < e[0] * e[1] * e[2]; j += blockDim.x) {
+      const int j2 = j % e[2], j1 = (j / e[2]) % e[1], j0 = j / (e[2] * e[1]);
+      const int cc[3] = {o[0] + j0, o[1] + j1, o[2] + j2};
+      const long long i = ((long long)cc[0] * cs.n[1] + cc[1]) * cs.n[2] + cc[2];
+      epilogue_cell(p, fb, prims_out, i, cc, ncs, dt, smax, rmin);
+    }
+    if (bp.reduce_dt) dt_block_reduce(p.dt_state, smax, rmin);
+  }
+}
+
 __global__ void batch_slot_init_kernel(double* dt_states, int ncases) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncases) return;
@@ -94,36 +154,51 @@ __global__ void batch_slot_init_kernel(double* dt_states, int ncases) {
   red[1] = (unsigned long long)0x7ff0000000000000ull;
 }
 
-int launch_batch_sweep(const gbf_case* c, const BatchParams& bp, int threads, size_t smem, int ctas,
+// The face kernel of axis `axis` for the batch's scheme.
+int launch_batch_faces(const gbf_case* c, int axis, const BatchParams& bp, int threads, size_t smem, int ctas,
                        cudaStream_t s) {
   const int grid = std::max(1, std::min(ctas, bp.ntiles));
   // WENO5-Z / MUSCL / CHAR-ROE with HLLC or Rusanov here, the other inviscid
   // schemes in gbf_batch_schemes.cu
   const bool here = (c->riemann == GBF_RIEMANN_HLLC || c->riemann == GBF_RIEMANN_RUSANOV) &&
                     (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE || c->recon <= GBF_RECON_MINMOD_AD);
-  if (!here) return launch_batch_sweep_schemes(c, bp, grid, threads, smem, s);
+  if (!here) return launch_batch_faces_schemes(c, axis, bp, grid, threads, smem, s);
   const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
-    return hllc ? launch_batch_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
-                : launch_batch_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
+    return hllc ? launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
+                : launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
   switch (c->recon) {
     case GBF_RECON_WENO5Z:
-      return hllc ? launch_batch_one<GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
-                  : launch_batch_one<GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
     case GBF_RECON_MINMOD:
-      return hllc ? launch_batch_one<GBF_RECON_MINMOD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
-                  : launch_batch_one<GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
     default:
-      return hllc ? launch_batch_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
-                  : launch_batch_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem,
+                                                                                    s);
   }
+}
+
+// One batched stage: the face kernels of every active axis, then the epilogue.
+int launch_batch_stage(const gbf_case* c, const BatchParams& bp, const size_t smem[3], int threads, int ctas,
+                       cudaStream_t s) {
+  int st;
+  for (int a = 0; a < 3; ++a) {
+    if (!((bp.base.active_mask >> a) & 1)) continue;
+    if ((st = launch_batch_faces(c, a, bp, threads, smem[a], ctas, s)) != GBF_OK) return st;
+  }
+  const int grid = std::max(1, std::min(ctas, bp.ntiles));
+  batch_epilogue_kernel<<<grid, threads, 0, s>>>(bp);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
 // Scheme checks shared by init and advance; fills the base params from a
 // representative case (the largest tile shape fits every case).
 int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                 const int32_t* worklist, int ntiles, const gbf_tile* tile, BatchParams* bp,
-                int* threads, size_t* smem) {
+                int* threads, size_t smem[3]) {
   if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
   if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_GRAVITY))
     return GBF_ERR_UNSUPPORTED;
@@ -141,10 +216,21 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
   CaseInfo ci;
   if ((st = make_case_info(&rep, &ci)) != GBF_OK) return st;
   SweepParams p;
-  if ((st = make_sweep_params(&rep, ci, tile, &p, threads, smem)) != GBF_OK) return st;
+  size_t sweep_smem;
+  if ((st = make_sweep_params(&rep, ci, tile, &p, threads, &sweep_smem)) != GBF_OK) return st;
   // the tile shape must be the one the work list was built with
   for (int a = 0; a < 3; ++a)
     if (p.t[a] != std::max(1, tile->t[a]) && rep.n[a] > 1) return GBF_ERR_INVALID_ARGUMENT;
+  // shared memory of each axis' face kernel: a tile's faces along the axis,
+  // one more on the last tile of a line
+  for (int a = 0; a < 3; ++a) {
+    smem[a] = 0;
+    if (!((ci.active_mask >> a) & 1)) continue;
+    FaceTile ft{};
+    for (int b = 0; b < 3; ++b) ft.t[b] = p.t[b] + (b == a ? 1 : 0);
+    smem[a] = face_smem(&rep, ft, a);
+    if (smem[a] > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  }
   BatchParams b{};
   b.base = p;
   b.cases = cases;
@@ -216,8 +302,11 @@ extern "C" int gbf_batch_worklist(const int32_t* cells, const double* dx, int nc
   return record_status(batch_worklist(cells, dx, ncases, tile, cases, worklist, capacity, nitems, total_doubles));
 }
 
+// Workspace: two stage states and two primitive buffers (total_doubles each)
+// and the face fluxes of three axes (2 total_doubles each: a case's faces of
+// an axis are at most 2 N per variable).
 extern "C" size_t gbf_batch_workspace_bytes(int64_t total_doubles) {
-  return total_doubles > 0 ? (size_t)2 * (size_t)total_doubles * sizeof(double) : 0;
+  return total_doubles > 0 ? (size_t)10 * (size_t)total_doubles * sizeof(double) : 0;
 }
 
 static int gbf_batch_init_impl(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
@@ -225,8 +314,8 @@ static int gbf_batch_init_impl(const gbf_case* scheme, const gbf_batch_case* cas
                               const double* cons, double* dt_states, double t0, void* stream) {
   BatchParams bp;
   int threads;
-  size_t smem;
-  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
+  size_t smem[3];
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, smem);
   if (st != GBF_OK) return st;
   if (!cons || !dt_states) return GBF_ERR_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
@@ -252,30 +341,43 @@ static int gbf_batch_advance_impl(const gbf_case* scheme, const gbf_batch_case* 
                                  int64_t total_doubles, int steps, void* stream) {
   BatchParams bp;
   int threads;
-  size_t smem;
-  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
+  size_t smem[3];
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, smem);
   if (st != GBF_OK) return st;
   if (!cons || !dt_states || !workspace || steps < 0 || total_doubles <= 0) return GBF_ERR_INVALID_ARGUMENT;
   if (ctas <= 0) {
-    int dev = 0, sms = 152;
+    int dev = 0, sms = kSms;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     ctas = 2 * sms;
   }
   cudaStream_t s = (cudaStream_t)stream;
   double* A = (double*)workspace;
   double* B = A + total_doubles;
+  double* W[2] = {B + total_doubles, B + 2 * total_doubles};
+  for (int a = 0; a < 3; ++a) bp.faces[a] = B + (3 + 2 * a) * total_doubles;
   const int cb = (ncases + 127) / 128;
+  const int grid = std::max(1, std::min(ctas, ntiles));
   bp.dt_states = dt_states;
+  if (steps == 0) return GBF_OK;
+  // the primitives of U^n, once per call; every stage then writes those of its new state
+  bp.cons = cons;
+  batch_prims_kernel<<<grid, threads, 0, s>>>(bp, scheme->gamma - 1.0, W[0]);
+  int wn = 0;
   for (int step = 0; step < steps; ++step) {
+    const int w1 = 1 - wn, w2 = wn;
     bp.stage = 0; bp.cons = cons; bp.cons0 = cons; bp.out = A; bp.reduce_dt = 0;
-    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    bp.prims = W[wn]; bp.prims_out = W[w1];
+    if ((st = launch_batch_stage(scheme, bp, smem, threads, ctas, s)) != GBF_OK) return st;
     bp.stage = 1; bp.cons = A; bp.cons0 = cons; bp.out = B;
-    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    bp.prims = W[w1]; bp.prims_out = W[w2];
+    if ((st = launch_batch_stage(scheme, bp, smem, threads, ctas, s)) != GBF_OK) return st;
     bp.stage = 2; bp.cons = B; bp.cons0 = cons; bp.out = cons; bp.reduce_dt = 1;
-    if ((st = launch_batch_sweep(scheme, bp, threads, smem, ctas, s)) != GBF_OK) return st;
+    bp.prims = W[w2]; bp.prims_out = W[w1];
+    if ((st = launch_batch_stage(scheme, bp, smem, threads, ctas, s)) != GBF_OK) return st;
     batch_dt_kernel<<<cb, 128, 0, s>>>(cases, ncases, dt_states, scheme->cfl, scheme->eps,
                                        scheme->fixed_dt, 1, 0.0, 0);
     if (cudaGetLastError() != cudaSuccess) return GBF_ERR_CUDA;
+    wn = w1;
   }
   return GBF_OK;
 }

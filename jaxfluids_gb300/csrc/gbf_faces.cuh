@@ -45,9 +45,6 @@ struct FaceBuffers {
   double* lf_alpha;
 };
 
-// One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
-// Reads the stage primitives p.prims (and, for the conservative
-// reconstructions, the stage conservatives p.cons), MODE_STAGE_P semantics.
 // Whether a face kernel shares the smoothness indicators' window terms
 // between faces (reconstruct_pair_shared): the WENO5 family on primitive
 // variables without dissipative fluxes (whose stencils read the primitive
@@ -59,24 +56,18 @@ struct FaceShare {
                                 (RECON == GBF_RECON_WENO5Z || RECON == GBF_RECON_WENO5JS || RECON == GBF_RECON_TENO5);
 };
 
-// Two CTAs per SM (at most 128 registers; the inviscid kernels use about 95
-// and spill nothing).  The kernels issue FP64 instructions at the rate of a
-// pure DFMA chain on this part; a third CTA (at most 85 registers, spilling)
-// measured the same time on TGV 128^3.
+// The faces of axis AX in one face tile: origin o (logical face coordinates),
+// fe faces per axis, nf faces per line along AX; fluxes to out[v * faces +
+// face] (faces of the axis laid out [E0][E1][E2], E_AX = nf).  Reads the stage
+// primitives p.prims (and, for the conservative reconstructions, p.cons),
+// MODE_STAGE_P semantics.  smem: the pencil (and the shared terms) sized by
+// face_smem.  Returns the thread's Lax-Friedrichs face speed maximum (speed
+// pass 1).
 template <int AX, int RECON, int RIEMANN, int VISC>
-__global__ void __launch_bounds__(256, 2)
-    face_flux_kernel(const SweepParams p, const FaceTile ft, const FaceBuffers fb) {
-  extern __shared__ double smem[];
+__device__ __forceinline__ double face_tile_body(const SweepParams& p, const int o[3], const int fe[3], int nf,
+                                                 double* out, double* smem) {
   constexpr int R = ReconTraits<RECON>::R;
   constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
-  const int b = blockIdx.x;
-  const int b2 = b % ft.tiles[2];
-  const int b1 = (b / ft.tiles[2]) % ft.tiles[1];
-  const int b0 = b / (ft.tiles[2] * ft.tiles[1]);
-  const int o[3] = {b0 * ft.t[0], b1 * ft.t[1], b2 * ft.t[2]};
-  int fe[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) fe[a] = min(ft.t[a], ((a == AX) ? ft.nf : p.n[a]) - o[a]);
   // pencil: the stencil cells of the tile's faces, o[AX] - R .. o[AX] + fe[AX] - 2 + R
   int pe[3] = {fe[0], fe[1], fe[2]};
   pe[AX] += 2 * R - 1;
@@ -154,9 +145,8 @@ __global__ void __launch_bounds__(256, 2)
     __syncthreads();
   }
   int ext[3] = {p.n[0], p.n[1], p.n[2]};
-  ext[AX] = ft.nf;
+  ext[AX] = nf;
   const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
-  double* out = fb.flux[AX];
   double smax_faces = 0.0;
   for (int f = threadIdx.x; f < fvol; f += blockDim.x) {
     const int f2 = f % fe[2];
@@ -176,7 +166,122 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * nfaces + g] = F[v];
   }
+  return smax_faces;
+}
+
+// One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
+// Two CTAs per SM (at most 128 registers; the inviscid kernels use about 95
+// and spill nothing).  The kernels issue FP64 instructions at the rate of a
+// pure DFMA chain on this part; a third CTA (at most 85 registers, spilling)
+// measured the same time on TGV 128^3.
+template <int AX, int RECON, int RIEMANN, int VISC>
+__global__ void __launch_bounds__(256, 2)
+    face_flux_kernel(const SweepParams p, const FaceTile ft, const FaceBuffers fb) {
+  extern __shared__ double smem[];
+  const int b = blockIdx.x;
+  const int b2 = b % ft.tiles[2];
+  const int b1 = (b / ft.tiles[2]) % ft.tiles[1];
+  const int b0 = b / (ft.tiles[2] * ft.tiles[1]);
+  const int o[3] = {b0 * ft.t[0], b1 * ft.t[1], b2 * ft.t[2]};
+  int fe[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) fe[a] = min(ft.t[a], ((a == AX) ? ft.nf : p.n[a]) - o[a]);
+  const double smax_faces = face_tile_body<AX, RECON, RIEMANN, VISC>(p, o, fe, ft.nf, fb.flux[AX], smem);
   if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass == 1) lf_speed_reduce<AX>(p, smax_faces);
+}
+
+// The cell epilogue of a stage at cell i (logical coordinates c, cs cells):
+// rhs = ((0 + d_x) + d_y) + d_z with d_a = (1/dx_a)(F[i - 1/2] - F[i + 1/2])
+// (space_solver.py:266-314, :597-599), gravity (space_solver.py:377-384), the
+// RK combination (RK3.py:27-62, time_integrator.py:34-58) into p.out, the
+// primitives of the new state into prims_out, and (p.reduce_dt) the maximum
+// signal speed and minimum density of the new state (time_step_size.py:96-109)
+// folded into smax, rmin.
+__device__ __forceinline__ void epilogue_cell(const SweepParams& p, const FaceBuffers& fb, double* prims_out,
+                                              long long i, const int c[3], long long cs, double dt, double& smax,
+                                              double& rmin) {
+  double acc[5];
+  bool first = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (!(p.active_mask & (1 << a))) continue;
+    int ext[3] = {p.n[0], p.n[1], p.n[2]};
+    ext[a] = fb.nf[a];
+    const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
+    int lo[3] = {c[0], c[1], c[2]};
+    const long long flo = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
+    lo[a] = (c[a] + 1 == fb.nf[a]) ? 0 : c[a] + 1;  // periodic: face N - 1/2 is face -1/2
+    const long long fhi = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
+    const double* F = fb.flux[a];
+    const double odx = p.one_dx[a];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double d = odx * (F[v * nfaces + flo] - F[v * nfaces + fhi]);
+      acc[v] = first ? d : __dadd_rn(acc[v], d);
+    }
+    first = false;
+  }
+  double U[5], Un[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + i];
+  if (p.gravity) add_gravity(acc, U, p.g);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double U0 = (p.stage == 0) ? U[v] : p.cons0[v * cs + i];
+    Un[v] = rk3_combine(p.stage, U[v], U0, acc[v], dt);
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) p.out[v * cs + i] = Un[v];
+  if (!prims_out && !p.reduce_dt) return;
+  double P[5];
+  prims_from_cons(Un, P, p.fp.gm1);
+  if (prims_out) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) prims_out[v * cs + i] = P[v];
+  }
+  if (p.reduce_dt) {
+    const double cc = speed_of_sound(P[4], P[0], p.fp);
+    double s = 0.0;
+    if (p.active_mask & 1) s = s + (fabs(P[1]) + cc);
+    if (p.active_mask & 2) s = s + (fabs(P[2]) + cc);
+    if (p.active_mask & 4) s = s + (fabs(P[3]) + cc);
+    smax = fmax(smax, s);
+    rmin = fmin(rmin, P[0]);
+  }
+}
+
+// The block's maximum signal speed and minimum density into the time-step
+// slots dt_state[2], dt_state[3] (order-preserving bits): warp shuffle ->
+// shared memory -> one atomic per CTA (max / min are exact).  Every thread
+// of the block calls it.
+__device__ __forceinline__ void dt_block_reduce(double* dt_state, double smax, double rmin) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+    rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+  }
+  __shared__ double red[2][32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = smax;
+    red[1][w] = rmin;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = blockDim.x >> 5;
+    smax = (threadIdx.x < nw) ? red[0][threadIdx.x] : 0.0;
+    rmin = (threadIdx.x < nw) ? red[1][threadIdx.x] : __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
+      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
+    }
+    if (threadIdx.x == 0) {
+      atomicMax(reinterpret_cast<unsigned long long*>(dt_state + 2), ordered_bits(smax));
+      atomicMin(reinterpret_cast<unsigned long long*>(dt_state + 3), ordered_bits(rmin));
+    }
+  }
+  __syncthreads();
 }
 
 // Host side ------------------------------------------------------------------

@@ -46,6 +46,10 @@ int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t sm
 // The Lax-Friedrichs speed slots of the current device (gbf_sweep.cu).
 int lf_alpha_on_current_device(double** out);
 
+// Dynamic shared memory of a face kernel of axis `axis` with face tile ft
+// (gbf_stage.cu).
+size_t face_smem(const gbf_case* c, const FaceTile& ft, int axis);
+
 // Lax-Friedrichs speed (mode 1) and tie (mode 2) passes of the face kernels
 // for the adjoint (gbf_stage.cu).
 int launch_lf_face_pass(const gbf_case* c, const CaseInfo& ci, const double* U, const double* P, double* alpha,

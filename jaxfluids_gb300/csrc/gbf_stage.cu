@@ -10,12 +10,8 @@ namespace gbf {
 
 namespace {
 
-// The cell epilogue of a stage: rhs = ((0 + d_x) + d_y) + d_z with
-// d_a = (1/dx_a)(F[i - 1/2] - F[i + 1/2]) (space_solver.py:266-314, :597-599),
-// gravity (space_solver.py:377-384), the RK combination (RK3.py:27-62,
-// time_integrator.py:34-58) into p.out, the primitives of the new state into
-// prims_out, and (p.reduce_dt) the maximum signal speed and minimum density
-// of the new state (time_step_size.py:96-109).
+// The cell epilogue of a stage over every cell of the case (epilogue_cell,
+// dt_block_reduce in gbf_faces.cuh).
 __global__ void __launch_bounds__(256) stage_epilogue_kernel(const SweepParams p, const FaceBuffers fb,
                                                              double* prims_out) {
   const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
@@ -29,83 +25,9 @@ __global__ void __launch_bounds__(256) stage_epilogue_kernel(const SweepParams p
     const int c1 = (int)(r % p.n[1]);
     const int c0 = (int)(r / p.n[1]);
     const int c[3] = {c0, c1, c2};
-    double acc[5];
-    bool first = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (!(p.active_mask & (1 << a))) continue;
-      int ext[3] = {p.n[0], p.n[1], p.n[2]};
-      ext[a] = fb.nf[a];
-      const long long nfaces = (long long)ext[0] * ext[1] * ext[2];
-      int lo[3] = {c0, c1, c2};
-      const long long flo = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
-      lo[a] = (c[a] + 1 == fb.nf[a]) ? 0 : c[a] + 1;  // periodic: face N - 1/2 is face -1/2
-      const long long fhi = ((long long)lo[0] * ext[1] + lo[1]) * ext[2] + lo[2];
-      const double* F = fb.flux[a];
-      const double odx = p.one_dx[a];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const double d = odx * (F[v * nfaces + flo] - F[v * nfaces + fhi]);
-        acc[v] = first ? d : __dadd_rn(acc[v], d);
-      }
-      first = false;
-    }
-    double U[5], Un[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + i];
-    if (p.gravity) add_gravity(acc, U, p.g);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const double U0 = (p.stage == 0) ? U[v] : p.cons0[v * cs + i];
-      Un[v] = rk3_combine(p.stage, U[v], U0, acc[v], dt);
-    }
-#pragma unroll
-    for (int v = 0; v < 5; ++v) p.out[v * cs + i] = Un[v];
-    if (!prims_out && !p.reduce_dt) continue;
-    double P[5];
-    prims_from_cons(Un, P, p.fp.gm1);
-    if (prims_out) {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) prims_out[v * cs + i] = P[v];
-    }
-    if (p.reduce_dt) {
-      const double cc = speed_of_sound(P[4], P[0], p.fp);
-      double s = 0.0;
-      if (p.active_mask & 1) s = s + (fabs(P[1]) + cc);
-      if (p.active_mask & 2) s = s + (fabs(P[2]) + cc);
-      if (p.active_mask & 4) s = s + (fabs(P[3]) + cc);
-      smax = fmax(smax, s);
-      rmin = fmin(rmin, P[0]);
-    }
+    epilogue_cell(p, fb, prims_out, i, c, cs, dt, smax, rmin);
   }
-  if (!p.reduce_dt) return;
-  // warp shuffle -> shared -> one atomic per CTA; max/min are exact
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
-    smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
-    rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
-  }
-  __shared__ double red[2][32];
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    red[0][w] = smax;
-    red[1][w] = rmin;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = blockDim.x >> 5;
-    smax = (threadIdx.x < nw) ? red[0][threadIdx.x] : 0.0;
-    rmin = (threadIdx.x < nw) ? red[1][threadIdx.x] : __longlong_as_double(0x7ff0000000000000LL);
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
-      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
-    }
-    if (threadIdx.x == 0) {
-      atomicMax(reinterpret_cast<unsigned long long*>(p.dt_state + 2), ordered_bits(smax));
-      atomicMin(reinterpret_cast<unsigned long long*>(p.dt_state + 3), ordered_bits(rmin));
-    }
-  }
+  if (p.reduce_dt) dt_block_reduce(p.dt_state, smax, rmin);
 }
 
 bool periodic_axis(const gbf_case* c, int a) { return c->bc[2 * a] == GBF_BC_PERIODIC; }
@@ -162,6 +84,8 @@ int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, F
   return GBF_OK;
 }
 
+}  // namespace
+
 // Shared memory of a face kernel: the pencil (primitives; conservatives too for
 // the conservative reconstructions) and, for the kernels of FaceShare
 // (gbf_faces.cuh), the three window-term arrays of the smoothness indicators.
@@ -183,6 +107,8 @@ size_t face_smem(const gbf_case* c, const FaceTile& ft, int axis) {
   }
   return (size_t)((cons_pencil ? 10 : (share ? 20 : 5)) * pv + 5 * sv) * sizeof(double);
 }
+
+namespace {
 
 // The face kernel of the case's scheme family (as launch_sweep_schemes picks
 // the tile kernel's).
