@@ -74,21 +74,26 @@ __device__ __forceinline__ void batch_tile(const SweepParams& p, const gbf_batch
   }
 }
 
+// The item's case parameters live in shared memory, written once per item by
+// one thread (a per-thread copy would cost every thread the whole struct in
+// local memory).
 template <int AX, int RECON, int RIEMANN>
 __global__ void __launch_bounds__(256, 2) batch_face_kernel(const BatchParams bp) {
   extern __shared__ double smem[];
+  __shared__ SweepParams sp;
   for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
     const int c = bp.worklist[2 * item];
     const int tile = bp.worklist[2 * item + 1];
-    SweepParams p;
-    batch_case_params(bp, c, p);
+    if (threadIdx.x == 0) batch_case_params(bp, c, sp);
+    __syncthreads();
+    const SweepParams& p = sp;
     const gbf_batch_case& cs = bp.cases[c];
     int b[3], o[3], fe[3];
     batch_tile(p, cs, tile, b, o, fe);
     const int nf = batch_faces_per_line(p, AX);
     if (b[AX] == cs.tiles[AX] - 1) fe[AX] = nf - o[AX];  // the line's last faces
     face_tile_body<AX, RECON, RIEMANN, 0>(p, o, fe, nf, bp.faces[AX] + 2 * cs.offset, smem);
-    __syncthreads();  // the next item restages the shared pencil
+    __syncthreads();  // the next item rewrites the parameters and restages the pencil
   }
 }
 
