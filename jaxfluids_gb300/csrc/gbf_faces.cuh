@@ -36,6 +36,14 @@ struct FaceTile {
   int nf;
 };
 
+// The face tiles of one launch over several axes: the blocks of axis a are
+// start[a] .. start[a + 1] - 1 (none for an axis not launched); start[3] is
+// the grid.
+struct FaceTiles {
+  FaceTile ft[3];
+  int start[4];
+};
+
 // Face buffers of a stage: flux[a][v * faces_a + face], faces of axis a laid
 // out [E0][E1][E2] with E_a = nf[a] and the other extents the cell counts;
 // lf_alpha: the Lax-Friedrichs speed slots (3 doubles of the same workspace).
@@ -169,16 +177,11 @@ __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int
   return smax_faces;
 }
 
-// One face kernel: the faces of axis AX in tile blockIdx.x, fluxes to fb.
-// Two CTAs per SM (at most 128 registers; the inviscid kernels use about 95
-// and spill nothing).  The kernels issue FP64 instructions at the rate of a
-// pure DFMA chain on this part; a third CTA (at most 85 registers, spilling)
-// measured the same time on TGV 128^3.
+// The faces of axis AX in face tile b of ft, fluxes to fb; Lax-Friedrichs'
+// speed pass 1 reduces the tile's face speeds.
 template <int AX, int RECON, int RIEMANN, int VISC>
-__global__ void __launch_bounds__(256, 2)
-    face_flux_kernel(const SweepParams p, const FaceTile ft, const FaceBuffers fb) {
-  extern __shared__ double smem[];
-  const int b = blockIdx.x;
+__device__ __forceinline__ void face_tile(const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb, int b,
+                                          double* smem) {
   const int b2 = b % ft.tiles[2];
   const int b1 = (b / ft.tiles[2]) % ft.tiles[1];
   const int b0 = b / (ft.tiles[2] * ft.tiles[1]);
@@ -188,6 +191,26 @@ __global__ void __launch_bounds__(256, 2)
   for (int a = 0; a < 3; ++a) fe[a] = min(ft.t[a], ((a == AX) ? ft.nf : p.n[a]) - o[a]);
   const double smax_faces = face_tile_body<AX, RECON, RIEMANN, VISC>(p, o, fe, ft.nf, fb.flux[AX], smem);
   if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass == 1) lf_speed_reduce<AX>(p, smax_faces);
+}
+
+// One face kernel for the listed axes: block blockIdx.x is a face tile of the
+// axis whose block range holds it, so the tiles of all axes share one launch
+// (the last wave of one axis overlaps the next axis' tiles).  Two CTAs per SM
+// (at most 128 registers; the inviscid kernels use about 110 and spill
+// nothing).  The kernels issue FP64 instructions at the rate of a pure DFMA
+// chain on this part; a third CTA (at most 85 registers, spilling) measured
+// the same time on TGV 128^3.
+template <int RECON, int RIEMANN, int VISC>
+__global__ void __launch_bounds__(256, 2)
+    face_flux_kernel(const SweepParams p, const FaceTiles fts, const FaceBuffers fb) {
+  extern __shared__ double smem[];
+  const int b = blockIdx.x;
+  if (b < fts.start[1])
+    face_tile<0, RECON, RIEMANN, VISC>(p, fts.ft[0], fb, b - fts.start[0], smem);
+  else if (b < fts.start[2])
+    face_tile<1, RECON, RIEMANN, VISC>(p, fts.ft[1], fb, b - fts.start[1], smem);
+  else
+    face_tile<2, RECON, RIEMANN, VISC>(p, fts.ft[2], fb, b - fts.start[2], smem);
 }
 
 // The cell epilogue of a stage at cell i (logical coordinates c, cs cells):
@@ -286,29 +309,25 @@ __device__ __forceinline__ void dt_block_reduce(double* dt_state, double smax, d
 
 // Host side ------------------------------------------------------------------
 
-// Launch the face kernel of axis `axis` for one scheme (instantiated per
-// scheme family in gbf_faces_<family>.cu).
+// Launch the face kernel of the axes fts lists for one scheme (instantiated
+// per scheme family in gbf_sweep_<family>.cu).
 template <int RECON, int RIEMANN, int VISC>
-int launch_faces_one(int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb, int threads,
-                     size_t smem, cudaStream_t s) {
-  const int grid = ft.tiles[0] * ft.tiles[1] * ft.tiles[2];
-  auto go = [&](auto kern) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return GBF_ERR_CUDA;
-    kern<<<grid, threads, smem, s>>>(p, ft, fb);
-    return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
-  };
-  if (axis == 0) return go(face_flux_kernel<0, RECON, RIEMANN, VISC>);
-  if (axis == 1) return go(face_flux_kernel<1, RECON, RIEMANN, VISC>);
-  return go(face_flux_kernel<2, RECON, RIEMANN, VISC>);
+int launch_faces_one(const SweepParams& p, const FaceTiles& fts, const FaceBuffers& fb, int threads, size_t smem,
+                     cudaStream_t s) {
+  auto kern = face_flux_kernel<RECON, RIEMANN, VISC>;
+  if (fts.start[3] <= 0) return GBF_OK;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return GBF_ERR_CUDA;
+  kern<<<fts.start[3], threads, smem, s>>>(p, fts, fb);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
 template <int RECON, int VISC>
-int launch_faces_riemann(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_riemann(int riemann, const SweepParams& p, const FaceTiles& fts, const FaceBuffers& fb,
                          int threads, size_t smem, cudaStream_t s) {
-  if (riemann == GBF_RIEMANN_HLLC) return launch_faces_one<RECON, GBF_RIEMANN_HLLC, VISC>(axis, p, ft, fb, threads, smem, s);
-  if (riemann == GBF_RIEMANN_HLL) return launch_faces_one<RECON, GBF_RIEMANN_HLL, VISC>(axis, p, ft, fb, threads, smem, s);
-  return launch_faces_one<RECON, GBF_RIEMANN_RUSANOV, VISC>(axis, p, ft, fb, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLLC) return launch_faces_one<RECON, GBF_RIEMANN_HLLC, VISC>(p, fts, fb, threads, smem, s);
+  if (riemann == GBF_RIEMANN_HLL) return launch_faces_one<RECON, GBF_RIEMANN_HLL, VISC>(p, fts, fb, threads, smem, s);
+  return launch_faces_one<RECON, GBF_RIEMANN_RUSANOV, VISC>(p, fts, fb, threads, smem, s);
 }
 
 }  // namespace gbf

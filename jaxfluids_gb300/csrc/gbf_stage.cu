@@ -32,16 +32,17 @@ __global__ void __launch_bounds__(256) stage_epilogue_kernel(const SweepParams p
 
 bool periodic_axis(const gbf_case* c, int a) { return c->bc[2 * a] == GBF_BC_PERIODIC; }
 
-// Face tile of the face kernel of `axis`.  Each face is a long FP64
-// computation, so the tiles of a launch finish together and an SM idles once
-// its last tile is done: the tile count per SM sets the tail.  Tiles of 512
-// faces on 256 threads (16 along the axis; across it 2 x 16 in 3-D, 32 in
-// 2-D, the contiguous axis widest) when that still gives at least 12 tiles
-// per SM (TGV 128^3: 27), else 128 faces on 128 threads (16 along the axis,
-// 8 across; KH 512^2: 13 tiles per SM instead of 3.4, measured 14 % faster;
-// the larger tiles coalesce and reuse L1 better, 0.4-1.5 % on the 3-D
-// workloads).  In 1-D the tile runs along the axis.  A user tile (gbf_tile)
-// gives the extents of every face kernel directly.
+// Face tile of the faces of `axis`.  Each face is a long FP64 computation, so
+// the tiles of a launch finish together and an SM idles once its last tile is
+// done: the tile count per SM sets the tail.  Tiles of 512 faces on 256
+// threads (16 along the axis; across it 2 x 16 in 3-D, 32 in 2-D, the
+// contiguous axis widest) when the case has at least 12 x 512 cells per SM
+// (TGV 128^3: 27 tiles per SM and axis), else 128 faces on 128 threads (16
+// along the axis, 8 across; KH 512^2: 13 tiles per SM instead of 3.4,
+// measured 14 % faster; the larger tiles coalesce and reuse L1 better,
+// 0.4-1.5 % on the 3-D workloads).  The choice is the same for every axis,
+// whose tiles share one launch.  In 1-D the tile runs along the axis.  A user
+// tile (gbf_tile) gives the extents of every face kernel directly.
 
 int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, FaceTile* ft, int* threads) {
   int t[3] = {1, 1, 1};
@@ -54,8 +55,7 @@ int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, F
     int others[2], k = 0;
     for (int a = 0; a < 3; ++a)
       if (a != axis && (ci.active_mask & (1 << a))) others[k++] = a;
-    const long long faces = ci.cells / ci.n[axis] * nf;
-    const bool large = faces >= 12LL * kSms * 512;
+    const bool large = ci.cells >= 12LL * kSms * 512;
     thr = large ? 256 : 128;
     if (k == 0) {
       t[axis] = thr;
@@ -84,7 +84,35 @@ int make_face_tile(const CaseInfo& ci, const gbf_tile* tile, int axis, int nf, F
   return GBF_OK;
 }
 
+// The face tiles of the axes in `mask` (nf faces per line each), one launch.
+int make_face_tiles(const CaseInfo& ci, const gbf_tile* tile, int mask, const int nf[3], FaceTiles* fts,
+                    int* threads) {
+  int start = 0;
+  *threads = 0;
+  for (int a = 0; a < 3; ++a) {
+    fts->start[a] = start;
+    fts->ft[a] = FaceTile{{1, 1, 1}, {1, 1, 1}, 0};
+    if (!(mask & (1 << a))) continue;
+    int thr;
+    const int st = make_face_tile(ci, tile, a, nf[a], &fts->ft[a], &thr);
+    if (st != GBF_OK) return st;
+    if (*threads && thr != *threads) return GBF_ERR_INVALID_ARGUMENT;
+    *threads = thr;
+    start += fts->ft[a].tiles[0] * fts->ft[a].tiles[1] * fts->ft[a].tiles[2];
+  }
+  fts->start[3] = start;
+  return GBF_OK;
+}
+
 }  // namespace
+
+// Shared memory of the face kernel of a tile set: the largest of its axes'.
+size_t face_smem_tiles(const gbf_case* c, const FaceTiles& fts) {
+  size_t m = 0;
+  for (int a = 0; a < 3; ++a)
+    if (fts.start[a + 1] > fts.start[a]) m = std::max(m, face_smem(c, fts.ft[a], a));
+  return m;
+}
 
 // Shared memory of a face kernel: the pencil (primitives; conservatives too for
 // the conservative reconstructions) and, for the kernels of FaceShare
@@ -112,7 +140,7 @@ namespace {
 
 // The face kernel of the case's scheme family (as launch_sweep_schemes picks
 // the tile kernel's).
-int launch_faces(const gbf_case* c, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces(const gbf_case* c, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
                  int threads, size_t smem, cudaStream_t s) {
   const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
   const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
@@ -120,40 +148,40 @@ int launch_faces(const gbf_case* c, int axis, const SweepParams& p, const FaceTi
   const int r = c->riemann;
   if (cons && !(c->flags & GBF_FLAG_NO_CONVECTIVE)) {
     if (c->recon_var == GBF_RECVAR_CONSERVATIVE)
-      return visc ? launch_faces_cons_visc(r, axis, p, ft, fb, threads, smem, s)
-                  : launch_faces_cons(r, axis, p, ft, fb, threads, smem, s);
-    return visc ? launch_faces_charcons_visc(r, axis, p, ft, fb, threads, smem, s)
-                : launch_faces_charcons(r, axis, p, ft, fb, threads, smem, s);
+      return visc ? launch_faces_cons_visc(r, p, ft, fb, threads, smem, s)
+                  : launch_faces_cons(r, p, ft, fb, threads, smem, s);
+    return visc ? launch_faces_charcons_visc(r, p, ft, fb, threads, smem, s)
+                : launch_faces_charcons(r, p, ft, fb, threads, smem, s);
   }
   if (visc) {
-    if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_faces_dissipative(axis, p, ft, fb, threads, smem, s);
+    if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_faces_dissipative(p, ft, fb, threads, smem, s);
     const bool c4 = c->dissipative_stencil[0] == GBF_CENTRAL4 && c->dissipative_stencil[1] == GBF_CENTRAL4 &&
                     c->dissipative_stencil[2] == GBF_CENTRAL4;
     if (chr)
-      return c4 ? launch_faces_char_visc_c4(r, axis, p, ft, fb, threads, smem, s)
-                : launch_faces_char_visc(r, axis, p, ft, fb, threads, smem, s);
+      return c4 ? launch_faces_char_visc_c4(r, p, ft, fb, threads, smem, s)
+                : launch_faces_char_visc(r, p, ft, fb, threads, smem, s);
     switch (c->recon) {
       case GBF_RECON_WENO5Z:
-        return c4 ? launch_faces_weno_visc_c4(r, axis, p, ft, fb, threads, smem, s)
-                  : launch_faces_weno_visc(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_WENO5JS: return launch_faces_weno5js_visc(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_TENO5: return launch_faces_teno5_visc(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_WENO3JS: return launch_faces_visc_weno3js(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_WENO3Z: return launch_faces_visc_weno3z(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_MINMOD: return launch_faces_visc_minmod(r, axis, p, ft, fb, threads, smem, s);
-      case GBF_RECON_MINMOD_AD: return launch_faces_visc_minmod_ad(r, axis, p, ft, fb, threads, smem, s);
+        return c4 ? launch_faces_weno_visc_c4(r, p, ft, fb, threads, smem, s)
+                  : launch_faces_weno_visc(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO5JS: return launch_faces_weno5js_visc(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_TENO5: return launch_faces_teno5_visc(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO3JS: return launch_faces_visc_weno3js(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_WENO3Z: return launch_faces_visc_weno3z(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_MINMOD: return launch_faces_visc_minmod(r, p, ft, fb, threads, smem, s);
+      case GBF_RECON_MINMOD_AD: return launch_faces_visc_minmod_ad(r, p, ft, fb, threads, smem, s);
       default: return GBF_ERR_UNSUPPORTED;
     }
   }
-  if (chr) return launch_faces_char(r, axis, p, ft, fb, threads, smem, s);
+  if (chr) return launch_faces_char(r, p, ft, fb, threads, smem, s);
   switch (c->recon) {
-    case GBF_RECON_WENO5Z: return launch_faces_weno(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_WENO5JS: return launch_faces_weno5js(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_TENO5: return launch_faces_teno5(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_WENO3JS: return launch_faces_weno3js(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_WENO3Z: return launch_faces_weno3z(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_MINMOD: return launch_faces_minmod(r, axis, p, ft, fb, threads, smem, s);
-    case GBF_RECON_MINMOD_AD: return launch_faces_minmod_ad(r, axis, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO5Z: return launch_faces_weno(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO5JS: return launch_faces_weno5js(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_TENO5: return launch_faces_teno5(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO3JS: return launch_faces_weno3js(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_WENO3Z: return launch_faces_weno3z(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_MINMOD: return launch_faces_minmod(r, p, ft, fb, threads, smem, s);
+    case GBF_RECON_MINMOD_AD: return launch_faces_minmod_ad(r, p, ft, fb, threads, smem, s);
     default: return GBF_ERR_UNSUPPORTED;
   }
 }
@@ -213,23 +241,21 @@ int launch_lf_face_pass(const gbf_case* c, const CaseInfo& ci, const double* U, 
   for (int a = 0; a < 3; ++a)
     if (ci.active_mask & (1 << a)) fb.nf[a] = periodic_axis(c, a) ? ci.n[a] : ci.n[a] + 1;
   fb.lf_alpha = alpha;
-  for (int a = 0; a < 3; ++a) {
-    if (!(ci.active_mask & (1 << a)) || (mode == 2 && a != axis)) continue;
-    FaceTile ft;
-    int threads;
-    if ((st = make_face_tile(ci, nullptr, a, fb.nf[a], &ft, &threads)) != GBF_OK) return st;
-    const size_t smem = face_smem(c, ft, a);
-    if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
-    if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
-  }
+  const int mask = (mode == 2) ? (ci.active_mask & (1 << axis)) : ci.active_mask;
+  FaceTiles fts;
+  int threads;
+  if ((st = make_face_tiles(ci, nullptr, mask, fb.nf, &fts, &threads)) != GBF_OK) return st;
+  const size_t smem = face_smem_tiles(c, fts);
+  if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  if ((st = launch_faces(c, q, fts, fb, threads, smem, s)) != GBF_OK) return st;
   if (out) *out = q;
   return GBF_OK;
 }
 
 // p carries the stage: prims (primitives of p.cons), cons, cons0, out, stage,
 // reduce_dt, dt_state.  prims_out (may be null) receives the primitives of
-// the new state.  Lax-Friedrichs runs a speed pass of each axis' face kernel
-// before its flux pass (LaxFriedrichs.py:25-47).
+// the new state.  Lax-Friedrichs runs a speed pass of the face kernel before
+// its flux pass (LaxFriedrichs.py:25-47).
 int launch_rk3_stage(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
                      const FaceBuffers& fb, double* prims_out, cudaStream_t s) {
   const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
@@ -240,20 +266,18 @@ int launch_rk3_stage(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile
     if (!q.lf_alpha) return GBF_ERR_INVALID_ARGUMENT;
     if (cudaMemsetAsync(q.lf_alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
   }
-  for (int a = 0; a < 3; ++a) {
-    if (!(ci.active_mask & (1 << a))) continue;
-    FaceTile ft;
-    int threads;
-    if ((st = make_face_tile(ci, tile, a, fb.nf[a], &ft, &threads)) != GBF_OK) return st;
-    const size_t smem = face_smem(c, ft, a);
-    if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
-    if (lf) {
-      q.speed_pass = 1;
-      if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
-      q.speed_pass = 0;
-    }
-    if ((st = launch_faces(c, a, q, ft, fb, threads, smem, s)) != GBF_OK) return st;
+  // the faces of every active axis in one launch
+  FaceTiles fts;
+  int threads;
+  if ((st = make_face_tiles(ci, tile, ci.active_mask, fb.nf, &fts, &threads)) != GBF_OK) return st;
+  const size_t smem = face_smem_tiles(c, fts);
+  if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  if (lf) {
+    q.speed_pass = 1;
+    if ((st = launch_faces(c, q, fts, fb, threads, smem, s)) != GBF_OK) return st;
+    q.speed_pass = 0;
   }
+  if ((st = launch_faces(c, q, fts, fb, threads, smem, s)) != GBF_OK) return st;
   long long grid = (ci.cells + 255) / 256;
   grid = std::min<long long>(grid, 152 * 8);
   stage_epilogue_kernel<<<(int)grid, 256, 0, s>>>(q, fb, prims_out);

@@ -15,9 +15,9 @@ int launch_sweep_charcons(bool visc, int riemann, int mode, const SweepParams& p
   return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
 }
 
-int launch_faces_charcons(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_charcons(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<RECON_WENO5Z_CHARCONS, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<RECON_WENO5Z_CHARCONS, 0>(riemann, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -10,9 +10,9 @@ int launch_sweep_dissipative(int mode, const SweepParams& p, int threads, size_t
   return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
 }
 
-int launch_faces_dissipative(int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_dissipative(const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
                              int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_one<GBF_RECON_MINMOD, RIEMANN_NONE, 1>(axis, p, ft, fb, threads, smem, s);
+  return launch_faces_one<GBF_RECON_MINMOD, RIEMANN_NONE, 1>(p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -63,9 +63,9 @@ int launch_sweep_char_visc_c4(int riemann, int mode, const SweepParams& p, int t
 
 
 // Face kernels of the fused stages, one entry per scheme family
-// (gbf_sweep_<family>.cu): the faces of one axis.
+// (gbf_sweep_<family>.cu): the faces of the axes ft lists, one launch.
 #define GBF_FACES_ARGS \
-  int axis, const SweepParams &p, const FaceTile &ft, const FaceBuffers &fb, int threads, size_t smem, cudaStream_t s
+  const SweepParams &p, const FaceTiles &ft, const FaceBuffers &fb, int threads, size_t smem, cudaStream_t s
 int launch_faces_weno(int riemann, GBF_FACES_ARGS);
 int launch_faces_weno_visc(int riemann, GBF_FACES_ARGS);
 int launch_faces_weno_visc_c4(int riemann, GBF_FACES_ARGS);

@@ -13,14 +13,14 @@ int launch_sweep_muscl(int recon, int riemann, int mode, const SweepParams& p, i
   return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
 }
 
-int launch_faces_minmod(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_minmod(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<GBF_RECON_MINMOD, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<GBF_RECON_MINMOD, 0>(riemann, p, ft, fb, threads, smem, s);
 }
 
-int launch_faces_minmod_ad(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_minmod_ad(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<GBF_RECON_MINMOD_AD, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<GBF_RECON_MINMOD_AD, 0>(riemann, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

@@ -25,14 +25,14 @@ int launch_sweep_weno_family(int recon, int riemann, int mode, const SweepParams
   }
 }
 
-int launch_faces_weno3js(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_weno3js(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<GBF_RECON_WENO3JS, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<GBF_RECON_WENO3JS, 0>(riemann, p, ft, fb, threads, smem, s);
 }
 
-int launch_faces_weno3z(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_weno3z(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<GBF_RECON_WENO3Z, 0>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<GBF_RECON_WENO3Z, 0>(riemann, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf

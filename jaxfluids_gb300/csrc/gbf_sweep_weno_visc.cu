@@ -10,9 +10,9 @@ int launch_sweep_weno_visc(int riemann, int mode, const SweepParams& p, int thre
   return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
 }
 
-int launch_faces_weno_visc(int riemann, int axis, const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb,
+int launch_faces_weno_visc(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {
-  return launch_faces_riemann<GBF_RECON_WENO5Z, 1>(riemann, axis, p, ft, fb, threads, smem, s);
+  return launch_faces_riemann<GBF_RECON_WENO5Z, 1>(riemann, p, ft, fb, threads, smem, s);
 }
 
 }  // namespace gbf
