@@ -42,10 +42,10 @@ BYTES_PER_CELL_UPDATE = 320.0
 # reference's algorithm (oracle/flop_count.py; pinned by tests/test_flop_count.py).
 FP64_FLOP_ALGORITHMIC = {"tgv": 8280.0, "viscous": 11190.0}
 # FP64 thread instructions (DADD + DMUL + DFMA) executed per cell and stage
-# by the three face kernels, from the ncu capture of TGV 128^3 (summary in the
+# by the face kernels of the three axes, from the ncu capture of TGV 128^3 (summary in the
 # profiles directory); the epilogue adds the primitives of the new state.
 FP64_INST_FACES_PER_CELL_STAGE = 2974.8
-# DRAM bytes (read + write) of one RK stage at 128^3 (three face kernels and
+# DRAM bytes (read + write) of one RK stage at 128^3 (the faces of three axes and
 # the epilogue) from the same capture; 120 B/cell algorithmic for stages 2, 3.
 DRAM_BYTES_PER_STAGE = 964.7e6
 
@@ -541,7 +541,7 @@ def main():
         t_dev = tt.item()
     value = world * cells * args.steps / t_dev
 
-    # ---- per-stage time (three face kernels + epilogue; same stream, CUDA events) ----
+    # ---- per-stage time (face kernel + epilogue; same stream, CUDA events) ----
     ka = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     kb = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     for k in range(3):
@@ -567,7 +567,7 @@ def main():
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_source": peak_src,
         "traffic": None if viscous else DRAM_BYTES_PER_STAGE,
-        "launch": "one RK stage: face_flux_kernel x, y, z + stage_epilogue_kernel",
+        "launch": "one RK stage: face_flux_kernel (x, y, z faces) + stage_epilogue_kernel",
         "fp64": {
             "peak_tflops_measured": fp64_peak,  # DFMA chains, 2 FLOP per instruction
             "flop_per_cell_update_algorithmic": flop_alg,
@@ -630,7 +630,9 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             # per advance(1): the stage primitives of U^n, three stages of one face
             # kernel per axis and one epilogue, the time-step kernel
-            "gpu_launches": (1 + 3 * (3 + 1) + 1) * args.steps, "clocks": clocks, "wall_s": wall,
+            # per step: the primitives of U^n (convert_kernel), per stage one
+            # face-kernel launch (every axis) and the epilogue, the next dt
+            "gpu_launches": (1 + 3 * (1 + 1) + 1) * args.steps, "clocks": clocks, "wall_s": wall,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         }
         print(json.dumps(line), flush=True)
