@@ -45,9 +45,10 @@ FP64_FLOP_ALGORITHMIC = {"tgv": 8280.0, "viscous": 11190.0}
 # by the face kernels of the three axes, from the ncu capture of TGV 128^3 (summary in the
 # profiles directory); the epilogue adds the primitives of the new state.
 FP64_INST_FACES_PER_CELL_STAGE = 2974.8
-# DRAM bytes (read + write) of one RK stage at 128^3 (the faces of three axes and
-# the epilogue) from the same capture; 120 B/cell algorithmic for stages 2, 3.
-DRAM_BYTES_PER_STAGE = 964.7e6
+# DRAM bytes (read + write) of one RK stage at 128^3 (the one face launch of
+# the three axes, 466.7 MB, and the epilogue, 579.9 MB) from the ncu captures
+# of the same build; 120 B/cell algorithmic for stages 2, 3.
+DRAM_BYTES_PER_STAGE = 1046.6e6
 
 
 def tgv_state(n, device, dtype=torch.float64):

@@ -1,7 +1,7 @@
 // Batched fused TVD-RK3 over many independent cases of uneven size.
 //
 // Each RK stage walks a work list of (case, tile) pairs: one face-kernel
-// launch per active axis and one epilogue launch (gbf_batch.cuh), with the
+// launch for every active axis and one epilogue launch (gbf_batch.cuh), with the
 // case's sizes, cell widths, state offsets and time-step slots.  Small cases
 // that would each leave most of the GPU idle (a 64^2 case is 16 tiles of
 // 16 x 16) thereby share every launch, and the whole step (per stage the face
@@ -154,41 +154,39 @@ __global__ void batch_slot_init_kernel(double* dt_states, int ncases) {
   red[1] = (unsigned long long)0x7ff0000000000000ull;
 }
 
-// The face kernel of axis `axis` for the batch's scheme.
-int launch_batch_faces(const gbf_case* c, int axis, const BatchParams& bp, int threads, size_t smem, int ctas,
+// The face kernel (every active axis) for the batch's scheme.
+int launch_batch_faces(const gbf_case* c, const BatchParams& bp, int threads, size_t smem, int ctas,
                        cudaStream_t s) {
-  const int grid = std::max(1, std::min(ctas, bp.ntiles));
+  int na = 0;
+  for (int a = 0; a < 3; ++a) na += (bp.base.active_mask >> a) & 1;
+  const int grid = (int)std::max(1LL, std::min((long long)ctas, (long long)na * bp.ntiles));
   // WENO5-Z / MUSCL / CHAR-ROE with HLLC or Rusanov here, the other inviscid
   // schemes in gbf_batch_schemes.cu
   const bool here = (c->riemann == GBF_RIEMANN_HLLC || c->riemann == GBF_RIEMANN_RUSANOV) &&
                     (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE || c->recon <= GBF_RECON_MINMOD_AD);
-  if (!here) return launch_batch_faces_schemes(c, axis, bp, grid, threads, smem, s);
+  if (!here) return launch_batch_faces_schemes(c, bp, grid, threads, smem, s);
   const bool hllc = c->riemann == GBF_RIEMANN_HLLC;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE)
-    return hllc ? launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
-                : launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
+    return hllc ? launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                : launch_batch_faces_one<RECON_WENO5Z_CHAR, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
   switch (c->recon) {
     case GBF_RECON_WENO5Z:
-      return hllc ? launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
-                  : launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_WENO5Z, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
     case GBF_RECON_MINMOD:
-      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
-                  : launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_MINMOD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
     default:
-      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s)
-                  : launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem,
-                                                                                    s);
+      return hllc ? launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s)
+                  : launch_batch_faces_one<GBF_RECON_MINMOD_AD, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
   }
 }
 
-// One batched stage: the face kernels of every active axis, then the epilogue.
-int launch_batch_stage(const gbf_case* c, const BatchParams& bp, const size_t smem[3], int threads, int ctas,
+// One batched stage: the face kernel (every active axis), then the epilogue.
+int launch_batch_stage(const gbf_case* c, const BatchParams& bp, size_t smem, int threads, int ctas,
                        cudaStream_t s) {
   int st;
-  for (int a = 0; a < 3; ++a) {
-    if (!((bp.base.active_mask >> a) & 1)) continue;
-    if ((st = launch_batch_faces(c, a, bp, threads, smem[a], ctas, s)) != GBF_OK) return st;
-  }
+  if ((st = launch_batch_faces(c, bp, threads, smem, ctas, s)) != GBF_OK) return st;
   const int grid = std::max(1, std::min(ctas, bp.ntiles));
   batch_epilogue_kernel<<<grid, threads, 0, s>>>(bp);
   return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
@@ -198,7 +196,7 @@ int launch_batch_stage(const gbf_case* c, const BatchParams& bp, const size_t sm
 // representative case (the largest tile shape fits every case).
 int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
                 const int32_t* worklist, int ntiles, const gbf_tile* tile, BatchParams* bp,
-                int* threads, size_t smem[3]) {
+                int* threads, size_t* smem) {
   if (!scheme || !cases || !worklist || ncases <= 0 || ntiles <= 0 || !tile) return GBF_ERR_INVALID_ARGUMENT;
   if (scheme->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT | GBF_FLAG_INTERPOLATION_LIMITER | GBF_FLAG_GRAVITY))
     return GBF_ERR_UNSUPPORTED;
@@ -221,16 +219,16 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
   // the tile shape must be the one the work list was built with
   for (int a = 0; a < 3; ++a)
     if (p.t[a] != std::max(1, tile->t[a]) && rep.n[a] > 1) return GBF_ERR_INVALID_ARGUMENT;
-  // shared memory of each axis' face kernel: a tile's faces along the axis,
-  // one more on the last tile of a line
+  // shared memory of the face kernel: the largest of the axes' (a tile's faces
+  // along the axis, one more on the last tile of a line)
+  *smem = 0;
   for (int a = 0; a < 3; ++a) {
-    smem[a] = 0;
     if (!((ci.active_mask >> a) & 1)) continue;
     FaceTile ft{};
     for (int b = 0; b < 3; ++b) ft.t[b] = p.t[b] + (b == a ? 1 : 0);
-    smem[a] = face_smem(&rep, ft, a);
-    if (smem[a] > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+    *smem = std::max(*smem, face_smem(&rep, ft, a));
   }
+  if (*smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
   BatchParams b{};
   b.base = p;
   b.cases = cases;
@@ -314,8 +312,8 @@ static int gbf_batch_init_impl(const gbf_case* scheme, const gbf_batch_case* cas
                               const double* cons, double* dt_states, double t0, void* stream) {
   BatchParams bp;
   int threads;
-  size_t smem[3];
-  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, smem);
+  size_t smem;
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
   if (st != GBF_OK) return st;
   if (!cons || !dt_states) return GBF_ERR_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
@@ -341,8 +339,8 @@ static int gbf_batch_advance_impl(const gbf_case* scheme, const gbf_batch_case* 
                                  int64_t total_doubles, int steps, void* stream) {
   BatchParams bp;
   int threads;
-  size_t smem[3];
-  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, smem);
+  size_t smem;
+  int st = batch_setup(scheme, cases, ncases, worklist, ntiles, tile, &bp, &threads, &smem);
   if (st != GBF_OK) return st;
   if (!cons || !dt_states || !workspace || steps < 0 || total_doubles <= 0) return GBF_ERR_INVALID_ARGUMENT;
   if (ctas <= 0) {

@@ -4,8 +4,8 @@
 // inviscid schemes).
 //
 // A stage of the batch is the single-case fused stage (gbf_faces.cuh) over a
-// work list of (case, tile) pairs: per active axis one launch of the face
-// kernel walks the list, each item computing every face of its cell tile
+// work list of (case, tile) pairs: one launch of the face kernel walks the
+// list once per active axis, each item computing every face of its cell tile
 // along that axis (the last tile along the axis also the closing face of a
 // non-periodic line) into the case's face buffer; then one epilogue launch
 // walks the list again, each item forming its cells' divergence, RK
@@ -74,45 +74,62 @@ __device__ __forceinline__ void batch_tile(const SweepParams& p, const gbf_batch
   }
 }
 
-// The item's case parameters live in shared memory, written once per item by
-// one thread (a per-thread copy would cost every thread the whole struct in
-// local memory).
+// The faces of axis AX of one work item (its cell tile; the last tile of a
+// line also the closing face) into the case's face buffer.
 template <int AX, int RECON, int RIEMANN>
+__device__ __forceinline__ void batch_face_item(const BatchParams& bp, const SweepParams& p, const gbf_batch_case& cs,
+                                                int tile, double* smem) {
+  int b[3], o[3], fe[3];
+  batch_tile(p, cs, tile, b, o, fe);
+  const int nf = batch_faces_per_line(p, AX);
+  if (b[AX] == cs.tiles[AX] - 1) fe[AX] = nf - o[AX];  // the line's last faces
+  face_tile_body<AX, RECON, RIEMANN, 0>(p, o, fe, nf, bp.faces[AX] + 2 * cs.offset, smem);
+}
+
+// The faces of every active axis of every work item in one launch: the CTAs
+// loop over (axis, item) pairs, the items of the first active axis first, so
+// one tail per stage remains.  The item's case parameters live in shared
+// memory, written once per item by one thread (a per-thread copy would cost
+// every thread the whole struct in local memory).
+template <int RECON, int RIEMANN>
 __global__ void __launch_bounds__(256, 2) batch_face_kernel(const BatchParams bp) {
   extern __shared__ double smem[];
   __shared__ SweepParams sp;
-  for (int item = blockIdx.x; item < bp.ntiles; item += gridDim.x) {
+  int axes[3], na = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    if ((bp.base.active_mask >> a) & 1) axes[na++] = a;
+  const long long pairs = (long long)na * bp.ntiles;
+  for (long long v = blockIdx.x; v < pairs; v += gridDim.x) {
+    const int ax = axes[v / bp.ntiles];
+    const int item = (int)(v % bp.ntiles);
     const int c = bp.worklist[2 * item];
     const int tile = bp.worklist[2 * item + 1];
     if (threadIdx.x == 0) batch_case_params(bp, c, sp);
     __syncthreads();
-    const SweepParams& p = sp;
     const gbf_batch_case& cs = bp.cases[c];
-    int b[3], o[3], fe[3];
-    batch_tile(p, cs, tile, b, o, fe);
-    const int nf = batch_faces_per_line(p, AX);
-    if (b[AX] == cs.tiles[AX] - 1) fe[AX] = nf - o[AX];  // the line's last faces
-    face_tile_body<AX, RECON, RIEMANN, 0>(p, o, fe, nf, bp.faces[AX] + 2 * cs.offset, smem);
-    __syncthreads();  // the next item rewrites the parameters and restages the pencil
+    if (ax == 0)
+      batch_face_item<0, RECON, RIEMANN>(bp, sp, cs, tile, smem);
+    else if (ax == 1)
+      batch_face_item<1, RECON, RIEMANN>(bp, sp, cs, tile, smem);
+    else
+      batch_face_item<2, RECON, RIEMANN>(bp, sp, cs, tile, smem);
+    __syncthreads();  // the next pair rewrites the parameters and restages the pencil
   }
 }
 
 template <int RECON, int RIEMANN>
-int launch_batch_faces_one(int axis, const BatchParams& bp, int grid, int threads, size_t smem, cudaStream_t s) {
-  auto go = [&](auto kern) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return GBF_ERR_CUDA;
-    kern<<<grid, threads, smem, s>>>(bp);
-    return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
-  };
-  if (axis == 0) return go(batch_face_kernel<0, RECON, RIEMANN>);
-  if (axis == 1) return go(batch_face_kernel<1, RECON, RIEMANN>);
-  return go(batch_face_kernel<2, RECON, RIEMANN>);
+int launch_batch_faces_one(const BatchParams& bp, int grid, int threads, size_t smem, cudaStream_t s) {
+  auto kern = batch_face_kernel<RECON, RIEMANN>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return GBF_ERR_CUDA;
+  kern<<<grid, threads, smem, s>>>(bp);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
 }
 
 // The schemes of gbf_batch_schemes.cu: WENO5-JS, TENO5, WENO3-JS, WENO3-Z with
 // HLLC, HLL or Rusanov, and HLL with WENO5-Z, MUSCL and CHAR-PRIMITIVE.
-int launch_batch_faces_schemes(const gbf_case* c, int axis, const BatchParams& bp, int grid, int threads,
-                               size_t smem, cudaStream_t s);
+int launch_batch_faces_schemes(const gbf_case* c, const BatchParams& bp, int grid, int threads, size_t smem,
+                               cudaStream_t s);
 
 }  // namespace gbf

@@ -6,20 +6,20 @@ namespace gbf {
 namespace {
 
 template <int RECON>
-int by_riemann(int riemann, int axis, const BatchParams& bp, int grid, int threads, size_t smem, cudaStream_t s) {
+int by_riemann(int riemann, const BatchParams& bp, int grid, int threads, size_t smem, cudaStream_t s) {
   if (riemann == GBF_RIEMANN_HLLC)
-    return launch_batch_faces_one<RECON, GBF_RIEMANN_HLLC>(axis, bp, grid, threads, smem, s);
+    return launch_batch_faces_one<RECON, GBF_RIEMANN_HLLC>(bp, grid, threads, smem, s);
   if (riemann == GBF_RIEMANN_HLL)
-    return launch_batch_faces_one<RECON, GBF_RIEMANN_HLL>(axis, bp, grid, threads, smem, s);
-  return launch_batch_faces_one<RECON, GBF_RIEMANN_RUSANOV>(axis, bp, grid, threads, smem, s);
+    return launch_batch_faces_one<RECON, GBF_RIEMANN_HLL>(bp, grid, threads, smem, s);
+  return launch_batch_faces_one<RECON, GBF_RIEMANN_RUSANOV>(bp, grid, threads, smem, s);
 }
 
 }  // namespace
 
-int launch_batch_faces_weno5_family(int recon, int riemann, int axis, const BatchParams& bp, int grid,
+int launch_batch_faces_weno5_family(int recon, int riemann, const BatchParams& bp, int grid,
                                     int threads, size_t smem, cudaStream_t s) {
-  if (recon == GBF_RECON_WENO5JS) return by_riemann<GBF_RECON_WENO5JS>(riemann, axis, bp, grid, threads, smem, s);
-  return by_riemann<GBF_RECON_TENO5>(riemann, axis, bp, grid, threads, smem, s);
+  if (recon == GBF_RECON_WENO5JS) return by_riemann<GBF_RECON_WENO5JS>(riemann, bp, grid, threads, smem, s);
+  return by_riemann<GBF_RECON_TENO5>(riemann, bp, grid, threads, smem, s);
 }
 
 }  // namespace gbf
