@@ -199,6 +199,53 @@ class OracleRun:
         return time.perf_counter() - t0
 
 
+class CPortRun:
+    """The plain-C restatement of the reference (oracle/jf_rhs.c, compiled with
+    OpenMP on every host core, contraction off; bitwise equal to the torch
+    restatement) advancing the TGV n^3 workload step by step: the same initial
+    condition, scheme and CFL time step as the GPU run, each face computed
+    once per stage as the reference's face arrays hold them."""
+
+    def __init__(self, n):
+        import ctypes
+        import __graft_entry__
+        from oracle import jf_oracle as O
+        so = __graft_entry__.build_oracle_c()
+        if not so:
+            raise RuntimeError("no C compiler for the oracle's C restatement")
+        f = ctypes.CDLL(so).jf_rk3_steps
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                      ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                      ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                      ctypes.POINTER(ctypes.c_double)]
+        f.restype = ctypes.c_int
+        self.U = tgv_state(n, "cpu").numpy().copy()
+        self.P = O.prims_from_cons(torch.from_numpy(self.U), 1.4).numpy().copy()
+        dx = 2 * math.pi / n
+        self.t = ctypes.c_double(0.0)
+        self._byref = ctypes.byref
+        self.args = (self.U.ctypes.data, self.P.ctypes.data, (ctypes.c_int * 3)(n, n, n), 3,
+                     (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 1.0 / dx), dx, 0.5, 1.4, O.STENCIL_EPS,
+                     0, 0, (ctypes.c_int * 6)(0, 0, 0, 0, 0, 0))  # PRIMITIVE, HLLC, periodic
+        self.f = f
+        self.cells = n ** 3
+
+    def step(self):
+        """One RK3 step (the CFL time step of its initial state); returns its wall time (s)."""
+        t0 = time.perf_counter()
+        if self.f(*self.args, 1, self._byref(self.t)) != 0:
+            raise RuntimeError("the C restatement failed")
+        return time.perf_counter() - t0
+
+
+def cpu_port(n, threads):
+    """The fastest CPU restatement available: the C one (OpenMP), else the torch one."""
+    try:
+        return CPortRun(n), f"C, OpenMP, {threads} threads"
+    except (RuntimeError, OSError):
+        return OracleRun(n, threads), f"torch float64, {threads} threads"
+
+
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's algorithm
     (JAX is installed on neither machine, so the reference itself cannot run)
@@ -207,13 +254,13 @@ def run_reference(args, rank, world):
         return
     threads = os.cpu_count() or 1
     n = args.n if args.n else N_TGV
-    run = OracleRun(n, threads)
+    run, how = cpu_port(n, threads)
     for _ in range(max(0, args.warmup)):
         run.step()
     total_t = sum(run.step() for _ in range(args.steps))
     value = run.cells * args.steps / total_t
     sample = (f"TGV {n}^3, {args.warmup} warm-up + {args.steps} timed RK3 steps, CPU restatement of the "
-              f"reference (torch float64, {threads} threads on {cpu_model()}); the JAX reference is not installed")
+              f"reference ({how} on {cpu_model()}); the JAX reference is not installed")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
@@ -604,14 +651,14 @@ def main():
            "steps": e2e_steps}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not viscous:
         threads = os.cpu_count() or 1
-        run = OracleRun(n, threads)
+        run, how = cpu_port(n, threads)
         run.step()  # warm-up
         el = sum(run.step() for _ in range(3))
         cpu = {"value": run.cells * 3 / el, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"TGV {n}^3 (the same workload), 1 warm-up + 3 timed RK3 steps ({el:.1f} s), CPU "
-                         f"restatement of the reference (torch float64, {threads} threads)",
+                         f"restatement of the reference ({how})",
                "cpu_model": cpu_model()}
 
     if rank == 0:

@@ -3,7 +3,8 @@
  * of the single-phase right-hand side for WENO5-Z on primitive or characteristic
  * variables with HLLC, HLL (Einfeldt signal speeds) or Rusanov fluxes, on a
  * halo-filled primitive buffer, with its own face halos, CFL time step and
- * TVD-RK3 steps.  It is written independently of the torch restatement in
+ * TVD-RK3 steps; multi-threaded with OpenMP where built with it (the CPU
+ * baseline of the benchmark).  It is written independently of the torch restatement in
  * jf_oracle.py and follows
  * the same reference operations in the same order, so the two must agree
  * bitwise; the tests check that (tests/test_oracle_c.py).  Compile without
@@ -31,6 +32,14 @@
 #include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
+
+/* Built with -fopenmp the cell and face loops run on every host core (the
+   arithmetic of each cell and face is unchanged, so the results are too). */
+#ifdef _OPENMP
+#define JF_OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define JF_OMP_FOR
+#endif
 
 static double weno5z(double u0, double u1, double u2, double u3, double u4, double eps) {
   const double t0 = u0 - 2.0 * u1 + u2, t1 = u0 - 4.0 * u1 + 3.0 * u2;
@@ -237,7 +246,7 @@ static void face_states(double w[6][5], int axis, int mode, double gamma, double
  * rhs[5][n0][n1][n2] of the primitive halo buffer P[5][h0][h1][h2]
  * (h_a = n_a + 2 nh on active axes, 1 on inactive ones), axes summed in order
  * from the first active one; mode as face_states, riemann as riemann_flux.
- * Returns 0.
+ * Returns 0, or -2 when out of memory.
  */
 int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
                   int mode, int riemann, double* rhs) {
@@ -252,28 +261,44 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
   for (int a = 0; a < 3; ++a) {
     if (n[a] <= 1) continue;
     const size_t stride = (a == 0) ? (size_t)h[1] * h[2] : (a == 1) ? (size_t)h[2] : 1;
+    /* the N + 1 faces of every line along a, each once (face f between cells
+       f - 1 and f), laid out [f0][f1][f2] with N + 1 along a */
+    int e[3] = {n[0], n[1], n[2]};
+    e[a] = n[a] + 1;
+    const size_t nfaces = (size_t)e[0] * e[1] * e[2];
+    double* F = (double*)malloc(5 * nfaces * sizeof(double));
+    if (!F) return -2;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i0 = 0; i0 < e[0]; ++i0)
+      for (int i1 = 0; i1 < e[1]; ++i1)
+        for (int i2 = 0; i2 < e[2]; ++i2) {
+          const int g[3] = {i0 + lo[0], i1 + lo[1], i2 + lo[2]};
+          const size_t c0 = ((size_t)g[0] * h[1] + g[1]) * h[2] + g[2];
+          double w[6][5], PL[5], PR[5], Ff[5];
+          for (int v = 0; v < 5; ++v)
+            for (int k = 0; k < 6; ++k) w[k][v] = P[v * hcs + c0 + (ptrdiff_t)(k - 3) * (ptrdiff_t)stride];
+          face_states(w, a, mode, gamma, eps, PL, PR);
+          riemann_flux(PL, PR, a + 1, gamma, riemann, Ff);
+          const size_t o = ((size_t)i0 * e[1] + i1) * e[2] + i2;
+          for (int v = 0; v < 5; ++v) F[v * nfaces + o] = Ff[v];
+        }
+    const size_t fstride = (a == 0) ? (size_t)e[1] * e[2] : (a == 1) ? (size_t)e[2] : 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (int i0 = 0; i0 < n[0]; ++i0)
       for (int i1 = 0; i1 < n[1]; ++i1)
         for (int i2 = 0; i2 < n[2]; ++i2) {
-          const int idx[3] = {i0, i1, i2};
-          /* fluxes of the faces left (f = c) and right (f = c + 1) of this cell */
-          double F[2][5];
-          for (int side = 0; side < 2; ++side) {
-            int g[3] = {idx[0] + lo[0], idx[1] + lo[1], idx[2] + lo[2]};
-            g[a] += side;  /* face between buffer cells g[a] - 1 and g[a] */
-            const size_t c0 = ((size_t)g[0] * h[1] + g[1]) * h[2] + g[2];
-            double w[6][5], PL[5], PR[5];
-            for (int v = 0; v < 5; ++v)
-              for (int k = 0; k < 6; ++k) w[k][v] = P[v * hcs + c0 + (ptrdiff_t)(k - 3) * (ptrdiff_t)stride];
-            face_states(w, a, mode, gamma, eps, PL, PR);
-            riemann_flux(PL, PR, a + 1, gamma, riemann, F[side]);
-          }
+          const size_t fo = ((size_t)i0 * e[1] + i1) * e[2] + i2;  /* the face left of the cell */
           const size_t o = ((size_t)i0 * n[1] + i1) * n[2] + i2;
           for (int v = 0; v < 5; ++v) {
-            const double r = one_dx[a] * (F[0][v] - F[1][v]);
+            const double r = one_dx[a] * (F[v * nfaces + fo] - F[v * nfaces + fo + fstride]);
             rhs[v * cs + o] = first ? r : rhs[v * cs + o] + r;
           }
         }
+    free(F);
     first = 0;
   }
   return 0;
@@ -368,6 +393,7 @@ int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_
   if (!Ph || !Un || !rhs) st = -2;
   /* interior primitives -> halo buffer, then its face halos */
 #define JF_LOAD_HALO()                                                                    \
+  JF_OMP_FOR                                                                              \
   for (int i0 = 0; i0 < n[0]; ++i0)                                                       \
     for (int i1 = 0; i1 < n[1]; ++i1)                                                     \
       for (int i2 = 0; i2 < n[2]; ++i2) {                                                 \
@@ -380,25 +406,36 @@ int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_
   static const double kDtMult[3] = {1.0, 0.25, 2.0 / 3.0};
   static const double kCons[2][2] = {{0.25, 0.75}, {2.0 / 3.0, 1.0 / 3.0}};
   for (int step = 0; st == 0 && step < steps; ++step) {
+    /* the largest signal speed sum (non-negative: the maximum is exact in any order) */
     double amax = 0.0;
-    int first = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : amax)
+#endif
     for (size_t o = 0; o < cs; ++o) {
       const double c = sqrt(gamma * P[4 * cs + o] / P[o]);
       double s = 0.0;
       for (int a = 0; a < 3; ++a)
         if (n[a] > 1) s = s + (fabs(P[(a + 1) * cs + o]) + c);
-      if (first || s > amax) amax = s;
-      first = 0;
+      if (s > amax) amax = s;
     }
     const double dt = min_cell_size / (amax + 2.220446049250313e-16) * cfl;
     memcpy(Un, U, 5 * cs * sizeof(double));
     for (int stage = 0; stage < 3; ++stage) {
-      jf_rhs_weno5z(Ph, n, nh, one_dx, gamma, eps, mode, riemann, rhs);
+      if (jf_rhs_weno5z(Ph, n, nh, one_dx, gamma, eps, mode, riemann, rhs) != 0) {
+        st = -2;
+        break;
+      }
       const double ts = dt * kDtMult[stage];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
       for (size_t k = 0; k < 5 * cs; ++k) {
         const double base = stage > 0 ? kCons[stage - 1][0] * U[k] + kCons[stage - 1][1] * Un[k] : U[k];
         U[k] = base + ts * rhs[k];
       }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
       for (size_t o = 0; o < cs; ++o) {
         double u5[5], p5[5];
         for (int v = 0; v < 5; ++v) u5[v] = U[v * cs + o];
