@@ -61,6 +61,46 @@ def test_batched_steps_equal_single_case_steps(kw):
         assert batch.dt[i].item() == f.dt.item() and batch.t[i].item() == f.t.item()
 
 
+GEOMETRIES = [
+    # 3-D periodic cases of different sizes (the last tile of a periodic line
+    # holds no closing face), smooth random-phase states
+    ("3d-periodic", [(12, 16, 10), (16, 16, 16), (8, 12, 20)], "PERIODIC", (8, 8, 8)),
+    # 2-D: periodic along x, zero-gradient along y
+    ("2d-mixed", [(40, 24, 1), (16, 48, 1), (33, 17, 1)], {"east": "PERIODIC", "west": "PERIODIC",
+                                                             "north": "ZEROGRADIENT", "south": "ZEROGRADIENT"},
+     (16, 16, 1)),
+    # 1-D zero-gradient lines of uneven length
+    ("1d-zg", [(200, 1, 1), (77, 1, 1), (256, 1, 1)], {"east": "ZEROGRADIENT", "west": "ZEROGRADIENT"},
+     (64, 1, 1)),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,cells,bc,tile", GEOMETRIES, ids=[g[0] for g in GEOMETRIES])
+def test_batched_geometries_equal_single_case_steps(name, cells, bc, tile):
+    """1-D to 3-D cases, periodic and zero-gradient lines, tiles that do not
+    divide the cells: every batched case advances bitwise like itself alone."""
+    from jaxfluids_gb300 import BatchedRK3, CaseConfig, FusedRK3, build
+    from tests.cases import generic_cons
+    build.build()
+    faces = ("east", "west", "north", "south", "top", "bottom")
+    cfgs = []
+    for c in cells:
+        b = dict(bc) if isinstance(bc, dict) else {f: bc for f, a in zip(faces, (0, 0, 1, 1, 2, 2)) if c[a] > 1}
+        cfgs.append(CaseConfig(cells=c, bc=b))
+    states = [generic_cons(c, seed=10 + i) for i, c in enumerate(cells)]
+    batch = BatchedRK3(cfgs, tile=tile, threads=128)
+    batch.set_states([s.cuda() for s in states])
+    batch.advance(4)
+    for i, c in enumerate(cfgs):
+        f = FusedRK3(c)
+        f.set_state(states[i].cuda())
+        f.advance(4)
+        torch.cuda.synchronize()
+        assert torch.equal(batch.case_view(i), f.cons), i
+        assert batch.dt[i].item() == f.dt.item() and batch.t[i].item() == f.t.item()
+
+
 @pytest.mark.gpu
 def test_graph_replay_and_retile_match_eager():
     from jaxfluids_gb300 import BatchedRK3, build
