@@ -1,33 +1,33 @@
-// Fused finite-volume sweep kernel.
+// Per-face finite-volume building blocks and the tile sweep kernel.
 //
-// One CTA owns a tile of T0 x T1 x T2 cells.  For each active axis it stages
-// the primitives of the tile extended by the stencil radius R along that axis
-// (a "pencil box") in shared memory, computes every face flux of the tile
-// exactly once (one face per thread), and adds (1/dx)(F[i-1/2] - F[i+1/2]) to
-// per-thread right-hand-side accumulators in registers.  The epilogue either
-// stores the right-hand side (MODE_RHS, the SpaceSolver.compute_rhs drop-in)
-// or applies the TVD-RK3 stage combination in place of the state
-// (MODE_STAGE, the fused hot path), optionally reducing the next CFL time
-// step of the new state.
+// face_flux (one face from a staged pencil: reconstruction, limiter, Riemann
+// flux, dissipative flux) is shared by the fused stages' face kernels
+// (gbf_faces.cuh), the batched stages (gbf_batch.cuh) and the tile sweep
+// kernel here.  The tile sweep kernel is the drop-in right-hand side
+// (MODE_RHS, SpaceSolver.compute_rhs on halo buffers): one CTA owns a tile of
+// T0 x T1 x T2 cells; for each active axis it stages the primitives of the
+// tile extended by the stencil radius R along that axis (a "pencil box") in
+// shared memory, computes every face flux of the tile once (one face per
+// thread), and adds (1/dx)(F[i-1/2] - F[i+1/2]) to per-thread right-hand-side
+// accumulators in registers, which the epilogue stores.
 //
 // The path is FP64-arithmetic bound on GB300 (about 2 FP64 lanes per SM and
-// clock against kilobytes of FP64 work per cell), so the layout minimises
-// repeated FP64 work rather than HBM traffic: faces are computed once per
-// tile (redundancy (T+1)/T per axis), the primitive conversion of a pencil
-// box is cheap next to the face work, and the state is re-read from L2 for
-// each axis.
+// clock against kilobytes of FP64 work per cell), so the layouts minimise
+// repeated FP64 work rather than HBM traffic.
 #pragma once
 
 #include "gbf_physics.cuh"
 
 namespace gbf {
 
-// MODE_RHS: halo primitive buffer in, rhs out (drop-in).
-// MODE_STAGE: interior conservatives in, RK stage out (primitives of each
-//   pencil derived on the fly).
-// MODE_STAGE_P: as MODE_STAGE, but the primitives of the stage state come from
-//   an interior primitive buffer computed once per stage (used by the viscous
-//   and heat-conduction path, whose face stencils reach across the tile).
+// Where a stencil's primitives come from:
+// MODE_RHS: a halo primitive buffer (the drop-in right-hand side).
+// MODE_STAGE: interior conservatives, the primitives of each staged cell
+//   derived on the way in, boundary rules by index remapping (the adjoint's
+//   pencils).
+// MODE_STAGE_P: an interior primitive buffer computed once per stage,
+//   boundary rules by index remapping (the fused and batched stages' face
+//   kernels; the dissipative stencils read it directly).
 enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_STAGE_P = 2 };
 
 // Boundary values that vary along a face (gbf_case::bc_field_values /
