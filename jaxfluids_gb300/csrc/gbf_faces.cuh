@@ -1,11 +1,12 @@
-// The fused TVD-RK3 stage as per-axis face kernels plus one cell epilogue.
+// The fused TVD-RK3 stage as a face kernel plus one cell epilogue.
 //
 // A stage of the hot path computes every face flux of the grid exactly once.
-// For each active axis a face kernel covers the faces along that axis with
-// tiles of faces (16 along the axis, the rest across it; the contiguous axis
-// widest), stages the primitives of the tile's stencil cells in shared memory
-// (from the stage's primitive buffer, boundary conditions by index remap) and
-// writes the face fluxes to a face buffer of that axis.  The epilogue kernel
+// One face-kernel launch covers the faces of every active axis with tiles of
+// faces of one axis each (16 along the axis, the rest across it; the
+// contiguous axis widest); a tile stages the primitives of its stencil cells
+// in shared memory (from the stage's primitive buffer, boundary conditions by
+// index remap) and writes the face fluxes to the face buffer of its axis.
+// The epilogue kernel
 // (stage_epilogue_kernel, gbf_stage.cu) then forms, per cell, the divergence
 // in the reference's axis order, the RK stage combination, the primitives of
 // the new state (the next stage's input, simulation_manager.py:943-944) and,
