@@ -2,7 +2,8 @@
 
 * TGV 128^3 (WENO5-Z + HLLC, PRIMITIVE, periodic): one right-hand side through
   the drop-in path (<= 1e-12 relative) and 20 fused CFL steps (<= 1e-10),
-  every time step equal.
+  every time step equal; and all 500 steps of the stated run against the
+  oracle's C restatement.
 * Viscous TGV 256^3 (Re 1600, Pr 0.71, WENO5-Z on Roe-characteristic variables
   + HLLC + CENTRAL4 viscous and heat fluxes): one right-hand side and one fused
   step.
@@ -90,6 +91,44 @@ def _rhs_and_steps(oc, cc, prims, steps):
 def test_tgv_128_rhs_and_20_steps():
     oc, cc = both((128, 128, 128), "PERIODIC", ranges=TWO_PI)
     _rhs_and_steps(oc, cc, tgv_prims(128), 20)
+
+
+def test_tgv_128_all_500_steps_against_the_c_restatement():
+    """The inviscid TGV as stated: 128^3, 500 CFL steps, every step's time step
+    from the state at its start, against the oracle's plain-C restatement
+    (bitwise equal to the torch oracle, tests/test_oracle_c.py; OpenMP on the
+    host's cores, about two minutes on 16 cores): the final conservatives and
+    time bitwise equal."""
+    import ctypes
+    import __graft_entry__
+    from jaxfluids_gb300 import FusedRK3
+    so = __graft_entry__.build_oracle_c()
+    if not so:
+        pytest.skip("no C compiler for the oracle's C restatement")
+    f_c = ctypes.CDLL(so).jf_rk3_steps
+    f_c.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double)]
+    f_c.restype = ctypes.c_int
+    n, steps = 128, 500
+    oc, cc = both((n, n, n), "PERIODIC", ranges=TWO_PI)
+    P0 = tgv_prims(n).contiguous()
+    U0 = O.cons_from_prims(P0, oc.gamma).contiguous()
+    f = FusedRK3(cc)
+    f.set_state(U0.cuda(), prims=P0.cuda())
+    f.advance(steps)
+    U = U0.numpy().copy()
+    P = P0.numpy().copy()
+    dx = 2 * math.pi / n
+    t = ctypes.c_double(0.0)
+    assert f_c(U.ctypes.data, P.ctypes.data, (ctypes.c_int * 3)(n, n, n), 3,
+               (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 1.0 / dx), dx, oc.cfl, oc.gamma, O.STENCIL_EPS, 0, 0,
+               (ctypes.c_int * 6)(0, 0, 0, 0, 0, 0), steps, ctypes.byref(t)) == 0
+    cons = f.cons.cpu()
+    assert float(f.t) == t.value
+    assert rel_err(cons, torch.from_numpy(U)) <= 1e-10
+    assert torch.equal(cons, torch.from_numpy(U))
 
 
 def test_viscous_tgv_256_char_roe_rhs_and_one_step():
