@@ -20,7 +20,9 @@
   checkpoints every 50) against central differences in 16 random directions
   at h = 1e-6 relative.
 * The batched path on four quadrant problems with sides 64, 128, 192 and 512
-  (states from default_rng(1000 + i)), 10 steps, against the oracle case by case.
+  (states from default_rng(1000 + i)), 10 steps, against the oracle case by
+  case, and 300 steps (the batched configuration's) against the oracle's C
+  restatement.
 
 The kernels follow the reference's operation order, so the forward results are
 also asserted bitwise equal.  The oracle runs on the host's cores: these tests
@@ -270,3 +272,48 @@ def test_batch_with_a_512_case_against_the_oracle():
         got = batch.case_view(i).cpu()
         assert rel_err(got, refs[i]) <= 1e-10, sides[i]
         assert torch.equal(got, refs[i]), sides[i]
+
+
+def test_batch_300_steps_against_the_c_restatement():
+    """The batched configuration's step count (300 CFL steps per case, each case
+    its own time step) on cases of sides 64, 128, 192 and 512 (states from
+    default_rng(1000 + i)), against the oracle's plain-C restatement (OpenMP)
+    started from the same conservatives' primitives: every case bitwise."""
+    import ctypes
+    import __graft_entry__
+    from jaxfluids_gb300 import BatchedRK3, CaseConfig
+    so = __graft_entry__.build_oracle_c()
+    if not so:
+        pytest.skip("no C compiler for the oracle's C restatement")
+    f_c = ctypes.CDLL(so).jf_rk3_steps
+    f_c.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double)]
+    f_c.restype = ctypes.c_int
+    sides, steps = (64, 128, 192, 512), 300
+    zg = {f: "ZEROGRADIENT" for f in ("east", "west", "north", "south")}
+    cfgs = [CaseConfig(cells=(s, s, 1), bc=dict(zg)) for s in sides]
+    states = []
+    for i, s in enumerate(sides):
+        oc, _ = both((s, s, 1), "ZEROGRADIENT")
+        U, _ = O.initialize(quadrant_prims(s, s, seed=1000 + i), oc)
+        states.append(U[oc.interior()].contiguous())
+    batch = BatchedRK3(cfgs)
+    batch.set_states([u.cuda() for u in states])
+    batch.advance(steps)
+    torch.cuda.synchronize()
+    for i, s in enumerate(sides):
+        oc, _ = both((s, s, 1), "ZEROGRADIENT")
+        U = states[i].numpy().copy()
+        # the batch's first stage reads the primitives of its conservatives
+        P = O.prims_from_cons(states[i], oc.gamma).numpy().copy()
+        dx = 1.0 / s
+        t = ctypes.c_double(0.0)
+        assert f_c(U.ctypes.data, P.ctypes.data, (ctypes.c_int * 3)(s, s, 1), oc.nh,
+                   (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 0.0), dx, oc.cfl, oc.gamma, O.STENCIL_EPS, 0, 0,
+                   (ctypes.c_int * 6)(1, 1, 1, 1, 1, 1), steps, ctypes.byref(t)) == 0
+        got = batch.case_view(i).cpu()
+        assert batch.t[i].item() == t.value, s
+        assert torch.equal(got, torch.from_numpy(U)), s
+
