@@ -376,9 +376,26 @@ static void prims_from_cons(const double U[5], double P[5], double gamma) {
  * |u_i| + c, plus eps) times cfl.  *t is advanced by the dts.  Returns 0, -1
  * for a boundary type it does not fill, -2 when out of memory.
  */
+static int rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
+                     double cfl, double fixed_dt, double gamma, double eps, int mode, int riemann, const int bc[6],
+                     int steps, double* t);
+
 int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
                  double cfl, double gamma, double eps, int mode, int riemann, const int bc[6], int steps,
                  double* t) {
+  return rk3_steps(U, P, n, nh, one_dx, min_cell_size, cfl, 0.0, gamma, eps, mode, riemann, bc, steps, t);
+}
+
+/* As jf_rk3_steps with a fixed time step dt (time_control's fixed_timestep,
+   the feed-forward semantics). */
+int jf_rk3_steps_fixed_dt(double* U, double* P, const int n[3], int nh, const double one_dx[3], double dt,
+                          double gamma, double eps, int mode, int riemann, const int bc[6], int steps, double* t) {
+  return rk3_steps(U, P, n, nh, one_dx, 1.0, 1.0, dt, gamma, eps, mode, riemann, bc, steps, t);
+}
+
+static int rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
+                     double cfl, double fixed_dt, double gamma, double eps, int mode, int riemann, const int bc[6],
+                     int steps, double* t) {
   int h[3], lo[3];
   for (int a = 0; a < 3; ++a) {
     h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
@@ -418,7 +435,7 @@ int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_
         if (n[a] > 1) s = s + (fabs(P[(a + 1) * cs + o]) + c);
       if (s > amax) amax = s;
     }
-    const double dt = min_cell_size / (amax + 2.220446049250313e-16) * cfl;
+    const double dt = fixed_dt > 0.0 ? fixed_dt : min_cell_size / (amax + 2.220446049250313e-16) * cfl;
     memcpy(Un, U, 5 * cs * sizeof(double));
     for (int stage = 0; stage < 3; ++stage) {
       if (jf_rhs_weno5z(Ph, n, nh, one_dx, gamma, eps, mode, riemann, rhs) != 0) {

@@ -15,7 +15,8 @@
   initial state (WENO-Z's weights on nearly flat stencils): a one-ulp change
   of the initial rho v moves the oracle's own gradient by 1.5e-3 (max norm)
   there, while its v-field gradient moves by 1.4e-11; that part is held to
-  1e-2.
+  1e-2.  The forward run as stated (1000 fixed-dt steps) against the oracle's
+  C restatement, bitwise.
 * The same Kelvin-Helmholtz gradient as stated (1000 steps, uniform
   checkpoints every 50) against central differences in 16 random directions
   at h = 1e-6 relative.
@@ -243,6 +244,37 @@ def test_kh_512_adjoint_1000_steps_against_central_differences():
         cs.append(abs(fd - an) / float(dv.norm() * d.norm()))
     assert max(cs) <= 1e-5, cs
     assert sorted(rel)[len(rel) // 2] <= 1e-2, rel
+
+
+def test_kh_512_1000_fixed_dt_steps_against_the_c_restatement():
+    """The Kelvin-Helmholtz forward run as stated (512^2, 1000 steps at the
+    fixed CFL 0.5 time step of the initial state, feed-forward semantics)
+    through the adjoint's forward path, against the oracle's C restatement:
+    the final state bitwise equal."""
+    import ctypes
+    import __graft_entry__
+    from jaxfluids_gb300.adjoint import AdjointRK3
+    so = __graft_entry__.build_oracle_c()
+    if not so:
+        pytest.skip("no C compiler for the oracle's C restatement")
+    f_c = ctypes.CDLL(so).jf_rk3_steps_fixed_dt
+    f_c.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                    ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double)]
+    f_c.restype = ctypes.c_int
+    n, steps = 512, 1000
+    oc, cc = both((n, n, 1), "PERIODIC")
+    U0 = _kh_cons(n, 7)
+    dt = float(O.compute_dt(O.buffers_from_interior_cons(U0, oc)[1], oc))
+    UN = AdjointRK3(cc, dt=dt).advance(U0.cuda(), steps).cpu()
+    U = U0.numpy().copy()
+    P = O.prims_from_cons(U0, oc.gamma).numpy().copy()
+    t = ctypes.c_double(0.0)
+    assert f_c(U.ctypes.data, P.ctypes.data, (ctypes.c_int * 3)(n, n, 1), oc.nh,
+               (ctypes.c_double * 3)(float(n), float(n), 0.0), dt, oc.gamma, O.STENCIL_EPS, 0, 0,
+               (ctypes.c_int * 6)(0, 0, 0, 0, 0, 0), steps, ctypes.byref(t)) == 0
+    assert torch.equal(UN, torch.from_numpy(U))
 
 
 def test_batch_with_a_512_case_against_the_oracle():
