@@ -228,7 +228,8 @@ int batch_setup(const gbf_case* scheme, const gbf_batch_case* cases, int ncases,
     for (int b = 0; b < 3; ++b) ft.t[b] = p.t[b] + (b == a ? 1 : 0);
     *smem = std::max(*smem, face_smem(&rep, ft, a));
   }
-  if (*smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  // (plus the kernel's static copy of an item's parameters)
+  if (*smem + sizeof(SweepParams) > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
   BatchParams b{};
   b.base = p;
   b.cases = cases;
