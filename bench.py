@@ -34,6 +34,8 @@ sys.path.insert(0, ROOT)
 N_TGV = 128
 METRIC = "FP64 cell-updates/s (TGV 128^3, WENO5-Z+HLLC, TVD-RK3)"
 UNIT = "cell-updates/s"
+VISCOUS_METRIC = "FP64 cell-updates/s (viscous TGV {n}^3 Re 1600, WENO5-Z CHAR-ROE+HLLC+CENTRAL4, TVD-RK3)"
+VISCOUS_SCHEME = "WENO5-Z CHAR-PRIMITIVE (ROE) + HLLC/Einfeldt + CENTRAL4 viscous/heat, TVD-RK3, CFL 0.5"
 # Algorithmic HBM bytes per cell-update: stage 1 reads U^n and writes U^1
 # (80 B); stages 2 and 3 read U^k and U^n and write (120 B each) -> 320 B.
 BYTES_PER_CELL_UPDATE = 320.0
@@ -204,29 +206,41 @@ class CPortRun:
     OpenMP on every host core, contraction off; bitwise equal to the torch
     restatement) advancing the TGV n^3 workload step by step: the same initial
     condition, scheme and CFL time step as the GPU run, each face computed
-    once per stage as the reference's face arrays hold them."""
+    once per stage as the reference's face arrays hold them.  viscous: the
+    viscous TGV's scheme (CHAR-PRIMITIVE with the Roe state, HLLC, CENTRAL4
+    viscous and heat fluxes, Re 1600, Pr 0.71) and its dt limits."""
 
-    def __init__(self, n):
+    def __init__(self, n, viscous=False):
         import ctypes
         import __graft_entry__
         from oracle import jf_oracle as O
         so = __graft_entry__.build_oracle_c()
         if not so:
             raise RuntimeError("no C compiler for the oracle's C restatement")
-        f = ctypes.CDLL(so).jf_rk3_steps
-        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
-                      ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                      ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
-                      ctypes.POINTER(ctypes.c_double)]
-        f.restype = ctypes.c_int
+        lib = ctypes.CDLL(so)
+        head = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                ctypes.c_double, ctypes.c_int, ctypes.c_int]
         self.U = tgv_state(n, "cpu").numpy().copy()
         self.P = O.prims_from_cons(torch.from_numpy(self.U), 1.4).numpy().copy()
         dx = 2 * math.pi / n
         self.t = ctypes.c_double(0.0)
         self._byref = ctypes.byref
-        self.args = (self.U.ctypes.data, self.P.ctypes.data, (ctypes.c_int * 3)(n, n, n), 3,
-                     (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 1.0 / dx), dx, 0.5, 1.4, O.STENCIL_EPS,
-                     0, 0, (ctypes.c_int * 6)(0, 0, 0, 0, 0, 0))  # PRIMITIVE, HLLC, periodic
+        odx = (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 1.0 / dx)
+        if viscous:
+            cfg = viscous_tgv_config(n)
+            f = lib.jf_rk3_steps_visc
+            f.argtypes = head + [ctypes.c_double] * 5 + [ctypes.c_int] * 4 + [ctypes.POINTER(ctypes.c_double)]
+            cp = cfg.gamma / (cfg.gamma - 1.0) * cfg.R
+            self.args = (self.U.ctypes.data, self.P.ctypes.data, (ctypes.c_int * 3)(n, n, n), cfg.nh, odx, dx,
+                         cfg.cfl, cfg.gamma, O.STENCIL_EPS, 2, 0,  # CHAR-PRIMITIVE (ROE), HLLC
+                         cfg.mu, cfg.bulk_viscosity, cfg.kappa, cp, cfg.R, 1, 1, 1)
+        else:
+            f = lib.jf_rk3_steps
+            f.argtypes = head + [ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+            self.args = (self.U.ctypes.data, self.P.ctypes.data, (ctypes.c_int * 3)(n, n, n), 3, odx, dx, 0.5, 1.4,
+                         O.STENCIL_EPS, 0, 0, (ctypes.c_int * 6)(0, 0, 0, 0, 0, 0))  # PRIMITIVE, HLLC, periodic
+        f.restype = ctypes.c_int
         self.f = f
         self.cells = n ** 3
 
@@ -238,36 +252,48 @@ class CPortRun:
         return time.perf_counter() - t0
 
 
-def cpu_port(n, threads):
-    """The fastest CPU restatement available: the C one (OpenMP), else the torch one."""
+def cpu_port(n, threads, viscous=False):
+    """The fastest CPU restatement available: the C one (OpenMP), else the torch
+    one (inviscid TGV only)."""
     try:
-        return CPortRun(n), f"C, OpenMP, {threads} threads"
+        return CPortRun(n, viscous), f"C, OpenMP, {threads} threads"
     except (RuntimeError, OSError):
+        if viscous:
+            raise
         return OracleRun(n, threads), f"torch float64, {threads} threads"
 
 
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's algorithm
     (JAX is installed on neither machine, so the reference itself cannot run)
-    on the same TGV 128^3 workload, all host threads, W warm-up + K timed steps."""
+    on the same workload (TGV 128^3, or the viscous TGV 256^3 with
+    --workload viscous), all host threads, W warm-up + K timed steps."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n = args.n if args.n else N_TGV
-    run, how = cpu_port(n, threads)
+    viscous = args.workload == "viscous"
+    n = args.n if args.n else (256 if viscous else N_TGV)
+    run, how = cpu_port(n, threads, viscous)
     for _ in range(max(0, args.warmup)):
         run.step()
     total_t = sum(run.step() for _ in range(args.steps))
     value = run.cells * args.steps / total_t
-    sample = (f"TGV {n}^3, {args.warmup} warm-up + {args.steps} timed RK3 steps, CPU restatement of the "
+    name = "viscous TGV" if viscous else "TGV"
+    sample = (f"{name} {n}^3, {args.warmup} warm-up + {args.steps} timed RK3 steps, CPU restatement of the "
               f"reference ({how} on {cpu_model()}); the JAX reference is not installed")
+    if viscous:
+        metric = VISCOUS_METRIC.format(n=n)
+        config = {"workload": f"3-D viscous Taylor-Green vortex {n}^3 periodic, Re 1600, Pr 0.71, Ma 0.1",
+                  "cells": n ** 3, "scheme": VISCOUS_SCHEME}
+    else:
+        metric = METRIC
+        config = {"workload": f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4",
+                  "cells": n ** 3, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"}
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "impl": "reference", "metric": metric, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4",
-                   "cells": n ** 3, "scheme": "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"},
+        "data": "synthetic", "config": config,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                          "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -651,19 +677,18 @@ def main():
            "steps": e2e_steps}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline and not viscous:
+    if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        run, how = cpu_port(n, threads)
+        run, how = cpu_port(n, threads, viscous)
         run.step()  # warm-up
         el = sum(run.step() for _ in range(3))
         cpu = {"value": run.cells * 3 / el, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"TGV {n}^3 (the same workload), 1 warm-up + 3 timed RK3 steps ({el:.1f} s), CPU "
-                         f"restatement of the reference ({how})",
+               "sample": f"{'viscous ' if viscous else ''}TGV {n}^3 (the same workload), 1 warm-up + 3 timed RK3 "
+                         f"steps ({el:.1f} s), CPU restatement of the reference ({how})",
                "cpu_model": cpu_model()}
 
     if rank == 0:
-        metric = METRIC if not viscous else \
-            f"FP64 cell-updates/s (viscous TGV {n}^3 Re 1600, WENO5-Z CHAR-ROE+HLLC+CENTRAL4, TVD-RK3)"
+        metric = METRIC if not viscous else VISCOUS_METRIC.format(n=n)
         line = {
             "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
@@ -671,8 +696,7 @@ def main():
             "config": {"workload": (f"3-D viscous Taylor-Green vortex {n}^3 periodic, Re 1600, Pr 0.71, Ma 0.1"
                                     if viscous else f"3-D inviscid Taylor-Green vortex {n}^3 periodic, Ma 0.1, gamma 1.4"),
                        "cells": cells,
-                       "scheme": ("WENO5-Z CHAR-PRIMITIVE (ROE) + HLLC/Einfeldt + CENTRAL4 viscous/heat, TVD-RK3, CFL 0.5"
-                                  if viscous else "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"),
+                       "scheme": (VISCOUS_SCHEME if viscous else "WENO5-Z PRIMITIVE + HLLC/Einfeldt, TVD-RK3, CFL 0.5"),
                        "parallelism": f"replicas x{world}",
                        "l2": "256 MiB buffer written between timed steps (per-step CUDA events)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,

@@ -1,7 +1,8 @@
 /*
  * Test infrastructure, not product code: a second CPU restatement, in plain C,
  * of the single-phase right-hand side for WENO5-Z on primitive or characteristic
- * variables with HLLC, HLL (Einfeldt signal speeds) or Rusanov fluxes, on a
+ * variables with HLLC, HLL (Einfeldt signal speeds) or Rusanov fluxes, with
+ * CENTRAL4 viscous and heat fluxes on periodic boxes, on a
  * halo-filled primitive buffer, with its own face halos, CFL time step and
  * TVD-RK3 steps; multi-threaded with OpenMP where built with it (the CPU
  * baseline of the benchmark).  It is written independently of the torch restatement in
@@ -25,7 +26,11 @@
  *   divergence       solvers/space_solver.py:266-314, :597-599
  *   face halos       halos/outer/material.py:868-894,
  *                    halos/outer/boundary_condition.py:539-604
- *   time step        time_integration/time_step_size.py:15-157 (inviscid)
+ *   viscous, heat    solvers/source_term_solver.py:188-254, :264-350,
+ *                    :504-580; deriv_center_4.py, deriv_face_4.py, central_4.py;
+ *                    space_solver.py:565-585
+ *   time step        time_integration/time_step_size.py:15-157 (CFL, viscous
+ *                    and heat limits)
  *   TVD-RK3          time_integration/RK3.py:27-62, simulation_manager.py:670-1077
  */
 #include <math.h>
@@ -243,6 +248,148 @@ static void face_states(double w[6][5], int axis, int mode, double gamma, double
 }
 
 /*
+ * Viscous and heat fluxes with CENTRAL4 stencils on periodic axes
+ * (source_term_solver.py:188-254, :264-350, :414-448, :504-580;
+ * deriv_center_4.py:37-49, deriv_face_4.py:37-50, central_4.py:39-50), added
+ * to a face's convective flux as compute_rhs_xi does (space_solver.py:565-585:
+ * F[1:5] += -visc, then F[4] += heat).  The face-normal stencils read the
+ * face halos; the centre derivatives of the velocity are evaluated once per
+ * interior cell and read across the box's ends by the periodic wrap (the
+ * reference reads the same values from its filled edge halos).
+ */
+typedef struct {
+  int viscous, heat, heat_production;
+  double mu1, mu2, kappa, R, mu, cp;
+} Diss;
+
+typedef struct {
+  const double* P;  /* the primitive halo buffer */
+  size_t hcs, cs;
+  int n[3], h[3], lo[3];
+  double* dc[3][3]; /* dc[i][a]: d u_a / d x_i at the interior cell centres, i active */
+} DissCells;
+
+/* primitive v of interior-relative cell g (coordinates -nh .. n + nh - 1 on active axes) */
+static double hget(const DissCells* b, int v, const int g[3]) {
+  return b->P[v * b->hcs + ((size_t)(g[0] + b->lo[0]) * b->h[1] + (g[1] + b->lo[1])) * b->h[2] + (g[2] + b->lo[2])];
+}
+
+static double c4_center(double odx, double m2, double m1, double p1, double p2) {
+  return odx * (1.0 / 12.0 * (m2 - p2) + 8.0 / 12.0 * (p1 - m1));
+}
+static double c4_face_deriv(double odx, double m2, double m1, double c0, double p1) {
+  return odx * (1.0 / 24.0 * (m2 - p1) + 27.0 / 24.0 * (c0 - m1));
+}
+static double c4_face_interp(double m2, double m1, double c0, double p1) {
+  return -1.0 / 16.0 * (m2 + p1) + 9.0 / 16.0 * (m1 + c0);
+}
+
+/* the centre derivatives of every interior cell (viscous cases); 0 or -2 */
+static int diss_cells_init(DissCells* b, const Diss* d, const double one_dx[3]) {
+  memset(b->dc, 0, sizeof(b->dc));
+  if (!d->viscous) return 0;
+  for (int i = 0; i < 3; ++i) {
+    if (b->n[i] <= 1) continue;
+    for (int a = 0; a < 3; ++a) {
+      b->dc[i][a] = (double*)malloc(b->cs * sizeof(double));
+      if (!b->dc[i][a]) return -2;
+    }
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (b->n[i] <= 1) continue;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i0 = 0; i0 < b->n[0]; ++i0)
+      for (int i1 = 0; i1 < b->n[1]; ++i1)
+        for (int i2 = 0; i2 < b->n[2]; ++i2) {
+          const size_t o = ((size_t)i0 * b->n[1] + i1) * b->n[2] + i2;
+          for (int a = 0; a < 3; ++a) {
+            double u[5];
+            for (int k = -2; k <= 2; ++k) {
+              int g[3] = {i0, i1, i2};
+              g[i] += k;
+              u[k + 2] = hget(b, 1 + a, g);
+            }
+            b->dc[i][a][o] = c4_center(one_dx[i], u[0], u[1], u[3], u[4]);
+          }
+        }
+  }
+  return 0;
+}
+
+static void diss_cells_free(DissCells* b) {
+  for (int i = 0; i < 3; ++i)
+    for (int a = 0; a < 3; ++a) free(b->dc[i][a]);
+}
+
+static void add_dissipative(const DissCells* b, const Diss* d, const int q[3], int ax, const double one_dx[3],
+                            double F[5]) {
+  const int* n = b->n;
+  const double odx = one_dx[ax];
+  /* the four cells q - 2 .. q + 1 along ax of face q */
+  int g[4][3];
+  size_t wo[4];
+  for (int k = 0; k < 4; ++k) {
+    g[k][0] = q[0];
+    g[k][1] = q[1];
+    g[k][2] = q[2];
+    g[k][ax] += k - 2;
+    int x = g[k][ax];
+    x = x < 0 ? x + n[ax] : (x >= n[ax] ? x - n[ax] : x);
+    int w[3] = {g[k][0], g[k][1], g[k][2]};
+    w[ax] = x;
+    wo[k] = ((size_t)w[0] * n[1] + w[1]) * n[2] + w[2];
+  }
+  if (d->viscous) {
+    double vel[3][4];
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 4; ++k) vel[a][k] = hget(b, 1 + a, g[k]);
+    double gr[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int a = 0; a < 3; ++a) gr[a][ax] = c4_face_deriv(odx, vel[a][0], vel[a][1], vel[a][2], vel[a][3]);
+    for (int i = 0; i < 3; ++i) {
+      if (i == ax || n[i] <= 1) continue;
+      for (int which = 0; which < 2; ++which) {
+        const int a = which == 0 ? ax : i;
+        const double* dc = b->dc[i][a];
+        gr[a][i] = c4_face_interp(dc[wo[0]], dc[wo[1]], dc[wo[2]], dc[wo[3]]);
+      }
+    }
+    double tau[3];
+    for (int k = 0; k < 3; ++k) tau[k] = n[k] > 1 ? d->mu1 * (gr[ax][k] + gr[k][ax]) : 0.0;
+    double tr = 0.0;
+    int first = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (n[k] <= 1) continue;
+      tr = first ? gr[k][k] : tr + gr[k][k];
+      first = 0;
+    }
+    tau[ax] = tau[ax] + d->mu2 * tr;
+    double vt = 0.0;
+    if (d->heat_production) {
+      first = 1;
+      for (int k = 0; k < 3; ++k) {
+        if (n[k] <= 1) continue;
+        const double vf = c4_face_interp(vel[k][0], vel[k][1], vel[k][2], vel[k][3]);
+        vt = first ? tau[k] * vf : vt + tau[k] * vf;
+        first = 0;
+      }
+    }
+    for (int k = 0; k < 3; ++k) F[1 + k] = F[1 + k] + -tau[k];
+    F[4] = F[4] + -vt;
+  }
+  if (d->heat) {
+    double T[4];
+    for (int k = 0; k < 4; ++k) T[k] = hget(b, 4, g[k]) / (hget(b, 0, g[k]) * d->R);
+    const double dT = c4_face_deriv(odx, T[0], T[1], T[2], T[3]);
+    F[4] = F[4] + -d->kappa * dT;
+  }
+}
+
+static int rhs_impl(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
+                    int mode, int riemann, const Diss* diss, double* rhs);
+
+/*
  * rhs[5][n0][n1][n2] of the primitive halo buffer P[5][h0][h1][h2]
  * (h_a = n_a + 2 nh on active axes, 1 on inactive ones), axes summed in order
  * from the first active one; mode as face_states, riemann as riemann_flux.
@@ -250,6 +397,21 @@ static void face_states(double w[6][5], int axis, int mode, double gamma, double
  */
 int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
                   int mode, int riemann, double* rhs) {
+  return rhs_impl(P, n, nh, one_dx, gamma, eps, mode, riemann, NULL, rhs);
+}
+
+/* As jf_rhs_weno5z with CENTRAL4 viscous (viscous != 0) and heat (heat != 0)
+   fluxes on a periodic box: mu, bulk viscosity, kappa, cp and R of the
+   material, heat_production as is_viscous_heat_production. */
+int jf_rhs_weno5z_visc(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
+                       int mode, int riemann, double mu, double bulk, double kappa, double cp, double R,
+                       int viscous, int heat, int heat_production, double* rhs) {
+  const Diss d = {viscous, heat, heat_production, mu, bulk - 2.0 / 3.0 * mu, kappa, R, mu, cp};
+  return rhs_impl(P, n, nh, one_dx, gamma, eps, mode, riemann, &d, rhs);
+}
+
+static int rhs_impl(const double* P, const int n[3], int nh, const double one_dx[3], double gamma, double eps,
+                    int mode, int riemann, const Diss* diss, double* rhs) {
   int h[3], lo[3];
   for (int a = 0; a < 3; ++a) {
     h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
@@ -257,6 +419,11 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
   }
   const size_t hcs = (size_t)h[0] * h[1] * h[2];
   const size_t cs = (size_t)n[0] * n[1] * n[2];
+  DissCells db = {P, hcs, cs, {n[0], n[1], n[2]}, {h[0], h[1], h[2]}, {lo[0], lo[1], lo[2]}, {{0}}};
+  if (diss && diss_cells_init(&db, diss, one_dx) != 0) {
+    diss_cells_free(&db);
+    return -2;
+  }
   int first = 1;
   for (int a = 0; a < 3; ++a) {
     if (n[a] <= 1) continue;
@@ -267,7 +434,10 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
     e[a] = n[a] + 1;
     const size_t nfaces = (size_t)e[0] * e[1] * e[2];
     double* F = (double*)malloc(5 * nfaces * sizeof(double));
-    if (!F) return -2;
+    if (!F) {
+      if (diss) diss_cells_free(&db);
+      return -2;
+    }
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -281,6 +451,10 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
             for (int k = 0; k < 6; ++k) w[k][v] = P[v * hcs + c0 + (ptrdiff_t)(k - 3) * (ptrdiff_t)stride];
           face_states(w, a, mode, gamma, eps, PL, PR);
           riemann_flux(PL, PR, a + 1, gamma, riemann, Ff);
+          if (diss) {
+            const int q[3] = {i0, i1, i2};
+            add_dissipative(&db, diss, q, a, one_dx, Ff);
+          }
           const size_t o = ((size_t)i0 * e[1] + i1) * e[2] + i2;
           for (int v = 0; v < 5; ++v) F[v * nfaces + o] = Ff[v];
         }
@@ -301,6 +475,7 @@ int jf_rhs_weno5z(const double* P, const int n[3], int nh, const double one_dx[3
     free(F);
     first = 0;
   }
+  if (diss) diss_cells_free(&db);
   return 0;
 }
 
@@ -378,24 +553,37 @@ static void prims_from_cons(const double U[5], double P[5], double gamma) {
  */
 static int rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
                      double cfl, double fixed_dt, double gamma, double eps, int mode, int riemann, const int bc[6],
-                     int steps, double* t);
+                     const Diss* diss, int steps, double* t);
 
 int jf_rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
                  double cfl, double gamma, double eps, int mode, int riemann, const int bc[6], int steps,
                  double* t) {
-  return rk3_steps(U, P, n, nh, one_dx, min_cell_size, cfl, 0.0, gamma, eps, mode, riemann, bc, steps, t);
+  return rk3_steps(U, P, n, nh, one_dx, min_cell_size, cfl, 0.0, gamma, eps, mode, riemann, bc, NULL, steps, t);
+}
+
+/* As jf_rk3_steps with CENTRAL4 viscous and heat fluxes (as
+   jf_rhs_weno5z_visc; every face PERIODIC) and their time-step limits
+   (time_step_size.py:111-150). */
+int jf_rk3_steps_visc(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
+                      double cfl, double gamma, double eps, int mode, int riemann, double mu, double bulk,
+                      double kappa, double cp, double R, int viscous, int heat, int heat_production, int steps,
+                      double* t) {
+  static const int kPeriodic[6] = {0, 0, 0, 0, 0, 0};
+  const Diss d = {viscous, heat, heat_production, mu, bulk - 2.0 / 3.0 * mu, kappa, R, mu, cp};
+  return rk3_steps(U, P, n, nh, one_dx, min_cell_size, cfl, 0.0, gamma, eps, mode, riemann, kPeriodic, &d, steps,
+                   t);
 }
 
 /* As jf_rk3_steps with a fixed time step dt (time_control's fixed_timestep,
    the feed-forward semantics). */
 int jf_rk3_steps_fixed_dt(double* U, double* P, const int n[3], int nh, const double one_dx[3], double dt,
                           double gamma, double eps, int mode, int riemann, const int bc[6], int steps, double* t) {
-  return rk3_steps(U, P, n, nh, one_dx, 1.0, 1.0, dt, gamma, eps, mode, riemann, bc, steps, t);
+  return rk3_steps(U, P, n, nh, one_dx, 1.0, 1.0, dt, gamma, eps, mode, riemann, bc, NULL, steps, t);
 }
 
 static int rk3_steps(double* U, double* P, const int n[3], int nh, const double one_dx[3], double min_cell_size,
                      double cfl, double fixed_dt, double gamma, double eps, int mode, int riemann, const int bc[6],
-                     int steps, double* t) {
+                     const Diss* diss, int steps, double* t) {
   int h[3], lo[3];
   for (int a = 0; a < 3; ++a) {
     h[a] = n[a] > 1 ? n[a] + 2 * nh : 1;
@@ -435,10 +623,37 @@ static int rk3_steps(double* U, double* P, const int n[3], int nh, const double 
         if (n[a] > 1) s = s + (fabs(P[(a + 1) * cs + o]) + c);
       if (s > amax) amax = s;
     }
-    const double dt = fixed_dt > 0.0 ? fixed_dt : min_cell_size / (amax + 2.220446049250313e-16) * cfl;
+    double dt = min_cell_size / (amax + 2.220446049250313e-16);
+    if (diss && diss->viscous) {
+      /* nu = mu / rho, dt_v = (3/14) dx^2 / (max nu + eps) */
+      double numax = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : numax)
+#endif
+      for (size_t o = 0; o < cs; ++o) {
+        const double nu = diss->mu / P[o];
+        if (nu > numax) numax = nu;
+      }
+      const double dt_v = 3.0 / 14.0 * (min_cell_size * min_cell_size) / (numax + 2.220446049250313e-16);
+      if (dt_v < dt) dt = dt_v;
+    }
+    if (diss && diss->heat) {
+      /* alpha = kappa / (rho cp), dt_h = 0.1 dx^2 / (max alpha + eps) */
+      double amx = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : amx)
+#endif
+      for (size_t o = 0; o < cs; ++o) {
+        const double al = diss->kappa / (P[o] * diss->cp);
+        if (al > amx) amx = al;
+      }
+      const double dt_h = 0.1 * (min_cell_size * min_cell_size) / (amx + 2.220446049250313e-16);
+      if (dt_h < dt) dt = dt_h;
+    }
+    dt = fixed_dt > 0.0 ? fixed_dt : dt * cfl;
     memcpy(Un, U, 5 * cs * sizeof(double));
     for (int stage = 0; stage < 3; ++stage) {
-      if (jf_rhs_weno5z(Ph, n, nh, one_dx, gamma, eps, mode, riemann, rhs) != 0) {
+      if (rhs_impl(Ph, n, nh, one_dx, gamma, eps, mode, riemann, diss, rhs) != 0) {
         st = -2;
         break;
       }

@@ -6,7 +6,8 @@
   oracle's C restatement.
 * Viscous TGV 256^3 (Re 1600, Pr 0.71, WENO5-Z on Roe-characteristic variables
   + HLLC + CENTRAL4 viscous and heat fluxes): one right-hand side and one fused
-  step.
+  step against the torch oracle, and 30 CFL steps against the oracle's C
+  restatement.
 * Kelvin-Helmholtz 512^2 (periodic, noise from default_rng(7)): the
   right-hand-side VJP against the oracle's autograd (<= 1e-11) and a 5-step
   fixed-dt gradient of 1/2 ||rho(T) - rho_target||^2 with respect to the
@@ -140,6 +141,48 @@ def test_viscous_tgv_256_char_roe_rhs_and_one_step():
     oc, cc = both((256, 256, 256), "PERIODIC", ranges=TWO_PI, nh=4, recon_var="CHAR-PRIMITIVE",
                   frozen_state="ROE", viscous=True, heat=True, mu=1.0 / 1600, prandtl=0.71)
     _rhs_and_steps(oc, cc, tgv_prims(256), 1)
+
+
+def test_viscous_tgv_256_30_steps_against_the_c_restatement():
+    """The viscous TGV at its stated size (256^3, Re 1600, Pr 0.71, CHAR-ROE
+    WENO5-Z + HLLC + CENTRAL4 viscous and heat fluxes, CFL 0.5 with the
+    viscous and heat limits): 30 steps of the fused path against the oracle's
+    C restatement (bitwise equal to the torch oracle, tests/test_oracle_c.py;
+    OpenMP on the host's cores, a few minutes): final conservatives and time
+    bitwise equal."""
+    import ctypes
+    import __graft_entry__
+    from jaxfluids_gb300 import FusedRK3
+    so = __graft_entry__.build_oracle_c()
+    if not so:
+        pytest.skip("no C compiler for the oracle's C restatement")
+    f_c = ctypes.CDLL(so).jf_rk3_steps_visc
+    f_c.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                    ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                    ctypes.c_double, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int] * 4 + \
+        [ctypes.POINTER(ctypes.c_double)]
+    f_c.restype = ctypes.c_int
+    n, steps = 256, 30
+    oc, cc = both((n, n, n), "PERIODIC", ranges=TWO_PI, nh=4, recon_var="CHAR-PRIMITIVE",
+                  frozen_state="ROE", viscous=True, heat=True, mu=1.0 / 1600, prandtl=0.71)
+    P0 = tgv_prims(n).contiguous()
+    U0 = O.cons_from_prims(P0, oc.gamma).contiguous()
+    f = FusedRK3(cc)
+    f.set_state(U0.cuda(), prims=P0.cuda())
+    f.advance(steps)
+    cons = f.cons.cpu()
+    t_gpu = float(f.t)
+    del f
+    U = U0.numpy().copy()
+    P = P0.numpy().copy()
+    dx = 2 * math.pi / n
+    t = ctypes.c_double(0.0)
+    assert f_c(U.ctypes.data, P.ctypes.data, (ctypes.c_int * 3)(n, n, n), oc.nh,
+               (ctypes.c_double * 3)(1.0 / dx, 1.0 / dx, 1.0 / dx), dx, oc.cfl, oc.gamma, O.STENCIL_EPS, 2, 0,
+               oc.mu, oc.bulk_viscosity, oc.kappa(), oc.cp(), oc.R, 1, 1, 1, steps, ctypes.byref(t)) == 0
+    assert t_gpu == t.value
+    assert rel_err(cons, torch.from_numpy(U)) <= 1e-10
+    assert torch.equal(cons, torch.from_numpy(U))
 
 
 def _kh_cons(n, seed):

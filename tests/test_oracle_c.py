@@ -2,7 +2,9 @@
 right-hand side (oracle/jf_rhs.c: WENO5-Z on primitives or on their
 characteristic variables with the ARITHMETIC or ROE frozen state, HLLC with
 Einfeldt speeds, HLL or Rusanov) against the torch oracle, on periodic, zero-gradient and symmetry
-halos in 1-D to 3-D, each side filling its own halos from the same interior.
+halos in 1-D to 3-D, each side filling its own halos from the same interior;
+and with CENTRAL4 viscous and heat fluxes on periodic boxes, the right-hand
+side and RK3 steps under each of the three time-step limits.
 Built here with the system C compiler, contraction off."""
 import ctypes
 import os
@@ -183,3 +185,87 @@ def test_c_and_torch_oracles_agree_on_sod_200_to_end_time(crhs):
              ctypes.c_int(steps), ctypes.byref(tc)) == 0
     assert steps > 50 and tc.value == t
     assert torch.equal(torch.from_numpy(Uc), U[inner])
+
+
+VISC_CASES = [("tgv-3d", (12, 10, 8)), ("tgv-2d", (16, 12, 1))]
+DISS = {"visc-heat": dict(viscous=True, heat=True), "visc": dict(viscous=True, heat=False),
+        "heat": dict(viscous=False, heat=True),
+        "visc-heat-noproduction": dict(viscous=True, heat=True, viscous_heat_production=False)}
+
+
+def _visc_args(oc):
+    return (oc.mu, oc.bulk_viscosity, oc.kappa(), oc.cp(), oc.R, int(oc.viscous), int(oc.heat),
+            int(oc.viscous_heat_production))
+
+
+def _rough_tgv(cells, seed):
+    prims = tgv_prims(max(cells))[:, :cells[0], :cells[1], :cells[2]].contiguous().clone()
+    rng = np.random.default_rng(seed)
+    # relative noise: density and pressure stay positive
+    return prims * (1.0 + torch.from_numpy(0.05 * rng.uniform(-1.0, 1.0, prims.shape)))
+
+
+@pytest.mark.parametrize("diss", list(DISS))
+@pytest.mark.parametrize("mode", [0, 2], ids=["primitive", "char-roe"])
+@pytest.mark.parametrize("name,cells", VISC_CASES, ids=[c[0] for c in VISC_CASES])
+def test_c_viscous_rhs_matches_torch_oracle(name, cells, mode, diss):
+    """CENTRAL4 viscous and heat fluxes on a periodic box, added to the
+    WENO5-Z + HLLC flux of every face: the C right-hand side equals the torch
+    oracle's bitwise."""
+    import __graft_entry__
+    f = ctypes.CDLL(__graft_entry__.build_oracle_c()).jf_rhs_weno5z_visc
+    f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                  ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 5 + \
+        [ctypes.c_int] * 3 + [ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    oc, _ = both(cells, "PERIODIC", nh=4, riemann="HLLC", mu=0.01, bulk_viscosity=0.003, prandtl=0.72, **MODES[mode],
+                 **DISS[diss])
+    U, P = O.initialize(_rough_tgv(cells, 7), oc)
+    ref = O.compute_rhs(U, P, oc)
+    Pn = np.ascontiguousarray(P.numpy())
+    out = np.empty(ref.shape, dtype=np.float64)
+    odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
+    assert f(Pn.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, 0,
+             *_visc_args(oc), out.ctypes.data) == 0
+    assert torch.equal(torch.from_numpy(out), ref)
+
+
+@pytest.mark.parametrize("limit,mu,heat", [("heat", 0.5, True), ("viscous", 1.0, False), ("cfl", 0.05, True)])
+@pytest.mark.parametrize("mode", [0, 2], ids=["primitive", "char-roe"])
+def test_c_viscous_rk3_steps_match_torch_oracle(mode, limit, mu, heat):
+    """CFL, viscous and heat time-step limits (mu chosen so that `limit`
+    decides dt), three stages: the C steps equal the torch oracle's bitwise
+    (states and time)."""
+    import __graft_entry__
+    f = ctypes.CDLL(__graft_entry__.build_oracle_c()).jf_rk3_steps_visc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_double, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int] * 4 + \
+        [ctypes.POINTER(ctypes.c_double)]
+    f.restype = ctypes.c_int
+    cells = (12, 10, 8)
+    oc, _ = both(cells, "PERIODIC", nh=4, riemann="HLLC", mu=mu, prandtl=0.72, viscous=True, heat=heat, cfl=0.5,
+                 **MODES[mode])
+    U, P = O.initialize(_rough_tgv(cells, 11), oc)
+    Pi = P[oc.interior()]
+    c = O.speed_of_sound(Pi[4], Pi[0], oc.gamma)
+    dts = {"cfl": O.rdiv(oc.min_cell_size, (sum(torch.abs(Pi[i + 1]) + c for i in range(3))).max() + O.EPS),
+           "viscous": O.rdiv(3.0 / 14.0 * oc.min_cell_size ** 2, O.rdiv(oc.mu, Pi[0]).max() + O.EPS)}
+    if heat:
+        dts["heat"] = O.rdiv(0.1 * oc.min_cell_size ** 2, O.rdiv(oc.kappa(), Pi[0] * oc.cp()).max() + O.EPS)
+    assert min(dts, key=lambda k: dts[k].item()) == limit
+    inner = oc.interior()
+    Uc = np.ascontiguousarray(U[inner].numpy())
+    Pc = np.ascontiguousarray(P[inner].numpy())
+    t, steps = 0.0, 3
+    for _ in range(steps):
+        dt = O.compute_dt(P, oc)
+        U, P = O.rk3_step(U, P, dt, oc)
+        t += dt.item()
+    tc = ctypes.c_double(0.0)
+    odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) for a in range(3)])
+    assert f(Uc.ctypes.data, Pc.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, odx, oc.min_cell_size, oc.cfl,
+             oc.gamma, O.STENCIL_EPS, mode, 0, *_visc_args(oc), steps, ctypes.byref(tc)) == 0
+    assert tc.value == t
+    assert torch.equal(torch.from_numpy(Uc), U[inner])
+    assert torch.equal(torch.from_numpy(Pc), P[inner])
