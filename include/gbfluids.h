@@ -63,9 +63,10 @@ extern "C" {
 #define GBF_RIEMANN_HLL 2     /* riemann_solvers/HLL.py */
 /* riemann_solvers/LaxFriedrichs.py: Rusanov's flux with one dissipation speed
  * per axis, the maximum of |u| + c over every reconstructed face state of the
- * axis (reduced by an extra reconstruction pass; the pass's scratch is a
- * per-device array, so Lax-Friedrichs evaluations on concurrent streams of one
- * device must not overlap) */
+ * axis (reduced by an extra reconstruction pass into the caller's workspace:
+ * gbf_rhs_ws, the fused steps and the adjoint; gbf_rhs and gbf_rhs_cons, which
+ * take none, use a per-device array, so their Lax-Friedrichs evaluations on
+ * concurrent streams of one device must not overlap) */
 #define GBF_RIEMANN_LAXFRIEDRICHS 3
 
 /* signal_speed (solvers/riemann_solvers/__init__.py:27) */
@@ -211,6 +212,16 @@ int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile*
  * (gbf_rhs returns GBF_ERR_INVALID_ARGUMENT for them); read by no other case. */
 int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
                  void* stream);
+
+/* As gbf_rhs_cons (cons may be null for the reconstructions that do not read
+ * it) with a caller workspace of gbf_rhs_workspace_bytes(c) bytes of device
+ * memory, 8-byte aligned: Lax-Friedrichs keeps its three axis speeds there
+ * instead of in the per-device slots, so evaluations on concurrent streams,
+ * each with its own workspace, share no state.  0 bytes (workspace may be
+ * null) for every other scheme, and for an invalid case. */
+size_t gbf_rhs_workspace_bytes(const gbf_case* c);
+int gbf_rhs_ws(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
+               void* workspace, void* stream);
 
 /*
  * Face halos (and, for viscous cases, edge halos) of the primitive buffer and,

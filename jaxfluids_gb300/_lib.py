@@ -36,7 +36,8 @@ FLAG_INTERPOLATION_LIMITER, FLAG_LIMIT_VELOCITY, FLAG_GRAVITY = 16, 32, 64
 
 # every symbol include/gbfluids.h declares
 EXPORTS = (
-    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_rhs_cons", "gbf_halo_fill", "gbf_volume_force",
+    "gbf_abi_version", "gbf_last_status", "gbf_status_string", "gbf_case_check", "gbf_rhs", "gbf_rhs_cons",
+    "gbf_rhs_workspace_bytes", "gbf_rhs_ws", "gbf_halo_fill", "gbf_volume_force",
     "gbf_prims_from_cons", "gbf_cons_from_prims", "gbf_stage_integrate",
     "gbf_dt_workspace_bytes", "gbf_dt", "gbf_rk3_workspace_bytes", "gbf_rk3_init",
     "gbf_rk3_advance", "gbf_rk3_advance_noalloc",
@@ -111,6 +112,8 @@ def load() -> ctypes.CDLL:
         "gbf_case_check": (I, [C]),
         "gbf_rhs": (I, [C, P, P, T, P]),
         "gbf_rhs_cons": (I, [C, P, P, P, T, P]),
+        "gbf_rhs_workspace_bytes": (ctypes.c_size_t, [C]),
+        "gbf_rhs_ws": (I, [C, P, P, P, T, P, P]),
         "gbf_halo_fill": (I, [C, P, P, P]),
         "gbf_volume_force": (I, [C, P, P, P]),
         "gbf_prims_from_cons": (I, [C, P, P, ctypes.c_int64, P]),

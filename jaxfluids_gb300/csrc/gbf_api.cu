@@ -199,33 +199,16 @@ int gbf_case_check(const gbf_case* c) {
 }
 
 
-static int gbf_rhs_impl(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
+// The drop-in right-hand side: cons is read by the conservative
+// reconstructions only (required there, ignored elsewhere); ws holds the
+// Lax-Friedrichs speeds (null: the per-device slots).
+static int rhs_common(const gbf_case* c, const double* prims, const double* cons, bool cons_given, double* rhs,
+                      const gbf_tile* tile, double* ws, void* stream) {
   CaseInfo ci;
   int st = check_case(c, &ci);
   if (st != GBF_OK) return st;
-  if (!prims || !rhs) return GBF_ERR_INVALID_ARGUMENT;
-  if (!aligned8(prims) || !aligned8(rhs)) return GBF_ERR_ALIGNMENT;
-  SweepParams p;
-  int threads;
-  size_t smem;
-  st = make_sweep_params(c, ci, tile, &p, &threads, &smem);
-  if (st != GBF_OK) return st;
-  p.prims_halo = prims;
-  p.out = rhs;
-  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS);
-}
-
-int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
-  return record_status(gbf_rhs_impl(c, prims, rhs, tile, stream));
-}
-
-static int gbf_rhs_cons_impl(const gbf_case* c, const double* prims, const double* cons, double* rhs,
-                             const gbf_tile* tile, void* stream) {
-  CaseInfo ci;
-  int st = check_case(c, &ci);
-  if (st != GBF_OK) return st;
-  if (!prims || !rhs || !cons) return GBF_ERR_INVALID_ARGUMENT;
-  if (!aligned8(prims) || !aligned8(rhs) || !aligned8(cons)) return GBF_ERR_ALIGNMENT;
+  if (!prims || !rhs || (cons_given && !cons)) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(prims) || !aligned8(rhs) || (cons && !aligned8(cons))) return GBF_ERR_ALIGNMENT;
   SweepParams p;
   int threads;
   size_t smem;
@@ -234,12 +217,36 @@ static int gbf_rhs_cons_impl(const gbf_case* c, const double* prims, const doubl
   p.prims_halo = prims;
   p.cons_halo = cons;
   p.out = rhs;
-  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS);
+  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS, ws);
+}
+
+int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
+  return record_status(rhs_common(c, prims, nullptr, false, rhs, tile, nullptr, stream));
 }
 
 int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
                  void* stream) {
-  return record_status(gbf_rhs_cons_impl(c, prims, cons, rhs, tile, stream));
+  return record_status(rhs_common(c, prims, cons, true, rhs, tile, nullptr, stream));
+}
+
+size_t gbf_rhs_workspace_bytes(const gbf_case* c) {
+  CaseInfo ci;
+  if (check_case(c, &ci) != GBF_OK) return 0;
+  const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+  return lf ? 4 * sizeof(double) : 0;
+}
+
+static int gbf_rhs_ws_impl(const gbf_case* c, const double* prims, const double* cons, double* rhs,
+                           const gbf_tile* tile, void* workspace, void* stream) {
+  const size_t need = gbf_rhs_workspace_bytes(c);
+  if (need && !workspace) return GBF_ERR_INVALID_ARGUMENT;
+  if (need && !aligned8(workspace)) return GBF_ERR_ALIGNMENT;
+  return rhs_common(c, prims, cons, false, rhs, tile, need ? static_cast<double*>(workspace) : nullptr, stream);
+}
+
+int gbf_rhs_ws(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
+               void* workspace, void* stream) {
+  return record_status(gbf_rhs_ws_impl(c, prims, cons, rhs, tile, workspace, stream));
 }
 
 static int gbf_volume_force_impl(const gbf_case* c, const double* cons, double* rhs, void* stream) {

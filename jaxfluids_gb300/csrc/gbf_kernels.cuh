@@ -39,9 +39,10 @@ void fill_bc_fields(const gbf_case* c, BcFields* bf);
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
                       int* threads, size_t* smem, bool for_vjp = false);
 
-// launch the sweep kernel instantiation for (recon, riemann, mode)
+// launch the sweep kernel instantiation for (recon, riemann, mode); lf_ws:
+// the three Lax-Friedrichs axis speeds (null: the per-device slots)
 int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem,
-                 cudaStream_t s, int mode);
+                 cudaStream_t s, int mode, double* lf_ws = nullptr);
 
 // The Lax-Friedrichs speed slots of the current device (gbf_sweep.cu).
 int lf_alpha_on_current_device(double** out);

@@ -184,14 +184,15 @@ int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, s
 }  // namespace
 
 // Lax-Friedrichs (LaxFriedrichs.py:25-47) runs the Rusanov instantiation twice:
-// a pass reducing the axis' max |u| + c over the face states, then the flux
-// pass with that speed.
-int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s, int mode) {
+// a pass reducing the axis' max |u| + c over the face states (into lf_ws, or
+// the per-device slots), then the flux pass with that speed.
+int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s, int mode,
+                 double* lf_ws) {
   if (c->riemann != GBF_RIEMANN_LAXFRIEDRICHS || (c->flags & GBF_FLAG_NO_CONVECTIVE))
     return launch_sweep_schemes(c, p, threads, smem, s, mode);
-  double* alpha = nullptr;
-  int st = lf_alpha_on_current_device(&alpha);
-  if (st != GBF_OK) return st;
+  double* alpha = lf_ws;
+  int st = GBF_OK;
+  if (!alpha && (st = lf_alpha_on_current_device(&alpha)) != GBF_OK) return st;
   if (cudaMemsetAsync(alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
   SweepParams q = p;
   q.lf_alpha = alpha;

@@ -47,12 +47,17 @@ int copy_if_distinct(const void* in, void* out, size_t bytes, cudaStream_t s) {
 }
 
 // compute_rhs: halo buffers of the primitives and conservatives in, interior
-// right-hand side out; the volume force (gravity) added when the case has it.
+// right-hand side out (and a workspace of gbf_rhs_workspace_bytes(c) bytes,
+// at least one); the volume force (gravity) added when the case has it.
 ffi::Error RhsImpl(cudaStream_t stream, ffi::Buffer<ffi::F64> prims, ffi::Buffer<ffi::F64> cons,
-                   ffi::ResultBuffer<ffi::F64> rhs, ffi::Span<const int64_t> desc) {
+                   ffi::ResultBuffer<ffi::F64> rhs, ffi::ResultBuffer<ffi::U8> workspace,
+                   ffi::Span<const int64_t> desc) {
   gbf_case c;
   int st = unpack(desc, &c);
-  if (st == GBF_OK) st = gbf_rhs_cons(&c, prims.typed_data(), cons.typed_data(), rhs->typed_data(), nullptr, stream);
+  if (st == GBF_OK && workspace->size_bytes() < gbf_rhs_workspace_bytes(&c)) st = GBF_ERR_SIZE;
+  if (st == GBF_OK)
+    st = gbf_rhs_ws(&c, prims.typed_data(), cons.typed_data(), rhs->typed_data(), nullptr,
+                    workspace->untyped_data(), stream);
   if (st == GBF_OK && (c.flags & GBF_FLAG_GRAVITY))
     st = gbf_volume_force(&c, cons.typed_data(), rhs->typed_data(), stream);
   return status_error(st);
@@ -122,6 +127,7 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(gbf_rhs_ffi, RhsImpl,
                                   .Arg<ffi::Buffer<ffi::F64>>()   // primitives, halo buffer
                                   .Arg<ffi::Buffer<ffi::F64>>()   // conservatives, halo buffer
                                   .Ret<ffi::Buffer<ffi::F64>>()   // rhs, interior
+                                  .Ret<ffi::Buffer<ffi::U8>>()    // workspace
                                   .Attr<ffi::Span<const int64_t>>("desc"));
 
 XLA_FFI_DEFINE_HANDLER_SYMBOL(gbf_rk3_init_ffi, Rk3InitImpl,

@@ -236,7 +236,9 @@ def space_solver_class():
                                                            numerical_setup, halo_manager, gravity)
             if self.gb300_config.time_varying_faces:
                 raise NotImplementedError("boundary values varying in time are not on the FFI path")
-            self.gb300_desc = pack_case(self.gb300_config.to_c())
+            c = self.gb300_config.to_c()
+            self.gb300_desc = pack_case(c)
+            self.gb300_ws_bytes = max(1, int(_lib.load().gbf_rhs_workspace_bytes(ctypes.byref(c))))
 
         def compute_rhs(self, conservatives, primitives, temperature, physical_simulation_time,
                         physical_timestep_size, levelset=None, volume_fraction=None, apertures=None,
@@ -251,7 +253,8 @@ def space_solver_class():
             import jax.numpy as jnp
             register_ffi_targets()
             shape = (5,) + tuple(int(n) for n in self.domain_information.device_number_of_cells)
-            rhs = jax.ffi.ffi_call("gbf_rhs", jax.ShapeDtypeStruct(shape, jnp.float64))(
+            rhs, _ = jax.ffi.ffi_call("gbf_rhs", (jax.ShapeDtypeStruct(shape, jnp.float64),
+                                                  jax.ShapeDtypeStruct((self.gb300_ws_bytes,), jnp.uint8)))(
                 primitives, conservatives, desc=self.gb300_desc)
             return (IntegrationBuffers(EulerIntegrationBuffers(rhs, None, None, None)),
                     PositivityCounter(None, None, None, None, None), DiscretizationCounter(None, None))

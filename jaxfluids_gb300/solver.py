@@ -147,8 +147,13 @@ class SpaceSolver(_Base):
         shape = self.config.halo_shape()
         rhs = torch.empty(self.config.interior_shape(), dtype=torch.float64, device=primitives.device)
         tile = ctypes.byref(self.tile) if self.tile is not None else None
-        _lib.check(self.lib.gbf_rhs_cons(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
-                                         _ptr(conservatives, shape, "conservatives"), _ptr(rhs), tile, _stream()),
+        # Lax-Friedrichs' axis speeds: a workspace per call from torch's
+        # stream-ordered allocator, so calls on concurrent streams share none
+        nws = int(self.lib.gbf_rhs_workspace_bytes(ctypes.byref(self.case)))
+        ws = torch.empty(max(1, nws // 8), dtype=torch.float64, device=primitives.device) if nws else None
+        _lib.check(self.lib.gbf_rhs_ws(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
+                                       _ptr(conservatives, shape, "conservatives") if conservatives is not None
+                                       else None, _ptr(rhs), tile, _ptr(ws) if ws is not None else None, _stream()),
                    "compute_rhs")
         if self.config.gravity is not None:
             # volume forces from the conservatives (space_solver.py:377-384)

@@ -123,3 +123,22 @@ def test_conservative_reconstructions_need_the_conservatives(lib):
     # gravity: the drop-in volume force validates before any device call
     g = _case(gravity=(0.0, -1.0, 0.0))
     assert lib.gbf_volume_force(ctypes.byref(g), None, buf, None) == _lib.GBF_ERR_INVALID_ARGUMENT
+
+
+def test_rhs_workspace_holds_the_lax_friedrichs_speeds(lib):
+    """gbf_rhs_ws: 32 bytes of workspace for Lax-Friedrichs (its three axis
+    speeds), none for the other schemes or an invalid case; a missing or
+    misaligned Lax-Friedrichs workspace is refused before any device call."""
+    lf = _case(riemann="LAX-FRIEDRICHS")
+    assert lib.gbf_rhs_workspace_bytes(ctypes.byref(lf)) == 32
+    assert lib.gbf_rhs_workspace_bytes(ctypes.byref(_case())) == 0
+    bad = _case(riemann="LAX-FRIEDRICHS")
+    bad.nh = 1
+    assert lib.gbf_rhs_workspace_bytes(ctypes.byref(bad)) == 0
+    buf = ctypes.c_void_p(8)
+    assert lib.gbf_rhs_ws(ctypes.byref(lf), buf, None, buf, None, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_rhs_ws(ctypes.byref(lf), buf, None, buf, None, ctypes.c_void_p(12), None) == \
+        _lib.GBF_ERR_ALIGNMENT
+    # the conservative reconstructions still need the conservatives
+    cv = _case(recon_var="CONSERVATIVE")
+    assert lib.gbf_rhs_ws(ctypes.byref(cv), buf, None, buf, None, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
