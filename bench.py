@@ -46,11 +46,14 @@ FP64_FLOP_ALGORITHMIC = {"tgv": 8280.0, "viscous": 11190.0}
 # FP64 thread instructions (DADD + DMUL + DFMA) executed per cell and stage
 # by the face kernels of the three axes, from the ncu capture of TGV 128^3 (summary in the
 # profiles directory); the epilogue adds the primitives of the new state.
-FP64_INST_FACES_PER_CELL_STAGE = 2974.8
-# DRAM bytes (read + write) of one RK stage at 128^3 (the one face launch of
-# the three axes, 466.7 MB, and the epilogue, 579.9 MB) from the ncu captures
-# of the same build; 120 B/cell algorithmic for stages 2, 3.
-DRAM_BYTES_PER_STAGE = 1046.6e6
+# Viscous CHAR-ROE + HLLC + CENTRAL4: 3 x 1 347.2 per face (viscous TGV 128^3 capture).
+FP64_INST_FACES_PER_CELL_STAGE = {"tgv": 2974.8, "viscous": 4041.6}
+# DRAM bytes (read + write) of one RK stage at 128^3 from the ncu captures of
+# the same build, averaged over the three stages: TGV, the one face launch of
+# the three axes (466.7 MB) and the epilogue (579.9 MB); viscous TGV, 473.3 MB
+# and 548.9 MB.  Both scale with the cells (the face buffers, the stage
+# primitives and the states are per cell); 120 B/cell algorithmic for stages 2, 3.
+DRAM_BYTES_PER_STAGE_128 = {"tgv": 1046.6e6, "viscous": 1022.3e6}
 
 
 def tgv_state(n, device, dtype=torch.float64):
@@ -636,20 +639,22 @@ def main():
         pass
     achieved = bytes_per_stage / stage_s / 1e9
     fp64_peak = fp64_peak_tflops(device)
-    flop_alg = FP64_FLOP_ALGORITHMIC["viscous" if viscous else "tgv"]
+    kind = "viscous" if viscous else "tgv"
+    flop_alg = FP64_FLOP_ALGORITHMIC[kind]
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_source": peak_src,
-        "traffic": None if viscous else DRAM_BYTES_PER_STAGE,
+        "traffic": DRAM_BYTES_PER_STAGE_128[kind] * cells / 128 ** 3,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage at 128^3"
+                          + ("" if n == 128 else f", scaled by the cells to {n}^3"),
         "launch": "one RK stage: face_flux_kernel (x, y, z faces) + stage_epilogue_kernel",
         "fp64": {
             "peak_tflops_measured": fp64_peak,  # DFMA chains, 2 FLOP per instruction
             "flop_per_cell_update_algorithmic": flop_alg,
             "achieved_tflops_algorithmic": flop_alg * cells / per_step_s / 1e12,
             "frac_algorithmic": flop_alg * cells / per_step_s / 1e12 / fp64_peak,
-            "inst_per_cell_stage_faces": None if viscous else FP64_INST_FACES_PER_CELL_STAGE,
-            "frac_issue_faces": None if viscous else
-            FP64_INST_FACES_PER_CELL_STAGE * cells / stage_s / (fp64_peak * 1e12 / 2.0),
+            "inst_per_cell_stage_faces": FP64_INST_FACES_PER_CELL_STAGE[kind],
+            "frac_issue_faces": FP64_INST_FACES_PER_CELL_STAGE[kind] * cells / stage_s / (fp64_peak * 1e12 / 2.0),
         },
     }
 
