@@ -333,8 +333,8 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  * of the cotangent to each argument of a max/min tie, zero derivative of
  * sign, where() passes the selected branch; the Lax-Friedrichs speed's
  * cotangent to the face states attaining the maximum, shared as jnp.max and
- * jnp.maximum share it).  Every reconstruction but MINMOD (PRIMITIVE WENO5-Z,
- * WENO5-JS, TENO5, WENO3-JS, WENO3-Z, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
+ * jnp.maximum share it).  Every reconstruction (PRIMITIVE WENO5-Z, WENO5-JS,
+ * TENO5, WENO3-JS, WENO3-Z, MINMOD, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
  * and CHAR-CONSERVATIVE with WENO5-Z and either frozen state), HLLC and HLL
  * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter on
  * the PRIMITIVE reconstructions, gravity, and the CENTRAL4 / CENTRAL2 viscous

@@ -458,8 +458,6 @@ int vjp_check(const gbf_case* c) {
   // the interpolation limiter is reversed on the PRIMITIVE paths
   if ((c->flags & GBF_FLAG_INTERPOLATION_LIMITER) && c->recon_var != GBF_RECVAR_PRIMITIVE)
     return GBF_ERR_UNSUPPORTED;
-  // every reconstruction but MINMOD (whose differentiable form is MINMOD-AD)
-  if (c->recon == GBF_RECON_MINMOD) return GBF_ERR_UNSUPPORTED;
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
   // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
   if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;

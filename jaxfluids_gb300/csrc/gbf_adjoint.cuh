@@ -208,8 +208,41 @@ __device__ __forceinline__ void minmod_ad_vjp(double b0, double b1, double b2, d
   }
 }
 
+// Reverse of muscl_minmod<J>(b0, b1, b2) (muscl3.py:53-75, limiter.py:9-10):
+// out = b1 +- 0.5 lim du with lim = max(0, min(1, r)); the limiter passes the
+// ratio's derivative inside (0, 1) and half of it at r = 0 and at r = 1, where
+// jnp.minimum / jnp.maximum split a tie evenly; the ratio's branch is the one
+// the forward selects (jnp.where routes no cotangent to the other).
+template <int J>
+__device__ __forceinline__ void minmod_vjp(double b0, double b1, double b2, double eps, double g,
+                                           double& db0, double& db1, double& db2) {
+  const double dc = (J == 0) ? b2 - b1 : b1 - b2;
+  const double du = (J == 0) ? b1 - b0 : b0 - b1;
+  const bool upwind = du >= eps;
+  const double num = upwind ? dc : dc + eps;
+  const double den = upwind ? du + 1e-10 : du + eps;
+  const double r = num / den;
+  const double m = fmin(1.0, r);
+  const double lim = fmax(0.0, m);
+  const double s = (J == 0) ? 0.5 : -0.5;  // out = b1 + s lim du
+  const double wmin = (r < 1.0) ? 1.0 : ((r == 1.0) ? 0.5 : 0.0);
+  const double wmax = (m > 0.0) ? 1.0 : ((m == 0.0) ? 0.5 : 0.0);
+  const double g_r = s * du * g * (wmin * wmax);
+  const double g_dc = g_r / den;            // d r / d num = 1 / den
+  const double g_du = s * lim * g - g_dc * r;  // explicit du, and d r / d den = -r / den
+  if (J == 0) {  // dc = b2 - b1, du = b1 - b0
+    db2 += g_dc;
+    db1 += g - g_dc + g_du;
+    db0 -= g_du;
+  } else {  // dc = b1 - b2, du = b0 - b1
+    db1 += g + g_dc - g_du;
+    db2 -= g_dc;
+    db0 += g_du;
+  }
+}
+
 // Reverse of reconstruct_pair<RECON> for the four-cell stencils (WENO3-JS,
-// WENO3-Z, MINMOD-AD): dw[k] = gL dL/dw_k + gR dR/dw_k.  The five-point WENO
+// WENO3-Z, MINMOD, MINMOD-AD): dw[k] = gL dL/dw_k + gR dR/dw_k.  The five-point WENO
 // stencils take the single-pass value-and-gradient route (weno5z_jac,
 // weno5js_jac) in the tile kernel instead.
 template <int RECON>
@@ -238,6 +271,18 @@ template <>
 __device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_WENO3Z>(const double* w, double eps,
                                                                         double gL, double gR, double* dw) {
   weno3_pair_vjp<true>(w, eps, gL, gR, dw);
+}
+
+template <>
+__device__ __forceinline__ void reconstruct_pair_vjp<GBF_RECON_MINMOD>(const double* w, double eps,
+                                                                        double gL, double gR, double* dw) {
+  double d[4] = {0, 0, 0, 0};
+  minmod_vjp<0>(w[0], w[1], w[2], eps, gL, d[0], d[1], d[2]);
+  minmod_vjp<1>(w[3], w[2], w[1], eps, gR, d[3], d[2], d[1]);
+  dw[0] = d[0];
+  dw[1] = d[1];
+  dw[2] = d[2];
+  dw[3] = d[3];
 }
 
 template <>

@@ -93,6 +93,8 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     (dict(recon="TENO5"), True),
     (dict(riemann="LAX-FRIEDRICHS"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon="MINMOD-AD", nh=4), True),
+    (dict(recon="MINMOD", nh=4), True),
+    (dict(riemann="LAX-FRIEDRICHS", recon="MINMOD", nh=4), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-PRIMITIVE"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CONSERVATIVE"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-CONSERVATIVE"), True),

@@ -133,6 +133,15 @@ VJP_CASES = [
     ("3d-char-roe-hll", (16, 12, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
                                                    "riemann": "HLL"}, "generic"),
     ("sod-minmodad-hll", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "HLL"}, "sod"),
+    # MINMOD: the limiter max(0, min(1, r)) clips on the smooth fields' steep
+    # parts and passes r on their flat ones
+    ("sod-minmod-hllc", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD"}, "sod"),
+    ("2d-minmod-hllc", (40, 36, 1), "PERIODIC", {"nh": 4, "recon": "MINMOD"}, "generic"),
+    ("3d-minmod-lf-zg", (12, 10, 14), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD", "riemann": "LAX-FRIEDRICHS"},
+     "generic"),
+    ("2d-minmod-rusanov-viscous", (24, 20, 1), "PERIODIC", {"nh": 4, "recon": "MINMOD", "riemann": "RUSANOV",
+                                                             "viscous": True, "heat": True, "mu": 0.02,
+                                                             "prandtl": 0.71}, "generic"),
     # CONSERVATIVE: WENO5-Z on the conservatives
     ("2d-cons-hllc", (32, 28, 1), "PERIODIC", {"recon_var": "CONSERVATIVE"}, "generic"),
     ("3d-cons-hll-zg", (12, 14, 10), "ZEROGRADIENT", {"recon_var": "CONSERVATIVE", "riemann": "HLL"}, "generic"),

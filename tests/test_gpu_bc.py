@@ -235,8 +235,6 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
     oc, cc = both(cells, bc, bc_values=vals, **kw)
-    if cc.recon == "MINMOD":
-        pytest.skip("the adjoint is built for MINMOD-AD, not MINMOD")
     if cc.interpolation_limiter and cc.recon_var != "PRIMITIVE":
         pytest.skip("the interpolation limiter is reversed on the PRIMITIVE reconstructions only")
     # smooth random-phase fields: WENO-Z's derivative amplifies rounding by
