@@ -133,6 +133,8 @@ class SpaceSolver(_Base):
             tile = material_manager
         super().__init__(config)
         self.tile = tile
+        # bytes of Lax-Friedrichs' axis speeds (0 for the other schemes)
+        self.rhs_ws_bytes = int(self.lib.gbf_rhs_workspace_bytes(ctypes.byref(self.case)))
 
     def compute_rhs(self, conservatives: torch.Tensor, primitives: torch.Tensor,
                     temperature: Optional[torch.Tensor], physical_simulation_time: float,
@@ -149,7 +151,7 @@ class SpaceSolver(_Base):
         tile = ctypes.byref(self.tile) if self.tile is not None else None
         # Lax-Friedrichs' axis speeds: a workspace per call from torch's
         # stream-ordered allocator, so calls on concurrent streams share none
-        nws = int(self.lib.gbf_rhs_workspace_bytes(ctypes.byref(self.case)))
+        nws = self.rhs_ws_bytes
         ws = torch.empty(max(1, nws // 8), dtype=torch.float64, device=primitives.device) if nws else None
         _lib.check(self.lib.gbf_rhs_ws(ctypes.byref(self.case), _ptr(primitives, shape, "primitives"),
                                        _ptr(conservatives, shape, "conservatives") if conservatives is not None
