@@ -63,10 +63,8 @@ extern "C" {
 #define GBF_RIEMANN_HLL 2     /* riemann_solvers/HLL.py */
 /* riemann_solvers/LaxFriedrichs.py: Rusanov's flux with one dissipation speed
  * per axis, the maximum of |u| + c over every reconstructed face state of the
- * axis (reduced by an extra reconstruction pass into the caller's workspace:
- * gbf_rhs_ws, the fused steps and the adjoint; gbf_rhs and gbf_rhs_cons, which
- * take none, use a per-device array, so their Lax-Friedrichs evaluations on
- * concurrent streams of one device must not overlap) */
+ * axis (reduced by an extra reconstruction pass into the workspace of the
+ * call) */
 #define GBF_RIEMANN_LAXFRIEDRICHS 3
 
 /* signal_speed (solvers/riemann_solvers/__init__.py:27) */
@@ -171,10 +169,13 @@ typedef struct gbf_case {
   double gravity[3];     /* forcings.gravity, with GBF_FLAG_GRAVITY */
 } gbf_case;
 
-/* Launch shape of the fused sweep kernels; all-zero picks the built-in default
- * (2-D 15x32, 3-D 8x8x8 inviscid PRIMITIVE or 7x8x8 CHAR/viscous and adjoint,
- * 1-D 256).  Cells per tile at most 4 x threads; the staged pencil and face
- * slots must fit 227 KB of shared memory (GBF_ERR_INVALID_ARGUMENT otherwise). */
+/* Launch shape of the tile kernels; all-zero picks the built-in defaults.  For
+ * the face kernels (the right-hand side and the fused stages) t gives the
+ * faces per tile (default 16 along the face axis and 2 x 16 or 32 across it,
+ * 16 x 8 on small cases); for the adjoint's tile kernels and the batched
+ * stages the cells per tile (2-D 15x32, 3-D 7x8x8, 1-D 256).  The staged
+ * stencil cells must fit 227 KB of shared memory (GBF_ERR_INVALID_ARGUMENT
+ * otherwise). */
 typedef struct gbf_tile {
   int32_t t[3];          /* cells per tile along each axis (1 on inactive axes) */
   int32_t threads;       /* threads per CTA (multiple of 32, 32..256) */
@@ -201,7 +202,12 @@ int gbf_case_check(const gbf_case* c);
  * buffer.  Replaces SpaceSolver.compute_rhs (solvers/space_solver.py:151-453,
  * per axis compute_rhs_xi :456-674) for the single-phase GODUNOV path:
  * reconstruct -> Riemann flux -> (1/dx)(F[i-1/2] - F[i+1/2]) summed over
- * the active axes in x, y, z order.  prims: halo buffer; rhs: interior buffer.
+ * the active axes in x, y, z order.  prims: halo buffer, read as it is (its
+ * halos are the caller's); rhs: interior buffer.  The face fluxes of every
+ * axis (N + 1 per line, as the reference's face arrays) go through a device
+ * buffer of gbf_rhs_workspace_bytes(c) bytes, allocated for the call with
+ * cudaMallocAsync on `stream` and released on it (gbf_rhs_ws takes it from
+ * the caller instead).
  */
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream);
 
@@ -215,10 +221,10 @@ int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, dou
 
 /* As gbf_rhs_cons (cons may be null for the reconstructions that do not read
  * it) with a caller workspace of gbf_rhs_workspace_bytes(c) bytes of device
- * memory, 8-byte aligned: Lax-Friedrichs keeps its three axis speeds there
- * instead of in the per-device slots, so evaluations on concurrent streams,
- * each with its own workspace, share no state.  0 bytes (workspace may be
- * null) for every other scheme, and for an invalid case. */
+ * memory, 8-byte aligned: the face fluxes (5 doubles per face of every active
+ * axis, N + 1 faces per line) and the Lax-Friedrichs axis speeds, so the call
+ * allocates nothing and evaluations on concurrent streams, each with its own
+ * workspace, share no state.  0 bytes for an invalid case. */
 size_t gbf_rhs_workspace_bytes(const gbf_case* c);
 int gbf_rhs_ws(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,
                void* workspace, void* stream);

@@ -199,9 +199,11 @@ int gbf_case_check(const gbf_case* c) {
 }
 
 
-// The drop-in right-hand side: cons is read by the conservative
-// reconstructions only (required there, ignored elsewhere); ws holds the
-// Lax-Friedrichs speeds (null: the per-device slots).
+// The drop-in right-hand side: the face kernels on the caller's halo buffers
+// (cons read by the conservative reconstructions only: required there,
+// ignored elsewhere) and a divergence epilogue.  ws: the face buffers and the
+// Lax-Friedrichs speed slots (rhs_face_doubles); null: allocated for the call
+// from the device's stream-ordered pool and released on the same stream.
 static int rhs_common(const gbf_case* c, const double* prims, const double* cons, bool cons_given, double* rhs,
                       const gbf_tile* tile, double* ws, void* stream) {
   CaseInfo ci;
@@ -217,7 +219,13 @@ static int rhs_common(const gbf_case* c, const double* prims, const double* cons
   p.prims_halo = prims;
   p.cons_halo = cons;
   p.out = rhs;
-  return launch_sweep(c, p, threads, smem, (cudaStream_t)stream, MODE_RHS, ws);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ws) return launch_rhs_faces(c, ci, tile, p, ws, s);
+  void* tmp = nullptr;
+  if (cudaMallocAsync(&tmp, (size_t)rhs_face_doubles(ci) * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
+  st = launch_rhs_faces(c, ci, tile, p, static_cast<double*>(tmp), s);
+  if (cudaFreeAsync(tmp, s) != cudaSuccess && st == GBF_OK) st = GBF_ERR_CUDA;
+  return st;
 }
 
 int gbf_rhs(const gbf_case* c, const double* prims, double* rhs, const gbf_tile* tile, void* stream) {
@@ -232,16 +240,17 @@ int gbf_rhs_cons(const gbf_case* c, const double* prims, const double* cons, dou
 size_t gbf_rhs_workspace_bytes(const gbf_case* c) {
   CaseInfo ci;
   if (check_case(c, &ci) != GBF_OK) return 0;
-  const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
-  return lf ? 4 * sizeof(double) : 0;
+  return (size_t)rhs_face_doubles(ci) * sizeof(double);
 }
 
 static int gbf_rhs_ws_impl(const gbf_case* c, const double* prims, const double* cons, double* rhs,
                            const gbf_tile* tile, void* workspace, void* stream) {
-  const size_t need = gbf_rhs_workspace_bytes(c);
-  if (need && !workspace) return GBF_ERR_INVALID_ARGUMENT;
-  if (need && !aligned8(workspace)) return GBF_ERR_ALIGNMENT;
-  return rhs_common(c, prims, cons, false, rhs, tile, need ? static_cast<double*>(workspace) : nullptr, stream);
+  CaseInfo ci;
+  int st = check_case(c, &ci);
+  if (st != GBF_OK) return st;
+  if (!workspace) return GBF_ERR_INVALID_ARGUMENT;
+  if (!aligned8(workspace)) return GBF_ERR_ALIGNMENT;
+  return rhs_common(c, prims, cons, false, rhs, tile, static_cast<double*>(workspace), stream);
 }
 
 int gbf_rhs_ws(const gbf_case* c, const double* prims, const double* cons, double* rhs, const gbf_tile* tile,

@@ -67,12 +67,14 @@ struct FaceShare {
 
 // The faces of axis AX in one face tile: origin o (logical face coordinates),
 // fe faces per axis, nf faces per line along AX; fluxes to out[v * faces +
-// face] (faces of the axis laid out [E0][E1][E2], E_AX = nf).  Reads the stage
-// primitives p.prims (and, for the conservative reconstructions, p.cons),
-// MODE_STAGE_P semantics.  smem: the pencil (and the shared terms) sized by
-// face_smem.  Returns the thread's Lax-Friedrichs face speed maximum (speed
-// pass 1).
-template <int AX, int RECON, int RIEMANN, int VISC>
+// face] (faces of the axis laid out [E0][E1][E2], E_AX = nf).  MODE_STAGE_P:
+// reads the stage primitives p.prims (and, for the conservative
+// reconstructions, p.cons), boundary conditions by index remapping; MODE_RHS:
+// reads the caller's halo buffers p.prims_halo (and p.cons_halo) as they are
+// (the drop-in right-hand side).  smem: the pencil (and the shared terms)
+// sized by face_smem.  Returns the thread's Lax-Friedrichs face speed maximum
+// (speed pass 1).
+template <int AX, int RECON, int RIEMANN, int VISC, int MODE = MODE_STAGE_P>
 __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int o[3], const int fe[3], int nf,
                                                  double* out, double* smem) {
   constexpr int R = ReconTraits<RECON>::R;
@@ -82,7 +84,7 @@ __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int
   pe[AX] += 2 * R - 1;
   const int pvol = pe[0] * pe[1] * pe[2];
   if (RIEMANN != RIEMANN_NONE) {
-    stage_pencil<AX, R, MODE_STAGE_P, CONS>(p, o, pe, pvol, smem);
+    stage_pencil<AX, R, MODE, CONS>(p, o, pe, pvol, smem);
     __syncthreads();
   }
   const int fvol = fe[0] * fe[1] * fe[2];
@@ -137,7 +139,7 @@ __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int
         int g[3] = {gc[0], gc[1], gc[2]};
         g[AX] += kax;
         g[ax2] += k2;
-        return global_prim<MODE_STAGE_P>(p, v, g[0], g[1], g[2]);
+        return global_prim<MODE>(p, v, g[0], g[1], g[2]);
       };
       if (p.heat) sm_vis[i] = cell(4, 0, AX, 0) / (cell(0, 0, AX, 0) * p.R);
       if (p.viscous) {
@@ -168,7 +170,7 @@ __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int
     sf[AX] += 2;
     const DissShared ds{VISC > 0 ? sm_vis + idx3(sf[0], sf[1], sf[2], se[1], se[2]) : nullptr, svol, sstride};
     double F[5];
-    if (!face_flux<AX, RECON, RIEMANN, MODE_STAGE_P, VISC, SHARE>(p, smem, pvol, pstride, base, q, F, smax_faces,
+    if (!face_flux<AX, RECON, RIEMANN, MODE, VISC, SHARE>(p, smem, pvol, pstride, base, q, F, smax_faces,
                                                                    sm_win, ds))
       continue;
     const long long g = ((long long)q[0] * ext[1] + q[1]) * ext[2] + q[2];
@@ -180,7 +182,7 @@ __device__ __forceinline__ double face_tile_body(const SweepParams& p, const int
 
 // The faces of axis AX in face tile b of ft, fluxes to fb; Lax-Friedrichs'
 // speed pass 1 reduces the tile's face speeds.
-template <int AX, int RECON, int RIEMANN, int VISC>
+template <int AX, int RECON, int RIEMANN, int VISC, int MODE>
 __device__ __forceinline__ void face_tile(const SweepParams& p, const FaceTile& ft, const FaceBuffers& fb, int b,
                                           double* smem) {
   const int b2 = b % ft.tiles[2];
@@ -190,7 +192,7 @@ __device__ __forceinline__ void face_tile(const SweepParams& p, const FaceTile& 
   int fe[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) fe[a] = min(ft.t[a], ((a == AX) ? ft.nf : p.n[a]) - o[a]);
-  const double smax_faces = face_tile_body<AX, RECON, RIEMANN, VISC>(p, o, fe, ft.nf, fb.flux[AX], smem);
+  const double smax_faces = face_tile_body<AX, RECON, RIEMANN, VISC, MODE>(p, o, fe, ft.nf, fb.flux[AX], smem);
   if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass == 1) lf_speed_reduce<AX>(p, smax_faces);
 }
 
@@ -201,30 +203,24 @@ __device__ __forceinline__ void face_tile(const SweepParams& p, const FaceTile& 
 // nothing).  The kernels issue FP64 instructions at the rate of a pure DFMA
 // chain on this part; a third CTA (at most 85 registers, spilling) measured
 // the same time on TGV 128^3.
-template <int RECON, int RIEMANN, int VISC>
+template <int RECON, int RIEMANN, int VISC, int MODE>
 __global__ void __launch_bounds__(256, 2)
     face_flux_kernel(const SweepParams p, const FaceTiles fts, const FaceBuffers fb) {
   extern __shared__ double smem[];
   const int b = blockIdx.x;
   if (b < fts.start[1])
-    face_tile<0, RECON, RIEMANN, VISC>(p, fts.ft[0], fb, b - fts.start[0], smem);
+    face_tile<0, RECON, RIEMANN, VISC, MODE>(p, fts.ft[0], fb, b - fts.start[0], smem);
   else if (b < fts.start[2])
-    face_tile<1, RECON, RIEMANN, VISC>(p, fts.ft[1], fb, b - fts.start[1], smem);
+    face_tile<1, RECON, RIEMANN, VISC, MODE>(p, fts.ft[1], fb, b - fts.start[1], smem);
   else
-    face_tile<2, RECON, RIEMANN, VISC>(p, fts.ft[2], fb, b - fts.start[2], smem);
+    face_tile<2, RECON, RIEMANN, VISC, MODE>(p, fts.ft[2], fb, b - fts.start[2], smem);
 }
 
-// The cell epilogue of a stage at cell i (logical coordinates c, cs cells):
-// rhs = ((0 + d_x) + d_y) + d_z with d_a = (1/dx_a)(F[i - 1/2] - F[i + 1/2])
-// (space_solver.py:266-314, :597-599), gravity (space_solver.py:377-384), the
-// RK combination (RK3.py:27-62, time_integrator.py:34-58) into p.out, the
-// primitives of the new state into prims_out, and (p.reduce_dt) the maximum
-// signal speed and minimum density of the new state (time_step_size.py:96-109)
-// folded into smax, rmin.
-__device__ __forceinline__ void epilogue_cell(const SweepParams& p, const FaceBuffers& fb, double* prims_out,
-                                              long long i, const int c[3], long long cs, double dt, double& smax,
-                                              double& rmin) {
-  double acc[5];
+// The right-hand side of cell c (logical coordinates) from the face buffers:
+// acc = ((0 + d_x) + d_y) + d_z with d_a = (1/dx_a)(F[i - 1/2] - F[i + 1/2])
+// (space_solver.py:266-314, :597-599).
+__device__ __forceinline__ void divergence_cell(const SweepParams& p, const FaceBuffers& fb, const int c[3],
+                                                double acc[5]) {
   bool first = true;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -245,6 +241,19 @@ __device__ __forceinline__ void epilogue_cell(const SweepParams& p, const FaceBu
     }
     first = false;
   }
+}
+
+// The cell epilogue of a stage at cell i (logical coordinates c, cs cells):
+// the right-hand side (divergence_cell), gravity (space_solver.py:377-384), the
+// RK combination (RK3.py:27-62, time_integrator.py:34-58) into p.out, the
+// primitives of the new state into prims_out, and (p.reduce_dt) the maximum
+// signal speed and minimum density of the new state (time_step_size.py:96-109)
+// folded into smax, rmin.
+__device__ __forceinline__ void epilogue_cell(const SweepParams& p, const FaceBuffers& fb, double* prims_out,
+                                              long long i, const int c[3], long long cs, double dt, double& smax,
+                                              double& rmin) {
+  double acc[5];
+  divergence_cell(p, fb, c, acc);
   double U[5], Un[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + i];
@@ -311,11 +320,14 @@ __device__ __forceinline__ void dt_block_reduce(double* dt_state, double smax, d
 // Host side ------------------------------------------------------------------
 
 // Launch the face kernel of the axes fts lists for one scheme (instantiated
-// per scheme family in gbf_sweep_<family>.cu).
+// per scheme family in gbf_sweep_<family>.cu): MODE_RHS when p carries the
+// caller's halo buffers (p.prims_halo, the drop-in right-hand side), else
+// MODE_STAGE_P (the fused stages).
 template <int RECON, int RIEMANN, int VISC>
 int launch_faces_one(const SweepParams& p, const FaceTiles& fts, const FaceBuffers& fb, int threads, size_t smem,
                      cudaStream_t s) {
-  auto kern = face_flux_kernel<RECON, RIEMANN, VISC>;
+  auto kern = p.prims_halo ? face_flux_kernel<RECON, RIEMANN, VISC, MODE_RHS>
+                           : face_flux_kernel<RECON, RIEMANN, VISC, MODE_STAGE_P>;
   if (fts.start[3] <= 0) return GBF_OK;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return GBF_ERR_CUDA;

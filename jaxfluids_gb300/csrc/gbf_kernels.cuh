@@ -39,13 +39,13 @@ void fill_bc_fields(const gbf_case* c, BcFields* bf);
 int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, SweepParams* p,
                       int* threads, size_t* smem, bool for_vjp = false);
 
-// launch the sweep kernel instantiation for (recon, riemann, mode); lf_ws:
-// the three Lax-Friedrichs axis speeds (null: the per-device slots)
-int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem,
-                 cudaStream_t s, int mode, double* lf_ws = nullptr);
-
-// The Lax-Friedrichs speed slots of the current device (gbf_sweep.cu).
-int lf_alpha_on_current_device(double** out);
+// The drop-in right-hand side (gbf_stage.cu): doubles of its workspace (the
+// face buffers, N + 1 faces per line on every active axis, and the
+// Lax-Friedrichs speed slots) and the face kernels plus divergence on the
+// halo buffers p.prims_halo (p.cons_halo), into the interior buffer p.out.
+long long rhs_face_doubles(const CaseInfo& ci);
+int launch_rhs_faces(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
+                     double* workspace, cudaStream_t s);
 
 // Dynamic shared memory of a face kernel of axis `axis` with face tile ft
 // (gbf_stage.cu).

@@ -1,7 +1,9 @@
 // One fused TVD-RK3 stage on interior buffers: the face kernels of every
 // active axis (gbf_faces.cuh), then the cell epilogue.  Used by the fused
 // stepping (gbf_rk3_advance, gbf_rk3_stage, the allocation-free variant) and
-// by the adjoint's recomputation of stage states.
+// by the adjoint's recomputation of stage states.  The drop-in right-hand side
+// runs the same face kernels on the caller's halo buffers and a divergence
+// epilogue (launch_rhs_faces).
 #include <algorithm>
 
 #include "gbf_sweep_launch.cuh"
@@ -28,6 +30,24 @@ __global__ void __launch_bounds__(256) stage_epilogue_kernel(const SweepParams p
     epilogue_cell(p, fb, prims_out, i, c, cs, dt, smax, rmin);
   }
   if (p.reduce_dt) dt_block_reduce(p.dt_state, smax, rmin);
+}
+
+// The drop-in right-hand side of every cell: the divergence of the face
+// buffers into p.out (interior layout), nothing else.
+__global__ void __launch_bounds__(256) rhs_epilogue_kernel(const SweepParams p, const FaceBuffers fb) {
+  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cs;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int c2 = (int)(i % p.n[2]);
+    const long long r = i / p.n[2];
+    const int c1 = (int)(r % p.n[1]);
+    const int c0 = (int)(r / p.n[1]);
+    const int c[3] = {c0, c1, c2};
+    double acc[5];
+    divergence_cell(p, fb, c, acc);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) p.out[v * cs + i] = acc[v];
+  }
 }
 
 bool periodic_axis(const gbf_case* c, int a) { return c->bc[2 * a] == GBF_BC_PERIODIC; }
@@ -256,6 +276,65 @@ int launch_lf_face_pass(const gbf_case* c, const CaseInfo& ci, const double* U, 
 // reduce_dt, dt_state.  prims_out (may be null) receives the primitives of
 // the new state.  Lax-Friedrichs runs a speed pass of the face kernel before
 // its flux pass (LaxFriedrichs.py:25-47).
+// Drop-in: every face of the reference's face arrays (N + 1 per line, also on
+// a PERIODIC axis, whose end faces read the caller's halos as they are).
+long long rhs_face_doubles(const CaseInfo& ci) {
+  long long total = 4;
+  for (int a = 0; a < 3; ++a) {
+    if (!(ci.active_mask & (1 << a))) continue;
+    long long f = ci.n[a] + 1;
+    for (int b = 0; b < 3; ++b)
+      if (b != a) f *= ci.n[b];
+    total += 5 * f;
+  }
+  return total;
+}
+
+int launch_rhs_faces(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
+                     double* workspace, cudaStream_t s) {
+  if (!p.prims_halo || !p.out || !workspace) return GBF_ERR_INVALID_ARGUMENT;
+  // the conservative reconstructions read the caller's conservatives
+  const bool cons = c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
+  if (cons && !(c->flags & GBF_FLAG_NO_CONVECTIVE) && !p.cons_halo) return GBF_ERR_INVALID_ARGUMENT;
+  FaceBuffers fb;
+  double* base = workspace;
+  for (int a = 0; a < 3; ++a) {
+    fb.flux[a] = nullptr;
+    fb.nf[a] = 0;
+    if (!(ci.active_mask & (1 << a))) continue;
+    fb.nf[a] = ci.n[a] + 1;
+    long long f = fb.nf[a];
+    for (int b = 0; b < 3; ++b)
+      if (b != a) f *= ci.n[b];
+    fb.flux[a] = base;
+    base += 5 * f;
+  }
+  fb.lf_alpha = base;
+  const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);
+  SweepParams q = p;
+  int st;
+  if (lf) {
+    q.lf_alpha = fb.lf_alpha;
+    if (cudaMemsetAsync(q.lf_alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
+  }
+  FaceTiles fts;
+  int threads;
+  if ((st = make_face_tiles(ci, tile, ci.active_mask, fb.nf, &fts, &threads)) != GBF_OK) return st;
+  const size_t smem = face_smem_tiles(c, fts);
+  if (smem > 227 * 1024) return GBF_ERR_INVALID_ARGUMENT;
+  if (lf) {
+    // LaxFriedrichs.py:35-38: the axis speeds over every face state first
+    q.speed_pass = 1;
+    if ((st = launch_faces(c, q, fts, fb, threads, smem, s)) != GBF_OK) return st;
+    q.speed_pass = 0;
+  }
+  if ((st = launch_faces(c, q, fts, fb, threads, smem, s)) != GBF_OK) return st;
+  long long grid = (ci.cells + 255) / 256;
+  grid = std::min<long long>(grid, 152 * 8);
+  rhs_epilogue_kernel<<<(int)grid, 256, 0, s>>>(q, fb);
+  return cudaGetLastError() == cudaSuccess ? GBF_OK : GBF_ERR_CUDA;
+}
+
 int launch_rk3_stage(const gbf_case* c, const CaseInfo& ci, const gbf_tile* tile, const SweepParams& p,
                      const FaceBuffers& fb, double* prims_out, cudaStream_t s) {
   const bool lf = c->riemann == GBF_RIEMANN_LAXFRIEDRICHS && !(c->flags & GBF_FLAG_NO_CONVECTIVE);

@@ -1,5 +1,5 @@
-// Launch parameters of the sweep kernel and dispatch to the scheme families
-// (gbf_sweep_<family>.cu instantiate the kernels).
+// Kernel parameters of a case (SweepParams) and its boundary constants and
+// fields, shared by the face kernels, the batched stages and the adjoint.
 #include <algorithm>
 
 #include "gbf_sweep_launch.cuh"
@@ -51,13 +51,12 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
     for (int a = 0; a < 3; ++a) t[a] = std::max(1, tile->t[a]);
     if (tile->threads > 0) thr = tile->threads;
   } else {
-    // defaults: ~512-cell tiles, longest along the contiguous (last active)
-    // axis.  A face sweep runs one face per thread; 15 x 32 (2-D) and
+    // defaults of the cell tiles (the adjoint's tile kernels; the face
+    // kernels take their own face tiles, gbf_stage.cu): ~512-cell tiles,
+    // longest along the contiguous (last active) axis.  15 x 32 (2-D) and
     // 7 x 8 x 8 (3-D) tiles have 495..512 faces per axis, two full rounds of
-    // 256 threads instead of a third round on a quarter of the warps (measured
-    // on GB300: 2-D forward -9 %, 3-D viscous CHAR forward -4 %, 3-D adjoint
-    // -6 %).  The inviscid 3-D forward, two CTAs per SM, is flat across shapes
-    // and keeps 8 x 8 x 8.
+    // 256 threads instead of a third round on a quarter of the warps
+    // (measured on GB300: 3-D adjoint -6 %).
     for (int a = 0; a < 3; ++a) t[a] = 1;
     if (dim == 1) {
       for (int a = 0; a < 3; ++a)
@@ -99,8 +98,6 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
     t[a] = std::min(t[a], ci.n[a]);
   }
   if (thr % 32 != 0 || thr < 32 || thr > 256) return GBF_ERR_INVALID_ARGUMENT;
-  const long long tvol = (long long)t[0] * t[1] * t[2];
-  if (tvol > (long long)kSweepMaxCellsPerThread * thr) return GBF_ERR_INVALID_ARGUMENT;
   const int R = radius_of(c->recon);
   long long pmax = 0, fmax = 0;
   for (int a = 0; a < 3; ++a) {
@@ -151,98 +148,5 @@ int make_sweep_params(const gbf_case* c, const CaseInfo& ci, const gbf_tile* til
   *smem = bytes;
   return GBF_OK;
 }
-
-namespace {
-
-// Lax-Friedrichs dissipation speeds (bits of three non-negative doubles), one
-// array per device; its address is looked up once per device, before any
-// graph capture (the first launch of a case).
-__device__ unsigned long long g_lf_alpha[3];
-constexpr int kLfMaxDevices = 64;
-double* g_lf_alpha_ptr[kLfMaxDevices] = {};
-
-}  // namespace
-
-int lf_alpha_on_current_device(double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return GBF_ERR_CUDA;
-  if (dev < 0 || dev >= kLfMaxDevices) return GBF_ERR_UNSUPPORTED;
-  if (!g_lf_alpha_ptr[dev]) {
-    void* a = nullptr;
-    if (cudaGetSymbolAddress(&a, g_lf_alpha) != cudaSuccess || !a) return GBF_ERR_CUDA;
-    g_lf_alpha_ptr[dev] = static_cast<double*>(a);
-  }
-  *out = g_lf_alpha_ptr[dev];
-  return GBF_OK;
-}
-
-namespace {
-
-int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
-                         int mode);
-
-}  // namespace
-
-// Lax-Friedrichs (LaxFriedrichs.py:25-47) runs the Rusanov instantiation twice:
-// a pass reducing the axis' max |u| + c over the face states (into lf_ws, or
-// the per-device slots), then the flux pass with that speed.
-int launch_sweep(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s, int mode,
-                 double* lf_ws) {
-  if (c->riemann != GBF_RIEMANN_LAXFRIEDRICHS || (c->flags & GBF_FLAG_NO_CONVECTIVE))
-    return launch_sweep_schemes(c, p, threads, smem, s, mode);
-  double* alpha = lf_ws;
-  int st = GBF_OK;
-  if (!alpha && (st = lf_alpha_on_current_device(&alpha)) != GBF_OK) return st;
-  if (cudaMemsetAsync(alpha, 0, 3 * sizeof(double), s) != cudaSuccess) return GBF_ERR_CUDA;
-  SweepParams q = p;
-  q.lf_alpha = alpha;
-  q.speed_pass = 1;
-  q.reduce_dt = 0;
-  if ((st = launch_sweep_schemes(c, q, threads, smem, s, mode)) != GBF_OK) return st;
-  q.speed_pass = 0;
-  q.reduce_dt = p.reduce_dt;
-  return launch_sweep_schemes(c, q, threads, smem, s, mode);
-}
-
-namespace {
-
-int launch_sweep_schemes(const gbf_case* c, const SweepParams& p, int threads, size_t smem, cudaStream_t s,
-                         int mode) {
-  const bool visc = (c->flags & (GBF_FLAG_VISCOUS | GBF_FLAG_HEAT)) != 0;
-  const bool chr = c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE;
-  const bool cons = c->recon_var == GBF_RECVAR_CONSERVATIVE || c->recon_var == GBF_RECVAR_CHAR_CONSERVATIVE;
-  if (cons && !(c->flags & GBF_FLAG_NO_CONVECTIVE)) {
-    if (visc && mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
-    if (!visc && mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
-    if (mode == MODE_RHS && !p.cons_halo) return GBF_ERR_INVALID_ARGUMENT;  // needs the conservatives
-    return (c->recon_var == GBF_RECVAR_CONSERVATIVE)
-               ? launch_sweep_cons(visc, c->riemann, mode, p, threads, smem, s)
-               : launch_sweep_charcons(visc, c->riemann, mode, p, threads, smem, s);
-  }
-  if (visc) {
-    // dissipative fluxes read the primitive buffer (MODE_STAGE_P) or the halo buffer
-    if (mode == MODE_STAGE) return GBF_ERR_UNSUPPORTED;
-    if (c->flags & GBF_FLAG_NO_CONVECTIVE) return launch_sweep_dissipative(mode, p, threads, smem, s);
-    const bool c4 = c->dissipative_stencil[0] == GBF_CENTRAL4 && c->dissipative_stencil[1] == GBF_CENTRAL4 &&
-                    c->dissipative_stencil[2] == GBF_CENTRAL4;
-    if (chr)
-      return c4 ? launch_sweep_char_visc_c4(c->riemann, mode, p, threads, smem, s)
-                : launch_sweep_char_visc(c->riemann, mode, p, threads, smem, s);
-    if (c->recon == GBF_RECON_WENO5Z)
-      return c4 ? launch_sweep_weno_visc_c4(c->riemann, mode, p, threads, smem, s)
-                : launch_sweep_weno_visc(c->riemann, mode, p, threads, smem, s);
-    if (c->recon == GBF_RECON_WENO5JS) return launch_sweep_weno5js_visc(c->riemann, mode, p, threads, smem, s);
-    if (c->recon == GBF_RECON_TENO5) return launch_sweep_teno5_visc(c->riemann, mode, p, threads, smem, s);
-    return launch_sweep_short_visc(c->recon, c->riemann, mode, p, threads, smem, s);
-  }
-  if (mode == MODE_STAGE_P) return GBF_ERR_UNSUPPORTED;
-  if (chr) return launch_sweep_char(c->riemann, mode, p, threads, smem, s);
-  if (c->recon == GBF_RECON_WENO5Z) return launch_sweep_weno(c->riemann, mode, p, threads, smem, s);
-  if (c->recon == GBF_RECON_MINMOD || c->recon == GBF_RECON_MINMOD_AD)
-    return launch_sweep_muscl(c->recon, c->riemann, mode, p, threads, smem, s);
-  return launch_sweep_weno_family(c->recon, c->riemann, mode, p, threads, smem, s);
-}
-
-}  // namespace
 
 }  // namespace gbf

@@ -1,15 +1,12 @@
-// Per-face finite-volume building blocks and the tile sweep kernel.
+// Per-face finite-volume building blocks.
 //
 // face_flux (one face from a staged pencil: reconstruction, limiter, Riemann
-// flux, dissipative flux) is shared by the fused stages' face kernels
-// (gbf_faces.cuh), the batched stages (gbf_batch.cuh) and the tile sweep
-// kernel here.  The tile sweep kernel is the drop-in right-hand side
-// (MODE_RHS, SpaceSolver.compute_rhs on halo buffers): one CTA owns a tile of
-// T0 x T1 x T2 cells; for each active axis it stages the primitives of the
-// tile extended by the stencil radius R along that axis (a "pencil box") in
-// shared memory, computes every face flux of the tile once (one face per
-// thread), and adds (1/dx)(F[i-1/2] - F[i+1/2]) to per-thread right-hand-side
-// accumulators in registers, which the epilogue stores.
+// flux, dissipative flux) is shared by the face kernels (gbf_faces.cuh: the
+// fused stages and the drop-in right-hand side) and the batched stages
+// (gbf_batch.cuh); stage_pencil stages the primitives of a tile's stencil
+// cells (a "pencil box": the tile extended by the stencil radius R along the
+// face axis) in shared memory from the caller's halo buffer or the stage's
+// interior buffer, boundary conditions by index remapping.
 //
 // The path is FP64-arithmetic bound on GB300 (about 2 FP64 lanes per SM and
 // clock against kilobytes of FP64 work per cell), so the layouts minimise
@@ -675,77 +672,6 @@ __device__ __forceinline__ void lf_speed_reduce(const SweepParams& p, double sma
               (unsigned long long)__double_as_longlong(smax_faces));
 }
 
-template <int AX, int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
-__device__ __forceinline__ void sweep_axis(const SweepParams& p, const int o[3], const int ext[3],
-                                           double* sm_prim, double* sm_flux,
-                                           double (&acc)[MAXC][5], bool first) {
-  constexpr int R = ReconTraits<RECON>::R;
-  constexpr bool CONS = RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS;
-  const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
-
-  // pencil box extents
-  int pe[3] = {ext[0], ext[1], ext[2]};
-  pe[AX] += 2 * R;
-  const int pvol = pe[0] * pe[1] * pe[2];
-
-  if (RIEMANN != RIEMANN_NONE) {
-    stage_pencil<AX, R, MODE, CONS>(p, o, pe, pvol, sm_prim);
-    __syncthreads();
-  }
-
-  // ---- face fluxes, one face per thread --------------------------------
-  int fe[3] = {ext[0], ext[1], ext[2]};
-  fe[AX] += 1;
-  const int fvol = fe[0] * fe[1] * fe[2];
-  const int pstride = (AX == 0) ? pe[1] * pe[2] : ((AX == 1) ? pe[2] : 1);
-  double smax_faces = 0.0;  // Lax-Friedrichs speed pass
-  for (int f = tid; f < fvol; f += nthr) {
-    const int f2 = f % fe[2];
-    const int r = f / fe[2];
-    const int f1 = r % fe[1];
-    const int f0 = r / fe[1];
-    // face f_AX lies between pencil cells f_AX + R - 1 and f_AX + R; the
-    // stencil starts R cells left of the face, i.e. at pencil cell f_AX.
-    const int base = idx3(f0, f1, f2, pe[1], pe[2]);
-    const int q[3] = {o[0] + f0, o[1] + f1, o[2] + f2};
-    double F[5];
-    if (!face_flux<AX, RECON, RIEMANN, MODE, VISC>(p, sm_prim, pvol, pstride, base, q, F, smax_faces)) continue;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) sm_flux[v * fvol + f] = F[v];
-  }
-  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) {
-    lf_speed_reduce<AX>(p, smax_faces);
-    __syncthreads();  // the pencil is restaged by the next axis
-    return;
-  }
-  __syncthreads();
-
-  // ---- divergence into the per-thread accumulators ---------------------
-  const int cvol = ext[0] * ext[1] * ext[2];
-  const int fstride = (AX == 0) ? fe[1] * fe[2] : ((AX == 1) ? fe[2] : 1);
-  const double odx = p.one_dx[AX];
-#pragma unroll
-  for (int k = 0; k < MAXC; ++k) {
-    const int c = tid + k * nthr;
-    if (c < cvol) {
-      const int c2 = c % ext[2];
-      const int r = c / ext[2];
-      const int c1 = r % ext[1];
-      const int c0 = r / ext[1];
-      const int fl = idx3(c0, c1, c2, fe[1], fe[2]);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        // space_solver.py:597-599: one_dx * (F[:-1] - F[1:])
-        const double d = odx * (sm_flux[v * fvol + fl] - sm_flux[v * fvol + fl + fstride]);
-        acc[k][v] = first ? d : __dadd_rn(acc[k][v], d);
-      }
-    }
-  }
-  __syncthreads();
-}
-
-
 // RK3 coefficients (RK3.py:27-29)
 __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, double rhs, double dt) {
   // time_integrator.py:34-58 + RK3.py:31-62: buf = a U + b U0 (stages 1, 2),
@@ -757,140 +683,6 @@ __device__ __forceinline__ double rk3_combine(int stage, double U, double U0, do
   }
   const double b = __dadd_rn(__dmul_rn(2.0 / 3.0, U), __dmul_rn(1.0 / 3.0, U0));
   return __dadd_rn(b, __dmul_rn(__dmul_rn(dt, 2.0 / 3.0), rhs));
-}
-
-// One tile (index b of the case described by p) of the fused sweep.
-template <int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
-__device__ __forceinline__ void sweep_tile(const SweepParams& p, int b, double* smem) {
-  const int b2 = b % p.tiles[2];
-  const int b1 = (b / p.tiles[2]) % p.tiles[1];
-  const int b0 = b / (p.tiles[2] * p.tiles[1]);
-  const int o[3] = {b0 * p.t[0], b1 * p.t[1], b2 * p.t[2]};
-  const int ext[3] = {min(p.t[0], p.n[0] - o[0]), min(p.t[1], p.n[1] - o[1]),
-                      min(p.t[2], p.n[2] - o[2])};
-
-  // shared memory: pencil primitives, then face fluxes
-  constexpr int R = ReconTraits<RECON>::R;
-  int pmax = 0;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    if (p.active_mask & (1 << a)) {
-      int v = (p.t[0] + (a == 0 ? 2 * R : 0)) * (p.t[1] + (a == 1 ? 2 * R : 0)) *
-              (p.t[2] + (a == 2 ? 2 * R : 0));
-      pmax = max(pmax, v);
-    }
-  }
-  // (the conservative reconstructions stage the conservatives too)
-  constexpr int PV = (RECON == RECON_WENO5Z_CONS || RECON == RECON_WENO5Z_CHARCONS) ? 10 : 5;
-  double* sm_prim = smem;
-  double* sm_flux = smem + PV * pmax;
-
-  double acc[MAXC][5];
-#pragma unroll
-  for (int k = 0; k < MAXC; ++k)
-#pragma unroll
-    for (int v = 0; v < 5; ++v) acc[k][v] = 0.0;
-
-  bool first = true;
-  if (p.active_mask & 1) {
-    sweep_axis<0, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
-    first = false;
-  }
-  if (p.active_mask & 2) {
-    sweep_axis<1, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
-    first = false;
-  }
-  if (p.active_mask & 4) {
-    sweep_axis<2, RECON, RIEMANN, MODE, MAXC, VISC>(p, o, ext, sm_prim, sm_flux, acc, first);
-  }
-  if (RIEMANN == GBF_RIEMANN_RUSANOV && p.speed_pass) return;  // speeds only, nothing to store
-
-  // ---- epilogue ---------------------------------------------------------
-  const long long cs = (long long)p.n[0] * p.n[1] * p.n[2];
-  const int cvol = ext[0] * ext[1] * ext[2];
-  double smax = 0.0;
-  double rmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
-  double dt = 0.0;
-  if (MODE != MODE_RHS) dt = p.dt_state[0];
-#pragma unroll
-  for (int k = 0; k < MAXC; ++k) {
-    const int c = threadIdx.x + k * blockDim.x;
-    if (c < cvol) {
-      const int c2 = c % ext[2];
-      const int r = c / ext[2];
-      const int c1 = r % ext[1];
-      const int c0 = r / ext[1];
-      const long long off = ((long long)(o[0] + c0) * p.n[1] + (o[1] + c1)) * p.n[2] + (o[2] + c2);
-      if (MODE == MODE_RHS) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) p.out[v * cs + off] = acc[k][v];
-      } else {  // MODE_STAGE, MODE_STAGE_P
-        double U[5], Un[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) U[v] = p.cons[v * cs + off];
-        if (p.gravity) add_gravity(acc[k], U, p.g);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          const double U0 = (p.stage == 0) ? U[v] : p.cons0[v * cs + off];
-          Un[v] = rk3_combine(p.stage, U[v], U0, acc[k][v], dt);
-        }
-#pragma unroll
-        for (int v = 0; v < 5; ++v) p.out[v * cs + off] = Un[v];
-        if (p.reduce_dt) {
-          // time_step_size.py:96-109 on the primitives of the new state
-          double P[5];
-          prims_from_cons(Un, P, p.fp.gm1);
-          const double cc = speed_of_sound(P[4], P[0], p.fp);
-          double s = 0.0;
-          if (p.active_mask & 1) s = s + (fabs(P[1]) + cc);
-          if (p.active_mask & 2) s = s + (fabs(P[2]) + cc);
-          if (p.active_mask & 4) s = s + (fabs(P[3]) + cc);
-          smax = fmax(smax, s);
-          rmin = fmin(rmin, P[0]);
-        }
-      }
-    }
-  }
-  if (MODE != MODE_RHS && p.reduce_dt) {
-    // warp shuffle -> shared -> one atomic per CTA; max/min are exact, so the
-    // result does not depend on the reduction order.
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
-      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
-    }
-    __shared__ double red[2][32];
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-      red[0][w] = smax;
-      red[1][w] = rmin;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      const int nw = blockDim.x >> 5;
-      smax = (threadIdx.x < nw) ? red[0][threadIdx.x] : 0.0;
-      rmin = (threadIdx.x < nw) ? red[1][threadIdx.x] : __longlong_as_double(0x7ff0000000000000LL);
-#pragma unroll
-      for (int d = 16; d > 0; d >>= 1) {
-        smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, d));
-        rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
-      }
-      if (threadIdx.x == 0) {
-        atomicMax(reinterpret_cast<unsigned long long*>(p.dt_state + 2), ordered_bits(smax));
-        atomicMin(reinterpret_cast<unsigned long long*>(p.dt_state + 3), ordered_bits(rmin));
-      }
-    }
-    __syncthreads();  // red[] is reused by the next tile of a persistent CTA
-  }
-}
-
-// Two CTAs per SM: the register cap (128) costs the CHAR and viscous variants
-// a few spilled values but doubles their resident warps (viscous CHAR-ROE TGV
-// 128^3: 3.15e7 -> 3.31e7 cell-updates/s); the others fit 128 registers anyway.
-template <int RECON, int RIEMANN, int MODE, int MAXC, int VISC>
-__global__ void __launch_bounds__(256, 2) sweep_kernel(const SweepParams p) {
-  extern __shared__ double smem[];
-  sweep_tile<RECON, RIEMANN, MODE, MAXC, VISC>(p, blockIdx.x, smem);
 }
 
 }  // namespace gbf

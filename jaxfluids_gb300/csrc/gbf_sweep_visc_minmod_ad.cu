@@ -1,12 +1,7 @@
-// Sweep kernels: MUSCL3 with the MINMOD-AD limiter on primitive variables with viscous / heat fluxes.
+// Face kernels: MUSCL3 with the MINMOD-AD limiter on primitive variables with viscous / heat fluxes.
 #include "gbf_sweep_launch.cuh"
 
 namespace gbf {
-
-int launch_sweep_visc_minmod_ad(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_MINMOD_AD, MODE_RHS, 1>(riemann, p, threads, smem, s);
-  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
-}
 
 int launch_faces_visc_minmod_ad(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {

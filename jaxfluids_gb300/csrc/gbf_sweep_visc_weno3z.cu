@@ -1,12 +1,7 @@
-// Sweep kernels: WENO3-Z on primitive variables with viscous / heat fluxes.
+// Face kernels: WENO3-Z on primitive variables with viscous / heat fluxes.
 #include "gbf_sweep_launch.cuh"
 
 namespace gbf {
-
-int launch_sweep_visc_weno3z(int riemann, int mode, const SweepParams& p, int threads, size_t smem, cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO3Z, MODE_RHS, 1>(riemann, p, threads, smem, s);
-  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
-}
 
 int launch_faces_visc_weno3z(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {

@@ -1,14 +1,8 @@
-// Sweep kernels: WENO5-Z on primitive variables with viscous / heat fluxes on
+// Face kernels: WENO5-Z on primitive variables with viscous / heat fluxes on
 // CENTRAL4 stencils fixed at compile time (the dissipative_fluxes defaults).
 #include "gbf_sweep_launch.cuh"
 
 namespace gbf {
-
-int launch_sweep_weno_visc_c4(int riemann, int mode, const SweepParams& p, int threads, size_t smem,
-                              cudaStream_t s) {
-  if (mode == MODE_RHS) return launch_sweep_riemann<GBF_RECON_WENO5Z, MODE_RHS, 2>(riemann, p, threads, smem, s);
-  return GBF_ERR_UNSUPPORTED;  // fused stages run the face kernels
-}
 
 int launch_faces_weno_visc_c4(int riemann, const SweepParams& p, const FaceTiles& ft, const FaceBuffers& fb,
     int threads, size_t smem, cudaStream_t s) {

@@ -127,20 +127,22 @@ def test_conservative_reconstructions_need_the_conservatives(lib):
     assert lib.gbf_volume_force(ctypes.byref(g), None, buf, None) == _lib.GBF_ERR_INVALID_ARGUMENT
 
 
-def test_rhs_workspace_holds_the_lax_friedrichs_speeds(lib):
-    """gbf_rhs_ws: 32 bytes of workspace for Lax-Friedrichs (its three axis
-    speeds), none for the other schemes or an invalid case; a missing or
-    misaligned Lax-Friedrichs workspace is refused before any device call."""
-    lf = _case(riemann="LAX-FRIEDRICHS")
-    assert lib.gbf_rhs_workspace_bytes(ctypes.byref(lf)) == 32
-    assert lib.gbf_rhs_workspace_bytes(ctypes.byref(_case())) == 0
+def test_rhs_workspace_holds_the_face_buffers(lib):
+    """gbf_rhs_ws: the workspace holds the face buffers of the reference's face
+    arrays (N + 1 faces per line on every active axis, periodic ones too) and
+    the Lax-Friedrichs speed slots; 0 bytes for an invalid case; a missing or
+    misaligned workspace is refused before any device call."""
+    for kw in ({}, {"riemann": "LAX-FRIEDRICHS"}, {"bc": {f: "PERIODIC" for f in ("east", "west", "north", "south")}}):
+        c = _case(**kw)
+        assert lib.gbf_rhs_workspace_bytes(ctypes.byref(c)) == (5 * (33 * 24 + 32 * 25) + 4) * 8
     bad = _case(riemann="LAX-FRIEDRICHS")
     bad.nh = 1
     assert lib.gbf_rhs_workspace_bytes(ctypes.byref(bad)) == 0
+    lf = _case(riemann="LAX-FRIEDRICHS")
     buf = ctypes.c_void_p(8)
     assert lib.gbf_rhs_ws(ctypes.byref(lf), buf, None, buf, None, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
     assert lib.gbf_rhs_ws(ctypes.byref(lf), buf, None, buf, None, ctypes.c_void_p(12), None) == \
         _lib.GBF_ERR_ALIGNMENT
     # the conservative reconstructions still need the conservatives
     cv = _case(recon_var="CONSERVATIVE")
-    assert lib.gbf_rhs_ws(ctypes.byref(cv), buf, None, buf, None, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
+    assert lib.gbf_rhs_ws(ctypes.byref(cv), buf, None, buf, None, buf, None) == _lib.GBF_ERR_INVALID_ARGUMENT
