@@ -424,6 +424,62 @@ def kh_state(n, seed, device):
     return torch.from_numpy(U).to(device)
 
 
+def run_dropin(args):
+    """The drop-in right-hand side: SpaceSolver.compute_rhs (gbf_rhs_ws, the
+    call GB300SpaceSolver's FFI handler makes) on the halo buffers of the TGV
+    n^3 state after W fused warm-up steps (not the symmetric initial state),
+    K calls timed with CUDA events, L2 overwritten between calls; beside it a
+    fused stage (one third of a fused step) on the same state."""
+    from jaxfluids_gb300 import FusedRK3, SpaceSolver, build
+    from jaxfluids_gb300.solver import EquationManager, HaloManager
+    build.build()
+    device = torch.device("cuda", 0)
+    n = args.n if args.n else N_TGV
+    cfg = tgv_config(n)
+    f = FusedRK3(cfg, device)
+    f.set_state(tgv_state(n, device))
+    f.advance(max(3, args.warmup))
+    U0 = f.cons.clone()
+    hs = cfg.halo_shape()
+    inner = (slice(None),) + tuple(slice(cfg.nh, cfg.nh + n) for _ in range(3))
+    Uh = torch.zeros(hs, dtype=torch.float64, device=device)
+    Ph = torch.zeros(hs, dtype=torch.float64, device=device)
+    Uh[inner] = U0
+    Ph[inner] = EquationManager(cfg).get_primitives_from_conservatives(U0.contiguous())
+    Ph, Uh = HaloManager(cfg).perform_halo_update_material(Ph, 0.0, conservatives=Uh)
+    solver = SpaceSolver(cfg)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    for _ in range(3):
+        solver.compute_rhs(Uh, Ph, None, 0.0, 0.0)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k, (a, b) in enumerate(ev):
+        flush.fill_(float(k))
+        a.record()
+        solver.compute_rhs(Uh, Ph, None, 0.0, 0.0)
+        b.record()
+    torch.cuda.synchronize()
+    t_rhs = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
+    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k, (a, b) in enumerate(fev):
+        flush.fill_(float(k))
+        a.record()
+        f.advance(1)
+        b.record()
+    torch.cuda.synchronize()
+    t_stage = sum(a.elapsed_time(b) for a, b in fev) / 1e3 / args.steps / 3.0
+    cells = n ** 3
+    line = {"metric": f"FP64 cell right-hand sides/s (drop-in compute_rhs, TGV {n}^3, WENO5-Z+HLLC)",
+            "value": cells / t_rhs, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_rhs": 1e3 * t_rhs, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"TGV {n}^3 after {max(3, args.warmup)} fused steps, halo buffers filled by "
+                                   "the halo update", "entry": "SpaceSolver.compute_rhs -> gbf_rhs_ws",
+                       "l2": "256 MiB buffer written between timed calls"},
+            "fused_stage_ms": 1e3 * t_stage, "rhs_over_fused_stage": t_rhs / t_stage,
+            "gpu_launches": 2 * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """Gradient of 1/2 ||rho(T) - rho_target||^2 w.r.t. the initial state through
     args.adj_steps fixed-dt RK3 steps (dt = CFL 0.5 step of the initial state),
@@ -541,7 +597,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=None, help="grid side (default 128 inviscid, 256 viscous)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "viscous", "batch", "batch-small", "adjoint", "viscous-adjoint"])
+    ap.add_argument("--workload", default="tgv",
+                    choices=["tgv", "viscous", "batch", "batch-small", "adjoint", "viscous-adjoint", "dropin"])
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=None, help="default 1000 (KH), 200 (viscous TGV)")
     ap.add_argument("--adj-slots", type=int, default=2, help="binomial checkpoint slots (viscous adjoint)")
@@ -556,6 +613,8 @@ def main():
     if args.workload == "adjoint":
         args.adj_steps = args.adj_steps or 1000
         return run_adjoint(args)
+    if args.workload == "dropin":
+        return run_dropin(args)
     if args.workload == "viscous-adjoint":
         args.adj_steps = args.adj_steps or 200
         return run_viscous_adjoint(args)
