@@ -6,9 +6,9 @@ compute_rhs -> stage integration -> primitives from conservatives -> halo
 update, three times per TVD-RK3 step, and the CFL time step afterwards.
 
 ``FusedRK3`` is the hot path: it keeps only the interior conservatives
-([5, Nx, Ny, Nz]) and advances them with one fused sweep kernel per RK stage
-(boundary conditions by index remapping, no halo buffers) plus one tiny
-time-step kernel per step; dt and t stay on the device, so a run of steps
+([5, Nx, Ny, Nz]) and advances them with one face-kernel launch and one cell
+epilogue per RK stage (boundary conditions by index remapping, no halo
+buffers) plus one tiny time-step kernel per step; dt and t stay on the device, so a run of steps
 needs no host synchronisation and can be captured in a CUDA graph.
 """
 from __future__ import annotations
