@@ -160,6 +160,43 @@ def fp64_peak_tflops(device):
     return flops / best / 1e12
 
 
+def run_probe(args):
+    """The arithmetic-rate probes (libgbfprobe.so): per operation the rate of
+    8 independent chains per thread on 152 x 8 CTAs of 256 threads, and its
+    cost in DFMA slots.  DDIV_ZERO divides a zero dividend (the division's
+    general path, which the kernels' zero-dividend shortcut avoids)."""
+    import ctypes
+    from jaxfluids_gb300 import build
+    device = torch.device("cuda", 0)
+    lib = ctypes.CDLL(build.build_probe())
+    lib.gbf_probe_arith.restype = ctypes.c_int
+    lib.gbf_probe_arith.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p]
+    blocks, threads, iters = 152 * 8, 256, 512
+    out = torch.empty(blocks * threads, dtype=torch.float64, device=device)
+    s = torch.cuda.current_stream()
+    st = ctypes.c_void_p(s.cuda_stream)
+    rates = {}
+    for name, mode in (("dfma", 0), ("ddiv", 1), ("ddiv_zero_dividend", 4), ("dsqrt", 2)):
+        lib.gbf_probe_arith(mode, ctypes.c_void_p(out.data_ptr()), blocks, threads, 16, st)
+        torch.cuda.synchronize()
+        best = math.inf
+        for _ in range(3):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            lib.gbf_probe_arith(mode, ctypes.c_void_p(out.data_ptr()), blocks, threads, iters, st)
+            b.record(s)
+            b.synchronize()
+            best = min(best, a.elapsed_time(b) / 1e3)
+        rates[name] = 8.0 * iters * blocks * threads / best
+    line = {"metric": "FP64 operation rates (independent chains)", "unit": "G ops/s",
+            "value": rates["dfma"] / 1e9, "dtype": "f64", "n_gpus": 1,
+            "rates_gops": {k: v / 1e9 for k, v in rates.items()},
+            "dfma_slots_per_op": {k: rates["dfma"] / v for k, v in rates.items()}}
+    print(json.dumps(line), flush=True)
+
+
 def cpu_model():
     """CPU model string of this host (lscpu's Model name, else /proc/cpuinfo)."""
     try:
@@ -598,7 +635,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="grid side (default 128 inviscid, 256 viscous)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="tgv",
-                    choices=["tgv", "viscous", "batch", "batch-small", "adjoint", "viscous-adjoint", "dropin"])
+                    choices=["tgv", "viscous", "batch", "batch-small", "adjoint", "viscous-adjoint", "dropin",
+                             "probe"])
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=None, help="default 1000 (KH), 200 (viscous TGV)")
     ap.add_argument("--adj-slots", type=int, default=2, help="binomial checkpoint slots (viscous adjoint)")
@@ -615,6 +653,8 @@ def main():
         return run_adjoint(args)
     if args.workload == "dropin":
         return run_dropin(args)
+    if args.workload == "probe":
+        return run_probe(args)
     if args.workload == "viscous-adjoint":
         args.adj_steps = args.adj_steps or 200
         return run_viscous_adjoint(args)

@@ -25,6 +25,25 @@ struct FaceParams {
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
 
+// a / b, the IEEE quotient, with a zero dividend answered without dividing:
+// (+-0) / b for a non-zero, non-NaN b (infinities included) is the zero
+// carrying the XOR of the operands' signs, exactly what the division returns.  The division takes a
+// general path for a zero dividend that costs 19 FP64 instructions on GB300
+// against 8 on its common path (measured with ncu), and flat stencils (WENO's
+// |beta0 - beta2| = 0), resting fluid and symmetric states give zero
+// dividends on many faces.
+// The operand tests are integer operations on the halves of the operands (a
+// floating-point compare would take an FP64 issue slot).
+__device__ __forceinline__ double div0(double a, double b) {
+  const unsigned ahi = (unsigned)__double2hiint(a), alo = (unsigned)__double2loint(a);
+  const unsigned bhi = (unsigned)__double2hiint(b), blo = (unsigned)__double2loint(b);
+  const bool a_zero = ((ahi & 0x7fffffffu) | alo) == 0u;
+  const bool b_nonzero = ((bhi & 0x7fffffffu) | blo) != 0u;
+  const bool b_nan = (bhi & 0x7ff00000u) == 0x7ff00000u && (((bhi & 0x000fffffu) | blo) != 0u);
+  if (a_zero && b_nonzero && !b_nan) return __hiloint2double((int)((ahi ^ bhi) & 0x80000000u), 0);
+  return a / b;
+}
+
 // ---------------------------------------------------------------------------
 // Ideal gas and equation layout
 // ---------------------------------------------------------------------------
@@ -118,9 +137,9 @@ __device__ __forceinline__ void weno5_smoothness_shared(double u0, double u1, do
 __device__ __forceinline__ double weno5z_from_beta(double b0, double b1, double b2, double u0, double u1,
                                                    double u2, double u3, double u4, double eps) {
   const double tau5 = fabs(b0 - b2);
-  const double a0 = 0.1 * (1.0 + tau5 / (b0 + eps));
-  const double a1 = 0.6 * (1.0 + tau5 / (b1 + eps));
-  const double a2 = 0.3 * (1.0 + tau5 / (b2 + eps));
+  const double a0 = 0.1 * (1.0 + div0(tau5, b0 + eps));
+  const double a1 = 0.6 * (1.0 + div0(tau5, b1 + eps));
+  const double a2 = 0.3 * (1.0 + div0(tau5, b2 + eps));
   return weno5_combine(a0, a1, a2, u0, u1, u2, u3, u4);
 }
 
@@ -157,7 +176,7 @@ __device__ __forceinline__ void teno5_weights(double b0, double b1, double b2, d
                                               double& o1, double& o2) {
   const double tau5 = fabs(__dsub_rn(b0, b2));
   auto gamma = [&](double b) {
-    const double x = __dadd_rn(1.0, __ddiv_rn(tau5, __dadd_rn(b, eps)));
+    const double x = __dadd_rn(1.0, div0(tau5, __dadd_rn(b, eps)));
     const double x2 = __dmul_rn(x, x);
     return __dmul_rn(x2, __dmul_rn(x2, x2));
   };
@@ -202,8 +221,8 @@ __device__ __forceinline__ double weno3(double u0, double u1, double u2, double 
   double a0, a1;
   if (Z) {
     const double tau3 = fabs(b0 - b1);
-    a0 = (1.0 / 3.0) * (1.0 + tau3 / (b0 + eps));
-    a1 = (2.0 / 3.0) * (1.0 + tau3 / (b1 + eps));
+    a0 = (1.0 / 3.0) * (1.0 + div0(tau3, b0 + eps));
+    a1 = (2.0 / 3.0) * (1.0 + div0(tau3, b1 + eps));
   } else {
     a0 = (1.0 / 3.0) * (1.0 / (b0 * b0 + eps));
     a1 = (2.0 / 3.0) * (1.0 / (b1 * b1 + eps));
@@ -220,7 +239,7 @@ template <int J>
 __device__ __forceinline__ double muscl_minmod(double b0, double b1, double b2, double eps) {
   const double dc = (J == 0) ? b2 - b1 : b1 - b2;
   const double du = (J == 0) ? b1 - b0 : b0 - b1;
-  const double r = (du >= eps) ? dc / (du + 1e-10) : (dc + eps) / (du + eps);
+  const double r = (du >= eps) ? div0(dc, du + 1e-10) : (dc + eps) / (du + eps);
   const double lim = fmax(0.0, fmin(1.0, r));
   return (J == 0) ? b1 + 0.5 * lim * du : b1 - 0.5 * lim * du;
 }
@@ -230,7 +249,7 @@ template <int J>
 __device__ __forceinline__ double minmod_ad(double b0, double b1, double b2, double eps) {
   const double dc = (J == 0) ? b2 - b1 : b1 - b2;
   const double du = (J == 0) ? b1 - b0 : b0 - b1;
-  const double r = (du >= eps) ? dc / (du + 1e-100) : (dc + eps) / (du + eps);
+  const double r = (du >= eps) ? div0(dc, du + 1e-100) : (dc + eps) / (du + eps);
   return (r < 0.0) ? b1 : ((r < 1.0) ? 0.5 * (b1 + b2) : fma(-0.5, b0, 1.5 * b1));
 }
 
@@ -449,7 +468,7 @@ __device__ __forceinline__ void frozen_state_full(const double L[5], const doubl
     const double sL = sqrt(L[0]);
     const double sR = sqrt(R[0]);
 #pragma unroll
-    for (int v = 1; v < 5; ++v) z.pa[v] = (sL * L[v] + sR * R[v]) / (sL + sR);
+    for (int v = 1; v < 5; ++v) z.pa[v] = div0(sL * L[v] + sR * R[v], sL + sR);
     z.pa[0] = sqrt(L[0] * R[0]);
     const double rho_div = 1.0 / (sL + sR);
     const double HL = total_enthalpy(L[4], L[0], L[1], L[2], L[3], fp.gm1);
@@ -728,7 +747,7 @@ __device__ __forceinline__ void hllc(const double PL[5], const double PR[5], con
   // compute_sstar, signal_speeds.py:159-199
   const double rdL = PL[0] * (SL - PL[N]);
   const double rdR = PR[0] * (SR - PR[N]);
-  const double Ss = ((PR[4] - PL[4]) + (PL[N] * rdL - PR[N] * rdR)) / (rdL - rdR);
+  const double Ss = div0((PR[4] - PL[4]) + (PL[N] * rdL - PR[N] * rdR), rdL - rdR);
   // F = 0.5 (1 + sign S*) F*_L + 0.5 (1 - sign S*) F*_R.  With S* != 0 one
   // weight is exactly 0 and the other exactly 1, so only the upwind star flux
   // is formed (a finite F* times 0 adds a signed zero, which changes nothing
@@ -806,7 +825,7 @@ __device__ __forceinline__ void hll(const double PL[5], const double PR[5], cons
   const double SLR = SL * SR;
   const double den = (SR - SL) + fp.eps;
 #pragma unroll
-  for (int v = 0; v < 5; ++v) F[v] = ((SR * FL[v] - SL * FR[v]) + SLR * (UR[v] - UL[v])) / den;
+  for (int v = 0; v < 5; ++v) F[v] = div0((SR * FL[v] - SL * FR[v]) + SLR * (UR[v] - UL[v]), den);
 }
 
 // Face flux without a convective part (GBF_FLAG_NO_CONVECTIVE): flux_xi =

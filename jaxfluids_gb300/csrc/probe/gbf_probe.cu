@@ -10,13 +10,14 @@
 #define GBF_PROBE_DDIV 1
 #define GBF_PROBE_DSQRT 2
 #define GBF_PROBE_FFMA 3
+#define GBF_PROBE_DDIV_ZERO 4  // divisions whose dividend is zero
 
 namespace {
 
 constexpr int kChains = 8;
 
 template <int MODE>
-__global__ void probe_kernel(double* out, int iters, double seed) {
+__global__ void probe_kernel(double* out, int iters, double seed, double num) {
   double a[kChains];
 #pragma unroll
   for (int k = 0; k < kChains; ++k) a[k] = seed + 1e-3 * (threadIdx.x + k);
@@ -26,7 +27,10 @@ __global__ void probe_kernel(double* out, int iters, double seed) {
 #pragma unroll
     for (int k = 0; k < kChains; ++k) {
       if (MODE == GBF_PROBE_DFMA) a[k] = fma(a[k], m, c);
-      if (MODE == GBF_PROBE_DDIV) a[k] = c + 1.0 / a[k];
+      // num is a run-time value (1.25, or 0 for the zero dividend), so the
+      // compiler cannot turn the division into a reciprocal
+      if (MODE == GBF_PROBE_DDIV) a[k] = c + num / a[k];
+      if (MODE == GBF_PROBE_DDIV_ZERO) a[k] = 1.5 + (num * a[k]) / a[k];
       if (MODE == GBF_PROBE_DSQRT) a[k] = sqrt(a[k]) + 0.5;
       if (MODE == GBF_PROBE_FFMA) a[k] = (double)fmaf((float)a[k], 0.9999f, 1e-7f);
     }
@@ -61,9 +65,12 @@ extern "C" int gbf_probe_arith(int mode, double* out, int blocks, int threads, i
   if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) return -1;
   cudaStream_t s = (cudaStream_t)stream;
   switch (mode) {
-    case GBF_PROBE_DFMA: probe_kernel<GBF_PROBE_DFMA><<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
-    case GBF_PROBE_DDIV: probe_kernel<GBF_PROBE_DDIV><<<blocks, threads, 0, s>>>(out, iters, 1.5); break;
-    case GBF_PROBE_DSQRT: probe_kernel<GBF_PROBE_DSQRT><<<blocks, threads, 0, s>>>(out, iters, 2.0); break;
+    case GBF_PROBE_DFMA: probe_kernel<GBF_PROBE_DFMA><<<blocks, threads, 0, s>>>(out, iters, 1.0, 0.0); break;
+    case GBF_PROBE_DDIV: probe_kernel<GBF_PROBE_DDIV><<<blocks, threads, 0, s>>>(out, iters, 1.5, 1.25); break;
+    case GBF_PROBE_DSQRT: probe_kernel<GBF_PROBE_DSQRT><<<blocks, threads, 0, s>>>(out, iters, 2.0, 0.0); break;
+    case GBF_PROBE_DDIV_ZERO:
+      probe_kernel<GBF_PROBE_DDIV_ZERO><<<blocks, threads, 0, s>>>(out, iters, 1.5, 0.0);
+      break;
     case GBF_PROBE_FFMA: probe_ffma_kernel<<<blocks, threads, 0, s>>>(out, iters, 1.0); break;
     default: return -1;
   }
