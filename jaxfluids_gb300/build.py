@@ -83,11 +83,14 @@ def build_ffi(force: bool = False):
 
 def build_probe(force: bool = False) -> str:
     """libgbfprobe.so: the FP64 / FP32 rate probe the benchmark times."""
+    deps = [PROBE_SRC, os.path.abspath(__file__), os.path.join(CSRC, "gbf_physics.cuh"),
+            os.path.join(ROOT, "include", "gbfluids.h")]
     if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= max(
-            os.path.getmtime(PROBE_SRC), os.path.getmtime(os.path.abspath(__file__))):
+            os.path.getmtime(p) for p in deps):
         return PROBE_LIB
     tmp = PROBE_LIB + ".tmp"
-    cmd = [_nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", tmp, "-lcudart"]
+    cmd = [_nvcc(), *ARCH, "-O3", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-shared",
+           f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", PROBE_SRC, "-o", tmp, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {PROBE_SRC}:\n{r.stdout}\n{r.stderr}")

@@ -1,9 +1,15 @@
 // Arithmetic-rate probes used by the benchmark to measure this GPU's FP64
 // roofline (no FP64 peak is published for the part): independent dependency
-// chains per thread, results stored so nothing is optimised away.  Built as
-// its own library (libgbfprobe.so), apart from the product library; only the
-// benchmark loads it.
+// chains per thread, results stored so nothing is optimised away; and the
+// kernels' zero-dividend division (gbf::div0) beside the IEEE division, for
+// the test that compares them bit for bit.  Built as its own library
+// (libgbfprobe.so), apart from the product library; only the benchmark and
+// the tests load it.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "gbf_physics.cuh"
 
 // modes of gbf_probe_arith
 #define GBF_PROBE_DFMA 0
@@ -56,7 +62,26 @@ __global__ void probe_ffma_kernel(double* out, int iters, double seed) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+__global__ void div0_kernel(const double* a, const double* b, double* q_div0, double* q_ieee, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    q_div0[i] = gbf::div0(a[i], b[i]);
+    q_ieee[i] = __ddiv_rn(a[i], b[i]);
+  }
+}
+
 }  // namespace
+
+// q_div0[i] = gbf::div0(a[i], b[i]) and q_ieee[i] = a[i] / b[i] (IEEE, round
+// to nearest) for i < n.  Returns 0, or -1 for invalid arguments, -3 for a
+// launch error.
+extern "C" int gbf_probe_div0(const double* a, const double* b, double* q_div0, double* q_ieee, long long n,
+                              void* stream) {
+  if (!a || !b || !q_div0 || !q_ieee || n <= 0) return -1;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 8);
+  div0_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q_div0, q_ieee, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 // Runs `iters` iterations of 8 independent dependency chains of one operation
 // per thread (blocks x threads threads) and stores one value per thread in
