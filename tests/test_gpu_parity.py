@@ -179,6 +179,41 @@ def test_lax_friedrichs_dropin_on_concurrent_streams():
             assert torch.equal(r.cpu(), refs[k])
 
 
+@pytest.mark.parametrize("kw", [{}, {"recon_var": "CONSERVATIVE"}, {"riemann": "LAX-FRIEDRICHS"}],
+                         ids=["primitive", "conservative", "lax-friedrichs"])
+def test_allocating_dropin_entry_points_match_the_workspace_one(kw):
+    """gbf_rhs / gbf_rhs_cons (face buffers allocated stream-ordered per call)
+    and gbf_rhs_ws (the caller's workspace) through the C ABI on a side
+    stream: the same right-hand side bitwise, equal to the oracle's."""
+    import ctypes
+    from jaxfluids_gb300 import _lib
+    cells = (20, 12, 18)
+    oc, cc = both(cells, "PERIODIC", ranges=((0, 2 * math.pi),) * 3, **kw)
+    U, P = O.initialize(tgv_prims(20)[:, :20, :12, :18].contiguous(), oc)
+    ref = O.compute_rhs(U, P, oc)
+    lib = _lib.load()
+    case = cc.to_c()
+    Ug, Pg = U.cuda().contiguous(), P.cuda().contiguous()
+    outs = [torch.empty(ref.shape, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ws = torch.empty(int(lib.gbf_rhs_workspace_bytes(ctypes.byref(case))) // 8, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        st = ctypes.c_void_p(side.cuda_stream)
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        if kw.get("recon_var") != "CONSERVATIVE":
+            assert lib.gbf_rhs(ctypes.byref(case), ptr(Pg), ptr(outs[0]), None, st) == 0
+        else:
+            assert lib.gbf_rhs(ctypes.byref(case), ptr(Pg), ptr(outs[0]), None, st) == _lib.GBF_ERR_INVALID_ARGUMENT
+            outs[0] = None
+        assert lib.gbf_rhs_cons(ctypes.byref(case), ptr(Pg), ptr(Ug), ptr(outs[1]), None, st) == 0
+        assert lib.gbf_rhs_ws(ctypes.byref(case), ptr(Pg), ptr(Ug), ptr(outs[2]), None, ptr(ws), st) == 0
+    torch.cuda.synchronize()
+    for out in outs:
+        if out is not None:
+            assert torch.equal(out.cpu(), ref)
+
+
 def test_rhs_xz_plane_with_inactive_middle_axis():
     oc, cc = both((32, 1, 24), ZG)
     q = quadrant_prims(32, 24, seed=3)  # [rho, u, v, p] on (32, 24)
