@@ -205,27 +205,28 @@ def _rough_tgv(cells, seed):
     return prims * (1.0 + torch.from_numpy(0.05 * rng.uniform(-1.0, 1.0, prims.shape)))
 
 
+@pytest.mark.parametrize("riemann", list(RIEMANN), ids=[v.lower() for v in RIEMANN.values()])
 @pytest.mark.parametrize("diss", list(DISS))
-@pytest.mark.parametrize("mode", [0, 2], ids=["primitive", "char-roe"])
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["primitive", "char-arithmetic", "char-roe"])
 @pytest.mark.parametrize("name,cells", VISC_CASES, ids=[c[0] for c in VISC_CASES])
-def test_c_viscous_rhs_matches_torch_oracle(name, cells, mode, diss):
+def test_c_viscous_rhs_matches_torch_oracle(name, cells, mode, diss, riemann):
     """CENTRAL4 viscous and heat fluxes on a periodic box, added to the
-    WENO5-Z + HLLC flux of every face: the C right-hand side equals the torch
-    oracle's bitwise."""
+    WENO5-Z (primitive or characteristic) + HLLC / Rusanov / HLL flux of every
+    face: the C right-hand side equals the torch oracle's bitwise."""
     import __graft_entry__
     f = ctypes.CDLL(__graft_entry__.build_oracle_c()).jf_rhs_weno5z_visc
     f.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 5 + \
         [ctypes.c_int] * 3 + [ctypes.c_void_p]
     f.restype = ctypes.c_int
-    oc, _ = both(cells, "PERIODIC", nh=4, riemann="HLLC", mu=0.01, bulk_viscosity=0.003, prandtl=0.72, **MODES[mode],
-                 **DISS[diss])
+    oc, _ = both(cells, "PERIODIC", nh=4, riemann=RIEMANN[riemann], mu=0.01, bulk_viscosity=0.003, prandtl=0.72,
+                 **MODES[mode], **DISS[diss])
     U, P = O.initialize(_rough_tgv(cells, 7), oc)
     ref = O.compute_rhs(U, P, oc)
     Pn = np.ascontiguousarray(P.numpy())
     out = np.empty(ref.shape, dtype=np.float64)
     odx = (ctypes.c_double * 3)(*[oc.one_cell_size(a) if cells[a] > 1 else 0.0 for a in range(3)])
-    assert f(Pn.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, 0,
+    assert f(Pn.ctypes.data, (ctypes.c_int * 3)(*cells), oc.nh, odx, oc.gamma, O.STENCIL_EPS, mode, riemann,
              *_visc_args(oc), out.ctypes.data) == 0
     assert torch.equal(torch.from_numpy(out), ref)
 
