@@ -343,7 +343,7 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  * TENO5, WENO3-JS, WENO3-Z, MINMOD, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
  * and CHAR-CONSERVATIVE with WENO5-Z and either frozen state), HLLC and HLL
  * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter on
- * the PRIMITIVE reconstructions, gravity, and the CENTRAL4 / CENTRAL2 viscous
+ * the PRIMITIVE and CHAR-PRIMITIVE reconstructions, gravity, and the CENTRAL4 / CENTRAL2 viscous
  * and heat fluxes (source_term_solver.py:188-350); other setups return
  * GBF_ERR_UNSUPPORTED.
  *

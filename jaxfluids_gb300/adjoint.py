@@ -49,8 +49,8 @@ class AdjointRK3:
         nb = int(self.lib.gbf_vjp_workspace_bytes(ctypes.byref(self.case)))
         if nb == 0:
             raise NotImplementedError("no adjoint for this setup (the interpolation limiter beside a "
-                                      "characteristic or conservative reconstruction, or HLLC / HLL with "
-                                      "signal speeds other than EINFELDT)")
+                                      "conservative reconstruction, or HLLC / HLL with signal speeds other "
+                                      "than EINFELDT)")
         self.ws = torch.empty(nb // 8, dtype=torch.float64, device=self.device)
         self.dt_dev = torch.full((), self.dt, dtype=torch.float64, device=self.device)
         self.forward_steps = 0  # steps advanced, including recomputation

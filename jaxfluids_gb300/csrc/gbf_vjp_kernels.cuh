@@ -102,8 +102,24 @@ __device__ __forceinline__ void char_face_vjp(const VjpParams& vp, const double*
   PR[I::m0] = cR[I::e0];
   PR[I::m1] = cR[I::e1];
   PR[4] = cc * rho_a * (cR[0] + cR[4]);
+  // the interpolation limiter on the back-projected face primitives: a
+  // replaced primitive is the one of the cell beside the face (window cells
+  // 2 and 3), which takes its cotangent directly
+  unsigned mL = 0, mR = 0;
+  if (vp.sp.limiter) {
+    mL = positivity_limit(PL, win + 2 * ps, pvol, vp.sp.limiter);
+    mR = positivity_limit(PR, win + 3 * ps, pvol, vp.sp.limiter);
+  }
   double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
   face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+  double limL[5], limR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    limL[v] = (mL & (1u << v)) ? dPL[v] : 0.0;
+    limR[v] = (mR & (1u << v)) ? dPR[v] : 0.0;
+    if (mL & (1u << v)) dPL[v] = 0.0;
+    if (mR & (1u << v)) dPR[v] = 0.0;
+  }
   // back-projection reverse
   double drho_a = 0.0, dc = 0.0, dcc = 0.0;
   double gL[5], gR[5];
@@ -158,8 +174,8 @@ __device__ __forceinline__ void char_face_vjp(const VjpParams& vp, const double*
   frozen_state_vjp(Lc, Rc, fp, drho_a, dc, dcc, dLc, dRc);
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    SL(v, 2) += dLc[v];
-    SL(v, 3) += dRc[v];
+    SL(v, 2) += dLc[v] + limL[v];
+    SL(v, 3) += dRc[v] + limR[v];
   }
 }
 

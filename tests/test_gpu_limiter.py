@@ -2,7 +2,8 @@
 solvers/positivity/limiter_interpolation.py:82-210) on the CUDA path against
 the oracle: the right-hand side bitwise where the limiter replaces face states,
 and its reverse (the replaced primitives' cotangents go to the cell beside the
-face) against the oracle's autograd."""
+face) against the oracle's autograd, on primitive and characteristic
+reconstructions."""
 import math
 
 import pytest
@@ -34,12 +35,27 @@ def _dip_prims(n=48):
     return torch.stack([rho, u, p]).reshape(3, n, 1, 1)
 
 
-CASES = [(r, s, lv) for r in ("WENO5-Z", "WENO5-JS", "WENO3-Z", "MINMOD-AD") for s in ("HLLC", "RUSANOV")
-         for lv in (False, True)]
+CASES = [(r, s, lv) for r in ("WENO5-Z", "WENO5-JS", "WENO3-Z", "MINMOD-AD", "CHAR-ARITHMETIC", "CHAR-ROE")
+         for s in ("HLLC", "RUSANOV") for lv in (False, True)]
+CHAR = {"CHAR-ARITHMETIC": dict(recon_var="CHAR-PRIMITIVE", frozen_state="ARITHMETIC"),
+        "CHAR-ROE": dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE")}
 
 
 def _ids(c):
     return f"{c[0]}-{c[1]}" + ("-limit-velocity" if c[2] else "")
+
+
+def _face_pressures(P, oc, j):
+    """Reconstructed face pressures of side j along x, before the limiter
+    (the oracle's primitive or characteristic reconstruction)."""
+    if oc.recon_var != "CHAR-PRIMITIVE":
+        return O.reconstruct_xi(P, oc, 0, j)[4]
+    rho_a, c, cc = O.frozen_state(P, oc, 0)
+    win = [P[O._stencil_slice(oc, 0, k)] for k in range(-3, 3)]
+    chars = [O.chars_from_prims([w[v] for v in range(5)], rho_a, c, cc, 0) for w in win]
+    order = (0, 1, 2, 3, 4) if j == 0 else (5, 4, 3, 2, 1)
+    ch = [O.weno5z_stencil(*[chars[k][v] for k in order]) for v in range(5)]
+    return O.prims_from_chars(ch, rho_a, c, cc, 0)[4]
 
 
 @pytest.mark.parametrize("recon,riemann,limit_velocity", CASES, ids=[_ids(c) for c in CASES])
@@ -47,10 +63,11 @@ def test_limiter_rhs_bitwise_and_vjp(recon, riemann, limit_velocity):
     from jaxfluids_gb300 import SimulationManager
     from jaxfluids_gb300.adjoint import AdjointRK3
     n = 48
-    oc, cc = both((n, 1, 1), {f: "PERIODIC" for f in O.FACES}, recon=recon, riemann=riemann,
-                  interpolation_limiter=True, limit_velocity=limit_velocity)
+    kw = CHAR.get(recon, {"recon": recon})
+    oc, cc = both((n, 1, 1), {f: "PERIODIC" for f in O.FACES}, riemann=riemann,
+                  interpolation_limiter=True, limit_velocity=limit_velocity, **kw)
     U, P = O.initialize(_dip_prims(n), oc)
-    limited = sum(int((O.reconstruct_xi(P, oc, 0, j)[4] < O.LIMITER_EPS_PRESSURE).sum()) for j in (0, 1))
+    limited = sum(int((_face_pressures(P, oc, j) < O.LIMITER_EPS_PRESSURE).sum()) for j in (0, 1))
     assert limited > 0, "the case must exercise the limiter"
     ref = O.compute_rhs(U, P, oc)
     sim = SimulationManager(cc)
@@ -78,9 +95,9 @@ def test_limiter_fused_steps():
     assert rel_err(f.cons, Ur[oc.interior()]) <= 1e-10
 
 
-def test_char_limiter_has_no_adjoint():
+def test_conservative_limiter_has_no_adjoint():
     from jaxfluids_gb300.adjoint import AdjointRK3
-    _, cc = both((32, 1, 1), {f: "PERIODIC" for f in O.FACES}, recon_var="CHAR-PRIMITIVE",
+    _, cc = both((32, 1, 1), {f: "PERIODIC" for f in O.FACES}, recon_var="CONSERVATIVE",
                  interpolation_limiter=True)
     with pytest.raises(NotImplementedError):
         AdjointRK3(cc, dt=1e-4)
