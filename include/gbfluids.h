@@ -342,8 +342,8 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  * jnp.maximum share it).  Every reconstruction (PRIMITIVE WENO5-Z, WENO5-JS,
  * TENO5, WENO3-JS, WENO3-Z, MINMOD, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
  * and CHAR-CONSERVATIVE with WENO5-Z and either frozen state), HLLC and HLL
- * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter on
- * the PRIMITIVE and CHAR-PRIMITIVE reconstructions, gravity, and the CENTRAL4 / CENTRAL2 viscous
+ * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter,
+ * gravity, and the CENTRAL4 / CENTRAL2 viscous
  * and heat fluxes (source_term_solver.py:188-350); other setups return
  * GBF_ERR_UNSUPPORTED.
  *

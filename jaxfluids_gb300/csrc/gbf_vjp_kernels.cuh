@@ -39,6 +39,51 @@ __device__ __forceinline__ void face_riemann_vjp(const VjpParams& vp, const doub
     riemann_flux_vjp<AX, RIEMANN>(PL, PR, vp.sp.fp, dF, dPL, dPR);
 }
 
+// face_riemann_vjp on the face states after the interpolation limiter
+// (positivity_limit against the primitives of window cells 2 and 3: variable
+// stride pvol, cell stride ps from win): PL, PR are limited in place, and the
+// cotangent of a replaced face primitive, which is the cell's primitive, goes
+// to limL / limR instead of dPL / dPR.
+template <int AX, int RIEMANN>
+__device__ __forceinline__ void face_riemann_limited_vjp(const VjpParams& vp, const double* win, int pvol, int ps,
+                                                         double PL[5], double PR[5], const double dF[5],
+                                                         double dPL[5], double dPR[5], double limL[5],
+                                                         double limR[5], double& dalpha) {
+  unsigned mL = 0, mR = 0;
+  if (vp.sp.limiter) {
+    mL = positivity_limit(PL, win + 2 * ps, pvol, vp.sp.limiter);
+    mR = positivity_limit(PR, win + 3 * ps, pvol, vp.sp.limiter);
+  }
+  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    limL[v] = (mL & (1u << v)) ? dPL[v] : 0.0;
+    limR[v] = (mR & (1u << v)) ? dPR[v] : 0.0;
+    if (mL & (1u << v)) dPL[v] = 0.0;
+    if (mR & (1u << v)) dPR[v] = 0.0;
+  }
+}
+
+// Cotangents of the primitives of window cells 2 and 3 (limL, limR) onto
+// their conservatives (the staged conservatives behind the primitives,
+// win + 5 pvol), added to slot(v, 2) and slot(v, 3) = slot[(v * 6 + k) * fvol].
+__device__ __forceinline__ void cell_prims_cotangent_to_cons(const VjpParams& vp, const double* win, int pvol,
+                                                             int ps, const double limL[5], const double limR[5],
+                                                             double* slot, int fvol) {
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const double* lim = side == 0 ? limL : limR;
+    if (lim[0] == 0.0 && lim[1] == 0.0 && lim[2] == 0.0 && lim[3] == 0.0 && lim[4] == 0.0) continue;
+    const int k = 2 + side;
+    double Uc[5], dUc[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Uc[v] = win[(5 + v) * pvol + k * ps];
+    prims_from_cons_vjp(Uc, lim, vp.sp.fp.gm1, dUc);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) slot[(v * 6 + k) * fvol] += dUc[v];
+  }
+}
+
 // CHAR-PRIMITIVE face (char_reconstruct of the forward): frozen state of the
 // two cells adjacent to the face, characteristic variables of the six window
 // cells, WENO5-Z with its gradients on each, back-projection, Riemann VJP, and
@@ -236,8 +281,9 @@ __device__ __forceinline__ void charcons_face_vjp(const VjpParams& vp, const dou
   }
   prims_from_cons(UL, PL, fp.gm1);
   prims_from_cons(UR, PR, fp.gm1);
+  double limL[5], limR[5];
   double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+  face_riemann_limited_vjp<AX, RIEMANN>(vp, win, pvol, ps, PL, PR, dF, dPL, dPR, limL, limR, dalpha);
   double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
   prims_from_cons_vjp(UL, dPL, fp.gm1, dUL);
   prims_from_cons_vjp(UR, dPR, fp.gm1, dUR);
@@ -288,6 +334,12 @@ __device__ __forceinline__ void charcons_face_vjp(const VjpParams& vp, const dou
   left_eigvecs_cons_vjp<AX>(z, G, dz);
   double dLp[5] = {0, 0, 0, 0, 0}, dRp[5] = {0, 0, 0, 0, 0};
   frozen_state_full_vjp(L, R, fp, z, dz, dLp, dRp);
+  // the limiter's replaced face primitives are those of cells 2 and 3 too
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    dLp[v] += limL[v];
+    dRp[v] += limR[v];
+  }
   // the frozen state reads the primitives of cells 2 and 3: on to their conservatives
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
@@ -330,8 +382,9 @@ __device__ __forceinline__ void cons_face_vjp(const VjpParams& vp, const double*
   }
   prims_from_cons(UL, PL, fp.gm1);
   prims_from_cons(UR, PR, fp.gm1);
+  double limL[5], limR[5];
   double dPL[5] = {0, 0, 0, 0, 0}, dPR[5] = {0, 0, 0, 0, 0};
-  face_riemann_vjp<AX, RIEMANN>(vp, PL, PR, dF, dPL, dPR, dalpha);
+  face_riemann_limited_vjp<AX, RIEMANN>(vp, win, pvol, ps, PL, PR, dF, dPL, dPR, limL, limR, dalpha);
   double dUL[5] = {0, 0, 0, 0, 0}, dUR[5] = {0, 0, 0, 0, 0};
   prims_from_cons_vjp(UL, dPL, fp.gm1, dUL);
   prims_from_cons_vjp(UR, dPR, fp.gm1, dUR);
@@ -349,6 +402,7 @@ __device__ __forceinline__ void cons_face_vjp(const VjpParams& vp, const double*
     for (int k = 1; k < 5; ++k) SL(v, k) = gL * jl[k] + gR * jr[5 - k];
     SL(v, 5) = gR * jr[0];
   }
+  cell_prims_cotangent_to_cons(vp, win, pvol, ps, limL, limR, slot, fvol);
 }
 
 template <int AX, int RECON, int RIEMANN>

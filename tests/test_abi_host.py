@@ -99,9 +99,9 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CONSERVATIVE"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-CONSERVATIVE"), True),
     (dict(recon_var="CONSERVATIVE"), True),
-    (dict(recon_var="CONSERVATIVE", interpolation_limiter=True), False),
+    (dict(recon_var="CONSERVATIVE", interpolation_limiter=True), True),
     (dict(recon_var="CHAR-CONSERVATIVE", frozen_state="ROE"), True),
-    (dict(recon_var="CHAR-CONSERVATIVE", interpolation_limiter=True), False),
+    (dict(recon_var="CHAR-CONSERVATIVE", interpolation_limiter=True), True),
     (dict(recon_var="CHAR-PRIMITIVE", interpolation_limiter=True), True),
     (dict(interpolation_limiter=True), True),
     (dict(nh=4, viscous=True, mu=0.01, convective=False), True),

@@ -235,8 +235,6 @@ def test_bc_rhs_vjp_matches_oracle_autograd(name):
     from jaxfluids_gb300.adjoint import AdjointRK3
     _, cells, bc, vals, kw, kind = _case(name)
     oc, cc = both(cells, bc, bc_values=vals, **kw)
-    if cc.interpolation_limiter and cc.recon_var not in ("PRIMITIVE", "CHAR-PRIMITIVE"):
-        pytest.skip("the interpolation limiter is reversed on the primitive and characteristic reconstructions")
     # smooth random-phase fields: WENO-Z's derivative amplifies rounding by
     # up to 1/eps where stencils are flat, e.g. zero-gradient halos of a
     # piecewise-constant state, so the comparison uses fields with none

@@ -2,8 +2,8 @@
 solvers/positivity/limiter_interpolation.py:82-210) on the CUDA path against
 the oracle: the right-hand side bitwise where the limiter replaces face states,
 and its reverse (the replaced primitives' cotangents go to the cell beside the
-face) against the oracle's autograd, on primitive and characteristic
-reconstructions."""
+face) against the oracle's autograd, on primitive, characteristic,
+conservative and characteristic-conservative reconstructions."""
 import math
 
 import pytest
@@ -35,10 +35,12 @@ def _dip_prims(n=48):
     return torch.stack([rho, u, p]).reshape(3, n, 1, 1)
 
 
-CASES = [(r, s, lv) for r in ("WENO5-Z", "WENO5-JS", "WENO3-Z", "MINMOD-AD", "CHAR-ARITHMETIC", "CHAR-ROE")
-         for s in ("HLLC", "RUSANOV") for lv in (False, True)]
 CHAR = {"CHAR-ARITHMETIC": dict(recon_var="CHAR-PRIMITIVE", frozen_state="ARITHMETIC"),
-        "CHAR-ROE": dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE")}
+        "CHAR-ROE": dict(recon_var="CHAR-PRIMITIVE", frozen_state="ROE"),
+        "CONSERVATIVE": dict(recon_var="CONSERVATIVE"),
+        "CHARCONS-ROE": dict(recon_var="CHAR-CONSERVATIVE", frozen_state="ROE")}
+CASES = [(r, s, lv) for r in ("WENO5-Z", "WENO5-JS", "WENO3-Z", "MINMOD-AD") + tuple(CHAR)
+         for s in ("HLLC", "RUSANOV") for lv in (False, True)]
 
 
 def _ids(c):
@@ -48,12 +50,23 @@ def _ids(c):
 def _face_pressures(P, oc, j):
     """Reconstructed face pressures of side j along x, before the limiter
     (the oracle's primitive or characteristic reconstruction)."""
-    if oc.recon_var != "CHAR-PRIMITIVE":
+    if oc.recon_var == "PRIMITIVE":
         return O.reconstruct_xi(P, oc, 0, j)[4]
+    order = (0, 1, 2, 3, 4) if j == 0 else (5, 4, 3, 2, 1)
+    if oc.recon_var in ("CONSERVATIVE", "CHAR-CONSERVATIVE"):
+        U = O.cons_from_prims(P, oc.gamma)
+        if oc.recon_var == "CONSERVATIVE":
+            Uj = O.reconstruct_xi(U, oc, 0, j)
+        else:
+            Rm, Lm = O.eigvecs_conservatives(P, oc, 0)
+            win = [U[O._stencil_slice(oc, 0, k)] for k in range(-3, 3)]
+            chars = [O._matvec5(Lm, [w[v] for v in range(5)]) for w in win]
+            ch = [O.weno5z_stencil(*[chars[k][v] for k in order]) for v in range(5)]
+            Uj = torch.stack(O._matvec5(Rm, ch), 0)
+        return O.prims_from_cons(Uj, oc.gamma)[4]
     rho_a, c, cc = O.frozen_state(P, oc, 0)
     win = [P[O._stencil_slice(oc, 0, k)] for k in range(-3, 3)]
     chars = [O.chars_from_prims([w[v] for v in range(5)], rho_a, c, cc, 0) for w in win]
-    order = (0, 1, 2, 3, 4) if j == 0 else (5, 4, 3, 2, 1)
     ch = [O.weno5z_stencil(*[chars[k][v] for k in order]) for v in range(5)]
     return O.prims_from_chars(ch, rho_a, c, cc, 0)[4]
 
@@ -93,11 +106,3 @@ def test_limiter_fused_steps():
     f.set_state(U[oc.interior()].contiguous().cuda())
     f.advance(4)
     assert rel_err(f.cons, Ur[oc.interior()]) <= 1e-10
-
-
-def test_conservative_limiter_has_no_adjoint():
-    from jaxfluids_gb300.adjoint import AdjointRK3
-    _, cc = both((32, 1, 1), {f: "PERIODIC" for f in O.FACES}, recon_var="CONSERVATIVE",
-                 interpolation_limiter=True)
-    with pytest.raises(NotImplementedError):
-        AdjointRK3(cc, dt=1e-4)
