@@ -342,10 +342,9 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  * jnp.maximum share it).  Every reconstruction (PRIMITIVE WENO5-Z, WENO5-JS,
  * TENO5, WENO3-JS, WENO3-Z, MINMOD, MINMOD-AD; CHAR-PRIMITIVE, CONSERVATIVE
  * and CHAR-CONSERVATIVE with WENO5-Z and either frozen state), HLLC and HLL
- * with Einfeldt speeds, Rusanov, Lax-Friedrichs, the interpolation limiter,
- * gravity, and the CENTRAL4 / CENTRAL2 viscous
- * and heat fluxes (source_term_solver.py:188-350); other setups return
- * GBF_ERR_UNSUPPORTED.
+ * with every signal-speed estimate, Rusanov, Lax-Friedrichs, the interpolation
+ * limiter, gravity, and the CENTRAL4 / CENTRAL2 viscous and heat fluxes
+ * (source_term_solver.py:188-350): every setup the forward accepts.
  *
  * gbf_rhs_vjp: out = J(U)^T w with J = d rhs / d U at the interior state
  *   `cons`; w, out interior [5][N].  workspace: gbf_vjp_workspace_bytes(c)

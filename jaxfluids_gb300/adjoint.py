@@ -48,8 +48,7 @@ class AdjointRK3:
         self.fwd = FusedRK3(self.config, self.device, tile)
         nb = int(self.lib.gbf_vjp_workspace_bytes(ctypes.byref(self.case)))
         if nb == 0:
-            raise NotImplementedError("no adjoint for this setup (HLLC / HLL with signal speeds other than "
-                                      "EINFELDT)")
+            raise NotImplementedError("no adjoint for this setup")
         self.ws = torch.empty(nb // 8, dtype=torch.float64, device=self.device)
         self.dt_dev = torch.full((), self.dt, dtype=torch.float64, device=self.device)
         self.forward_steps = 0  # steps advanced, including recomputation

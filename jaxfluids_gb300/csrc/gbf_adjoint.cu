@@ -456,8 +456,6 @@ inline int grid_for(long long n) {
 int vjp_check(const gbf_case* c) {
   if (c->flags & GBF_FLAG_NO_CONVECTIVE) return GBF_OK;  // no convective scheme to reverse
   if (c->recon_var == GBF_RECVAR_CHAR_PRIMITIVE && c->recon != GBF_RECON_WENO5Z) return GBF_ERR_UNSUPPORTED;
-  // HLLC and HLL are reversed with Einfeldt wave speeds; Rusanov has its own
-  if (c->riemann != GBF_RIEMANN_RUSANOV && c->signal_speed != GBF_SIGNAL_EINFELDT) return GBF_ERR_UNSUPPORTED;
   return GBF_OK;
 }
 

@@ -517,6 +517,141 @@ __device__ __forceinline__ void einfeldt_vjp(const Einfeldt& e, double uL, doubl
   drR += dsR * 0.5 * e.isR;
 }
 
+// The wave speeds of every signal_speed estimate (signal_speeds.py:10-157,
+// :201-231; the forward's signal_speeds in gbf_physics.cuh) recomputed for a
+// reverse pass: EINFELDT through Einfeldt above; DAVIS, ARITHMETIC and RUSANOV
+// as min / max of two candidates (X, Y); TORO with the pressure estimate.
+struct WaveSpeeds {
+  int kind;
+  Einfeldt e;
+  double X1, X2, Y1, Y2;         // SL = min(X1, X2), SR = max(Y1, Y2) (RUSANOV: Y = |u| + c)
+  double ppvrs, pstar, g, qL, qR;  // TORO
+  double SL, SR;
+};
+
+__device__ __forceinline__ void wave_speeds_fwd(int kind, double uL, double uR, double rL, double rR, double pL,
+                                                double pR, double cL, double cR, double gamma, WaveSpeeds& w) {
+  w.kind = kind;
+  switch (kind) {
+    case GBF_SIGNAL_EINFELDT:
+      einfeldt_fwd(uL, uR, rL, rR, cL, cR, w.e);
+      w.SL = w.e.SL;
+      w.SR = w.e.SR;
+      break;
+    case GBF_SIGNAL_DAVIS:
+      w.X1 = uL - cL;
+      w.X2 = uR - cR;
+      w.Y1 = uL + cL;
+      w.Y2 = uR + cR;
+      w.SL = fmin(w.X1, w.X2);
+      w.SR = fmax(w.Y1, w.Y2);
+      break;
+    case GBF_SIGNAL_ARITHMETIC: {
+      const double um = 0.5 * (uL + uR), am = 0.5 * (cL + cR);
+      w.X1 = um - am;
+      w.X2 = uL - cL;
+      w.Y1 = um + am;
+      w.Y2 = uR + cR;
+      w.SL = fmin(w.X1, w.X2);
+      w.SR = fmax(w.Y1, w.Y2);
+      break;
+    }
+    case GBF_SIGNAL_RUSANOV:
+      w.Y1 = fabs(uL) + cL;
+      w.Y2 = fabs(uR) + cR;
+      w.SR = fmax(w.Y1, w.Y2);
+      w.SL = -w.SR;
+      break;
+    default: {  // TORO
+      const double rho_bar = 0.5 * (rL + rR), a_bar = 0.5 * (cL + cR);
+      w.ppvrs = 0.5 * (pL + pR) - 0.5 * (uR - uL) * rho_bar * a_bar;
+      w.pstar = fmax(0.0, w.ppvrs);
+      w.g = (gamma + 1) * 0.5 / gamma;
+      w.qL = (w.pstar <= pL) ? 1.0 : sqrt(1 + w.g * (w.pstar / pL - 1));
+      w.qR = (w.pstar <= pR) ? 1.0 : sqrt(1 + w.g * (w.pstar / pR - 1));
+      w.SL = uL - cL * w.qL;
+      w.SR = uR + cR * w.qR;
+      break;
+    }
+  }
+}
+
+// Reverse of wave_speeds_fwd: cotangents dSL, dSR added to those of the normal
+// velocities, densities, sound speeds and (TORO) pressures of both sides.
+__device__ __forceinline__ void wave_speeds_vjp(const WaveSpeeds& w, double uL, double uR, double rL, double rR,
+                                                double pL, double pR, double cL, double cR, double dSL, double dSR,
+                                                double& duL, double& duR, double& drL, double& drR, double& dcL,
+                                                double& dcR, double& dpL, double& dpR) {
+  switch (w.kind) {
+    case GBF_SIGNAL_EINFELDT:
+      einfeldt_vjp(w.e, uL, uR, cL, cR, dSL, dSR, duL, duR, drL, drR, dcL, dcR);
+      break;
+    case GBF_SIGNAL_DAVIS: {
+      const double wx = min_weight_a(w.X1, w.X2), wy = max_weight_a(w.Y1, w.Y2);
+      const double dX1 = dSL * wx, dX2 = dSL * (1.0 - wx), dY1 = dSR * wy, dY2 = dSR * (1.0 - wy);
+      duL += dX1 + dY1;
+      dcL += dY1 - dX1;
+      duR += dX2 + dY2;
+      dcR += dY2 - dX2;
+      break;
+    }
+    case GBF_SIGNAL_ARITHMETIC: {
+      const double wx = min_weight_a(w.X1, w.X2), wy = max_weight_a(w.Y1, w.Y2);
+      const double dX1 = dSL * wx, dX2 = dSL * (1.0 - wx), dY1 = dSR * wy, dY2 = dSR * (1.0 - wy);
+      const double dum = dX1 + dY1, dam = dY1 - dX1;
+      duL += 0.5 * dum + dX2;
+      duR += 0.5 * dum + dY2;
+      dcL += 0.5 * dam - dX2;
+      dcR += 0.5 * dam + dY2;
+      break;
+    }
+    case GBF_SIGNAL_RUSANOV: {
+      const double dsp = dSR - dSL;
+      const double wy = max_weight_a(w.Y1, w.Y2);
+      const double daL = dsp * wy, daR = dsp * (1.0 - wy);
+      duL += daL * jabs_grad(uL);
+      dcL += daL;
+      duR += daR * jabs_grad(uR);
+      dcR += daR;
+      break;
+    }
+    default: {  // TORO: SL = uL - cL qL, SR = uR + cR qR
+      duL += dSL;
+      dcL -= dSL * w.qL;
+      const double dqL = -dSL * cL;
+      duR += dSR;
+      dcR += dSR * w.qR;
+      const double dqR = dSR * cR;
+      double dps = 0.0;
+      // q = sqrt(1 + g (p* / p - 1)) where p* > p: dq/dp* = g / (2 q p), dq/dp = -g p* / (2 q p^2)
+      if (w.pstar > pL) {
+        const double h = dqL * w.g * 0.5 / (w.qL * pL);
+        dps += h;
+        dpL -= h * w.pstar / pL;
+      }
+      if (w.pstar > pR) {
+        const double h = dqR * w.g * 0.5 / (w.qR * pR);
+        dps += h;
+        dpR -= h * w.pstar / pR;
+      }
+      // p* = max(0, p_pvrs); p_pvrs = (pL + pR) / 2 - (uR - uL) rho_bar a_bar / 2
+      const double dpv = dps * max_weight_a(w.ppvrs, 0.0);
+      const double rho_bar = 0.5 * (rL + rR), a_bar = 0.5 * (cL + cR);
+      dpL += 0.5 * dpv;
+      dpR += 0.5 * dpv;
+      const double ddu = -0.5 * dpv * rho_bar * a_bar;
+      duR += ddu;
+      duL -= ddu;
+      const double drb = -0.5 * dpv * (uR - uL) * a_bar, dab = -0.5 * dpv * (uR - uL) * rho_bar;
+      drL += 0.5 * drb;
+      drR += 0.5 * drb;
+      dcL += 0.5 * dab;
+      dcR += 0.5 * dab;
+      break;
+    }
+  }
+}
+
 // Reverse of c = sqrt(y), y = gamma p / rho for one side: dc onto dP[0], dP[4].
 __device__ __forceinline__ void sound_speed_vjp(const FaceSide& S, double gamma, double dc, double dP[5]) {
   const double dy = dc * 0.5 * S.ic;
@@ -524,8 +659,8 @@ __device__ __forceinline__ void sound_speed_vjp(const FaceSide& S, double gamma,
   dP[4] += dy * S.ir * gamma;
 }
 
-// Reverse of hllc<AX> with Einfeldt wave speeds (HLLC.py:80-126,
-// signal_speeds.py:109-133, :159-199); the cons of the face states are
+// Reverse of hllc<AX> with any signal-speed estimate (HLLC.py:80-126,
+// signal_speeds.py:10-199); the cons of the face states are
 // recomputed and reversed too.  dPL, dPR are accumulated.
 template <int AX>
 __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5], const FaceParams& fp,
@@ -537,8 +672,8 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   face_side(PL, gamma, igm1, L);
   face_side(PR, gamma, igm1, R);
   const double uL = PL[N], uR = PR[N], rL = PL[0], rR = PR[0], pL = PL[4], pR = PR[4];
-  Einfeldt e;
-  einfeldt_fwd(uL, uR, rL, rR, L.c, R.c, e);
+  WaveSpeeds e;
+  wave_speeds_fwd(fp.signal_speed, uL, uR, rL, rR, pL, pR, L.c, R.c, gamma, e);
   const double SL = e.SL, SR = e.SR;
   const double rdL = rL * (SL - uL), rdR = rR * (SR - uR);
   const double num = (pR - pL) + (__dmul_rn(uL, rdL) - __dmul_rn(uR, rdR));
@@ -574,20 +709,22 @@ __device__ __forceinline__ void hllc_vjp(const double PL[5], const double PR[5],
   duL -= drdL * rL;
   dSR += drdR * rR;
   duR -= drdR * rR;
-  double dcL = 0.0, dcR = 0.0;
-  einfeldt_vjp(e, uL, uR, L.c, R.c, dSL, dSR, duL, duR, drL, drR, dcL, dcR);
+  double dcL = 0.0, dcR = 0.0, dpL = 0.0, dpR = 0.0;
+  wave_speeds_vjp(e, uL, uR, rL, rR, pL, pR, L.c, R.c, dSL, dSR, duL, duR, drL, drR, dcL, dcR, dpL, dpR);
   sound_speed_vjp(L, gamma, dcL, dPL);
   sound_speed_vjp(R, gamma, dcR, dPR);
   dPL[0] += drL;
   dPR[0] += drR;
   dPL[N] += duL;
   dPR[N] += duR;
+  dPL[4] += dpL;
+  dPR[4] += dpR;
   // U = cons(P)
   cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
   cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }
 
-// Reverse of hll<AX> with Einfeldt wave speeds (HLL.py:28-58):
+// Reverse of hll<AX> with any signal-speed estimate (HLL.py:28-58):
 // F = N / den, N = SR FL - SL FR + SL SR (UR - UL), den = SR - SL + eps,
 // SL = min(sL, 0), SR = max(sR, 0).
 template <int AX>
@@ -600,8 +737,8 @@ __device__ __forceinline__ void hll_vjp(const double PL[5], const double PR[5], 
   face_side(PL, gamma, igm1, L);
   face_side(PR, gamma, igm1, R);
   const double uL = PL[N], uR = PR[N];
-  Einfeldt e;
-  einfeldt_fwd(uL, uR, PL[0], PR[0], L.c, R.c, e);
+  WaveSpeeds e;
+  wave_speeds_fwd(fp.signal_speed, uL, uR, PL[0], PR[0], PL[4], PR[4], L.c, R.c, gamma, e);
   const double SL = fmin(e.SL, 0.0), SR = fmax(e.SR, 0.0);
   double FL[5], FR[5];
   physical_flux<AX>(PL, L.U, FL);
@@ -628,14 +765,17 @@ __device__ __forceinline__ void hll_vjp(const double PL[5], const double PR[5], 
   const double dsR = dSR * max_weight_a(e.SR, 0.0);
   physical_flux_vjp<AX>(PL, L.U, dFL, dPL, dUL);
   physical_flux_vjp<AX>(PR, R.U, dFR, dPR, dUR);
-  double duL = 0.0, duR = 0.0, drL = 0.0, drR = 0.0, dcL = 0.0, dcR = 0.0;
-  einfeldt_vjp(e, uL, uR, L.c, R.c, dsL, dsR, duL, duR, drL, drR, dcL, dcR);
+  double duL = 0.0, duR = 0.0, drL = 0.0, drR = 0.0, dcL = 0.0, dcR = 0.0, dpL = 0.0, dpR = 0.0;
+  wave_speeds_vjp(e, uL, uR, PL[0], PR[0], PL[4], PR[4], L.c, R.c, dsL, dsR, duL, duR, drL, drR, dcL, dcR, dpL,
+                  dpR);
   sound_speed_vjp(L, gamma, dcL, dPL);
   sound_speed_vjp(R, gamma, dcR, dPR);
   dPL[0] += drL;
   dPR[0] += drR;
   dPL[N] += duL;
   dPR[N] += duR;
+  dPL[4] += dpL;
+  dPR[4] += dpR;
   cons_from_prims_vjp(PL, dUL, L.ir, igm1, dPL);
   cons_from_prims_vjp(PR, dUR, R.ir, igm1, dPR);
 }

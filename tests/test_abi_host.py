@@ -75,10 +75,10 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     assert lib.gbf_rk3_stage(ctypes.byref(c), 0, buf, ctypes.c_void_p(24), ctypes.c_void_p(16), buf, None, None,
                              None) == _lib.GBF_ERR_INVALID_ARGUMENT
     assert lib.gbf_last_status() == _lib.GBF_ERR_INVALID_ARGUMENT
-    # the stage VJP rejects schemes the adjoint does not cover (HLL with Davis speeds)
+    # the stage VJP validates its stage index before any device call
     hll = _case(riemann="HLL", signal_speed="DAVIS")
-    assert lib.gbf_rk3_stage_vjp(ctypes.byref(hll), 1, buf, buf, buf, ctypes.c_void_p(16), ctypes.c_void_p(24),
-                                 buf, None, None) == _lib.GBF_ERR_UNSUPPORTED
+    assert lib.gbf_rk3_stage_vjp(ctypes.byref(hll), 3, buf, buf, buf, ctypes.c_void_p(16), ctypes.c_void_p(24),
+                                 buf, None, None) == _lib.GBF_ERR_INVALID_ARGUMENT
     # a solver handle needs a valid case
     bad = _case()
     bad.nh = 1
@@ -95,6 +95,11 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     (dict(riemann="LAX-FRIEDRICHS", recon="MINMOD-AD", nh=4), True),
     (dict(recon="MINMOD", nh=4), True),
     (dict(riemann="LAX-FRIEDRICHS", recon="MINMOD", nh=4), True),
+    (dict(signal_speed="DAVIS"), True),
+    (dict(signal_speed="ARITHMETIC"), True),
+    (dict(signal_speed="RUSANOV"), True),
+    (dict(signal_speed="TORO"), True),
+    (dict(riemann="HLL", signal_speed="TORO"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-PRIMITIVE"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CONSERVATIVE"), True),
     (dict(riemann="LAX-FRIEDRICHS", recon_var="CHAR-CONSERVATIVE"), True),

@@ -133,6 +133,16 @@ VJP_CASES = [
     ("3d-char-roe-hll", (16, 12, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
                                                    "riemann": "HLL"}, "generic"),
     ("sod-minmodad-hll", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD-AD", "riemann": "HLL"}, "sod"),
+    # every signal-speed estimate of HLLC and HLL
+    ("2d-weno-hllc-davis", (40, 36, 1), "PERIODIC", {"signal_speed": "DAVIS"}, "generic"),
+    ("2d-weno-hllc-arith-zg", (24, 20, 1), "ZEROGRADIENT", {"signal_speed": "ARITHMETIC"}, "generic"),
+    ("2d-weno-hllc-rusanov-speed", (40, 36, 1), "PERIODIC", {"signal_speed": "RUSANOV"}, "generic"),
+    ("2d-weno-hllc-toro", (40, 36, 1), "PERIODIC", {"signal_speed": "TORO"}, "generic"),
+    ("2d-weno-hll-toro", (32, 28, 1), "PERIODIC", {"riemann": "HLL", "signal_speed": "TORO"}, "generic"),
+    ("3d-char-roe-hll-davis", (12, 10, 14), "PERIODIC", {"recon_var": "CHAR-PRIMITIVE", "frozen_state": "ROE",
+                                                          "riemann": "HLL", "signal_speed": "DAVIS"}, "generic"),
+    ("2d-cons-hllc-arith", (24, 20, 1), "PERIODIC", {"recon_var": "CONSERVATIVE", "signal_speed": "ARITHMETIC"},
+     "generic"),
     # MINMOD: the limiter max(0, min(1, r)) clips on the smooth fields' steep
     # parts and passes r on their flat ones
     ("sod-minmod-hllc", (40, 1, 1), "ZEROGRADIENT", {"nh": 4, "recon": "MINMOD"}, "sod"),
