@@ -354,7 +354,7 @@ int gbf_solver_time(gbf_solver* s, double* dt_t, void* stream);
  *   from U^n = `cons` with the device time step *dt (stage states recomputed).
  *   workspace: gbf_vjp_workspace_bytes(c).  lam_out must not alias lam.
  */
-size_t gbf_vjp_workspace_bytes(const gbf_case* c);  /* 0: invalid case, or no adjoint for it */
+size_t gbf_vjp_workspace_bytes(const gbf_case* c);  /* 0: invalid case */
 int gbf_rhs_vjp(const gbf_case* c, const double* cons, const double* w, double* out, void* workspace,
                 const gbf_tile* tile, void* stream);
 int gbf_rk3_step_vjp(const gbf_case* c, const double* cons, const double* dt, const double* lam,

@@ -112,7 +112,8 @@ def test_stage_entry_points_validate_before_any_device_call(lib):
     (dict(nh=4, viscous=True, mu=0.01, convective=False), True),
 ])
 def test_adjoint_coverage_is_reported_without_a_device(lib, kw, has_adjoint):
-    """gbf_vjp_workspace_bytes is 0 exactly for the setups without an adjoint."""
+    """Every valid setup has an adjoint: gbf_vjp_workspace_bytes is non-zero
+    for each (and 0 only for an invalid case)."""
     c = _case(**kw)
     assert lib.gbf_case_check(ctypes.byref(c)) == _lib.GBF_OK
     assert (lib.gbf_vjp_workspace_bytes(ctypes.byref(c)) > 0) == has_adjoint
